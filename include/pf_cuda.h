@@ -1,0 +1,214 @@
+/*
+ * pf_cuda.h - C ABI of the GB300-native backend for libprofit's
+ * image-generation path (profile evaluation with adaptive subsampling, sky and
+ * psf profiles, PSF convolution).
+ *
+ * This is the boundary a libprofit build would bind to add a CUDA environment
+ * beside its OpenCL one and a CUDA convolver type:
+ *   - pf_env_*            replaces get_opencl_environment / OpenCLEnv
+ *                         (include/profit/opencl.h:79-168); PF_ENV_DOUBLE plays
+ *                         the role of OpenCLEnvImpl::use_double
+ *                         (include/profit/opencl_impl.h:122).
+ *   - pf_model_evaluate   is what Model::evaluate (src/model.cpp:259-320) calls
+ *                         when a CUDA environment is set, in place of the
+ *                         per-profile RadialProfile::evaluate dispatch
+ *                         (src/radial.cpp:262-287): one call renders the whole
+ *                         model (all profiles, convolution, crop) on the GPU.
+ *   - pf_convolve         is Convolver::convolve (src/convolve.cpp:55-79) for
+ *                         a ConvolverType::CUDA created by create_convolver
+ *                         (src/convolve.cpp:521-584).
+ *   - pf_batch_*, pf_forward, pf_backward: the batched path (many models in
+ *                         one launch sequence) and its adjoint; they have no
+ *                         counterpart in the reference.
+ * Parameter names, defaults, validation messages and error categories are the
+ * reference's (Profile::parameter, src/profile.cpp:69-163; the validate()
+ * methods; include/profit/exceptions.h:41-104). No function throws; each
+ * returns a pf_status and leaves a message readable with pf_last_error().
+ *
+ * All pointers are plain host pointers unless the parameter name ends in _dev
+ * (device memory). Streams are cudaStream_t passed as void*.
+ */
+#ifndef PF_CUDA_H
+#define PF_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__) || defined(__clang__)
+#define PF_API __attribute__((visibility("default")))
+#else
+#define PF_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pf_status {
+	PF_OK = 0,
+	PF_ERR_INVALID_PARAMETER = 1, /* profit::invalid_parameter */
+	PF_ERR_UNKNOWN_PARAMETER = 2, /* profit::unknown_parameter */
+	PF_ERR_CUDA = 3,              /* a CUDA runtime call failed (profit::opencl_error analogue) */
+	PF_ERR_NO_MEMORY = 4,
+	PF_ERR_DEVICE_LIMIT = 5,      /* a bounded device-side resource was exceeded */
+	PF_ERR_UNSUPPORTED = 6,
+	PF_ERR_INTERNAL = 7
+} pf_status;
+
+/* Profile kinds, by the names Model::add_profile accepts (src/model.cpp:103-135). */
+enum pf_profile_kind {
+	PF_SERSIC = 0,
+	PF_CORESERSIC = 1,
+	PF_MOFFAT = 2,
+	PF_FERRER = 3,
+	PF_KING = 4,
+	PF_BROKENEXP = 5,
+	PF_SKY = 6,
+	PF_PSF = 7,
+	PF_NULL = 8
+};
+
+/* Parameter slots of pf_profile_desc.par. Slots 0-5 are the radial
+ * parameters common to all six radial profiles (src/radial.cpp:741-746);
+ * slots from 6 on are profile-specific:
+ *   sersic      6 re, 7 nser                       (src/sersic.cpp:352-360)
+ *   coresersic  6 re, 7 nser, 8 rb, 9 a, 10 b      (src/coresersic.cpp:131-141)
+ *   moffat      6 fwhm, 7 con                      (src/moffat.cpp:101-107)
+ *   ferrer      6 rout, 7 a, 8 b                   (src/ferrer.cpp:111-122)
+ *   king        6 rc, 7 rt, 8 a                    (src/king.cpp:110-118)
+ *   brokenexp   6 h1, 7 h2, 8 rb, 9 a              (src/brokenexponential.cpp:141-150)
+ *   sky         6 bg                               (src/sky.cpp:65-71)
+ *   psf         0 xcen, 1 ycen, 2 mag              (src/psf.cpp:147-156)
+ */
+enum pf_param_slot {
+	PF_P_XCEN = 0, PF_P_YCEN = 1, PF_P_MAG = 2, PF_P_ANG = 3, PF_P_AXRAT = 4, PF_P_BOX = 5,
+	PF_P_X0 = 6
+};
+#define PF_NPAR 12
+
+/* One profile. The sub-pixel integration controls are the reference's
+ * (src/radial.cpp:738-751); defaults: rough 0, adjust 1, resolution 9,
+ * max_recursions 2, acc 0.1 (1 for ferrer), rscale_switch 1, rscale_max 0. */
+typedef struct pf_profile_desc {
+	int32_t kind;
+	int32_t convolve;      /* Profile "convolve" (default 0, src/profile.cpp:38-45) */
+	int32_t rough;
+	int32_t adjust;
+	int32_t rescale_flux;  /* sersic only */
+	uint32_t resolution;
+	uint32_t max_recursions;
+	double acc;
+	double rscale_switch;
+	double rscale_max;
+	double par[PF_NPAR];
+} pf_profile_desc;
+
+enum pf_convolver {
+	PF_CONV_AUTO = 0,   /* autotuner choice (direct for the double mode) */
+	PF_CONV_BRUTE = 1,  /* shared-memory-tiled direct convolution */
+	PF_CONV_FFT = 2     /* Stockham FFT convolution */
+};
+
+/* One model: Model(width, height) with its setters (include/profit/model.h:130-330). */
+typedef struct pf_model_desc {
+	uint32_t width, height;
+	double scale_x, scale_y;          /* set_image_pixel_scale */
+	double magzero;                   /* set_magzero */
+	uint32_t finesampling;            /* set_finesampling (>= 1) */
+	int32_t return_finesampled;       /* set_return_finesampled */
+	uint32_t first_profile;           /* this model's profiles are [first, first + n) */
+	uint32_t n_profiles;
+	int64_t psf_offset;               /* element offset of the raw PSF in psf_pool, -1: none */
+	uint32_t psf_w, psf_h;            /* set_psf (normalised to unit sum on the device) */
+	double psf_scale_x, psf_scale_y;  /* set_psf_pixel_scale */
+	int32_t convolver;                /* pf_convolver */
+	int32_t reserved;
+} pf_model_desc;
+
+typedef struct pf_env pf_env;
+typedef struct pf_batch pf_batch;
+
+/* Environment flags */
+#define PF_ENV_DOUBLE 0x1u   /* plain FP64 path: the reference's arithmetic and subsampling decisions */
+
+/* Last error message of the calling thread. */
+PF_API const char *pf_last_error(void);
+
+/* Library version ("<major>.<minor>.<patch>") and build information. */
+PF_API const char *pf_version(void);
+
+/* Creates an environment on CUDA device `device` (get_opencl_environment
+ * analogue, include/profit/opencl.h:159-168). */
+PF_API pf_status pf_env_create(int device, uint32_t flags, pf_env **env);
+PF_API void pf_env_destroy(pf_env *env);
+
+/*
+ * Model::evaluate for one model with host buffers (src/model.cpp:259-320):
+ * validates like analyze_inputs, draws every profile into the padded drawing
+ * area, convolves the profiles with convolve=1 by the model's PSF, adds,
+ * crops the PSF padding, optionally downsamples. `image` receives
+ * out_w * out_h doubles (query the size with pf_model_output_dims).
+ */
+PF_API pf_status pf_model_output_dims(const pf_model_desc *model, const pf_profile_desc *profiles,
+                               uint32_t *out_w, uint32_t *out_h);
+PF_API pf_status pf_model_evaluate(pf_env *env, const pf_model_desc *model, const pf_profile_desc *profiles,
+                            const double *psf, double *image, uint32_t *out_w, uint32_t *out_h);
+
+/*
+ * Convolver::convolve with ConvolverType::CUDA and crop = true
+ * (src/convolve.cpp:55-79): `out` (w*h) = src convolved with krn, zero
+ * boundary, the kernel's centre at (kw/2, kh/2); output pixels whose mask
+ * byte is 0 are 0 (mask may be NULL). Host buffers.
+ */
+PF_API pf_status pf_convolve(pf_env *env, const double *src, uint32_t w, uint32_t h,
+                      const double *krn, uint32_t kw, uint32_t kh, const uint8_t *mask,
+                      double *out);
+
+/*
+ * Batched path. pf_batch_create copies the descriptors, the PSF pool (host,
+ * psf_pool_len doubles) and sizes every device buffer once; pf_forward then
+ * allocates nothing. Output images of all models are packed back to back;
+ * pf_batch_layout reports each model's offset (n_models + 1 entries) and
+ * output dims (2 per model).
+ */
+PF_API pf_status pf_batch_create(pf_env *env, const pf_model_desc *models, size_t n_models,
+                          const pf_profile_desc *profiles, size_t n_profiles,
+                          const double *psf_pool, size_t psf_pool_len, pf_batch **batch);
+PF_API void pf_batch_destroy(pf_batch *batch);
+PF_API pf_status pf_batch_layout(const pf_batch *batch, uint64_t *offsets, uint32_t *dims,
+                          uint64_t *total_pixels);
+
+/* Replaces every profile's par[] (n_profiles * PF_NPAR doubles, host), as a
+ * fitting loop does between evaluations. Integration controls keep their
+ * batch-creation values. */
+PF_API pf_status pf_batch_set_params(pf_batch *batch, const double *params);
+
+/* Same, from device memory, stream-ordered (no host synchronisation). */
+PF_API pf_status pf_batch_set_params_dev(pf_batch *batch, const double *params_dev, void *stream);
+
+/*
+ * Renders every model of the batch. images_dev: total_pixels floats (double
+ * for a PF_ENV_DOUBLE environment). flux_dev (optional): n_models doubles,
+ * each model's total flux summed in FP64. Stream-ordered; returns once the
+ * work is enqueued (device-side limit violations are reported by
+ * pf_batch_check).
+ */
+PF_API pf_status pf_forward(pf_batch *batch, void *images_dev, double *flux_dev, void *stream);
+
+/* Synchronises `stream` and reports any device-side error of earlier calls. */
+PF_API pf_status pf_batch_check(pf_batch *batch, void *stream);
+
+/* Records, on the next pf_forward, per radial profile and drawing pixel the
+ * deepest subsampling level reached (-1: not evaluated, 0: evaluate_at used
+ * directly, k: subsample_pixel recursed to level k-1) and the number of
+ * subsample_pixel calls per level (PROFIT_DEBUG's n_integrations,
+ * src/radial.cpp:71-79). */
+PF_API pf_status pf_batch_record_depth(pf_batch *batch, int enable);
+PF_API pf_status pf_batch_depth(pf_batch *batch, int8_t *depth, size_t depth_len,
+                         int64_t *level_counts /* n_profiles * 32 */);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PF_CUDA_H */

@@ -1,0 +1,471 @@
+"""GB300-native backend for libprofit's image-generation path.
+
+The host-side classes mirror libprofit's C++ interface for this path so that
+code written against it reads the same:
+
+    profit::Model            -> Model (add_profile, set_psf, set_image_pixel_scale,
+                                set_psf_pixel_scale, set_magzero, set_finesampling,
+                                set_return_finesampled, set_cuda_env, evaluate)
+    Profile::parameter       -> Profile.parameter(name, value) / parameter("name=value")
+                                (src/profile.cpp:84-163: same names, types, messages)
+    get_opencl_environment   -> get_cuda_environment(device, use_double)
+    create_convolver("cuda") -> create_convolver("cuda").convolve(src, krn, mask)
+    exceptions               -> InvalidParameter, UnknownParameter, CudaError
+                                (include/profit/exceptions.h:41-104)
+
+Everything computes on the GPU through the C ABI of include/pf_cuda.h
+(libpfcuda.so); Batch exposes the batched path (many models per launch).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _ffi
+from ._ffi import KINDS, NPAR
+
+__all__ = ["Model", "Profile", "CUDAEnv", "get_cuda_environment", "create_convolver", "Batch",
+           "ProfitError", "InvalidParameter", "UnknownParameter", "CudaError", "version"]
+
+
+class ProfitError(RuntimeError):
+    """profit::exception"""
+
+
+class InvalidParameter(ProfitError):
+    """profit::invalid_parameter"""
+
+
+class UnknownParameter(ProfitError):
+    """profit::unknown_parameter"""
+
+
+class CudaError(ProfitError):
+    """A CUDA runtime failure (the role profit::opencl_error plays for OpenCL)."""
+
+
+class DeviceLimit(ProfitError):
+    """A bounded device-side resource was exceeded."""
+
+
+class Unsupported(ProfitError):
+    """A parameter combination the CUDA backend does not support."""
+
+
+_ERRORS = {
+    _ffi.PF_ERR_INVALID_PARAMETER: InvalidParameter,
+    _ffi.PF_ERR_UNKNOWN_PARAMETER: UnknownParameter,
+    _ffi.PF_ERR_CUDA: CudaError,
+    _ffi.PF_ERR_NO_MEMORY: CudaError,
+    _ffi.PF_ERR_DEVICE_LIMIT: DeviceLimit,
+    _ffi.PF_ERR_UNSUPPORTED: Unsupported,
+    _ffi.PF_ERR_INTERNAL: ProfitError,
+}
+
+
+def _check(status):
+    if status != _ffi.PF_OK:
+        msg = _ffi.load().pf_last_error().decode()
+        raise _ERRORS.get(status, ProfitError)(msg)
+
+
+def version():
+    return _ffi.load().pf_version().decode()
+
+
+# Parameter registry per profile kind: name -> (type, slot). Slots index
+# pf_profile_desc.par; the control parameters live in named fields.
+_RADIAL_COMMON = {"xcen": 0, "ycen": 1, "mag": 2, "ang": 3, "axrat": 4, "box": 5}
+_SPECIFIC = {
+    "sersic": {"re": 6, "nser": 7},
+    "coresersic": {"re": 6, "nser": 7, "rb": 8, "a": 9, "b": 10},
+    "moffat": {"fwhm": 6, "con": 7},
+    "ferrer": {"rout": 6, "a": 7, "b": 8},
+    "king": {"rc": 6, "rt": 7, "a": 8},
+    "brokenexp": {"h1": 6, "h2": 7, "rb": 8, "a": 9},
+    "sky": {"bg": 6},
+    "psf": {"xcen": 0, "ycen": 1, "mag": 2},
+    "null": {},
+}
+# constructor defaults (src/radial.cpp:724-752 and each profile's constructor)
+_DEFAULTS = {
+    "sersic": {"re": 1.0, "nser": 1.0},
+    "coresersic": {"re": 1.0, "rb": 1.0, "nser": 4.0, "a": 1.0, "b": 1.0},
+    "moffat": {"fwhm": 3.0, "con": 2.0},
+    "ferrer": {"rout": 3.0, "a": 1.0, "b": 1.0},
+    "king": {"rc": 1.0, "rt": 3.0, "a": 2.0},
+    "brokenexp": {"h1": 1.0, "h2": 1.0, "rb": 1.0, "a": 1.0},
+    "sky": {"bg": 0.0},
+    "psf": {"xcen": 0.0, "ycen": 0.0, "mag": 0.0},
+    "null": {},
+}
+_RADIAL = ("sersic", "coresersic", "moffat", "ferrer", "king", "brokenexp")
+
+
+class Profile:
+    """A profile of a Model; parameters are set with parameter()."""
+
+    def __init__(self, name):
+        kind = "ferrer" if name == "ferrers" else name
+        if kind not in KINDS:
+            raise InvalidParameter("Unknown profile name: %s" % name)
+        self.name = name
+        self.kind = kind
+        d = _ffi.ProfileDesc()
+        d.kind = KINDS[kind]
+        d.convolve = 0
+        d.rough = 0
+        d.adjust = 1
+        d.rescale_flux = 0
+        d.resolution = 9
+        d.max_recursions = 2
+        d.acc = 1.0 if kind == "ferrer" else 0.1
+        d.rscale_switch = 1.0
+        d.rscale_max = 0.0
+        vals = [0.0] * NPAR
+        if kind in _RADIAL:
+            vals[:6] = [0.0, 0.0, 15.0, 0.0, 1.0, 0.0]
+        for k, v in _DEFAULTS[kind].items():
+            vals[_SPECIFIC[kind][k]] = v
+        d.par[:] = vals
+        self.desc = d
+
+    # name -> type ("bool", "unsigned int", "double") for this kind
+    def _types(self):
+        t = {"convolve": "bool"}
+        if self.kind in _RADIAL:
+            t.update({"rough": "bool", "adjust": "bool", "force_cpu": "bool",
+                      "max_recursions": "unsigned int", "resolution": "unsigned int",
+                      "acc": "double", "rscale_switch": "double", "rscale_max": "double"})
+            t.update({k: "double" for k in _RADIAL_COMMON})
+        if self.kind == "sersic":
+            t["rescale_flux"] = "bool"
+        t.update({k: "double" for k in _SPECIFIC[self.kind]})
+        return t
+
+    def parameter(self, name, value=None):
+        """parameter(name, value) or parameter("name=value")
+        (Profile::parameter, src/profile.cpp:84-163)."""
+        if value is None:
+            parts = name.split("=")
+            if len(parts) != 2:
+                raise InvalidParameter("missing = in parameter: %s" % name)
+            pname, sval = parts[0].strip(), parts[1].strip()
+            t = self._types().get(pname)
+            try:
+                if t == "bool":
+                    conv = bool(int(sval, 10))
+                elif t == "unsigned int":
+                    conv = int(sval, 10)
+                    if conv < 0:
+                        raise ValueError(sval)
+                elif t == "double":
+                    conv = float(sval)
+                else:
+                    raise KeyError(pname)
+            except (KeyError, ValueError):
+                raise UnknownParameter("Profile %s doesn't support parameter %s, or parameter has invalid "
+                                       "value: %s" % (self.name, pname, sval))
+            return self._set(pname, conv, t)
+        if isinstance(value, bool):
+            t = "bool"
+        elif isinstance(value, (int, np.integer)):
+            t = "unsigned int"
+        else:
+            t = "double"
+        known = self._types()
+        if known.get(name) != t:
+            # an int given for a double parameter is accepted as a double
+            if t == "unsigned int" and known.get(name) == "double":
+                t = "double"
+                value = float(value)
+            else:
+                raise InvalidParameter("Unknown %s parameter in profile %s: %s" % (t, self.name, name))
+        return self._set(name, value, t)
+
+    def _set(self, name, value, t):
+        d = self.desc
+        if name in ("convolve", "rough", "adjust", "rescale_flux"):
+            setattr(d, name, int(bool(value)))
+        elif name == "force_cpu":
+            pass  # no CPU path exists behind the CUDA backend
+        elif name in ("resolution", "max_recursions"):
+            setattr(d, name, int(value))
+        elif name in ("acc", "rscale_switch", "rscale_max"):
+            setattr(d, name, float(value))
+        elif self.kind in _RADIAL and name in _RADIAL_COMMON:
+            d.par[_RADIAL_COMMON[name]] = float(value)
+        else:
+            d.par[_SPECIFIC[self.kind][name]] = float(value)
+        return self
+
+    def get(self, name):
+        d = self.desc
+        if name in ("convolve", "rough", "adjust", "rescale_flux", "resolution", "max_recursions",
+                    "acc", "rscale_switch", "rscale_max"):
+            return getattr(d, name)
+        if self.kind in _RADIAL and name in _RADIAL_COMMON:
+            return d.par[_RADIAL_COMMON[name]]
+        return d.par[_SPECIFIC[self.kind][name]]
+
+
+class CUDAEnv:
+    """A CUDA environment (get_opencl_environment analogue). use_double selects
+    the plain FP64 path (the reference's arithmetic and subsampling decisions)."""
+
+    def __init__(self, device=0, use_double=True):
+        lib = _ffi.load()
+        h = ctypes.c_void_p()
+        _check(lib.pf_env_create(int(device), _ffi.PF_ENV_DOUBLE if use_double else 0, ctypes.byref(h)))
+        self._h = h
+        self.device = device
+        self.use_double = use_double
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            _ffi.load().pf_env_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def get_cuda_environment(device=0, use_double=True):
+    return CUDAEnv(device, use_double)
+
+
+_default_env = None
+
+
+def _env_or_default(env):
+    global _default_env
+    if env is not None:
+        return env
+    if _default_env is None:
+        _default_env = CUDAEnv(0, True)
+    return _default_env
+
+
+class Model:
+    """profit::Model for the CUDA backend (include/profit/model.h)."""
+
+    def __init__(self, width=0, height=0):
+        self.width = int(width)
+        self.height = int(height)
+        self.profiles = []
+        self.psf = None
+        self.scale = (1.0, 1.0)
+        self.psf_scale = (1.0, 1.0)
+        self.magzero = 0.0
+        self.finesampling = 1
+        self.return_finesampled = True
+        self.env = None
+        self.convolver = _ffi.PF_CONV_AUTO
+
+    def add_profile(self, name):
+        p = Profile(name)
+        self.profiles.append(p)
+        return p
+
+    def set_dimensions(self, dims):
+        self.width, self.height = int(dims[0]), int(dims[1])
+
+    def set_psf(self, psf):
+        self.psf = None if psf is None else np.ascontiguousarray(psf, dtype=np.float64)
+
+    def set_image_pixel_scale(self, scale):
+        self.scale = (float(scale[0]), float(scale[1]))
+
+    def set_psf_pixel_scale(self, scale):
+        self.psf_scale = (float(scale[0]), float(scale[1]))
+
+    def set_magzero(self, magzero):
+        self.magzero = float(magzero)
+
+    def set_finesampling(self, fs):
+        if int(fs) == 0:
+            raise InvalidParameter("finesampling must be > 0")
+        self.finesampling = int(fs)
+
+    def set_return_finesampled(self, flag):
+        self.return_finesampled = bool(flag)
+
+    def set_cuda_env(self, env):
+        self.env = env
+
+    def set_convolver(self, convolver):
+        self.convolver = convolver.kind if isinstance(convolver, Convolver) else int(convolver)
+
+    def _descs(self, first_profile=0, psf_offset=None):
+        m = _ffi.ModelDesc()
+        m.width, m.height = self.width, self.height
+        m.scale_x, m.scale_y = self.scale
+        m.magzero = self.magzero
+        m.finesampling = self.finesampling
+        m.return_finesampled = int(self.return_finesampled)
+        m.first_profile = first_profile
+        m.n_profiles = len(self.profiles)
+        if self.psf is not None:
+            m.psf_h, m.psf_w = self.psf.shape
+            m.psf_offset = 0 if psf_offset is None else psf_offset
+        else:
+            m.psf_offset = -1
+        m.psf_scale_x, m.psf_scale_y = self.psf_scale
+        m.convolver = self.convolver
+        profs = (_ffi.ProfileDesc * max(1, len(self.profiles)))()
+        for i, p in enumerate(self.profiles):
+            profs[i] = p.desc
+        return m, profs
+
+    def output_dims(self):
+        m, profs = self._descs()
+        w, h = ctypes.c_uint32(), ctypes.c_uint32()
+        _check(_ffi.load().pf_model_output_dims(ctypes.byref(m), profs, ctypes.byref(w), ctypes.byref(h)))
+        return w.value, h.value
+
+    def evaluate(self):
+        """Model::evaluate: returns the image as a (height, width) float64 array."""
+        env = _env_or_default(self.env)
+        m, profs = self._descs()
+        w, h = self.output_dims()
+        out = np.zeros(w * h, dtype=np.float64)
+        ow, oh = ctypes.c_uint32(), ctypes.c_uint32()
+        psf_ptr = None if self.psf is None else self.psf.ctypes.data_as(ctypes.c_void_p)
+        _check(_ffi.load().pf_model_evaluate(env.handle, ctypes.byref(m), profs, psf_ptr,
+                                             out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ow),
+                                             ctypes.byref(oh)))
+        return out.reshape(oh.value, ow.value)
+
+
+class Convolver:
+    """A ConvolverType::CUDA convolver (create_convolver, src/convolve.cpp:521-584)."""
+
+    def __init__(self, kind=_ffi.PF_CONV_BRUTE, env=None):
+        self.kind = kind
+        self.env = env
+
+    def convolve(self, src, krn, mask=None):
+        env = _env_or_default(self.env)
+        src = np.ascontiguousarray(src, dtype=np.float64)
+        krn = np.ascontiguousarray(krn, dtype=np.float64)
+        out = np.zeros_like(src)
+        mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        _check(_ffi.load().pf_convolve(env.handle, src.ctypes.data_as(ctypes.c_void_p), src.shape[1],
+                                       src.shape[0], krn.ctypes.data_as(ctypes.c_void_p), krn.shape[1],
+                                       krn.shape[0], None if mk is None else mk.ctypes.data_as(ctypes.c_void_p),
+                                       out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+
+def create_convolver(kind="cuda", env=None):
+    names = {"cuda": _ffi.PF_CONV_BRUTE, "cuda-brute": _ffi.PF_CONV_BRUTE, "cuda-fft": _ffi.PF_CONV_FFT}
+    if kind not in names:
+        raise InvalidParameter("Unsupported convolver type: %s" % kind)
+    return Convolver(names[kind], env)
+
+
+class Batch:
+    """Many models rendered by one launch sequence (pf_batch_* / pf_forward).
+
+    Device buffers are torch tensors (or any object with data_ptr()); the
+    batch sizes all its scratch once at construction."""
+
+    def __init__(self, models, env=None):
+        self.env = _env_or_default(env)
+        self.models = list(models)
+        n_prof = sum(len(m.profiles) for m in self.models)
+        mds = (_ffi.ModelDesc * max(1, len(self.models)))()
+        pds = (_ffi.ProfileDesc * max(1, n_prof))()
+        psfs = []
+        first, psf_off = 0, 0
+        for i, m in enumerate(self.models):
+            md, pd = m._descs(first_profile=first, psf_offset=psf_off if m.psf is not None else None)
+            mds[i] = md
+            for j in range(len(m.profiles)):
+                pds[first + j] = pd[j]
+            first += len(m.profiles)
+            if m.psf is not None:
+                psfs.append(m.psf.ravel())
+                psf_off += m.psf.size
+        self.psf_pool = np.ascontiguousarray(np.concatenate(psfs) if psfs else np.zeros(0), dtype=np.float64)
+        self.n_profiles = n_prof
+        h = ctypes.c_void_p()
+        lib = _ffi.load()
+        _check(lib.pf_batch_create(self.env.handle, mds, len(self.models), pds, n_prof,
+                                   self.psf_pool.ctypes.data_as(ctypes.c_void_p) if self.psf_pool.size else None,
+                                   self.psf_pool.size, ctypes.byref(h)))
+        self._h = h
+        n = len(self.models)
+        offs = (ctypes.c_uint64 * (n + 1))()
+        dims = (ctypes.c_uint32 * max(1, 2 * n))()
+        total = ctypes.c_uint64()
+        _check(lib.pf_batch_layout(h, offs, dims, ctypes.byref(total)))
+        self.offsets = [int(offs[i]) for i in range(n + 1)]
+        self.dims = [(int(dims[2 * i]), int(dims[2 * i + 1])) for i in range(n)]
+        self.total_pixels = int(total.value)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def forward(self, images, flux=None, stream=None):
+        """Renders into `images` (device buffer of total_pixels elements,
+        float64 for a use_double environment)."""
+        _check(_ffi.load().pf_forward(self._h, ctypes.c_void_p(images.data_ptr()),
+                                      None if flux is None else ctypes.c_void_p(flux.data_ptr()),
+                                      None if stream is None else ctypes.c_void_p(stream)))
+
+    def check(self, stream=None):
+        _check(_ffi.load().pf_batch_check(self._h, None if stream is None else ctypes.c_void_p(stream)))
+
+    def set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float64).reshape(self.n_profiles, NPAR)
+        _check(_ffi.load().pf_batch_set_params(self._h, p.ctypes.data_as(ctypes.c_void_p)))
+
+    def set_params_dev(self, params, stream=None):
+        _check(_ffi.load().pf_batch_set_params_dev(self._h, ctypes.c_void_p(params.data_ptr()),
+                                                   None if stream is None else ctypes.c_void_p(stream)))
+
+    def record_depth(self, enable=True):
+        _check(_ffi.load().pf_batch_record_depth(self._h, int(bool(enable))))
+
+    def depth(self):
+        """Per profile: (depth map over its model's drawing area, 32 level counts)."""
+        sizes = []
+        for m_idx, m in enumerate(self.models):
+            w, h = _drawing_dims(m)
+            sizes += [(h, w)] * len(m.profiles)
+        total = sum(h * w for h, w in sizes)
+        buf = np.zeros(max(1, total), dtype=np.int8)
+        counts = np.zeros(max(1, self.n_profiles) * 32, dtype=np.int64)
+        _check(_ffi.load().pf_batch_depth(self._h, buf.ctypes.data_as(ctypes.c_void_p), total,
+                                          counts.ctypes.data_as(ctypes.c_void_p)))
+        out, off = [], 0
+        for i, (h, w) in enumerate(sizes):
+            out.append((buf[off:off + h * w].reshape(h, w), counts[32 * i:32 * (i + 1)]))
+            off += h * w
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _ffi.load().pf_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _drawing_dims(model):
+    conv = any(p.desc.convolve for p in model.profiles)
+    px = model.psf.shape[1] // 2 if (conv and model.psf is not None) else 0
+    py = model.psf.shape[0] // 2 if (conv and model.psf is not None) else 0
+    return model.width * model.finesampling + 2 * px, model.height * model.finesampling + 2 * py

@@ -1,0 +1,456 @@
+// Plain FP64 path: the reference's arithmetic on the GPU.
+//
+// eval_tiles64 renders every profile of every model of a batch into the
+// drawing areas: one warp per tile of 32 pixels of a row, profiles in model
+// order, so each pixel accumulates exactly as Model::produce_image does
+// (src/model.cpp:332-346; "image[i] += flux_scale * pixel_val" per profile,
+// src/radial.cpp:341). Pixels that RadialProfile::evaluate_cpu would
+// subsample (src/radial.cpp:323-339) are integrated by the whole warp: the
+// res x res sub-points of a box are spread over the lanes, every sub-point
+// gets its value and accuracy test as in subsample_pixel
+// (src/radial.cpp:55-135), failing sub-points are visited depth-first in the
+// reference's order, and each box's total is formed by one lane in the
+// reference's summation order. The recursion tree is recomputed on the device
+// instead of being shipped through the host level by level as the OpenCL
+// path does (src/radial.cpp:567-673).
+//
+// finish64 produces the output image: model_image + (to_convolve convolved
+// with the PSF) (src/model.cpp:344-356), the convolution done directly with
+// the associative brute-force summation order (row dot products,
+// src/convolve.cpp:158-231) but only for the pixels that survive the crop of
+// the PSF padding (src/model.cpp:288-306), then Image::downsample(SUM)
+// (src/image.cpp:250-262) when the model is finesampled and not returned so.
+//
+// Compiled with -fmad=false (no contraction, like the reference's x86-64 build).
+#include <cstdint>
+
+#include "pf_device.cuh"
+#include "profiles_f64.cuh"
+
+namespace pf {
+
+namespace {
+
+constexpr int kWarps64 = 4;
+
+struct Frame64 {
+	double x0, x1, y0, y1;
+	double hx, hy;
+	double total;
+	unsigned int mask[kMaskWords];
+};
+
+struct WarpScratch64 {
+	Frame64 fr[kMaxLevels];
+	double vals[kMaxRes * kMaxRes];
+};
+
+// Coordinate of sub-point i of a box starting at x0 with half bin h: the
+// reference advances x by h twice per sub-point and uses it after the first
+// advance (src/radial.cpp:83-108), i.e. 2i+1 successive additions.
+__device__ __forceinline__ double sub_coord(double x0, double h, unsigned int i)
+{
+	double x = x0;
+	for (unsigned int t = 0; t < 2 * i + 1; t++) {
+		x += h;
+	}
+	return x;
+}
+
+// Evaluates all sub-points of box fr[L]; leaves the non-failing total and the
+// failing-point mask in fr[L].
+__device__ void eval_frame64(const ProfileDev &P, WarpScratch64 &ws, int L, unsigned int res,
+                             unsigned int max_rec, int lane, unsigned long long *counts)
+{
+	Frame64 &f = ws.fr[L];
+	const double x0 = f.x0, x1 = f.x1, y0 = f.y0, y1 = f.y1;
+	const double xbin = (x1 - x0) / res;
+	const double ybin = (y1 - y0) / res;
+	const double hx = xbin / 2.;
+	const double hy = ybin / 2.;
+	const bool recurse = res > 1 && (unsigned int)L < max_rec;
+	const unsigned int n = res * res;
+	if (counts && lane == 0 && L < kLevelCounts) {
+		atomicAdd(&counts[L], 1ull);
+	}
+	for (unsigned int base = 0; base < n; base += 32) {
+		const unsigned int idx = base + lane;
+		bool fail = false;
+		if (idx < n) {
+			const unsigned int i = idx / res, j = idx % res;
+			const double x = sub_coord(x0, hx, i);
+			const double y = sub_coord(y0, hy, j);
+			double xp, yp;
+			f64::to_profile(P, x, y, xp, yp);
+			const double subval = f64::evaluate_at(P, xp, yp);
+			if (recurse) {
+				const double dyp = (-xbin * P.sin_ang + ybin * P.cos_ang) / P.par[PF_P_AXRAT];
+				const double testval = f64::evaluate_at(P, fabs(xp), fabs(yp) + fabs(dyp));
+				fail = fabs(testval / subval - 1.0) > P.acc;
+			}
+			ws.vals[idx] = subval;
+		}
+		const unsigned int word = __ballot_sync(0xffffffffu, fail);
+		if (lane == 0) {
+			f.mask[base >> 5] = word;
+		}
+	}
+	__syncwarp();
+	if (lane == 0) {
+		double total = 0;
+		for (unsigned int idx = 0; idx < n; idx++) {
+			if (!((f.mask[idx >> 5] >> (idx & 31)) & 1u)) {
+				total += ws.vals[idx];
+			}
+		}
+		f.total = total;
+		f.hx = hx;
+		f.hy = hy;
+	}
+	__syncwarp();
+}
+
+// subsample_pixel(x0, x1, y0, y1, 0, max_rec, res) computed by the whole warp.
+__device__ double warp_subsample64(const ProfileDev &P, WarpScratch64 &ws, double x0, double x1, double y0,
+                                   double y1, unsigned int res, unsigned int max_rec, int lane,
+                                   unsigned long long *counts, int &deepest)
+{
+	if (lane == 0) {
+		ws.fr[0].x0 = x0;
+		ws.fr[0].x1 = x1;
+		ws.fr[0].y0 = y0;
+		ws.fr[0].y1 = y1;
+	}
+	__syncwarp();
+	int L = 0;
+	deepest = 1;
+	eval_frame64(P, ws, 0, res, max_rec, lane, counts);
+	const unsigned int nwords = (res * res + 31) / 32;
+	while (true) {
+		Frame64 &f = ws.fr[L];
+		int k = -1;
+		for (unsigned int w = 0; w < nwords; w++) {
+			const unsigned int mw = f.mask[w];
+			if (mw) {
+				k = (int)(w * 32 + __ffs(mw) - 1);
+				break;
+			}
+		}
+		__syncwarp();
+		if (k >= 0) {
+			const unsigned int i = (unsigned int)k / res, j = (unsigned int)k % res;
+			const double x = sub_coord(f.x0, f.hx, i);
+			const double y = sub_coord(f.y0, f.hy, j);
+			if (lane == 0) {
+				f.mask[k >> 5] &= ~(1u << (k & 31));
+				Frame64 &c = ws.fr[L + 1];
+				c.x0 = x - f.hx;
+				c.x1 = x + f.hx;
+				c.y0 = y - f.hy;
+				c.y1 = y + f.hy;
+			}
+			__syncwarp();
+			L++;
+			if (L + 1 > deepest) deepest = L + 1;
+			eval_frame64(P, ws, L, res, max_rec, lane, counts);
+		}
+		else {
+			const double v = f.total / (res * res);
+			if (L == 0) {
+				return v;
+			}
+			L--;
+			if (lane == 0) {
+				ws.fr[L].total += v;
+			}
+			__syncwarp();
+		}
+	}
+}
+
+__device__ __forceinline__ unsigned int bind_psf(double value, unsigned int max)  // src/psf.cpp:47-55
+{
+	int intval = (int)floor(value);
+	if (intval < 0) return 0;
+	unsigned int u = (unsigned int)intval;
+	return u < max ? u : max;
+}
+
+// PsfProfile::evaluate for one drawing pixel (src/psf.cpp:58-145, including
+// the offset.x / offset.y mix-up of lines 79-82). Returns false if the pixel
+// is outside the stamp.
+__device__ bool psf_pixel64(const ProfileDev &P, const ModelDev &m, const double *psf, unsigned int pix_x,
+                            unsigned int pix_y, double &out)
+{
+	const double xcen = P.par[PF_P_XCEN], ycen = P.par[PF_P_YCEN];
+	const double scale_x = m.sx, scale_y = m.sy;
+	const double psf_scale_x = m.psf_scale_x, psf_scale_y = m.psf_scale_y;
+	const unsigned int width = m.draw_w, height = m.draw_h;
+	const unsigned int psf_width = m.psf_w, psf_height = m.psf_h;
+	const double off_x = m.pad_x, off_y = m.pad_y;
+	const double origin_x = xcen + off_x * scale_x - psf_width * psf_scale_x / 2;
+	const double end_x = xcen + off_y * scale_y + psf_width * psf_scale_x / 2;
+	const double origin_y = ycen + off_x * scale_x - psf_height * psf_scale_y / 2;
+	const double end_y = ycen + off_y * scale_y + psf_height * psf_scale_y / 2;
+	const unsigned int x0 = bind_psf(origin_x / scale_x, width - 1);
+	const unsigned int y0 = bind_psf(origin_y / scale_y, height - 1);
+	const unsigned int x1 = bind_psf(end_x / scale_x, width - 1);
+	const unsigned int y1 = bind_psf(end_y / scale_y, height - 1);
+	if (pix_x < x0 || pix_x > x1 || pix_y < y0 || pix_y > y1) {
+		return false;
+	}
+	const double y = pix_y * scale_y;
+	const double x = pix_x * scale_x;
+	const int psf_pix_x0 = (int)bind_psf(floor((x - origin_x) / psf_scale_x), psf_width - 1);
+	const int psf_pix_x1 = (int)bind_psf(floor((x - origin_x + scale_x) / psf_scale_x), psf_height - 1);
+	const int psf_pix_y0 = (int)bind_psf(floor((y - origin_y) / psf_scale_y), psf_width - 1);
+	const int psf_pix_y1 = (int)bind_psf(floor((y - origin_y + scale_y) / psf_scale_y), psf_height - 1);
+	double val = 0;
+	for (int py = psf_pix_y0; py <= psf_pix_y1; py++) {
+		const double psf_y = py * psf_scale_y + origin_y;
+		for (int px = psf_pix_x0; px <= psf_pix_x1; px++) {
+			const double psf_x = px * psf_scale_x + origin_x;
+			const double ix = fmin(x + scale_x, psf_x + psf_scale_x) - fmax(x, psf_x);
+			const double iy = fmin(y + scale_y, psf_y + psf_scale_y) - fmax(y, psf_y);
+			val += psf[px + py * psf_width] * (ix * iy) / (psf_scale_x * psf_scale_y);
+		}
+	}
+	out = val * P.psf_mag_scale;
+	return true;
+}
+
+__global__ void __launch_bounds__(kWarps64 * 32)
+eval_tiles64_kernel(const ModelDev *__restrict__ models, int n_models, const ProfileDev *__restrict__ profs,
+                    const double *__restrict__ psf_pool, double *__restrict__ conv_img,
+                    double *__restrict__ direct_img, long long n_tiles, unsigned int *tile_counter,
+                    DebugRec dbg)
+{
+	__shared__ WarpScratch64 scratch[kWarps64];
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	WarpScratch64 &ws = scratch[warp];
+	while (true) {
+		unsigned int t = 0;
+		if (lane == 0) {
+			t = atomicAdd(tile_counter, 1u);
+		}
+		const long long tile = (long long)__shfl_sync(0xffffffffu, t, 0);
+		if (tile >= n_tiles) {
+			break;
+		}
+		const int mi = find_model(models, n_models, tile);
+		const ModelDev &m = models[mi];
+		const long long local = tile - m.tile_base;
+		const unsigned int row = (unsigned int)(local / m.tiles_per_row);
+		const int col0 = (int)(local % m.tiles_per_row) * 32;
+		const int col1 = min(col0 + 31, (int)m.draw_w - 1);
+		const unsigned int px = (unsigned int)col0 + lane;
+		const bool active = px < m.draw_w;
+		const double sx = m.sx, sy = m.sy;
+		const double half_xbin = sx / 2.;
+		const double half_ybin = sy / 2.;
+		const double *psf = m.psf_off >= 0 ? psf_pool + m.psf_off : nullptr;
+		double acc_conv = 0, acc_direct = 0;
+
+		for (int q = 0; q < m.n_profiles; q++) {
+			const int pi = m.first_profile + q;
+			const ProfileDev &P = profs[pi];
+			double add = 0;
+			bool has = false;
+			if (P.kind == PF_SKY) {
+				add = P.bg;
+				has = active;
+			}
+			else if (P.kind == PF_PSF) {
+				if (active && psf) {
+					has = psf_pixel64(P, m, psf, px, row, add);
+				}
+			}
+			else if (P.kind <= PF_BROKENEXP) {
+				if ((int)row < P.bby0 || (int)row > P.bby1 || col1 < P.bbx0 || col0 > P.bbx1) {
+					continue;
+				}
+				const double y = half_ybin + row * sy;
+				const double x = half_xbin + px * sx;
+				double xp, yp;
+				f64::to_profile(P, x, y, xp, yp);
+				const double r_prof = sqrt(xp * xp + yp * yp);
+				double pixel_val = 0;
+				int depth = 0;
+				bool need_ss = false;
+				if (P.rscale_max > 0 && r_prof / P.rscale > P.rscale_max) {
+					pixel_val = 0.;
+					depth = -1;
+				}
+				else if (P.rough || r_prof / P.rscale > P.rscale_switch) {
+					pixel_val = f64::evaluate_at(P, xp, yp);
+				}
+				else {
+					need_ss = true;
+				}
+				unsigned int pending = __ballot_sync(0xffffffffu, need_ss && active);
+				unsigned long long *counts = dbg.counts ? dbg.counts + (size_t)pi * kLevelCounts : nullptr;
+				while (pending) {
+					const int s = __ffs(pending) - 1;
+					pending &= pending - 1;
+					const double xs = __shfl_sync(0xffffffffu, x, s);
+					const double ys = __shfl_sync(0xffffffffu, y, s);
+					unsigned int res = P.resolution, max_rec = P.max_recursions;
+					if (P.kind == PF_SERSIC) {  // src/sersic.cpp:331-347
+						const bool center_pixel = fabs(xs - P.xc) < m.scale_x && fabs(ys - P.yc) < m.scale_y;
+						if (P.adjust && center_pixel && P.par[7] > 1) {
+							res = 8;
+							max_rec = 10;
+						}
+					}
+					if (res > (unsigned int)kMaxRes) res = kMaxRes;
+					if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
+					int deepest = 0;
+					const double v = warp_subsample64(P, ws, xs - half_xbin, xs + half_xbin, ys - half_ybin,
+					                                  ys + half_ybin, res, max_rec, lane, counts, deepest);
+					if (lane == s) {
+						pixel_val = v;
+						depth = deepest;
+					}
+				}
+				if (dbg.depth && active) {
+					dbg.depth[P.depth_off + (size_t)row * m.draw_w + px] = (int8_t)depth;
+				}
+				add = P.flux_scale * pixel_val;
+				has = active;
+			}
+			if (has) {
+				if (P.convolve) acc_conv += add;
+				else acc_direct += add;
+			}
+		}
+		if (active) {
+			const size_t idx = (size_t)m.draw_off + (size_t)row * m.draw_w + px;
+			if (m.conv_required) conv_img[idx] = acc_conv;
+			direct_img[idx] = acc_direct;
+		}
+	}
+}
+
+__device__ __forceinline__ int find_model_out(const ModelDev *models, int n_models, long long g)
+{
+	int lo = 0, hi = n_models - 1;
+	while (lo < hi) {
+		int mid = (lo + hi + 1) >> 1;
+		if (models[mid].out_off <= g) lo = mid; else hi = mid - 1;
+	}
+	return lo;
+}
+
+// Associative brute-force convolution of one pixel (src/convolve.cpp:158-231):
+// row dot products of the source against the reversed kernel, zero outside.
+__device__ __forceinline__ double conv_pixel64(const double *src, unsigned int src_width, unsigned int src_height,
+                                               const double *krn, unsigned int krn_width, unsigned int krn_height,
+                                               unsigned int dx, unsigned int dy)
+{
+	const unsigned int krn_half_width = krn_width / 2, krn_half_height = krn_height / 2;
+	unsigned int l_min = 0, l_max = krn_height, k_min = 0, k_max = krn_width;
+	if (dy < krn_half_height) l_min = krn_half_height - dy;
+	else if ((dy + krn_half_height) >= src_height) l_max = src_height + krn_half_height - dy;
+	if (dx < krn_half_width) k_min = krn_half_width - dx;
+	else if ((dx + krn_half_width) >= src_width) k_max = src_width + krn_half_width - dx;
+	const long long kn = (long long)krn_width * krn_height;
+	double pixel = 0;
+	for (unsigned int l = l_min; l < l_max; l++) {
+		// row l of the reversed kernel against the matching source row
+		const long long srow = (long long)(dy + l - krn_half_height) * src_width + (long long)dx - krn_half_width;
+		const long long krow = kn - 1 - (long long)l * krn_width;
+		double dot = 0;
+		for (unsigned int k = k_min; k < k_max; k++) {
+			dot += src[srow + k] * krn[krow - k];
+		}
+		pixel += dot;
+	}
+	return pixel;
+}
+
+// One drawing pixel of the final model image: model_image + convolved to_convolve.
+__device__ __forceinline__ double drawn_pixel64(const ModelDev &m, const double *psf, const double *conv_img,
+                                                const double *direct_img, unsigned int dx, unsigned int dy)
+{
+	double v = direct_img[m.draw_off + (size_t)dy * m.draw_w + dx];
+	if (m.conv_required) {
+		v += conv_pixel64(conv_img + m.draw_off, m.draw_w, m.draw_h, psf, m.psf_w, m.psf_h, dx, dy);
+	}
+	return v;
+}
+
+__global__ void convolve64_kernel(const double *__restrict__ src, unsigned int w, unsigned int h,
+                                  const double *__restrict__ krn, unsigned int kw, unsigned int kh,
+                                  const uint8_t *__restrict__ mask, double *__restrict__ out)
+{
+	const long long n = (long long)w * h;
+	for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+		if (mask && !mask[g]) {
+			out[g] = 0;
+			continue;
+		}
+		out[g] = conv_pixel64(src, w, h, krn, kw, kh, (unsigned int)(g % w), (unsigned int)(g / w));
+	}
+}
+
+__global__ void finish64_kernel(const ModelDev *__restrict__ models, int n_models, const double *__restrict__ psf_pool,
+                                const double *__restrict__ conv_img, const double *__restrict__ direct_img,
+                                double *__restrict__ out, long long total_out)
+{
+	for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total_out;
+	     g += (long long)gridDim.x * blockDim.x) {
+		const int mi = find_model_out(models, n_models, g);
+		const ModelDev &m = models[mi];
+		const long long local = g - m.out_off;
+		const unsigned int ox = (unsigned int)(local % m.out_w), oy = (unsigned int)(local / m.out_w);
+		const double *psf = m.psf_off >= 0 ? psf_pool + m.psf_off : nullptr;
+		double v;
+		if (m.fs > 1 && !m.return_fs) {
+			v = 0;
+			for (unsigned int r = oy * m.fs; r < min((oy + 1) * m.fs, m.crop_h); r++) {
+				for (unsigned int c = ox * m.fs; c < min((ox + 1) * m.fs, m.crop_w); c++) {
+					v += drawn_pixel64(m, psf, conv_img, direct_img, c + m.pad_x, r + m.pad_y);
+				}
+			}
+		}
+		else {
+			v = drawn_pixel64(m, psf, conv_img, direct_img, ox + m.pad_x, oy + m.pad_y);
+		}
+		out[g] = v;
+	}
+}
+
+}  // namespace
+
+void launch_eval64(const ModelDev *models, int n_models, const ProfileDev *profs, const double *psf_pool,
+                   double *conv_img, double *direct_img, long long n_tiles, unsigned int *tile_counter,
+                   DebugRec dbg, int n_sm, cudaStream_t stream)
+{
+	int blocks = n_sm * 8;
+	long long need = (n_tiles + kWarps64 - 1) / kWarps64;
+	if (need < blocks) blocks = (int)(need > 0 ? need : 1);
+	eval_tiles64_kernel<<<blocks, kWarps64 * 32, 0, stream>>>(models, n_models, profs, psf_pool, conv_img,
+	                                                          direct_img, n_tiles, tile_counter, dbg);
+}
+
+void launch_convolve64(const double *src, unsigned int w, unsigned int h, const double *krn, unsigned int kw,
+                       unsigned int kh, const uint8_t *mask, double *out, int n_sm, cudaStream_t stream)
+{
+	const long long n = (long long)w * h;
+	long long need = (n + 255) / 256;
+	int blocks = (int)(need < (long long)n_sm * 16 ? need : (long long)n_sm * 16);
+	if (blocks < 1) blocks = 1;
+	convolve64_kernel<<<blocks, 256, 0, stream>>>(src, w, h, krn, kw, kh, mask, out);
+}
+
+void launch_finish64(const ModelDev *models, int n_models, const double *psf_pool, const double *conv_img,
+                     const double *direct_img, double *out, long long total_out, int n_sm, cudaStream_t stream)
+{
+	int threads = 256;
+	long long need = (total_out + threads - 1) / threads;
+	int blocks = (int)(need < (long long)n_sm * 16 ? need : (long long)n_sm * 16);
+	if (blocks < 1) blocks = 1;
+	finish64_kernel<<<blocks, threads, 0, stream>>>(models, n_models, psf_pool, conv_img, direct_img, out, total_out);
+}
+
+}  // namespace pf

@@ -1,0 +1,664 @@
+// Host side of the C ABI declared in include/pf_cuda.h.
+//
+// Validation follows Model::analyze_inputs (src/model.cpp:186-219) and the
+// profiles' validate() methods with the reference's messages; the drawing
+// geometry follows Model::analyze_expansion_requirements
+// (src/model.cpp:152-184) for models without a calculation mask. Every
+// device buffer of a batch is sized once, at pf_batch_create; pf_forward only
+// enqueues kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/pf_cuda.h"
+#include "pf_device.cuh"
+
+namespace pf {
+void launch_setup(const ModelDev *models, ProfileDev *profs, int n_profiles, int n_models,
+                  unsigned int *tile_counter, unsigned int *err, const double *psf_raw, double *psf_norm,
+                  bool have_psf, cudaStream_t stream);
+void launch_eval64(const ModelDev *models, int n_models, const ProfileDev *profs, const double *psf_pool,
+                   double *conv_img, double *direct_img, long long n_tiles, unsigned int *tile_counter,
+                   DebugRec dbg, int n_sm, cudaStream_t stream);
+void launch_finish64(const ModelDev *models, int n_models, const double *psf_pool, const double *conv_img,
+                     const double *direct_img, double *out, long long total_out, int n_sm, cudaStream_t stream);
+void launch_convolve64(const double *src, unsigned int w, unsigned int h, const double *krn, unsigned int kw,
+                       unsigned int kh, const uint8_t *mask, double *out, int n_sm, cudaStream_t stream);
+void launch_flux_sum(const ModelDev *models, int n_models, const void *images, int is_double, double *flux,
+                     cudaStream_t stream);
+void launch_set_params(ProfileDev *profs, int n_profiles, const double *params, cudaStream_t stream);
+}  // namespace pf
+
+namespace {
+
+thread_local std::string g_last_error;
+
+pf_status fail(pf_status s, const std::string &msg)
+{
+	g_last_error = msg;
+	return s;
+}
+
+#define PF_CUDA_TRY(call)                                                                              \
+	do {                                                                                               \
+		cudaError_t e_ = (call);                                                                       \
+		if (e_ != cudaSuccess) {                                                                       \
+			return fail(e_ == cudaErrorMemoryAllocation ? PF_ERR_NO_MEMORY : PF_ERR_CUDA,              \
+			            std::string(#call) + ": " + cudaGetErrorString(e_));                           \
+		}                                                                                              \
+	} while (0)
+
+bool is_radial(int kind) { return kind >= PF_SERSIC && kind <= PF_BROKENEXP; }
+
+// Profile::validate of every kind, with the reference's messages.
+pf_status validate_profile(const pf_profile_desc &d, bool model_has_psf)
+{
+	const double *v = d.par;
+	if (d.kind < PF_SERSIC || d.kind > PF_NULL) {
+		return fail(PF_ERR_INVALID_PARAMETER, "Unknown profile kind " + std::to_string(d.kind));
+	}
+	if (is_radial(d.kind)) {  // src/radial.cpp:204-214
+		if (v[PF_P_AXRAT] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "axrat <= 0, must have axrat > 0");
+		if (v[PF_P_AXRAT] > 1) return fail(PF_ERR_INVALID_PARAMETER, "axrat > 1, must have axrat <= 1");
+		if (v[PF_P_BOX] <= -2) return fail(PF_ERR_INVALID_PARAMETER, "box <= -2, must have box > -2");
+	}
+	switch (d.kind) {
+	case PF_SERSIC:  // src/sersic.cpp:207-218
+		if (v[6] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "re <= 0, must have re > 0");
+		if (v[7] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "nser <= 0, must have nser > 0");
+		break;
+	case PF_CORESERSIC:  // src/coresersic.cpp:61-82
+		if (v[6] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "re <= 0, must have re > 0");
+		if (v[8] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "rb <= 0, must have rb > 0");
+		if (v[7] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "nser <= 0, must have nser > 0");
+		if (v[9] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "a <= 0, must have a > 0");
+		if (v[10] > 1.999) return fail(PF_ERR_INVALID_PARAMETER, "b > 1.999, must have b < 1.999");
+		break;
+	case PF_MOFFAT:  // src/moffat.cpp:60-71
+		if (v[6] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "fwhm <= 0, must have fwhm > 0");
+		if (v[7] < 0) return fail(PF_ERR_INVALID_PARAMETER, "con < 0, must have con >= 0");
+		break;
+	case PF_FERRER:  // src/ferrer.cpp:62-76
+		if (v[6] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "rout <= 0, must have rout >= 0");
+		if (v[7] < 0) return fail(PF_ERR_INVALID_PARAMETER, "a < 0, must have a >= 0");
+		if (v[8] > 2) return fail(PF_ERR_INVALID_PARAMETER, "b > 2, must have b <= 2");
+		break;
+	case PF_KING:  // src/king.cpp:61-74
+		if (v[6] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "rc <= 0, must have rc > 0");
+		if (v[7] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "rt <= 0, must have rt > 0");
+		if (v[8] < 0) return fail(PF_ERR_INVALID_PARAMETER, "a < 0, must have a >=0");
+		break;
+	case PF_BROKENEXP:  // src/brokenexponential.cpp:96-109
+		if (v[6] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "h1 <= 0, must have h1 > 0");
+		if (v[7] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "h2 <= 0, must have h2 > 0");
+		if (v[8] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "rb <= 0, must have rb > 0");
+		break;
+	case PF_PSF:  // src/psf.cpp:39-45
+		if (!model_has_psf) {
+			return fail(PF_ERR_INVALID_PARAMETER, "No psf present in the model, cannot produce a psf profile");
+		}
+		break;
+	default:
+		break;
+	}
+	if (is_radial(d.kind) && !d.rough) {
+		// the device holds at most kMaxLevels nested sub-pixel boxes per warp
+		unsigned int levels = d.max_recursions;
+		if (d.kind == PF_SERSIC && d.adjust) levels = std::max(levels, 10u);
+		if (levels + 1 > (unsigned int)pf::kMaxLevels) {
+			return fail(PF_ERR_UNSUPPORTED, "max_recursions > " + std::to_string(pf::kMaxLevels - 1) +
+			                                    " is not supported by the CUDA backend");
+		}
+		if (!d.adjust && d.resolution > (unsigned int)pf::kMaxRes) {
+			return fail(PF_ERR_UNSUPPORTED, "resolution > " + std::to_string(pf::kMaxRes) +
+			                                    " is not supported by the CUDA backend");
+		}
+	}
+	return PF_OK;
+}
+
+struct Geometry {
+	uint32_t pad_x, pad_y, draw_w, draw_h, crop_w, crop_h, out_w, out_h;
+	bool conv;
+};
+
+// Model::analyze_inputs + analyze_expansion_requirements without a mask
+pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles, Geometry &g)
+{
+	if (m.width == 0 || m.height == 0) return fail(PF_ERR_INVALID_PARAMETER, "Model's requested dimensions are 0");
+	if (m.scale_x <= 0) return fail(PF_ERR_INVALID_PARAMETER, "Model's scale_x cannot be negative or zero");
+	if (m.scale_y <= 0) return fail(PF_ERR_INVALID_PARAMETER, "Model's scale_y cannot be negative or zero");
+	if (m.finesampling == 0) return fail(PF_ERR_INVALID_PARAMETER, "finesampling must be > 0");
+	const bool has_psf = m.psf_offset >= 0 && m.psf_w > 0 && m.psf_h > 0;
+	g.conv = false;
+	for (uint32_t i = 0; i < m.n_profiles; i++) {
+		g.conv |= profiles[m.first_profile + i].convolve != 0;
+	}
+	if (g.conv && !has_psf) {
+		return fail(PF_ERR_INVALID_PARAMETER, "No psf provided but profile(s) requested convolution");
+	}
+	for (uint32_t i = 0; i < m.n_profiles; i++) {
+		pf_status s = validate_profile(profiles[m.first_profile + i], has_psf);
+		if (s != PF_OK) return s;
+	}
+	g.pad_x = g.conv ? m.psf_w / 2 : 0;
+	g.pad_y = g.conv ? m.psf_h / 2 : 0;
+	g.crop_w = m.width * m.finesampling;
+	g.crop_h = m.height * m.finesampling;
+	g.draw_w = g.crop_w + 2 * g.pad_x;
+	g.draw_h = g.crop_h + 2 * g.pad_y;
+	g.out_w = g.crop_w;
+	g.out_h = g.crop_h;
+	if (m.finesampling > 1 && !m.return_finesampled) {
+		g.out_w = (g.crop_w + m.finesampling - 1) / m.finesampling;
+		g.out_h = (g.crop_h + m.finesampling - 1) / m.finesampling;
+	}
+	return PF_OK;
+}
+
+}  // namespace
+
+struct pf_env {
+	int device = 0;
+	uint32_t flags = 0;
+	int n_sm = 1;
+	cudaStream_t stream = nullptr;
+};
+
+struct pf_batch {
+	pf_env *env = nullptr;
+	bool dbl = true;
+	std::vector<pf_model_desc> models;
+	std::vector<pf_profile_desc> profiles;
+	std::vector<pf::ModelDev> mdev;
+	pf::ProfileDev *h_profiles = nullptr;   // pinned staging copy
+	bool params_dirty = true;
+	pf::ModelDev *d_models = nullptr;
+	pf::ProfileDev *d_profiles = nullptr;
+	double *d_psf_raw = nullptr;
+	double *d_psf_norm = nullptr;
+	size_t psf_len = 0;
+	void *d_conv = nullptr;
+	void *d_direct = nullptr;
+	size_t draw_total = 0;
+	unsigned int *d_counter = nullptr;
+	unsigned int *d_err = nullptr;
+	long long n_tiles = 0;
+	uint64_t total_out = 0;
+	bool record = false;
+	int8_t *d_depth = nullptr;
+	size_t depth_total = 0;
+	unsigned long long *d_counts = nullptr;
+};
+
+extern "C" {
+
+const char *pf_last_error(void) { return g_last_error.c_str(); }
+
+const char *pf_version(void) { return "0.1.0 (libprofit 1.9.3 image path, sm_103a)"; }
+
+pf_status pf_env_create(int device, uint32_t flags, pf_env **env)
+{
+	if (!env) return fail(PF_ERR_INVALID_PARAMETER, "env is NULL");
+	*env = nullptr;
+	int count = 0;
+	PF_CUDA_TRY(cudaGetDeviceCount(&count));
+	if (device < 0 || device >= count) {
+		return fail(PF_ERR_INVALID_PARAMETER, "no CUDA device " + std::to_string(device));
+	}
+	PF_CUDA_TRY(cudaSetDevice(device));
+	pf_env *e = new (std::nothrow) pf_env();
+	if (!e) return fail(PF_ERR_NO_MEMORY, "out of host memory");
+	e->device = device;
+	e->flags = flags;
+	cudaError_t err = cudaDeviceGetAttribute(&e->n_sm, cudaDevAttrMultiProcessorCount, device);
+	if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+	if (err != cudaSuccess) {
+		delete e;
+		return fail(PF_ERR_CUDA, std::string("pf_env_create: ") + cudaGetErrorString(err));
+	}
+	*env = e;
+	return PF_OK;
+}
+
+void pf_env_destroy(pf_env *env)
+{
+	if (!env) return;
+	cudaSetDevice(env->device);
+	if (env->stream) cudaStreamDestroy(env->stream);
+	delete env;
+}
+
+pf_status pf_model_output_dims(const pf_model_desc *model, const pf_profile_desc *profiles, uint32_t *out_w,
+                               uint32_t *out_h)
+{
+	if (!model || (!profiles && model->n_profiles)) return fail(PF_ERR_INVALID_PARAMETER, "NULL model or profiles");
+	pf_model_desc m = *model;
+	m.first_profile = 0;
+	Geometry g;
+	pf_status s = model_geometry(m, profiles, g);
+	if (s != PF_OK) return s;
+	if (out_w) *out_w = g.out_w;
+	if (out_h) *out_h = g.out_h;
+	return PF_OK;
+}
+
+void pf_batch_destroy(pf_batch *b)
+{
+	if (!b) return;
+	cudaSetDevice(b->env->device);
+	cudaFree(b->d_models);
+	cudaFree(b->d_profiles);
+	cudaFree(b->d_psf_raw);
+	cudaFree(b->d_psf_norm);
+	cudaFree(b->d_conv);
+	cudaFree(b->d_direct);
+	cudaFree(b->d_counter);
+	cudaFree(b->d_err);
+	cudaFree(b->d_depth);
+	cudaFree(b->d_counts);
+	cudaFreeHost(b->h_profiles);
+	delete b;
+}
+
+static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, size_t n_models,
+                                   const pf_profile_desc *profiles, size_t n_profiles, const double *psf_pool,
+                                   size_t psf_pool_len, pf_batch *b)
+{
+	b->env = env;
+	b->dbl = (env->flags & PF_ENV_DOUBLE) != 0;
+	b->models.assign(models, models + n_models);
+	b->profiles.assign(profiles, profiles + n_profiles);
+	b->mdev.resize(n_models);
+	std::vector<int32_t> owner(n_profiles, -1);
+	int64_t draw_off = 0, out_off = 0, tile_base = 0;
+	bool any_psf = false;
+	for (size_t i = 0; i < n_models; i++) {
+		const pf_model_desc &m = models[i];
+		if ((uint64_t)m.first_profile + m.n_profiles > n_profiles) {
+			return fail(PF_ERR_INVALID_PARAMETER, "model " + std::to_string(i) + ": profile range out of bounds");
+		}
+		if (m.psf_offset >= 0 && (uint64_t)m.psf_offset + (uint64_t)m.psf_w * m.psf_h > psf_pool_len) {
+			return fail(PF_ERR_INVALID_PARAMETER, "model " + std::to_string(i) + ": PSF outside the PSF pool");
+		}
+		Geometry g;
+		pf_status s = model_geometry(m, profiles, g);
+		if (s != PF_OK) {
+			g_last_error = "model " + std::to_string(i) + ": " + g_last_error;
+			return s;
+		}
+		for (uint32_t q = 0; q < m.n_profiles; q++) {
+			if (owner[m.first_profile + q] != -1) {
+				return fail(PF_ERR_INVALID_PARAMETER, "profile " + std::to_string(m.first_profile + q) +
+				                                          " belongs to two models");
+			}
+			owner[m.first_profile + q] = (int32_t)i;
+		}
+		pf::ModelDev &d = b->mdev[i];
+		std::memset(&d, 0, sizeof(d));
+		d.width = m.width;
+		d.height = m.height;
+		d.fs = m.finesampling;
+		d.return_fs = m.return_finesampled != 0;
+		d.draw_w = g.draw_w;
+		d.draw_h = g.draw_h;
+		d.pad_x = g.pad_x;
+		d.pad_y = g.pad_y;
+		d.crop_w = g.crop_w;
+		d.crop_h = g.crop_h;
+		d.out_w = g.out_w;
+		d.out_h = g.out_h;
+		d.scale_x = m.scale_x;
+		d.scale_y = m.scale_y;
+		d.sx = m.scale_x / m.finesampling;
+		d.sy = m.scale_y / m.finesampling;
+		d.magzero = m.magzero;
+		d.first_profile = (int32_t)m.first_profile;
+		d.n_profiles = (int32_t)m.n_profiles;
+		d.conv_required = g.conv;
+		d.convolver = m.convolver;
+		const bool has_psf = m.psf_offset >= 0 && m.psf_w > 0 && m.psf_h > 0;
+		d.psf_off = has_psf ? m.psf_offset : -1;
+		any_psf |= has_psf;
+		d.psf_w = m.psf_w;
+		d.psf_h = m.psf_h;
+		d.psf_scale_x = m.psf_scale_x;
+		d.psf_scale_y = m.psf_scale_y;
+		d.draw_off = draw_off;
+		d.out_off = out_off;
+		d.tile_base = tile_base;
+		d.tiles_per_row = (g.draw_w + 31) / 32;
+		draw_off += (int64_t)g.draw_w * g.draw_h;
+		out_off += (int64_t)g.out_w * g.out_h;
+		tile_base += (int64_t)d.tiles_per_row * g.draw_h;
+	}
+	b->draw_total = (size_t)draw_off;
+	b->total_out = (uint64_t)out_off;
+	b->n_tiles = tile_base;
+	if (b->n_tiles >= (1ll << 32)) {
+		return fail(PF_ERR_UNSUPPORTED, "batch too large: more than 2^32 tiles of 32 pixels");
+	}
+	if (!b->dbl) {
+		return fail(PF_ERR_UNSUPPORTED, "the single-precision path is not available in this build");
+	}
+
+	PF_CUDA_TRY(cudaMallocHost(&b->h_profiles, sizeof(pf::ProfileDev) * std::max<size_t>(1, n_profiles)));
+	std::memset(b->h_profiles, 0, sizeof(pf::ProfileDev) * std::max<size_t>(1, n_profiles));
+	int64_t depth_off = 0;
+	for (size_t i = 0; i < n_profiles; i++) {
+		const pf_profile_desc &s = profiles[i];
+		pf::ProfileDev &p = b->h_profiles[i];
+		p.kind = s.kind;
+		p.convolve = s.convolve != 0;
+		p.rough = s.rough != 0;
+		p.adjust = s.adjust != 0;
+		p.rescale_flux = s.rescale_flux != 0;
+		p.resolution_in = s.resolution;
+		p.max_recursions = s.max_recursions;
+		p.acc_in = s.acc;
+		p.rscale_switch_in = s.rscale_switch;
+		p.rscale_max_in = s.rscale_max;
+		std::memcpy(p.par, s.par, sizeof(p.par));
+		p.model = owner[i] < 0 ? 0 : owner[i];
+		p.depth_off = depth_off;
+		if (owner[i] >= 0) {
+			const pf::ModelDev &m = b->mdev[owner[i]];
+			depth_off += (int64_t)m.draw_w * m.draw_h;
+		}
+		if (owner[i] < 0) {
+			p.kind = PF_NULL;  // not referenced by any model
+		}
+	}
+	b->depth_total = (size_t)depth_off;
+
+	PF_CUDA_TRY(cudaMalloc(&b->d_models, sizeof(pf::ModelDev) * std::max<size_t>(1, n_models)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_profiles, sizeof(pf::ProfileDev) * std::max<size_t>(1, n_profiles)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_counter, sizeof(unsigned int)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_err, sizeof(unsigned int)));
+	PF_CUDA_TRY(cudaMemset(b->d_err, 0, sizeof(unsigned int)));
+	const size_t elem = b->dbl ? sizeof(double) : sizeof(float);
+	PF_CUDA_TRY(cudaMalloc(&b->d_conv, elem * std::max<size_t>(1, b->draw_total)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_direct, elem * std::max<size_t>(1, b->draw_total)));
+	b->psf_len = psf_pool_len;
+	if (psf_pool_len) {
+		PF_CUDA_TRY(cudaMalloc(&b->d_psf_raw, sizeof(double) * psf_pool_len));
+		PF_CUDA_TRY(cudaMalloc(&b->d_psf_norm, sizeof(double) * psf_pool_len));
+		PF_CUDA_TRY(cudaMemcpy(b->d_psf_raw, psf_pool, sizeof(double) * psf_pool_len, cudaMemcpyHostToDevice));
+	}
+	if (n_models) {
+		PF_CUDA_TRY(cudaMemcpy(b->d_models, b->mdev.data(), sizeof(pf::ModelDev) * n_models, cudaMemcpyHostToDevice));
+	}
+	if (any_psf) {
+		// PSF normalisation (Model::set_psf), once per batch
+		pf::launch_setup(b->d_models, b->d_profiles, 0, (int)n_models, b->d_counter, b->d_err, b->d_psf_raw,
+		                 b->d_psf_norm, true, env->stream);
+		PF_CUDA_TRY(cudaGetLastError());
+		PF_CUDA_TRY(cudaStreamSynchronize(env->stream));
+	}
+	b->params_dirty = true;
+	return PF_OK;
+}
+
+pf_status pf_batch_create(pf_env *env, const pf_model_desc *models, size_t n_models, const pf_profile_desc *profiles,
+                          size_t n_profiles, const double *psf_pool, size_t psf_pool_len, pf_batch **batch)
+{
+	if (!env || !batch || (!models && n_models) || (!profiles && n_profiles) || (!psf_pool && psf_pool_len)) {
+		return fail(PF_ERR_INVALID_PARAMETER, "pf_batch_create: NULL argument");
+	}
+	*batch = nullptr;
+	PF_CUDA_TRY(cudaSetDevice(env->device));
+	pf_batch *b = new (std::nothrow) pf_batch();
+	if (!b) return fail(PF_ERR_NO_MEMORY, "out of host memory");
+	pf_status s = batch_create_impl(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, b);
+	if (s != PF_OK) {
+		b->env = env;
+		pf_batch_destroy(b);
+		return s;
+	}
+	*batch = b;
+	return PF_OK;
+}
+
+pf_status pf_batch_layout(const pf_batch *b, uint64_t *offsets, uint32_t *dims, uint64_t *total_pixels)
+{
+	if (!b) return fail(PF_ERR_INVALID_PARAMETER, "batch is NULL");
+	for (size_t i = 0; i < b->mdev.size(); i++) {
+		if (offsets) offsets[i] = (uint64_t)b->mdev[i].out_off;
+		if (dims) {
+			dims[2 * i] = b->mdev[i].out_w;
+			dims[2 * i + 1] = b->mdev[i].out_h;
+		}
+	}
+	if (offsets) offsets[b->mdev.size()] = b->total_out;
+	if (total_pixels) *total_pixels = b->total_out;
+	return PF_OK;
+}
+
+pf_status pf_batch_set_params(pf_batch *b, const double *params)
+{
+	if (!b || !params) return fail(PF_ERR_INVALID_PARAMETER, "pf_batch_set_params: NULL argument");
+	for (size_t i = 0; i < b->profiles.size(); i++) {
+		pf_profile_desc d = b->profiles[i];
+		std::memcpy(d.par, params + i * PF_NPAR, sizeof(d.par));
+		const pf::ModelDev &m = b->mdev[b->h_profiles[i].model];
+		pf_status s = validate_profile(d, m.psf_off >= 0);
+		if (s != PF_OK) {
+			g_last_error = "profile " + std::to_string(i) + ": " + g_last_error;
+			return s;
+		}
+	}
+	for (size_t i = 0; i < b->profiles.size(); i++) {
+		std::memcpy(b->profiles[i].par, params + i * PF_NPAR, sizeof(double) * PF_NPAR);
+		std::memcpy(b->h_profiles[i].par, params + i * PF_NPAR, sizeof(double) * PF_NPAR);
+	}
+	b->params_dirty = true;
+	return PF_OK;
+}
+
+pf_status pf_batch_set_params_dev(pf_batch *b, const double *params_dev, void *stream_ptr)
+{
+	if (!b || !params_dev) return fail(PF_ERR_INVALID_PARAMETER, "pf_batch_set_params_dev: NULL argument");
+	cudaStream_t stream = stream_ptr ? (cudaStream_t)stream_ptr : b->env->stream;
+	PF_CUDA_TRY(cudaSetDevice(b->env->device));
+	if (b->params_dirty) {
+		// descriptors first, so that the device copy is complete before the scatter
+		PF_CUDA_TRY(cudaMemcpyAsync(b->d_profiles, b->h_profiles,
+		                            sizeof(pf::ProfileDev) * std::max<size_t>(1, b->profiles.size()),
+		                            cudaMemcpyHostToDevice, stream));
+		b->params_dirty = false;
+	}
+	pf::launch_set_params(b->d_profiles, (int)b->profiles.size(), params_dev, stream);
+	PF_CUDA_TRY(cudaGetLastError());
+	return PF_OK;
+}
+
+pf_status pf_batch_record_depth(pf_batch *b, int enable)
+{
+	if (!b) return fail(PF_ERR_INVALID_PARAMETER, "batch is NULL");
+	PF_CUDA_TRY(cudaSetDevice(b->env->device));
+	b->record = enable != 0;
+	if (b->record && !b->d_depth) {
+		PF_CUDA_TRY(cudaMalloc(&b->d_depth, std::max<size_t>(1, b->depth_total)));
+		PF_CUDA_TRY(cudaMalloc(&b->d_counts, sizeof(unsigned long long) * pf::kLevelCounts *
+		                                         std::max<size_t>(1, b->profiles.size())));
+	}
+	return PF_OK;
+}
+
+pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stream_ptr)
+{
+	if (!b || (!images_dev && b->total_out)) return fail(PF_ERR_INVALID_PARAMETER, "pf_forward: NULL argument");
+	cudaStream_t stream = stream_ptr ? (cudaStream_t)stream_ptr : b->env->stream;
+	PF_CUDA_TRY(cudaSetDevice(b->env->device));
+	const int n_models = (int)b->mdev.size();
+	const int n_profiles = (int)b->profiles.size();
+	if (n_models == 0) return PF_OK;
+	if (b->params_dirty) {
+		PF_CUDA_TRY(cudaMemcpyAsync(b->d_profiles, b->h_profiles, sizeof(pf::ProfileDev) * std::max(1, n_profiles),
+		                            cudaMemcpyHostToDevice, stream));
+		b->params_dirty = false;
+	}
+	pf::DebugRec dbg{nullptr, nullptr};
+	if (b->record) {
+		PF_CUDA_TRY(cudaMemsetAsync(b->d_depth, 0xff, std::max<size_t>(1, b->depth_total), stream));
+		PF_CUDA_TRY(cudaMemsetAsync(b->d_counts, 0, sizeof(unsigned long long) * pf::kLevelCounts *
+		                                               std::max(1, n_profiles), stream));
+		dbg.depth = b->d_depth;
+		dbg.counts = b->d_counts;
+	}
+	pf::launch_setup(b->d_models, b->d_profiles, n_profiles, n_models, b->d_counter, b->d_err, nullptr, nullptr,
+	                 false, stream);
+	pf::launch_eval64(b->d_models, n_models, b->d_profiles, b->d_psf_norm, (double *)b->d_conv,
+	                  (double *)b->d_direct, b->n_tiles, b->d_counter, dbg, b->env->n_sm, stream);
+	pf::launch_finish64(b->d_models, n_models, b->d_psf_norm, (const double *)b->d_conv,
+	                    (const double *)b->d_direct, (double *)images_dev, (long long)b->total_out, b->env->n_sm,
+	                    stream);
+	if (flux_dev) {
+		pf::launch_flux_sum(b->d_models, n_models, images_dev, 1, flux_dev, stream);
+	}
+	PF_CUDA_TRY(cudaGetLastError());
+	return PF_OK;
+}
+
+pf_status pf_batch_check(pf_batch *b, void *stream_ptr)
+{
+	if (!b) return fail(PF_ERR_INVALID_PARAMETER, "batch is NULL");
+	cudaStream_t stream = stream_ptr ? (cudaStream_t)stream_ptr : b->env->stream;
+	PF_CUDA_TRY(cudaSetDevice(b->env->device));
+	PF_CUDA_TRY(cudaStreamSynchronize(stream));
+	unsigned int err = 0;
+	PF_CUDA_TRY(cudaMemcpy(&err, b->d_err, sizeof(err), cudaMemcpyDeviceToHost));
+	if (err & (pf::ERR_LEVELS | pf::ERR_RES)) {
+		return fail(PF_ERR_DEVICE_LIMIT, "a profile needed more sub-pixel levels or a finer resolution than the "
+		                                 "device supports; its pixels were clamped");
+	}
+	return PF_OK;
+}
+
+pf_status pf_batch_depth(pf_batch *b, int8_t *depth, size_t depth_len, int64_t *level_counts)
+{
+	if (!b) return fail(PF_ERR_INVALID_PARAMETER, "batch is NULL");
+	if (!b->record) return fail(PF_ERR_INVALID_PARAMETER, "depth recording is not enabled");
+	PF_CUDA_TRY(cudaSetDevice(b->env->device));
+	PF_CUDA_TRY(cudaStreamSynchronize(b->env->stream));
+	PF_CUDA_TRY(cudaDeviceSynchronize());
+	if (depth) {
+		PF_CUDA_TRY(cudaMemcpy(depth, b->d_depth, std::min(depth_len, b->depth_total), cudaMemcpyDeviceToHost));
+	}
+	if (level_counts) {
+		std::vector<unsigned long long> tmp(pf::kLevelCounts * b->profiles.size());
+		if (!tmp.empty()) {
+			PF_CUDA_TRY(cudaMemcpy(tmp.data(), b->d_counts, sizeof(unsigned long long) * tmp.size(),
+			                       cudaMemcpyDeviceToHost));
+		}
+		for (size_t i = 0; i < tmp.size(); i++) level_counts[i] = (int64_t)tmp[i];
+	}
+	return PF_OK;
+}
+
+pf_status pf_model_evaluate(pf_env *env, const pf_model_desc *model, const pf_profile_desc *profiles,
+                            const double *psf, double *image, uint32_t *out_w, uint32_t *out_h)
+{
+	if (!env || !model || !image || (!profiles && model->n_profiles)) {
+		return fail(PF_ERR_INVALID_PARAMETER, "pf_model_evaluate: NULL argument");
+	}
+	pf_model_desc m = *model;
+	m.first_profile = 0;
+	const bool has_psf = psf && m.psf_w > 0 && m.psf_h > 0;
+	m.psf_offset = has_psf ? 0 : -1;
+	pf_batch *b = nullptr;
+	pf_status s = pf_batch_create(env, &m, 1, profiles, m.n_profiles, has_psf ? psf : nullptr,
+	                              has_psf ? (size_t)m.psf_w * m.psf_h : 0, &b);
+	if (s != PF_OK) return s;
+	const size_t n = b->total_out;
+	double *d_out = nullptr;
+	cudaError_t e = cudaMalloc(&d_out, sizeof(double) * std::max<size_t>(1, n));
+	if (e != cudaSuccess) {
+		pf_batch_destroy(b);
+		return fail(PF_ERR_NO_MEMORY, std::string("pf_model_evaluate: ") + cudaGetErrorString(e));
+	}
+	s = pf_forward(b, d_out, nullptr, nullptr);
+	if (s == PF_OK) s = pf_batch_check(b, nullptr);
+	if (s == PF_OK) {
+		e = cudaMemcpy(image, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost);
+		if (e != cudaSuccess) s = fail(PF_ERR_CUDA, std::string("pf_model_evaluate: ") + cudaGetErrorString(e));
+	}
+	if (s == PF_OK) {
+		if (out_w) *out_w = b->mdev[0].out_w;
+		if (out_h) *out_h = b->mdev[0].out_h;
+	}
+	cudaFree(d_out);
+	pf_batch_destroy(b);
+	return s;
+}
+
+pf_status pf_convolve(pf_env *env, const double *src, uint32_t w, uint32_t h, const double *krn, uint32_t kw,
+                      uint32_t kh, const uint8_t *mask, double *out)
+{
+	if (!env || !src || !krn || !out) return fail(PF_ERR_INVALID_PARAMETER, "pf_convolve: NULL argument");
+	if (w == 0 || h == 0 || kw == 0 || kh == 0) return fail(PF_ERR_INVALID_PARAMETER, "pf_convolve: empty image");
+	PF_CUDA_TRY(cudaSetDevice(env->device));
+	// Convolver::convolve: an image smaller than the kernel is first extended
+	// to max(src, krn), whose y component repeats the x maximum
+	// (include/profit/image.h:204-207), and the result cropped back.
+	uint32_t ew = w, eh = h;
+	if (!(w >= kw && h >= kh)) {
+		ew = std::max(w, kw);
+		eh = ew;
+	}
+	const size_t n = (size_t)ew * eh, kn = (size_t)kw * kh;
+	std::vector<double> ext;
+	std::vector<uint8_t> emask;
+	const double *s_host = src;
+	const uint8_t *m_host = mask;
+	if (ew != w || eh != h) {
+		ext.assign(n, 0.0);
+		for (uint32_t y = 0; y < h && y < eh; y++) std::memcpy(&ext[(size_t)y * ew], src + (size_t)y * w, sizeof(double) * w);
+		s_host = ext.data();
+		if (mask) {
+			emask.assign(n, 0);
+			for (uint32_t y = 0; y < h && y < eh; y++) std::memcpy(&emask[(size_t)y * ew], mask + (size_t)y * w, w);
+			m_host = emask.data();
+		}
+	}
+	double *d_src = nullptr, *d_krn = nullptr, *d_out = nullptr;
+	uint8_t *d_mask = nullptr;
+	pf_status s = PF_OK;
+	cudaError_t e = cudaMalloc(&d_src, sizeof(double) * n);
+	if (e == cudaSuccess) e = cudaMalloc(&d_out, sizeof(double) * n);
+	if (e == cudaSuccess) e = cudaMalloc(&d_krn, sizeof(double) * kn);
+	if (e == cudaSuccess && m_host) e = cudaMalloc(&d_mask, n);
+	if (e == cudaSuccess) e = cudaMemcpy(d_src, s_host, sizeof(double) * n, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemcpy(d_krn, krn, sizeof(double) * kn, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess && m_host) e = cudaMemcpy(d_mask, m_host, n, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) {
+		pf::launch_convolve64(d_src, ew, eh, d_krn, kw, kh, d_mask, d_out, env->n_sm, env->stream);
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess) e = cudaStreamSynchronize(env->stream);
+	if (e == cudaSuccess) {
+		if (ew == w && eh == h) {
+			e = cudaMemcpy(out, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost);
+		}
+		else {
+			// crop back to the original size (result.crop(dims - diff), top-left aligned)
+			std::vector<double> tmp(n);
+			e = cudaMemcpy(tmp.data(), d_out, sizeof(double) * n, cudaMemcpyDeviceToHost);
+			for (uint32_t y = 0; y < h; y++) std::memcpy(out + (size_t)y * w, &tmp[(size_t)y * ew], sizeof(double) * w);
+		}
+	}
+	if (e != cudaSuccess) s = fail(PF_ERR_CUDA, std::string("pf_convolve: ") + cudaGetErrorString(e));
+	cudaFree(d_src);
+	cudaFree(d_krn);
+	cudaFree(d_out);
+	cudaFree(d_mask);
+	return s;
+}
+
+}  // extern "C"

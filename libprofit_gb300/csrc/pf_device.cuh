@@ -1,0 +1,110 @@
+// Device-side data layout shared by the kernels of the GB300 backend.
+//
+// A batch is a set of models (pf_model_desc) and their profiles
+// (pf_profile_desc). For each model the device holds, back to back in HBM:
+//   * its drawing area (width*fs + 2*pad_x) x (height*fs + 2*pad_y), the
+//     padded canvas Model::produce_image draws into (src/model.cpp:322-360),
+//     twice: "conv" (profiles with convolve = 1, the to_convolve image) and
+//     "direct" (the rest, the model_image), both row-major;
+//   * its output image (cropped, optionally downsampled), row-major, in the
+//     caller's buffer.
+// Work is dispatched in tiles of 32 consecutive drawing pixels of one row,
+// one warp per tile, tiles of all models numbered consecutively.
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/pf_cuda.h"
+
+namespace pf {
+
+constexpr int kMaxLevels = 16;   // subsample_pixel recursion levels held per warp
+constexpr int kMaxRes = 16;      // largest sub-pixel resolution (res*res <= 256)
+constexpr int kMaskWords = (kMaxRes * kMaxRes + 31) / 32;
+constexpr int kLevelCounts = 32;
+
+// sersic r_factor specialisations (src/sersic.cpp:79-159)
+enum RFactor : int { RF_GENERAL = 0, RF_POINTFIVE, RF_ONE, RF_TWO, RF_THREE, RF_FOUR, RF_EIGHT, RF_SIXTEEN };
+
+enum DevError : unsigned int {
+	ERR_NONE = 0,
+	ERR_LEVELS = 1u << 0,    // max_recursions beyond kMaxLevels - 1
+	ERR_RES = 1u << 1,       // resolution beyond kMaxRes
+	ERR_NONFINITE = 1u << 2, // (informational) a non-finite constant was produced
+};
+
+struct ModelDev {
+	uint32_t width, height, fs, return_fs;
+	uint32_t draw_w, draw_h, pad_x, pad_y;
+	uint32_t crop_w, crop_h, out_w, out_h;
+	double scale_x, scale_y;   // image pixel scale (Model::scale)
+	double sx, sy;             // drawing pixel scale (scale / finesampling)
+	double magzero;
+	int32_t first_profile, n_profiles;
+	int32_t conv_required, convolver;
+	int64_t psf_off;           // offset of the normalised PSF in the device PSF pool, -1 none
+	uint32_t psf_w, psf_h;
+	double psf_scale_x, psf_scale_y;
+	int64_t draw_off;          // pixel offset of the drawing area in the conv / direct scratch
+	int64_t out_off;           // pixel offset of the output image
+	int64_t tile_base;         // first tile number of this model
+	uint32_t tiles_per_row;
+	uint32_t pad0;
+};
+
+struct ProfileDev {
+	// from the descriptor (never modified on the device)
+	int32_t kind, convolve, rough, adjust, rescale_flux;
+	uint32_t resolution_in, max_recursions;
+	int32_t model;
+	double acc_in, rscale_switch_in, rscale_max_in;
+	double par[PF_NPAR];
+	// working copies after RadialProfile::initial_calculations' adjustments
+	uint32_t resolution;
+	int32_t pad1;
+	double acc, rscale_switch, rscale_max;
+	// computed by the setup kernel (RadialProfile::initial_calculations and evaluate)
+	int32_t rf_boxy, rf_t;
+	double rscale, ie, bn, lumtot, rescale_factor;
+	double cos_ang, sin_ang, xc, yc;
+	double flux_scale;
+	double bg;                 // sky: bg / fs^2
+	double psf_mag_scale;      // psf: 10^(-0.4 (mag - magzero))
+	int32_t bbx0, bbx1, bby0, bby1;   // drawing pixels outside are exactly zero
+	int64_t depth_off;         // offset of this profile's depth map (debug recording)
+	// single-precision copies for the FP32 path (setup kernel)
+	float fxc_hi, fxc_lo, fyc_hi, fyc_lo;  // centre as an unevaluated float sum
+	float fcos, fsin, finv_axrat, finv_rscale;
+	float fswitch, frmax, facc, fflux_scale;
+	float fbg;
+	int32_t fboxy;
+	float fpar[12];            // per-kind folded constants, FP_* slots
+};
+
+// Slots of ProfileDev::fpar (folded by the setup kernel)
+enum FParSlot : int {
+	FP_B = 0, FP_INVB = 1,                         // box + 2 and its inverse
+	FP_S_INV_RE2 = 2, FP_S_HALF_INV_N = 3, FP_S_INV_RE = 4, FP_S_INV_NB = 5, FP_S_K = 6,
+	FP_C_A = 2, FP_C_B_OVER_A = 3, FP_C_INV_RB = 4, FP_C_RB_A = 5, FP_C_INV_RE_A = 6, FP_C_K = 7, FP_C_INV_NA = 8,
+	FP_M_INV_RS2 = 2, FP_M_INV_RS = 3, FP_M_CON = 4,
+	FP_F_INV_ROUT = 2, FP_F_A = 3, FP_F_2MB = 4,
+	FP_K_RT = 2, FP_K_INV_RC = 3, FP_K_A = 4, FP_K_INV_A = 5, FP_K_TEMP = 6,
+	FP_E_RB = 2, FP_E_A = 3, FP_E_INV_A = 4, FP_E_INV_H1 = 5, FP_E_EXPO = 6,
+};
+
+struct DebugRec {
+	int8_t *depth;             // per profile drawing-area depth maps, or nullptr
+	unsigned long long *counts;// n_profiles * kLevelCounts, or nullptr
+};
+
+__device__ __forceinline__ int find_model(const ModelDev *models, int n_models, long long tile)
+{
+	int lo = 0, hi = n_models - 1;
+	while (lo < hi) {
+		int mid = (lo + hi + 1) >> 1;
+		if (models[mid].tile_base <= tile) lo = mid; else hi = mid - 1;
+	}
+	return lo;
+}
+
+}  // namespace pf

@@ -1,0 +1,311 @@
+// Per-profile setup on the device, in FP64, one thread per profile:
+// RadialProfile::initial_calculations (src/radial.cpp:137-199) with each
+// profile's get_rscale / get_lumtot / adjust_* overrides, the centre shift of
+// RadialProfile::evaluate (src/radial.cpp:253-255), the flux scale
+// (src/radial.cpp:219-222, src/sersic.cpp:319-325), the sky level
+// (src/sky.cpp:42-45) and the psf profile's magnitude scale (src/psf.cpp:66).
+// Also the per-model PSF normalisation of Model::set_psf
+// (include/profit/model.h:148-158, src/image.cpp:204-215).
+// Compiled with -fmad=false: the reference's arithmetic is not contracted.
+#include <cmath>
+
+#include "pf_device.cuh"
+#include "profiles_f64.cuh"
+#include "specfun.cuh"
+
+namespace pf {
+
+namespace {
+
+struct CoreSersicIntegrand {  // src/coresersic.cpp:80-87
+	const ProfileDev *p;
+	__device__ double operator()(double r) const
+	{
+		const double re = p->par[6], nser = p->par[7], rb = p->par[8], a = p->par[9], b = p->par[10];
+		return r * pow(1 + pow(r / rb, -a), b / a) *
+		       exp(-p->bn * pow((pow(r, a) + pow(rb, a)) / pow(re, a), 1 / (nser * a)));
+	}
+};
+
+struct KingIntegrand {  // src/king.cpp:76-84
+	const ProfileDev *p;
+	__device__ double operator()(double r) const
+	{
+		const double rc = p->par[6], rt = p->par[7], a = p->par[8];
+		if (r < rt) {
+			return r * pow(1 / pow(1 + pow(r / rc, 2), 1 / a) - 1 / pow(1 + pow(rt / rc, 2), 1 / a), a);
+		}
+		return 0;
+	}
+};
+
+struct BrokenExpIntegrand {  // src/brokenexponential.cpp:111-113
+	const ProfileDev *p;
+	__device__ double operator()(double r) const
+	{
+		return r * f64::broken_exponential(r, p->par[6], p->par[7], p->par[8], p->par[9]);
+	}
+};
+
+__device__ double get_rscale(const ProfileDev &p)
+{
+	switch (p.kind) {
+	case PF_SERSIC: case PF_CORESERSIC: return p.par[6];
+	case PF_MOFFAT: return p.par[6] / (2 * sqrt(pow(2, (1 / p.par[7])) - 1));  // src/moffat.cpp:81-83
+	case PF_FERRER: return p.par[6];
+	case PF_KING: return p.par[7];
+	case PF_BROKENEXP: return p.par[6] * 4;
+	}
+	return 0;
+}
+
+__device__ double get_lumtot(ProfileDev &p)
+{
+	switch (p.kind) {
+	case PF_SERSIC: {  // src/sersic.cpp:283-289
+		const double re = p.par[6], nser = p.par[7];
+		double g_factor = sf::gammafn(2 * nser);
+		return pow(re, 2) * 2 * M_PI * nser * g_factor * exp(p.bn) / pow(p.bn, 2 * nser);
+	}
+	case PF_CORESERSIC:  // src/coresersic.cpp:92-104
+		return 2 * M_PI * sf::qag(CoreSersicIntegrand{&p}, 0., 0., true, 1e-4, 1e-4, nullptr);
+	case PF_MOFFAT:  // src/moffat.cpp:77-79
+		return pow(p.rscale, 2) * M_PI / (p.par[7] - 1);
+	case PF_FERRER: {  // src/ferrer.cpp:78-101
+		const double a = p.par[7], b = p.par[8];
+		double g_factor = a * sf::beta(a, 1 + 2 / (2 - b));
+		return pow(p.par[6], 2) * M_PI * g_factor;
+	}
+	case PF_KING:  // src/king.cpp:87-96
+		return 2 * M_PI * sf::qag(KingIntegrand{&p}, 0., p.par[7], false, 1e-4, 1e-4, nullptr);
+	case PF_BROKENEXP:  // src/brokenexponential.cpp:115-126
+		return 2 * M_PI * sf::qag(BrokenExpIntegrand{&p}, 0., 0., true, 1e-4, 1e-4, nullptr);
+	}
+	return 0;
+}
+
+__device__ double sersic_fluxfrac(const ProfileDev &p, double fraction)  // src/sersic.cpp:257-260
+{
+	double ratio = sf::qgamma(fraction, 2 * p.par[7]) / p.bn;
+	return p.par[6] * pow(ratio, p.par[7]);
+}
+
+__device__ double moffat_fluxfrac(const ProfileDev &p, double fraction)  // src/moffat.cpp:73-75
+{
+	return p.rscale * sqrt(pow(1 - fraction, 1 / (1 - p.par[7])) - 1);
+}
+
+__device__ double adjust_rscale_switch(const ProfileDev &p)
+{
+	switch (p.kind) {
+	case PF_SERSIC: {  // src/sersic.cpp:262-272
+		const double nser = p.par[7];
+		double rs = ceil(sersic_fluxfrac(p, 1. - nser * nser / 2e3));
+		rs = sf::dmax(sf::dmin(rs, 20.), 2.);
+		return rs / p.par[6];
+	}
+	case PF_MOFFAT: {  // src/moffat.cpp:88-91
+		double rs = sf::dmax(moffat_fluxfrac(p, 0.9999), 1.823 * p.par[6]);
+		return sf::dmax(sf::dmin(rs, 20.), 2.) / p.rscale;
+	}
+	case PF_CORESERSIC: return 1;     // src/coresersic.cpp:119-121
+	case PF_FERRER: return 0.5;       // src/ferrer.cpp:103-105
+	case PF_KING: return 0.5;         // src/king.cpp:98-100
+	case PF_BROKENEXP: return 1;      // src/brokenexponential.cpp:128-130
+	}
+	return 1;
+}
+
+__device__ double adjust_rscale_max(const ProfileDev &p)
+{
+	switch (p.kind) {
+	case PF_SERSIC: return ceil(sf::dmax(sersic_fluxfrac(p, 0.9999), 2.) / p.par[6]);  // src/sersic.cpp:274-276
+	case PF_MOFFAT: return ceil(sf::dmax(moffat_fluxfrac(p, 0.9999), 2.) / p.rscale);  // src/moffat.cpp:93-95
+	case PF_CORESERSIC: return 100;
+	case PF_FERRER: return 1;
+	case PF_KING: return 1.5;
+	case PF_BROKENEXP: return 100;
+	}
+	return 0;
+}
+
+__device__ double adjust_acc(const ProfileDev &p, double acc)
+{
+	switch (p.kind) {
+	case PF_SERSIC:  // src/sersic.cpp:278-281
+		acc /= sqrt(p.par[7]);
+		return sf::dmax(0.1, acc) / p.par[PF_P_AXRAT];
+	case PF_MOFFAT:  // src/moffat.cpp:97-99
+		return 0.1 / p.par[PF_P_AXRAT];
+	}
+	return acc;
+}
+
+__device__ bool almost_equals(double x, double y)  // src/utils.cpp:101-103 with e = 1e-10
+{
+	return fabs(x - y) < fabs(1e-10);
+}
+
+__device__ void choose_rfactor(ProfileDev &p)  // src/sersic.cpp:225-255
+{
+	const double box = p.par[PF_P_BOX];
+	double inv_exponent = p.par[7];
+	p.rf_boxy = box != 0;
+	if (box != 0) {
+		inv_exponent *= (box + 2);
+	}
+	if (almost_equals(inv_exponent, 0.5)) p.rf_t = RF_POINTFIVE;
+	else if (almost_equals(inv_exponent, 1)) p.rf_t = RF_ONE;
+	else if (almost_equals(inv_exponent, 2)) p.rf_t = RF_TWO;
+	else if (almost_equals(inv_exponent, 3)) p.rf_t = RF_THREE;
+	else if (almost_equals(inv_exponent, 4)) p.rf_t = RF_FOUR;
+	else if (almost_equals(inv_exponent, 8)) p.rf_t = RF_EIGHT;
+	else if (almost_equals(inv_exponent, 16)) p.rf_t = RF_SIXTEEN;
+	else p.rf_t = RF_GENERAL;
+}
+
+__device__ int clamp_index(double v, int lo, int hi)
+{
+	if (!(v > lo)) return lo;   // also catches NaN
+	if (v > hi) return hi;
+	return (int)v;
+}
+
+__device__ void radial_setup(ProfileDev &p, const ModelDev &m, unsigned int *err)
+{
+	if (p.kind == PF_SERSIC) {
+		choose_rfactor(p);
+	}
+	if (p.kind == PF_SERSIC || p.kind == PF_CORESERSIC) {  // src/sersic.cpp:297, src/coresersic.cpp:112
+		p.bn = sf::qgamma(0.5, 2 * p.par[7]);
+	}
+	p.rscale = get_rscale(p);
+	const double box = p.par[PF_P_BOX], axrat = p.par[PF_P_AXRAT];
+	double b2 = box + 2;
+	double r_box = M_PI * b2 / (2 * sf::beta(1 / b2, 1 / b2));
+	double lumtot = get_lumtot(p) * axrat / r_box;
+	p.lumtot = lumtot;
+	p.ie = pow(10, -0.4 * (p.par[PF_P_MAG] - m.magzero)) / lumtot;
+	if (p.adjust) {
+		p.rscale_switch = adjust_rscale_switch(p);
+		unsigned int res = (unsigned int)ceil(160 / (p.rscale_switch * p.rscale));
+		res += res % 2;
+		res = res < 16U ? res : 16U;
+		res = res > 4U ? res : 4U;
+		p.resolution = res;
+		if (p.rscale_max == 0) {
+			p.rscale_max = adjust_rscale_max(p);
+		}
+		p.acc = adjust_acc(p, p.acc);
+	}
+	double angrad = fmod(p.par[PF_P_ANG] + 90, 360.) * M_PI / 180.;
+	p.cos_ang = cos(angrad);
+	p.sin_ang = sin(angrad);
+	p.rescale_factor = 1;
+	if (p.kind == PF_SERSIC && p.adjust && p.rescale_flux) {  // src/sersic.cpp:302-311
+		double flux_r = p.bn * pow(p.rscale_max / p.par[6], 1 / p.par[7]);
+		flux_r = sf::pgamma(flux_r, 2 * p.par[7]);
+		p.rescale_factor = 1 / flux_r;
+	}
+	p.xc = p.par[PF_P_XCEN] + m.pad_x * m.sx;
+	p.yc = p.par[PF_P_YCEN] + m.pad_y * m.sy;
+	double flux_scale = m.sx * m.sy * p.ie;
+	if (p.kind == PF_SERSIC && p.rescale_flux) {
+		flux_scale *= p.rescale_factor;
+	}
+	p.flux_scale = flux_scale;
+
+	// Culling box: r_prof >= the pixel centre's distance to (xc, yc) because
+	// axrat <= 1, so a pixel whose centre is farther than rscale_max * rscale
+	// is exactly 0 (src/radial.cpp:323-325). One pixel of margin.
+	p.bbx0 = 0;
+	p.bby0 = 0;
+	p.bbx1 = (int)m.draw_w - 1;
+	p.bby1 = (int)m.draw_h - 1;
+	if (p.rscale_max > 0) {
+		double R = p.rscale_max * p.rscale;
+		if (R == R && R < 1e12) {
+			p.bbx0 = clamp_index(floor((p.xc - R) / m.sx - 0.5) - 1, 0, (int)m.draw_w);
+			p.bbx1 = clamp_index(ceil((p.xc + R) / m.sx - 0.5) + 1, -1, (int)m.draw_w - 1);
+			p.bby0 = clamp_index(floor((p.yc - R) / m.sy - 0.5) - 1, 0, (int)m.draw_h);
+			p.bby1 = clamp_index(ceil((p.yc + R) / m.sy - 0.5) + 1, -1, (int)m.draw_h - 1);
+		}
+	}
+	unsigned int max_res = p.resolution;
+	unsigned int max_rec = p.max_recursions;
+	if (p.kind == PF_SERSIC && p.adjust && p.par[7] > 1) {  // central pixel, src/sersic.cpp:339-345
+		max_res = max_res > 8U ? max_res : 8U;
+		max_rec = max_rec > 10U ? max_rec : 10U;
+	}
+	if (!p.rough) {
+		if (max_rec + 1 > (unsigned int)kMaxLevels) atomicOr(err, (unsigned int)ERR_LEVELS);
+		if (max_res > (unsigned int)kMaxRes) atomicOr(err, (unsigned int)ERR_RES);
+	}
+}
+
+}  // namespace
+
+__global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs, int n_profiles,
+                                      unsigned int *tile_counter, unsigned int *err)
+{
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		*tile_counter = 0;
+	}
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= n_profiles) {
+		return;
+	}
+	ProfileDev p = profs[t];
+	const ModelDev &m = models[p.model];
+	p.resolution = p.resolution_in;
+	p.acc = p.acc_in;
+	p.rscale_switch = p.rscale_switch_in;
+	p.rscale_max = p.rscale_max_in;
+	if (p.kind >= PF_SERSIC && p.kind <= PF_BROKENEXP) {
+		radial_setup(p, m, err);
+	}
+	else if (p.kind == PF_SKY) {
+		p.bg = p.par[6] / (m.fs * m.fs);  // src/sky.cpp:42-45
+	}
+	else if (p.kind == PF_PSF) {
+		p.psf_mag_scale = pow(10, -0.4 * (p.par[PF_P_MAG] - m.magzero));
+	}
+	profs[t] = p;
+}
+
+// One block per model: sum in element order (std::accumulate), then divide.
+__global__ void normalise_psf_kernel(const ModelDev *models, const double *raw, double *norm)
+{
+	const ModelDev &m = models[blockIdx.x];
+	if (m.psf_off < 0) {
+		return;
+	}
+	const size_t n = (size_t)m.psf_w * m.psf_h;
+	__shared__ double total;
+	if (threadIdx.x == 0) {
+		double s = 0.;
+		for (size_t i = 0; i < n; i++) s += raw[m.psf_off + i];
+		total = s;
+	}
+	__syncthreads();
+	const double s = total;
+	for (size_t i = threadIdx.x; i < n; i += blockDim.x) {
+		double v = raw[m.psf_off + i];
+		norm[m.psf_off + i] = s > 0 ? v / s : v;
+	}
+}
+
+void launch_setup(const ModelDev *models, ProfileDev *profs, int n_profiles, int n_models,
+                  unsigned int *tile_counter, unsigned int *err, const double *psf_raw, double *psf_norm,
+                  bool have_psf, cudaStream_t stream)
+{
+	int threads = 64;
+	int blocks = (n_profiles + threads - 1) / threads;
+	if (blocks < 1) blocks = 1;
+	setup_profiles_kernel<<<blocks, threads, 0, stream>>>(models, profs, n_profiles, tile_counter, err);
+	if (have_psf && n_models > 0) {
+		normalise_psf_kernel<<<n_models, 128, 0, stream>>>(models, psf_raw, psf_norm);
+	}
+}
+
+}  // namespace pf
