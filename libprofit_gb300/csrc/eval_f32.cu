@@ -1,0 +1,461 @@
+// Batched single-precision path: FP32 profile values, FP64 where precision
+// decides the result.
+//
+// Same structure as the plain FP64 path (eval_f64.cu): one warp per 32-pixel
+// row tile of a model's drawing area, the model's profiles in order, and a
+// warp-cooperative depth-first recursion for the pixels that
+// RadialProfile::evaluate_cpu subsamples (src/radial.cpp:291-344,
+// subsample_pixel src/radial.cpp:55-135). The differences:
+//   * profile values are computed in FP32 (profiles_f32.cuh), coordinates
+//     relative to the profile centre, the pixel centre formed with an
+//     error-free float product so that it keeps full relative precision;
+//   * each sub-pixel box is tracked in FP64 relative to the profile centre
+//     (corner and bin), so that boxes 8^-11 pixel wide at the centre of a
+//     high-index Sersic profile keep their geometry; the points inside a box
+//     are FP32 offsets from its corner;
+//   * every decision the reference takes by comparison -- the accuracy test
+//     |testval/subval - 1| > acc, r/rscale > rscale_max, r/rscale >
+//     rscale_switch, the sersic central-pixel test -- is re-taken in FP64
+//     when the FP32 operands fall inside a guard band around the threshold or
+//     are not finite, so the subsampling tree is the FP64 tree;
+//   * box totals are warp reductions in FP32; the final images are FP32.
+#include <cstdint>
+
+#include "pf_device.cuh"
+#include "profiles_f32.cuh"
+#include "profiles_f64.cuh"
+#include "psf_profile.cuh"
+
+namespace pf {
+
+namespace {
+
+constexpr int kWarps32 = 8;
+// relative half-width of the band around a threshold inside which an FP32
+// comparison is re-taken in FP64 (FP32 operands carry a few 1e-7 error)
+constexpr float kGuardAcc = 1e-4f;
+constexpr float kGuardRadius = 2e-5f;
+
+struct FrameM {
+	double dx0, dy0;   // box corner relative to the profile centre
+	double bx, by;     // box size
+	float total;       // sum of the accepted sub-point values, then children
+	unsigned int mask[kMaskWords];
+};
+
+struct WarpScratchM {
+	FrameM fr[kMaxLevels];
+};
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+	return v;
+}
+
+// FP64 value and accuracy test of one sub-point (the rare re-taken decisions)
+__device__ bool test_f64(const ProfileDev &P, double dx, double dy, double xbin, double ybin, float &subval)
+{
+	const double xp = dx * P.cos_ang + dy * P.sin_ang;
+	const double yp = (-dx * P.sin_ang + dy * P.cos_ang) / P.par[PF_P_AXRAT];
+	const double s = f64::evaluate_at(P, xp, yp);
+	const double dyp = (-xbin * P.sin_ang + ybin * P.cos_ang) / P.par[PF_P_AXRAT];
+	const double t = f64::evaluate_at(P, fabs(xp), fabs(yp) + fabs(dyp));
+	subval = (float)s;
+	return fabs(t / s - 1.0) > P.acc;
+}
+
+__device__ float value_f64(const ProfileDev &P, double dx, double dy)
+{
+	const double xp = dx * P.cos_ang + dy * P.sin_ang;
+	const double yp = (-dx * P.sin_ang + dy * P.cos_ang) / P.par[PF_P_AXRAT];
+	return (float)f64::evaluate_at(P, xp, yp);
+}
+
+__device__ void eval_frame_m(const ProfileDev &P, WarpScratchM &ws, int L, unsigned int res, float inv_res,
+                             double dinv_res, unsigned int max_rec, int lane, unsigned long long *counts)
+{
+	FrameM &f = ws.fr[L];
+	const double dx0 = f.dx0, dy0 = f.dy0;
+	const double xbin = f.bx * dinv_res, ybin = f.by * dinv_res;
+	const float fdx0 = (float)dx0, fdy0 = (float)dy0;
+	const float fxbin = (float)f.bx * inv_res, fybin = (float)f.by * inv_res;
+	const bool recurse = res > 1 && (unsigned int)L < max_rec;
+	const unsigned int n = res * res;
+	const float c = P.fcos, s = P.fsin, iq = P.finv_axrat;
+	const float fdyp = fabsf((-fxbin * s + fybin * c) * iq);
+	if (counts && lane == 0 && L < kLevelCounts) {
+		atomicAdd(&counts[L], 1ull);
+	}
+	float part = 0.f;
+	for (unsigned int base = 0; base < n; base += 32) {
+		const unsigned int idx = base + lane;
+		bool fail = false;
+		if (idx < n) {
+			const unsigned int i = idx / res, j = idx % res;
+			const float dx = fdx0 + ((float)i + 0.5f) * fxbin;
+			const float dy = fdy0 + ((float)j + 0.5f) * fybin;
+			const float xp = dx * c + dy * s;
+			const float yp = (dy * c - dx * s) * iq;
+			float sub = f32::evaluate_at(P, xp, yp);
+			if (recurse) {
+				const float t = f32::evaluate_at(P, fabsf(xp), fabsf(yp) + fdyp);
+				const float d = fabsf(t / sub - 1.f);
+				if (!(isfinite(d) && isfinite(sub)) || fabsf(d - P.facc) <= kGuardAcc * (P.facc + 1.f)) {
+					fail = test_f64(P, dx0 + (i + 0.5) * xbin, dy0 + (j + 0.5) * ybin, xbin, ybin, sub);
+				}
+				else {
+					fail = d > P.facc;
+				}
+			}
+			else if (!isfinite(sub)) {
+				sub = value_f64(P, dx0 + (i + 0.5) * xbin, dy0 + (j + 0.5) * ybin);
+			}
+			if (!fail) part += sub;
+		}
+		const unsigned int word = __ballot_sync(0xffffffffu, fail);
+		if (lane == 0) f.mask[base >> 5] = word;
+	}
+	part = warp_sum(part);
+	if (lane == 0) f.total = part;
+	__syncwarp();
+}
+
+// subsample_pixel on a box given relative to the profile centre
+__device__ float warp_subsample_m(const ProfileDev &P, WarpScratchM &ws, double dx0, double dy0, double bx,
+                                  double by, unsigned int res, unsigned int max_rec, int lane,
+                                  unsigned long long *counts, int &deepest)
+{
+	if (lane == 0) {
+		ws.fr[0].dx0 = dx0;
+		ws.fr[0].dy0 = dy0;
+		ws.fr[0].bx = bx;
+		ws.fr[0].by = by;
+	}
+	__syncwarp();
+	const float inv_res = 1.f / (float)res;
+	const float inv_res2 = 1.f / (float)(res * res);
+	const double dinv_res = 1.0 / res;
+	int L = 0;
+	deepest = 1;
+	eval_frame_m(P, ws, 0, res, inv_res, dinv_res, max_rec, lane, counts);
+	const unsigned int nwords = (res * res + 31) / 32;
+	while (true) {
+		FrameM &f = ws.fr[L];
+		int k = -1;
+		for (unsigned int w = 0; w < nwords; w++) {
+			const unsigned int mw = f.mask[w];
+			if (mw) {
+				k = (int)(w * 32 + __ffs(mw) - 1);
+				break;
+			}
+		}
+		__syncwarp();
+		if (k >= 0) {
+			if (lane == 0) {
+				const unsigned int i = (unsigned int)k / res, j = (unsigned int)k % res;
+				const double cbx = f.bx * dinv_res, cby = f.by * dinv_res;
+				f.mask[k >> 5] &= ~(1u << (k & 31));
+				FrameM &ch = ws.fr[L + 1];
+				ch.dx0 = f.dx0 + i * cbx;
+				ch.dy0 = f.dy0 + j * cby;
+				ch.bx = cbx;
+				ch.by = cby;
+			}
+			__syncwarp();
+			L++;
+			if (L + 1 > deepest) deepest = L + 1;
+			eval_frame_m(P, ws, L, res, inv_res, dinv_res, max_rec, lane, counts);
+		}
+		else {
+			const float v = f.total * inv_res2;
+			if (L == 0) {
+				return v;
+			}
+			L--;
+			if (lane == 0) ws.fr[L].total += v;
+			__syncwarp();
+		}
+	}
+}
+
+__global__ void __launch_bounds__(kWarps32 * 32)
+eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const ProfileDev *__restrict__ profs,
+                    const double *__restrict__ psf_pool, float *__restrict__ conv_img, float *__restrict__ direct_img,
+                    long long n_tiles, unsigned int *tile_counter, DebugRec dbg)
+{
+	__shared__ WarpScratchM scratch[kWarps32];
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	WarpScratchM &ws = scratch[warp];
+	while (true) {
+		unsigned int t = 0;
+		if (lane == 0) t = atomicAdd(tile_counter, 1u);
+		const long long tile = (long long)__shfl_sync(0xffffffffu, t, 0);
+		if (tile >= n_tiles) break;
+		const int mi = find_model(models, n_models, tile);
+		const ModelDev &m = models[mi];
+		const long long local = tile - m.tile_base;
+		const unsigned int row = (unsigned int)(local / m.tiles_per_row);
+		const int col0 = (int)(local % m.tiles_per_row) * 32;
+		const int col1 = min(col0 + 31, (int)m.draw_w - 1);
+		const unsigned int px = (unsigned int)col0 + lane;
+		const bool active = px < m.draw_w;
+		const double *psf = m.psf_off >= 0 ? psf_pool + m.psf_off : nullptr;
+		// pixel centre (i + 1/2) * scale as an unevaluated float sum
+		const float cx = (float)px + 0.5f, cy = (float)row + 0.5f;
+		const float xh = cx * m.fsx_hi, yh = cy * m.fsy_hi;
+		const float xl = fmaf(cx, m.fsx_hi, -xh) + cx * m.fsx_lo;
+		const float yl = fmaf(cy, m.fsy_hi, -yh) + cy * m.fsy_lo;
+		float acc_conv = 0.f, acc_direct = 0.f;
+
+		for (int q = 0; q < m.n_profiles; q++) {
+			const int pi = m.first_profile + q;
+			const ProfileDev &P = profs[pi];
+			float add = 0.f;
+			bool has = false;
+			if (P.kind == PF_SKY) {
+				add = P.fbg;
+				has = active;
+			}
+			else if (P.kind == PF_PSF) {
+				double v = 0;
+				if (active && psf && psf_pixel64(P, m, psf, px, row, v)) {
+					add = (float)v;
+					has = true;
+				}
+			}
+			else if (P.kind <= PF_BROKENEXP) {
+				if ((int)row < P.bby0 || (int)row > P.bby1 || col1 < P.bbx0 || col0 > P.bbx1) {
+					continue;
+				}
+				const float dx = (xh - P.fxc_hi) + (xl - P.fxc_lo);
+				const float dy = (yh - P.fyc_hi) + (yl - P.fyc_lo);
+				const float xp = dx * P.fcos + dy * P.fsin;
+				const float yp = (dy * P.fcos - dx * P.fsin) * P.finv_axrat;
+				const float rr = sqrtf(xp * xp + yp * yp) * P.finv_rscale;
+				bool beyond = P.frmax > 0.f && rr > P.frmax;
+				bool outside = rr > P.fswitch;
+				const bool amb = (P.frmax > 0.f && fabsf(rr - P.frmax) <= kGuardRadius * P.frmax) ||
+				                 fabsf(rr - P.fswitch) <= kGuardRadius * P.fswitch || !isfinite(rr);
+				if (amb && active) {
+					// the reference's r_prof, in FP64 (src/radial.cpp:313-326)
+					const double x = m.sx / 2. + px * m.sx, y = m.sy / 2. + row * m.sy;
+					double xp64, yp64;
+					f64::to_profile(P, x, y, xp64, yp64);
+					const double r64 = sqrt(xp64 * xp64 + yp64 * yp64);
+					beyond = P.rscale_max > 0 && r64 / P.rscale > P.rscale_max;
+					outside = r64 / P.rscale > P.rscale_switch;
+				}
+				float pixel_val = 0.f;
+				int depth = 0;
+				bool need_ss = false;
+				if (beyond) {
+					depth = -1;
+				}
+				else if (P.rough || outside) {
+					pixel_val = f32::evaluate_at(P, xp, yp);
+					if (!isfinite(pixel_val)) pixel_val = value_f64(P, (double)dx, (double)dy);
+				}
+				else {
+					need_ss = true;
+				}
+				unsigned int pending = __ballot_sync(0xffffffffu, need_ss && active);
+				unsigned long long *counts = dbg.counts ? dbg.counts + (size_t)pi * kLevelCounts : nullptr;
+				while (pending) {
+					const int src = __ffs(pending) - 1;
+					pending &= pending - 1;
+					const unsigned int spx = (unsigned int)col0 + src;
+					const float sdx = __shfl_sync(0xffffffffu, dx, src);
+					const float sdy = __shfl_sync(0xffffffffu, dy, src);
+					unsigned int res = P.resolution, max_rec = P.max_recursions;
+					if (P.kind == PF_SERSIC && P.adjust && P.par[7] > 1) {  // src/sersic.cpp:331-347
+						bool center = fabsf(sdx) < m.fscale_x && fabsf(sdy) < m.fscale_y;
+						if (fabsf(fabsf(sdx) - m.fscale_x) <= 1e-5f * m.fscale_x ||
+						    fabsf(fabsf(sdy) - m.fscale_y) <= 1e-5f * m.fscale_y) {
+							const double x = m.sx / 2. + spx * m.sx, y = m.sy / 2. + row * m.sy;
+							center = fabs(x - P.xc) < m.scale_x && fabs(y - P.yc) < m.scale_y;
+						}
+						if (center) {
+							res = 8;
+							max_rec = 10;
+						}
+					}
+					if (res > (unsigned int)kMaxRes) res = kMaxRes;
+					if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
+					// pixel box relative to the profile centre, in FP64
+					const double bdx0 = (double)spx * m.sx - P.xc;
+					const double bdy0 = (double)row * m.sy - P.yc;
+					int deepest = 0;
+					const float v = warp_subsample_m(P, ws, bdx0, bdy0, m.sx, m.sy, res, max_rec, lane, counts,
+					                                 deepest);
+					if (lane == src) {
+						pixel_val = v;
+						depth = deepest;
+					}
+				}
+				if (dbg.depth && active) {
+					dbg.depth[P.depth_off + (size_t)row * m.draw_w + px] = (int8_t)depth;
+				}
+				add = P.fflux_scale * pixel_val;
+				has = active;
+			}
+			if (has) {
+				if (P.convolve) acc_conv += add;
+				else acc_direct += add;
+			}
+		}
+		if (active) {
+			const size_t idx = (size_t)m.draw_off + (size_t)row * m.draw_w + px;
+			if (m.conv_required) conv_img[idx] = acc_conv;
+			direct_img[idx] = acc_direct;
+		}
+	}
+}
+
+// ---------------------------------------------------------------- finish
+
+constexpr int kConvTileW = 32;   // output tile width (one warp across)
+constexpr int kConvTileH = 32;   // output tile height
+constexpr int kConvRows = 4;     // output rows per thread (register blocking)
+
+__device__ __forceinline__ int find_model_out(const ModelDev *models, int n_models, long long g)
+{
+	int lo = 0, hi = n_models - 1;
+	while (lo < hi) {
+		int mid = (lo + hi + 1) >> 1;
+		if (models[mid].out_off <= g) lo = mid; else hi = mid - 1;
+	}
+	return lo;
+}
+
+// Output tiles of all models, numbered consecutively; one block per tile.
+// The block stages the source patch and the reversed PSF in shared memory
+// and convolves directly (FP32 FMA), adds the direct image and writes the
+// cropped output. Models without convolution copy (and downsample).
+__global__ void __launch_bounds__(kConvTileW * (kConvTileH / kConvRows))
+finish32_kernel(const ModelDev *__restrict__ models, int n_models, const float *__restrict__ psf32,
+                const float *__restrict__ conv_img, const float *__restrict__ direct_img, float *__restrict__ out,
+                const long long *__restrict__ tile_base_out, long long n_out_tiles)
+{
+	extern __shared__ float smem[];
+	for (long long tile = blockIdx.x; tile < n_out_tiles; tile += gridDim.x) {
+		int lo = 0, hi = n_models - 1;
+		while (lo < hi) {
+			int mid = (lo + hi + 1) >> 1;
+			if (tile_base_out[mid] <= tile) lo = mid; else hi = mid - 1;
+		}
+		const ModelDev &m = models[lo];
+		const long long local = tile - tile_base_out[lo];
+		// output tiles cover the crop area (before downsampling)
+		const int tiles_x = (m.crop_w + kConvTileW - 1) / kConvTileW;
+		const int ox0 = (int)(local % tiles_x) * kConvTileW;
+		const int oy0 = (int)(local / tiles_x) * kConvTileH;
+		const int tx = threadIdx.x % kConvTileW, ty = threadIdx.x / kConvTileW;
+		const bool downsample = m.fs > 1 && !m.return_fs;
+		float res[kConvRows];
+		for (int r = 0; r < kConvRows; r++) res[r] = 0.f;
+		if (m.conv_required) {
+			const int kw = (int)m.psf_w, kh = (int)m.psf_h;
+			const int pw = kConvTileW + kw - 1, ph = kConvTileH + kh - 1;
+			float *s_src = smem;
+			float *s_krn = smem + pw * ph;
+			// source patch: drawing pixels (ox0 + pad_x - kw/2 .. , oy0 + pad_y - kh/2 ..)
+			const int sx0 = ox0 + (int)m.pad_x - kw / 2, sy0 = oy0 + (int)m.pad_y - kh / 2;
+			const float *src = conv_img + m.draw_off;
+			for (int i = threadIdx.x; i < pw * ph; i += blockDim.x) {
+				const int yy = sy0 + i / pw, xx = sx0 + i % pw;
+				float v = 0.f;
+				if (xx >= 0 && xx < (int)m.draw_w && yy >= 0 && yy < (int)m.draw_h) v = src[(size_t)yy * m.draw_w + xx];
+				s_src[i] = v;
+			}
+			const float *krn = psf32 + m.psf_off;
+			const int kn = kw * kh;
+			for (int i = threadIdx.x; i < kn; i += blockDim.x) s_krn[i] = krn[kn - 1 - i];  // reversed
+			__syncthreads();
+			// out(x, y) = sum_{l,k} src(x + k, y + l) * rev(k, l) within the patch
+			const int yb = ty * kConvRows;
+			for (int k = 0; k < kw; k++) {
+				const float *col = s_src + yb * pw + tx + k;
+				float win[kConvRows];
+#pragma unroll
+				for (int r = 0; r < kConvRows; r++) win[r] = 0.f;
+				for (int l = 0; l < kh + kConvRows - 1; l++) {
+					const float sv = col[l * pw];
+#pragma unroll
+					for (int r = 0; r < kConvRows; r++) {
+						const int kl = l - r;
+						if (kl >= 0 && kl < kh) res[r] = fmaf(sv, s_krn[kl * kw + k], res[r]);
+					}
+				}
+			}
+			__syncthreads();
+		}
+		const float *direct = direct_img + m.draw_off;
+		for (int r = 0; r < kConvRows; r++) {
+			const int ox = ox0 + tx, oy = oy0 + ty * kConvRows + r;
+			if (ox < (int)m.crop_w && oy < (int)m.crop_h) {
+				const float v = direct[(size_t)(oy + m.pad_y) * m.draw_w + ox + m.pad_x] + res[r];
+				if (downsample) {
+					atomicAdd(&out[m.out_off + (size_t)(oy / m.fs) * m.out_w + ox / m.fs], v);
+				}
+				else {
+					out[m.out_off + (size_t)oy * m.out_w + ox] = v;
+				}
+			}
+		}
+	}
+}
+
+__global__ void psf_to_float_kernel(const double *in, float *out, long long n)
+{
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+		out[i] = (float)in[i];
+}
+
+}  // namespace
+
+void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs, const double *psf_pool,
+                   float *conv_img, float *direct_img, long long n_tiles, unsigned int *tile_counter, DebugRec dbg,
+                   int n_sm, cudaStream_t stream)
+{
+	int blocks = n_sm * 4;
+	long long need = (n_tiles + kWarps32 - 1) / kWarps32;
+	if (need < blocks) blocks = (int)(need > 0 ? need : 1);
+	eval_tiles32_kernel<<<blocks, kWarps32 * 32, 0, stream>>>(models, n_models, profs, psf_pool, conv_img, direct_img,
+	                                                          n_tiles, tile_counter, dbg);
+}
+
+size_t finish32_smem(unsigned int max_psf_w, unsigned int max_psf_h)
+{
+	return sizeof(float) * ((size_t)(kConvTileW + max_psf_w - 1) * (kConvTileH + max_psf_h - 1) +
+	                        (size_t)max_psf_w * max_psf_h);
+}
+
+long long finish32_tiles(unsigned int crop_w, unsigned int crop_h)
+{
+	return (long long)((crop_w + kConvTileW - 1) / kConvTileW) * ((crop_h + kConvTileH - 1) / kConvTileH);
+}
+
+void launch_finish32(const ModelDev *models, int n_models, const float *psf32, const float *conv_img,
+                     const float *direct_img, float *out, const long long *tile_base_out, long long n_out_tiles,
+                     size_t smem, int n_sm, cudaStream_t stream)
+{
+	int blocks = (int)(n_out_tiles < (long long)n_sm * 16 ? n_out_tiles : (long long)n_sm * 16);
+	if (blocks < 1) blocks = 1;
+	finish32_kernel<<<blocks, kConvTileW * (kConvTileH / kConvRows), smem, stream>>>(
+	    models, n_models, psf32, conv_img, direct_img, out, tile_base_out, n_out_tiles);
+}
+
+cudaError_t finish32_configure(size_t smem)
+{
+	return cudaFuncSetAttribute(finish32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+void launch_psf_to_float(const double *in, float *out, long long n, cudaStream_t stream)
+{
+	if (n <= 0) return;
+	psf_to_float_kernel<<<(int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096), 256, 0, stream>>>(in, out, n);
+}
+
+}  // namespace pf

@@ -33,6 +33,16 @@ void launch_convolve64(const double *src, unsigned int w, unsigned int h, const 
 void launch_flux_sum(const ModelDev *models, int n_models, const void *images, int is_double, double *flux,
                      cudaStream_t stream);
 void launch_set_params(ProfileDev *profs, int n_profiles, const double *params, cudaStream_t stream);
+void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs, const double *psf_pool,
+                   float *conv_img, float *direct_img, long long n_tiles, unsigned int *tile_counter, DebugRec dbg,
+                   int n_sm, cudaStream_t stream);
+size_t finish32_smem(unsigned int max_psf_w, unsigned int max_psf_h);
+long long finish32_tiles(unsigned int crop_w, unsigned int crop_h);
+void launch_finish32(const ModelDev *models, int n_models, const float *psf32, const float *conv_img,
+                     const float *direct_img, float *out, const long long *tile_base_out, long long n_out_tiles,
+                     size_t smem, int n_sm, cudaStream_t stream);
+cudaError_t finish32_configure(size_t smem);
+void launch_psf_to_float(const double *in, float *out, long long n, cudaStream_t stream);
 }  // namespace pf
 
 namespace {
@@ -195,6 +205,12 @@ struct pf_batch {
 	int8_t *d_depth = nullptr;
 	size_t depth_total = 0;
 	unsigned long long *d_counts = nullptr;
+	// single-precision path
+	float *d_psf32 = nullptr;
+	long long *d_tile_base_out = nullptr;
+	long long n_out_tiles = 0;
+	size_t finish_smem = 0;
+	bool any_downsample = false;
 };
 
 extern "C" {
@@ -263,6 +279,8 @@ void pf_batch_destroy(pf_batch *b)
 	cudaFree(b->d_err);
 	cudaFree(b->d_depth);
 	cudaFree(b->d_counts);
+	cudaFree(b->d_psf32);
+	cudaFree(b->d_tile_base_out);
 	cudaFreeHost(b->h_profiles);
 	delete b;
 }
@@ -318,6 +336,12 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		d.scale_y = m.scale_y;
 		d.sx = m.scale_x / m.finesampling;
 		d.sy = m.scale_y / m.finesampling;
+		d.fsx_hi = (float)d.sx;
+		d.fsx_lo = (float)(d.sx - (double)d.fsx_hi);
+		d.fsy_hi = (float)d.sy;
+		d.fsy_lo = (float)(d.sy - (double)d.fsy_hi);
+		d.fscale_x = (float)m.scale_x;
+		d.fscale_y = (float)m.scale_y;
 		d.magzero = m.magzero;
 		d.first_profile = (int32_t)m.first_profile;
 		d.n_profiles = (int32_t)m.n_profiles;
@@ -344,8 +368,25 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 	if (b->n_tiles >= (1ll << 32)) {
 		return fail(PF_ERR_UNSUPPORTED, "batch too large: more than 2^32 tiles of 32 pixels");
 	}
+	std::vector<long long> tile_base_out(std::max<size_t>(1, n_models), 0);
 	if (!b->dbl) {
-		return fail(PF_ERR_UNSUPPORTED, "the single-precision path is not available in this build");
+		unsigned int max_kw = 1, max_kh = 1;
+		long long t = 0;
+		for (size_t i = 0; i < n_models; i++) {
+			const pf::ModelDev &d = b->mdev[i];
+			tile_base_out[i] = t;
+			t += pf::finish32_tiles(d.crop_w, d.crop_h);
+			if (d.conv_required) {
+				max_kw = std::max(max_kw, d.psf_w);
+				max_kh = std::max(max_kh, d.psf_h);
+			}
+			b->any_downsample |= d.fs > 1 && !d.return_fs;
+		}
+		b->n_out_tiles = t;
+		b->finish_smem = pf::finish32_smem(max_kw, max_kh);
+		if (b->finish_smem > 227 * 1024) {
+			return fail(PF_ERR_UNSUPPORTED, "PSF too large for the shared-memory direct convolution");
+		}
 	}
 
 	PF_CUDA_TRY(cudaMallocHost(&b->h_profiles, sizeof(pf::ProfileDev) * std::max<size_t>(1, n_profiles)));
@@ -398,8 +439,18 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		// PSF normalisation (Model::set_psf), once per batch
 		pf::launch_setup(b->d_models, b->d_profiles, 0, (int)n_models, b->d_counter, b->d_err, b->d_psf_raw,
 		                 b->d_psf_norm, true, env->stream);
+		if (!b->dbl) {
+			PF_CUDA_TRY(cudaMalloc(&b->d_psf32, sizeof(float) * psf_pool_len));
+			pf::launch_psf_to_float(b->d_psf_norm, b->d_psf32, (long long)psf_pool_len, env->stream);
+		}
 		PF_CUDA_TRY(cudaGetLastError());
 		PF_CUDA_TRY(cudaStreamSynchronize(env->stream));
+	}
+	if (!b->dbl) {
+		PF_CUDA_TRY(cudaMalloc(&b->d_tile_base_out, sizeof(long long) * tile_base_out.size()));
+		PF_CUDA_TRY(cudaMemcpy(b->d_tile_base_out, tile_base_out.data(), sizeof(long long) * tile_base_out.size(),
+		                       cudaMemcpyHostToDevice));
+		PF_CUDA_TRY(pf::finish32_configure(b->finish_smem));
 	}
 	b->params_dirty = true;
 	return PF_OK;
@@ -514,13 +565,25 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 	}
 	pf::launch_setup(b->d_models, b->d_profiles, n_profiles, n_models, b->d_counter, b->d_err, nullptr, nullptr,
 	                 false, stream);
-	pf::launch_eval64(b->d_models, n_models, b->d_profiles, b->d_psf_norm, (double *)b->d_conv,
-	                  (double *)b->d_direct, b->n_tiles, b->d_counter, dbg, b->env->n_sm, stream);
-	pf::launch_finish64(b->d_models, n_models, b->d_psf_norm, (const double *)b->d_conv,
-	                    (const double *)b->d_direct, (double *)images_dev, (long long)b->total_out, b->env->n_sm,
-	                    stream);
+	if (b->dbl) {
+		pf::launch_eval64(b->d_models, n_models, b->d_profiles, b->d_psf_norm, (double *)b->d_conv,
+		                  (double *)b->d_direct, b->n_tiles, b->d_counter, dbg, b->env->n_sm, stream);
+		pf::launch_finish64(b->d_models, n_models, b->d_psf_norm, (const double *)b->d_conv,
+		                    (const double *)b->d_direct, (double *)images_dev, (long long)b->total_out,
+		                    b->env->n_sm, stream);
+	}
+	else {
+		pf::launch_eval32(b->d_models, n_models, b->d_profiles, b->d_psf_norm, (float *)b->d_conv,
+		                  (float *)b->d_direct, b->n_tiles, b->d_counter, dbg, b->env->n_sm, stream);
+		if (b->any_downsample) {
+			PF_CUDA_TRY(cudaMemsetAsync(images_dev, 0, sizeof(float) * b->total_out, stream));
+		}
+		pf::launch_finish32(b->d_models, n_models, b->d_psf32, (const float *)b->d_conv, (const float *)b->d_direct,
+		                    (float *)images_dev, b->d_tile_base_out, b->n_out_tiles, b->finish_smem, b->env->n_sm,
+		                    stream);
+	}
 	if (flux_dev) {
-		pf::launch_flux_sum(b->d_models, n_models, images_dev, 1, flux_dev, stream);
+		pf::launch_flux_sum(b->d_models, n_models, images_dev, b->dbl ? 1 : 0, flux_dev, stream);
 	}
 	PF_CUDA_TRY(cudaGetLastError());
 	return PF_OK;
@@ -577,8 +640,9 @@ pf_status pf_model_evaluate(pf_env *env, const pf_model_desc *model, const pf_pr
 	                              has_psf ? (size_t)m.psf_w * m.psf_h : 0, &b);
 	if (s != PF_OK) return s;
 	const size_t n = b->total_out;
-	double *d_out = nullptr;
-	cudaError_t e = cudaMalloc(&d_out, sizeof(double) * std::max<size_t>(1, n));
+	const size_t elem = b->dbl ? sizeof(double) : sizeof(float);
+	void *d_out = nullptr;
+	cudaError_t e = cudaMalloc(&d_out, elem * std::max<size_t>(1, n));
 	if (e != cudaSuccess) {
 		pf_batch_destroy(b);
 		return fail(PF_ERR_NO_MEMORY, std::string("pf_model_evaluate: ") + cudaGetErrorString(e));
@@ -586,7 +650,14 @@ pf_status pf_model_evaluate(pf_env *env, const pf_model_desc *model, const pf_pr
 	s = pf_forward(b, d_out, nullptr, nullptr);
 	if (s == PF_OK) s = pf_batch_check(b, nullptr);
 	if (s == PF_OK) {
-		e = cudaMemcpy(image, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost);
+		if (b->dbl) {
+			e = cudaMemcpy(image, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost);
+		}
+		else {
+			std::vector<float> tmp(n);
+			e = cudaMemcpy(tmp.data(), d_out, sizeof(float) * n, cudaMemcpyDeviceToHost);
+			for (size_t i = 0; i < n; i++) image[i] = tmp[i];
+		}
 		if (e != cudaSuccess) s = fail(PF_ERR_CUDA, std::string("pf_model_evaluate: ") + cudaGetErrorString(e));
 	}
 	if (s == PF_OK) {

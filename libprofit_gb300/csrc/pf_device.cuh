@@ -50,6 +50,8 @@ struct ModelDev {
 	int64_t tile_base;         // first tile number of this model
 	uint32_t tiles_per_row;
 	uint32_t pad0;
+	float fsx_hi, fsx_lo, fsy_hi, fsy_lo;  // drawing pixel scale as unevaluated float sums
+	float fscale_x, fscale_y;              // image pixel scale (sersic central pixel test)
 };
 
 struct ProfileDev {

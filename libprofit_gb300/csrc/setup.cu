@@ -171,6 +171,81 @@ __device__ int clamp_index(double v, int lo, int hi)
 	return (int)v;
 }
 
+// Constants of the FP32 path (profiles_f32.cuh), folded once per profile.
+__device__ void fold_single_precision(ProfileDev &p)
+{
+	const double box = p.par[PF_P_BOX];
+	const double B = box + 2;
+	p.fxc_hi = (float)p.xc;
+	p.fxc_lo = (float)(p.xc - (double)p.fxc_hi);
+	p.fyc_hi = (float)p.yc;
+	p.fyc_lo = (float)(p.yc - (double)p.fyc_hi);
+	p.fcos = (float)p.cos_ang;
+	p.fsin = (float)p.sin_ang;
+	p.finv_axrat = (float)(1 / p.par[PF_P_AXRAT]);
+	p.finv_rscale = (float)(1 / p.rscale);
+	p.fswitch = (float)p.rscale_switch;
+	p.frmax = (float)p.rscale_max;
+	p.facc = (float)p.acc;
+	p.fflux_scale = (float)p.flux_scale;
+	p.fboxy = box != 0;
+	float *c = p.fpar;
+	for (int i = 0; i < 12; i++) c[i] = 0.f;
+	c[FP_B] = (float)B;
+	c[FP_INVB] = (float)(1 / B);
+	const double log2e = 1.4426950408889634;
+	switch (p.kind) {
+	case PF_SERSIC: {
+		const double re = p.par[6], n = p.par[7];
+		c[FP_S_INV_RE2] = (float)(1 / (re * re));
+		c[FP_S_HALF_INV_N] = (float)(0.5 / n);
+		c[FP_S_INV_RE] = (float)(1 / re);
+		c[FP_S_INV_NB] = (float)(1 / (n * B));
+		c[FP_S_K] = (float)(p.bn * log2e);
+		break;
+	}
+	case PF_CORESERSIC: {
+		const double re = p.par[6], n = p.par[7], rb = p.par[8], a = p.par[9], b = p.par[10];
+		c[FP_C_A] = (float)a;
+		c[FP_C_B_OVER_A] = (float)(b / a);
+		c[FP_C_INV_RB] = (float)(1 / rb);
+		c[FP_C_RB_A] = (float)pow(rb, a);
+		c[FP_C_INV_RE_A] = (float)(1 / pow(re, a));
+		c[FP_C_K] = (float)(p.bn * log2e);
+		c[FP_C_INV_NA] = (float)(1 / (n * a));
+		break;
+	}
+	case PF_MOFFAT:
+		c[FP_M_INV_RS2] = (float)(1 / (p.rscale * p.rscale));
+		c[FP_M_INV_RS] = (float)(1 / p.rscale);
+		c[FP_M_CON] = (float)p.par[7];
+		break;
+	case PF_FERRER:
+		c[FP_F_INV_ROUT] = (float)(1 / p.rscale);
+		c[FP_F_A] = (float)p.par[7];
+		c[FP_F_2MB] = (float)(2 - p.par[8]);
+		break;
+	case PF_KING: {
+		const double rc = p.par[6], rt = p.par[7], a = p.par[8];
+		c[FP_K_RT] = (float)rt;
+		c[FP_K_INV_RC] = (float)(1 / rc);
+		c[FP_K_A] = (float)a;
+		c[FP_K_INV_A] = (float)(1 / a);
+		c[FP_K_TEMP] = (float)(1 / pow(1 + pow(rt / rc, 2), 1 / a));
+		break;
+	}
+	case PF_BROKENEXP: {
+		const double h1 = p.par[6], h2 = p.par[7], rb = p.par[8], a = p.par[9];
+		c[FP_E_RB] = (float)rb;
+		c[FP_E_A] = (float)a;
+		c[FP_E_INV_A] = (float)(1 / a);
+		c[FP_E_INV_H1] = (float)(1 / h1);
+		c[FP_E_EXPO] = (float)(1 / h1 - 1 / h2);
+		break;
+	}
+	}
+}
+
 __device__ void radial_setup(ProfileDev &p, const ModelDev &m, unsigned int *err)
 {
 	if (p.kind == PF_SERSIC) {
@@ -231,6 +306,7 @@ __device__ void radial_setup(ProfileDev &p, const ModelDev &m, unsigned int *err
 			p.bby1 = clamp_index(ceil((p.yc + R) / m.sy - 0.5) + 1, -1, (int)m.draw_h - 1);
 		}
 	}
+	fold_single_precision(p);
 	unsigned int max_res = p.resolution;
 	unsigned int max_rec = p.max_recursions;
 	if (p.kind == PF_SERSIC && p.adjust && p.par[7] > 1) {  // central pixel, src/sersic.cpp:339-345
@@ -266,6 +342,7 @@ __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs,
 	}
 	else if (p.kind == PF_SKY) {
 		p.bg = p.par[6] / (m.fs * m.fs);  // src/sky.cpp:42-45
+		p.fbg = (float)p.bg;
 	}
 	else if (p.kind == PF_PSF) {
 		p.psf_mag_scale = pow(10, -0.4 * (p.par[PF_P_MAG] - m.magzero));
