@@ -1,0 +1,400 @@
+"""Benchmark: batched model + VJP evaluations per second on one GB300.
+
+Workload (default): 1024 models of 256x256 pixels, each a sersic bulge
+(nser U[2,6]) plus a sersic disk (nser U[0.7,1.3]) convolved with a 25x25
+Moffat PSF; data = the model at parameters perturbed by N(0, 5 %) plus
+Gaussian noise (sigma = 1 % of each model's peak); one step = upload the
+parameter vector, render every model (FP32 values, FP64 geometry and
+decisions), chi^2 per model and d chi^2 / d (all 16 parameters of every
+model) in FP64. Inputs are synthetic and seeded (workloads.py).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun each rank renders its own copy of the workload (weak scaling,
+no collective on the data path); rank 0 prints one JSON line.
+--impl reference times the CPU oracle port of the reference's
+Model::evaluate (OpenMP over all host cores) on a bounded sample of the same
+workload, gradients by central differences (2 x 16 + 1 evaluations per model).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "batched model+VJP evals/s (FP32, ≤1e-5 rel flux err) vs plain FP64 GPU; Mpix/s"
+N_PAR_MODEL = 16
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--models", type=int, default=1024)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, value):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_problem(models, seed_offset, env64, torch):
+    """Workload specs, the batch parameter matrix and the data (rendered by
+    the FP64 path at perturbed parameters, plus noise)."""
+    import libprofit_gb300 as pg
+    import workloads as W
+    specs = W.cfg4(models)
+    par = W.param_matrix(specs)
+    rng = np.random.Generator(np.random.PCG64(4000 + seed_offset))
+    pert = par.copy()
+    pert[:, :8] *= 1 + 0.05 * rng.standard_normal((pert.shape[0], 8))
+    pert[:, 4] = np.clip(pert[:, 4], 0.05, 1.0)  # axrat stays valid
+    pert[:, 7] = np.clip(pert[:, 7], 0.3, 10.0)
+    b64 = pg.Batch([W.to_model(s, env64) for s in specs], env64)
+    b64.set_params(pert)
+    img64 = torch.zeros(b64.total_pixels, dtype=torch.float64, device="cuda")
+    b64.forward(img64)
+    b64.check()
+    data = img64.cpu().numpy()
+    sigma = np.empty_like(data)
+    for i in range(len(specs)):
+        a, z = b64.offsets[i], b64.offsets[i + 1]
+        s = 0.01 * data[a:z].max()
+        sigma[a:z] = s
+        data[a:z] += rng.normal(0, s, z - a)
+    b64.close()
+    return specs, par, data, sigma
+
+
+def cpu_baseline_sample(specs, par, budget_s=8.0):
+    """Oracle port (C restatement of the reference CPU path, OpenMP on every
+    host core): forward + central-difference gradient (2*16+1 evaluations) per
+    model on a bounded sample of the workload's models. Returns models/s."""
+    from oracle import oracle as O
+    import workloads as W
+    O.build(with_ref=False)
+    threads = os.cpu_count() or 1
+    t0 = time.time()
+    done = 0
+    rows = 0
+    for s in specs:
+        n = len(s["profiles"])
+        case = W.to_oracle_case(s)
+        O.evaluate(case, threads=threads)
+        for j in range(n):
+            kind, params = s["profiles"][j]
+            for k in ("xcen", "ycen", "mag", "ang", "axrat", "box", "re", "nser"):
+                for sgn in (1, -1):
+                    p2 = dict(params)
+                    p2[k] = p2[k] + sgn * 1e-6 * max(abs(p2[k]), 1e-3)
+                    profs = list(s["profiles"])
+                    profs[j] = (kind, p2)
+                    O.evaluate(O.Case(s["width"], s["height"], profs, psf=s.get("psf")), threads=threads)
+        done += 1
+        rows += n
+        if time.time() - t0 > budget_s:
+            break
+    dt = time.time() - t0
+    return done / dt, threads, done, dt
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the CPU oracle port on the host cores, rank 0 only."""
+    if rank != 0:
+        return
+    import workloads as W
+    specs = W.cfg4(args.models)
+    par = W.param_matrix(specs)
+    vals = []
+    for _ in range(max(1, args.warmup // 3)):
+        cpu_baseline_sample(specs[:1], par, budget_s=0.1)
+    t_all = time.time()
+    for step in range(max(1, args.steps // 10)):
+        v, threads, done, dt = cpu_baseline_sample(specs[step:], par, budget_s=5.0)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {"metric": METRIC, "value": value, "unit": "models/s", "n_gpus": args.gpus, "steps": len(vals),
+            "warmup": max(1, args.warmup // 3), "ms_per_step": 1000.0 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "1024 models 256x256, sersic bulge+disk, 25x25 Moffat PSF, model+VJP",
+                       "models": args.models},
+            "cpu_baseline": {"value": value, "unit": "models/s", "cores": threads, "kind": "port",
+                             "sample": "models rendered + 33-point central-difference gradient until 5 s per step"},
+            "e2e": {"value": value, "unit": "models/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.time() - t_all}
+    print(json.dumps(line), flush=True)
+
+
+# FP32-pipe work per evaluate_at of the sersic profile, counted from
+# profiles_f32.cuh / eval_f32.cu (FMA = 2 flops, other FP32 ops 1, each MUFU
+# op weighted 8, its issue cost against the FMA pipe: 128 vs 16 per SM-clock).
+FLOP_EVAL = 2 * 7 + 5 + 3 * 8        # coordinates + base + rf + exp: 43
+FLOP_GRAD = FLOP_EVAL + 40 + 4 * 8   # + the derivative chain (sersic_grad): 115
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build_cuda()
+    import libprofit_gb300 as pg
+    import workloads as W
+
+    torch.cuda.set_device(local)
+    env64 = pg.get_cuda_environment(local, use_double=True)
+    env32 = pg.get_cuda_environment(local, use_double=False, profile=True)
+    specs, par, data_np, sigma_np = make_problem(args.models, rank, env64, torch)
+    n_models = len(specs)
+    batch = pg.Batch([W.to_model(s, env32) for s in specs], env32)
+    batch.enable_adjoint()
+    n_prof = batch.n_profiles
+    img = torch.zeros(batch.total_pixels, dtype=torch.float32, device="cuda")
+    data = torch.tensor(data_np, dtype=torch.float32, device="cuda")
+    sigma = torch.tensor(sigma_np, dtype=torch.float32, device="cuda")
+    chi2 = torch.zeros(n_models, dtype=torch.float64, device="cuda")
+    grad = torch.zeros(n_prof * 12, dtype=torch.float64, device="cuda")
+    params = torch.tensor(par.ravel(), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+
+    def step():
+        batch.set_params_dev(params, stream=sh)
+        batch.forward_backward(img, data, sigma, chi2, grad, stream=sh)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    batch.check(stream=sh)
+    batch.stats(reset=True)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    batch.check(stream=sh)
+    stages = batch.stats(reset=True)
+    ms = max_over_ranks(world, ms)
+    ms_per_step = ms / args.steps
+    value = world * n_models * args.steps / (ms / 1000.0)
+    pix_per_step = sum(w * h for (w, h) in batch.dims)
+
+    # e2e through the public API with host buffers: parameters in from pinned
+    # host memory, chi^2 and gradients back to pinned host memory, every step
+    h_par = torch.tensor(par.ravel(), dtype=torch.float64).pin_memory()
+    h_chi2 = torch.zeros(n_models, dtype=torch.float64).pin_memory()
+    h_grad = torch.zeros(n_prof * 12, dtype=torch.float64).pin_memory()
+    e2e_steps = max(3, args.steps // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for _ in range(e2e_steps):
+            params.copy_(h_par, non_blocking=True)
+            step()
+            h_chi2.copy_(chi2, non_blocking=True)
+            h_grad.copy_(grad, non_blocking=True)
+            stream.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * n_models * e2e_steps / max_over_ranks(world, e2e_s)
+    batch.stats(reset=True)
+
+    # evaluate_at calls per step (the tree's algorithmic work), from one
+    # recorded forward pass
+    batch.record_depth(True)
+    with torch.cuda.stream(stream):
+        batch.forward(img, stream=sh)
+    torch.cuda.synchronize()
+    counts = np.zeros(32)
+    for _, c in batch.depth():
+        counts += c
+    batch.record_depth(False)
+    evals = float(counts[30] + counts[31])
+
+    # the plain FP64 per-model path (forward + VJP, one model per launch sequence)
+    fp64_rates = []
+    if rank == 0:
+        for i in range(4):
+            spec = specs[i]
+            b1 = pg.Batch([W.to_model(spec, env64)], env64)
+            b1.enable_adjoint()
+            a, z = b1.offsets[0], b1.offsets[1]
+            im1 = torch.zeros(z - a, dtype=torch.float64, device="cuda")
+            d1 = torch.tensor(data_np[batch.offsets[i]:batch.offsets[i + 1]], dtype=torch.float64, device="cuda")
+            s1 = torch.tensor(sigma_np[batch.offsets[i]:batch.offsets[i + 1]], dtype=torch.float64, device="cuda")
+            c1 = torch.zeros(1, dtype=torch.float64, device="cuda")
+            g1 = torch.zeros(len(spec["profiles"]) * 12, dtype=torch.float64, device="cuda")
+            with torch.cuda.stream(stream):
+                b1.forward_backward(im1, d1, s1, c1, g1, stream=sh)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            reps = 3
+            with torch.cuda.stream(stream):
+                for _ in range(reps):
+                    b1.forward_backward(im1, d1, s1, c1, g1, stream=sh)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            fp64_rates.append(reps / (e0.elapsed_time(e1) / 1000.0))
+            b1.close()
+    fp64_rate = statistics.median(fp64_rates) if fp64_rates else None
+
+    if rank != 0:
+        return
+
+    # roofline of the dominant stage (stage times from CUDA events on the stream)
+    per_step = {k: stages[k] / max(1, args.steps) for k in
+                ("setup_ms", "eval_ms", "finish_ms", "chi2_ms", "adjoint_conv_ms", "backward_ms")}
+    dom = max(per_step, key=per_step.get)
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s at the sampled clock
+    work = {"eval_ms": evals * FLOP_EVAL, "backward_ms": evals * FLOP_GRAD}
+    if dom in work:
+        achieved = work[dom] / (per_step[dom] / 1000.0) / 1e12
+        roof = {"bound": "fp32", "kernel": dom.replace("_ms", ""), "achieved": achieved, "peak": fp32_peak,
+                "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                "evals_per_step": evals, "flop_per_eval": FLOP_EVAL if dom == "eval_ms" else FLOP_GRAD,
+                "peak_note": "nominal FP32 FMA peak at the sampled median SM clock (no measured FP32 peak)"}
+    else:
+        roof = {"bound": "fp32", "kernel": dom.replace("_ms", ""), "achieved": None, "peak": fp32_peak,
+                "unit": "TFLOP/s", "frac": None, "traffic": None}
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, threads, done, dt = cpu_baseline_sample(specs, par, budget_s=8.0)
+        cpu = {"value": v, "unit": "models/s", "cores": threads, "kind": "port",
+               "sample": "%d model(s) rendered + 33-point central-difference gradient in %.1f s" % (done, dt)}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "models/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "%d models 256x256, sersic bulge+disk, 25x25 Moffat PSF, model+VJP (chi2 + 16 "
+                               "gradients per model)" % n_models, "models_per_gpu": n_models,
+                   "pixels_per_model": 65536, "l2": "inputs larger than L2 (images+data %.0f MB)" %
+                   (2 * 4 * pix_per_step / 1e6)},
+        "mpix_per_s": world * pix_per_step * args.steps / (ms / 1000.0) / 1e6,
+        "fp64_per_model_evals_per_s": fp64_rate,
+        "ratio_vs_fp64_per_model": (value / world) / fp64_rate if fp64_rate else None,
+        "stage_ms_per_step": per_step,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "models/s", "h2d_bytes_per_step": int(par.size * 8),
+                "d2h_bytes_per_step": int(n_models * 8 + n_prof * 12 * 8)},
+        # per step: parameter scatter, setup, eval, finish, chi2, adjoint conv, backward, gradient reduce
+        "gpu_launches": int(args.steps * 8),
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

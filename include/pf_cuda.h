@@ -130,6 +130,19 @@ typedef struct pf_batch pf_batch;
 
 /* Environment flags */
 #define PF_ENV_DOUBLE 0x1u   /* plain FP64 path: the reference's arithmetic and subsampling decisions */
+#define PF_ENV_PROFILE 0x2u  /* time every stage with CUDA events (the profiling OpenCL
+                                environment's OpenCL_times, include/profit/opencl.h:50-71) */
+
+/* Per-stage device times accumulated since the last reset (PF_ENV_PROFILE). */
+typedef struct pf_stage_times {
+	double setup_ms;         /* per-profile constants */
+	double eval_ms;          /* profile evaluation with subsampling */
+	double finish_ms;        /* convolution, add, crop, downsample */
+	double chi2_ms;          /* chi^2 and its cotangent */
+	double adjoint_conv_ms;  /* transposed convolution */
+	double backward_ms;      /* adjoint evaluation and gradient reduction */
+	uint64_t forward_calls, backward_calls;
+} pf_stage_times;
 
 /* Last error message of the calling thread. */
 PF_API const char *pf_last_error(void);
@@ -194,6 +207,33 @@ PF_API pf_status pf_batch_set_params_dev(pf_batch *batch, const double *params_d
  * pf_batch_check).
  */
 PF_API pf_status pf_forward(pf_batch *batch, void *images_dev, double *flux_dev, void *stream);
+
+/*
+ * Adjoint (no counterpart in the reference, which has no derivatives).
+ * pf_batch_enable_adjoint sizes the adjoint's device buffers once; then
+ * pf_backward, given the images pf_forward rendered (images_dev), returns
+ *   chi2_dev[m]  = sum over model m's pixels of ((image - data) / sigma)^2
+ *                  (sigma_dev may be NULL: sigma = 1), in FP64;
+ *   grad_dev[p * PF_NPAR + k] = d L / d par[k] of profile p (FP64), where L
+ *                  is the chi^2 above, or, when cotangent_dev is not NULL,
+ *                  L = sum cotangent * image (the vector-Jacobian product of
+ *                  the images; chi2 is then 0).
+ * data/sigma/cotangent have the images' layout and precision. The
+ * subsampling tree of every pixel is recomputed, not stored, and held fixed.
+ * Supported: sersic (all parameters; not rescale_flux), sky (bg), null.
+ * pf_forward_backward = pf_forward followed by pf_backward.
+ */
+PF_API pf_status pf_batch_enable_adjoint(pf_batch *batch);
+PF_API pf_status pf_backward(pf_batch *batch, const void *images_dev, const void *data_dev,
+                             const void *sigma_dev, const void *cotangent_dev, double *chi2_dev,
+                             double *grad_dev, void *stream);
+PF_API pf_status pf_forward_backward(pf_batch *batch, void *images_dev, const void *data_dev,
+                                     const void *sigma_dev, double *chi2_dev, double *grad_dev,
+                                     void *stream);
+
+/* Synchronises the batch's work and returns the stage times recorded so far
+ * (all zero unless the environment has PF_ENV_PROFILE); `reset` clears them. */
+PF_API pf_status pf_batch_stats(pf_batch *batch, pf_stage_times *times, int reset);
 
 /* Synchronises `stream` and reports any device-side error of earlier calls. */
 PF_API pf_status pf_batch_check(pf_batch *batch, void *stream);

@@ -212,10 +212,11 @@ class CUDAEnv:
     """A CUDA environment (get_opencl_environment analogue). use_double selects
     the plain FP64 path (the reference's arithmetic and subsampling decisions)."""
 
-    def __init__(self, device=0, use_double=True):
+    def __init__(self, device=0, use_double=True, profile=False):
         lib = _ffi.load()
         h = ctypes.c_void_p()
-        _check(lib.pf_env_create(int(device), _ffi.PF_ENV_DOUBLE if use_double else 0, ctypes.byref(h)))
+        flags = (_ffi.PF_ENV_DOUBLE if use_double else 0) | (_ffi.PF_ENV_PROFILE if profile else 0)
+        _check(lib.pf_env_create(int(device), flags, ctypes.byref(h)))
         self._h = h
         self.device = device
         self.use_double = use_double
@@ -236,8 +237,8 @@ class CUDAEnv:
             pass
 
 
-def get_cuda_environment(device=0, use_double=True):
-    return CUDAEnv(device, use_double)
+def get_cuda_environment(device=0, use_double=True, profile=False):
+    return CUDAEnv(device, use_double, profile)
 
 
 _default_env = None
@@ -416,13 +417,14 @@ class Batch:
 
     def forward(self, images, flux=None, stream=None):
         """Renders into `images` (device buffer of total_pixels elements,
-        float64 for a use_double environment)."""
+        float64 for a use_double environment), on `stream` (a cudaStream_t
+        handle; by default torch's current stream)."""
         _check(_ffi.load().pf_forward(self._h, ctypes.c_void_p(images.data_ptr()),
                                       None if flux is None else ctypes.c_void_p(flux.data_ptr()),
-                                      None if stream is None else ctypes.c_void_p(stream)))
+                                      _stream_arg(stream)))
 
     def check(self, stream=None):
-        _check(_ffi.load().pf_batch_check(self._h, None if stream is None else ctypes.c_void_p(stream)))
+        _check(_ffi.load().pf_batch_check(self._h, _stream_arg(stream)))
 
     def set_params(self, params):
         p = np.ascontiguousarray(params, dtype=np.float64).reshape(self.n_profiles, NPAR)
@@ -430,7 +432,28 @@ class Batch:
 
     def set_params_dev(self, params, stream=None):
         _check(_ffi.load().pf_batch_set_params_dev(self._h, ctypes.c_void_p(params.data_ptr()),
-                                                   None if stream is None else ctypes.c_void_p(stream)))
+                                                   _stream_arg(stream)))
+
+    def stats(self, reset=False):
+        """Per-stage device milliseconds (environment created with profile=True)."""
+        t = _ffi.StageTimes()
+        _check(_ffi.load().pf_batch_stats(self._h, ctypes.byref(t), int(bool(reset))))
+        return {name: getattr(t, name) for name, _ in _ffi.StageTimes._fields_}
+
+    def enable_adjoint(self):
+        """Sizes the adjoint's device buffers (pf_batch_enable_adjoint)."""
+        _check(_ffi.load().pf_batch_enable_adjoint(self._h))
+
+    def backward(self, images, data=None, sigma=None, cotangent=None, chi2=None, grad=None, stream=None):
+        """chi^2 per model and d chi^2 / d par (or, with a cotangent, the
+        vector-Jacobian product of the images) into the given device buffers."""
+        _check(_ffi.load().pf_backward(self._h, _ptr(images), _ptr(data), _ptr(sigma), _ptr(cotangent),
+                                       _ptr(chi2), _ptr(grad), _stream_arg(stream)))
+
+    def forward_backward(self, images, data, sigma=None, chi2=None, grad=None, stream=None):
+        """One model + VJP evaluation: render, then chi^2 and its gradient."""
+        _check(_ffi.load().pf_forward_backward(self._h, _ptr(images), _ptr(data), _ptr(sigma), _ptr(chi2),
+                                               _ptr(grad), _stream_arg(stream)))
 
     def record_depth(self, enable=True):
         _check(_ffi.load().pf_batch_record_depth(self._h, int(bool(enable))))
@@ -462,6 +485,28 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+_CUDA_STREAM_LEGACY = 0x1  # cudaStreamLegacy
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream_arg(stream):
+    """The cudaStream_t to pass: the given handle, else torch's current
+    stream (its legacy default stream is handle 0, passed as cudaStreamLegacy
+    because NULL selects the environment's own stream in the C ABI)."""
+    if stream is None:
+        try:
+            import torch
+            stream = torch.cuda.current_stream().cuda_stream
+        except Exception:
+            return None
+    if hasattr(stream, "cuda_stream"):
+        stream = stream.cuda_stream
+    return ctypes.c_void_p(stream if stream else _CUDA_STREAM_LEGACY)
 
 
 def _drawing_dims(model):

@@ -50,8 +50,18 @@ class ModelDesc(ctypes.Structure):
                 ("convolver", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
+class StageTimes(ctypes.Structure):
+    _fields_ = [("setup_ms", ctypes.c_double), ("eval_ms", ctypes.c_double), ("finish_ms", ctypes.c_double),
+                ("chi2_ms", ctypes.c_double), ("adjoint_conv_ms", ctypes.c_double),
+                ("backward_ms", ctypes.c_double), ("forward_calls", ctypes.c_uint64),
+                ("backward_calls", ctypes.c_uint64)]
+
+
+PF_ENV_PROFILE = 0x2
+
 _P = ctypes.c_void_p
 _SIGNATURES = {
+    "pf_batch_stats": (ctypes.c_int, [_P, ctypes.POINTER(StageTimes), ctypes.c_int]),
     "pf_last_error": (ctypes.c_char_p, []),
     "pf_version": (ctypes.c_char_p, []),
     "pf_env_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint32, ctypes.POINTER(_P)]),
@@ -71,6 +81,9 @@ _SIGNATURES = {
     "pf_batch_set_params_dev": (ctypes.c_int, [_P, _P, _P]),
     "pf_forward": (ctypes.c_int, [_P, _P, _P, _P]),
     "pf_batch_check": (ctypes.c_int, [_P, _P]),
+    "pf_batch_enable_adjoint": (ctypes.c_int, [_P]),
+    "pf_backward": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
+    "pf_forward_backward": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "pf_batch_record_depth": (ctypes.c_int, [_P, ctypes.c_int]),
     "pf_batch_depth": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
 }

@@ -87,6 +87,7 @@ __device__ void eval_frame_m(const ProfileDev &P, WarpScratchM &ws, int L, unsig
 	const float fdyp = fabsf((-fxbin * s + fybin * c) * iq);
 	if (counts && lane == 0 && L < kLevelCounts) {
 		atomicAdd(&counts[L], 1ull);
+		atomicAdd(&counts[kCountSubEvals], (unsigned long long)(recurse ? 2 * n : n));
 	}
 	float part = 0.f;
 	for (unsigned int base = 0; base < n; base += 32) {
@@ -262,6 +263,10 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 				}
 				unsigned int pending = __ballot_sync(0xffffffffu, need_ss && active);
 				unsigned long long *counts = dbg.counts ? dbg.counts + (size_t)pi * kLevelCounts : nullptr;
+				if (counts) {
+					const unsigned int nd = __popc(__ballot_sync(0xffffffffu, active && !beyond && !need_ss));
+					if (lane == 0 && nd) atomicAdd(&counts[kCountDirectEvals], (unsigned long long)nd);
+				}
 				while (pending) {
 					const int src = __ffs(pending) - 1;
 					pending &= pending - 1;

@@ -73,6 +73,7 @@ __device__ void eval_frame64(const ProfileDev &P, WarpScratch64 &ws, int L, unsi
 	const unsigned int n = res * res;
 	if (counts && lane == 0 && L < kLevelCounts) {
 		atomicAdd(&counts[L], 1ull);
+		atomicAdd(&counts[kCountSubEvals], (unsigned long long)(recurse ? 2 * n : n));
 	}
 	for (unsigned int base = 0; base < n; base += 32) {
 		const unsigned int idx = base + lane;
@@ -239,6 +240,10 @@ eval_tiles64_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 				}
 				unsigned int pending = __ballot_sync(0xffffffffu, need_ss && active);
 				unsigned long long *counts = dbg.counts ? dbg.counts + (size_t)pi * kLevelCounts : nullptr;
+				if (counts) {
+					const unsigned int nd = __popc(__ballot_sync(0xffffffffu, active && depth == 0 && !need_ss));
+					if (lane == 0 && nd) atomicAdd(&counts[kCountDirectEvals], (unsigned long long)nd);
+				}
 				while (pending) {
 					const int s = __ffs(pending) - 1;
 					pending &= pending - 1;

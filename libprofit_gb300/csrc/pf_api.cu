@@ -43,6 +43,22 @@ void launch_finish32(const ModelDev *models, int n_models, const float *psf32, c
                      size_t smem, int n_sm, cudaStream_t stream);
 cudaError_t finish32_configure(size_t smem);
 void launch_psf_to_float(const double *in, float *out, long long n, cudaStream_t stream);
+int backward_band_rows();
+template <typename T>
+void launch_chi2(const ModelDev *models, int n_models, const void *img, const void *data, const void *sigma,
+                 const void *cot, void *gout, double *chi2, cudaStream_t stream);
+template <typename T>
+size_t adjoint_conv_smem(unsigned int kw, unsigned int kh);
+long long adjoint_conv_tiles(unsigned int draw_w, unsigned int draw_h);
+template <typename T>
+cudaError_t adjoint_conv_configure(size_t smem);
+template <typename T>
+void launch_adjoint_conv(const ModelDev *models, int n_models, const void *psf, const void *gout, void *gsrc,
+                         const long long *tile_base, long long n_tiles, size_t smem, int n_sm, cudaStream_t stream);
+template <typename T>
+void launch_backward(const ModelDev *models, int n_models, const ProfileDev *profs, int n_profiles, const void *gout,
+                     const void *gsrc, const long long *band_base, const long long *part_base, long long n_items,
+                     double *partial, double *grad, int n_sm, cudaStream_t stream);
 }  // namespace pf
 
 namespace {
@@ -211,7 +227,66 @@ struct pf_batch {
 	long long n_out_tiles = 0;
 	size_t finish_smem = 0;
 	bool any_downsample = false;
+	// adjoint
+	bool adjoint = false;
+	void *d_gout = nullptr;
+	void *d_gsrc = nullptr;
+	double *d_partial = nullptr;
+	long long *d_band_base = nullptr;
+	long long *d_part_base = nullptr;
+	long long *d_adj_tile_base = nullptr;
+	long long n_band_items = 0;
+	long long n_adj_tiles = 0;
+	size_t adj_smem = 0;
+	// stage timing (PF_ENV_PROFILE)
+	struct EventPair {
+		cudaEvent_t a, b;
+		int stage;
+	};
+	std::vector<EventPair> ev_pool;
+	size_t ev_used = 0;
+	double stage_ms[6] = {0, 0, 0, 0, 0, 0};
+	uint64_t forward_calls = 0, backward_calls = 0;
 };
+
+namespace {
+
+enum Stage { ST_SETUP = 0, ST_EVAL, ST_FINISH, ST_CHI2, ST_ADJCONV, ST_BACKWARD };
+
+void fold_stage_times(pf_batch *b)
+{
+	for (size_t i = 0; i < b->ev_used; i++) {
+		float ms = 0.f;
+		if (cudaEventSynchronize(b->ev_pool[i].b) == cudaSuccess &&
+		    cudaEventElapsedTime(&ms, b->ev_pool[i].a, b->ev_pool[i].b) == cudaSuccess) {
+			b->stage_ms[b->ev_pool[i].stage] += ms;
+		}
+	}
+	b->ev_used = 0;
+}
+
+// Records the start of a stage on `s`; returns the slot to close, or -1.
+long stage_begin(pf_batch *b, int stage, cudaStream_t s)
+{
+	if (!(b->env->flags & PF_ENV_PROFILE)) return -1;
+	if (b->ev_used >= 4096) fold_stage_times(b);
+	if (b->ev_used == b->ev_pool.size()) {
+		pf_batch::EventPair p{};
+		if (cudaEventCreate(&p.a) != cudaSuccess || cudaEventCreate(&p.b) != cudaSuccess) return -1;
+		b->ev_pool.push_back(p);
+	}
+	const size_t slot = b->ev_used++;
+	b->ev_pool[slot].stage = stage;
+	cudaEventRecord(b->ev_pool[slot].a, s);
+	return (long)slot;
+}
+
+void stage_end(pf_batch *b, long slot, cudaStream_t s)
+{
+	if (slot >= 0) cudaEventRecord(b->ev_pool[(size_t)slot].b, s);
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -281,6 +356,16 @@ void pf_batch_destroy(pf_batch *b)
 	cudaFree(b->d_counts);
 	cudaFree(b->d_psf32);
 	cudaFree(b->d_tile_base_out);
+	cudaFree(b->d_gout);
+	cudaFree(b->d_gsrc);
+	cudaFree(b->d_partial);
+	cudaFree(b->d_band_base);
+	cudaFree(b->d_part_base);
+	cudaFree(b->d_adj_tile_base);
+	for (auto &p : b->ev_pool) {
+		cudaEventDestroy(p.a);
+		cudaEventDestroy(p.b);
+	}
 	cudaFreeHost(b->h_profiles);
 	delete b;
 }
@@ -563,25 +648,36 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 		dbg.depth = b->d_depth;
 		dbg.counts = b->d_counts;
 	}
+	long t = stage_begin(b, ST_SETUP, stream);
 	pf::launch_setup(b->d_models, b->d_profiles, n_profiles, n_models, b->d_counter, b->d_err, nullptr, nullptr,
 	                 false, stream);
+	stage_end(b, t, stream);
 	if (b->dbl) {
+		t = stage_begin(b, ST_EVAL, stream);
 		pf::launch_eval64(b->d_models, n_models, b->d_profiles, b->d_psf_norm, (double *)b->d_conv,
 		                  (double *)b->d_direct, b->n_tiles, b->d_counter, dbg, b->env->n_sm, stream);
+		stage_end(b, t, stream);
+		t = stage_begin(b, ST_FINISH, stream);
 		pf::launch_finish64(b->d_models, n_models, b->d_psf_norm, (const double *)b->d_conv,
 		                    (const double *)b->d_direct, (double *)images_dev, (long long)b->total_out,
 		                    b->env->n_sm, stream);
+		stage_end(b, t, stream);
 	}
 	else {
+		t = stage_begin(b, ST_EVAL, stream);
 		pf::launch_eval32(b->d_models, n_models, b->d_profiles, b->d_psf_norm, (float *)b->d_conv,
 		                  (float *)b->d_direct, b->n_tiles, b->d_counter, dbg, b->env->n_sm, stream);
+		stage_end(b, t, stream);
+		t = stage_begin(b, ST_FINISH, stream);
 		if (b->any_downsample) {
 			PF_CUDA_TRY(cudaMemsetAsync(images_dev, 0, sizeof(float) * b->total_out, stream));
 		}
 		pf::launch_finish32(b->d_models, n_models, b->d_psf32, (const float *)b->d_conv, (const float *)b->d_direct,
 		                    (float *)images_dev, b->d_tile_base_out, b->n_out_tiles, b->finish_smem, b->env->n_sm,
 		                    stream);
+		stage_end(b, t, stream);
 	}
+	b->forward_calls++;
 	if (flux_dev) {
 		pf::launch_flux_sum(b->d_models, n_models, images_dev, b->dbl ? 1 : 0, flux_dev, stream);
 	}
@@ -623,6 +719,132 @@ pf_status pf_batch_depth(pf_batch *b, int8_t *depth, size_t depth_len, int64_t *
 		for (size_t i = 0; i < tmp.size(); i++) level_counts[i] = (int64_t)tmp[i];
 	}
 	return PF_OK;
+}
+
+pf_status pf_batch_enable_adjoint(pf_batch *b)
+{
+	if (!b) return fail(PF_ERR_INVALID_PARAMETER, "batch is NULL");
+	if (b->adjoint) return PF_OK;
+	for (size_t i = 0; i < b->profiles.size(); i++) {
+		const pf_profile_desc &d = b->profiles[i];
+		const bool ok = (d.kind == PF_SERSIC && !d.rescale_flux) || d.kind == PF_SKY || d.kind == PF_NULL;
+		if (!ok) {
+			return fail(PF_ERR_UNSUPPORTED, "profile " + std::to_string(i) +
+			                                    ": the adjoint supports sersic (without rescale_flux), sky and null");
+		}
+	}
+	PF_CUDA_TRY(cudaSetDevice(b->env->device));
+	const size_t elem = b->dbl ? sizeof(double) : sizeof(float);
+	const int band_rows = pf::backward_band_rows();
+	const size_t n_models = b->mdev.size();
+	std::vector<long long> band_base(std::max<size_t>(1, n_models)), part_base(std::max<size_t>(1, n_models)),
+	    adj_tile_base(std::max<size_t>(1, n_models));
+	long long items = 0, parts = 0, tiles = 0;
+	unsigned int max_kw = 1, max_kh = 1;
+	for (size_t i = 0; i < n_models; i++) {
+		const pf::ModelDev &m = b->mdev[i];
+		const long long bands = (m.draw_h + band_rows - 1) / band_rows;
+		band_base[i] = items;
+		part_base[i] = parts;
+		adj_tile_base[i] = tiles;
+		items += bands;
+		parts += bands * m.n_profiles * pf::kGradSlots;
+		tiles += pf::adjoint_conv_tiles(m.draw_w, m.draw_h);
+		if (m.conv_required) {
+			max_kw = std::max(max_kw, m.psf_w);
+			max_kh = std::max(max_kh, m.psf_h);
+		}
+	}
+	b->n_band_items = items;
+	b->n_adj_tiles = tiles;
+	b->adj_smem = b->dbl ? pf::adjoint_conv_smem<double>(max_kw, max_kh) : pf::adjoint_conv_smem<float>(max_kw, max_kh);
+	if (b->adj_smem > 227 * 1024) return fail(PF_ERR_UNSUPPORTED, "PSF too large for the adjoint convolution");
+	PF_CUDA_TRY(cudaMalloc(&b->d_gout, elem * std::max<uint64_t>(1, b->total_out)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_gsrc, elem * std::max<size_t>(1, b->draw_total)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_partial, sizeof(double) * std::max<long long>(1, parts)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_band_base, sizeof(long long) * band_base.size()));
+	PF_CUDA_TRY(cudaMalloc(&b->d_part_base, sizeof(long long) * part_base.size()));
+	PF_CUDA_TRY(cudaMalloc(&b->d_adj_tile_base, sizeof(long long) * adj_tile_base.size()));
+	PF_CUDA_TRY(cudaMemcpy(b->d_band_base, band_base.data(), sizeof(long long) * band_base.size(), cudaMemcpyHostToDevice));
+	PF_CUDA_TRY(cudaMemcpy(b->d_part_base, part_base.data(), sizeof(long long) * part_base.size(), cudaMemcpyHostToDevice));
+	PF_CUDA_TRY(cudaMemcpy(b->d_adj_tile_base, adj_tile_base.data(), sizeof(long long) * adj_tile_base.size(),
+	                       cudaMemcpyHostToDevice));
+	PF_CUDA_TRY(b->dbl ? pf::adjoint_conv_configure<double>(b->adj_smem) : pf::adjoint_conv_configure<float>(b->adj_smem));
+	if (b->dbl && !b->d_psf_norm) {
+		// no PSF anywhere: the adjoint convolution is never launched
+	}
+	b->adjoint = true;
+	return PF_OK;
+}
+
+pf_status pf_backward(pf_batch *b, const void *images_dev, const void *data_dev, const void *sigma_dev,
+                      const void *cotangent_dev, double *chi2_dev, double *grad_dev, void *stream_ptr)
+{
+	if (!b) return fail(PF_ERR_INVALID_PARAMETER, "batch is NULL");
+	if (!b->adjoint) return fail(PF_ERR_INVALID_PARAMETER, "pf_batch_enable_adjoint has not been called");
+	if (!grad_dev || (!cotangent_dev && (!images_dev || !data_dev))) {
+		return fail(PF_ERR_INVALID_PARAMETER, "pf_backward: NULL argument");
+	}
+	cudaStream_t stream = stream_ptr ? (cudaStream_t)stream_ptr : b->env->stream;
+	PF_CUDA_TRY(cudaSetDevice(b->env->device));
+	const int n_models = (int)b->mdev.size(), n_profiles = (int)b->profiles.size();
+	if (n_models == 0) return PF_OK;
+	bool any_conv = false;
+	for (const auto &m : b->mdev) any_conv |= m.conv_required != 0;
+	long t = stage_begin(b, ST_CHI2, stream);
+	if (b->dbl) pf::launch_chi2<double>(b->d_models, n_models, images_dev, data_dev, sigma_dev, cotangent_dev,
+	                                    b->d_gout, chi2_dev, stream);
+	else pf::launch_chi2<float>(b->d_models, n_models, images_dev, data_dev, sigma_dev, cotangent_dev, b->d_gout,
+	                            chi2_dev, stream);
+	stage_end(b, t, stream);
+	if (any_conv) {
+		t = stage_begin(b, ST_ADJCONV, stream);
+		if (b->dbl) pf::launch_adjoint_conv<double>(b->d_models, n_models, b->d_psf_norm, b->d_gout, b->d_gsrc,
+		                                            b->d_adj_tile_base, b->n_adj_tiles, b->adj_smem, b->env->n_sm,
+		                                            stream);
+		else pf::launch_adjoint_conv<float>(b->d_models, n_models, b->d_psf32, b->d_gout, b->d_gsrc,
+		                                    b->d_adj_tile_base, b->n_adj_tiles, b->adj_smem, b->env->n_sm, stream);
+		stage_end(b, t, stream);
+	}
+	t = stage_begin(b, ST_BACKWARD, stream);
+	if (b->dbl) pf::launch_backward<double>(b->d_models, n_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc,
+	                                        b->d_band_base, b->d_part_base, b->n_band_items, b->d_partial, grad_dev,
+	                                        b->env->n_sm, stream);
+	else pf::launch_backward<float>(b->d_models, n_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc,
+	                                b->d_band_base, b->d_part_base, b->n_band_items, b->d_partial, grad_dev,
+	                                b->env->n_sm, stream);
+	stage_end(b, t, stream);
+	b->backward_calls++;
+	PF_CUDA_TRY(cudaGetLastError());
+	return PF_OK;
+}
+
+pf_status pf_batch_stats(pf_batch *b, pf_stage_times *times, int reset)
+{
+	if (!b || !times) return fail(PF_ERR_INVALID_PARAMETER, "pf_batch_stats: NULL argument");
+	PF_CUDA_TRY(cudaSetDevice(b->env->device));
+	fold_stage_times(b);
+	times->setup_ms = b->stage_ms[ST_SETUP];
+	times->eval_ms = b->stage_ms[ST_EVAL];
+	times->finish_ms = b->stage_ms[ST_FINISH];
+	times->chi2_ms = b->stage_ms[ST_CHI2];
+	times->adjoint_conv_ms = b->stage_ms[ST_ADJCONV];
+	times->backward_ms = b->stage_ms[ST_BACKWARD];
+	times->forward_calls = b->forward_calls;
+	times->backward_calls = b->backward_calls;
+	if (reset) {
+		for (double &v : b->stage_ms) v = 0;
+		b->forward_calls = b->backward_calls = 0;
+	}
+	return PF_OK;
+}
+
+pf_status pf_forward_backward(pf_batch *b, void *images_dev, const void *data_dev, const void *sigma_dev,
+                              double *chi2_dev, double *grad_dev, void *stream)
+{
+	pf_status s = pf_forward(b, images_dev, nullptr, stream);
+	if (s != PF_OK) return s;
+	return pf_backward(b, images_dev, data_dev, sigma_dev, nullptr, chi2_dev, grad_dev, stream);
 }
 
 pf_status pf_model_evaluate(pf_env *env, const pf_model_desc *model, const pf_profile_desc *profiles,

@@ -21,7 +21,9 @@ namespace pf {
 constexpr int kMaxLevels = 16;   // subsample_pixel recursion levels held per warp
 constexpr int kMaxRes = 16;      // largest sub-pixel resolution (res*res <= 256)
 constexpr int kMaskWords = (kMaxRes * kMaxRes + 31) / 32;
-constexpr int kLevelCounts = 32;
+constexpr int kLevelCounts = 32;       // per profile: subsample_pixel calls per level in [0, 16), then
+constexpr int kCountDirectEvals = 30;  // evaluate_at calls made directly on pixel centres
+constexpr int kCountSubEvals = 31;     // evaluate_at calls made inside subsample_pixel
 
 // sersic r_factor specialisations (src/sersic.cpp:79-159)
 enum RFactor : int { RF_GENERAL = 0, RF_POINTFIVE, RF_ONE, RF_TWO, RF_THREE, RF_FOUR, RF_EIGHT, RF_SIXTEEN };
@@ -81,6 +83,17 @@ struct ProfileDev {
 	float fbg;
 	int32_t fboxy;
 	float fpar[12];            // per-kind folded constants, FP_* slots
+	// adjoint: d bn / d nser and d ln(flux_scale) / d par[k] (setup kernel)
+	double dbn;
+	double dlnfs[PF_NPAR];
+	int32_t grad_ok;           // the adjoint supports this profile
+	float fbn, fdbn, fnser, fre;
+};
+
+// Gradient accumulators of one profile in the adjoint: the pixel value (for
+// the flux-scale derivatives) and the shape derivatives d ln f / d par.
+enum GradSlot : int {
+	G_V = 0, G_XCEN, G_YCEN, G_ANG, G_AXRAT, G_BOX, G_X0, G_X1, kGradSlots
 };
 
 // Slots of ProfileDev::fpar (folded by the setup kernel)

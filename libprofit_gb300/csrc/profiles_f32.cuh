@@ -70,17 +70,24 @@ __device__ __forceinline__ float evaluate_at(const ProfileDev &p, float x, float
 		return ex2(-c[FP_M_CON] * lg2(1.f + r2));
 	}
 	case PF_FERRER: {
+		// (1 - rf^(2-b))^a with 1 - rf^(2-b) = -expm1((2-b) ln rf): no cancellation near rf = 1
 		const float rf = boxy_r(p, x, y) * c[FP_F_INV_ROUT];
 		if (rf < 1.f) {
-			return ex2(c[FP_F_A] * lg2(1.f - ex2(c[FP_F_2MB] * lg2(rf))));
+			return ex2(c[FP_F_A] * lg2(-expm1f(c[FP_F_2MB] * logf(rf))));
 		}
 		return 0.f;
 	}
 	case PF_KING: {
+		// u^(-1/a) - ut^(-1/a) = temp * expm1(ln(ut/u) / a), ln(ut/u) = log1p((rt^2 - r^2) / (rc^2 u)),
+		// with u = 1 + (r/rc)^2: accurate up to the truncation radius rt
 		const float r = boxy_r(p, x, y);
-		if (r < c[FP_K_RT]) {
+		const float rt = c[FP_K_RT];
+		if (r < rt) {
 			const float q = r * c[FP_K_INV_RC];
-			return ex2(c[FP_K_A] * lg2(ex2(-c[FP_K_INV_A] * lg2(1.f + q * q)) - c[FP_K_TEMP]));
+			const float u = 1.f + q * q;
+			const float w = (rt - r) * (rt + r) * (c[FP_K_INV_RC] * c[FP_K_INV_RC]) / u;
+			const float diff = c[FP_K_TEMP] * expm1f(c[FP_K_INV_A] * log1pf(w));
+			return ex2(c[FP_K_A] * lg2(diff));
 		}
 		return 0.f;
 	}

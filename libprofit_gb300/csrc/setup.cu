@@ -246,6 +246,38 @@ __device__ void fold_single_precision(ProfileDev &p)
 	}
 }
 
+// Constants of the adjoint. For a sersic profile
+//   ln flux_scale = const - 0.4 ln(10) mag - ln lumtot(re, n) - ln axrat + ln r_box(box)
+// with ln lumtot = 2 ln re + ln(2 pi) + ln n + lnGamma(2n) + bn - 2n ln bn
+// (src/sersic.cpp:283-289) and r_box = pi B / (2 beta(1/B, 1/B)), B = box + 2
+// (src/radial.cpp:150-152). bn(n) solves P(2n, bn) = 1/2; its derivative is
+// taken by a fourth-order central difference of the inverse.
+__device__ void adjoint_constants(ProfileDev &p)
+{
+	for (int k = 0; k < PF_NPAR; k++) p.dlnfs[k] = 0.;
+	p.dbn = 0.;
+	p.grad_ok = 0;
+	if (p.kind != PF_SERSIC || p.rescale_flux) {
+		return;
+	}
+	const double n = p.par[7], re = p.par[6], q = p.par[PF_P_AXRAT], B = p.par[PF_P_BOX] + 2;
+	const double h = 1e-3 * n;
+	const double b1 = sf::qgamma(0.5, 2 * (n + h)), bm1 = sf::qgamma(0.5, 2 * (n - h));
+	const double b2 = sf::qgamma(0.5, 2 * (n + 2 * h)), bm2 = sf::qgamma(0.5, 2 * (n - 2 * h));
+	const double dbn = (8 * (b1 - bm1) - (b2 - bm2)) / (12 * h);
+	p.dbn = dbn;
+	p.dlnfs[PF_P_MAG] = -0.4 * log(10.);
+	p.dlnfs[PF_P_AXRAT] = -1 / q;
+	p.dlnfs[PF_P_BOX] = 1 / B + (2 / (B * B)) * (sf::digamma(1 / B) - sf::digamma(2 / B));
+	p.dlnfs[6] = -2 / re;
+	p.dlnfs[7] = -(1 / n + 2 * sf::digamma(2 * n) + dbn - 2 * log(p.bn) - 2 * n * dbn / p.bn);
+	p.fbn = (float)p.bn;
+	p.fdbn = (float)dbn;
+	p.fnser = (float)n;
+	p.fre = (float)re;
+	p.grad_ok = 1;
+}
+
 __device__ void radial_setup(ProfileDev &p, const ModelDev &m, unsigned int *err)
 {
 	if (p.kind == PF_SERSIC) {
@@ -307,6 +339,7 @@ __device__ void radial_setup(ProfileDev &p, const ModelDev &m, unsigned int *err
 		}
 	}
 	fold_single_precision(p);
+	adjoint_constants(p);
 	unsigned int max_res = p.resolution;
 	unsigned int max_rec = p.max_recursions;
 	if (p.kind == PF_SERSIC && p.adjust && p.par[7] > 1) {  // central pixel, src/sersic.cpp:339-345
@@ -343,6 +376,7 @@ __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs,
 	else if (p.kind == PF_SKY) {
 		p.bg = p.par[6] / (m.fs * m.fs);  // src/sky.cpp:42-45
 		p.fbg = (float)p.bg;
+		p.grad_ok = 1;
 	}
 	else if (p.kind == PF_PSF) {
 		p.psf_mag_scale = pow(10, -0.4 * (p.par[PF_P_MAG] - m.magzero));

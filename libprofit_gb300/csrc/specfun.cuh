@@ -51,6 +51,21 @@ __device__ inline double beta(double a, double b)
 	return exp(lgamma(a) + lgamma(b) - lgamma(a + b));
 }
 
+// Digamma psi(x) for x > 0: upward recurrence psi(x) = psi(x+1) - 1/x to
+// x >= 10, then the asymptotic series ln x - 1/(2x) - sum B_2k / (2k x^2k)
+// (DLMF 5.15.8, 5.11.2) through the x^-12 term.
+__device__ inline double digamma(double x)
+{
+	double acc = 0.;
+	while (x < 10.) {
+		acc -= 1. / x;
+		x += 1.;
+	}
+	const double r = 1. / x, r2 = r * r;
+	const double series = r2 * (1. / 12 - r2 * (1. / 120 - r2 * (1. / 252 - r2 * (1. / 240 - r2 * (1. / 132)))));
+	return acc + log(x) - 0.5 * r - series;
+}
+
 constexpr double kFpMin = 1e-300;
 
 __device__ inline double pgamma_series(double a, double x)
