@@ -88,67 +88,6 @@ __device__ __forceinline__ T g_direct(const ModelDev &m, const T *gout, int x, i
 	return gout[m.out_off + (size_t)cy * m.out_w + cx];
 }
 
-// ---------------------------------------------------- transposed convolution
-
-constexpr int kAdjTile = 32;
-constexpr int kAdjRows = 4;
-
-// g_src(q) = sum_j G(q + j - h') K(j), h' = kw - 1 - kw/2, over the drawing
-// area of every convolved model; one block per 32x32 drawing tile.
-template <typename T>
-__global__ void __launch_bounds__(kAdjTile * (kAdjTile / kAdjRows))
-adjoint_conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restrict__ psf,
-                    const T *__restrict__ gout, T *__restrict__ gsrc, const long long *__restrict__ tile_base,
-                    long long n_tiles)
-{
-	extern __shared__ unsigned char smem_raw[];
-	T *smem = reinterpret_cast<T *>(smem_raw);
-	for (long long tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-		int lo = 0, hi = n_models - 1;
-		while (lo < hi) {
-			int mid = (lo + hi + 1) >> 1;
-			if (tile_base[mid] <= tile) lo = mid; else hi = mid - 1;
-		}
-		const ModelDev &m = models[lo];
-		if (!m.conv_required) continue;
-		const long long local = tile - tile_base[lo];
-		const int tiles_x = (m.draw_w + kAdjTile - 1) / kAdjTile;
-		const int x0 = (int)(local % tiles_x) * kAdjTile, y0 = (int)(local / tiles_x) * kAdjTile;
-		const int kw = (int)m.psf_w, kh = (int)m.psf_h;
-		const int hx = kw - 1 - kw / 2, hy = kh - 1 - kh / 2;
-		const int pw = kAdjTile + kw - 1, ph = kAdjTile + kh - 1;
-		T *s_g = smem;
-		T *s_k = smem + pw * ph;
-		for (int i = threadIdx.x; i < pw * ph; i += blockDim.x) {
-			s_g[i] = g_direct(m, gout, x0 - hx + i % pw, y0 - hy + i / pw);
-		}
-		const T *k = psf + m.psf_off;
-		for (int i = threadIdx.x; i < kw * kh; i += blockDim.x) s_k[i] = k[i];
-		__syncthreads();
-		const int tx = threadIdx.x % kAdjTile, yb = (threadIdx.x / kAdjTile) * kAdjRows;
-		T res[kAdjRows];
-#pragma unroll
-		for (int r = 0; r < kAdjRows; r++) res[r] = 0;
-		for (int jx = 0; jx < kw; jx++) {
-			const T *col = s_g + yb * pw + tx + jx;
-			for (int l = 0; l < kh + kAdjRows - 1; l++) {
-				const T gv = col[l * pw];
-#pragma unroll
-				for (int r = 0; r < kAdjRows; r++) {
-					const int jy = l - r;
-					if (jy >= 0 && jy < kh) res[r] += gv * s_k[jy * kw + jx];
-				}
-			}
-		}
-		for (int r = 0; r < kAdjRows; r++) {
-			const int x = x0 + tx, y = y0 + yb + r;
-			if (x < (int)m.draw_w && y < (int)m.draw_h) gsrc[m.draw_off + (size_t)y * m.draw_w + x] = res[r];
-		}
-		__syncthreads();
-	}
-}
-
-// ------------------------------------------------------------- sersic grads
 
 // value and shape derivatives d ln f / d theta of the sersic profile at
 // profile coordinates (xp, yp); acc[] += weight * f * (1, d/dxcen, d/dycen,
@@ -537,32 +476,6 @@ void launch_chi2(const ModelDev *models, int n_models, const void *img, const vo
 	                                             (const T *)cot, (T *)gout, chi2);
 }
 
-template <typename T>
-size_t adjoint_conv_smem(unsigned int kw, unsigned int kh)
-{
-	return sizeof(T) * ((size_t)(kAdjTile + kw - 1) * (kAdjTile + kh - 1) + (size_t)kw * kh);
-}
-
-long long adjoint_conv_tiles(unsigned int draw_w, unsigned int draw_h)
-{
-	return (long long)((draw_w + kAdjTile - 1) / kAdjTile) * ((draw_h + kAdjTile - 1) / kAdjTile);
-}
-
-template <typename T>
-cudaError_t adjoint_conv_configure(size_t smem)
-{
-	return cudaFuncSetAttribute(adjoint_conv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-}
-
-template <typename T>
-void launch_adjoint_conv(const ModelDev *models, int n_models, const void *psf, const void *gout, void *gsrc,
-                         const long long *tile_base, long long n_tiles, size_t smem, int n_sm, cudaStream_t stream)
-{
-	int blocks = (int)(n_tiles < (long long)n_sm * 16 ? n_tiles : (long long)n_sm * 16);
-	if (blocks < 1) blocks = 1;
-	adjoint_conv_kernel<T><<<blocks, kAdjTile * (kAdjTile / kAdjRows), smem, stream>>>(
-	    models, n_models, (const T *)psf, (const T *)gout, (T *)gsrc, tile_base, n_tiles);
-}
 
 template <typename T>
 void launch_backward(const ModelDev *models, int n_models, const ProfileDev *profs, int n_profiles, const void *gout,
@@ -581,14 +494,6 @@ template void launch_chi2<float>(const ModelDev *, int, const void *, const void
                                  double *, cudaStream_t);
 template void launch_chi2<double>(const ModelDev *, int, const void *, const void *, const void *, const void *,
                                   void *, double *, cudaStream_t);
-template size_t adjoint_conv_smem<float>(unsigned int, unsigned int);
-template size_t adjoint_conv_smem<double>(unsigned int, unsigned int);
-template cudaError_t adjoint_conv_configure<float>(size_t);
-template cudaError_t adjoint_conv_configure<double>(size_t);
-template void launch_adjoint_conv<float>(const ModelDev *, int, const void *, const void *, void *, const long long *,
-                                         long long, size_t, int, cudaStream_t);
-template void launch_adjoint_conv<double>(const ModelDev *, int, const void *, const void *, void *,
-                                          const long long *, long long, size_t, int, cudaStream_t);
 template void launch_backward<float>(const ModelDev *, int, const ProfileDev *, int, const void *, const void *,
                                      const long long *, const long long *, long long, double *, double *, int,
                                      cudaStream_t);

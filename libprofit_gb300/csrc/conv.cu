@@ -1,0 +1,228 @@
+// Register-blocked direct convolution on the CUDA cores, for the batched path.
+//
+// Both directions of the PSF convolution of Model::produce_image
+// (src/model.cpp:344-356; the convolution itself is the brute-force one of
+// src/convolve.cpp:158-231, zero outside the source):
+//   forward  out(o) = direct(o + pad) + sum_{k,l} src(o + pad + (k,l) - h) rev(k,l)
+//            over the output pixels, then the crop, optionally SUM-downsampled;
+//   adjoint  g_src(q) = sum_{k,l} G(q + (k,l) - h') psf(k,l), h' = size - 1 - h,
+//            over the drawing area, G = the output cotangent placed at the crop.
+// A block stages a source patch and the (reversed or not) PSF, zero-padded to
+// a multiple of 4 columns, in shared memory. Each thread owns a 4-wide by
+// R-tall block of outputs; it reads every source row of its patch once, as
+// 16-byte vectors, and applies it to all the kernel rows that touch it,
+// taking four kernel taps per 16-byte broadcast read, so that a shared-memory
+// read feeds up to 4 R FMAs.
+#include <cstdint>
+
+#include "pf_device.cuh"
+
+namespace pf {
+
+namespace {
+
+template <typename T>
+struct ConvShape;
+template <>
+struct ConvShape<float> {
+	static constexpr int TX = 16, TY = 16, R = 8;  // 64 x 128 outputs per block
+};
+template <>
+struct ConvShape<double> {
+	static constexpr int TX = 16, TY = 8, R = 4;   // 64 x 32 outputs per block
+};
+
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+	using type = float4;
+};
+template <>
+struct Vec4<double> {
+	using type = double4;
+};
+
+enum ConvMode { CONV_FORWARD = 0, CONV_ADJOINT = 1 };
+
+__device__ __forceinline__ int find_tile_model(const long long *base, int n_models, long long tile)
+{
+	int lo = 0, hi = n_models - 1;
+	while (lo < hi) {
+		int mid = (lo + hi + 1) >> 1;
+		if (base[mid] <= tile) lo = mid; else hi = mid - 1;
+	}
+	return lo;
+}
+
+// cotangent of drawing pixel (x, y) (0 in the padding, SUM-downsampling aware)
+template <typename T>
+__device__ __forceinline__ T cot_at(const ModelDev &m, const T *gout, int x, int y)
+{
+	const int cx = x - (int)m.pad_x, cy = y - (int)m.pad_y;
+	if (cx < 0 || cy < 0 || cx >= (int)m.crop_w || cy >= (int)m.crop_h) return (T)0;
+	if (m.fs > 1 && !m.return_fs) return gout[m.out_off + (size_t)(cy / m.fs) * m.out_w + cx / m.fs];
+	return gout[m.out_off + (size_t)cy * m.out_w + cx];
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(ConvShape<T>::TX * ConvShape<T>::TY)
+conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restrict__ psf, const T *__restrict__ in,
+            const T *__restrict__ direct, T *__restrict__ out, const long long *__restrict__ tile_base,
+            long long n_tiles)
+{
+	constexpr int TX = ConvShape<T>::TX, TY = ConvShape<T>::TY, R = ConvShape<T>::R;
+	constexpr int BW = TX * 4, BH = TY * R;  // outputs per block
+	using V4 = typename Vec4<T>::type;
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	T *smem = reinterpret_cast<T *>(smem_raw);
+	const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+	for (long long tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+		const int mi = find_tile_model(tile_base, n_models, tile);
+		const ModelDev &m = models[mi];
+		if (!m.conv_required && MODE == CONV_ADJOINT) continue;
+		const long long local = tile - tile_base[mi];
+		const int ow = MODE == CONV_FORWARD ? (int)m.crop_w : (int)m.draw_w;
+		const int oh = MODE == CONV_FORWARD ? (int)m.crop_h : (int)m.draw_h;
+		const int tiles_x = (ow + BW - 1) / BW;
+		const int x0 = (int)(local % tiles_x) * BW, y0 = (int)(local / tiles_x) * BH;
+		T acc[R][4];
+#pragma unroll
+		for (int r = 0; r < R; r++)
+#pragma unroll
+			for (int c = 0; c < 4; c++) acc[r][c] = 0;
+		if (m.conv_required) {
+			const int kw = (int)m.psf_w, kh = (int)m.psf_h;
+			const int kwp = (kw + 3) & ~3;
+			const int pw = BW + kwp, ph = BH + kh - 1;
+			T *s_src = smem;
+			T *s_k = smem + pw * ph;
+			// patch origin in the source (drawing) image
+			int sx0, sy0;
+			if (MODE == CONV_FORWARD) {
+				sx0 = x0 + (int)m.pad_x - kw / 2;
+				sy0 = y0 + (int)m.pad_y - kh / 2;
+			}
+			else {
+				sx0 = x0 - (kw - 1 - kw / 2);
+				sy0 = y0 - (kh - 1 - kh / 2);
+			}
+			const T *src = in + (MODE == CONV_FORWARD ? m.draw_off : 0);
+			for (int i = threadIdx.x; i < pw * ph; i += blockDim.x) {
+				const int xx = sx0 + i % pw, yy = sy0 + i / pw;
+				T v = 0;
+				if (MODE == CONV_FORWARD) {
+					if (xx >= 0 && xx < (int)m.draw_w && yy >= 0 && yy < (int)m.draw_h && i % pw < BW + kw - 1)
+						v = src[(size_t)yy * m.draw_w + xx];
+				}
+				else {
+					if (i % pw < BW + kw - 1) v = cot_at(m, in, xx, yy);
+				}
+				s_src[i] = v;
+			}
+			const T *k = psf + m.psf_off;
+			const int kn = kw * kh;
+			for (int i = threadIdx.x; i < kwp * kh; i += blockDim.x) {
+				const int kx = i % kwp, ky = i / kwp;
+				T v = 0;
+				if (kx < kw) v = MODE == CONV_FORWARD ? k[kn - 1 - (ky * kw + kx)] : k[ky * kw + kx];
+				s_k[i] = v;
+			}
+			__syncthreads();
+			const int xb = tx * 4, yb = ty * R;
+			for (int s = 0; s < R + kh - 1; s++) {
+				const T *srow = s_src + (yb + s) * pw + xb;
+				for (int kb = 0; kb < kwp; kb += 4) {
+					const V4 w0 = *reinterpret_cast<const V4 *>(srow + kb);
+					const V4 w1 = *reinterpret_cast<const V4 *>(srow + kb + 4);
+					const T w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+					for (int r = 0; r < R; r++) {
+						const int l = s - r;
+						if (l >= 0 && l < kh) {
+							const V4 kv4 = *reinterpret_cast<const V4 *>(s_k + l * kwp + kb);
+							const T kv[4] = {kv4.x, kv4.y, kv4.z, kv4.w};
+#pragma unroll
+							for (int c = 0; c < 4; c++)
+#pragma unroll
+								for (int q = 0; q < 4; q++) acc[r][c] = fma(w[c + q], kv[q], acc[r][c]);
+						}
+					}
+				}
+			}
+			__syncthreads();
+		}
+		const int xo = x0 + tx * 4;
+#pragma unroll
+		for (int r = 0; r < R; r++) {
+			const int yo = y0 + ty * R + r;
+			if (yo >= oh) continue;
+#pragma unroll
+			for (int c = 0; c < 4; c++) {
+				const int x = xo + c;
+				if (x >= ow) continue;
+				if (MODE == CONV_FORWARD) {
+					const T v = direct[m.draw_off + (size_t)(yo + m.pad_y) * m.draw_w + x + m.pad_x] + acc[r][c];
+					if (m.fs > 1 && !m.return_fs) atomicAdd(&out[m.out_off + (size_t)(yo / m.fs) * m.out_w + x / m.fs], v);
+					else out[m.out_off + (size_t)yo * m.out_w + x] = v;
+				}
+				else {
+					out[m.draw_off + (size_t)yo * m.draw_w + x] = acc[r][c];
+				}
+			}
+		}
+	}
+}
+
+}  // namespace
+
+template <typename T>
+long long conv_tiles(unsigned int w, unsigned int h)
+{
+	constexpr int BW = ConvShape<T>::TX * 4, BH = ConvShape<T>::TY * ConvShape<T>::R;
+	return (long long)((w + BW - 1) / BW) * ((h + BH - 1) / BH);
+}
+
+template <typename T>
+size_t conv_smem(unsigned int kw, unsigned int kh)
+{
+	constexpr int BW = ConvShape<T>::TX * 4, BH = ConvShape<T>::TY * ConvShape<T>::R;
+	const size_t kwp = (kw + 3) & ~3u;
+	return sizeof(T) * ((BW + kwp) * (BH + kh - 1) + kwp * kh);
+}
+
+template <typename T>
+cudaError_t conv_configure(size_t smem)
+{
+	cudaError_t e = cudaFuncSetAttribute(conv_kernel<T, CONV_FORWARD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e != cudaSuccess) return e;
+	return cudaFuncSetAttribute(conv_kernel<T, CONV_ADJOINT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+template <typename T>
+void launch_conv(int mode, const ModelDev *models, int n_models, const T *psf, const T *in, const T *direct, T *out,
+                 const long long *tile_base, long long n_tiles, size_t smem, int n_sm, cudaStream_t stream)
+{
+	const int threads = ConvShape<T>::TX * ConvShape<T>::TY;
+	int blocks = (int)(n_tiles < (long long)n_sm * 8 ? n_tiles : (long long)n_sm * 8);
+	if (blocks < 1) blocks = 1;
+	if (mode == CONV_FORWARD)
+		conv_kernel<T, CONV_FORWARD><<<blocks, threads, smem, stream>>>(models, n_models, psf, in, direct, out,
+		                                                                 tile_base, n_tiles);
+	else
+		conv_kernel<T, CONV_ADJOINT><<<blocks, threads, smem, stream>>>(models, n_models, psf, in, direct, out,
+		                                                                 tile_base, n_tiles);
+}
+
+template long long conv_tiles<float>(unsigned int, unsigned int);
+template long long conv_tiles<double>(unsigned int, unsigned int);
+template size_t conv_smem<float>(unsigned int, unsigned int);
+template size_t conv_smem<double>(unsigned int, unsigned int);
+template cudaError_t conv_configure<float>(size_t);
+template cudaError_t conv_configure<double>(size_t);
+template void launch_conv<float>(int, const ModelDev *, int, const float *, const float *, const float *, float *,
+                                 const long long *, long long, size_t, int, cudaStream_t);
+template void launch_conv<double>(int, const ModelDev *, int, const double *, const double *, const double *,
+                                  double *, const long long *, long long, size_t, int, cudaStream_t);
+
+}  // namespace pf

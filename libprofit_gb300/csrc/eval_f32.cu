@@ -318,100 +318,6 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 	}
 }
 
-// ---------------------------------------------------------------- finish
-
-constexpr int kConvTileW = 32;   // output tile width (one warp across)
-constexpr int kConvTileH = 32;   // output tile height
-constexpr int kConvRows = 4;     // output rows per thread (register blocking)
-
-__device__ __forceinline__ int find_model_out(const ModelDev *models, int n_models, long long g)
-{
-	int lo = 0, hi = n_models - 1;
-	while (lo < hi) {
-		int mid = (lo + hi + 1) >> 1;
-		if (models[mid].out_off <= g) lo = mid; else hi = mid - 1;
-	}
-	return lo;
-}
-
-// Output tiles of all models, numbered consecutively; one block per tile.
-// The block stages the source patch and the reversed PSF in shared memory
-// and convolves directly (FP32 FMA), adds the direct image and writes the
-// cropped output. Models without convolution copy (and downsample).
-__global__ void __launch_bounds__(kConvTileW * (kConvTileH / kConvRows))
-finish32_kernel(const ModelDev *__restrict__ models, int n_models, const float *__restrict__ psf32,
-                const float *__restrict__ conv_img, const float *__restrict__ direct_img, float *__restrict__ out,
-                const long long *__restrict__ tile_base_out, long long n_out_tiles)
-{
-	extern __shared__ float smem[];
-	for (long long tile = blockIdx.x; tile < n_out_tiles; tile += gridDim.x) {
-		int lo = 0, hi = n_models - 1;
-		while (lo < hi) {
-			int mid = (lo + hi + 1) >> 1;
-			if (tile_base_out[mid] <= tile) lo = mid; else hi = mid - 1;
-		}
-		const ModelDev &m = models[lo];
-		const long long local = tile - tile_base_out[lo];
-		// output tiles cover the crop area (before downsampling)
-		const int tiles_x = (m.crop_w + kConvTileW - 1) / kConvTileW;
-		const int ox0 = (int)(local % tiles_x) * kConvTileW;
-		const int oy0 = (int)(local / tiles_x) * kConvTileH;
-		const int tx = threadIdx.x % kConvTileW, ty = threadIdx.x / kConvTileW;
-		const bool downsample = m.fs > 1 && !m.return_fs;
-		float res[kConvRows];
-		for (int r = 0; r < kConvRows; r++) res[r] = 0.f;
-		if (m.conv_required) {
-			const int kw = (int)m.psf_w, kh = (int)m.psf_h;
-			const int pw = kConvTileW + kw - 1, ph = kConvTileH + kh - 1;
-			float *s_src = smem;
-			float *s_krn = smem + pw * ph;
-			// source patch: drawing pixels (ox0 + pad_x - kw/2 .. , oy0 + pad_y - kh/2 ..)
-			const int sx0 = ox0 + (int)m.pad_x - kw / 2, sy0 = oy0 + (int)m.pad_y - kh / 2;
-			const float *src = conv_img + m.draw_off;
-			for (int i = threadIdx.x; i < pw * ph; i += blockDim.x) {
-				const int yy = sy0 + i / pw, xx = sx0 + i % pw;
-				float v = 0.f;
-				if (xx >= 0 && xx < (int)m.draw_w && yy >= 0 && yy < (int)m.draw_h) v = src[(size_t)yy * m.draw_w + xx];
-				s_src[i] = v;
-			}
-			const float *krn = psf32 + m.psf_off;
-			const int kn = kw * kh;
-			for (int i = threadIdx.x; i < kn; i += blockDim.x) s_krn[i] = krn[kn - 1 - i];  // reversed
-			__syncthreads();
-			// out(x, y) = sum_{l,k} src(x + k, y + l) * rev(k, l) within the patch
-			const int yb = ty * kConvRows;
-			for (int k = 0; k < kw; k++) {
-				const float *col = s_src + yb * pw + tx + k;
-				float win[kConvRows];
-#pragma unroll
-				for (int r = 0; r < kConvRows; r++) win[r] = 0.f;
-				for (int l = 0; l < kh + kConvRows - 1; l++) {
-					const float sv = col[l * pw];
-#pragma unroll
-					for (int r = 0; r < kConvRows; r++) {
-						const int kl = l - r;
-						if (kl >= 0 && kl < kh) res[r] = fmaf(sv, s_krn[kl * kw + k], res[r]);
-					}
-				}
-			}
-			__syncthreads();
-		}
-		const float *direct = direct_img + m.draw_off;
-		for (int r = 0; r < kConvRows; r++) {
-			const int ox = ox0 + tx, oy = oy0 + ty * kConvRows + r;
-			if (ox < (int)m.crop_w && oy < (int)m.crop_h) {
-				const float v = direct[(size_t)(oy + m.pad_y) * m.draw_w + ox + m.pad_x] + res[r];
-				if (downsample) {
-					atomicAdd(&out[m.out_off + (size_t)(oy / m.fs) * m.out_w + ox / m.fs], v);
-				}
-				else {
-					out[m.out_off + (size_t)oy * m.out_w + ox] = v;
-				}
-			}
-		}
-	}
-}
-
 __global__ void psf_to_float_kernel(const double *in, float *out, long long n)
 {
 	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -429,32 +335,6 @@ void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs
 	if (need < blocks) blocks = (int)(need > 0 ? need : 1);
 	eval_tiles32_kernel<<<blocks, kWarps32 * 32, 0, stream>>>(models, n_models, profs, psf_pool, conv_img, direct_img,
 	                                                          n_tiles, tile_counter, dbg);
-}
-
-size_t finish32_smem(unsigned int max_psf_w, unsigned int max_psf_h)
-{
-	return sizeof(float) * ((size_t)(kConvTileW + max_psf_w - 1) * (kConvTileH + max_psf_h - 1) +
-	                        (size_t)max_psf_w * max_psf_h);
-}
-
-long long finish32_tiles(unsigned int crop_w, unsigned int crop_h)
-{
-	return (long long)((crop_w + kConvTileW - 1) / kConvTileW) * ((crop_h + kConvTileH - 1) / kConvTileH);
-}
-
-void launch_finish32(const ModelDev *models, int n_models, const float *psf32, const float *conv_img,
-                     const float *direct_img, float *out, const long long *tile_base_out, long long n_out_tiles,
-                     size_t smem, int n_sm, cudaStream_t stream)
-{
-	int blocks = (int)(n_out_tiles < (long long)n_sm * 16 ? n_out_tiles : (long long)n_sm * 16);
-	if (blocks < 1) blocks = 1;
-	finish32_kernel<<<blocks, kConvTileW * (kConvTileH / kConvRows), smem, stream>>>(
-	    models, n_models, psf32, conv_img, direct_img, out, tile_base_out, n_out_tiles);
-}
-
-cudaError_t finish32_configure(size_t smem)
-{
-	return cudaFuncSetAttribute(finish32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 void launch_psf_to_float(const double *in, float *out, long long n, cudaStream_t stream)

@@ -36,25 +36,20 @@ void launch_set_params(ProfileDev *profs, int n_profiles, const double *params, 
 void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs, const double *psf_pool,
                    float *conv_img, float *direct_img, long long n_tiles, unsigned int *tile_counter, DebugRec dbg,
                    int n_sm, cudaStream_t stream);
-size_t finish32_smem(unsigned int max_psf_w, unsigned int max_psf_h);
-long long finish32_tiles(unsigned int crop_w, unsigned int crop_h);
-void launch_finish32(const ModelDev *models, int n_models, const float *psf32, const float *conv_img,
-                     const float *direct_img, float *out, const long long *tile_base_out, long long n_out_tiles,
-                     size_t smem, int n_sm, cudaStream_t stream);
-cudaError_t finish32_configure(size_t smem);
+template <typename T>
+long long conv_tiles(unsigned int w, unsigned int h);
+template <typename T>
+size_t conv_smem(unsigned int kw, unsigned int kh);
+template <typename T>
+cudaError_t conv_configure(size_t smem);
+template <typename T>
+void launch_conv(int mode, const ModelDev *models, int n_models, const T *psf, const T *in, const T *direct, T *out,
+                 const long long *tile_base, long long n_tiles, size_t smem, int n_sm, cudaStream_t stream);
 void launch_psf_to_float(const double *in, float *out, long long n, cudaStream_t stream);
 int backward_band_rows();
 template <typename T>
 void launch_chi2(const ModelDev *models, int n_models, const void *img, const void *data, const void *sigma,
                  const void *cot, void *gout, double *chi2, cudaStream_t stream);
-template <typename T>
-size_t adjoint_conv_smem(unsigned int kw, unsigned int kh);
-long long adjoint_conv_tiles(unsigned int draw_w, unsigned int draw_h);
-template <typename T>
-cudaError_t adjoint_conv_configure(size_t smem);
-template <typename T>
-void launch_adjoint_conv(const ModelDev *models, int n_models, const void *psf, const void *gout, void *gsrc,
-                         const long long *tile_base, long long n_tiles, size_t smem, int n_sm, cudaStream_t stream);
 template <typename T>
 void launch_backward(const ModelDev *models, int n_models, const ProfileDev *profs, int n_profiles, const void *gout,
                      const void *gsrc, const long long *band_base, const long long *part_base, long long n_items,
@@ -460,7 +455,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		for (size_t i = 0; i < n_models; i++) {
 			const pf::ModelDev &d = b->mdev[i];
 			tile_base_out[i] = t;
-			t += pf::finish32_tiles(d.crop_w, d.crop_h);
+			t += pf::conv_tiles<float>(d.crop_w, d.crop_h);
 			if (d.conv_required) {
 				max_kw = std::max(max_kw, d.psf_w);
 				max_kh = std::max(max_kh, d.psf_h);
@@ -468,7 +463,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 			b->any_downsample |= d.fs > 1 && !d.return_fs;
 		}
 		b->n_out_tiles = t;
-		b->finish_smem = pf::finish32_smem(max_kw, max_kh);
+		b->finish_smem = pf::conv_smem<float>(max_kw, max_kh);
 		if (b->finish_smem > 227 * 1024) {
 			return fail(PF_ERR_UNSUPPORTED, "PSF too large for the shared-memory direct convolution");
 		}
@@ -535,7 +530,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		PF_CUDA_TRY(cudaMalloc(&b->d_tile_base_out, sizeof(long long) * tile_base_out.size()));
 		PF_CUDA_TRY(cudaMemcpy(b->d_tile_base_out, tile_base_out.data(), sizeof(long long) * tile_base_out.size(),
 		                       cudaMemcpyHostToDevice));
-		PF_CUDA_TRY(pf::finish32_configure(b->finish_smem));
+		PF_CUDA_TRY(pf::conv_configure<float>(b->finish_smem));
 	}
 	b->params_dirty = true;
 	return PF_OK;
@@ -672,9 +667,9 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 		if (b->any_downsample) {
 			PF_CUDA_TRY(cudaMemsetAsync(images_dev, 0, sizeof(float) * b->total_out, stream));
 		}
-		pf::launch_finish32(b->d_models, n_models, b->d_psf32, (const float *)b->d_conv, (const float *)b->d_direct,
-		                    (float *)images_dev, b->d_tile_base_out, b->n_out_tiles, b->finish_smem, b->env->n_sm,
-		                    stream);
+		pf::launch_conv<float>(0, b->d_models, n_models, b->d_psf32, (const float *)b->d_conv,
+		                       (const float *)b->d_direct, (float *)images_dev, b->d_tile_base_out, b->n_out_tiles,
+		                       b->finish_smem, b->env->n_sm, stream);
 		stage_end(b, t, stream);
 	}
 	b->forward_calls++;
@@ -749,7 +744,7 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 		adj_tile_base[i] = tiles;
 		items += bands;
 		parts += bands * m.n_profiles * pf::kGradSlots;
-		tiles += pf::adjoint_conv_tiles(m.draw_w, m.draw_h);
+		tiles += b->dbl ? pf::conv_tiles<double>(m.draw_w, m.draw_h) : pf::conv_tiles<float>(m.draw_w, m.draw_h);
 		if (m.conv_required) {
 			max_kw = std::max(max_kw, m.psf_w);
 			max_kh = std::max(max_kh, m.psf_h);
@@ -757,7 +752,7 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	}
 	b->n_band_items = items;
 	b->n_adj_tiles = tiles;
-	b->adj_smem = b->dbl ? pf::adjoint_conv_smem<double>(max_kw, max_kh) : pf::adjoint_conv_smem<float>(max_kw, max_kh);
+	b->adj_smem = b->dbl ? pf::conv_smem<double>(max_kw, max_kh) : pf::conv_smem<float>(max_kw, max_kh);
 	if (b->adj_smem > 227 * 1024) return fail(PF_ERR_UNSUPPORTED, "PSF too large for the adjoint convolution");
 	PF_CUDA_TRY(cudaMalloc(&b->d_gout, elem * std::max<uint64_t>(1, b->total_out)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_gsrc, elem * std::max<size_t>(1, b->draw_total)));
@@ -769,7 +764,7 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	PF_CUDA_TRY(cudaMemcpy(b->d_part_base, part_base.data(), sizeof(long long) * part_base.size(), cudaMemcpyHostToDevice));
 	PF_CUDA_TRY(cudaMemcpy(b->d_adj_tile_base, adj_tile_base.data(), sizeof(long long) * adj_tile_base.size(),
 	                       cudaMemcpyHostToDevice));
-	PF_CUDA_TRY(b->dbl ? pf::adjoint_conv_configure<double>(b->adj_smem) : pf::adjoint_conv_configure<float>(b->adj_smem));
+	PF_CUDA_TRY(b->dbl ? pf::conv_configure<double>(b->adj_smem) : pf::conv_configure<float>(b->adj_smem));
 	if (b->dbl && !b->d_psf_norm) {
 		// no PSF anywhere: the adjoint convolution is never launched
 	}
@@ -799,11 +794,12 @@ pf_status pf_backward(pf_batch *b, const void *images_dev, const void *data_dev,
 	stage_end(b, t, stream);
 	if (any_conv) {
 		t = stage_begin(b, ST_ADJCONV, stream);
-		if (b->dbl) pf::launch_adjoint_conv<double>(b->d_models, n_models, b->d_psf_norm, b->d_gout, b->d_gsrc,
-		                                            b->d_adj_tile_base, b->n_adj_tiles, b->adj_smem, b->env->n_sm,
-		                                            stream);
-		else pf::launch_adjoint_conv<float>(b->d_models, n_models, b->d_psf32, b->d_gout, b->d_gsrc,
-		                                    b->d_adj_tile_base, b->n_adj_tiles, b->adj_smem, b->env->n_sm, stream);
+		if (b->dbl) pf::launch_conv<double>(1, b->d_models, n_models, b->d_psf_norm, (const double *)b->d_gout,
+		                                    nullptr, (double *)b->d_gsrc, b->d_adj_tile_base, b->n_adj_tiles,
+		                                    b->adj_smem, b->env->n_sm, stream);
+		else pf::launch_conv<float>(1, b->d_models, n_models, b->d_psf32, (const float *)b->d_gout, nullptr,
+		                            (float *)b->d_gsrc, b->d_adj_tile_base, b->n_adj_tiles, b->adj_smem,
+		                            b->env->n_sm, stream);
 		stage_end(b, t, stream);
 	}
 	t = stage_begin(b, ST_BACKWARD, stream);

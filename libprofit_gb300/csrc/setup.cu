@@ -84,9 +84,18 @@ __device__ double get_lumtot(ProfileDev &p)
 	return 0;
 }
 
-__device__ double sersic_fluxfrac(const ProfileDev &p, double fraction)  // src/sersic.cpp:257-260
+// Inverse-gamma values a sersic profile's setup needs, solved by separate
+// lanes of the profile's warp: P^-1(1 - n^2/2000, 2n) for the switch radius
+// and P^-1(0.9999, 2n) for rscale_max (SersicProfile::fluxfrac), and
+// d bn / d n for the adjoint.
+struct SersicSolves {
+	double q_switch, q_max, dbn;
+};
+
+// SersicProfile::fluxfrac (src/sersic.cpp:257-260) given qgamma(fraction, 2n)
+__device__ double sersic_fluxfrac(const ProfileDev &p, double qgamma_value)
 {
-	double ratio = sf::qgamma(fraction, 2 * p.par[7]) / p.bn;
+	double ratio = qgamma_value / p.bn;
 	return p.par[6] * pow(ratio, p.par[7]);
 }
 
@@ -95,12 +104,11 @@ __device__ double moffat_fluxfrac(const ProfileDev &p, double fraction)  // src/
 	return p.rscale * sqrt(pow(1 - fraction, 1 / (1 - p.par[7])) - 1);
 }
 
-__device__ double adjust_rscale_switch(const ProfileDev &p)
+__device__ double adjust_rscale_switch(const ProfileDev &p, const SersicSolves &sv)
 {
 	switch (p.kind) {
-	case PF_SERSIC: {  // src/sersic.cpp:262-272
-		const double nser = p.par[7];
-		double rs = ceil(sersic_fluxfrac(p, 1. - nser * nser / 2e3));
+	case PF_SERSIC: {  // src/sersic.cpp:262-272 (fraction 1 - nser^2 / 2e3)
+		double rs = ceil(sersic_fluxfrac(p, sv.q_switch));
 		rs = sf::dmax(sf::dmin(rs, 20.), 2.);
 		return rs / p.par[6];
 	}
@@ -116,10 +124,10 @@ __device__ double adjust_rscale_switch(const ProfileDev &p)
 	return 1;
 }
 
-__device__ double adjust_rscale_max(const ProfileDev &p)
+__device__ double adjust_rscale_max(const ProfileDev &p, const SersicSolves &sv)
 {
 	switch (p.kind) {
-	case PF_SERSIC: return ceil(sf::dmax(sersic_fluxfrac(p, 0.9999), 2.) / p.par[6]);  // src/sersic.cpp:274-276
+	case PF_SERSIC: return ceil(sf::dmax(sersic_fluxfrac(p, sv.q_max), 2.) / p.par[6]);  // src/sersic.cpp:274-276
 	case PF_MOFFAT: return ceil(sf::dmax(moffat_fluxfrac(p, 0.9999), 2.) / p.rscale);  // src/moffat.cpp:93-95
 	case PF_CORESERSIC: return 100;
 	case PF_FERRER: return 1;
@@ -250,9 +258,18 @@ __device__ void fold_single_precision(ProfileDev &p)
 //   ln flux_scale = const - 0.4 ln(10) mag - ln lumtot(re, n) - ln axrat + ln r_box(box)
 // with ln lumtot = 2 ln re + ln(2 pi) + ln n + lnGamma(2n) + bn - 2n ln bn
 // (src/sersic.cpp:283-289) and r_box = pi B / (2 beta(1/B, 1/B)), B = box + 2
-// (src/radial.cpp:150-152). bn(n) solves P(2n, bn) = 1/2; its derivative is
-// taken by a fourth-order central difference of the inverse.
-__device__ void adjoint_constants(ProfileDev &p)
+// (src/radial.cpp:150-152). bn(n) solves P(2n, bn) = 1/2, so by implicit
+// differentiation d bn / d n = -2 (dP/da)(2n, bn) / p(bn; 2n), p the gamma
+// density; dP/da is a central difference of P in its shape.
+__device__ double dbn_dn(double n, double bn)
+{
+	const double a = 2 * n, d = 1e-4 * a;
+	const double dpda = (sf::pgamma(bn, a + d) - sf::pgamma(bn, a - d)) / (2 * d);
+	const double pdf = exp((a - 1.) * log(bn) - bn - lgamma(a));
+	return -2 * dpda / pdf;
+}
+
+__device__ void adjoint_constants(ProfileDev &p, double dbn)
 {
 	for (int k = 0; k < PF_NPAR; k++) p.dlnfs[k] = 0.;
 	p.dbn = 0.;
@@ -261,10 +278,6 @@ __device__ void adjoint_constants(ProfileDev &p)
 		return;
 	}
 	const double n = p.par[7], re = p.par[6], q = p.par[PF_P_AXRAT], B = p.par[PF_P_BOX] + 2;
-	const double h = 1e-3 * n;
-	const double b1 = sf::qgamma(0.5, 2 * (n + h)), bm1 = sf::qgamma(0.5, 2 * (n - h));
-	const double b2 = sf::qgamma(0.5, 2 * (n + 2 * h)), bm2 = sf::qgamma(0.5, 2 * (n - 2 * h));
-	const double dbn = (8 * (b1 - bm1) - (b2 - bm2)) / (12 * h);
 	p.dbn = dbn;
 	p.dlnfs[PF_P_MAG] = -0.4 * log(10.);
 	p.dlnfs[PF_P_AXRAT] = -1 / q;
@@ -278,13 +291,13 @@ __device__ void adjoint_constants(ProfileDev &p)
 	p.grad_ok = 1;
 }
 
-__device__ void radial_setup(ProfileDev &p, const ModelDev &m, unsigned int *err)
+__device__ void radial_setup(ProfileDev &p, const ModelDev &m, double bn, const SersicSolves &sv, unsigned int *err)
 {
 	if (p.kind == PF_SERSIC) {
 		choose_rfactor(p);
 	}
 	if (p.kind == PF_SERSIC || p.kind == PF_CORESERSIC) {  // src/sersic.cpp:297, src/coresersic.cpp:112
-		p.bn = sf::qgamma(0.5, 2 * p.par[7]);
+		p.bn = bn;
 	}
 	p.rscale = get_rscale(p);
 	const double box = p.par[PF_P_BOX], axrat = p.par[PF_P_AXRAT];
@@ -294,14 +307,14 @@ __device__ void radial_setup(ProfileDev &p, const ModelDev &m, unsigned int *err
 	p.lumtot = lumtot;
 	p.ie = pow(10, -0.4 * (p.par[PF_P_MAG] - m.magzero)) / lumtot;
 	if (p.adjust) {
-		p.rscale_switch = adjust_rscale_switch(p);
+		p.rscale_switch = adjust_rscale_switch(p, sv);
 		unsigned int res = (unsigned int)ceil(160 / (p.rscale_switch * p.rscale));
 		res += res % 2;
 		res = res < 16U ? res : 16U;
 		res = res > 4U ? res : 4U;
 		p.resolution = res;
 		if (p.rscale_max == 0) {
-			p.rscale_max = adjust_rscale_max(p);
+			p.rscale_max = adjust_rscale_max(p, sv);
 		}
 		p.acc = adjust_acc(p, p.acc);
 	}
@@ -339,7 +352,7 @@ __device__ void radial_setup(ProfileDev &p, const ModelDev &m, unsigned int *err
 		}
 	}
 	fold_single_precision(p);
-	adjoint_constants(p);
+	adjoint_constants(p, sv.dbn);
 	unsigned int max_res = p.resolution;
 	unsigned int max_rec = p.max_recursions;
 	if (p.kind == PF_SERSIC && p.adjust && p.par[7] > 1) {  // central pixel, src/sersic.cpp:339-345
@@ -360,8 +373,33 @@ __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs,
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		*tile_counter = 0;
 	}
-	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	// one warp per profile: the independent inverse-gamma solves of a sersic
+	// profile run on separate lanes, lane 0 does the rest
+	const int lane = threadIdx.x & 31;
+	const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
 	if (t >= n_profiles) {
+		return;
+	}
+	const int kind = profs[t].kind;
+	const double nser = profs[t].par[7];
+	const bool sersic_like = kind == PF_SERSIC || kind == PF_CORESERSIC;
+	double bn = 0.;
+	if (sersic_like && lane == 0) {
+		bn = sf::qgamma(0.5, 2 * nser, sf::bn_guess(nser));
+	}
+	bn = __shfl_sync(0xffffffffu, bn, 0);
+	SersicSolves sv{0., 0., 0.};
+	if (kind == PF_SERSIC) {
+		double v = 0.;
+		const bool adjust = profs[t].adjust != 0;
+		if (lane == 1 && adjust) v = sf::qgamma(1. - nser * nser / 2e3, 2 * nser);
+		if (lane == 2 && adjust && profs[t].rscale_max_in == 0) v = sf::qgamma(0.9999, 2 * nser);
+		if (lane == 3 && !profs[t].rescale_flux) v = dbn_dn(nser, bn);
+		sv.q_switch = __shfl_sync(0xffffffffu, v, 1);
+		sv.q_max = __shfl_sync(0xffffffffu, v, 2);
+		sv.dbn = __shfl_sync(0xffffffffu, v, 3);
+	}
+	if (lane != 0) {
 		return;
 	}
 	ProfileDev p = profs[t];
@@ -371,7 +409,7 @@ __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs,
 	p.rscale_switch = p.rscale_switch_in;
 	p.rscale_max = p.rscale_max_in;
 	if (p.kind >= PF_SERSIC && p.kind <= PF_BROKENEXP) {
-		radial_setup(p, m, err);
+		radial_setup(p, m, bn, sv, err);
 	}
 	else if (p.kind == PF_SKY) {
 		p.bg = p.par[6] / (m.fs * m.fs);  // src/sky.cpp:42-45
@@ -410,10 +448,10 @@ void launch_setup(const ModelDev *models, ProfileDev *profs, int n_profiles, int
                   unsigned int *tile_counter, unsigned int *err, const double *psf_raw, double *psf_norm,
                   bool have_psf, cudaStream_t stream)
 {
-	int threads = 64;
-	int blocks = (n_profiles + threads - 1) / threads;
+	const int warps = 2;  // profiles per block
+	int blocks = (n_profiles + warps - 1) / warps;
 	if (blocks < 1) blocks = 1;
-	setup_profiles_kernel<<<blocks, threads, 0, stream>>>(models, profs, n_profiles, tile_counter, err);
+	setup_profiles_kernel<<<blocks, warps * 32, 0, stream>>>(models, profs, n_profiles, tile_counter, err);
 	if (have_psf && n_models > 0) {
 		normalise_psf_kernel<<<n_models, 128, 0, stream>>>(models, psf_raw, psf_norm);
 	}

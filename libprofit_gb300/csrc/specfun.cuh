@@ -118,21 +118,51 @@ __device__ inline double qgamma_upper(double x, double a)
 	return qgamma_cf(a, x);
 }
 
-// Inverse of P(a, .)
-__device__ inline double qgamma(double p, double a)
+// Starting point for bn = P^-1(1/2, 2n): the asymptotic series of Ciotti &
+// Bertin (1999, A&A 352, 447), eq. 18; refined to full precision by qgamma.
+__device__ inline double bn_guess(double n)
+{
+	if (n < 0.36) return -1.;
+	const double r = 1. / n;
+	return 2 * n - 1. / 3 + r * (4. / 405 + r * (46. / 25515 + r * (131. / 1148175 - r * (2194697. / 30690717750.))));
+}
+
+// Inverse of P(a, .). With a usable starting point (guess > 0) the root is
+// bracketed around it by doubling steps instead of from [0, max(a, 1)].
+__device__ inline double qgamma(double p, double a, double guess = -1.)
 {
 	if (!(p > 0.)) return 0.;
 	if (p >= 1.) return CUDART_INF;
 	const bool use_q = p > 0.5;
 	const double q = 1. - p;
 	double lo = 0., hi = a > 1. ? a : 1.;
-	for (int it = 0; it < 2000; it++) {
-		bool below = use_q ? (qgamma_upper(hi, a) > q) : (pgamma(hi, a) < p);
-		if (!below) break;
-		lo = hi;
-		hi *= 2.;
+	double x;
+	if (guess > 0.) {
+		// f(guess) decides which side of the root the guess lies on
+		const double f0 = use_q ? (q - qgamma_upper(guess, a)) : (pgamma(guess, a) - p);
+		if (f0 < 0.) {
+			lo = guess;
+			hi = guess * (1. + 1e-3);
+			while ((use_q ? (q - qgamma_upper(hi, a)) : (pgamma(hi, a) - p)) < 0.) {
+				lo = hi;
+				hi *= 2.;
+			}
+		}
+		else {
+			hi = guess;
+			lo = 0.;  // f(0) = -p < 0
+		}
+		x = guess;
 	}
-	double x = a;
+	else {
+		for (int it = 0; it < 2000; it++) {
+			bool below = use_q ? (qgamma_upper(hi, a) > q) : (pgamma(hi, a) < p);
+			if (!below) break;
+			lo = hi;
+			hi *= 2.;
+		}
+		x = a;
+	}
 	if (!(x > lo && x < hi)) {
 		x = 0.5 * (lo + hi);
 	}
