@@ -377,8 +377,9 @@ def run_ours(args, world, rank, local):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "models/s", "h2d_bytes_per_step": int(par.size * 8),
                 "d2h_bytes_per_step": int(n_models * 8 + n_prof * 12 * 8)},
-        # per step: parameter scatter, setup, eval, finish, chi2, adjoint conv, backward, gradient reduce
-        "gpu_launches": int(args.steps * 8),
+        # per step: parameter scatter, setup (solves + constants), eval, convolution, chi2, adjoint
+        # convolution, backward, gradient reduce
+        "gpu_launches": int(args.steps * 9),
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)

@@ -1,0 +1,381 @@
+/*
+ * profit_cuda.hpp - C++ host interface of the GB300 backend, mirroring the
+ * part of libprofit's public C++ API that drives image generation, over the
+ * C ABI of pf_cuda.h. Header-only; link against libpfcuda.so.
+ *
+ *   profit::Model                 -> profit_cuda::Model       (include/profit/model.h:60-408)
+ *   Model::add_profile            -> Model::add_profile       (src/model.cpp:103-135)
+ *   Profile::parameter            -> Profile::parameter       (src/profile.cpp:84-163)
+ *   Model::evaluate               -> Model::evaluate          (src/model.cpp:259-320)
+ *   get_opencl_environment        -> get_cuda_environment     (include/profit/opencl.h:159-168)
+ *   Model::set_opencl_env         -> Model::set_cuda_env      (include/profit/model.h:305-311)
+ *   create_convolver(type, prefs) -> create_convolver("cuda") (src/convolve.cpp:521-584)
+ *   Convolver::convolve           -> Convolver::convolve      (include/profit/convolve.h:98-99)
+ *   invalid_parameter, unknown_parameter, opencl_error
+ *                                 -> invalid_parameter, unknown_parameter, cuda_error
+ *                                    (include/profit/exceptions.h:41-104)
+ * Parameter names, types, defaults and validation messages are the
+ * reference's; errors become exceptions of the same categories.
+ */
+#ifndef PROFIT_CUDA_HPP
+#define PROFIT_CUDA_HPP
+
+#include <cstdint>
+#include <cstdlib>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "pf_cuda.h"
+
+namespace profit_cuda {
+
+class exception : public std::exception {
+public:
+	explicit exception(const std::string &what) : m_what(what) {}
+	const char *what() const noexcept override { return m_what.c_str(); }
+
+private:
+	std::string m_what;
+};
+
+class invalid_parameter : public exception {
+public:
+	explicit invalid_parameter(const std::string &what) : exception(what) {}
+};
+
+class unknown_parameter : public exception {
+public:
+	explicit unknown_parameter(const std::string &what) : exception(what) {}
+};
+
+class cuda_error : public exception {
+public:
+	explicit cuda_error(const std::string &what) : exception(what) {}
+};
+
+inline void check(pf_status s)
+{
+	if (s == PF_OK) return;
+	const std::string msg = pf_last_error();
+	if (s == PF_ERR_INVALID_PARAMETER) throw invalid_parameter(msg);
+	if (s == PF_ERR_UNKNOWN_PARAMETER) throw unknown_parameter(msg);
+	if (s == PF_ERR_CUDA || s == PF_ERR_NO_MEMORY) throw cuda_error(msg);
+	throw exception(msg);
+}
+
+/* A 2-D image: row-major doubles, element (x, y) at x + y * width
+ * (include/profit/image.h:664-823). */
+class Image {
+public:
+	Image() : m_w(0), m_h(0) {}
+	Image(unsigned int w, unsigned int h) : m_data((size_t)w * h, 0.0), m_w(w), m_h(h) {}
+	Image(std::vector<double> data, unsigned int w, unsigned int h) : m_data(std::move(data)), m_w(w), m_h(h)
+	{
+		if (m_data.size() != (size_t)w * h) throw std::invalid_argument("data.size() != w * h");
+	}
+	unsigned int getWidth() const { return m_w; }
+	unsigned int getHeight() const { return m_h; }
+	size_t size() const { return m_data.size(); }
+	double *data() { return m_data.data(); }
+	const double *data() const { return m_data.data(); }
+	double &operator[](size_t i) { return m_data[i]; }
+	double operator[](size_t i) const { return m_data[i]; }
+	double total() const
+	{
+		double s = 0;
+		for (double v : m_data) s += v;
+		return s;
+	}
+
+private:
+	std::vector<double> m_data;
+	unsigned int m_w, m_h;
+};
+
+/* A CUDA environment (OpenCLEnv analogue). use_double selects the plain FP64
+ * path that reproduces the reference's arithmetic. */
+class CUDAEnv {
+public:
+	CUDAEnv(int device, bool use_double) : m_env(nullptr)
+	{
+		check(pf_env_create(device, use_double ? PF_ENV_DOUBLE : 0u, &m_env));
+	}
+	~CUDAEnv() { pf_env_destroy(m_env); }
+	CUDAEnv(const CUDAEnv &) = delete;
+	CUDAEnv &operator=(const CUDAEnv &) = delete;
+	pf_env *get() const { return m_env; }
+
+private:
+	pf_env *m_env;
+};
+typedef std::shared_ptr<CUDAEnv> CUDAEnvPtr;
+
+inline CUDAEnvPtr get_cuda_environment(int device = 0, bool use_double = true)
+{
+	return std::make_shared<CUDAEnv>(device, use_double);
+}
+
+class Model;
+
+/* A profile of a Model (include/profit/profile.h:78-260). */
+class Profile {
+public:
+	Profile(const std::string &name, int kind) : m_name(name)
+	{
+		m_desc = pf_profile_desc();
+		m_desc.kind = kind;
+		m_desc.convolve = 0;
+		m_desc.rough = 0;
+		m_desc.adjust = 1;
+		m_desc.rescale_flux = 0;
+		m_desc.resolution = 9;
+		m_desc.max_recursions = 2;
+		m_desc.acc = kind == PF_FERRER ? 1.0 : 0.1;
+		m_desc.rscale_switch = 1.0;
+		m_desc.rscale_max = 0.0;
+		for (int i = 0; i < PF_NPAR; i++) m_desc.par[i] = 0.0;
+		if (is_radial()) {
+			m_desc.par[PF_P_MAG] = 15.0;
+			m_desc.par[PF_P_AXRAT] = 1.0;
+		}
+		// constructor defaults of each profile
+		switch (kind) {
+		case PF_SERSIC: set_slots({1.0, 1.0}); break;
+		case PF_CORESERSIC: set_slots({1.0, 4.0, 1.0, 1.0, 1.0}); break;
+		case PF_MOFFAT: set_slots({3.0, 2.0}); break;
+		case PF_FERRER: set_slots({3.0, 1.0, 1.0}); break;
+		case PF_KING: set_slots({1.0, 3.0, 2.0}); break;
+		case PF_BROKENEXP: set_slots({1.0, 1.0, 1.0, 1.0}); break;
+		default: break;
+		}
+	}
+
+	const std::string &get_name() const { return m_name; }
+	const pf_profile_desc &desc() const { return m_desc; }
+
+	void parameter(const std::string &name, double value)
+	{
+		double *slot = double_slot(name);
+		if (!slot) throw invalid_parameter("Unknown double parameter in profile " + m_name + ": " + name);
+		*slot = value;
+	}
+	void parameter(const std::string &name, bool value)
+	{
+		int32_t *slot = bool_slot(name);
+		if (!slot) throw invalid_parameter("Unknown bool parameter in profile " + m_name + ": " + name);
+		*slot = value ? 1 : 0;
+	}
+	void parameter(const std::string &name, unsigned int value)
+	{
+		uint32_t *slot = uint_slot(name);
+		if (!slot) throw invalid_parameter("Unknown unsigned int parameter in profile " + m_name + ": " + name);
+		*slot = value;
+	}
+	/* "name=value" */
+	void parameter(const std::string &spec)
+	{
+		const size_t eq = spec.find('=');
+		if (eq == std::string::npos || spec.find('=', eq + 1) != std::string::npos) {
+			throw invalid_parameter("missing = in parameter: " + spec);
+		}
+		const std::string name = trim(spec.substr(0, eq)), val = trim(spec.substr(eq + 1));
+		try {
+			if (int32_t *b = bool_slot(name)) {
+				*b = std::stoul(val, nullptr, 10) != 0;
+				return;
+			}
+			if (uint32_t *u = uint_slot(name)) {
+				*u = (uint32_t)std::stoul(val, nullptr, 10);
+				return;
+			}
+			if (double *d = double_slot(name)) {
+				*d = std::stod(val);
+				return;
+			}
+		}
+		catch (const std::logic_error &) {
+		}
+		throw unknown_parameter("Profile " + m_name + " doesn't support parameter " + name +
+		                        ", or parameter has invalid value: " + val);
+	}
+
+private:
+	bool is_radial() const { return m_desc.kind >= PF_SERSIC && m_desc.kind <= PF_BROKENEXP; }
+
+	void set_slots(std::initializer_list<double> vals)
+	{
+		int i = PF_P_X0;
+		for (double v : vals) m_desc.par[i++] = v;
+	}
+
+	static std::string trim(const std::string &s)
+	{
+		const size_t a = s.find_first_not_of(" \t"), b = s.find_last_not_of(" \t");
+		return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+	}
+
+	int32_t *bool_slot(const std::string &n)
+	{
+		if (n == "convolve") return &m_desc.convolve;
+		if (is_radial() && n == "rough") return &m_desc.rough;
+		if (is_radial() && n == "adjust") return &m_desc.adjust;
+		if (is_radial() && n == "force_cpu") return &m_force_cpu;  // accepted; there is no CPU path here
+		if (m_desc.kind == PF_SERSIC && n == "rescale_flux") return &m_desc.rescale_flux;
+		return nullptr;
+	}
+
+	uint32_t *uint_slot(const std::string &n)
+	{
+		if (is_radial() && n == "resolution") return &m_desc.resolution;
+		if (is_radial() && n == "max_recursions") return &m_desc.max_recursions;
+		return nullptr;
+	}
+
+	double *double_slot(const std::string &n)
+	{
+		static const std::map<int, std::vector<std::string>> specific = {
+		    {PF_SERSIC, {"re", "nser"}},
+		    {PF_CORESERSIC, {"re", "nser", "rb", "a", "b"}},
+		    {PF_MOFFAT, {"fwhm", "con"}},
+		    {PF_FERRER, {"rout", "a", "b"}},
+		    {PF_KING, {"rc", "rt", "a"}},
+		    {PF_BROKENEXP, {"h1", "h2", "rb", "a"}},
+		    {PF_SKY, {"bg"}},
+		};
+		static const char *common[] = {"xcen", "ycen", "mag", "ang", "axrat", "box"};
+		if (is_radial()) {
+			for (int i = 0; i < 6; i++)
+				if (n == common[i]) return &m_desc.par[i];
+			if (n == "acc") return &m_desc.acc;
+			if (n == "rscale_switch") return &m_desc.rscale_switch;
+			if (n == "rscale_max") return &m_desc.rscale_max;
+		}
+		if (m_desc.kind == PF_PSF) {
+			for (int i = 0; i < 3; i++)
+				if (n == common[i]) return &m_desc.par[i];
+		}
+		auto it = specific.find(m_desc.kind);
+		if (it != specific.end()) {
+			for (size_t i = 0; i < it->second.size(); i++)
+				if (n == it->second[i]) return &m_desc.par[PF_P_X0 + i];
+		}
+		return nullptr;
+	}
+
+	std::string m_name;
+	pf_profile_desc m_desc;
+	int32_t m_force_cpu = 0;
+};
+typedef std::shared_ptr<Profile> ProfilePtr;
+
+/* Model::evaluate on the GPU. */
+class Model {
+public:
+	Model(unsigned int width = 0, unsigned int height = 0) : m_width(width), m_height(height) {}
+
+	ProfilePtr add_profile(const std::string &name)
+	{
+		static const std::map<std::string, int> kinds = {
+		    {"sersic", PF_SERSIC}, {"coresersic", PF_CORESERSIC}, {"moffat", PF_MOFFAT},
+		    {"ferrer", PF_FERRER}, {"ferrers", PF_FERRER},       {"king", PF_KING},
+		    {"brokenexp", PF_BROKENEXP}, {"sky", PF_SKY},        {"psf", PF_PSF},
+		    {"null", PF_NULL}};
+		auto it = kinds.find(name);
+		if (it == kinds.end()) throw invalid_parameter("Unknown profile name: " + name);
+		m_profiles.push_back(std::make_shared<Profile>(name, it->second));
+		return m_profiles.back();
+	}
+
+	void set_dimensions(unsigned int w, unsigned int h) { m_width = w, m_height = h; }
+	void set_image_pixel_scale(const std::pair<double, double> &s) { m_scale = s; }
+	void set_psf_pixel_scale(const std::pair<double, double> &s) { m_psf_scale = s; }
+	void set_magzero(double magzero) { m_magzero = magzero; }
+	void set_finesampling(unsigned int fs)
+	{
+		if (fs == 0) throw std::invalid_argument("finesampling must be > 0");
+		m_finesampling = fs;
+	}
+	void set_return_finesampled(bool b) { m_return_finesampled = b; }
+	/* The PSF is normalised to unit sum on the device, as set_psf does. */
+	void set_psf(const Image &psf) { m_psf = psf; }
+	void set_cuda_env(const CUDAEnvPtr &env) { m_env = env; }
+	CUDAEnvPtr get_cuda_env() const { return m_env; }
+
+	Image evaluate()
+	{
+		if (!m_env) m_env = get_cuda_environment(0, true);
+		pf_model_desc m = desc();
+		std::vector<pf_profile_desc> profs;
+		for (auto &p : m_profiles) profs.push_back(p->desc());
+		uint32_t w = 0, h = 0;
+		check(pf_model_output_dims(&m, profs.data(), &w, &h));
+		Image out(w, h);
+		check(pf_model_evaluate(m_env->get(), &m, profs.data(), m_psf.size() ? m_psf.data() : nullptr, out.data(),
+		                        &w, &h));
+		return out;
+	}
+
+	pf_model_desc desc() const
+	{
+		pf_model_desc m = pf_model_desc();
+		m.width = m_width;
+		m.height = m_height;
+		m.scale_x = m_scale.first;
+		m.scale_y = m_scale.second;
+		m.magzero = m_magzero;
+		m.finesampling = m_finesampling;
+		m.return_finesampled = m_return_finesampled ? 1 : 0;
+		m.first_profile = 0;
+		m.n_profiles = (uint32_t)m_profiles.size();
+		m.psf_offset = m_psf.size() ? 0 : -1;
+		m.psf_w = m_psf.getWidth();
+		m.psf_h = m_psf.getHeight();
+		m.psf_scale_x = m_psf_scale.first;
+		m.psf_scale_y = m_psf_scale.second;
+		m.convolver = PF_CONV_AUTO;
+		return m;
+	}
+
+private:
+	unsigned int m_width, m_height;
+	std::pair<double, double> m_scale{1.0, 1.0}, m_psf_scale{1.0, 1.0};
+	double m_magzero = 0.0;
+	unsigned int m_finesampling = 1;
+	bool m_return_finesampled = true;
+	Image m_psf;
+	CUDAEnvPtr m_env;
+	std::vector<ProfilePtr> m_profiles;
+};
+
+/* ConvolverType::CUDA: a direct convolution on the GPU with the reference's
+ * semantics (src/convolve.cpp:55-79, crop = true). */
+class Convolver {
+public:
+	explicit Convolver(CUDAEnvPtr env) : m_env(std::move(env)) {}
+	Image convolve(const Image &src, const Image &krn, const std::vector<uint8_t> &mask = {})
+	{
+		Image out(src.getWidth(), src.getHeight());
+		check(pf_convolve(m_env->get(), src.data(), src.getWidth(), src.getHeight(), krn.data(), krn.getWidth(),
+		                  krn.getHeight(), mask.empty() ? nullptr : mask.data(), out.data()));
+		return out;
+	}
+
+private:
+	CUDAEnvPtr m_env;
+};
+typedef std::shared_ptr<Convolver> ConvolverPtr;
+
+inline ConvolverPtr create_convolver(const std::string &type, CUDAEnvPtr env = nullptr)
+{
+	if (type != "cuda") throw invalid_parameter("Unsupported convolver type: " + type);
+	return std::make_shared<Convolver>(env ? env : get_cuda_environment(0, true));
+}
+
+}  // namespace profit_cuda
+
+#endif /* PROFIT_CUDA_HPP */

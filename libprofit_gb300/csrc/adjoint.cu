@@ -134,9 +134,12 @@ __device__ __forceinline__ void sersic_grad(const ProfileDev &P, T xp, T yp, T w
 
 // ------------------------------------------------------------- backward eval
 
+// A sub-pixel box as in eval_f32.cu: its corner relative to the profile
+// centre as an unevaluated sum hi + lo in T (lo stays 0 in double), its size
+// and its eight running totals.
 template <typename T>
 struct FrameG {
-	double dx0, dy0, bx, by;
+	T xhi, xlo, yhi, ylo, bx, by;
 	T tot[kGradSlots];
 	unsigned int mask[kMaskWords];
 };
@@ -145,6 +148,25 @@ template <typename T>
 struct WarpScratchG {
 	FrameG<T> fr[kMaxLevels];
 };
+
+template <typename T>
+__device__ __forceinline__ void two_sum_t(T a, T b, T &s, T &e)
+{
+	s = a + b;
+	const T bb = s - a;
+	e = (a - (s - bb)) + (b - bb);
+}
+
+// hi + lo = i * (s_hi + s_lo) - (c_hi + c_lo), the product formed error-free
+__device__ __forceinline__ void corner_pair_b(float i, float s_hi, float s_lo, float c_hi, float c_lo, float &hi,
+                                              float &lo)
+{
+	const float p = i * s_hi;
+	const float ep = fmaf(i, s_hi, -p) + i * s_lo;
+	float e;
+	two_sum_t<float>(p, -c_hi, hi, e);
+	lo = (e + ep) - c_lo;
+}
 
 template <typename T>
 __device__ __forceinline__ T value_at(const ProfileDev &P, T xp, T yp)
@@ -164,14 +186,13 @@ __device__ bool test_f64b(const ProfileDev &P, double dx, double dy, double xbin
 }
 
 template <typename T>
-__device__ void eval_frame_g(const ProfileDev &P, WarpScratchG<T> &ws, int L, unsigned int res, double dinv_res,
+__device__ void eval_frame_g(const ProfileDev &P, WarpScratchG<T> &ws, int L, unsigned int res, T inv_res,
                              unsigned int max_rec, int lane)
 {
 	constexpr bool dbl = std::is_same<T, double>::value;
 	FrameG<T> &f = ws.fr[L];
-	const double dx0 = f.dx0, dy0 = f.dy0;
-	const double xbin = f.bx * dinv_res, ybin = f.by * dinv_res;
-	const T tdx0 = (T)dx0, tdy0 = (T)dy0, txbin = (T)xbin, tybin = (T)ybin;
+	const T xhi = f.xhi, xlo = f.xlo, yhi = f.yhi, ylo = f.ylo;
+	const T txbin = f.bx * inv_res, tybin = f.by * inv_res;
 	const bool recurse = res > 1 && (unsigned int)L < max_rec;
 	const unsigned int n = res * res;
 	const T c = dbl ? (T)P.cos_ang : (T)P.fcos, s = dbl ? (T)P.sin_ang : (T)P.fsin;
@@ -186,8 +207,9 @@ __device__ void eval_frame_g(const ProfileDev &P, WarpScratchG<T> &ws, int L, un
 		bool fail = false;
 		if (idx < n) {
 			const unsigned int i = idx / res, j = idx % res;
-			const T dx = tdx0 + ((T)i + (T)0.5) * txbin;
-			const T dy = tdy0 + ((T)j + (T)0.5) * tybin;
+			const T ox = ((T)i + (T)0.5) * txbin, oy = ((T)j + (T)0.5) * tybin;
+			const T dx = (xhi + ox) + xlo;
+			const T dy = (yhi + oy) + ylo;
 			const T xp = dx * c + dy * s;
 			const T yp = (dy * c - dx * s) * iq;
 			if (recurse) {
@@ -195,7 +217,8 @@ __device__ void eval_frame_g(const ProfileDev &P, WarpScratchG<T> &ws, int L, un
 				const T t = value_at<T>(P, fabs(xp), fabs(yp) + tdyp);
 				const T d = fabs(t / sv - (T)1);
 				if (!dbl && (!(isfinite(d) && isfinite(sv)) || fabs(d - acc_t) <= (T)kGuardAccB * (acc_t + (T)1))) {
-					fail = test_f64b(P, dx0 + (i + 0.5) * xbin, dy0 + (j + 0.5) * ybin, xbin, ybin);
+					fail = test_f64b(P, ((double)xhi + (double)xlo) + (double)ox,
+					                 ((double)yhi + (double)ylo) + (double)oy, (double)txbin, (double)tybin);
 				}
 				else {
 					fail = d > acc_t;
@@ -215,20 +238,22 @@ __device__ void eval_frame_g(const ProfileDev &P, WarpScratchG<T> &ws, int L, un
 }
 
 template <typename T>
-__device__ void warp_subsample_g(const ProfileDev &P, WarpScratchG<T> &ws, double dx0, double dy0, double bx,
-                                 double by, unsigned int res, unsigned int max_rec, int lane, T *out)
+__device__ void warp_subsample_g(const ProfileDev &P, WarpScratchG<T> &ws, T xhi, T xlo, T yhi, T ylo, T bx, T by,
+                                 unsigned int res, unsigned int max_rec, int lane, T *out)
 {
 	if (lane == 0) {
-		ws.fr[0].dx0 = dx0;
-		ws.fr[0].dy0 = dy0;
+		ws.fr[0].xhi = xhi;
+		ws.fr[0].xlo = xlo;
+		ws.fr[0].yhi = yhi;
+		ws.fr[0].ylo = ylo;
 		ws.fr[0].bx = bx;
 		ws.fr[0].by = by;
 	}
 	__syncwarp();
-	const double dinv_res = 1.0 / res;
+	const T inv_res = (T)1 / (T)res;
 	const T inv_res2 = (T)1 / (T)(res * res);
 	int L = 0;
-	eval_frame_g<T>(P, ws, 0, res, dinv_res, max_rec, lane);
+	eval_frame_g<T>(P, ws, 0, res, inv_res, max_rec, lane);
 	const unsigned int nwords = (res * res + 31) / 32;
 	while (true) {
 		FrameG<T> &f = ws.fr[L];
@@ -244,17 +269,20 @@ __device__ void warp_subsample_g(const ProfileDev &P, WarpScratchG<T> &ws, doubl
 		if (k >= 0) {
 			if (lane == 0) {
 				const unsigned int i = (unsigned int)k / res, j = (unsigned int)k % res;
-				const double cbx = f.bx * dinv_res, cby = f.by * dinv_res;
+				const T cbx = f.bx * inv_res, cby = f.by * inv_res;
 				f.mask[k >> 5] &= ~(1u << (k & 31));
 				FrameG<T> &ch = ws.fr[L + 1];
-				ch.dx0 = f.dx0 + i * cbx;
-				ch.dy0 = f.dy0 + j * cby;
+				T e;
+				two_sum_t<T>(f.xhi, (T)i * cbx, ch.xhi, e);
+				ch.xlo = f.xlo + e;
+				two_sum_t<T>(f.yhi, (T)j * cby, ch.yhi, e);
+				ch.ylo = f.ylo + e;
 				ch.bx = cbx;
 				ch.by = cby;
 			}
 			__syncwarp();
 			L++;
-			eval_frame_g<T>(P, ws, L, res, dinv_res, max_rec, lane);
+			eval_frame_g<T>(P, ws, L, res, inv_res, max_rec, lane);
 		}
 		else {
 			if (L == 0) {
@@ -337,7 +365,7 @@ backward_kernel(const ModelDev *__restrict__ models, int n_models, const Profile
 				}
 				// the forward pass's decisions for this pixel (eval_f32.cu / eval_f64.cu)
 				T xp, yp;
-				double bdx0 = 0, bdy0 = 0;
+				float fdx = 0.f, fdy = 0.f;
 				bool beyond, outside;
 				if (dbl) {
 					const double x = m.sx / 2. + px * m.sx, y = m.sy / 2. + row * m.sy;
@@ -356,6 +384,8 @@ backward_kernel(const ModelDev *__restrict__ models, int n_models, const Profile
 					const float yl = fmaf(cy, m.fsy_hi, -yh) + cy * m.fsy_lo;
 					const float dx = (xh - P.fxc_hi) + (xl - P.fxc_lo);
 					const float dy = (yh - P.fyc_hi) + (yl - P.fyc_lo);
+					fdx = dx;
+					fdy = dy;
 					xp = (T)(dx * P.fcos + dy * P.fsin);
 					yp = (T)((dy * P.fcos - dx * P.fsin) * P.finv_axrat);
 					const float rr = sqrtf((float)(xp * xp + yp * yp)) * P.finv_rscale;
@@ -391,20 +421,39 @@ backward_kernel(const ModelDev *__restrict__ models, int n_models, const Profile
 					const int src = __ffs(pending) - 1;
 					pending &= pending - 1;
 					const int spx = (int)(bc0 + (int)(t % ncols)) * 32 + src;
+					const float sdx = __shfl_sync(0xffffffffu, fdx, src);
+					const float sdy = __shfl_sync(0xffffffffu, fdy, src);
 					unsigned int res = P.resolution, max_rec = P.max_recursions;
 					if (P.adjust && P.par[7] > 1) {  // sersic central pixel (src/sersic.cpp:331-347)
-						const double x = m.sx / 2. + spx * m.sx, y = m.sy / 2. + row * m.sy;
-						if (fabs(x - P.xc) < m.scale_x && fabs(y - P.yc) < m.scale_y) {
+						bool center;
+						if (!dbl && fabsf(fabsf(sdx) - m.fscale_x) > 1e-5f * m.fscale_x &&
+						    fabsf(fabsf(sdy) - m.fscale_y) > 1e-5f * m.fscale_y) {
+							center = fabsf(sdx) < m.fscale_x && fabsf(sdy) < m.fscale_y;
+						}
+						else {
+							const double x = m.sx / 2. + spx * m.sx, y = m.sy / 2. + row * m.sy;
+							center = fabs(x - P.xc) < m.scale_x && fabs(y - P.yc) < m.scale_y;
+						}
+						if (center) {
 							res = 8;
 							max_rec = 10;
 						}
 					}
 					if (res > (unsigned int)kMaxRes) res = kMaxRes;
 					if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
-					bdx0 = (double)spx * m.sx - P.xc;
-					bdy0 = (double)row * m.sy - P.yc;
+					T bxh, bxl, byh, byl;
+					if constexpr (dbl) {
+						bxh = (T)((double)spx * m.sx - P.xc);
+						byh = (T)((double)row * m.sy - P.yc);
+						bxl = byl = 0;
+					}
+					else {
+						corner_pair_b((float)spx, m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
+						corner_pair_b((float)row, m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
+					}
 					T sums[kGradSlots];
-					warp_subsample_g<T>(P, ws, bdx0, bdy0, m.sx, m.sy, res, max_rec, lane, sums);
+					warp_subsample_g<T>(P, ws, bxh, bxl, byh, byl, dbl ? (T)m.sx : (T)m.fsx_hi,
+					                    dbl ? (T)m.sy : (T)m.fsy_hi, res, max_rec, lane, sums);
 					const T gs = __shfl_sync(0xffffffffu, g, src);
 					if (lane == 0) {
 #pragma unroll

@@ -40,7 +40,7 @@ struct Vec4<float> {
 };
 template <>
 struct Vec4<double> {
-	using type = double4;
+	using type = double4_16a;
 };
 
 enum ConvMode { CONV_FORWARD = 0, CONV_ADJOINT = 1 };

@@ -36,12 +36,35 @@ constexpr int kWarps32 = 8;
 constexpr float kGuardAcc = 1e-4f;
 constexpr float kGuardRadius = 2e-5f;
 
+// A sub-pixel box: its corner relative to the profile centre as an
+// unevaluated float sum (hi + lo), exact at the pixel level and updated with
+// an error-free addition per level, so that boxes far below float resolution
+// of the pixel coordinate keep their position; its size; its running total.
 struct FrameM {
-	double dx0, dy0;   // box corner relative to the profile centre
-	double bx, by;     // box size
-	float total;       // sum of the accepted sub-point values, then children
+	float xhi, xlo, yhi, ylo;  // corner relative to the profile centre
+	float bx, by;              // box size
+	float total;               // sum of the accepted sub-point values, then children
 	unsigned int mask[kMaskWords];
 };
+
+// s + e = a + b exactly (Knuth's two-sum)
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+	s = a + b;
+	const float bb = s - a;
+	e = (a - (s - bb)) + (b - bb);
+}
+
+// hi + lo = i * (s_hi + s_lo) - (c_hi + c_lo), the product formed error-free
+__device__ __forceinline__ void corner_pair(float i, float s_hi, float s_lo, float c_hi, float c_lo, float &hi,
+                                            float &lo)
+{
+	const float p = i * s_hi;
+	const float ep = fmaf(i, s_hi, -p) + i * s_lo;
+	float e;
+	two_sum(p, -c_hi, hi, e);
+	lo = (e + ep) - c_lo;
+}
 
 struct WarpScratchM {
 	FrameM fr[kMaxLevels];
@@ -74,13 +97,11 @@ __device__ float value_f64(const ProfileDev &P, double dx, double dy)
 }
 
 __device__ void eval_frame_m(const ProfileDev &P, WarpScratchM &ws, int L, unsigned int res, float inv_res,
-                             double dinv_res, unsigned int max_rec, int lane, unsigned long long *counts)
+                             unsigned int max_rec, int lane, unsigned long long *counts)
 {
 	FrameM &f = ws.fr[L];
-	const double dx0 = f.dx0, dy0 = f.dy0;
-	const double xbin = f.bx * dinv_res, ybin = f.by * dinv_res;
-	const float fdx0 = (float)dx0, fdy0 = (float)dy0;
-	const float fxbin = (float)f.bx * inv_res, fybin = (float)f.by * inv_res;
+	const float xhi = f.xhi, xlo = f.xlo, yhi = f.yhi, ylo = f.ylo;
+	const float fxbin = f.bx * inv_res, fybin = f.by * inv_res;
 	const bool recurse = res > 1 && (unsigned int)L < max_rec;
 	const unsigned int n = res * res;
 	const float c = P.fcos, s = P.fsin, iq = P.finv_axrat;
@@ -95,8 +116,9 @@ __device__ void eval_frame_m(const ProfileDev &P, WarpScratchM &ws, int L, unsig
 		bool fail = false;
 		if (idx < n) {
 			const unsigned int i = idx / res, j = idx % res;
-			const float dx = fdx0 + ((float)i + 0.5f) * fxbin;
-			const float dy = fdy0 + ((float)j + 0.5f) * fybin;
+			const float ox = ((float)i + 0.5f) * fxbin, oy = ((float)j + 0.5f) * fybin;
+			const float dx = (xhi + ox) + xlo;
+			const float dy = (yhi + oy) + ylo;
 			const float xp = dx * c + dy * s;
 			const float yp = (dy * c - dx * s) * iq;
 			float sub = f32::evaluate_at(P, xp, yp);
@@ -104,14 +126,16 @@ __device__ void eval_frame_m(const ProfileDev &P, WarpScratchM &ws, int L, unsig
 				const float t = f32::evaluate_at(P, fabsf(xp), fabsf(yp) + fdyp);
 				const float d = fabsf(t / sub - 1.f);
 				if (!(isfinite(d) && isfinite(sub)) || fabsf(d - P.facc) <= kGuardAcc * (P.facc + 1.f)) {
-					fail = test_f64(P, dx0 + (i + 0.5) * xbin, dy0 + (j + 0.5) * ybin, xbin, ybin, sub);
+					// re-taken in FP64 (rare): the point from the exact corner
+					fail = test_f64(P, ((double)xhi + (double)xlo) + (double)ox, ((double)yhi + (double)ylo) + (double)oy,
+					                (double)fxbin, (double)fybin, sub);
 				}
 				else {
 					fail = d > P.facc;
 				}
 			}
 			else if (!isfinite(sub)) {
-				sub = value_f64(P, dx0 + (i + 0.5) * xbin, dy0 + (j + 0.5) * ybin);
+				sub = value_f64(P, ((double)xhi + (double)xlo) + (double)ox, ((double)yhi + (double)ylo) + (double)oy);
 			}
 			if (!fail) part += sub;
 		}
@@ -124,23 +148,24 @@ __device__ void eval_frame_m(const ProfileDev &P, WarpScratchM &ws, int L, unsig
 }
 
 // subsample_pixel on a box given relative to the profile centre
-__device__ float warp_subsample_m(const ProfileDev &P, WarpScratchM &ws, double dx0, double dy0, double bx,
-                                  double by, unsigned int res, unsigned int max_rec, int lane,
+__device__ float warp_subsample_m(const ProfileDev &P, WarpScratchM &ws, float xhi, float xlo, float yhi, float ylo,
+                                  float bx, float by, unsigned int res, unsigned int max_rec, int lane,
                                   unsigned long long *counts, int &deepest)
 {
 	if (lane == 0) {
-		ws.fr[0].dx0 = dx0;
-		ws.fr[0].dy0 = dy0;
+		ws.fr[0].xhi = xhi;
+		ws.fr[0].xlo = xlo;
+		ws.fr[0].yhi = yhi;
+		ws.fr[0].ylo = ylo;
 		ws.fr[0].bx = bx;
 		ws.fr[0].by = by;
 	}
 	__syncwarp();
-	const float inv_res = 1.f / (float)res;
-	const float inv_res2 = 1.f / (float)(res * res);
-	const double dinv_res = 1.0 / res;
+	const float inv_res = __frcp_rn((float)res);
+	const float inv_res2 = __frcp_rn((float)(res * res));
 	int L = 0;
 	deepest = 1;
-	eval_frame_m(P, ws, 0, res, inv_res, dinv_res, max_rec, lane, counts);
+	eval_frame_m(P, ws, 0, res, inv_res, max_rec, lane, counts);
 	const unsigned int nwords = (res * res + 31) / 32;
 	while (true) {
 		FrameM &f = ws.fr[L];
@@ -156,18 +181,21 @@ __device__ float warp_subsample_m(const ProfileDev &P, WarpScratchM &ws, double 
 		if (k >= 0) {
 			if (lane == 0) {
 				const unsigned int i = (unsigned int)k / res, j = (unsigned int)k % res;
-				const double cbx = f.bx * dinv_res, cby = f.by * dinv_res;
+				const float cbx = f.bx * inv_res, cby = f.by * inv_res;
 				f.mask[k >> 5] &= ~(1u << (k & 31));
 				FrameM &ch = ws.fr[L + 1];
-				ch.dx0 = f.dx0 + i * cbx;
-				ch.dy0 = f.dy0 + j * cby;
+				float e;
+				two_sum(f.xhi, (float)i * cbx, ch.xhi, e);
+				ch.xlo = f.xlo + e;
+				two_sum(f.yhi, (float)j * cby, ch.yhi, e);
+				ch.ylo = f.ylo + e;
 				ch.bx = cbx;
 				ch.by = cby;
 			}
 			__syncwarp();
 			L++;
 			if (L + 1 > deepest) deepest = L + 1;
-			eval_frame_m(P, ws, L, res, inv_res, dinv_res, max_rec, lane, counts);
+			eval_frame_m(P, ws, L, res, inv_res, max_rec, lane, counts);
 		}
 		else {
 			const float v = f.total * inv_res2;
@@ -181,7 +209,7 @@ __device__ float warp_subsample_m(const ProfileDev &P, WarpScratchM &ws, double 
 	}
 }
 
-__global__ void __launch_bounds__(kWarps32 * 32)
+__global__ void __launch_bounds__(kWarps32 * 32, 2)
 eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const ProfileDev *__restrict__ profs,
                     const double *__restrict__ psf_pool, float *__restrict__ conv_img, float *__restrict__ direct_img,
                     long long n_tiles, unsigned int *tile_counter, DebugRec dbg)
@@ -288,12 +316,13 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 					}
 					if (res > (unsigned int)kMaxRes) res = kMaxRes;
 					if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
-					// pixel box relative to the profile centre, in FP64
-					const double bdx0 = (double)spx * m.sx - P.xc;
-					const double bdy0 = (double)row * m.sy - P.yc;
+					// pixel box corner (i * scale - centre) as an exact float pair
+					float bxh, bxl, byh, byl;
+					corner_pair((float)spx, m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
+					corner_pair((float)row, m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
 					int deepest = 0;
-					const float v = warp_subsample_m(P, ws, bdx0, bdy0, m.sx, m.sy, res, max_rec, lane, counts,
-					                                 deepest);
+					const float v = warp_subsample_m(P, ws, bxh, bxl, byh, byl, m.fsx_hi, m.fsy_hi, res, max_rec, lane,
+					                                 counts, deepest);
 					if (lane == src) {
 						pixel_val = v;
 						depth = deepest;

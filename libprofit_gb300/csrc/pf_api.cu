@@ -22,7 +22,7 @@
 namespace pf {
 void launch_setup(const ModelDev *models, ProfileDev *profs, int n_profiles, int n_models,
                   unsigned int *tile_counter, unsigned int *err, const double *psf_raw, double *psf_norm,
-                  bool have_psf, cudaStream_t stream);
+                  bool have_psf, double *solves, cudaStream_t stream);
 void launch_eval64(const ModelDev *models, int n_models, const ProfileDev *profs, const double *psf_pool,
                    double *conv_img, double *direct_img, long long n_tiles, unsigned int *tile_counter,
                    DebugRec dbg, int n_sm, cudaStream_t stream);
@@ -210,6 +210,7 @@ struct pf_batch {
 	size_t draw_total = 0;
 	unsigned int *d_counter = nullptr;
 	unsigned int *d_err = nullptr;
+	double *d_solves = nullptr;  // per profile: the inverse-gamma solves of the setup
 	long long n_tiles = 0;
 	uint64_t total_out = 0;
 	bool record = false;
@@ -347,6 +348,7 @@ void pf_batch_destroy(pf_batch *b)
 	cudaFree(b->d_direct);
 	cudaFree(b->d_counter);
 	cudaFree(b->d_err);
+	cudaFree(b->d_solves);
 	cudaFree(b->d_depth);
 	cudaFree(b->d_counts);
 	cudaFree(b->d_psf32);
@@ -502,6 +504,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 	PF_CUDA_TRY(cudaMalloc(&b->d_profiles, sizeof(pf::ProfileDev) * std::max<size_t>(1, n_profiles)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_counter, sizeof(unsigned int)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_err, sizeof(unsigned int)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_solves, sizeof(double) * 3 * std::max<size_t>(1, n_profiles)));
 	PF_CUDA_TRY(cudaMemset(b->d_err, 0, sizeof(unsigned int)));
 	const size_t elem = b->dbl ? sizeof(double) : sizeof(float);
 	PF_CUDA_TRY(cudaMalloc(&b->d_conv, elem * std::max<size_t>(1, b->draw_total)));
@@ -518,7 +521,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 	if (any_psf) {
 		// PSF normalisation (Model::set_psf), once per batch
 		pf::launch_setup(b->d_models, b->d_profiles, 0, (int)n_models, b->d_counter, b->d_err, b->d_psf_raw,
-		                 b->d_psf_norm, true, env->stream);
+		                 b->d_psf_norm, true, b->d_solves, env->stream);
 		if (!b->dbl) {
 			PF_CUDA_TRY(cudaMalloc(&b->d_psf32, sizeof(float) * psf_pool_len));
 			pf::launch_psf_to_float(b->d_psf_norm, b->d_psf32, (long long)psf_pool_len, env->stream);
@@ -645,7 +648,7 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 	}
 	long t = stage_begin(b, ST_SETUP, stream);
 	pf::launch_setup(b->d_models, b->d_profiles, n_profiles, n_models, b->d_counter, b->d_err, nullptr, nullptr,
-	                 false, stream);
+	                 false, b->d_solves, stream);
 	stage_end(b, t, stream);
 	if (b->dbl) {
 		t = stage_begin(b, ST_EVAL, stream);

@@ -367,40 +367,49 @@ __device__ void radial_setup(ProfileDev &p, const ModelDev &m, double bn, const 
 
 }  // namespace
 
+// The independent inverse-gamma solves of the sersic-like profiles, one per
+// thread, task-major so that each warp runs one kind of solve:
+//   task 0  bn = P^-1(1/2, 2n)                 (sersic, coresersic)
+//   task 1  P^-1(1 - n^2/2000, 2n)             (sersic switch radius, adjust)
+//   task 2  P^-1(0.9999, 2n)                   (sersic rscale_max, adjust, rscale_max = 0)
+__global__ void setup_solves_kernel(const ProfileDev *profs, int n_profiles, double *solves)
+{
+	const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+	if (t >= 3LL * n_profiles) {
+		return;
+	}
+	const int task = (int)(t / n_profiles), i = (int)(t % n_profiles);
+	const int kind = profs[i].kind;
+	const double nser = profs[i].par[7];
+	double v = 0.;
+	if (task == 0 && (kind == PF_SERSIC || kind == PF_CORESERSIC)) {
+		v = sf::qgamma(0.5, 2 * nser, sf::bn_guess(nser));
+	}
+	else if (task == 1 && kind == PF_SERSIC && profs[i].adjust) {
+		v = sf::qgamma(1. - nser * nser / 2e3, 2 * nser);
+	}
+	else if (task == 2 && kind == PF_SERSIC && profs[i].adjust && profs[i].rscale_max_in == 0) {
+		v = sf::qgamma(0.9999, 2 * nser);
+	}
+	solves[(size_t)i * 3 + task] = v;
+}
+
 __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs, int n_profiles,
-                                      unsigned int *tile_counter, unsigned int *err)
+                                      const double *solves, unsigned int *tile_counter, unsigned int *err)
 {
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		*tile_counter = 0;
 	}
-	// one warp per profile: the independent inverse-gamma solves of a sersic
-	// profile run on separate lanes, lane 0 does the rest
-	const int lane = threadIdx.x & 31;
-	const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= n_profiles) {
 		return;
 	}
 	const int kind = profs[t].kind;
 	const double nser = profs[t].par[7];
-	const bool sersic_like = kind == PF_SERSIC || kind == PF_CORESERSIC;
-	double bn = 0.;
-	if (sersic_like && lane == 0) {
-		bn = sf::qgamma(0.5, 2 * nser, sf::bn_guess(nser));
-	}
-	bn = __shfl_sync(0xffffffffu, bn, 0);
-	SersicSolves sv{0., 0., 0.};
-	if (kind == PF_SERSIC) {
-		double v = 0.;
-		const bool adjust = profs[t].adjust != 0;
-		if (lane == 1 && adjust) v = sf::qgamma(1. - nser * nser / 2e3, 2 * nser);
-		if (lane == 2 && adjust && profs[t].rscale_max_in == 0) v = sf::qgamma(0.9999, 2 * nser);
-		if (lane == 3 && !profs[t].rescale_flux) v = dbn_dn(nser, bn);
-		sv.q_switch = __shfl_sync(0xffffffffu, v, 1);
-		sv.q_max = __shfl_sync(0xffffffffu, v, 2);
-		sv.dbn = __shfl_sync(0xffffffffu, v, 3);
-	}
-	if (lane != 0) {
-		return;
+	const double bn = solves[(size_t)t * 3 + 0];
+	SersicSolves sv{solves[(size_t)t * 3 + 1], solves[(size_t)t * 3 + 2], 0.};
+	if (kind == PF_SERSIC && !profs[t].rescale_flux) {
+		sv.dbn = dbn_dn(nser, bn);
 	}
 	ProfileDev p = profs[t];
 	const ModelDev &m = models[p.model];
@@ -446,12 +455,16 @@ __global__ void normalise_psf_kernel(const ModelDev *models, const double *raw, 
 
 void launch_setup(const ModelDev *models, ProfileDev *profs, int n_profiles, int n_models,
                   unsigned int *tile_counter, unsigned int *err, const double *psf_raw, double *psf_norm,
-                  bool have_psf, cudaStream_t stream)
+                  bool have_psf, double *solves, cudaStream_t stream)
 {
-	const int warps = 2;  // profiles per block
-	int blocks = (n_profiles + warps - 1) / warps;
+	// single-warp blocks: the FP64-heavy work spreads over as many SMs as possible
+	if (n_profiles > 0) {
+		const long long tasks = 3LL * n_profiles;
+		setup_solves_kernel<<<(unsigned int)((tasks + 31) / 32), 32, 0, stream>>>(profs, n_profiles, solves);
+	}
+	int blocks = (n_profiles + 31) / 32;
 	if (blocks < 1) blocks = 1;
-	setup_profiles_kernel<<<blocks, warps * 32, 0, stream>>>(models, profs, n_profiles, tile_counter, err);
+	setup_profiles_kernel<<<blocks, 32, 0, stream>>>(models, profs, n_profiles, solves, tile_counter, err);
 	if (have_psf && n_models > 0) {
 		normalise_psf_kernel<<<n_models, 128, 0, stream>>>(models, psf_raw, psf_norm);
 	}
