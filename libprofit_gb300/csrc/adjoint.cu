@@ -175,7 +175,7 @@ __device__ __forceinline__ T value_at(const ProfileDev &P, T xp, T yp)
 	else return f32::evaluate_at(P, xp, yp);
 }
 
-__device__ bool test_f64b(const ProfileDev &P, double dx, double dy, double xbin, double ybin)
+__device__ __noinline__ bool test_f64b(const ProfileDev &P, double dx, double dy, double xbin, double ybin)
 {
 	const double xp = dx * P.cos_ang + dy * P.sin_ang;
 	const double yp = (-dx * P.sin_ang + dy * P.cos_ang) / P.par[PF_P_AXRAT];
@@ -206,8 +206,8 @@ __device__ void eval_frame_g(const ProfileDev &P, WarpScratchG<T> &ws, int L, un
 		const unsigned int idx = base + lane;
 		bool fail = false;
 		if (idx < n) {
-			const unsigned int i = idx / res, j = idx % res;
-			const T ox = ((T)i + (T)0.5) * txbin, oy = ((T)j + (T)0.5) * tybin;
+			const unsigned int i = div_res(idx, res_magic(res)), j = idx - i * res;
+			const T ox = ((T)small_int_to_float(i) + (T)0.5) * txbin, oy = ((T)small_int_to_float(j) + (T)0.5) * tybin;
 			const T dx = (xhi + ox) + xlo;
 			const T dy = (yhi + oy) + ylo;
 			const T xp = dx * c + dy * s;
@@ -268,14 +268,14 @@ __device__ void warp_subsample_g(const ProfileDev &P, WarpScratchG<T> &ws, T xhi
 		__syncwarp();
 		if (k >= 0) {
 			if (lane == 0) {
-				const unsigned int i = (unsigned int)k / res, j = (unsigned int)k % res;
+				const unsigned int i = div_res((unsigned int)k, res_magic(res)), j = (unsigned int)k - i * res;
 				const T cbx = f.bx * inv_res, cby = f.by * inv_res;
 				f.mask[k >> 5] &= ~(1u << (k & 31));
 				FrameG<T> &ch = ws.fr[L + 1];
 				T e;
-				two_sum_t<T>(f.xhi, (T)i * cbx, ch.xhi, e);
+				two_sum_t<T>(f.xhi, (T)small_int_to_float(i) * cbx, ch.xhi, e);
 				ch.xlo = f.xlo + e;
-				two_sum_t<T>(f.yhi, (T)j * cby, ch.yhi, e);
+				two_sum_t<T>(f.yhi, (T)small_int_to_float(j) * cby, ch.yhi, e);
 				ch.ylo = f.ylo + e;
 				ch.bx = cbx;
 				ch.by = cby;
@@ -352,8 +352,10 @@ backward_kernel(const ModelDev *__restrict__ models, int n_models, const Profile
 				if (lane == 0) t = atomicAdd(&tile_next, 1u);
 				t = __shfl_sync(0xffffffffu, t, 0);
 				if (t >= n_tiles) break;
-				const int row = br0 + (int)(t / ncols);
-				const int px = (bc0 + (int)(t % ncols)) * 32 + lane;
+				const int trow = (int)(t / (unsigned int)ncols);
+				const int tcol = bc0 + (int)(t - (unsigned int)(trow * ncols));
+				const int row = br0 + trow;
+				const int px = tcol * 32 + lane;
 				const bool active = px < (int)m.draw_w;
 				T g = 0;
 				if (active) {
@@ -378,7 +380,7 @@ backward_kernel(const ModelDev *__restrict__ models, int n_models, const Profile
 					outside = r64 / P.rscale > P.rscale_switch;
 				}
 				else {
-					const float cx = (float)px + 0.5f, cy = (float)row + 0.5f;
+					const float cx = small_int_to_float(px) + 0.5f, cy = small_int_to_float(row) + 0.5f;
 					const float xh = cx * m.fsx_hi, yh = cy * m.fsy_hi;
 					const float xl = fmaf(cx, m.fsx_hi, -xh) + cx * m.fsx_lo;
 					const float yl = fmaf(cy, m.fsy_hi, -yh) + cy * m.fsy_lo;
@@ -420,11 +422,11 @@ backward_kernel(const ModelDev *__restrict__ models, int n_models, const Profile
 				while (pending) {
 					const int src = __ffs(pending) - 1;
 					pending &= pending - 1;
-					const int spx = (int)(bc0 + (int)(t % ncols)) * 32 + src;
+					const int spx = tcol * 32 + src;
 					const float sdx = __shfl_sync(0xffffffffu, fdx, src);
 					const float sdy = __shfl_sync(0xffffffffu, fdy, src);
 					unsigned int res = P.resolution, max_rec = P.max_recursions;
-					if (P.adjust && P.par[7] > 1) {  // sersic central pixel (src/sersic.cpp:331-347)
+					if (P.center_boost) {  // sersic central pixel (src/sersic.cpp:331-347)
 						bool center;
 						if (!dbl && fabsf(fabsf(sdx) - m.fscale_x) > 1e-5f * m.fscale_x &&
 						    fabsf(fabsf(sdy) - m.fscale_y) > 1e-5f * m.fscale_y) {
@@ -448,8 +450,8 @@ backward_kernel(const ModelDev *__restrict__ models, int n_models, const Profile
 						bxl = byl = 0;
 					}
 					else {
-						corner_pair_b((float)spx, m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
-						corner_pair_b((float)row, m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
+						corner_pair_b(small_int_to_float(spx), m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
+						corner_pair_b(small_int_to_float(row), m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
 					}
 					T sums[kGradSlots];
 					warp_subsample_g<T>(P, ws, bxh, bxl, byh, byl, dbl ? (T)m.sx : (T)m.fsx_hi,

@@ -78,7 +78,7 @@ __device__ __forceinline__ float warp_sum(float v)
 }
 
 // FP64 value and accuracy test of one sub-point (the rare re-taken decisions)
-__device__ bool test_f64(const ProfileDev &P, double dx, double dy, double xbin, double ybin, float &subval)
+__device__ __noinline__ bool test_f64(const ProfileDev &P, double dx, double dy, double xbin, double ybin, float &subval)
 {
 	const double xp = dx * P.cos_ang + dy * P.sin_ang;
 	const double yp = (-dx * P.sin_ang + dy * P.cos_ang) / P.par[PF_P_AXRAT];
@@ -89,7 +89,7 @@ __device__ bool test_f64(const ProfileDev &P, double dx, double dy, double xbin,
 	return fabs(t / s - 1.0) > P.acc;
 }
 
-__device__ float value_f64(const ProfileDev &P, double dx, double dy)
+__device__ __noinline__ float value_f64(const ProfileDev &P, double dx, double dy)
 {
 	const double xp = dx * P.cos_ang + dy * P.sin_ang;
 	const double yp = (-dx * P.sin_ang + dy * P.cos_ang) / P.par[PF_P_AXRAT];
@@ -111,12 +111,13 @@ __device__ void eval_frame_m(const ProfileDev &P, WarpScratchM &ws, int L, unsig
 		atomicAdd(&counts[kCountSubEvals], (unsigned long long)(recurse ? 2 * n : n));
 	}
 	float part = 0.f;
+	const unsigned int magic = res_magic(res);
 	for (unsigned int base = 0; base < n; base += 32) {
 		const unsigned int idx = base + lane;
 		bool fail = false;
 		if (idx < n) {
-			const unsigned int i = idx / res, j = idx % res;
-			const float ox = ((float)i + 0.5f) * fxbin, oy = ((float)j + 0.5f) * fybin;
+			const unsigned int i = div_res(idx, magic), j = idx - i * res;
+			const float ox = (small_int_to_float(i) + 0.5f) * fxbin, oy = (small_int_to_float(j) + 0.5f) * fybin;
 			const float dx = (xhi + ox) + xlo;
 			const float dy = (yhi + oy) + ylo;
 			const float xp = dx * c + dy * s;
@@ -180,14 +181,14 @@ __device__ float warp_subsample_m(const ProfileDev &P, WarpScratchM &ws, float x
 		__syncwarp();
 		if (k >= 0) {
 			if (lane == 0) {
-				const unsigned int i = (unsigned int)k / res, j = (unsigned int)k % res;
+				const unsigned int i = div_res((unsigned int)k, res_magic(res)), j = (unsigned int)k - i * res;
 				const float cbx = f.bx * inv_res, cby = f.by * inv_res;
 				f.mask[k >> 5] &= ~(1u << (k & 31));
 				FrameM &ch = ws.fr[L + 1];
 				float e;
-				two_sum(f.xhi, (float)i * cbx, ch.xhi, e);
+				two_sum(f.xhi, small_int_to_float(i) * cbx, ch.xhi, e);
 				ch.xlo = f.xlo + e;
-				two_sum(f.yhi, (float)j * cby, ch.yhi, e);
+				two_sum(f.yhi, small_int_to_float(j) * cby, ch.yhi, e);
 				ch.ylo = f.ylo + e;
 				ch.bx = cbx;
 				ch.by = cby;
@@ -225,14 +226,14 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 		const int mi = find_model(models, n_models, tile);
 		const ModelDev &m = models[mi];
 		const long long local = tile - m.tile_base;
-		const unsigned int row = (unsigned int)(local / m.tiles_per_row);
-		const int col0 = (int)(local % m.tiles_per_row) * 32;
+		const unsigned int row = (unsigned int)local / m.tiles_per_row;
+		const int col0 = (int)((unsigned int)local - row * m.tiles_per_row) * 32;
 		const int col1 = min(col0 + 31, (int)m.draw_w - 1);
 		const unsigned int px = (unsigned int)col0 + lane;
 		const bool active = px < m.draw_w;
 		const double *psf = m.psf_off >= 0 ? psf_pool + m.psf_off : nullptr;
 		// pixel centre (i + 1/2) * scale as an unevaluated float sum
-		const float cx = (float)px + 0.5f, cy = (float)row + 0.5f;
+		const float cx = small_int_to_float(px) + 0.5f, cy = small_int_to_float(row) + 0.5f;
 		const float xh = cx * m.fsx_hi, yh = cy * m.fsy_hi;
 		const float xl = fmaf(cx, m.fsx_hi, -xh) + cx * m.fsx_lo;
 		const float yl = fmaf(cy, m.fsy_hi, -yh) + cy * m.fsy_lo;
@@ -302,7 +303,7 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 					const float sdx = __shfl_sync(0xffffffffu, dx, src);
 					const float sdy = __shfl_sync(0xffffffffu, dy, src);
 					unsigned int res = P.resolution, max_rec = P.max_recursions;
-					if (P.kind == PF_SERSIC && P.adjust && P.par[7] > 1) {  // src/sersic.cpp:331-347
+					if (P.center_boost) {  // src/sersic.cpp:331-347
 						bool center = fabsf(sdx) < m.fscale_x && fabsf(sdy) < m.fscale_y;
 						if (fabsf(fabsf(sdx) - m.fscale_x) <= 1e-5f * m.fscale_x ||
 						    fabsf(fabsf(sdy) - m.fscale_y) <= 1e-5f * m.fscale_y) {
@@ -318,8 +319,8 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 					if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
 					// pixel box corner (i * scale - centre) as an exact float pair
 					float bxh, bxl, byh, byl;
-					corner_pair((float)spx, m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
-					corner_pair((float)row, m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
+					corner_pair(small_int_to_float(spx), m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
+					corner_pair(small_int_to_float(row), m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
 					int deepest = 0;
 					const float v = warp_subsample_m(P, ws, bxh, bxl, byh, byl, m.fsx_hi, m.fsy_hi, res, max_rec, lane,
 					                                 counts, deepest);

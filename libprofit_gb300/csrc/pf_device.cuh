@@ -54,6 +54,13 @@ struct ModelDev {
 	uint32_t pad0;
 	float fsx_hi, fsx_lo, fsy_hi, fsy_lo;  // drawing pixel scale as unevaluated float sums
 	float fscale_x, fscale_y;              // image pixel scale (sersic central pixel test)
+	// FFT convolution (fft.cu): transform sizes and complex-element offsets of
+	// this model's work area (draw_h rows of fft_mx/2+1 bins) and PSF spectrum
+	// (fft_my rows of fft_mx/2+1 bins)
+	int32_t use_fft;
+	uint32_t fft_mx, fft_my;
+	int32_t pad2;
+	int64_t fft_work_off, fft_spec_off;
 };
 
 struct ProfileDev {
@@ -87,6 +94,7 @@ struct ProfileDev {
 	double dbn;
 	double dlnfs[PF_NPAR];
 	int32_t grad_ok;           // the adjoint supports this profile
+	int32_t center_boost;      // sersic, adjust and nser > 1: the central pixel uses res 8, 10 levels
 	float fbn, fdbn, fnser, fre;
 };
 
@@ -111,6 +119,17 @@ struct DebugRec {
 	int8_t *depth;             // per profile drawing-area depth maps, or nullptr
 	unsigned long long *counts;// n_profiles * kLevelCounts, or nullptr
 };
+
+// floor(idx / res) for idx < 256, res <= 16, by a 16-bit fixed-point
+// reciprocal (error < 256 / 65536 < 1 / res): no integer division
+__device__ __forceinline__ unsigned int div_res(unsigned int idx, unsigned int magic) { return (idx * magic) >> 16; }
+__host__ __device__ __forceinline__ unsigned int res_magic(unsigned int res) { return (65536u + res - 1) / res; }
+
+// (float)i for 0 <= i < 2^23 without a conversion instruction
+__device__ __forceinline__ float small_int_to_float(unsigned int i)
+{
+	return __int_as_float(0x4B000000 | (int)i) - 8388608.f;
+}
 
 __device__ __forceinline__ int find_model(const ModelDev *models, int n_models, long long tile)
 {

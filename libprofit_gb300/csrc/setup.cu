@@ -353,6 +353,7 @@ __device__ void radial_setup(ProfileDev &p, const ModelDev &m, double bn, const 
 	}
 	fold_single_precision(p);
 	adjoint_constants(p, sv.dbn);
+	p.center_boost = p.kind == PF_SERSIC && p.adjust && p.par[7] > 1;
 	unsigned int max_res = p.resolution;
 	unsigned int max_rec = p.max_recursions;
 	if (p.kind == PF_SERSIC && p.adjust && p.par[7] > 1) {  // central pixel, src/sersic.cpp:339-345
@@ -386,10 +387,11 @@ __global__ void setup_solves_kernel(const ProfileDev *profs, int n_profiles, dou
 		v = sf::qgamma(0.5, 2 * nser, sf::bn_guess(nser));
 	}
 	else if (task == 1 && kind == PF_SERSIC && profs[i].adjust) {
-		v = sf::qgamma(1. - nser * nser / 2e3, 2 * nser);
+		const double p = 1. - nser * nser / 2e3;
+		v = sf::qgamma(p, 2 * nser, sf::wilson_hilferty_guess(p, 2 * nser));
 	}
 	else if (task == 2 && kind == PF_SERSIC && profs[i].adjust && profs[i].rscale_max_in == 0) {
-		v = sf::qgamma(0.9999, 2 * nser);
+		v = sf::qgamma(0.9999, 2 * nser, sf::wilson_hilferty_guess(0.9999, 2 * nser));
 	}
 	solves[(size_t)i * 3 + task] = v;
 }

@@ -127,6 +127,19 @@ __device__ inline double bn_guess(double n)
 	return 2 * n - 1. / 3 + r * (4. / 405 + r * (46. / 25515 + r * (131. / 1148175 - r * (2194697. / 30690717750.))));
 }
 
+// Starting point for P^-1(p, a), a >= 1: the Wilson-Hilferty cube-root normal
+// approximation x = a (1 - 1/(9a) + z / (3 sqrt(a)))^3, z the standard normal
+// quantile of p (= sqrt(2) erfcinv(2 (1 - p))); relative error ~1e-3 for the
+// shapes used here, refined to full precision by qgamma.
+__device__ inline double wilson_hilferty_guess(double p, double a)
+{
+	if (a < 1. || !(p > 0.) || !(p < 1.)) return -1.;
+	const double z = 1.4142135623730951 * erfcinv(2. * (1. - p));
+	const double t = 1. - 1. / (9. * a) + z / (3. * sqrt(a));
+	if (!(t > 0.)) return -1.;
+	return a * t * t * t;
+}
+
 // Inverse of P(a, .). With a usable starting point (guess > 0) the root is
 // bracketed around it by doubling steps instead of from [0, max(a, 1)].
 __device__ inline double qgamma(double p, double a, double guess = -1.)
