@@ -301,7 +301,17 @@ class Model:
         self.env = env
 
     def set_convolver(self, convolver):
-        self.convolver = convolver.kind if isinstance(convolver, Convolver) else int(convolver)
+        """A Convolver from create_convolver, or "auto", "brute" or "fft"."""
+        names = {"auto": _ffi.PF_CONV_AUTO, "brute": _ffi.PF_CONV_BRUTE, "cuda": _ffi.PF_CONV_BRUTE,
+                 "cuda-brute": _ffi.PF_CONV_BRUTE, "fft": _ffi.PF_CONV_FFT, "cuda-fft": _ffi.PF_CONV_FFT}
+        if isinstance(convolver, Convolver):
+            self.convolver = convolver.kind
+        elif isinstance(convolver, str):
+            if convolver not in names:
+                raise InvalidParameter("Unsupported convolver type: %s" % convolver)
+            self.convolver = names[convolver]
+        else:
+            self.convolver = int(convolver)
 
     def _descs(self, first_profile=0, psf_offset=None):
         m = _ffi.ModelDesc()

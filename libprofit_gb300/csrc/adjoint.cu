@@ -32,8 +32,9 @@ namespace {
 
 constexpr int kBandRows = 16;    // drawing rows per backward work item
 constexpr int kWarpsB = 8;
-constexpr float kGuardAccB = 1e-4f;
-constexpr float kGuardRadiusB = 2e-5f;
+// the forward pass's guard bands (eval_f32.cu), so that both take the same decisions
+constexpr float kGuardAccB = 1.2e-5f;
+constexpr float kGuardRadiusB = 2e-6f;
 
 template <typename T>
 __device__ __forceinline__ T warp_sum_t(T v)

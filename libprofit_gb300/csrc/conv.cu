@@ -14,23 +14,34 @@
 // taking four kernel taps per 16-byte broadcast read, so that a shared-memory
 // read feeds up to 4 R FMAs.
 #include <cstdint>
+#include <type_traits>
 
 #include "pf_device.cuh"
 
 namespace pf {
 
+template <typename T>
+cudaError_t conv_configure(size_t smem, int shape);
+template <typename T>
+void launch_conv(int mode, int shape, const ModelDev *models, int n_models, const T *psf, const T *in, const T *direct,
+                 T *out, const long long *tile_base, long long n_tiles, size_t smem, int n_sm, cudaStream_t stream);
+
 namespace {
 
-template <typename T>
-struct ConvShape;
-template <>
-struct ConvShape<float> {
-	static constexpr int TX = 16, TY = 16, R = 8;  // 64 x 128 outputs per block
+// Block shapes: TX x TY threads, each 4 columns by R rows of outputs.
+//   float  0: 16 x 16 x 8 -> 64 x 128 outputs
+//   float  1: 14 x 14 x 5 -> 56 x 70
+//   float  2: 16 x 12 x 8 -> 64 x 96
+//   double 0: 16 x 8 x 4  -> 64 x 32
+// The host picks, per batch and direction, the shape that wastes the least
+// tile area over the images it convolves.
+struct Shape {
+	int tx, ty, r;
 };
-template <>
-struct ConvShape<double> {
-	static constexpr int TX = 16, TY = 8, R = 4;   // 64 x 32 outputs per block
-};
+__host__ __device__ constexpr Shape shape_of(bool dbl, int id)
+{
+	return dbl ? Shape{16, 8, 4} : (id == 1 ? Shape{14, 14, 5} : (id == 2 ? Shape{16, 12, 8} : Shape{16, 16, 8}));
+}
 
 template <typename T>
 struct Vec4;
@@ -65,13 +76,12 @@ __device__ __forceinline__ T cot_at(const ModelDev &m, const T *gout, int x, int
 	return gout[m.out_off + (size_t)cy * m.out_w + cx];
 }
 
-template <typename T, int MODE>
-__global__ void __launch_bounds__(ConvShape<T>::TX * ConvShape<T>::TY)
+template <typename T, int MODE, int TX, int TY, int R>
+__global__ void __launch_bounds__(TX * TY)
 conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restrict__ psf, const T *__restrict__ in,
             const T *__restrict__ direct, T *__restrict__ out, const long long *__restrict__ tile_base,
             long long n_tiles)
 {
-	constexpr int TX = ConvShape<T>::TX, TY = ConvShape<T>::TY, R = ConvShape<T>::R;
 	constexpr int BW = TX * 4, BH = TY * R;  // outputs per block
 	using V4 = typename Vec4<T>::type;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -177,52 +187,103 @@ conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restri
 }  // namespace
 
 template <typename T>
-long long conv_tiles(unsigned int w, unsigned int h)
+int conv_num_shapes()
 {
-	constexpr int BW = ConvShape<T>::TX * 4, BH = ConvShape<T>::TY * ConvShape<T>::R;
-	return (long long)((w + BW - 1) / BW) * ((h + BH - 1) / BH);
+	return std::is_same<T, double>::value ? 1 : 3;
 }
 
 template <typename T>
-size_t conv_smem(unsigned int kw, unsigned int kh)
+long long conv_tiles(unsigned int w, unsigned int h, int shape)
 {
-	constexpr int BW = ConvShape<T>::TX * 4, BH = ConvShape<T>::TY * ConvShape<T>::R;
+	const Shape sh = shape_of(std::is_same<T, double>::value, shape);
+	const unsigned int bw = sh.tx * 4, bh = sh.ty * sh.r;
+	return (long long)((w + bw - 1) / bw) * ((h + bh - 1) / bh);
+}
+
+template <typename T>
+size_t conv_smem(unsigned int kw, unsigned int kh, int shape)
+{
+	const Shape sh = shape_of(std::is_same<T, double>::value, shape);
+	const size_t bw = sh.tx * 4, bh = sh.ty * sh.r;
 	const size_t kwp = (kw + 3) & ~3u;
-	return sizeof(T) * ((BW + kwp) * (BH + kh - 1) + kwp * kh);
+	return sizeof(T) * ((bw + kwp) * (bh + kh - 1) + kwp * kh);
 }
 
-template <typename T>
-cudaError_t conv_configure(size_t smem)
+namespace {
+
+template <typename T, int TX, int TY, int R>
+cudaError_t configure_shape(size_t smem)
 {
-	cudaError_t e = cudaFuncSetAttribute(conv_kernel<T, CONV_FORWARD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	cudaError_t e = cudaFuncSetAttribute(conv_kernel<T, CONV_FORWARD, TX, TY, R>,
+	                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
-	return cudaFuncSetAttribute(conv_kernel<T, CONV_ADJOINT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	return cudaFuncSetAttribute(conv_kernel<T, CONV_ADJOINT, TX, TY, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                            (int)smem);
 }
 
-template <typename T>
-void launch_conv(int mode, const ModelDev *models, int n_models, const T *psf, const T *in, const T *direct, T *out,
-                 const long long *tile_base, long long n_tiles, size_t smem, int n_sm, cudaStream_t stream)
+template <typename T, int TX, int TY, int R>
+void launch_shape(int mode, const ModelDev *models, int n_models, const T *psf, const T *in, const T *direct, T *out,
+                  const long long *tile_base, long long n_tiles, size_t smem, int n_sm, cudaStream_t stream)
 {
-	const int threads = ConvShape<T>::TX * ConvShape<T>::TY;
 	int blocks = (int)(n_tiles < (long long)n_sm * 8 ? n_tiles : (long long)n_sm * 8);
 	if (blocks < 1) blocks = 1;
 	if (mode == CONV_FORWARD)
-		conv_kernel<T, CONV_FORWARD><<<blocks, threads, smem, stream>>>(models, n_models, psf, in, direct, out,
-		                                                                 tile_base, n_tiles);
+		conv_kernel<T, CONV_FORWARD, TX, TY, R><<<blocks, TX * TY, smem, stream>>>(models, n_models, psf, in, direct,
+		                                                                          out, tile_base, n_tiles);
 	else
-		conv_kernel<T, CONV_ADJOINT><<<blocks, threads, smem, stream>>>(models, n_models, psf, in, direct, out,
-		                                                                 tile_base, n_tiles);
+		conv_kernel<T, CONV_ADJOINT, TX, TY, R><<<blocks, TX * TY, smem, stream>>>(models, n_models, psf, in, direct,
+		                                                                          out, tile_base, n_tiles);
 }
 
-template long long conv_tiles<float>(unsigned int, unsigned int);
-template long long conv_tiles<double>(unsigned int, unsigned int);
-template size_t conv_smem<float>(unsigned int, unsigned int);
-template size_t conv_smem<double>(unsigned int, unsigned int);
-template cudaError_t conv_configure<float>(size_t);
-template cudaError_t conv_configure<double>(size_t);
-template void launch_conv<float>(int, const ModelDev *, int, const float *, const float *, const float *, float *,
-                                 const long long *, long long, size_t, int, cudaStream_t);
-template void launch_conv<double>(int, const ModelDev *, int, const double *, const double *, const double *,
-                                  double *, const long long *, long long, size_t, int, cudaStream_t);
+}  // namespace
+
+template <>
+cudaError_t conv_configure<float>(size_t smem, int shape)
+{
+	if (shape == 1) return configure_shape<float, 14, 14, 5>(smem);
+	if (shape == 2) return configure_shape<float, 16, 12, 8>(smem);
+	return configure_shape<float, 16, 16, 8>(smem);
+}
+
+template <>
+cudaError_t conv_configure<double>(size_t smem, int)
+{
+	return configure_shape<double, 16, 8, 4>(smem);
+}
+
+template <>
+void launch_conv<float>(int mode, int shape, const ModelDev *models, int n_models, const float *psf, const float *in,
+                        const float *direct, float *out, const long long *tile_base, long long n_tiles, size_t smem,
+                        int n_sm, cudaStream_t stream)
+{
+	if (shape == 1) launch_shape<float, 14, 14, 5>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
+	else if (shape == 2) launch_shape<float, 16, 12, 8>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
+	else launch_shape<float, 16, 16, 8>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
+}
+
+template <>
+void launch_conv<double>(int mode, int, const ModelDev *models, int n_models, const double *psf, const double *in,
+                         const double *direct, double *out, const long long *tile_base, long long n_tiles, size_t smem,
+                         int n_sm, cudaStream_t stream)
+{
+	launch_shape<double, 16, 8, 4>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
+}
+
+template <typename T>
+void conv_tile_dims(int shape, int *bw, int *bh)
+{
+	const Shape sh = shape_of(std::is_same<T, double>::value, shape);
+	*bw = sh.tx * 4;
+	*bh = sh.ty * sh.r;
+}
+
+template void conv_tile_dims<float>(int, int *, int *);
+template void conv_tile_dims<double>(int, int *, int *);
+template int conv_num_shapes<float>();
+template int conv_num_shapes<double>();
+template long long conv_tiles<float>(unsigned int, unsigned int, int);
+template long long conv_tiles<double>(unsigned int, unsigned int, int);
+template size_t conv_smem<float>(unsigned int, unsigned int, int);
+template size_t conv_smem<double>(unsigned int, unsigned int, int);
 
 }  // namespace pf

@@ -31,10 +31,13 @@ namespace pf {
 namespace {
 
 constexpr int kWarps32 = 8;
-// relative half-width of the band around a threshold inside which an FP32
-// comparison is re-taken in FP64 (FP32 operands carry a few 1e-7 error)
-constexpr float kGuardAcc = 1e-4f;
-constexpr float kGuardRadius = 2e-5f;
+// Half-width of the band around a threshold inside which an FP32 comparison is
+// re-taken in FP64. The FP32 profile values carry at most ~3e-6 relative
+// error (the exp2 argument K (1 - rf) reaches ~40, ~2.4e-6 of rounding, plus
+// the MUFU approximations), so |testval/subval - 1| is within 6e-6 (1 + d) of
+// its FP64 value; the band is twice that. Radii carry a few 1e-7.
+constexpr float kGuardAcc = 1.2e-5f;
+constexpr float kGuardRadius = 2e-6f;
 
 // A sub-pixel box: its corner relative to the profile centre as an
 // unevaluated float sum (hi + lo), exact at the pixel level and updated with

@@ -356,6 +356,7 @@ __global__ void finish64_kernel(const ModelDev *__restrict__ models, int n_model
 	     g += (long long)gridDim.x * blockDim.x) {
 		const int mi = find_model_out(models, n_models, g);
 		const ModelDev &m = models[mi];
+		if (m.use_fft) continue;  // written by the FFT convolution's last pass
 		const long long local = g - m.out_off;
 		const unsigned int ox = (unsigned int)(local % m.out_w), oy = (unsigned int)(local / m.out_w);
 		const double *psf = m.psf_off >= 0 ? psf_pool + m.psf_off : nullptr;

@@ -37,16 +37,31 @@ void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs
                    float *conv_img, float *direct_img, long long n_tiles, unsigned int *tile_counter, DebugRec dbg,
                    int n_sm, cudaStream_t stream);
 template <typename T>
-long long conv_tiles(unsigned int w, unsigned int h);
+int conv_num_shapes();
 template <typename T>
-size_t conv_smem(unsigned int kw, unsigned int kh);
+void conv_tile_dims(int shape, int *bw, int *bh);
 template <typename T>
-cudaError_t conv_configure(size_t smem);
+long long conv_tiles(unsigned int w, unsigned int h, int shape);
 template <typename T>
-void launch_conv(int mode, const ModelDev *models, int n_models, const T *psf, const T *in, const T *direct, T *out,
-                 const long long *tile_base, long long n_tiles, size_t smem, int n_sm, cudaStream_t stream);
+size_t conv_smem(unsigned int kw, unsigned int kh, int shape);
+template <typename T>
+cudaError_t conv_configure(size_t smem, int shape);
+template <typename T>
+void launch_conv(int mode, int shape, const ModelDev *models, int n_models, const T *psf, const T *in, const T *direct,
+                 T *out, const long long *tile_base, long long n_tiles, size_t smem, int n_sm, cudaStream_t stream);
 void launch_psf_to_float(const double *in, float *out, long long n, cudaStream_t stream);
 int backward_band_rows();
+int fft_job_size();
+template <typename T>
+size_t fft_smem(int n, int count);
+template <typename T>
+cudaError_t fft_configure(size_t smem);
+template <typename T>
+void launch_twiddles(void *tw, int nmax, cudaStream_t stream);
+template <typename T>
+void launch_fft_pass(int pass, const ModelDev *models, const void *jobs, int n_jobs, const T *src, const T *psf,
+                     void *work, void *spec, const T *direct, T *out, const void *tw, int nmax, size_t smem,
+                     cudaStream_t stream);
 template <typename T>
 void launch_chi2(const ModelDev *models, int n_models, const void *img, const void *data, const void *sigma,
                  const void *cot, void *gout, double *chi2, cudaStream_t stream);
@@ -223,6 +238,17 @@ struct pf_batch {
 	long long n_out_tiles = 0;
 	size_t finish_smem = 0;
 	bool any_downsample = false;
+	int fwd_shape = 0, adj_shape = 0;  // convolution block shapes (conv.cu)
+	// FFT convolution
+	bool any_fft = false;
+	int fft_nmax = 0;
+	void *d_fft_work = nullptr;
+	void *d_fft_spec = nullptr;
+	void *d_fft_tw = nullptr;
+	void *d_fft_jobs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+	int fft_njobs[5] = {0, 0, 0, 0, 0};
+	size_t fft_smem_bytes = 0;
+	int64_t fft_work_elems = 0, fft_spec_elems = 0;
 	// adjoint
 	bool adjoint = false;
 	void *d_gout = nullptr;
@@ -353,6 +379,10 @@ void pf_batch_destroy(pf_batch *b)
 	cudaFree(b->d_counts);
 	cudaFree(b->d_psf32);
 	cudaFree(b->d_tile_base_out);
+	cudaFree(b->d_fft_work);
+	cudaFree(b->d_fft_spec);
+	cudaFree(b->d_fft_tw);
+	for (void *p : b->d_fft_jobs) cudaFree(p);
 	cudaFree(b->d_gout);
 	cudaFree(b->d_gsrc);
 	cudaFree(b->d_partial);
@@ -366,6 +396,120 @@ void pf_batch_destroy(pf_batch *b)
 	cudaFreeHost(b->h_profiles);
 	delete b;
 }
+
+}  // extern "C"
+
+namespace {
+
+struct HostFftJob {
+	int model, first, count, pad;
+};
+
+// The convolution block shape covering the given images with the least tile area.
+template <typename T>
+int best_conv_shape(const std::vector<std::pair<unsigned int, unsigned int>> &dims)
+{
+	int best = 0;
+	double best_area = -1;
+	for (int s = 0; s < pf::conv_num_shapes<T>(); s++) {
+		double area = 0;
+		int bw = 0, bh = 0;
+		pf::conv_tile_dims<T>(s, &bw, &bh);
+		for (const auto &d : dims) {
+			area += (double)pf::conv_tiles<T>(d.first, d.second, s) * bw * bh;
+		}
+		if (best_area < 0 || area < best_area) {
+			best_area = area;
+			best = s;
+		}
+	}
+	return best;
+}
+
+unsigned int next_pow2(unsigned int v)
+{
+	unsigned int p = 2;
+	while (p < v) p <<= 1;
+	return p;
+}
+
+// Picks direct or FFT convolution per model and lays out the FFT buffers and
+// job lists. An explicit PF_CONV_BRUTE / PF_CONV_FFT is obeyed; PF_CONV_AUTO
+// keeps the plain FP64 path on the direct convolution (the reference's
+// default BRUTE convolver and summation order) and, for the FP32 path, takes
+// the cheaper of the two by a cost model of this GPU: direct = 2 P^2 flop per
+// output pixel at 35 TFLOP/s; FFT = its HBM bytes at 3 TB/s plus
+// 5 N log2 N flop per transform at 10 TFLOP/s.
+pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5])
+{
+	const int nmax = b->dbl ? 4096 : 8192;
+	const int per_block = b->dbl ? 4096 : 8192;  // complex elements of one ping-pong half in shared memory
+	int64_t work = 0, spec = 0;
+	int used_nmax = 2;
+	for (size_t i = 0; i < b->mdev.size(); i++) {
+		pf::ModelDev &d = b->mdev[i];
+		d.use_fft = 0;
+		if (!d.conv_required) continue;
+		const unsigned int mx = next_pow2(d.crop_w + d.psf_w), my = next_pow2(d.crop_h + d.psf_h);
+		bool fft = false;
+		if (d.convolver == PF_CONV_FFT) {
+			if (b->dbl && d.fs > 1 && !d.return_fs) {
+				return fail(PF_ERR_UNSUPPORTED, "model " + std::to_string(i) +
+				                                    ": FFT convolution with SUM downsampling needs the single-precision path");
+			}
+			if ((int)mx > nmax || (int)my > nmax) {
+				return fail(PF_ERR_UNSUPPORTED, "model " + std::to_string(i) + ": FFT size above " +
+				                                    std::to_string(nmax) + " in this precision");
+			}
+			fft = true;
+		}
+		else if (d.convolver == PF_CONV_AUTO && !b->dbl && (int)mx <= nmax && (int)my <= nmax) {
+			const double nb = mx / 2 + 1;
+			const double direct_s = 2.0 * d.crop_w * d.crop_h * d.psf_w * d.psf_h / 35e12;
+			const double bytes = nb * 8 * (2.0 * d.draw_h + 2.0 * d.crop_h + my) +
+			                     4.0 * ((double)d.draw_w * d.draw_h + 2.0 * d.crop_w * d.crop_h);
+			const double flops = 5.0 * (d.draw_h * mx * std::log2((double)mx) + 2 * nb * my * std::log2((double)my) +
+			                            d.crop_h * mx * std::log2((double)mx));
+			fft = bytes / 3e12 + flops / 10e12 < direct_s;
+		}
+		if (!fft) continue;
+		d.use_fft = 1;
+		d.fft_mx = mx;
+		d.fft_my = my;
+		const int64_t nb = mx / 2 + 1;
+		d.fft_work_off = work;
+		d.fft_spec_off = spec;
+		work += (int64_t)d.draw_h * nb;
+		spec += (int64_t)my * nb;
+		used_nmax = std::max(used_nmax, (int)std::max(mx, my));
+		const int cr = std::max(1, std::min(16, per_block / (int)mx));
+		const int cc = std::max(1, std::min(16, per_block / (int)my));
+		for (unsigned int r = 0; r < d.draw_h; r += cr) jobs[0].push_back({(int)i, (int)r, (int)std::min<unsigned int>(cr, d.draw_h - r), 0});
+		for (int c = 0; c < nb; c += cc) jobs[1].push_back({(int)i, c, (int)std::min<int64_t>(cc, nb - c), 0});
+		for (unsigned int r = 0; r < d.crop_h; r += cr) jobs[2].push_back({(int)i, (int)r, (int)std::min<unsigned int>(cr, d.crop_h - r), 0});
+		for (unsigned int r = 0; r < d.psf_h; r += cr) jobs[3].push_back({(int)i, (int)r, (int)std::min<unsigned int>(cr, d.psf_h - r), 0});
+		for (int c = 0; c < nb; c += cc) jobs[4].push_back({(int)i, c, (int)std::min<int64_t>(cc, nb - c), 0});
+		b->any_fft = true;
+	}
+	b->fft_nmax = used_nmax;
+	b->fft_work_elems = work;
+	b->fft_spec_elems = spec;
+	// the shared memory of the largest job: two halves of count x n complex values
+	size_t smem = 0;
+	for (int p = 0; p < 5; p++) {
+		for (const auto &j : jobs[p]) {
+			const pf::ModelDev &d = b->mdev[j.model];
+			const int n = (p == 1 || p == 4) ? (int)d.fft_my : (int)d.fft_mx;
+			smem = std::max(smem, b->dbl ? pf::fft_smem<double>(n, j.count) : pf::fft_smem<float>(n, j.count));
+		}
+	}
+	b->fft_smem_bytes = smem;
+	return PF_OK;
+}
+
+}  // namespace
+
+extern "C" {
 
 static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, size_t n_models,
                                    const pf_profile_desc *profiles, size_t n_profiles, const double *psf_pool,
@@ -450,22 +594,33 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 	if (b->n_tiles >= (1ll << 32)) {
 		return fail(PF_ERR_UNSUPPORTED, "batch too large: more than 2^32 tiles of 32 pixels");
 	}
+	std::vector<HostFftJob> fft_jobs[5];
+	pf_status fs = plan_fft(b, fft_jobs);
+	if (fs != PF_OK) return fs;
 	std::vector<long long> tile_base_out(std::max<size_t>(1, n_models), 0);
 	if (!b->dbl) {
 		unsigned int max_kw = 1, max_kh = 1;
+		std::vector<std::pair<unsigned int, unsigned int>> conv_dims;
+		for (size_t i = 0; i < n_models; i++) {
+			const pf::ModelDev &d = b->mdev[i];
+			if (!d.use_fft) conv_dims.push_back({d.crop_w, d.crop_h});
+		}
+		b->fwd_shape = best_conv_shape<float>(conv_dims);
 		long long t = 0;
 		for (size_t i = 0; i < n_models; i++) {
 			const pf::ModelDev &d = b->mdev[i];
 			tile_base_out[i] = t;
-			t += pf::conv_tiles<float>(d.crop_w, d.crop_h);
-			if (d.conv_required) {
-				max_kw = std::max(max_kw, d.psf_w);
-				max_kh = std::max(max_kh, d.psf_h);
+			if (!d.use_fft) {  // models convolved by FFT are finished by its last pass
+				t += pf::conv_tiles<float>(d.crop_w, d.crop_h, b->fwd_shape);
+				if (d.conv_required) {
+					max_kw = std::max(max_kw, d.psf_w);
+					max_kh = std::max(max_kh, d.psf_h);
+				}
 			}
 			b->any_downsample |= d.fs > 1 && !d.return_fs;
 		}
 		b->n_out_tiles = t;
-		b->finish_smem = pf::conv_smem<float>(max_kw, max_kh);
+		b->finish_smem = pf::conv_smem<float>(max_kw, max_kh, b->fwd_shape);
 		if (b->finish_smem > 227 * 1024) {
 			return fail(PF_ERR_UNSUPPORTED, "PSF too large for the shared-memory direct convolution");
 		}
@@ -533,7 +688,44 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		PF_CUDA_TRY(cudaMalloc(&b->d_tile_base_out, sizeof(long long) * tile_base_out.size()));
 		PF_CUDA_TRY(cudaMemcpy(b->d_tile_base_out, tile_base_out.data(), sizeof(long long) * tile_base_out.size(),
 		                       cudaMemcpyHostToDevice));
-		PF_CUDA_TRY(pf::conv_configure<float>(b->finish_smem));
+		PF_CUDA_TRY(pf::conv_configure<float>(b->finish_smem, b->fwd_shape));
+	}
+	if (b->any_fft) {
+		// FFT buffers, twiddles and, once per batch, the PSF spectra
+		if ((size_t)pf::fft_job_size() != sizeof(HostFftJob)) return fail(PF_ERR_INTERNAL, "FFT job layout");
+		const size_t celem = b->dbl ? 2 * sizeof(double) : 2 * sizeof(float);
+		PF_CUDA_TRY(cudaMalloc(&b->d_fft_work, celem * std::max<int64_t>(1, b->fft_work_elems)));
+		PF_CUDA_TRY(cudaMalloc(&b->d_fft_spec, celem * std::max<int64_t>(1, b->fft_spec_elems)));
+		PF_CUDA_TRY(cudaMalloc(&b->d_fft_tw, celem * (b->fft_nmax / 2)));
+		for (int p = 0; p < 5; p++) {
+			b->fft_njobs[p] = (int)fft_jobs[p].size();
+			PF_CUDA_TRY(cudaMalloc(&b->d_fft_jobs[p], sizeof(HostFftJob) * std::max<size_t>(1, fft_jobs[p].size())));
+			if (!fft_jobs[p].empty()) {
+				PF_CUDA_TRY(cudaMemcpy(b->d_fft_jobs[p], fft_jobs[p].data(), sizeof(HostFftJob) * fft_jobs[p].size(),
+				                       cudaMemcpyHostToDevice));
+			}
+		}
+		if (b->fft_smem_bytes > 227 * 1024) return fail(PF_ERR_UNSUPPORTED, "FFT too large for shared memory");
+		if (b->dbl) {
+			PF_CUDA_TRY(pf::fft_configure<double>(b->fft_smem_bytes));
+			pf::launch_twiddles<double>(b->d_fft_tw, b->fft_nmax, env->stream);
+			for (int p = 3; p <= 4; p++) {
+				pf::launch_fft_pass<double>(p, b->d_models, b->d_fft_jobs[p], b->fft_njobs[p], nullptr, b->d_psf_norm,
+				                            b->d_fft_work, b->d_fft_spec, nullptr, nullptr, b->d_fft_tw, b->fft_nmax,
+				                            b->fft_smem_bytes, env->stream);
+			}
+		}
+		else {
+			PF_CUDA_TRY(pf::fft_configure<float>(b->fft_smem_bytes));
+			pf::launch_twiddles<float>(b->d_fft_tw, b->fft_nmax, env->stream);
+			for (int p = 3; p <= 4; p++) {
+				pf::launch_fft_pass<float>(p, b->d_models, b->d_fft_jobs[p], b->fft_njobs[p], nullptr, b->d_psf32,
+				                           b->d_fft_work, b->d_fft_spec, nullptr, nullptr, b->d_fft_tw, b->fft_nmax,
+				                           b->fft_smem_bytes, env->stream);
+			}
+		}
+		PF_CUDA_TRY(cudaGetLastError());
+		PF_CUDA_TRY(cudaStreamSynchronize(env->stream));
 	}
 	b->params_dirty = true;
 	return PF_OK;
@@ -659,6 +851,11 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 		pf::launch_finish64(b->d_models, n_models, b->d_psf_norm, (const double *)b->d_conv,
 		                    (const double *)b->d_direct, (double *)images_dev, (long long)b->total_out,
 		                    b->env->n_sm, stream);
+		for (int p = 0; b->any_fft && p <= 2; p++) {
+			pf::launch_fft_pass<double>(p, b->d_models, b->d_fft_jobs[p], b->fft_njobs[p], (const double *)b->d_conv,
+			                            nullptr, b->d_fft_work, b->d_fft_spec, (const double *)b->d_direct,
+			                            (double *)images_dev, b->d_fft_tw, b->fft_nmax, b->fft_smem_bytes, stream);
+		}
 		stage_end(b, t, stream);
 	}
 	else {
@@ -670,9 +867,14 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 		if (b->any_downsample) {
 			PF_CUDA_TRY(cudaMemsetAsync(images_dev, 0, sizeof(float) * b->total_out, stream));
 		}
-		pf::launch_conv<float>(0, b->d_models, n_models, b->d_psf32, (const float *)b->d_conv,
+		pf::launch_conv<float>(0, b->fwd_shape, b->d_models, n_models, b->d_psf32, (const float *)b->d_conv,
 		                       (const float *)b->d_direct, (float *)images_dev, b->d_tile_base_out, b->n_out_tiles,
 		                       b->finish_smem, b->env->n_sm, stream);
+		for (int p = 0; b->any_fft && p <= 2; p++) {
+			pf::launch_fft_pass<float>(p, b->d_models, b->d_fft_jobs[p], b->fft_njobs[p], (const float *)b->d_conv,
+			                           nullptr, b->d_fft_work, b->d_fft_spec, (const float *)b->d_direct,
+			                           (float *)images_dev, b->d_fft_tw, b->fft_nmax, b->fft_smem_bytes, stream);
+		}
 		stage_end(b, t, stream);
 	}
 	b->forward_calls++;
@@ -739,6 +941,11 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	    adj_tile_base(std::max<size_t>(1, n_models));
 	long long items = 0, parts = 0, tiles = 0;
 	unsigned int max_kw = 1, max_kh = 1;
+	std::vector<std::pair<unsigned int, unsigned int>> conv_dims;
+	for (const auto &m : b->mdev) {
+		if (m.conv_required) conv_dims.push_back({m.draw_w, m.draw_h});
+	}
+	b->adj_shape = b->dbl ? best_conv_shape<double>(conv_dims) : best_conv_shape<float>(conv_dims);
 	for (size_t i = 0; i < n_models; i++) {
 		const pf::ModelDev &m = b->mdev[i];
 		const long long bands = (m.draw_h + band_rows - 1) / band_rows;
@@ -747,15 +954,17 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 		adj_tile_base[i] = tiles;
 		items += bands;
 		parts += bands * m.n_profiles * pf::kGradSlots;
-		tiles += b->dbl ? pf::conv_tiles<double>(m.draw_w, m.draw_h) : pf::conv_tiles<float>(m.draw_w, m.draw_h);
 		if (m.conv_required) {
+			tiles += b->dbl ? pf::conv_tiles<double>(m.draw_w, m.draw_h, b->adj_shape)
+			                : pf::conv_tiles<float>(m.draw_w, m.draw_h, b->adj_shape);
 			max_kw = std::max(max_kw, m.psf_w);
 			max_kh = std::max(max_kh, m.psf_h);
 		}
 	}
 	b->n_band_items = items;
 	b->n_adj_tiles = tiles;
-	b->adj_smem = b->dbl ? pf::conv_smem<double>(max_kw, max_kh) : pf::conv_smem<float>(max_kw, max_kh);
+	b->adj_smem = b->dbl ? pf::conv_smem<double>(max_kw, max_kh, b->adj_shape)
+	                     : pf::conv_smem<float>(max_kw, max_kh, b->adj_shape);
 	if (b->adj_smem > 227 * 1024) return fail(PF_ERR_UNSUPPORTED, "PSF too large for the adjoint convolution");
 	PF_CUDA_TRY(cudaMalloc(&b->d_gout, elem * std::max<uint64_t>(1, b->total_out)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_gsrc, elem * std::max<size_t>(1, b->draw_total)));
@@ -767,7 +976,8 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	PF_CUDA_TRY(cudaMemcpy(b->d_part_base, part_base.data(), sizeof(long long) * part_base.size(), cudaMemcpyHostToDevice));
 	PF_CUDA_TRY(cudaMemcpy(b->d_adj_tile_base, adj_tile_base.data(), sizeof(long long) * adj_tile_base.size(),
 	                       cudaMemcpyHostToDevice));
-	PF_CUDA_TRY(b->dbl ? pf::conv_configure<double>(b->adj_smem) : pf::conv_configure<float>(b->adj_smem));
+	PF_CUDA_TRY(b->dbl ? pf::conv_configure<double>(b->adj_smem, b->adj_shape)
+	                   : pf::conv_configure<float>(b->adj_smem, b->adj_shape));
 	if (b->dbl && !b->d_psf_norm) {
 		// no PSF anywhere: the adjoint convolution is never launched
 	}
@@ -797,10 +1007,10 @@ pf_status pf_backward(pf_batch *b, const void *images_dev, const void *data_dev,
 	stage_end(b, t, stream);
 	if (any_conv) {
 		t = stage_begin(b, ST_ADJCONV, stream);
-		if (b->dbl) pf::launch_conv<double>(1, b->d_models, n_models, b->d_psf_norm, (const double *)b->d_gout,
+		if (b->dbl) pf::launch_conv<double>(1, b->adj_shape, b->d_models, n_models, b->d_psf_norm, (const double *)b->d_gout,
 		                                    nullptr, (double *)b->d_gsrc, b->d_adj_tile_base, b->n_adj_tiles,
 		                                    b->adj_smem, b->env->n_sm, stream);
-		else pf::launch_conv<float>(1, b->d_models, n_models, b->d_psf32, (const float *)b->d_gout, nullptr,
+		else pf::launch_conv<float>(1, b->adj_shape, b->d_models, n_models, b->d_psf32, (const float *)b->d_gout, nullptr,
 		                            (float *)b->d_gsrc, b->d_adj_tile_base, b->n_adj_tiles, b->adj_smem,
 		                            b->env->n_sm, stream);
 		stage_end(b, t, stream);

@@ -128,6 +128,8 @@ def to_model(spec, env=None):
     import libprofit_gb300 as pg
     m = pg.Model(spec["width"], spec["height"])
     m.set_magzero(spec.get("magzero", 0.0))
+    if spec.get("convolver") in ("fft", "brute", "auto"):
+        m.set_convolver(spec["convolver"])
     if spec.get("psf") is not None:
         m.set_psf(spec["psf"])
     if env is not None:
