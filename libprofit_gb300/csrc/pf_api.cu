@@ -1114,6 +1114,8 @@ pf_status pf_convolve(pf_env *env, const double *src, uint32_t w, uint32_t h, co
 		ew = std::max(w, kw);
 		eh = ew;
 	}
+	// Surface::extend refuses a smaller height (include/profit/image.h:305-311)
+	if (eh < h) return fail(PF_ERR_INVALID_PARAMETER, "pf_convolve: new_height should be >= height");
 	const size_t n = (size_t)ew * eh, kn = (size_t)kw * kh;
 	std::vector<double> ext;
 	std::vector<uint8_t> emask;
@@ -1136,9 +1138,10 @@ pf_status pf_convolve(pf_env *env, const double *src, uint32_t w, uint32_t h, co
 	if (e == cudaSuccess) e = cudaMalloc(&d_out, sizeof(double) * n);
 	if (e == cudaSuccess) e = cudaMalloc(&d_krn, sizeof(double) * kn);
 	if (e == cudaSuccess && m_host) e = cudaMalloc(&d_mask, n);
-	if (e == cudaSuccess) e = cudaMemcpy(d_src, s_host, sizeof(double) * n, cudaMemcpyHostToDevice);
-	if (e == cudaSuccess) e = cudaMemcpy(d_krn, krn, sizeof(double) * kn, cudaMemcpyHostToDevice);
-	if (e == cudaSuccess && m_host) e = cudaMemcpy(d_mask, m_host, n, cudaMemcpyHostToDevice);
+	// on the kernel's stream: a pageable copy may return before its DMA ends
+	if (e == cudaSuccess) e = cudaMemcpyAsync(d_src, s_host, sizeof(double) * n, cudaMemcpyHostToDevice, env->stream);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(d_krn, krn, sizeof(double) * kn, cudaMemcpyHostToDevice, env->stream);
+	if (e == cudaSuccess && m_host) e = cudaMemcpyAsync(d_mask, m_host, n, cudaMemcpyHostToDevice, env->stream);
 	if (e == cudaSuccess) {
 		pf::launch_convolve64(d_src, ew, eh, d_krn, kw, kh, d_mask, d_out, env->n_sm, env->stream);
 		e = cudaGetLastError();

@@ -142,3 +142,7 @@ def test_convolver_matches_reference_brute(env, oracle_lib):
     ext[:10, :10] = src
     ref = O.convolve_brute(ext, krn)[:10, :10]
     np.testing.assert_allclose(conv.convolve(src, krn), ref, rtol=1e-13, atol=0)
+    # the extension's height repeats the width maximum; one below the image's
+    # height is refused, as Surface::extend refuses it
+    with pytest.raises(pg.InvalidParameter):
+        conv.convolve(rng.random((40, 10)), rng.random((15, 15)))
