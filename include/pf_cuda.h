@@ -178,6 +178,40 @@ PF_API pf_status pf_convolve(pf_env *env, const double *src, uint32_t w, uint32_
                       double *out);
 
 /*
+ * pf_convolve_noalloc: pf_convolve without allocating memory of any kind. No
+ * counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory at the moment they convolve:
+ * a fitting loop running beside a caching allocator that holds almost all of
+ * the device's memory (a cudaMalloc there fails), or a host thread feeding
+ * other streams whose work must not stall (cudaFree synchronises the whole
+ * device). Same arguments, results and errors as pf_convolve; the device work
+ * is the same kernel on the environment's stream, and the call returns after
+ * that stream has finished it.
+ *
+ * Its device scratch is a fixed array in this library's static device data,
+ * 17.5 MiB on each device: the image (after its extension to the kernel's
+ * size) may have at most PF_NOALLOC_MAX_PIXELS pixels and the kernel at most
+ * PF_NOALLOC_MAX_KERNEL_PIXELS; larger inputs are refused with
+ * PF_ERR_DEVICE_LIMIT and nothing is run (use pf_convolve for them). Nothing
+ * in the scratch needs to start at zero: every call writes every scratch
+ * element it reads.
+ *
+ * The first call on each device looks up the scratch's address, which can
+ * load this library's device code onto that device; make that first call
+ * before any stream capture. All calls on one device share the one scratch:
+ * calls that overlap in time on the same device (from several threads, or
+ * through several environments) race and give wrong results; serialise them.
+ * On success nothing is allocated; a failure records its message for
+ * pf_last_error as every entry point does.
+ */
+#define PF_NOALLOC_MAX_PIXELS (1u << 20)
+#define PF_NOALLOC_MAX_KERNEL_PIXELS (1u << 16)
+PF_API pf_status pf_convolve_noalloc(pf_env *env, const double *src, uint32_t w, uint32_t h,
+                              const double *krn, uint32_t kw, uint32_t kh, const uint8_t *mask,
+                              double *out);
+
+/*
  * Batched path. pf_batch_create copies the descriptors, the PSF pool (host,
  * psf_pool_len doubles) and sizes every device buffer once; pf_forward then
  * allocates nothing. Output images of all models are packed back to back;

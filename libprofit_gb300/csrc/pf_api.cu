@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -1164,6 +1165,120 @@ pf_status pf_convolve(pf_env *env, const double *src, uint32_t w, uint32_t h, co
 	cudaFree(d_out);
 	cudaFree(d_mask);
 	return s;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// pf_convolve_noalloc: pf_convolve with its device buffers in static device
+// data, for callers that must not allocate (see include/pf_cuda.h).
+
+namespace {
+
+// Layout of the scratch: source image, output image, kernel, mask; each part
+// starts on a 256-byte boundary.
+constexpr size_t kNaSrcOff = 0;
+constexpr size_t kNaOutOff = kNaSrcOff + sizeof(double) * PF_NOALLOC_MAX_PIXELS;
+constexpr size_t kNaKrnOff = kNaOutOff + sizeof(double) * PF_NOALLOC_MAX_PIXELS;
+constexpr size_t kNaMaskOff = kNaKrnOff + sizeof(double) * PF_NOALLOC_MAX_KERNEL_PIXELS;
+constexpr size_t kNaBytes = kNaMaskOff + PF_NOALLOC_MAX_PIXELS;
+static_assert(kNaOutOff % 256 == 0 && kNaKrnOff % 256 == 0 && kNaMaskOff % 256 == 0 && kNaBytes % 256 == 0,
+              "scratch parts must start on 256-byte boundaries");
+
+// Reserved with the module on each device, never by a call.
+static __device__ __align__(256) unsigned char g_convolve_scratch[kNaBytes];
+
+constexpr int kNaMaxDevices = 64;
+std::mutex g_convolve_scratch_mutex;
+unsigned char *g_convolve_scratch_addr[kNaMaxDevices] = {};
+
+// Address of g_convolve_scratch on `device`, which must be the current device.
+// Looked up on the first call for a device, then read from the table.
+pf_status convolve_scratch(int device, unsigned char **addr)
+{
+	if (device < 0 || device >= kNaMaxDevices) {
+		return fail(PF_ERR_DEVICE_LIMIT, "pf_convolve_noalloc: device ordinal beyond the scratch address table");
+	}
+	std::lock_guard<std::mutex> lock(g_convolve_scratch_mutex);
+	if (!g_convolve_scratch_addr[device]) {
+		void *p = nullptr;
+		cudaError_t e = cudaGetSymbolAddress(&p, g_convolve_scratch);
+		if (e != cudaSuccess) {
+			return fail(PF_ERR_CUDA, std::string("pf_convolve_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+		}
+		g_convolve_scratch_addr[device] = static_cast<unsigned char *>(p);
+	}
+	*addr = g_convolve_scratch_addr[device];
+	return PF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pf_status pf_convolve_noalloc(pf_env *env, const double *src, uint32_t w, uint32_t h, const double *krn, uint32_t kw,
+                              uint32_t kh, const uint8_t *mask, double *out)
+{
+	if (!env || !src || !krn || !out) return fail(PF_ERR_INVALID_PARAMETER, "pf_convolve_noalloc: NULL argument");
+	if (w == 0 || h == 0 || kw == 0 || kh == 0) {
+		return fail(PF_ERR_INVALID_PARAMETER, "pf_convolve_noalloc: empty image");
+	}
+	// the extension of pf_convolve (Convolver::convolve, src/convolve.cpp:63-74)
+	uint32_t ew = w, eh = h;
+	if (!(w >= kw && h >= kh)) {
+		ew = std::max(w, kw);
+		eh = ew;
+	}
+	if (eh < h) return fail(PF_ERR_INVALID_PARAMETER, "pf_convolve_noalloc: new_height should be >= height");
+	const size_t n = (size_t)ew * eh, kn = (size_t)kw * kh;
+	if (n > PF_NOALLOC_MAX_PIXELS) {
+		return fail(PF_ERR_DEVICE_LIMIT, "pf_convolve_noalloc: image of " + std::to_string(n) +
+		                                     " pixels (after extension to the kernel's size) exceeds the static "
+		                                     "scratch's " + std::to_string(PF_NOALLOC_MAX_PIXELS) +
+		                                     "; use pf_convolve");
+	}
+	if (kn > PF_NOALLOC_MAX_KERNEL_PIXELS) {
+		return fail(PF_ERR_DEVICE_LIMIT, "pf_convolve_noalloc: kernel of " + std::to_string(kn) +
+		                                     " pixels exceeds the static scratch's " +
+		                                     std::to_string(PF_NOALLOC_MAX_KERNEL_PIXELS) + "; use pf_convolve");
+	}
+	PF_CUDA_TRY(cudaSetDevice(env->device));
+	unsigned char *base = nullptr;
+	pf_status s = convolve_scratch(env->device, &base);
+	if (s != PF_OK) return s;
+	double *d_src = reinterpret_cast<double *>(base + kNaSrcOff);
+	double *d_out = reinterpret_cast<double *>(base + kNaOutOff);
+	double *d_krn = reinterpret_cast<double *>(base + kNaKrnOff);
+	uint8_t *d_mask = mask ? base + kNaMaskOff : nullptr;
+	cudaStream_t st = env->stream;
+	const bool extended = ew != w || eh != h;
+	const size_t row = sizeof(double) * w, erow = sizeof(double) * ew;
+	cudaError_t e = cudaSuccess;
+	if (extended) {
+		// zero extension, the original at the top left (Surface::extend, start 0)
+		e = cudaMemsetAsync(d_src, 0, sizeof(double) * n, st);
+		if (e == cudaSuccess) e = cudaMemcpy2DAsync(d_src, erow, src, row, row, h, cudaMemcpyHostToDevice, st);
+		if (e == cudaSuccess && mask) e = cudaMemsetAsync(d_mask, 0, n, st);
+		if (e == cudaSuccess && mask) e = cudaMemcpy2DAsync(d_mask, ew, mask, w, w, h, cudaMemcpyHostToDevice, st);
+	}
+	else {
+		e = cudaMemcpyAsync(d_src, src, sizeof(double) * n, cudaMemcpyHostToDevice, st);
+		if (e == cudaSuccess && mask) e = cudaMemcpyAsync(d_mask, mask, n, cudaMemcpyHostToDevice, st);
+	}
+	if (e == cudaSuccess) e = cudaMemcpyAsync(d_krn, krn, sizeof(double) * kn, cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) {
+		pf::launch_convolve64(d_src, ew, eh, d_krn, kw, kh, d_mask, d_out, env->n_sm, st);
+		e = cudaGetLastError();
+	}
+	// cropped back to the original size (result.crop(dims - diff), top-left aligned)
+	if (e == cudaSuccess) {
+		e = extended ? cudaMemcpy2DAsync(out, row, d_out, erow, row, h, cudaMemcpyDeviceToHost, st)
+		             : cudaMemcpyAsync(out, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
+	}
+	const cudaError_t sync = cudaStreamSynchronize(st);  // also on failure: nothing left in flight on the scratch
+	if (e == cudaSuccess) e = sync;
+	if (e != cudaSuccess) return fail(PF_ERR_CUDA, std::string("pf_convolve_noalloc: ") + cudaGetErrorString(e));
+	return PF_OK;
 }
 
 }  // extern "C"
