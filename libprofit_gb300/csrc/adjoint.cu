@@ -14,8 +14,8 @@
 //      S_theta = sum g sum_leaves w f d ln f / d theta, the subsampling tree
 //      recomputed exactly as the forward pass builds it and held fixed;
 //   3. d L / d theta = flux_scale (S_theta + d ln flux_scale / d theta * S_v).
-// Per-item partial sums are written in FP64 and reduced in a fixed order, so
-// gradients and chi^2 are deterministic.
+// Per (profile, row) partial sums are written in FP64 and reduced in a fixed
+// order, so gradients and chi^2 are deterministic.
 //
 // Profiles supported by the adjoint: sersic (all eight parameters xcen, ycen,
 // mag, ang, axrat, box, re, nser; not rescale_flux) and sky (bg).
@@ -30,8 +30,15 @@ namespace pf {
 
 namespace {
 
-constexpr int kBandRows = 16;    // drawing rows per backward work item
-constexpr int kWarpsB = 8;
+// Warps per block and blocks per SM of the backward pass's register budget
+// (4 and 3: up to 170 registers, 12 warps per SM).
+#ifndef PF_BACKWARD_WARPS
+#define PF_BACKWARD_WARPS 4
+#endif
+#ifndef PF_BACKWARD_MIN_BLOCKS
+#define PF_BACKWARD_MIN_BLOCKS 3
+#endif
+constexpr int kWarpsB = PF_BACKWARD_WARPS;
 // the forward pass's guard bands (eval_f32.cu), so that both take the same decisions
 constexpr float kGuardAccB = 1.2e-5f;
 constexpr float kGuardRadiusB = 2e-6f;
@@ -135,6 +142,63 @@ __device__ __forceinline__ void sersic_grad(const ProfileDev &P, T xp, T yp, T w
 
 // ------------------------------------------------------------- backward eval
 
+// FP32 sersic value and f * (1, d ln f / d theta) at profile coordinates
+// (xp, yp), into t[]: the quantities of sersic_grad<float>, from one chain of
+// base-2 logarithms and powers (special-function unit) shared by the value and
+// every derivative. Returns f.
+__device__ __forceinline__ float sersic_terms_f(const f32::Shape &P, float xp, float yp, float *t)
+{
+	constexpr float kLn2 = 0.6931471805599453f;
+	constexpr float kDeg = 0.017453292519943295f;
+	const float *c = P.c;
+	const float inv_re = c[FP_S_INV_RE];
+	const float ux = fabsf(xp) * inv_re, uy = fabsf(yp) * inv_re;
+	const float lx = f32::lg2(ux), ly = f32::lg2(uy);  // -inf at 0
+	float axm, aym;                                     // u^(B - 1)
+	if (!P.boxy) {
+		axm = ux;
+		aym = uy;
+	}
+	else {
+		const float bm1 = c[FP_B] - 1.f;
+		axm = f32::ex2(bm1 * lx);
+		aym = f32::ex2(bm1 * ly);
+	}
+	const float ax = axm * ux, ay = aym * uy;          // u^B
+	const float base = ax + ay;
+	const float lb = f32::lg2(base);
+	const float inv_nb = c[FP_S_INV_NB];
+	const float rf = f32::ex2(lb * inv_nb);             // base^(1 / (n B))
+	const float K = c[FP_S_K];
+	const float f = f32::ex2(K - K * rf);              // exp(-bn (rf - 1))
+	t[G_V] = f;
+	if (!(base > 0.f)) {  // the exact centre: rf = 0
+#pragma unroll
+		for (int k = 1; k < kGradSlots; k++) t[k] = 0.f;
+		t[G_X1] = f * P.dbn;
+		return f;
+	}
+	const float inv_n = 2.f * c[FP_S_HALF_INV_N];
+	const float A = -P.bn * rf;
+	const float inv_base = __fdividef(1.f, base);
+	const float anb = A * inv_n * inv_base;
+	const float dx = anb * copysignf(axm * inv_re, xp);  // A ax / (n xp base)
+	const float dy = anb * copysignf(aym * inv_re, yp);
+	const float lbase = lb * kLn2;
+	const float xl = ax > 0.f ? ax * lx * kLn2 : 0.f, yl = ay > 0.f ? ay * ly * kLn2 : 0.f;
+	const float db = A * inv_nb * ((xl + yl) * inv_base - lbase * c[FP_INVB]);
+	const float cs = P.cs, sn = P.sn, iq = P.iq;
+	const float q = __fdividef(1.f, iq);
+	t[G_XCEN] = f * (-cs * dx + (sn * iq) * dy);
+	t[G_YCEN] = f * (-sn * dx - (cs * iq) * dy);
+	t[G_ANG] = f * kDeg * (q * yp * dx - (xp * iq) * dy);
+	t[G_AXRAT] = f * (-(yp * iq) * dy);
+	t[G_BOX] = f * db;
+	t[G_X0] = f * (-A * inv_n * inv_re);
+	t[G_X1] = f * (A * (-lbase * inv_n * inv_nb) - P.dbn * (rf - 1.f));
+	return f;
+}
+
 // A sub-pixel box as in eval_f32.cu: its corner relative to the profile
 // centre as an unevaluated sum hi + lo in T (lo stays 0 in double), its size
 // and its eight running totals.
@@ -148,6 +212,7 @@ struct FrameG {
 template <typename T>
 struct WarpScratchG {
 	FrameG<T> fr[kMaxLevels];
+	unsigned int amb[kMaskWords];  // sub-points of the frame being evaluated whose decision is re-taken in FP64
 };
 
 template <typename T>
@@ -169,26 +234,46 @@ __device__ __forceinline__ void corner_pair_b(float i, float s_hi, float s_lo, f
 	lo = (e + ep) - c_lo;
 }
 
-template <typename T>
-__device__ __forceinline__ T value_at(const ProfileDev &P, T xp, T yp)
-{
-	if constexpr (std::is_same<T, double>::value) return f64::evaluate_at(P, xp, yp);
-	else return f32::evaluate_at(P, xp, yp);
-}
+// The FP32 path's rare FP64 re-takes. They take only single-precision and
+// integer arguments, so that no double-precision work is scheduled on the
+// common path. The one of the subsampling recursion is inlined (a call there
+// costs the whole kernel registers); the adjoint's profiles are sersics.
 
-__device__ __noinline__ bool test_f64b(const ProfileDev &P, double dx, double dy, double xbin, double ybin)
+// accuracy test of one sub-point, the point (xhi + xlo) + ox, (yhi + ylo) + oy
+__device__ __forceinline__ bool test_f64b(const ProfileDev &P, float xhi, float xlo, float yhi, float ylo, float ox,
+                                       float oy, float xbin, float ybin)
 {
+	const double dx = ((double)xhi + (double)xlo) + (double)ox;
+	const double dy = ((double)yhi + (double)ylo) + (double)oy;
 	const double xp = dx * P.cos_ang + dy * P.sin_ang;
 	const double yp = (-dx * P.sin_ang + dy * P.cos_ang) / P.par[PF_P_AXRAT];
-	const double sv = f64::evaluate_at(P, xp, yp);
-	const double dyp = (-xbin * P.sin_ang + ybin * P.cos_ang) / P.par[PF_P_AXRAT];
-	const double t = f64::evaluate_at(P, fabs(xp), fabs(yp) + fabs(dyp));
+	const double sv = f64::sersic(P, xp, yp);
+	const double dyp = (-(double)xbin * P.sin_ang + (double)ybin * P.cos_ang) / P.par[PF_P_AXRAT];
+	const double t = f64::sersic(P, fabs(xp), fabs(yp) + fabs(dyp));
 	return fabs(t / sv - 1.0) > P.acc;
 }
 
+// the reference's r_prof decisions for drawing pixel (px, row)
+// (src/radial.cpp:313-326): bit 0 beyond rscale_max, bit 1 beyond rscale_switch
+__device__ __noinline__ unsigned int radius_f64(const ProfileDev &P, const ModelDev &m, int px, int row)
+{
+	const double x = m.sx / 2. + px * m.sx, y = m.sy / 2. + row * m.sy;
+	double xp, yp;
+	f64::to_profile(P, x, y, xp, yp);
+	const double r = sqrt(xp * xp + yp * yp);
+	return (P.rscale_max > 0 && r / P.rscale > P.rscale_max ? 1u : 0u) | (r / P.rscale > P.rscale_switch ? 2u : 0u);
+}
+
+// the sersic central-pixel test (src/sersic.cpp:331-347)
+__device__ __noinline__ bool center_f64(const ProfileDev &P, const ModelDev &m, int px, int row)
+{
+	const double x = m.sx / 2. + px * m.sx, y = m.sy / 2. + row * m.sy;
+	return fabs(x - P.xc) < m.scale_x && fabs(y - P.yc) < m.scale_y;
+}
+
 template <typename T>
-__device__ void eval_frame_g(const ProfileDev &P, WarpScratchG<T> &ws, int L, unsigned int res, T inv_res,
-                             unsigned int max_rec, int lane)
+__device__ void eval_frame_g(const ProfileDev &P, const f32::Shape &sh, WarpScratchG<T> &ws, int L, unsigned int res,
+                             T inv_res, unsigned int max_rec, int lane)
 {
 	constexpr bool dbl = std::is_same<T, double>::value;
 	FrameG<T> &f = ws.fr[L];
@@ -196,39 +281,83 @@ __device__ void eval_frame_g(const ProfileDev &P, WarpScratchG<T> &ws, int L, un
 	const T txbin = f.bx * inv_res, tybin = f.by * inv_res;
 	const bool recurse = res > 1 && (unsigned int)L < max_rec;
 	const unsigned int n = res * res;
-	const T c = dbl ? (T)P.cos_ang : (T)P.fcos, s = dbl ? (T)P.sin_ang : (T)P.fsin;
-	const T iq = dbl ? (T)1 / (T)P.par[PF_P_AXRAT] : (T)P.finv_axrat;
-	const T acc_t = dbl ? (T)P.acc : (T)P.facc;
+	const T c = dbl ? (T)P.cos_ang : (T)sh.cs, s = dbl ? (T)P.sin_ang : (T)sh.sn;
+	const T iq = dbl ? (T)1 / (T)P.par[PF_P_AXRAT] : (T)sh.iq;
+	const T acc_t = dbl ? (T)P.acc : (T)sh.acc;
 	const T tdyp = fabs((-txbin * s + tybin * c) * iq);
+	const unsigned int magic = res_magic(res);
 	T part[kGradSlots];
 #pragma unroll
 	for (int k = 0; k < kGradSlots; k++) part[k] = 0;
+	unsigned int amb_any = 0;
 	for (unsigned int base = 0; base < n; base += 32) {
 		const unsigned int idx = base + lane;
-		bool fail = false;
+		bool fail = false, amb = false;
 		if (idx < n) {
-			const unsigned int i = div_res(idx, res_magic(res)), j = idx - i * res;
+			const unsigned int i = div_res(idx, magic), j = idx - i * res;
 			const T ox = ((T)small_int_to_float(i) + (T)0.5) * txbin, oy = ((T)small_int_to_float(j) + (T)0.5) * tybin;
 			const T dx = (xhi + ox) + xlo;
 			const T dy = (yhi + oy) + ylo;
 			const T xp = dx * c + dy * s;
 			const T yp = (dy * c - dx * s) * iq;
-			if (recurse) {
-				const T sv = value_at<T>(P, xp, yp);
-				const T t = value_at<T>(P, fabs(xp), fabs(yp) + tdyp);
-				const T d = fabs(t / sv - (T)1);
-				if (!dbl && (!(isfinite(d) && isfinite(sv)) || fabs(d - acc_t) <= (T)kGuardAccB * (acc_t + (T)1))) {
-					fail = test_f64b(P, ((double)xhi + (double)xlo) + (double)ox,
-					                 ((double)yhi + (double)ylo) + (double)oy, (double)txbin, (double)tybin);
+			if constexpr (dbl) {
+				if (recurse) {
+					const T sv = f64::evaluate_at(P, xp, yp);
+					const T t = f64::evaluate_at(P, fabs(xp), fabs(yp) + tdyp);
+					fail = fabs(t / sv - (T)1) > acc_t;
 				}
-				else {
-					fail = d > acc_t;
+				if (!fail) sersic_grad<T>(P, xp, yp, (T)1, part);
+			}
+			else {
+				float terms[kGradSlots];
+				const float sv = sersic_terms_f(sh, xp, yp, terms);
+				if (recurse) {
+					const float t = f32::value<f32::kSersicOnly>(sh, fabsf(xp), fabsf(yp) + tdyp);
+					const float d = fabsf(__fdividef(t, sv) - 1.f);
+					amb = !(isfinite(d) && isfinite(sv)) || fabsf(d - acc_t) <= kGuardAccB * (acc_t + 1.f);
+					fail = !amb && d > acc_t;
+				}
+				if (!fail && !amb) {
+#pragma unroll
+					for (int k = 0; k < kGradSlots; k++) part[k] += terms[k];
 				}
 			}
-			if (!fail) sersic_grad<T>(P, xp, yp, (T)1, part);
 		}
 		const unsigned int word = __ballot_sync(0xffffffffu, fail);
-		if (lane == 0) f.mask[base >> 5] = word;
+		const unsigned int aword = __ballot_sync(0xffffffffu, amb);
+		if (lane == 0) {
+			f.mask[base >> 5] = word;
+			ws.amb[base >> 5] = aword;
+		}
+		amb_any |= aword;
+	}
+	if constexpr (!dbl) {
+		if (amb_any) {
+			// the ambiguous sub-points, re-taken in FP64 (rare) from the exact
+			// corner, outside the loop above so that little state is live here
+			__syncwarp();
+			for (unsigned int base = 0; base < n; base += 32) {
+				const unsigned int aword = ws.amb[base >> 5];
+				if (!aword) continue;
+				bool fail = false;
+				if ((aword >> lane) & 1u) {
+					const unsigned int idx = base + lane;
+					const unsigned int i = div_res(idx, magic), j = idx - i * res;
+					const float ox = (small_int_to_float(i) + 0.5f) * txbin, oy = (small_int_to_float(j) + 0.5f) * tybin;
+					fail = test_f64b(P, xhi, xlo, yhi, ylo, ox, oy, txbin, tybin);
+					if (!fail) {
+						const float dx = (xhi + ox) + xlo;
+						const float dy = (yhi + oy) + ylo;
+						float terms[kGradSlots];
+						sersic_terms_f(sh, dx * c + dy * s, (dy * c - dx * s) * iq, terms);
+#pragma unroll
+						for (int k = 0; k < kGradSlots; k++) part[k] += terms[k];
+					}
+				}
+				const unsigned int word = __ballot_sync(0xffffffffu, fail);
+				if (lane == 0) f.mask[base >> 5] |= word;
+			}
+		}
 	}
 #pragma unroll
 	for (int k = 0; k < kGradSlots; k++) part[k] = warp_sum_t(part[k]);
@@ -239,8 +368,8 @@ __device__ void eval_frame_g(const ProfileDev &P, WarpScratchG<T> &ws, int L, un
 }
 
 template <typename T>
-__device__ void warp_subsample_g(const ProfileDev &P, WarpScratchG<T> &ws, T xhi, T xlo, T yhi, T ylo, T bx, T by,
-                                 unsigned int res, unsigned int max_rec, int lane, T *out)
+__device__ void warp_subsample_g(const ProfileDev &P, const f32::Shape &sh, WarpScratchG<T> &ws, T xhi, T xlo, T yhi,
+                                 T ylo, T bx, T by, unsigned int res, unsigned int max_rec, int lane, T *out)
 {
 	if (lane == 0) {
 		ws.fr[0].xhi = xhi;
@@ -254,7 +383,7 @@ __device__ void warp_subsample_g(const ProfileDev &P, WarpScratchG<T> &ws, T xhi
 	const T inv_res = (T)1 / (T)res;
 	const T inv_res2 = (T)1 / (T)(res * res);
 	int L = 0;
-	eval_frame_g<T>(P, ws, 0, res, inv_res, max_rec, lane);
+	eval_frame_g<T>(P, sh, ws, 0, res, inv_res, max_rec, lane);
 	const unsigned int nwords = (res * res + 31) / 32;
 	while (true) {
 		FrameG<T> &f = ws.fr[L];
@@ -283,7 +412,7 @@ __device__ void warp_subsample_g(const ProfileDev &P, WarpScratchG<T> &ws, T xhi
 			}
 			__syncwarp();
 			L++;
-			eval_frame_g<T>(P, ws, L, res, inv_res, max_rec, lane);
+			eval_frame_g<T>(P, sh, ws, L, res, inv_res, max_rec, lane);
 		}
 		else {
 			if (L == 0) {
@@ -299,208 +428,243 @@ __device__ void warp_subsample_g(const ProfileDev &P, WarpScratchG<T> &ws, T xhi
 	}
 }
 
-// One work item = one band of kBandRows drawing rows of one model. For each
-// profile of the model, the warps share the band's 32-pixel tiles, the
-// per-warp sums are reduced in a fixed order and written as FP64 partials.
+// Row items. Item k of the backward pass is row ring(k / n_profiles) of
+// profile k % n_profiles, ring(l) = centre row, centre row - 1, centre row + 1,
+// centre row - 2, ... of the profile's bounding box: every profile's central
+// rows (its subsampled pixels, the costly ones) come first, so that the
+// longest items start early and the tail of the pass is made of short ones.
+// Returns the drawing row of the item, or -1 if it has none.
+__device__ __forceinline__ int item_row(const ProfileDev &P, const ModelDev &m, int l)
+{
+	int lo, hi, centre;
+	if (P.kind == PF_SKY) {
+		lo = 0;
+		hi = (int)m.draw_h - 1;
+		centre = hi / 2;
+	}
+	else if (P.kind == PF_SERSIC) {
+		lo = max(0, P.bby0);
+		hi = min((int)m.draw_h - 1, P.bby1);
+		centre = (int)floorf(__fdividef(P.fyc_hi, m.fsy_hi));
+		centre = min(max(centre, lo), max(lo, hi));
+	}
+	else {
+		return -1;
+	}
+	const int half = (l + 1) >> 1;
+	const int row = (l & 1) ? centre - half : centre + half;
+	return row >= lo && row <= hi ? row : -1;
+}
+
+// One row of one profile: the cotangent-weighted value and shape derivatives
+// of the profile summed over the row's pixels, written as the FP64 partial of
+// (profile, row).
 template <typename T>
-__global__ void __launch_bounds__(kWarpsB * 32)
-backward_kernel(const ModelDev *__restrict__ models, int n_models, const ProfileDev *__restrict__ profs,
-                const T *__restrict__ gout, const T *__restrict__ gsrc, const long long *__restrict__ band_base,
-                const long long *__restrict__ part_base, long long n_items, double *__restrict__ partial)
+__device__ void backward_row(const ModelDev &m, const ProfileDev &P, int row, const T *__restrict__ gout,
+                             const T *__restrict__ gsrc, WarpScratchG<T> &ws, int lane, double *dst)
 {
 	constexpr bool dbl = std::is_same<T, double>::value;
-	__shared__ WarpScratchG<T> scratch[kWarpsB];
-	__shared__ double red[kWarpsB][kGradSlots];
-	__shared__ unsigned int tile_next;
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	WarpScratchG<T> &ws = scratch[warp];
-	for (long long item = blockIdx.x; item < n_items; item += gridDim.x) {
-		int lo = 0, hi = n_models - 1;
-		while (lo < hi) {
-			int mid = (lo + hi + 1) >> 1;
-			if (band_base[mid] <= item) lo = mid; else hi = mid - 1;
-		}
-		const ModelDev &m = models[lo];
-		const int band = (int)(item - band_base[lo]);
-		const int r0 = band * kBandRows, r1 = min(r0 + kBandRows, (int)m.draw_h);
-		const int tiles_per_row = (int)m.tiles_per_row;
-		for (int q = 0; q < m.n_profiles; q++) {
-			const ProfileDev &P = profs[m.first_profile + q];
-			double *dst = partial + part_base[lo] + ((long long)band * m.n_profiles + q) * kGradSlots;
-			const bool is_radial = P.kind == PF_SERSIC;
-			int br0 = r0, br1 = r1, bc0 = 0, bc1 = tiles_per_row;
-			if (is_radial) {
-				br0 = max(r0, P.bby0);
-				br1 = min(r1, P.bby1 + 1);
-				bc0 = max(0, P.bbx0 / 32);
-				bc1 = min(tiles_per_row, P.bbx1 / 32 + 1);
-			}
-			const bool work = (P.kind == PF_SKY || is_radial) && br0 < br1 && bc0 < bc1;
-			if (!work) {
-				if (threadIdx.x < kGradSlots) dst[threadIdx.x] = 0.;
-				continue;
-			}
-			if (threadIdx.x == 0) tile_next = 0;
-			__syncthreads();
-			const int ncols = bc1 - bc0;
-			const unsigned int n_tiles = (unsigned int)((br1 - br0) * ncols);
-			const T *gimg = P.convolve ? gsrc + m.draw_off : nullptr;
-			T acc[kGradSlots];
+	const bool is_sky = P.kind == PF_SKY;
+	const int tiles_per_row = (int)m.tiles_per_row;
+	int c0 = 0, c1 = tiles_per_row - 1;
+	if (!is_sky) {
+		c0 = max(0, P.bbx0) / 32;
+		c1 = min((int)m.draw_w - 1, P.bbx1) / 32;
+		if (P.bbx1 < 0) c1 = -1;
+	}
+	const T *gimg = P.convolve ? gsrc + m.draw_off : nullptr;
+	const f32::Shape sh = f32::load_shape(P);
+	T acc[kGradSlots];
 #pragma unroll
-			for (int k = 0; k < kGradSlots; k++) acc[k] = 0;
-			while (true) {
-				unsigned int t = 0;
-				if (lane == 0) t = atomicAdd(&tile_next, 1u);
-				t = __shfl_sync(0xffffffffu, t, 0);
-				if (t >= n_tiles) break;
-				const int trow = (int)(t / (unsigned int)ncols);
-				const int tcol = bc0 + (int)(t - (unsigned int)(trow * ncols));
-				const int row = br0 + trow;
-				const int px = tcol * 32 + lane;
-				const bool active = px < (int)m.draw_w;
-				T g = 0;
-				if (active) {
-					g = gimg ? gimg[(size_t)row * m.draw_w + px] : g_direct(m, gout, px, row);
-				}
-				if (P.kind == PF_SKY) {
-					acc[G_V] += g;
-					continue;
-				}
-				// the forward pass's decisions for this pixel (eval_f32.cu / eval_f64.cu)
-				T xp, yp;
-				float fdx = 0.f, fdy = 0.f;
-				bool beyond, outside;
-				if (dbl) {
-					const double x = m.sx / 2. + px * m.sx, y = m.sy / 2. + row * m.sy;
-					double xp64, yp64;
-					f64::to_profile(P, x, y, xp64, yp64);
-					xp = (T)xp64;
-					yp = (T)yp64;
-					const double r64 = sqrt(xp64 * xp64 + yp64 * yp64);
-					beyond = P.rscale_max > 0 && r64 / P.rscale > P.rscale_max;
-					outside = r64 / P.rscale > P.rscale_switch;
+	for (int k = 0; k < kGradSlots; k++) acc[k] = 0;
+	for (int tcol = c0; tcol <= c1; tcol++) {
+		const int px = tcol * 32 + lane;
+		const bool active = px < (int)m.draw_w;
+		T g = 0;
+		if (active) {
+			g = gimg ? gimg[(size_t)row * m.draw_w + px] : g_direct(m, gout, px, row);
+		}
+		if (is_sky) {
+			acc[G_V] += g;
+			continue;
+		}
+		// the forward pass's decisions for this pixel (eval_f32.cu / eval_f64.cu)
+		T xp, yp;
+		float fdx = 0.f, fdy = 0.f;
+		bool beyond, outside;
+		if constexpr (dbl) {
+			const double x = m.sx / 2. + px * m.sx, y = m.sy / 2. + row * m.sy;
+			double xp64, yp64;
+			f64::to_profile(P, x, y, xp64, yp64);
+			xp = (T)xp64;
+			yp = (T)yp64;
+			const double r64 = sqrt(xp64 * xp64 + yp64 * yp64);
+			beyond = P.rscale_max > 0 && r64 / P.rscale > P.rscale_max;
+			outside = r64 / P.rscale > P.rscale_switch;
+		}
+		else {
+			const float cx = small_int_to_float((unsigned int)px) + 0.5f;
+			const float cy = small_int_to_float((unsigned int)row) + 0.5f;
+			const float xh = cx * m.fsx_hi, yh = cy * m.fsy_hi;
+			const float xl = fmaf(cx, m.fsx_hi, -xh) + cx * m.fsx_lo;
+			const float yl = fmaf(cy, m.fsy_hi, -yh) + cy * m.fsy_lo;
+			const float dx = (xh - P.fxc_hi) + (xl - P.fxc_lo);
+			const float dy = (yh - P.fyc_hi) + (yl - P.fyc_lo);
+			fdx = dx;
+			fdy = dy;
+			xp = dx * sh.cs + dy * sh.sn;
+			yp = (dy * sh.cs - dx * sh.sn) * sh.iq;
+			const float rr = sqrtf(xp * xp + yp * yp) * P.finv_rscale;
+			beyond = P.frmax > 0.f && rr > P.frmax;
+			outside = rr > P.fswitch;
+			const bool amb = (P.frmax > 0.f && fabsf(rr - P.frmax) <= kGuardRadiusB * P.frmax) ||
+			                 fabsf(rr - P.fswitch) <= kGuardRadiusB * P.fswitch || !isfinite(rr);
+			if (amb && active) {
+				const unsigned int d = radius_f64(P, m, px, row);
+				beyond = (d & 1u) != 0;
+				outside = (d & 2u) != 0;
+			}
+		}
+		bool need_ss = false;
+		if (active && g != (T)0 && !beyond) {
+			if (P.rough || outside) {
+				if constexpr (dbl) {
+					T tmp[kGradSlots];
+#pragma unroll
+					for (int k = 0; k < kGradSlots; k++) tmp[k] = 0;
+					sersic_grad<T>(P, xp, yp, (T)1, tmp);
+#pragma unroll
+					for (int k = 0; k < kGradSlots; k++) acc[k] += g * tmp[k];
 				}
 				else {
-					const float cx = small_int_to_float(px) + 0.5f, cy = small_int_to_float(row) + 0.5f;
-					const float xh = cx * m.fsx_hi, yh = cy * m.fsy_hi;
-					const float xl = fmaf(cx, m.fsx_hi, -xh) + cx * m.fsx_lo;
-					const float yl = fmaf(cy, m.fsy_hi, -yh) + cy * m.fsy_lo;
-					const float dx = (xh - P.fxc_hi) + (xl - P.fxc_lo);
-					const float dy = (yh - P.fyc_hi) + (yl - P.fyc_lo);
-					fdx = dx;
-					fdy = dy;
-					xp = (T)(dx * P.fcos + dy * P.fsin);
-					yp = (T)((dy * P.fcos - dx * P.fsin) * P.finv_axrat);
-					const float rr = sqrtf((float)(xp * xp + yp * yp)) * P.finv_rscale;
-					beyond = P.frmax > 0.f && rr > P.frmax;
-					outside = rr > P.fswitch;
-					const bool amb = (P.frmax > 0.f && fabsf(rr - P.frmax) <= kGuardRadiusB * P.frmax) ||
-					                 fabsf(rr - P.fswitch) <= kGuardRadiusB * P.fswitch || !isfinite(rr);
-					if (amb && active) {
-						const double x = m.sx / 2. + px * m.sx, y = m.sy / 2. + row * m.sy;
-						double xp64, yp64;
-						f64::to_profile(P, x, y, xp64, yp64);
-						const double r64 = sqrt(xp64 * xp64 + yp64 * yp64);
-						beyond = P.rscale_max > 0 && r64 / P.rscale > P.rscale_max;
-						outside = r64 / P.rscale > P.rscale_switch;
-					}
-				}
-				bool need_ss = false;
-				if (active && g != (T)0 && !beyond) {
-					if (P.rough || outside) {
-						T tmp[kGradSlots];
+					float tmp[kGradSlots];
+					sersic_terms_f(sh, xp, yp, tmp);
 #pragma unroll
-						for (int k = 0; k < kGradSlots; k++) tmp[k] = 0;
-						sersic_grad<T>(P, xp, yp, (T)1, tmp);
-#pragma unroll
-						for (int k = 0; k < kGradSlots; k++) acc[k] += g * tmp[k];
-					}
-					else {
-						need_ss = true;
-					}
-				}
-				unsigned int pending = __ballot_sync(0xffffffffu, need_ss);
-				while (pending) {
-					const int src = __ffs(pending) - 1;
-					pending &= pending - 1;
-					const int spx = tcol * 32 + src;
-					const float sdx = __shfl_sync(0xffffffffu, fdx, src);
-					const float sdy = __shfl_sync(0xffffffffu, fdy, src);
-					unsigned int res = P.resolution, max_rec = P.max_recursions;
-					if (P.center_boost) {  // sersic central pixel (src/sersic.cpp:331-347)
-						bool center;
-						if (!dbl && fabsf(fabsf(sdx) - m.fscale_x) > 1e-5f * m.fscale_x &&
-						    fabsf(fabsf(sdy) - m.fscale_y) > 1e-5f * m.fscale_y) {
-							center = fabsf(sdx) < m.fscale_x && fabsf(sdy) < m.fscale_y;
-						}
-						else {
-							const double x = m.sx / 2. + spx * m.sx, y = m.sy / 2. + row * m.sy;
-							center = fabs(x - P.xc) < m.scale_x && fabs(y - P.yc) < m.scale_y;
-						}
-						if (center) {
-							res = 8;
-							max_rec = 10;
-						}
-					}
-					if (res > (unsigned int)kMaxRes) res = kMaxRes;
-					if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
-					T bxh, bxl, byh, byl;
-					if constexpr (dbl) {
-						bxh = (T)((double)spx * m.sx - P.xc);
-						byh = (T)((double)row * m.sy - P.yc);
-						bxl = byl = 0;
-					}
-					else {
-						corner_pair_b(small_int_to_float(spx), m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
-						corner_pair_b(small_int_to_float(row), m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
-					}
-					T sums[kGradSlots];
-					warp_subsample_g<T>(P, ws, bxh, bxl, byh, byl, dbl ? (T)m.sx : (T)m.fsx_hi,
-					                    dbl ? (T)m.sy : (T)m.fsy_hi, res, max_rec, lane, sums);
-					const T gs = __shfl_sync(0xffffffffu, g, src);
-					if (lane == 0) {
-#pragma unroll
-						for (int k = 0; k < kGradSlots; k++) acc[k] += gs * sums[k];
-					}
+					for (int k = 0; k < kGradSlots; k++) acc[k] += g * tmp[k];
 				}
 			}
+			else {
+				need_ss = true;
+			}
+		}
+		unsigned int pending = __ballot_sync(0xffffffffu, need_ss);
+		while (pending) {
+			const int src = __ffs(pending) - 1;
+			pending &= pending - 1;
+			const int spx = tcol * 32 + src;
+			const float sdx = __shfl_sync(0xffffffffu, fdx, src);
+			const float sdy = __shfl_sync(0xffffffffu, fdy, src);
+			unsigned int res = P.resolution, max_rec = P.max_recursions;
+			if (P.center_boost) {  // sersic central pixel (src/sersic.cpp:331-347)
+				bool center;
+				if (!dbl && fabsf(fabsf(sdx) - m.fscale_x) > 1e-5f * m.fscale_x &&
+				    fabsf(fabsf(sdy) - m.fscale_y) > 1e-5f * m.fscale_y) {
+					center = fabsf(sdx) < m.fscale_x && fabsf(sdy) < m.fscale_y;
+				}
+				else {
+					center = center_f64(P, m, spx, row);
+				}
+				if (center) {
+					res = 8;
+					max_rec = 10;
+				}
+			}
+			if (res > (unsigned int)kMaxRes) res = kMaxRes;
+			if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
+			T bxh, bxl, byh, byl;
+			if constexpr (dbl) {
+				bxh = (T)((double)spx * m.sx - P.xc);
+				byh = (T)((double)row * m.sy - P.yc);
+				bxl = byl = 0;
+			}
+			else {
+				corner_pair_b(small_int_to_float((unsigned int)spx), m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
+				corner_pair_b(small_int_to_float((unsigned int)row), m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
+			}
+			T sums[kGradSlots];
+			warp_subsample_g<T>(P, sh, ws, bxh, bxl, byh, byl, dbl ? (T)m.sx : (T)m.fsx_hi,
+			                    dbl ? (T)m.sy : (T)m.fsy_hi, res, max_rec, lane, sums);
+			const T gs = __shfl_sync(0xffffffffu, g, src);
+			if (lane == 0) {
 #pragma unroll
-			for (int k = 0; k < kGradSlots; k++) {
-				const double v = warp_sum_t((double)acc[k]);
-				if (lane == 0) red[warp][k] = v;
+				for (int k = 0; k < kGradSlots; k++) acc[k] += gs * sums[k];
 			}
-			__syncthreads();
-			if (threadIdx.x < kGradSlots) {
-				double s = 0;
-				for (int w = 0; w < kWarpsB; w++) s += red[w][threadIdx.x];
-				dst[threadIdx.x] = s;
-			}
-			__syncthreads();
+		}
+	}
+#pragma unroll
+	for (int k = 0; k < kGradSlots; k++) {
+		const double v = warp_sum_t((double)acc[k]);
+		if (lane == 0) dst[k] = v;
+	}
+}
+
+// Warps take chunks of 32 row items from a global counter; items without a
+// row cost one check.
+template <typename T>
+__global__ void __launch_bounds__(kWarpsB * 32, PF_BACKWARD_MIN_BLOCKS)
+backward_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restrict__ profs, unsigned int n_profiles,
+                const T *__restrict__ gout, const T *__restrict__ gsrc, const long long *__restrict__ prow_base,
+                unsigned int n_items, unsigned int *counter, double *__restrict__ partial)
+{
+	__shared__ WarpScratchG<T> scratch[kWarpsB];
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	WarpScratchG<T> &ws = scratch[warp];
+	while (true) {
+		unsigned int chunk = 0;
+		if (lane == 0) chunk = atomicAdd(counter, 32u);
+		chunk = __shfl_sync(0xffffffffu, chunk, 0);
+		if (chunk >= n_items) break;
+		const unsigned int k = chunk + (unsigned int)lane;
+		int p = 0, row = -1;
+		if (k < n_items) {
+			const unsigned int l = k / n_profiles;
+			p = (int)(k - l * n_profiles);
+			const ProfileDev &P = profs[p];
+			row = item_row(P, models[P.model], (int)l);
+		}
+		unsigned int todo = __ballot_sync(0xffffffffu, row >= 0);
+		while (todo) {
+			const int src = __ffs(todo) - 1;
+			todo &= todo - 1;
+			const int ip = __shfl_sync(0xffffffffu, p, src);
+			const int irow = __shfl_sync(0xffffffffu, row, src);
+			const ProfileDev &P = profs[ip];
+			backward_row<T>(models[P.model], P, irow, gout, gsrc, ws, lane,
+			                partial + (prow_base[ip] + irow) * (long long)kGradSlots);
 		}
 	}
 }
 
-// d L / d par for every profile: partials summed over the model's bands in
-// order, then scaled by the flux scale and its logarithmic derivatives.
+// d L / d par for every profile, one warp per profile: the (profile, row)
+// partials summed in a fixed order (lane l takes rows l, l + 32, ...; then a
+// fixed shuffle tree), then scaled by the flux scale and its logarithmic
+// derivatives.
 __global__ void grad_reduce_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restrict__ profs,
-                                   int n_profiles, const long long *__restrict__ part_base,
+                                   int n_profiles, const long long *__restrict__ prow_base,
                                    const double *__restrict__ partial, double *__restrict__ grad)
 {
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const int i = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+	const int lane = threadIdx.x & 31;
 	if (i >= n_profiles) return;
 	const ProfileDev &P = profs[i];
 	const ModelDev &m = models[P.model];
 	double *g = grad + (size_t)i * PF_NPAR;
-	for (int k = 0; k < PF_NPAR; k++) g[k] = 0.;
+	if (lane < PF_NPAR) g[lane] = 0.;
 	if (P.kind != PF_SERSIC && P.kind != PF_SKY) return;
-	const int q = i - m.first_profile;
-	const int n_bands = (m.draw_h + kBandRows - 1) / kBandRows;
+	int lo = 0, hi = (int)m.draw_h - 1;
+	if (P.kind == PF_SERSIC) {
+		lo = max(0, P.bby0);
+		hi = min(hi, P.bby1);
+	}
 	double S[kGradSlots];
 	for (int k = 0; k < kGradSlots; k++) S[k] = 0.;
-	for (int b = 0; b < n_bands; b++) {
-		const double *src = partial + part_base[P.model] + ((long long)b * m.n_profiles + q) * kGradSlots;
+	for (int r = lo + lane; r <= hi; r += 32) {
+		const double *src = partial + (prow_base[i] + r) * (long long)kGradSlots;
 		for (int k = 0; k < kGradSlots; k++) S[k] += src[k];
 	}
+	for (int k = 0; k < kGradSlots; k++) S[k] = warp_sum_t(S[k]);
+	__syncwarp();
+	if (lane != 0) return;
 	if (P.kind == PF_SKY) {
 		g[6] = S[G_V] / (m.fs * m.fs);  // d/d bg of bg / fs^2 on every pixel (src/sky.cpp:42-45)
 		return;
@@ -518,8 +682,6 @@ __global__ void grad_reduce_kernel(const ModelDev *__restrict__ models, const Pr
 
 }  // namespace
 
-int backward_band_rows() { return kBandRows; }
-
 template <typename T>
 void launch_chi2(const ModelDev *models, int n_models, const void *img, const void *data, const void *sigma,
                  const void *cot, void *gout, double *chi2, cudaStream_t stream)
@@ -530,27 +692,27 @@ void launch_chi2(const ModelDev *models, int n_models, const void *img, const vo
 
 
 template <typename T>
-void launch_backward(const ModelDev *models, int n_models, const ProfileDev *profs, int n_profiles, const void *gout,
-                     const void *gsrc, const long long *band_base, const long long *part_base, long long n_items,
+void launch_backward(const ModelDev *models, const ProfileDev *profs, int n_profiles, const void *gout,
+                     const void *gsrc, const long long *prow_base, unsigned int n_ring, unsigned int *counter,
                      double *partial, double *grad, int n_sm, cudaStream_t stream)
 {
-	int blocks = (int)(n_items < (long long)n_sm * 8 ? n_items : (long long)n_sm * 8);
-	if (blocks < 1) blocks = 1;
-	backward_kernel<T><<<blocks, kWarpsB * 32, 0, stream>>>(models, n_models, profs, (const T *)gout,
-	                                                        (const T *)gsrc, band_base, part_base, n_items, partial);
-	grad_reduce_kernel<<<(n_profiles + 127) / 128, 128, 0, stream>>>(models, profs, n_profiles, part_base, partial,
-	                                                                 grad);
+	if (n_profiles <= 0) return;
+	const unsigned int n_items = n_ring * (unsigned int)n_profiles;
+	backward_kernel<T><<<n_sm * PF_BACKWARD_MIN_BLOCKS, kWarpsB * 32, 0, stream>>>(models, profs, (unsigned int)n_profiles, (const T *)gout,
+	                                                          (const T *)gsrc, prow_base, n_items, counter, partial);
+	grad_reduce_kernel<<<(int)(((long long)n_profiles * 32 + 255) / 256), 256, 0, stream>>>(models, profs, n_profiles,
+	                                                                                       prow_base, partial, grad);
 }
 
 template void launch_chi2<float>(const ModelDev *, int, const void *, const void *, const void *, const void *, void *,
                                  double *, cudaStream_t);
 template void launch_chi2<double>(const ModelDev *, int, const void *, const void *, const void *, const void *,
                                   void *, double *, cudaStream_t);
-template void launch_backward<float>(const ModelDev *, int, const ProfileDev *, int, const void *, const void *,
-                                     const long long *, const long long *, long long, double *, double *, int,
+template void launch_backward<float>(const ModelDev *, const ProfileDev *, int, const void *, const void *,
+                                     const long long *, unsigned int, unsigned int *, double *, double *, int,
                                      cudaStream_t);
-template void launch_backward<double>(const ModelDev *, int, const ProfileDev *, int, const void *, const void *,
-                                      const long long *, const long long *, long long, double *, double *, int,
+template void launch_backward<double>(const ModelDev *, const ProfileDev *, int, const void *, const void *,
+                                      const long long *, unsigned int, unsigned int *, double *, double *, int,
                                       cudaStream_t);
 
 }  // namespace pf

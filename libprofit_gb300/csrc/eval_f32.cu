@@ -30,7 +30,18 @@ namespace pf {
 
 namespace {
 
-constexpr int kWarps32 = 8;
+// Warps per block and blocks per SM the register allocation is sized for: 4
+// and 4, 128 registers and 16 warps per SM (measured faster than 12 warps
+// with no spills at all).
+#ifndef PF_EVAL32_WARPS
+#define PF_EVAL32_WARPS 4
+#endif
+#ifndef PF_EVAL32_MIN_BLOCKS
+#define PF_EVAL32_MIN_BLOCKS 4
+#endif
+constexpr int kWarps32 = PF_EVAL32_WARPS;
+constexpr int kRingRows = 64;  // phase A: rows per profile, nearest its centre first
+constexpr int kRingCols = 4;   // phase A: tile columns per row (a 128-pixel window)
 // Half-width of the band around a threshold inside which an FP32 comparison is
 // re-taken in FP64. The FP32 profile values carry at most ~3e-6 relative
 // error (the exp2 argument K (1 - rf) reaches ~40, ~2.4e-6 of rounding, plus
@@ -71,6 +82,7 @@ __device__ __forceinline__ void corner_pair(float i, float s_hi, float s_lo, flo
 
 struct WarpScratchM {
 	FrameM fr[kMaxLevels];
+	unsigned int amb[kMaskWords];  // sub-points of the frame being evaluated whose decision is re-taken in FP64
 };
 
 __device__ __forceinline__ float warp_sum(float v)
@@ -80,34 +92,87 @@ __device__ __forceinline__ float warp_sum(float v)
 	return v;
 }
 
-// FP64 value and accuracy test of one sub-point (the rare re-taken decisions)
-__device__ __noinline__ bool test_f64(const ProfileDev &P, double dx, double dy, double xbin, double ybin, float &subval)
+// The rare FP64 re-takes. They take only single-precision and integer
+// arguments, so that no double-precision work is scheduled on the common
+// path; the two of the subsampling recursion are inlined (a call there costs
+// the whole kernel some 30 registers) and evaluate only the batch's kinds. A
+// point is given relative to the profile centre as (xa + xb) + xc,
+// (ya + yb) + yc, summed in FP64.
+
+// FP64 profile value for a kernel built for the kinds in KINDS
+template <unsigned int KINDS>
+__device__ __forceinline__ double value64(const ProfileDev &P, double x, double y)
 {
+	if constexpr (KINDS == f32::kSersicOnly) return f64::sersic(P, x, y);
+	else return f64::evaluate_at(P, x, y);
+}
+
+// value and accuracy test of one sub-point
+template <unsigned int KINDS>
+__device__ __forceinline__ bool test_f64(const ProfileDev &P, float xa, float xb, float xc, float ya, float yb,
+                                         float yc, float xbin, float ybin, float &subval)
+{
+	const double dx = ((double)xa + (double)xb) + (double)xc;
+	const double dy = ((double)ya + (double)yb) + (double)yc;
 	const double xp = dx * P.cos_ang + dy * P.sin_ang;
 	const double yp = (-dx * P.sin_ang + dy * P.cos_ang) / P.par[PF_P_AXRAT];
-	const double s = f64::evaluate_at(P, xp, yp);
-	const double dyp = (-xbin * P.sin_ang + ybin * P.cos_ang) / P.par[PF_P_AXRAT];
-	const double t = f64::evaluate_at(P, fabs(xp), fabs(yp) + fabs(dyp));
+	const double s = value64<KINDS>(P, xp, yp);
+	const double dyp = (-(double)xbin * P.sin_ang + (double)ybin * P.cos_ang) / P.par[PF_P_AXRAT];
+	const double t = value64<KINDS>(P, fabs(xp), fabs(yp) + fabs(dyp));
 	subval = (float)s;
 	return fabs(t / s - 1.0) > P.acc;
 }
 
-__device__ __noinline__ float value_f64(const ProfileDev &P, double dx, double dy)
+template <unsigned int KINDS>
+__device__ __forceinline__ float value_f64(const ProfileDev &P, float xa, float xb, float xc, float ya, float yb,
+                                           float yc)
 {
+	const double dx = ((double)xa + (double)xb) + (double)xc;
+	const double dy = ((double)ya + (double)yb) + (double)yc;
 	const double xp = dx * P.cos_ang + dy * P.sin_ang;
 	const double yp = (-dx * P.sin_ang + dy * P.cos_ang) / P.par[PF_P_AXRAT];
-	return (float)f64::evaluate_at(P, xp, yp);
+	return (float)value64<KINDS>(P, xp, yp);
 }
 
-__device__ void eval_frame_m(const ProfileDev &P, WarpScratchM &ws, int L, unsigned int res, float inv_res,
-                             unsigned int max_rec, int lane, unsigned long long *counts)
+// the reference's r_prof decisions for drawing pixel (px, row)
+// (src/radial.cpp:313-326): bit 0 beyond rscale_max, bit 1 beyond rscale_switch
+__device__ __noinline__ unsigned int radius_f64(const ProfileDev &P, const ModelDev &m, unsigned int px,
+                                                unsigned int row)
+{
+	const double x = m.sx / 2. + px * m.sx, y = m.sy / 2. + row * m.sy;
+	double xp, yp;
+	f64::to_profile(P, x, y, xp, yp);
+	const double r = sqrt(xp * xp + yp * yp);
+	return (P.rscale_max > 0 && r / P.rscale > P.rscale_max ? 1u : 0u) | (r / P.rscale > P.rscale_switch ? 2u : 0u);
+}
+
+// the sersic central-pixel test (src/sersic.cpp:331-347)
+__device__ __noinline__ bool center_f64(const ProfileDev &P, const ModelDev &m, unsigned int px, unsigned int row)
+{
+	const double x = m.sx / 2. + px * m.sx, y = m.sy / 2. + row * m.sy;
+	return fabs(x - P.xc) < m.scale_x && fabs(y - P.yc) < m.scale_y;
+}
+
+// the psf profile's stamp value at drawing pixel (px, row); false outside it
+__device__ __noinline__ bool psf_value(const ProfileDev &P, const ModelDev &m, const double *psf, unsigned int px,
+                                       unsigned int row, float &v)
+{
+	double d = 0;
+	const bool in = psf_pixel64(P, m, psf, px, row, d);
+	v = (float)d;
+	return in;
+}
+
+template <unsigned int KINDS>
+__device__ void eval_frame_m(const ProfileDev &P, const f32::Shape &sh, WarpScratchM &ws, int L, unsigned int res,
+                             float inv_res, unsigned int max_rec, int lane, unsigned long long *counts)
 {
 	FrameM &f = ws.fr[L];
 	const float xhi = f.xhi, xlo = f.xlo, yhi = f.yhi, ylo = f.ylo;
 	const float fxbin = f.bx * inv_res, fybin = f.by * inv_res;
 	const bool recurse = res > 1 && (unsigned int)L < max_rec;
 	const unsigned int n = res * res;
-	const float c = P.fcos, s = P.fsin, iq = P.finv_axrat;
+	const float c = sh.cs, s = sh.sn, iq = sh.iq, facc = sh.acc;
 	const float fdyp = fabsf((-fxbin * s + fybin * c) * iq);
 	if (counts && lane == 0 && L < kLevelCounts) {
 		atomicAdd(&counts[L], 1ull);
@@ -115,9 +180,10 @@ __device__ void eval_frame_m(const ProfileDev &P, WarpScratchM &ws, int L, unsig
 	}
 	float part = 0.f;
 	const unsigned int magic = res_magic(res);
+	unsigned int amb_any = 0;
 	for (unsigned int base = 0; base < n; base += 32) {
 		const unsigned int idx = base + lane;
-		bool fail = false;
+		bool fail = false, amb = false;
 		if (idx < n) {
 			const unsigned int i = div_res(idx, magic), j = idx - i * res;
 			const float ox = (small_int_to_float(i) + 0.5f) * fxbin, oy = (small_int_to_float(j) + 0.5f) * fybin;
@@ -125,26 +191,46 @@ __device__ void eval_frame_m(const ProfileDev &P, WarpScratchM &ws, int L, unsig
 			const float dy = (yhi + oy) + ylo;
 			const float xp = dx * c + dy * s;
 			const float yp = (dy * c - dx * s) * iq;
-			float sub = f32::evaluate_at(P, xp, yp);
+			const float sub = f32::value<KINDS>(sh, xp, yp);
 			if (recurse) {
-				const float t = f32::evaluate_at(P, fabsf(xp), fabsf(yp) + fdyp);
+				const float t = f32::value<KINDS>(sh, fabsf(xp), fabsf(yp) + fdyp);
 				const float d = fabsf(t / sub - 1.f);
-				if (!(isfinite(d) && isfinite(sub)) || fabsf(d - P.facc) <= kGuardAcc * (P.facc + 1.f)) {
-					// re-taken in FP64 (rare): the point from the exact corner
-					fail = test_f64(P, ((double)xhi + (double)xlo) + (double)ox, ((double)yhi + (double)ylo) + (double)oy,
-					                (double)fxbin, (double)fybin, sub);
-				}
-				else {
-					fail = d > P.facc;
-				}
+				amb = !(isfinite(d) && isfinite(sub)) || fabsf(d - facc) <= kGuardAcc * (facc + 1.f);
+				fail = !amb && d > facc;
 			}
-			else if (!isfinite(sub)) {
-				sub = value_f64(P, ((double)xhi + (double)xlo) + (double)ox, ((double)yhi + (double)ylo) + (double)oy);
+			else {
+				amb = !isfinite(sub);
 			}
-			if (!fail) part += sub;
+			if (!fail && !amb) part += sub;
 		}
 		const unsigned int word = __ballot_sync(0xffffffffu, fail);
-		if (lane == 0) f.mask[base >> 5] = word;
+		const unsigned int aword = __ballot_sync(0xffffffffu, amb);
+		if (lane == 0) {
+			f.mask[base >> 5] = word;
+			ws.amb[base >> 5] = aword;
+		}
+		amb_any |= aword;
+	}
+	if (amb_any) {
+		// the ambiguous sub-points, re-taken in FP64 (rare) from the exact
+		// corner, outside the loop above so that little state is live here
+		__syncwarp();
+		for (unsigned int base = 0; base < n; base += 32) {
+			const unsigned int aword = ws.amb[base >> 5];
+			if (!aword) continue;
+			bool fail = false;
+			if ((aword >> lane) & 1u) {
+				const unsigned int idx = base + lane;
+				const unsigned int i = div_res(idx, magic), j = idx - i * res;
+				const float ox = (small_int_to_float(i) + 0.5f) * fxbin, oy = (small_int_to_float(j) + 0.5f) * fybin;
+				float sub;
+				if (recurse) fail = test_f64<KINDS>(P, xhi, xlo, ox, yhi, ylo, oy, fxbin, fybin, sub);
+				else sub = value_f64<KINDS>(P, xhi, xlo, ox, yhi, ylo, oy);
+				if (!fail) part += sub;
+			}
+			const unsigned int word = __ballot_sync(0xffffffffu, fail);
+			if (lane == 0) f.mask[base >> 5] |= word;
+		}
 	}
 	part = warp_sum(part);
 	if (lane == 0) f.total = part;
@@ -152,9 +238,10 @@ __device__ void eval_frame_m(const ProfileDev &P, WarpScratchM &ws, int L, unsig
 }
 
 // subsample_pixel on a box given relative to the profile centre
-__device__ float warp_subsample_m(const ProfileDev &P, WarpScratchM &ws, float xhi, float xlo, float yhi, float ylo,
-                                  float bx, float by, unsigned int res, unsigned int max_rec, int lane,
-                                  unsigned long long *counts, int &deepest)
+template <unsigned int KINDS>
+__device__ float warp_subsample_m(const ProfileDev &P, const f32::Shape &sh, WarpScratchM &ws, float xhi, float xlo,
+                                  float yhi, float ylo, float bx, float by, unsigned int res, unsigned int max_rec,
+                                  int lane, unsigned long long *counts, int &deepest)
 {
 	if (lane == 0) {
 		ws.fr[0].xhi = xhi;
@@ -169,7 +256,7 @@ __device__ float warp_subsample_m(const ProfileDev &P, WarpScratchM &ws, float x
 	const float inv_res2 = __frcp_rn((float)(res * res));
 	int L = 0;
 	deepest = 1;
-	eval_frame_m(P, ws, 0, res, inv_res, max_rec, lane, counts);
+	eval_frame_m<KINDS>(P, sh, ws, 0, res, inv_res, max_rec, lane, counts);
 	const unsigned int nwords = (res * res + 31) / 32;
 	while (true) {
 		FrameM &f = ws.fr[L];
@@ -199,7 +286,7 @@ __device__ float warp_subsample_m(const ProfileDev &P, WarpScratchM &ws, float x
 			__syncwarp();
 			L++;
 			if (L + 1 > deepest) deepest = L + 1;
-			eval_frame_m(P, ws, L, res, inv_res, max_rec, lane, counts);
+			eval_frame_m<KINDS>(P, sh, ws, L, res, inv_res, max_rec, lane, counts);
 		}
 		else {
 			const float v = f.total * inv_res2;
@@ -213,140 +300,207 @@ __device__ float warp_subsample_m(const ProfileDev &P, WarpScratchM &ws, float x
 	}
 }
 
-__global__ void __launch_bounds__(kWarps32 * 32, 2)
+// One 32-pixel row tile of a model's drawing area: every profile of the model
+// in order, summed into the conv / direct images. KINDS: the radial profile
+// kinds of the batch.
+template <unsigned int KINDS>
+__device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, int n_models,
+                                          const ProfileDev *__restrict__ profs, const double *__restrict__ psf_pool,
+                                          float *__restrict__ conv_img, float *__restrict__ direct_img, long long tile,
+                                          WarpScratchM &ws, int lane, const DebugRec &dbg)
+{
+	const int mi = find_model(models, n_models, tile);
+	const ModelDev &m = models[mi];
+	const long long local = tile - m.tile_base;
+	const unsigned int row = (unsigned int)local / m.tiles_per_row;
+	const int col0 = (int)((unsigned int)local - row * m.tiles_per_row) * 32;
+	const int col1 = min(col0 + 31, (int)m.draw_w - 1);
+	const unsigned int px = (unsigned int)col0 + lane;
+	const bool active = px < m.draw_w;
+	const double *psf = m.psf_off >= 0 ? psf_pool + m.psf_off : nullptr;
+	// pixel centre (i + 1/2) * scale as an unevaluated float sum
+	const float cx = small_int_to_float(px) + 0.5f, cy = small_int_to_float(row) + 0.5f;
+	const float xh = cx * m.fsx_hi, yh = cy * m.fsy_hi;
+	const float xl = fmaf(cx, m.fsx_hi, -xh) + cx * m.fsx_lo;
+	const float yl = fmaf(cy, m.fsy_hi, -yh) + cy * m.fsy_lo;
+	float acc_conv = 0.f, acc_direct = 0.f;
+
+	for (int q = 0; q < m.n_profiles; q++) {
+		const int pi = m.first_profile + q;
+		const ProfileDev &P = profs[pi];
+		float add = 0.f;
+		bool has = false;
+		if (P.kind == PF_SKY) {
+			add = P.fbg;
+			has = active;
+		}
+		else if (P.kind == PF_PSF) {
+			if (active && psf) has = psf_value(P, m, psf, px, row, add);
+		}
+		else if (P.kind <= PF_BROKENEXP) {
+			if ((int)row < P.bby0 || (int)row > P.bby1 || col1 < P.bbx0 || col0 > P.bbx1) {
+				continue;
+			}
+			const f32::Shape sh = f32::load_shape(P);
+			const float dx = (xh - P.fxc_hi) + (xl - P.fxc_lo);
+			const float dy = (yh - P.fyc_hi) + (yl - P.fyc_lo);
+			const float xp = dx * sh.cs + dy * sh.sn;
+			const float yp = (dy * sh.cs - dx * sh.sn) * sh.iq;
+			const float rr = sqrtf(xp * xp + yp * yp) * P.finv_rscale;
+			bool beyond = P.frmax > 0.f && rr > P.frmax;
+			bool outside = rr > P.fswitch;
+			const bool amb = (P.frmax > 0.f && fabsf(rr - P.frmax) <= kGuardRadius * P.frmax) ||
+			                 fabsf(rr - P.fswitch) <= kGuardRadius * P.fswitch || !isfinite(rr);
+			if (amb && active) {
+				const unsigned int d = radius_f64(P, m, px, row);
+				beyond = (d & 1u) != 0;
+				outside = (d & 2u) != 0;
+			}
+			float pixel_val = 0.f;
+			int depth = 0;
+			bool need_ss = false;
+			if (beyond) {
+				depth = -1;
+			}
+			else if (P.rough || outside) {
+				pixel_val = f32::value<KINDS>(sh, xp, yp);
+				if (!isfinite(pixel_val)) pixel_val = value_f64<KINDS>(P, dx, 0.f, 0.f, dy, 0.f, 0.f);
+			}
+			else {
+				need_ss = true;
+			}
+			unsigned int pending = __ballot_sync(0xffffffffu, need_ss && active);
+			unsigned long long *counts = dbg.counts ? dbg.counts + (size_t)pi * kLevelCounts : nullptr;
+			if (counts) {
+				const unsigned int nd = __popc(__ballot_sync(0xffffffffu, active && !beyond && !need_ss));
+				if (lane == 0 && nd) atomicAdd(&counts[kCountDirectEvals], (unsigned long long)nd);
+			}
+			while (pending) {
+				const int src = __ffs(pending) - 1;
+				pending &= pending - 1;
+				const unsigned int spx = (unsigned int)col0 + src;
+				const float sdx = __shfl_sync(0xffffffffu, dx, src);
+				const float sdy = __shfl_sync(0xffffffffu, dy, src);
+				unsigned int res = P.resolution, max_rec = P.max_recursions;
+				if (P.center_boost) {  // src/sersic.cpp:331-347
+					bool center = fabsf(sdx) < m.fscale_x && fabsf(sdy) < m.fscale_y;
+					if (fabsf(fabsf(sdx) - m.fscale_x) <= 1e-5f * m.fscale_x ||
+					    fabsf(fabsf(sdy) - m.fscale_y) <= 1e-5f * m.fscale_y) {
+						center = center_f64(P, m, spx, row);
+					}
+					if (center) {
+						res = 8;
+						max_rec = 10;
+					}
+				}
+				if (res > (unsigned int)kMaxRes) res = kMaxRes;
+				if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
+				// pixel box corner (i * scale - centre) as an exact float pair
+				float bxh, bxl, byh, byl;
+				corner_pair(small_int_to_float(spx), m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
+				corner_pair(small_int_to_float(row), m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
+				int deepest = 0;
+				const float v = warp_subsample_m<KINDS>(P, sh, ws, bxh, bxl, byh, byl, m.fsx_hi, m.fsy_hi, res,
+				                                        max_rec, lane, counts, deepest);
+				if (lane == src) {
+					pixel_val = v;
+					depth = deepest;
+				}
+			}
+			if (dbg.depth && active) {
+				dbg.depth[P.depth_off + (size_t)row * m.draw_w + px] = (int8_t)depth;
+			}
+			add = P.fflux_scale * pixel_val;
+			has = active;
+		}
+		if (has) {
+			if (P.convolve) acc_conv += add;
+			else acc_direct += add;
+		}
+	}
+	if (active) {
+		const size_t idx = (size_t)m.draw_off + (size_t)row * m.draw_w + px;
+		if (m.conv_required) conv_img[idx] = acc_conv;
+		direct_img[idx] = acc_direct;
+	}
+}
+
+// Phase A item k (k < n_profiles * kRingRows * kRingCols): tile column
+// k % kRingCols of a window of the profile's subsampling box around its
+// centre, in the box's row ring(l), l = k /
+// (n_profiles * kRingCols) -- the centre row, the one above, the one below,
+// ... -- so that the rows nearest every profile's centre, where the
+// subsampling trees are deep, come first. Returns the global tile number, or
+// -1 if the item has none.
+__device__ __forceinline__ long long ring_tile(const ModelDev *__restrict__ models,
+                                               const ProfileDev *__restrict__ profs, unsigned int n_profiles,
+                                               unsigned int k)
+{
+	const unsigned int per_ring = n_profiles * kRingCols;
+	const unsigned int l = k / per_ring;
+	const unsigned int rem = k - l * per_ring;
+	const unsigned int p = rem / kRingCols;
+	const int c = (int)(rem - p * kRingCols);
+	const ProfileDev &P = profs[p];
+	if (P.sby1 < P.sby0 || P.sbx1 < P.sbx0) return -1;
+	const ModelDev &m = models[P.model];
+	int centre = (int)floorf(__fdividef(P.fyc_hi, m.fsy_hi));
+	centre = min(max(centre, P.sby0), P.sby1);
+	const int half = (int)((l + 1) >> 1);
+	const int row = (l & 1) ? centre - half : centre + half;
+	if (row < P.sby0 || row > P.sby1) return -1;
+	const int ctile = (int)floorf(__fdividef(P.fxc_hi, m.fsx_hi)) / 32;
+	const int tcol = max(P.sbx0 / 32, ctile - (kRingCols - 1) / 2) + c;
+	if (tcol > P.sbx1 / 32) return -1;
+	return m.tile_base + (long long)row * m.tiles_per_row + tcol;
+}
+
+// Work items: phase A (ring_tile, n_ring_items of them, a multiple of 32),
+// then phase B, every tile in order. Warps take 32 items at a time from a
+// global counter; a tile is evaluated by the item that first sets its bit in
+// `claims` (zeroed before the launch), so each tile exactly once.
+template <unsigned int KINDS>
+__global__ void __launch_bounds__(kWarps32 * 32, PF_EVAL32_MIN_BLOCKS)
 eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const ProfileDev *__restrict__ profs,
-                    const double *__restrict__ psf_pool, float *__restrict__ conv_img, float *__restrict__ direct_img,
-                    long long n_tiles, unsigned int *tile_counter, DebugRec dbg)
+                    unsigned int n_profiles, const double *__restrict__ psf_pool, float *__restrict__ conv_img,
+                    float *__restrict__ direct_img, unsigned int n_tiles, unsigned int n_ring_items,
+                    unsigned int *counter, unsigned int *claims, DebugRec dbg)
 {
 	__shared__ WarpScratchM scratch[kWarps32];
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	WarpScratchM &ws = scratch[warp];
+	const unsigned int n_items = n_ring_items + n_tiles;
 	while (true) {
-		unsigned int t = 0;
-		if (lane == 0) t = atomicAdd(tile_counter, 1u);
-		const long long tile = (long long)__shfl_sync(0xffffffffu, t, 0);
-		if (tile >= n_tiles) break;
-		const int mi = find_model(models, n_models, tile);
-		const ModelDev &m = models[mi];
-		const long long local = tile - m.tile_base;
-		const unsigned int row = (unsigned int)local / m.tiles_per_row;
-		const int col0 = (int)((unsigned int)local - row * m.tiles_per_row) * 32;
-		const int col1 = min(col0 + 31, (int)m.draw_w - 1);
-		const unsigned int px = (unsigned int)col0 + lane;
-		const bool active = px < m.draw_w;
-		const double *psf = m.psf_off >= 0 ? psf_pool + m.psf_off : nullptr;
-		// pixel centre (i + 1/2) * scale as an unevaluated float sum
-		const float cx = small_int_to_float(px) + 0.5f, cy = small_int_to_float(row) + 0.5f;
-		const float xh = cx * m.fsx_hi, yh = cy * m.fsy_hi;
-		const float xl = fmaf(cx, m.fsx_hi, -xh) + cx * m.fsx_lo;
-		const float yl = fmaf(cy, m.fsy_hi, -yh) + cy * m.fsy_lo;
-		float acc_conv = 0.f, acc_direct = 0.f;
-
-		for (int q = 0; q < m.n_profiles; q++) {
-			const int pi = m.first_profile + q;
-			const ProfileDev &P = profs[pi];
-			float add = 0.f;
-			bool has = false;
-			if (P.kind == PF_SKY) {
-				add = P.fbg;
-				has = active;
-			}
-			else if (P.kind == PF_PSF) {
-				double v = 0;
-				if (active && psf && psf_pixel64(P, m, psf, px, row, v)) {
-					add = (float)v;
-					has = true;
-				}
-			}
-			else if (P.kind <= PF_BROKENEXP) {
-				if ((int)row < P.bby0 || (int)row > P.bby1 || col1 < P.bbx0 || col0 > P.bbx1) {
-					continue;
-				}
-				const float dx = (xh - P.fxc_hi) + (xl - P.fxc_lo);
-				const float dy = (yh - P.fyc_hi) + (yl - P.fyc_lo);
-				const float xp = dx * P.fcos + dy * P.fsin;
-				const float yp = (dy * P.fcos - dx * P.fsin) * P.finv_axrat;
-				const float rr = sqrtf(xp * xp + yp * yp) * P.finv_rscale;
-				bool beyond = P.frmax > 0.f && rr > P.frmax;
-				bool outside = rr > P.fswitch;
-				const bool amb = (P.frmax > 0.f && fabsf(rr - P.frmax) <= kGuardRadius * P.frmax) ||
-				                 fabsf(rr - P.fswitch) <= kGuardRadius * P.fswitch || !isfinite(rr);
-				if (amb && active) {
-					// the reference's r_prof, in FP64 (src/radial.cpp:313-326)
-					const double x = m.sx / 2. + px * m.sx, y = m.sy / 2. + row * m.sy;
-					double xp64, yp64;
-					f64::to_profile(P, x, y, xp64, yp64);
-					const double r64 = sqrt(xp64 * xp64 + yp64 * yp64);
-					beyond = P.rscale_max > 0 && r64 / P.rscale > P.rscale_max;
-					outside = r64 / P.rscale > P.rscale_switch;
-				}
-				float pixel_val = 0.f;
-				int depth = 0;
-				bool need_ss = false;
-				if (beyond) {
-					depth = -1;
-				}
-				else if (P.rough || outside) {
-					pixel_val = f32::evaluate_at(P, xp, yp);
-					if (!isfinite(pixel_val)) pixel_val = value_f64(P, (double)dx, (double)dy);
-				}
-				else {
-					need_ss = true;
-				}
-				unsigned int pending = __ballot_sync(0xffffffffu, need_ss && active);
-				unsigned long long *counts = dbg.counts ? dbg.counts + (size_t)pi * kLevelCounts : nullptr;
-				if (counts) {
-					const unsigned int nd = __popc(__ballot_sync(0xffffffffu, active && !beyond && !need_ss));
-					if (lane == 0 && nd) atomicAdd(&counts[kCountDirectEvals], (unsigned long long)nd);
-				}
-				while (pending) {
-					const int src = __ffs(pending) - 1;
-					pending &= pending - 1;
-					const unsigned int spx = (unsigned int)col0 + src;
-					const float sdx = __shfl_sync(0xffffffffu, dx, src);
-					const float sdy = __shfl_sync(0xffffffffu, dy, src);
-					unsigned int res = P.resolution, max_rec = P.max_recursions;
-					if (P.center_boost) {  // src/sersic.cpp:331-347
-						bool center = fabsf(sdx) < m.fscale_x && fabsf(sdy) < m.fscale_y;
-						if (fabsf(fabsf(sdx) - m.fscale_x) <= 1e-5f * m.fscale_x ||
-						    fabsf(fabsf(sdy) - m.fscale_y) <= 1e-5f * m.fscale_y) {
-							const double x = m.sx / 2. + spx * m.sx, y = m.sy / 2. + row * m.sy;
-							center = fabs(x - P.xc) < m.scale_x && fabs(y - P.yc) < m.scale_y;
-						}
-						if (center) {
-							res = 8;
-							max_rec = 10;
-						}
-					}
-					if (res > (unsigned int)kMaxRes) res = kMaxRes;
-					if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
-					// pixel box corner (i * scale - centre) as an exact float pair
-					float bxh, bxl, byh, byl;
-					corner_pair(small_int_to_float(spx), m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
-					corner_pair(small_int_to_float(row), m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
-					int deepest = 0;
-					const float v = warp_subsample_m(P, ws, bxh, bxl, byh, byl, m.fsx_hi, m.fsy_hi, res, max_rec, lane,
-					                                 counts, deepest);
-					if (lane == src) {
-						pixel_val = v;
-						depth = deepest;
-					}
-				}
-				if (dbg.depth && active) {
-					dbg.depth[P.depth_off + (size_t)row * m.draw_w + px] = (int8_t)depth;
-				}
-				add = P.fflux_scale * pixel_val;
-				has = active;
-			}
-			if (has) {
-				if (P.convolve) acc_conv += add;
-				else acc_direct += add;
-			}
+		unsigned int chunk = 0;
+		if (lane == 0) chunk = atomicAdd(counter, 32u);
+		chunk = __shfl_sync(0xffffffffu, chunk, 0);
+		if (chunk >= n_items) break;
+		long long tile = -1;
+		unsigned int todo;
+		if (chunk >= n_ring_items) {
+			// phase B: 32 consecutive tiles, one claim word
+			const unsigned int t0 = chunk - n_ring_items;
+			const unsigned int left = n_tiles - t0;
+			const unsigned int valid = left >= 32 ? 0xffffffffu : (1u << left) - 1u;
+			unsigned int old = 0;
+			if (lane == 0) old = atomicOr(&claims[t0 >> 5], valid);
+			todo = valid & ~__shfl_sync(0xffffffffu, old, 0);
+			tile = (long long)t0 + lane;
 		}
-		if (active) {
-			const size_t idx = (size_t)m.draw_off + (size_t)row * m.draw_w + px;
-			if (m.conv_required) conv_img[idx] = acc_conv;
-			direct_img[idx] = acc_direct;
+		else {
+			tile = ring_tile(models, profs, n_profiles, chunk + (unsigned int)lane);
+			bool mine = false;
+			if (tile >= 0) {
+				const unsigned int bit = 1u << (tile & 31);
+				mine = (atomicOr(&claims[tile >> 5], bit) & bit) == 0;
+			}
+			todo = __ballot_sync(0xffffffffu, mine);
+		}
+		while (todo) {
+			const int src = __ffs(todo) - 1;
+			todo &= todo - 1;
+			const long long t = __shfl_sync(0xffffffffu, tile, src);
+			eval_tile<KINDS>(models, n_models, profs, psf_pool, conv_img, direct_img, t, ws, lane, dbg);
 		}
 	}
 }
@@ -359,15 +513,27 @@ __global__ void psf_to_float_kernel(const double *in, float *out, long long n)
 
 }  // namespace
 
-void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs, const double *psf_pool,
-                   float *conv_img, float *direct_img, long long n_tiles, unsigned int *tile_counter, DebugRec dbg,
-                   int n_sm, cudaStream_t stream)
+void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs, int n_profiles,
+                   const double *psf_pool, float *conv_img, float *direct_img, long long n_tiles,
+                   unsigned int *counter, unsigned int *claims, DebugRec dbg, bool sersic_only, int n_sm,
+                   cudaStream_t stream)
 {
-	int blocks = n_sm * 4;
-	long long need = (n_tiles + kWarps32 - 1) / kWarps32;
-	if (need < blocks) blocks = (int)(need > 0 ? need : 1);
-	eval_tiles32_kernel<<<blocks, kWarps32 * 32, 0, stream>>>(models, n_models, profs, psf_pool, conv_img, direct_img,
-	                                                          n_tiles, tile_counter, dbg);
+	const unsigned int n_ring = (unsigned int)n_profiles * kRingRows * kRingCols;
+	if (sersic_only) {
+		eval_tiles32_kernel<f32::kSersicOnly><<<n_sm * PF_EVAL32_MIN_BLOCKS, kWarps32 * 32, 0, stream>>>(
+		    models, n_models, profs, (unsigned int)n_profiles, psf_pool, conv_img, direct_img, (unsigned int)n_tiles,
+		    n_ring, counter, claims, dbg);
+	}
+	else {
+		eval_tiles32_kernel<f32::kAllKinds><<<n_sm * PF_EVAL32_MIN_BLOCKS, kWarps32 * 32, 0, stream>>>(
+		    models, n_models, profs, (unsigned int)n_profiles, psf_pool, conv_img, direct_img, (unsigned int)n_tiles,
+		    n_ring, counter, claims, dbg);
+	}
+}
+
+long long eval32_items(long long n_profiles, long long n_tiles)
+{
+	return n_profiles * kRingRows * kRingCols + n_tiles;
 }
 
 void launch_psf_to_float(const double *in, float *out, long long n, cudaStream_t stream)

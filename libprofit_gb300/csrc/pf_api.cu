@@ -34,9 +34,11 @@ void launch_convolve64(const double *src, unsigned int w, unsigned int h, const 
 void launch_flux_sum(const ModelDev *models, int n_models, const void *images, int is_double, double *flux,
                      cudaStream_t stream);
 void launch_set_params(ProfileDev *profs, int n_profiles, const double *params, cudaStream_t stream);
-void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs, const double *psf_pool,
-                   float *conv_img, float *direct_img, long long n_tiles, unsigned int *tile_counter, DebugRec dbg,
-                   int n_sm, cudaStream_t stream);
+void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs, int n_profiles,
+                   const double *psf_pool, float *conv_img, float *direct_img, long long n_tiles,
+                   unsigned int *counter, unsigned int *claims, DebugRec dbg, bool sersic_only, int n_sm,
+                   cudaStream_t stream);
+long long eval32_items(long long n_profiles, long long n_tiles);
 template <typename T>
 int conv_num_shapes();
 template <typename T>
@@ -51,7 +53,6 @@ template <typename T>
 void launch_conv(int mode, int shape, const ModelDev *models, int n_models, const T *psf, const T *in, const T *direct,
                  T *out, const long long *tile_base, long long n_tiles, size_t smem, int n_sm, cudaStream_t stream);
 void launch_psf_to_float(const double *in, float *out, long long n, cudaStream_t stream);
-int backward_band_rows();
 int fft_job_size();
 template <typename T>
 size_t fft_smem(int n, int count);
@@ -67,8 +68,8 @@ template <typename T>
 void launch_chi2(const ModelDev *models, int n_models, const void *img, const void *data, const void *sigma,
                  const void *cot, void *gout, double *chi2, cudaStream_t stream);
 template <typename T>
-void launch_backward(const ModelDev *models, int n_models, const ProfileDev *profs, int n_profiles, const void *gout,
-                     const void *gsrc, const long long *band_base, const long long *part_base, long long n_items,
+void launch_backward(const ModelDev *models, const ProfileDev *profs, int n_profiles, const void *gout,
+                     const void *gsrc, const long long *prow_base, unsigned int n_ring, unsigned int *counter,
                      double *partial, double *grad, int n_sm, cudaStream_t stream);
 }  // namespace pf
 
@@ -225,6 +226,8 @@ struct pf_batch {
 	void *d_direct = nullptr;
 	size_t draw_total = 0;
 	unsigned int *d_counter = nullptr;
+	unsigned int *d_claims = nullptr;   // FP32 eval: one bit per tile, set by the warp that evaluates it
+	bool sersic_only = false;           // every radial profile is a sersic: the FP32 kernels drop the other kinds
 	unsigned int *d_err = nullptr;
 	double *d_solves = nullptr;  // per profile: the inverse-gamma solves of the setup
 	long long n_tiles = 0;
@@ -254,11 +257,11 @@ struct pf_batch {
 	bool adjoint = false;
 	void *d_gout = nullptr;
 	void *d_gsrc = nullptr;
-	double *d_partial = nullptr;
-	long long *d_band_base = nullptr;
-	long long *d_part_base = nullptr;
+	double *d_partial = nullptr;        // kGradSlots FP64 per (profile, drawing row)
+	long long *d_prow_base = nullptr;   // first partial row of each profile
+	unsigned int *d_bwd_counter = nullptr;
+	unsigned int n_ring = 0;            // row items per profile: twice the tallest drawing area
 	long long *d_adj_tile_base = nullptr;
-	long long n_band_items = 0;
 	long long n_adj_tiles = 0;
 	size_t adj_smem = 0;
 	// stage timing (PF_ENV_PROFILE)
@@ -374,6 +377,7 @@ void pf_batch_destroy(pf_batch *b)
 	cudaFree(b->d_conv);
 	cudaFree(b->d_direct);
 	cudaFree(b->d_counter);
+	cudaFree(b->d_claims);
 	cudaFree(b->d_err);
 	cudaFree(b->d_solves);
 	cudaFree(b->d_depth);
@@ -387,8 +391,8 @@ void pf_batch_destroy(pf_batch *b)
 	cudaFree(b->d_gout);
 	cudaFree(b->d_gsrc);
 	cudaFree(b->d_partial);
-	cudaFree(b->d_band_base);
-	cudaFree(b->d_part_base);
+	cudaFree(b->d_prow_base);
+	cudaFree(b->d_bwd_counter);
 	cudaFree(b->d_adj_tile_base);
 	for (auto &p : b->ev_pool) {
 		cudaEventDestroy(p.a);
@@ -659,6 +663,17 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 	PF_CUDA_TRY(cudaMalloc(&b->d_models, sizeof(pf::ModelDev) * std::max<size_t>(1, n_models)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_profiles, sizeof(pf::ProfileDev) * std::max<size_t>(1, n_profiles)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_counter, sizeof(unsigned int)));
+	b->sersic_only = true;
+	for (size_t i = 0; i < n_profiles; i++) {
+		const int k = b->h_profiles[i].kind;
+		if (k <= PF_BROKENEXP && k != PF_SERSIC) b->sersic_only = false;
+	}
+	if (!b->dbl) {
+		if (pf::eval32_items((long long)n_profiles, b->n_tiles) >= (1ll << 31)) {
+			return fail(PF_ERR_UNSUPPORTED, "batch too large for one single-precision evaluation pass");
+		}
+		PF_CUDA_TRY(cudaMalloc(&b->d_claims, sizeof(unsigned int) * (size_t)std::max<long long>(1, (b->n_tiles + 31) / 32)));
+	}
 	PF_CUDA_TRY(cudaMalloc(&b->d_err, sizeof(unsigned int)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_solves, sizeof(double) * 3 * std::max<size_t>(1, n_profiles)));
 	PF_CUDA_TRY(cudaMemset(b->d_err, 0, sizeof(unsigned int)));
@@ -861,8 +876,11 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 	}
 	else {
 		t = stage_begin(b, ST_EVAL, stream);
-		pf::launch_eval32(b->d_models, n_models, b->d_profiles, b->d_psf_norm, (float *)b->d_conv,
-		                  (float *)b->d_direct, b->n_tiles, b->d_counter, dbg, b->env->n_sm, stream);
+		PF_CUDA_TRY(cudaMemsetAsync(b->d_claims, 0, sizeof(unsigned int) * (size_t)std::max<long long>(1, (b->n_tiles + 31) / 32),
+		                            stream));
+		pf::launch_eval32(b->d_models, n_models, b->d_profiles, n_profiles, b->d_psf_norm, (float *)b->d_conv,
+		                  (float *)b->d_direct, b->n_tiles, b->d_counter, b->d_claims, dbg, b->sersic_only,
+		                  b->env->n_sm, stream);
 		stage_end(b, t, stream);
 		t = stage_begin(b, ST_FINISH, stream);
 		if (b->any_downsample) {
@@ -936,11 +954,11 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	}
 	PF_CUDA_TRY(cudaSetDevice(b->env->device));
 	const size_t elem = b->dbl ? sizeof(double) : sizeof(float);
-	const int band_rows = pf::backward_band_rows();
 	const size_t n_models = b->mdev.size();
-	std::vector<long long> band_base(std::max<size_t>(1, n_models)), part_base(std::max<size_t>(1, n_models)),
-	    adj_tile_base(std::max<size_t>(1, n_models));
-	long long items = 0, parts = 0, tiles = 0;
+	std::vector<long long> adj_tile_base(std::max<size_t>(1, n_models));
+	std::vector<long long> prow_base(std::max<size_t>(1, b->profiles.size()), 0);
+	long long rows = 0, tiles = 0;
+	unsigned int max_h = 1;
 	unsigned int max_kw = 1, max_kh = 1;
 	std::vector<std::pair<unsigned int, unsigned int>> conv_dims;
 	for (const auto &m : b->mdev) {
@@ -949,12 +967,12 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	b->adj_shape = b->dbl ? best_conv_shape<double>(conv_dims) : best_conv_shape<float>(conv_dims);
 	for (size_t i = 0; i < n_models; i++) {
 		const pf::ModelDev &m = b->mdev[i];
-		const long long bands = (m.draw_h + band_rows - 1) / band_rows;
-		band_base[i] = items;
-		part_base[i] = parts;
+		for (int q = 0; q < m.n_profiles; q++) {
+			prow_base[m.first_profile + q] = rows;
+			rows += m.draw_h;
+		}
+		max_h = std::max(max_h, m.draw_h);
 		adj_tile_base[i] = tiles;
-		items += bands;
-		parts += bands * m.n_profiles * pf::kGradSlots;
 		if (m.conv_required) {
 			tiles += b->dbl ? pf::conv_tiles<double>(m.draw_w, m.draw_h, b->adj_shape)
 			                : pf::conv_tiles<float>(m.draw_w, m.draw_h, b->adj_shape);
@@ -962,19 +980,21 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 			max_kh = std::max(max_kh, m.psf_h);
 		}
 	}
-	b->n_band_items = items;
+	if ((unsigned long long)max_h * 2 * std::max<size_t>(1, b->profiles.size()) >= (1ull << 31)) {
+		return fail(PF_ERR_UNSUPPORTED, "too many profile rows for the adjoint's work counter");
+	}
+	b->n_ring = 2 * max_h;
 	b->n_adj_tiles = tiles;
 	b->adj_smem = b->dbl ? pf::conv_smem<double>(max_kw, max_kh, b->adj_shape)
 	                     : pf::conv_smem<float>(max_kw, max_kh, b->adj_shape);
 	if (b->adj_smem > 227 * 1024) return fail(PF_ERR_UNSUPPORTED, "PSF too large for the adjoint convolution");
 	PF_CUDA_TRY(cudaMalloc(&b->d_gout, elem * std::max<uint64_t>(1, b->total_out)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_gsrc, elem * std::max<size_t>(1, b->draw_total)));
-	PF_CUDA_TRY(cudaMalloc(&b->d_partial, sizeof(double) * std::max<long long>(1, parts)));
-	PF_CUDA_TRY(cudaMalloc(&b->d_band_base, sizeof(long long) * band_base.size()));
-	PF_CUDA_TRY(cudaMalloc(&b->d_part_base, sizeof(long long) * part_base.size()));
+	PF_CUDA_TRY(cudaMalloc(&b->d_partial, sizeof(double) * pf::kGradSlots * std::max<long long>(1, rows)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_prow_base, sizeof(long long) * prow_base.size()));
+	PF_CUDA_TRY(cudaMalloc(&b->d_bwd_counter, sizeof(unsigned int)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_adj_tile_base, sizeof(long long) * adj_tile_base.size()));
-	PF_CUDA_TRY(cudaMemcpy(b->d_band_base, band_base.data(), sizeof(long long) * band_base.size(), cudaMemcpyHostToDevice));
-	PF_CUDA_TRY(cudaMemcpy(b->d_part_base, part_base.data(), sizeof(long long) * part_base.size(), cudaMemcpyHostToDevice));
+	PF_CUDA_TRY(cudaMemcpy(b->d_prow_base, prow_base.data(), sizeof(long long) * prow_base.size(), cudaMemcpyHostToDevice));
 	PF_CUDA_TRY(cudaMemcpy(b->d_adj_tile_base, adj_tile_base.data(), sizeof(long long) * adj_tile_base.size(),
 	                       cudaMemcpyHostToDevice));
 	PF_CUDA_TRY(b->dbl ? pf::conv_configure<double>(b->adj_smem, b->adj_shape)
@@ -1017,12 +1037,12 @@ pf_status pf_backward(pf_batch *b, const void *images_dev, const void *data_dev,
 		stage_end(b, t, stream);
 	}
 	t = stage_begin(b, ST_BACKWARD, stream);
-	if (b->dbl) pf::launch_backward<double>(b->d_models, n_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc,
-	                                        b->d_band_base, b->d_part_base, b->n_band_items, b->d_partial, grad_dev,
+	PF_CUDA_TRY(cudaMemsetAsync(b->d_bwd_counter, 0, sizeof(unsigned int), stream));
+	if (b->dbl) pf::launch_backward<double>(b->d_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc,
+	                                        b->d_prow_base, b->n_ring, b->d_bwd_counter, b->d_partial, grad_dev,
 	                                        b->env->n_sm, stream);
-	else pf::launch_backward<float>(b->d_models, n_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc,
-	                                b->d_band_base, b->d_part_base, b->n_band_items, b->d_partial, grad_dev,
-	                                b->env->n_sm, stream);
+	else pf::launch_backward<float>(b->d_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc, b->d_prow_base,
+	                                b->n_ring, b->d_bwd_counter, b->d_partial, grad_dev, b->env->n_sm, stream);
 	stage_end(b, t, stream);
 	b->backward_calls++;
 	PF_CUDA_TRY(cudaGetLastError());

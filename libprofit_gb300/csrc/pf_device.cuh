@@ -82,6 +82,7 @@ struct ProfileDev {
 	double bg;                 // sky: bg / fs^2
 	double psf_mag_scale;      // psf: 10^(-0.4 (mag - magzero))
 	int32_t bbx0, bbx1, bby0, bby1;   // drawing pixels outside are exactly zero
+	int32_t sbx0, sbx1, sby0, sby1;   // drawing pixels outside are never subsampled (empty: x1 < x0)
 	int64_t depth_off;         // offset of this profile's depth map (debug recording)
 	// single-precision copies for the FP32 path (setup kernel)
 	float fxc_hi, fxc_lo, fyc_hi, fyc_lo;  // centre as an unevaluated float sum

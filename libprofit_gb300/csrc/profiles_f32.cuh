@@ -9,6 +9,11 @@
 // kernel into ProfileDev::fpar. Accuracy: a few 1e-7 relative in the bulk;
 // every decision that could flip because of it is re-taken in FP64 by the
 // caller (see eval_f32.cu).
+//
+// The kernels copy a profile's constants once into a Shape, held in
+// registers, and evaluate through value<KINDS>(), where KINDS is the set of
+// profile kinds the kernel is built for: a batch of sersic profiles only runs
+// code without the other five kinds' branches.
 #pragma once
 
 #include <cmath>
@@ -18,90 +23,155 @@
 namespace pf {
 namespace f32 {
 
+constexpr unsigned int kAllKinds = (1u << PF_SERSIC) | (1u << PF_CORESERSIC) | (1u << PF_MOFFAT) |
+                                   (1u << PF_FERRER) | (1u << PF_KING) | (1u << PF_BROKENEXP);
+constexpr unsigned int kSersicOnly = 1u << PF_SERSIC;
+
 __device__ __forceinline__ float ex2(float x) { return exp2f(x); }
 __device__ __forceinline__ float lg2(float x) { return __log2f(x); }
 
 // |x|^p for p > 0 (0 for x = 0)
 __device__ __forceinline__ float powabs(float x, float p) { return ex2(p * lg2(fabsf(x))); }
 
-// boxy radius: sqrt(x^2+y^2) or (|x|^B + |y|^B)^(1/B)
-__device__ __forceinline__ float boxy_r(const ProfileDev &p, float x, float y)
+// One profile's single-precision constants, copied once into registers.
+struct Shape {
+	int kind, boxy;
+	float c[12];           // ProfileDev::fpar, FP_* slots
+	float cs, sn, iq;      // cos, sin of the position angle + 90 deg; 1 / axrat
+	float acc;             // subsampling accuracy
+	float bn, dbn;         // sersic bn and d bn / d nser (adjoint)
+};
+
+__device__ __forceinline__ Shape load_shape(const ProfileDev &p)
 {
-	if (!p.fboxy) {
+	Shape s;
+	s.kind = p.kind;
+	s.boxy = p.fboxy;
+#pragma unroll
+	for (int i = 0; i < 12; i++) s.c[i] = p.fpar[i];
+	s.cs = p.fcos;
+	s.sn = p.fsin;
+	s.iq = p.finv_axrat;
+	s.acc = p.facc;
+	s.bn = p.fbn;
+	s.dbn = p.fdbn;
+	return s;
+}
+
+// boxy radius: sqrt(x^2+y^2) or (|x|^B + |y|^B)^(1/B)
+__device__ __forceinline__ float boxy_r(const Shape &s, float x, float y)
+{
+	if (!s.boxy) {
 		return sqrtf(x * x + y * y);
 	}
-	const float B = p.fpar[FP_B], invB = p.fpar[FP_INVB];
+	const float B = s.c[FP_B], invB = s.c[FP_INVB];
 	return ex2(invB * lg2(powabs(x, B) + powabs(y, B)));
+}
+
+__device__ __forceinline__ float sersic(const Shape &s, float x, float y)
+{
+	const float *c = s.c;
+	float base, e;
+	if (!s.boxy) {
+		base = (x * x + y * y) * c[FP_S_INV_RE2];  // (r/re)^2
+		e = c[FP_S_HALF_INV_N];                     // 1 / (2 n)
+	}
+	else {
+		base = powabs(x * c[FP_S_INV_RE], c[FP_B]) + powabs(y * c[FP_S_INV_RE], c[FP_B]);
+		e = c[FP_S_INV_NB];                          // 1 / (n B)
+	}
+	const float rf = ex2(e * lg2(base));
+	return ex2(c[FP_S_K] - c[FP_S_K] * rf);          // exp(-bn (rf - 1)), K = bn log2(e)
+}
+
+__device__ __forceinline__ float coresersic(const Shape &s, float x, float y)
+{
+	const float *c = s.c;
+	const float r = boxy_r(s, x, y);
+	const float a = c[FP_C_A];
+	const float core = ex2(c[FP_C_B_OVER_A] * lg2(1.f + ex2(-a * lg2(r * c[FP_C_INV_RB]))));
+	const float inner = (ex2(a * lg2(r)) + c[FP_C_RB_A]) * c[FP_C_INV_RE_A];
+	return core * ex2(-c[FP_C_K] * ex2(c[FP_C_INV_NA] * lg2(inner)));
+}
+
+__device__ __forceinline__ float moffat(const Shape &s, float x, float y)
+{
+	const float *c = s.c;
+	float r2;
+	if (!s.boxy) {
+		r2 = (x * x + y * y) * c[FP_M_INV_RS2];
+	}
+	else {
+		const float rf = boxy_r(s, x, y) * c[FP_M_INV_RS];
+		r2 = rf * rf;
+	}
+	return ex2(-c[FP_M_CON] * lg2(1.f + r2));
+}
+
+__device__ __forceinline__ float ferrer(const Shape &s, float x, float y)
+{
+	// (1 - rf^(2-b))^a with 1 - rf^(2-b) = -expm1((2-b) ln rf): no cancellation near rf = 1
+	const float *c = s.c;
+	const float rf = boxy_r(s, x, y) * c[FP_F_INV_ROUT];
+	if (rf < 1.f) {
+		return ex2(c[FP_F_A] * lg2(-expm1f(c[FP_F_2MB] * logf(rf))));
+	}
+	return 0.f;
+}
+
+__device__ __forceinline__ float king(const Shape &s, float x, float y)
+{
+	// u^(-1/a) - ut^(-1/a) = temp * expm1(ln(ut/u) / a), ln(ut/u) = log1p((rt^2 - r^2) / (rc^2 u)),
+	// with u = 1 + (r/rc)^2: accurate up to the truncation radius rt
+	const float *c = s.c;
+	const float r = boxy_r(s, x, y);
+	const float rt = c[FP_K_RT];
+	if (r < rt) {
+		const float q = r * c[FP_K_INV_RC];
+		const float u = 1.f + q * q;
+		const float w = (rt - r) * (rt + r) * (c[FP_K_INV_RC] * c[FP_K_INV_RC]) / u;
+		const float diff = c[FP_K_TEMP] * expm1f(c[FP_K_INV_A] * log1pf(w));
+		return ex2(c[FP_K_A] * lg2(diff));
+	}
+	return 0.f;
+}
+
+__device__ __forceinline__ float brokenexp(const Shape &s, float x, float y)
+{
+	const float *c = s.c;
+	const float r = boxy_r(s, x, y);
+	float base = r - c[FP_E_RB];
+	const float ab = c[FP_E_A] * base;
+	if (ab < 40.f) {
+		base = log1pf(__expf(ab)) * c[FP_E_INV_A];
+	}
+	return __expf(-r * c[FP_E_INV_H1] + c[FP_E_EXPO] * base);
+}
+
+// The profile value at profile coordinates (x, y), for a kernel built for the
+// profile kinds in KINDS.
+template <unsigned int KINDS>
+__device__ __forceinline__ float value(const Shape &s, float x, float y)
+{
+	if constexpr (KINDS == kSersicOnly) {
+		return sersic(s, x, y);
+	}
+	else {
+		switch (s.kind) {
+		case PF_SERSIC: return sersic(s, x, y);
+		case PF_CORESERSIC: return coresersic(s, x, y);
+		case PF_MOFFAT: return moffat(s, x, y);
+		case PF_FERRER: return ferrer(s, x, y);
+		case PF_KING: return king(s, x, y);
+		case PF_BROKENEXP: return brokenexp(s, x, y);
+		}
+		return 0.f;
+	}
 }
 
 __device__ __forceinline__ float evaluate_at(const ProfileDev &p, float x, float y)
 {
-	const float *c = p.fpar;
-	switch (p.kind) {
-	case PF_SERSIC: {
-		float base, e;
-		if (!p.fboxy) {
-			base = (x * x + y * y) * c[FP_S_INV_RE2];  // (r/re)^2
-			e = c[FP_S_HALF_INV_N];                     // 1 / (2 n)
-		}
-		else {
-			base = powabs(x * c[FP_S_INV_RE], c[FP_B]) + powabs(y * c[FP_S_INV_RE], c[FP_B]);
-			e = c[FP_S_INV_NB];                          // 1 / (n B)
-		}
-		const float rf = ex2(e * lg2(base));
-		return ex2(c[FP_S_K] - c[FP_S_K] * rf);          // exp(-bn (rf - 1)), K = bn log2(e)
-	}
-	case PF_CORESERSIC: {
-		const float r = boxy_r(p, x, y);
-		const float a = c[FP_C_A];
-		const float core = ex2(c[FP_C_B_OVER_A] * lg2(1.f + ex2(-a * lg2(r * c[FP_C_INV_RB]))));
-		const float inner = (ex2(a * lg2(r)) + c[FP_C_RB_A]) * c[FP_C_INV_RE_A];
-		return core * ex2(-c[FP_C_K] * ex2(c[FP_C_INV_NA] * lg2(inner)));
-	}
-	case PF_MOFFAT: {
-		float r2;
-		if (!p.fboxy) {
-			r2 = (x * x + y * y) * c[FP_M_INV_RS2];
-		}
-		else {
-			const float rf = boxy_r(p, x, y) * c[FP_M_INV_RS];
-			r2 = rf * rf;
-		}
-		return ex2(-c[FP_M_CON] * lg2(1.f + r2));
-	}
-	case PF_FERRER: {
-		// (1 - rf^(2-b))^a with 1 - rf^(2-b) = -expm1((2-b) ln rf): no cancellation near rf = 1
-		const float rf = boxy_r(p, x, y) * c[FP_F_INV_ROUT];
-		if (rf < 1.f) {
-			return ex2(c[FP_F_A] * lg2(-expm1f(c[FP_F_2MB] * logf(rf))));
-		}
-		return 0.f;
-	}
-	case PF_KING: {
-		// u^(-1/a) - ut^(-1/a) = temp * expm1(ln(ut/u) / a), ln(ut/u) = log1p((rt^2 - r^2) / (rc^2 u)),
-		// with u = 1 + (r/rc)^2: accurate up to the truncation radius rt
-		const float r = boxy_r(p, x, y);
-		const float rt = c[FP_K_RT];
-		if (r < rt) {
-			const float q = r * c[FP_K_INV_RC];
-			const float u = 1.f + q * q;
-			const float w = (rt - r) * (rt + r) * (c[FP_K_INV_RC] * c[FP_K_INV_RC]) / u;
-			const float diff = c[FP_K_TEMP] * expm1f(c[FP_K_INV_A] * log1pf(w));
-			return ex2(c[FP_K_A] * lg2(diff));
-		}
-		return 0.f;
-	}
-	case PF_BROKENEXP: {
-		const float r = boxy_r(p, x, y);
-		float base = r - c[FP_E_RB];
-		const float ab = c[FP_E_A] * base;
-		if (ab < 40.f) {
-			base = log1pf(__expf(ab)) * c[FP_E_INV_A];
-		}
-		return __expf(-r * c[FP_E_INV_H1] + c[FP_E_EXPO] * base);
-	}
-	}
-	return 0.f;
+	return value<kAllKinds>(load_shape(p), x, y);
 }
 
 }  // namespace f32

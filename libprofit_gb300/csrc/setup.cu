@@ -351,6 +351,24 @@ __device__ void radial_setup(ProfileDev &p, const ModelDev &m, double bn, const 
 			p.bby1 = clamp_index(ceil((p.yc + R) / m.sy - 0.5) + 1, -1, (int)m.draw_h - 1);
 		}
 	}
+	// Subsampling box: a pixel is subsampled only if r_prof <= rscale_switch *
+	// rscale (src/radial.cpp:327-331), so, as above, only within that distance
+	// of the centre. Used to schedule the costly tiles first.
+	p.sbx0 = p.sby0 = 0;
+	p.sbx1 = p.sby1 = -1;
+	if (p.kind <= PF_BROKENEXP && !p.rough) {
+		double R = p.rscale_switch * p.rscale;
+		if (R == R && R < 1e12) {
+			p.sbx0 = clamp_index(floor((p.xc - R) / m.sx - 0.5) - 1, 0, (int)m.draw_w);
+			p.sbx1 = clamp_index(ceil((p.xc + R) / m.sx - 0.5) + 1, -1, (int)m.draw_w - 1);
+			p.sby0 = clamp_index(floor((p.yc - R) / m.sy - 0.5) - 1, 0, (int)m.draw_h);
+			p.sby1 = clamp_index(ceil((p.yc + R) / m.sy - 0.5) + 1, -1, (int)m.draw_h - 1);
+		}
+		else {
+			p.sbx1 = (int)m.draw_w - 1;
+			p.sby1 = (int)m.draw_h - 1;
+		}
+	}
 	fold_single_precision(p);
 	adjoint_constants(p, sv.dbn);
 	p.center_boost = p.kind == PF_SERSIC && p.adjust && p.par[7] > 1;
