@@ -51,6 +51,34 @@ __device__ __forceinline__ T warp_sum_t(T v)
 	return v;
 }
 
+// Sums v[0..7] over the warp by a transposed butterfly: at each of the first
+// three steps a lane keeps half of its slots and receives its partner's other
+// half, so 8 slots cost 9 shuffles and 9 additions instead of 40 each. Returns,
+// in every lane, the total of slot (lane >> 2) & 7. The order of the
+// additions is fixed: the result is deterministic.
+template <typename T>
+__device__ __forceinline__ T warp_sum8(const T *v, int lane)
+{
+	const bool b4 = (lane & 16) != 0, b3 = (lane & 8) != 0, b2 = (lane & 4) != 0;
+	T w[4], u[2];
+#pragma unroll
+	for (int j = 0; j < 4; j++) {
+		const T send = b4 ? v[j] : v[j + 4];
+		const T keep = b4 ? v[j + 4] : v[j];
+		w[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+	}
+#pragma unroll
+	for (int j = 0; j < 2; j++) {
+		const T send = b3 ? w[j] : w[j + 2];
+		const T keep = b3 ? w[j + 2] : w[j];
+		u[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+	}
+	T t = (b2 ? u[1] : u[0]) + __shfl_xor_sync(0xffffffffu, b2 ? u[0] : u[1], 4);
+	t += __shfl_xor_sync(0xffffffffu, t, 2);
+	t += __shfl_xor_sync(0xffffffffu, t, 1);
+	return t;
+}
+
 // ------------------------------------------------------------ chi^2, g_out
 
 template <typename T>
@@ -359,11 +387,9 @@ __device__ void eval_frame_g(const ProfileDev &P, const f32::Shape &sh, WarpScra
 			}
 		}
 	}
-#pragma unroll
-	for (int k = 0; k < kGradSlots; k++) part[k] = warp_sum_t(part[k]);
-	if (lane == 0) {
-		for (int k = 0; k < kGradSlots; k++) f.tot[k] = part[k];
-	}
+	static_assert(kGradSlots == 8, "warp_sum8 reduces eight slots");
+	const T total = warp_sum8(part, lane);
+	if ((lane & 3) == 0) f.tot[lane >> 2] = total;
 	__syncwarp();
 }
 
@@ -456,28 +482,23 @@ __device__ __forceinline__ int item_row(const ProfileDev &P, const ModelDev &m, 
 	return row >= lo && row <= hi ? row : -1;
 }
 
-// One row of one profile: the cotangent-weighted value and shape derivatives
-// of the profile summed over the row's pixels, written as the FP64 partial of
-// (profile, row).
+// Tiles [c0, c1] of drawing row `row` of one profile, except tiles [s0, s1]:
+// the cotangent-weighted value and shape derivatives of the profile summed
+// over their pixels, written as one FP64 partial (eight slots) to dst.
 template <typename T>
-__device__ void backward_row(const ModelDev &m, const ProfileDev &P, int row, const T *__restrict__ gout,
-                             const T *__restrict__ gsrc, WarpScratchG<T> &ws, int lane, double *dst)
+__device__ void backward_row(const ModelDev &m, const ProfileDev &P, int row, int c0, int c1, int s0, int s1,
+                             const T *__restrict__ gout, const T *__restrict__ gsrc, WarpScratchG<T> &ws, int lane,
+                             double *dst)
 {
 	constexpr bool dbl = std::is_same<T, double>::value;
 	const bool is_sky = P.kind == PF_SKY;
-	const int tiles_per_row = (int)m.tiles_per_row;
-	int c0 = 0, c1 = tiles_per_row - 1;
-	if (!is_sky) {
-		c0 = max(0, P.bbx0) / 32;
-		c1 = min((int)m.draw_w - 1, P.bbx1) / 32;
-		if (P.bbx1 < 0) c1 = -1;
-	}
 	const T *gimg = P.convolve ? gsrc + m.draw_off : nullptr;
 	const f32::Shape sh = f32::load_shape(P);
 	T acc[kGradSlots];
 #pragma unroll
 	for (int k = 0; k < kGradSlots; k++) acc[k] = 0;
 	for (int tcol = c0; tcol <= c1; tcol++) {
+		if (tcol >= s0 && tcol <= s1) continue;
 		const int px = tcol * 32 + lane;
 		const bool active = px < (int)m.draw_w;
 		T g = 0;
@@ -591,34 +612,58 @@ __device__ void backward_row(const ModelDev &m, const ProfileDev &P, int row, co
 			}
 		}
 	}
+	double acc64[kGradSlots];
 #pragma unroll
-	for (int k = 0; k < kGradSlots; k++) {
-		const double v = warp_sum_t((double)acc[k]);
-		if (lane == 0) dst[k] = v;
-	}
+	for (int k = 0; k < kGradSlots; k++) acc64[k] = (double)acc[k];
+	const double total = warp_sum8(acc64, lane);
+	if ((lane & 3) == 0) dst[lane >> 2] = total;
 }
 
-// Warps take chunks of 32 row items from a global counter; items without a
-// row cost one check.
+// Work items, taken by warps 32 at a time from a global counter (items with
+// nothing to do cost one check):
+//   phase A, n_profiles * kRingRows * kRingCols items: profile p's ring tile
+//     (l, c) (pf_device.cuh), item k = (l * n_profiles + p) * kRingCols + c,
+//     each one tile with its own partial, so that the deepest subsampling
+//     trees -- the tiles nearest each profile's centre -- are spread over many
+//     warps and start first;
+//   phase B, n_profiles * n_ring items: profile p's drawing row ring(l) of its
+//     bounding box, item n_a + l * n_profiles + p, every tile of the row but
+//     its ring tiles, one partial per (profile, row).
 template <typename T>
 __global__ void __launch_bounds__(kWarpsB * 32, PF_BACKWARD_MIN_BLOCKS)
 backward_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restrict__ profs, unsigned int n_profiles,
                 const T *__restrict__ gout, const T *__restrict__ gsrc, const long long *__restrict__ prow_base,
-                unsigned int n_items, unsigned int *counter, double *__restrict__ partial)
+                unsigned int n_ring, unsigned int *counter, double *__restrict__ partial,
+                double *__restrict__ ring_partial)
 {
 	__shared__ WarpScratchG<T> scratch[kWarpsB];
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	WarpScratchG<T> &ws = scratch[warp];
+	const unsigned int n_a = n_profiles * (kRingRows * kRingCols);
+	const unsigned int n_items = n_a + n_ring * n_profiles;
 	while (true) {
 		unsigned int chunk = 0;
 		if (lane == 0) chunk = atomicAdd(counter, 32u);
 		chunk = __shfl_sync(0xffffffffu, chunk, 0);
 		if (chunk >= n_items) break;
 		const unsigned int k = chunk + (unsigned int)lane;
-		int p = 0, row = -1;
-		if (k < n_items) {
-			const unsigned int l = k / n_profiles;
-			p = (int)(k - l * n_profiles);
+		int p = 0, row = -1, tc = -1;
+		long long slot = 0;
+		if (k < n_a) {
+			const unsigned int per_ring = n_profiles * kRingCols;
+			const unsigned int l = k / per_ring;
+			const unsigned int rem = k - l * per_ring;
+			p = (int)(rem / kRingCols);
+			const int c = (int)(rem - (unsigned int)p * kRingCols);
+			const ProfileDev &P = profs[p];
+			if (P.kind == PF_SERSIC && !ring_tile_of(P, models[P.model], (int)l, c, row, tc)) row = -1;
+			if (P.kind != PF_SERSIC) row = -1;
+			slot = (((long long)p * kRingRows + l) * kRingCols + c) * kGradSlots;
+		}
+		else if (k < n_items) {
+			const unsigned int kb = k - n_a;
+			const unsigned int l = kb / n_profiles;
+			p = (int)(kb - l * n_profiles);
 			const ProfileDev &P = profs[p];
 			row = item_row(P, models[P.model], (int)l);
 		}
@@ -628,20 +673,35 @@ backward_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restric
 			todo &= todo - 1;
 			const int ip = __shfl_sync(0xffffffffu, p, src);
 			const int irow = __shfl_sync(0xffffffffu, row, src);
+			const int itc = __shfl_sync(0xffffffffu, tc, src);
+			const long long islot = __shfl_sync(0xffffffffu, slot, src);
 			const ProfileDev &P = profs[ip];
-			backward_row<T>(models[P.model], P, irow, gout, gsrc, ws, lane,
-			                partial + (prow_base[ip] + irow) * (long long)kGradSlots);
+			const ModelDev &m = models[P.model];
+			if (itc >= 0) {  // phase A: one ring tile
+				backward_row<T>(m, P, irow, itc, itc, 0, -1, gout, gsrc, ws, lane, ring_partial + islot);
+			}
+			else {           // phase B: the row but its ring tiles
+				int c0 = 0, c1 = (int)m.tiles_per_row - 1, s0 = 0, s1 = -1;
+				if (P.kind != PF_SKY) {
+					c0 = max(0, P.bbx0) / 32;
+					c1 = P.bbx1 < 0 ? -1 : min((int)m.draw_w - 1, P.bbx1) / 32;
+					ring_cols_of_row(P, m, irow, s0, s1);
+				}
+				backward_row<T>(m, P, irow, c0, c1, s0, s1, gout, gsrc, ws, lane,
+				                partial + (prow_base[ip] + irow) * (long long)kGradSlots);
+			}
 		}
 	}
 }
 
 // d L / d par for every profile, one warp per profile: the (profile, row)
-// partials summed in a fixed order (lane l takes rows l, l + 32, ...; then a
-// fixed shuffle tree), then scaled by the flux scale and its logarithmic
-// derivatives.
+// and ring-tile partials summed in a fixed order (lane l takes rows l, l + 32,
+// ... then ring slots l, l + 32, ...; then a fixed shuffle tree), then scaled
+// by the flux scale and its logarithmic derivatives.
 __global__ void grad_reduce_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restrict__ profs,
                                    int n_profiles, const long long *__restrict__ prow_base,
-                                   const double *__restrict__ partial, double *__restrict__ grad)
+                                   const double *__restrict__ partial, const double *__restrict__ ring_partial,
+                                   double *__restrict__ grad)
 {
 	const int i = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
 	const int lane = threadIdx.x & 31;
@@ -662,22 +722,32 @@ __global__ void grad_reduce_kernel(const ModelDev *__restrict__ models, const Pr
 		const double *src = partial + (prow_base[i] + r) * (long long)kGradSlots;
 		for (int k = 0; k < kGradSlots; k++) S[k] += src[k];
 	}
-	for (int k = 0; k < kGradSlots; k++) S[k] = warp_sum_t(S[k]);
-	__syncwarp();
+	if (P.kind == PF_SERSIC) {
+		for (int q = lane; q < kRingRows * kRingCols; q += 32) {
+			int row, tc;
+			if (!ring_tile_of(P, m, q / kRingCols, q % kRingCols, row, tc)) continue;
+			const double *src = ring_partial + ((long long)i * (kRingRows * kRingCols) + q) * kGradSlots;
+			for (int k = 0; k < kGradSlots; k++) S[k] += src[k];
+		}
+	}
+	const double total = warp_sum8(S, lane);
+	double T8[kGradSlots];
+#pragma unroll
+	for (int k = 0; k < kGradSlots; k++) T8[k] = __shfl_sync(0xffffffffu, total, 4 * k);
 	if (lane != 0) return;
 	if (P.kind == PF_SKY) {
-		g[6] = S[G_V] / (m.fs * m.fs);  // d/d bg of bg / fs^2 on every pixel (src/sky.cpp:42-45)
+		g[6] = T8[G_V] / (m.fs * m.fs);  // d/d bg of bg / fs^2 on every pixel (src/sky.cpp:42-45)
 		return;
 	}
 	const double fs_ = P.flux_scale;
-	g[PF_P_XCEN] = fs_ * S[G_XCEN];
-	g[PF_P_YCEN] = fs_ * S[G_YCEN];
-	g[PF_P_MAG] = fs_ * P.dlnfs[PF_P_MAG] * S[G_V];
-	g[PF_P_ANG] = fs_ * S[G_ANG];
-	g[PF_P_AXRAT] = fs_ * (S[G_AXRAT] + P.dlnfs[PF_P_AXRAT] * S[G_V]);
-	g[PF_P_BOX] = fs_ * (S[G_BOX] + P.dlnfs[PF_P_BOX] * S[G_V]);
-	g[6] = fs_ * (S[G_X0] + P.dlnfs[6] * S[G_V]);
-	g[7] = fs_ * (S[G_X1] + P.dlnfs[7] * S[G_V]);
+	g[PF_P_XCEN] = fs_ * T8[G_XCEN];
+	g[PF_P_YCEN] = fs_ * T8[G_YCEN];
+	g[PF_P_MAG] = fs_ * P.dlnfs[PF_P_MAG] * T8[G_V];
+	g[PF_P_ANG] = fs_ * T8[G_ANG];
+	g[PF_P_AXRAT] = fs_ * (T8[G_AXRAT] + P.dlnfs[PF_P_AXRAT] * T8[G_V]);
+	g[PF_P_BOX] = fs_ * (T8[G_BOX] + P.dlnfs[PF_P_BOX] * T8[G_V]);
+	g[6] = fs_ * (T8[G_X0] + P.dlnfs[6] * T8[G_V]);
+	g[7] = fs_ * (T8[G_X1] + P.dlnfs[7] * T8[G_V]);
 }
 
 }  // namespace
@@ -694,25 +764,32 @@ void launch_chi2(const ModelDev *models, int n_models, const void *img, const vo
 template <typename T>
 void launch_backward(const ModelDev *models, const ProfileDev *profs, int n_profiles, const void *gout,
                      const void *gsrc, const long long *prow_base, unsigned int n_ring, unsigned int *counter,
-                     double *partial, double *grad, int n_sm, cudaStream_t stream)
+                     double *partial, double *ring_partial, double *grad, int n_sm, cudaStream_t stream)
 {
 	if (n_profiles <= 0) return;
-	const unsigned int n_items = n_ring * (unsigned int)n_profiles;
-	backward_kernel<T><<<n_sm * PF_BACKWARD_MIN_BLOCKS, kWarpsB * 32, 0, stream>>>(models, profs, (unsigned int)n_profiles, (const T *)gout,
-	                                                          (const T *)gsrc, prow_base, n_items, counter, partial);
-	grad_reduce_kernel<<<(int)(((long long)n_profiles * 32 + 255) / 256), 256, 0, stream>>>(models, profs, n_profiles,
-	                                                                                       prow_base, partial, grad);
+	backward_kernel<T><<<n_sm * PF_BACKWARD_MIN_BLOCKS, kWarpsB * 32, 0, stream>>>(
+	    models, profs, (unsigned int)n_profiles, (const T *)gout, (const T *)gsrc, prow_base, n_ring, counter,
+	    partial, ring_partial);
+	grad_reduce_kernel<<<(int)(((long long)n_profiles * 32 + 255) / 256), 256, 0, stream>>>(
+	    models, profs, n_profiles, prow_base, partial, ring_partial, grad);
 }
+
+long long backward_items(long long n_profiles, long long n_ring)
+{
+	return n_profiles * (kRingRows * kRingCols) + n_profiles * n_ring;
+}
+
+long long backward_ring_slots() { return (long long)kRingRows * kRingCols * kGradSlots; }
 
 template void launch_chi2<float>(const ModelDev *, int, const void *, const void *, const void *, const void *, void *,
                                  double *, cudaStream_t);
 template void launch_chi2<double>(const ModelDev *, int, const void *, const void *, const void *, const void *,
                                   void *, double *, cudaStream_t);
 template void launch_backward<float>(const ModelDev *, const ProfileDev *, int, const void *, const void *,
-                                     const long long *, unsigned int, unsigned int *, double *, double *, int,
-                                     cudaStream_t);
+                                     const long long *, unsigned int, unsigned int *, double *, double *, double *,
+                                     int, cudaStream_t);
 template void launch_backward<double>(const ModelDev *, const ProfileDev *, int, const void *, const void *,
-                                      const long long *, unsigned int, unsigned int *, double *, double *, int,
-                                      cudaStream_t);
+                                      const long long *, unsigned int, unsigned int *, double *, double *, double *,
+                                      int, cudaStream_t);
 
 }  // namespace pf

@@ -40,8 +40,6 @@ namespace {
 #define PF_EVAL32_MIN_BLOCKS 4
 #endif
 constexpr int kWarps32 = PF_EVAL32_WARPS;
-constexpr int kRingRows = 64;  // phase A: rows per profile, nearest its centre first
-constexpr int kRingCols = 4;   // phase A: tile columns per row (a 128-pixel window)
 // Half-width of the band around a threshold inside which an FP32 comparison is
 // re-taken in FP64. The FP32 profile values carry at most ~3e-6 relative
 // error (the exp2 argument K (1 - rf) reaches ~40, ~2.4e-6 of rounding, plus
@@ -442,16 +440,9 @@ __device__ __forceinline__ long long ring_tile(const ModelDev *__restrict__ mode
 	const unsigned int p = rem / kRingCols;
 	const int c = (int)(rem - p * kRingCols);
 	const ProfileDev &P = profs[p];
-	if (P.sby1 < P.sby0 || P.sbx1 < P.sbx0) return -1;
 	const ModelDev &m = models[P.model];
-	int centre = (int)floorf(__fdividef(P.fyc_hi, m.fsy_hi));
-	centre = min(max(centre, P.sby0), P.sby1);
-	const int half = (int)((l + 1) >> 1);
-	const int row = (l & 1) ? centre - half : centre + half;
-	if (row < P.sby0 || row > P.sby1) return -1;
-	const int ctile = (int)floorf(__fdividef(P.fxc_hi, m.fsx_hi)) / 32;
-	const int tcol = max(P.sbx0 / 32, ctile - (kRingCols - 1) / 2) + c;
-	if (tcol > P.sbx1 / 32) return -1;
+	int row, tcol;
+	if (!ring_tile_of(P, m, (int)l, c, row, tcol)) return -1;
 	return m.tile_base + (long long)row * m.tiles_per_row + tcol;
 }
 

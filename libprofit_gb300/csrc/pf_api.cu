@@ -70,7 +70,9 @@ void launch_chi2(const ModelDev *models, int n_models, const void *img, const vo
 template <typename T>
 void launch_backward(const ModelDev *models, const ProfileDev *profs, int n_profiles, const void *gout,
                      const void *gsrc, const long long *prow_base, unsigned int n_ring, unsigned int *counter,
-                     double *partial, double *grad, int n_sm, cudaStream_t stream);
+                     double *partial, double *ring_partial, double *grad, int n_sm, cudaStream_t stream);
+long long backward_items(long long n_profiles, long long n_ring);
+long long backward_ring_slots();
 }  // namespace pf
 
 namespace {
@@ -258,6 +260,7 @@ struct pf_batch {
 	void *d_gout = nullptr;
 	void *d_gsrc = nullptr;
 	double *d_partial = nullptr;        // kGradSlots FP64 per (profile, drawing row)
+	double *d_ring_partial = nullptr;   // kGradSlots FP64 per (profile, ring tile)
 	long long *d_prow_base = nullptr;   // first partial row of each profile
 	unsigned int *d_bwd_counter = nullptr;
 	unsigned int n_ring = 0;            // row items per profile: twice the tallest drawing area
@@ -391,6 +394,7 @@ void pf_batch_destroy(pf_batch *b)
 	cudaFree(b->d_gout);
 	cudaFree(b->d_gsrc);
 	cudaFree(b->d_partial);
+	cudaFree(b->d_ring_partial);
 	cudaFree(b->d_prow_base);
 	cudaFree(b->d_bwd_counter);
 	cudaFree(b->d_adj_tile_base);
@@ -980,7 +984,7 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 			max_kh = std::max(max_kh, m.psf_h);
 		}
 	}
-	if ((unsigned long long)max_h * 2 * std::max<size_t>(1, b->profiles.size()) >= (1ull << 31)) {
+	if (pf::backward_items((long long)std::max<size_t>(1, b->profiles.size()), 2ll * max_h) >= (1ll << 31)) {
 		return fail(PF_ERR_UNSUPPORTED, "too many profile rows for the adjoint's work counter");
 	}
 	b->n_ring = 2 * max_h;
@@ -991,6 +995,8 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	PF_CUDA_TRY(cudaMalloc(&b->d_gout, elem * std::max<uint64_t>(1, b->total_out)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_gsrc, elem * std::max<size_t>(1, b->draw_total)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_partial, sizeof(double) * pf::kGradSlots * std::max<long long>(1, rows)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_ring_partial, sizeof(double) * pf::backward_ring_slots() *
+	                                               std::max<size_t>(1, b->profiles.size())));
 	PF_CUDA_TRY(cudaMalloc(&b->d_prow_base, sizeof(long long) * prow_base.size()));
 	PF_CUDA_TRY(cudaMalloc(&b->d_bwd_counter, sizeof(unsigned int)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_adj_tile_base, sizeof(long long) * adj_tile_base.size()));
@@ -1039,10 +1045,11 @@ pf_status pf_backward(pf_batch *b, const void *images_dev, const void *data_dev,
 	t = stage_begin(b, ST_BACKWARD, stream);
 	PF_CUDA_TRY(cudaMemsetAsync(b->d_bwd_counter, 0, sizeof(unsigned int), stream));
 	if (b->dbl) pf::launch_backward<double>(b->d_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc,
-	                                        b->d_prow_base, b->n_ring, b->d_bwd_counter, b->d_partial, grad_dev,
-	                                        b->env->n_sm, stream);
+	                                        b->d_prow_base, b->n_ring, b->d_bwd_counter, b->d_partial,
+	                                        b->d_ring_partial, grad_dev, b->env->n_sm, stream);
 	else pf::launch_backward<float>(b->d_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc, b->d_prow_base,
-	                                b->n_ring, b->d_bwd_counter, b->d_partial, grad_dev, b->env->n_sm, stream);
+	                                b->n_ring, b->d_bwd_counter, b->d_partial, b->d_ring_partial, grad_dev,
+	                                b->env->n_sm, stream);
 	stage_end(b, t, stream);
 	b->backward_calls++;
 	PF_CUDA_TRY(cudaGetLastError());

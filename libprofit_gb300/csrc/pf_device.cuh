@@ -132,6 +132,53 @@ __device__ __forceinline__ float small_int_to_float(unsigned int i)
 	return __int_as_float(0x4B000000 | (int)i) - 8388608.f;
 }
 
+// Costly tiles first (FP32 eval and backward). A profile's ring tiles lie in
+// its subsampling box: rows by distance from the row of its centre (ring
+// index l = 0: that row, 1: the row above, 2: the row below, ...; l <
+// kRingRows) and a window of kRingCols tile columns around the centre.
+constexpr int kRingRows = 64;
+constexpr int kRingCols = 4;
+
+__device__ __forceinline__ int ring_centre_row(const ProfileDev &P, const ModelDev &m)
+{
+	const int centre = (int)floorf(__fdividef(P.fyc_hi, m.fsy_hi));
+	return min(max(centre, P.sby0), P.sby1);
+}
+
+__device__ __forceinline__ int ring_first_col(const ProfileDev &P, const ModelDev &m)
+{
+	const int ctile = (int)floorf(__fdividef(P.fxc_hi, m.fsx_hi)) / 32;
+	return max(P.sbx0 / 32, ctile - (kRingCols - 1) / 2);
+}
+
+// The ring tile (l, c) of profile P: false if its box has none there.
+__device__ __forceinline__ bool ring_tile_of(const ProfileDev &P, const ModelDev &m, int l, int c, int &row,
+                                             int &tcol)
+{
+	if (P.sby1 < P.sby0 || P.sbx1 < P.sbx0) return false;
+	const int centre = ring_centre_row(P, m);
+	const int half = (l + 1) >> 1;
+	row = (l & 1) ? centre - half : centre + half;
+	if (row < P.sby0 || row > P.sby1) return false;
+	tcol = ring_first_col(P, m) + c;
+	return tcol <= P.sbx1 / 32;
+}
+
+// The tile columns [first, last] of drawing row `row` that are ring tiles of
+// P (last < first if none).
+__device__ __forceinline__ void ring_cols_of_row(const ProfileDev &P, const ModelDev &m, int row, int &first,
+                                                 int &last)
+{
+	first = 0;
+	last = -1;
+	if (P.sby1 < P.sby0 || P.sbx1 < P.sbx0 || row < P.sby0 || row > P.sby1) return;
+	const int centre = ring_centre_row(P, m);
+	const int l = row >= centre ? 2 * (row - centre) : 2 * (centre - row) - 1;
+	if (l >= kRingRows) return;
+	first = ring_first_col(P, m);
+	last = min(first + kRingCols - 1, P.sbx1 / 32);
+}
+
 __device__ __forceinline__ int find_model(const ModelDev *models, int n_models, long long tile)
 {
 	int lo = 0, hi = n_models - 1;
