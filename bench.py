@@ -41,6 +41,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--models", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--convolver", default="auto", choices=["auto", "brute", "fft"],
+                    help="convolution method of the FP32 batch (auto: the library's choice)")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="launch the step's kernels one by one instead of replaying its CUDA graph")
     return ap.parse_args()
 
 
@@ -233,7 +237,10 @@ def run_ours(args, world, rank, local):
     env32 = pg.get_cuda_environment(local, use_double=False, profile=True)
     specs, par, data_np, sigma_np = make_problem(args.models, rank, env64, torch)
     n_models = len(specs)
-    batch = pg.Batch([W.to_model(s, env32) for s in specs], env32)
+    models32 = [W.to_model(s, env32) for s in specs]
+    for m in models32:
+        m.set_convolver(args.convolver)
+    batch = pg.Batch(models32, env32)
     batch.enable_adjoint()
     n_prof = batch.n_profiles
     img = torch.zeros(batch.total_pixels, dtype=torch.float32, device="cuda")
@@ -246,8 +253,11 @@ def run_ours(args, world, rank, local):
     sh = stream.cuda_stream
 
     def step():
-        batch.set_params_dev(params, stream=sh)
-        batch.forward_backward(img, data, sigma, chi2, grad, stream=sh)
+        if args.no_graph:
+            batch.set_params_dev(params, stream=sh)
+            batch.forward_backward(img, data, sigma, chi2, grad, stream=sh)
+        else:  # pf_step_graph: the same nine kernels, one graph launch
+            batch.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -271,6 +281,16 @@ def run_ours(args, world, rank, local):
     clk = clocks.stop()
     batch.check(stream=sh)
     stages = batch.stats(reset=True)
+    launches = int(stages["kernel_launches"])  # this library's kernels in the timed region
+    if not args.no_graph:
+        # graph launches record no stage times: the breakdown comes from the
+        # same steps launched one by one (CUDA events around each stage)
+        with torch.cuda.stream(stream):
+            for _ in range(args.steps):
+                batch.set_params_dev(params, stream=sh)
+                batch.forward_backward(img, data, sigma, chi2, grad, stream=sh)
+        torch.cuda.synchronize()
+        stages = batch.stats(reset=True)
     ms = max_over_ranks(world, ms)
     ms_per_step = ms / args.steps
     value = world * n_models * args.steps / (ms / 1000.0)
@@ -377,9 +397,11 @@ def run_ours(args, world, rank, local):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "models/s", "h2d_bytes_per_step": int(par.size * 8),
                 "d2h_bytes_per_step": int(n_models * 8 + n_prof * 12 * 8)},
-        # per step: parameter scatter, setup (solves + constants), eval, convolution, chi2, adjoint
-        # convolution, backward, gradient reduce
-        "gpu_launches": int(args.steps * 9),
+        # counted by the library: per step the parameter scatter, setup (solves, constants),
+        # evaluation, convolution (direct and / or FFT passes), chi2, adjoint convolution,
+        # backward, gradient reduction
+        "gpu_launches": launches,
+        "graph": not args.no_graph,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)

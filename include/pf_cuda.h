@@ -132,6 +132,9 @@ typedef struct pf_batch pf_batch;
 #define PF_ENV_DOUBLE 0x1u   /* plain FP64 path: the reference's arithmetic and subsampling decisions */
 #define PF_ENV_PROFILE 0x2u  /* time every stage with CUDA events (the profiling OpenCL
                                 environment's OpenCL_times, include/profit/opencl.h:50-71) */
+#define PF_ENV_NO_AUTOTUNE 0x4u  /* single precision, PF_CONV_AUTO: choose brute force or FFT and
+                                    the direct block shape by the fixed cost model, never by
+                                    timing candidates on the device (reproducible choices) */
 
 /* Per-stage device times accumulated since the last reset (PF_ENV_PROFILE). */
 typedef struct pf_stage_times {
@@ -142,6 +145,7 @@ typedef struct pf_stage_times {
 	double adjoint_conv_ms;  /* transposed convolution */
 	double backward_ms;      /* adjoint evaluation and gradient reduction */
 	uint64_t forward_calls, backward_calls;
+	uint64_t kernel_launches;  /* this library's kernels launched (graph replays included) */
 } pf_stage_times;
 
 /* Last error message of the calling thread. */
@@ -264,6 +268,21 @@ PF_API pf_status pf_backward(pf_batch *batch, const void *images_dev, const void
 PF_API pf_status pf_forward_backward(pf_batch *batch, void *images_dev, const void *data_dev,
                                      const void *sigma_dev, double *chi2_dev, double *grad_dev,
                                      void *stream);
+
+/*
+ * One fitting step as a CUDA graph: pf_batch_set_params_dev(params_dev) (when
+ * params_dev is not NULL), pf_forward(images_dev), pf_backward(images_dev,
+ * data_dev, sigma_dev, chi2_dev, grad_dev) -- nine kernels -- captured into a
+ * graph on the first call and replayed by every later call with the same
+ * buffers, stream and depth recording: one launch per step. A call with other
+ * buffers or another stream captures anew. Parameters set on the host
+ * (pf_batch_set_params) are uploaded before the launch. The stream must be
+ * one the caller created (the default stream cannot be captured); stage
+ * times (PF_ENV_PROFILE) are not recorded for graph launches. No counterpart
+ * in the reference.
+ */
+PF_API pf_status pf_step_graph(pf_batch *batch, const double *params_dev, void *images_dev, const void *data_dev,
+                               const void *sigma_dev, double *chi2_dev, double *grad_dev, void *stream);
 
 /* Synchronises the batch's work and returns the stage times recorded so far
  * (all zero unless the environment has PF_ENV_PROFILE); `reset` clears them. */

@@ -210,12 +210,15 @@ class Profile:
 
 class CUDAEnv:
     """A CUDA environment (get_opencl_environment analogue). use_double selects
-    the plain FP64 path (the reference's arithmetic and subsampling decisions)."""
+    the plain FP64 path (the reference's arithmetic and subsampling decisions);
+    profile, per-stage CUDA-event timing; autotune=False, the fixed cost model
+    for the automatic convolution choice of large single-precision batches."""
 
-    def __init__(self, device=0, use_double=True, profile=False):
+    def __init__(self, device=0, use_double=True, profile=False, autotune=True):
         lib = _ffi.load()
         h = ctypes.c_void_p()
-        flags = (_ffi.PF_ENV_DOUBLE if use_double else 0) | (_ffi.PF_ENV_PROFILE if profile else 0)
+        flags = (_ffi.PF_ENV_DOUBLE if use_double else 0) | (_ffi.PF_ENV_PROFILE if profile else 0) | \
+            (0 if autotune else _ffi.PF_ENV_NO_AUTOTUNE)
         _check(lib.pf_env_create(int(device), flags, ctypes.byref(h)))
         self._h = h
         self.device = device
@@ -237,8 +240,8 @@ class CUDAEnv:
             pass
 
 
-def get_cuda_environment(device=0, use_double=True, profile=False):
-    return CUDAEnv(device, use_double, profile)
+def get_cuda_environment(device=0, use_double=True, profile=False, autotune=True):
+    return CUDAEnv(device, use_double, profile, autotune)
 
 
 _default_env = None
@@ -464,6 +467,13 @@ class Batch:
         """One model + VJP evaluation: render, then chi^2 and its gradient."""
         _check(_ffi.load().pf_forward_backward(self._h, _ptr(images), _ptr(data), _ptr(sigma), _ptr(chi2),
                                                _ptr(grad), _stream_arg(stream)))
+
+    def step_graph(self, params, images, data, sigma=None, chi2=None, grad=None, stream=None):
+        """set_params_dev(params) (if given) + forward_backward, captured once
+        into a CUDA graph and replayed (pf_step_graph); `stream` must be a
+        created stream (torch.cuda.Stream().cuda_stream)."""
+        _check(_ffi.load().pf_step_graph(self._h, _ptr(params), _ptr(images), _ptr(data), _ptr(sigma),
+                                         _ptr(chi2), _ptr(grad), _stream_arg(stream)))
 
     def record_depth(self, enable=True):
         _check(_ffi.load().pf_batch_record_depth(self._h, int(bool(enable))))

@@ -54,10 +54,11 @@ class StageTimes(ctypes.Structure):
     _fields_ = [("setup_ms", ctypes.c_double), ("eval_ms", ctypes.c_double), ("finish_ms", ctypes.c_double),
                 ("chi2_ms", ctypes.c_double), ("adjoint_conv_ms", ctypes.c_double),
                 ("backward_ms", ctypes.c_double), ("forward_calls", ctypes.c_uint64),
-                ("backward_calls", ctypes.c_uint64)]
+                ("backward_calls", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64)]
 
 
 PF_ENV_PROFILE = 0x2
+PF_ENV_NO_AUTOTUNE = 0x4
 
 _P = ctypes.c_void_p
 _SIGNATURES = {
@@ -86,6 +87,7 @@ _SIGNATURES = {
     "pf_batch_enable_adjoint": (ctypes.c_int, [_P]),
     "pf_backward": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "pf_forward_backward": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    "pf_step_graph": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "pf_batch_record_depth": (ctypes.c_int, [_P, ctypes.c_int]),
     "pf_batch_depth": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
 }

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <string>
@@ -39,6 +40,13 @@ void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs
                    unsigned int *counter, unsigned int *claims, DebugRec dbg, bool sersic_only, int n_sm,
                    cudaStream_t stream);
 long long eval32_items(long long n_profiles, long long n_tiles);
+int fft32_rows_per_job(int n);
+int fft32_cols_per_job(int n);
+cudaError_t fft32_configure();
+void launch_fft32_twiddles(void *tw, cudaStream_t stream);
+void launch_fft32(int pass, int mode, int n, const void *jobs, int n_jobs, const ModelDev *models, const float *src,
+                  const float *psf, void *work, void *spec, const float *direct, float *out, const void *tw,
+                  cudaStream_t stream);
 template <typename T>
 int conv_num_shapes();
 template <typename T>
@@ -255,6 +263,13 @@ struct pf_batch {
 	int fft_njobs[5] = {0, 0, 0, 0, 0};
 	size_t fft_smem_bytes = 0;
 	int64_t fft_work_elems = 0, fft_spec_elems = 0;
+	// single precision (fft32.cu): job lists per [mode: forward, adjoint,
+	// spectrum][pass: rows, columns, inverse rows], one per transform length
+	struct Fft32Jobs {
+		int n = 0, n_jobs = 0;
+		void *d_jobs = nullptr;
+	};
+	std::vector<Fft32Jobs> f32_jobs[3][3];
 	// adjoint
 	bool adjoint = false;
 	void *d_gout = nullptr;
@@ -267,6 +282,21 @@ struct pf_batch {
 	long long *d_adj_tile_base = nullptr;
 	long long n_adj_tiles = 0;
 	size_t adj_smem = 0;
+	// pf_step_graph: the captured step and the buffers, stream and recording
+	// state it was captured with
+	cudaGraphExec_t graph = nullptr;
+	struct GraphKey {
+		const void *params = nullptr, *images = nullptr, *data = nullptr, *sigma = nullptr;
+		const void *chi2 = nullptr, *grad = nullptr;
+		cudaStream_t stream = nullptr;
+		bool record = false;
+		bool operator==(const GraphKey &o) const
+		{
+			return params == o.params && images == o.images && data == o.data && sigma == o.sigma &&
+			       chi2 == o.chi2 && grad == o.grad && stream == o.stream && record == o.record;
+		}
+	} graph_key;
+	bool capturing = false;             // stage timing is off while a step is captured
 	// stage timing (PF_ENV_PROFILE)
 	struct EventPair {
 		cudaEvent_t a, b;
@@ -276,6 +306,7 @@ struct pf_batch {
 	size_t ev_used = 0;
 	double stage_ms[6] = {0, 0, 0, 0, 0, 0};
 	uint64_t forward_calls = 0, backward_calls = 0;
+	uint64_t kernel_launches = 0, graph_kernels = 0;
 };
 
 namespace {
@@ -297,7 +328,7 @@ void fold_stage_times(pf_batch *b)
 // Records the start of a stage on `s`; returns the slot to close, or -1.
 long stage_begin(pf_batch *b, int stage, cudaStream_t s)
 {
-	if (!(b->env->flags & PF_ENV_PROFILE)) return -1;
+	if (!(b->env->flags & PF_ENV_PROFILE) || b->capturing) return -1;
 	if (b->ev_used >= 4096) fold_stage_times(b);
 	if (b->ev_used == b->ev_pool.size()) {
 		pf_batch::EventPair p{};
@@ -373,6 +404,7 @@ void pf_batch_destroy(pf_batch *b)
 {
 	if (!b) return;
 	cudaSetDevice(b->env->device);
+	if (b->graph) cudaGraphExecDestroy(b->graph);
 	cudaFree(b->d_models);
 	cudaFree(b->d_profiles);
 	cudaFree(b->d_psf_raw);
@@ -391,6 +423,9 @@ void pf_batch_destroy(pf_batch *b)
 	cudaFree(b->d_fft_spec);
 	cudaFree(b->d_fft_tw);
 	for (void *p : b->d_fft_jobs) cudaFree(p);
+	for (auto &mode : b->f32_jobs)
+		for (auto &pass : mode)
+			for (auto &j : pass) cudaFree(j.d_jobs);
 	cudaFree(b->d_gout);
 	cudaFree(b->d_gsrc);
 	cudaFree(b->d_partial);
@@ -412,6 +447,13 @@ namespace {
 
 struct HostFftJob {
 	int model, first, count, pad;
+};
+
+// Choices made for a batch by the autotuner (pf_batch_create); defaults: the
+// fixed cost model.
+struct ConvPlan {
+	int shape = -1;                         // direct convolution block shape; -1: least tile area
+	const std::vector<int8_t> *auto_fft = nullptr;  // per model, PF_CONV_AUTO: 1 FFT, 0 direct
 };
 
 // The convolution block shape covering the given images with the least tile area.
@@ -449,7 +491,8 @@ unsigned int next_pow2(unsigned int v)
 // the cheaper of the two by a cost model of this GPU: direct = 2 P^2 flop per
 // output pixel at 35 TFLOP/s; FFT = its HBM bytes at 3 TB/s plus
 // 5 N log2 N flop per transform at 10 TFLOP/s.
-pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5])
+pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5], const double *psf_pool,
+                   std::map<int, std::vector<HostFftJob>> f32[3][3], const ConvPlan &plan)
 {
 	const int nmax = b->dbl ? 4096 : 8192;
 	const int per_block = b->dbl ? 4096 : 8192;  // complex elements of one ping-pong half in shared memory
@@ -472,6 +515,9 @@ pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5])
 			}
 			fft = true;
 		}
+		else if (d.convolver == PF_CONV_AUTO && !b->dbl && (int)mx <= nmax && (int)my <= nmax && plan.auto_fft) {
+			fft = (*plan.auto_fft)[i] != 0;
+		}
 		else if (d.convolver == PF_CONV_AUTO && !b->dbl && (int)mx <= nmax && (int)my <= nmax) {
 			const double nb = mx / 2 + 1;
 			const double direct_s = 2.0 * d.crop_w * d.crop_h * d.psf_w * d.psf_h / 35e12;
@@ -487,10 +533,41 @@ pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5])
 		d.fft_my = my;
 		const int64_t nb = mx / 2 + 1;
 		d.fft_work_off = work;
-		d.fft_spec_off = spec;
 		work += (int64_t)d.draw_h * nb;
-		spec += (int64_t)my * nb;
 		used_nmax = std::max(used_nmax, (int)std::max(mx, my));
+		if (!b->dbl) {
+			// models with the same PSF values and transform sizes share one spectrum
+			bool shared = false;
+			for (size_t q = 0; q < i && !shared; q++) {
+				const pf::ModelDev &e = b->mdev[q];
+				if (e.use_fft && e.fft_mx == mx && e.fft_my == my && e.psf_w == d.psf_w && e.psf_h == d.psf_h &&
+				    (e.psf_off == d.psf_off ||
+				     std::memcmp(psf_pool + e.psf_off, psf_pool + d.psf_off, sizeof(double) * d.psf_w * d.psf_h) == 0)) {
+					d.fft_spec_off = e.fft_spec_off;
+					shared = true;
+				}
+			}
+			const int rpj_x = pf::fft32_rows_per_job((int)mx), cpj_y = pf::fft32_cols_per_job((int)my);
+			auto add = [&](int mode, int pass, int n, int count, int per) {
+				for (int r = 0; r < count; r += per) f32[mode][pass][n].push_back({(int)i, r, std::min(per, count - r), 0});
+			};
+			if (!shared) {
+				d.fft_spec_off = spec;
+				spec += (int64_t)my * nb;
+				add(2, 0, (int)mx, (int)d.psf_h, rpj_x);
+				add(2, 1, (int)my, (int)nb, cpj_y);
+			}
+			add(0, 0, (int)mx, (int)d.draw_h, rpj_x);
+			add(0, 1, (int)my, (int)nb, cpj_y);
+			add(0, 2, (int)mx, (int)d.crop_h, rpj_x);
+			add(1, 0, (int)mx, (int)d.crop_h, rpj_x);
+			add(1, 1, (int)my, (int)nb, cpj_y);
+			add(1, 2, (int)mx, (int)d.draw_h, rpj_x);
+			b->any_fft = true;
+			continue;
+		}
+		d.fft_spec_off = spec;
+		spec += (int64_t)my * nb;
 		const int cr = std::max(1, std::min(16, per_block / (int)mx));
 		const int cc = std::max(1, std::min(16, per_block / (int)my));
 		for (unsigned int r = 0; r < d.draw_h; r += cr) jobs[0].push_back({(int)i, (int)r, (int)std::min<unsigned int>(cr, d.draw_h - r), 0});
@@ -522,7 +599,7 @@ extern "C" {
 
 static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, size_t n_models,
                                    const pf_profile_desc *profiles, size_t n_profiles, const double *psf_pool,
-                                   size_t psf_pool_len, pf_batch *b)
+                                   size_t psf_pool_len, pf_batch *b, const ConvPlan &plan)
 {
 	b->env = env;
 	b->dbl = (env->flags & PF_ENV_DOUBLE) != 0;
@@ -604,7 +681,8 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		return fail(PF_ERR_UNSUPPORTED, "batch too large: more than 2^32 tiles of 32 pixels");
 	}
 	std::vector<HostFftJob> fft_jobs[5];
-	pf_status fs = plan_fft(b, fft_jobs);
+	std::map<int, std::vector<HostFftJob>> f32_jobs[3][3];
+	pf_status fs = plan_fft(b, fft_jobs, psf_pool, f32_jobs, plan);
 	if (fs != PF_OK) return fs;
 	std::vector<long long> tile_base_out(std::max<size_t>(1, n_models), 0);
 	if (!b->dbl) {
@@ -614,7 +692,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 			const pf::ModelDev &d = b->mdev[i];
 			if (!d.use_fft) conv_dims.push_back({d.crop_w, d.crop_h});
 		}
-		b->fwd_shape = best_conv_shape<float>(conv_dims);
+		b->fwd_shape = plan.shape >= 0 ? plan.shape : best_conv_shape<float>(conv_dims);
 		long long t = 0;
 		for (size_t i = 0; i < n_models; i++) {
 			const pf::ModelDev &d = b->mdev[i];
@@ -716,7 +794,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		const size_t celem = b->dbl ? 2 * sizeof(double) : 2 * sizeof(float);
 		PF_CUDA_TRY(cudaMalloc(&b->d_fft_work, celem * std::max<int64_t>(1, b->fft_work_elems)));
 		PF_CUDA_TRY(cudaMalloc(&b->d_fft_spec, celem * std::max<int64_t>(1, b->fft_spec_elems)));
-		PF_CUDA_TRY(cudaMalloc(&b->d_fft_tw, celem * (b->fft_nmax / 2)));
+		PF_CUDA_TRY(cudaMalloc(&b->d_fft_tw, b->dbl ? celem * (b->fft_nmax / 2) : sizeof(float) * 2 * 8192));
 		for (int p = 0; p < 5; p++) {
 			b->fft_njobs[p] = (int)fft_jobs[p].size();
 			PF_CUDA_TRY(cudaMalloc(&b->d_fft_jobs[p], sizeof(HostFftJob) * std::max<size_t>(1, fft_jobs[p].size())));
@@ -725,7 +803,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 				                       cudaMemcpyHostToDevice));
 			}
 		}
-		if (b->fft_smem_bytes > 227 * 1024) return fail(PF_ERR_UNSUPPORTED, "FFT too large for shared memory");
+		if (b->dbl && b->fft_smem_bytes > 227 * 1024) return fail(PF_ERR_UNSUPPORTED, "FFT too large for shared memory");
 		if (b->dbl) {
 			PF_CUDA_TRY(pf::fft_configure<double>(b->fft_smem_bytes));
 			pf::launch_twiddles<double>(b->d_fft_tw, b->fft_nmax, env->stream);
@@ -736,12 +814,26 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 			}
 		}
 		else {
-			PF_CUDA_TRY(pf::fft_configure<float>(b->fft_smem_bytes));
-			pf::launch_twiddles<float>(b->d_fft_tw, b->fft_nmax, env->stream);
-			for (int p = 3; p <= 4; p++) {
-				pf::launch_fft_pass<float>(p, b->d_models, b->d_fft_jobs[p], b->fft_njobs[p], nullptr, b->d_psf32,
-				                           b->d_fft_work, b->d_fft_spec, nullptr, nullptr, b->d_fft_tw, b->fft_nmax,
-				                           b->fft_smem_bytes, env->stream);
+			for (int mode = 0; mode < 3; mode++) {
+				for (int pass = 0; pass < 3; pass++) {
+					for (const auto &kv : f32_jobs[mode][pass]) {
+						pf_batch::Fft32Jobs j;
+						j.n = kv.first;
+						j.n_jobs = (int)kv.second.size();
+						PF_CUDA_TRY(cudaMalloc(&j.d_jobs, sizeof(HostFftJob) * kv.second.size()));
+						b->f32_jobs[mode][pass].push_back(j);
+						PF_CUDA_TRY(cudaMemcpy(j.d_jobs, kv.second.data(), sizeof(HostFftJob) * kv.second.size(),
+						                       cudaMemcpyHostToDevice));
+					}
+				}
+			}
+			PF_CUDA_TRY(pf::fft32_configure());
+			pf::launch_fft32_twiddles(b->d_fft_tw, env->stream);
+			for (int pass = 0; pass < 2; pass++) {
+				for (const auto &j : b->f32_jobs[2][pass]) {
+					pf::launch_fft32(pass, 2, j.n, j.d_jobs, j.n_jobs, b->d_models, nullptr, b->d_psf32, b->d_fft_work,
+					                 b->d_fft_spec, nullptr, nullptr, b->d_fft_tw, env->stream);
+				}
 			}
 		}
 		PF_CUDA_TRY(cudaGetLastError());
@@ -749,6 +841,81 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 	}
 	b->params_dirty = true;
 	return PF_OK;
+}
+
+static pf_status create_planned(pf_env *env, const pf_model_desc *models, size_t n_models,
+                                const pf_profile_desc *profiles, size_t n_profiles, const double *psf_pool,
+                                size_t psf_pool_len, const ConvPlan &plan, pf_batch **batch)
+{
+	*batch = nullptr;
+	pf_batch *b = new (std::nothrow) pf_batch();
+	if (!b) return fail(PF_ERR_NO_MEMORY, "out of host memory");
+	pf_status s = batch_create_impl(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, b, plan);
+	if (s != PF_OK) {
+		b->env = env;
+		pf_batch_destroy(b);
+		return s;
+	}
+	*batch = b;
+	return PF_OK;
+}
+
+// Autotuner timings (ms, best of three after one warm-up launch) of the
+// forward convolution of a batch: its direct convolution with block shape
+// `shape` over every model it convolves directly, or its FFT passes.
+static double time_forward_conv(pf_batch *b, int shape, bool fft, float *out)
+{
+	cudaStream_t st = b->env->stream;
+	const int n_models = (int)b->mdev.size();
+	std::vector<long long> base(std::max<size_t>(1, b->mdev.size()), 0);
+	long long t = 0;
+	unsigned int max_kw = 1, max_kh = 1;
+	for (size_t i = 0; i < b->mdev.size(); i++) {
+		const pf::ModelDev &d = b->mdev[i];
+		base[i] = t;
+		if (d.use_fft) continue;
+		t += pf::conv_tiles<float>(d.crop_w, d.crop_h, shape);
+		if (d.conv_required) {
+			max_kw = std::max(max_kw, d.psf_w);
+			max_kh = std::max(max_kh, d.psf_h);
+		}
+	}
+	const size_t smem = pf::conv_smem<float>(max_kw, max_kh, shape);
+	long long *d_base = nullptr;
+	if (!fft && (smem > 227 * 1024 || cudaMalloc(&d_base, sizeof(long long) * base.size()) != cudaSuccess)) return -1;
+	if (!fft) {
+		cudaMemcpy(d_base, base.data(), sizeof(long long) * base.size(), cudaMemcpyHostToDevice);
+		pf::conv_configure<float>(smem, shape);
+	}
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	double best = -1;
+	for (int rep = 0; rep < 4; rep++) {
+		cudaEventRecord(e0, st);
+		if (fft) {
+			for (int pass = 0; pass < 3; pass++) {
+				for (const auto &j : b->f32_jobs[0][pass]) {
+					pf::launch_fft32(pass, 0, j.n, j.d_jobs, j.n_jobs, b->d_models, (const float *)b->d_conv, nullptr,
+					                 b->d_fft_work, b->d_fft_spec, (const float *)b->d_direct, out, b->d_fft_tw, st);
+				}
+			}
+		}
+		else if (t > 0) {
+			pf::launch_conv<float>(0, shape, b->d_models, n_models, b->d_psf32, (const float *)b->d_conv,
+			                       (const float *)b->d_direct, out, d_base, t, smem, b->env->n_sm, st);
+		}
+		cudaEventRecord(e1, st);
+		cudaEventSynchronize(e1);
+		float ms = 0;
+		cudaEventElapsedTime(&ms, e0, e1);
+		if (rep > 0 && (best < 0 || ms < best)) best = ms;
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(d_base);
+	if (!fft) pf::conv_configure<float>(b->finish_smem, b->fwd_shape);
+	return cudaGetLastError() == cudaSuccess ? best : -1;
 }
 
 pf_status pf_batch_create(pf_env *env, const pf_model_desc *models, size_t n_models, const pf_profile_desc *profiles,
@@ -759,16 +926,77 @@ pf_status pf_batch_create(pf_env *env, const pf_model_desc *models, size_t n_mod
 	}
 	*batch = nullptr;
 	PF_CUDA_TRY(cudaSetDevice(env->device));
-	pf_batch *b = new (std::nothrow) pf_batch();
-	if (!b) return fail(PF_ERR_NO_MEMORY, "out of host memory");
-	pf_status s = batch_create_impl(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, b);
-	if (s != PF_OK) {
-		b->env = env;
-		pf_batch_destroy(b);
-		return s;
+	const ConvPlan fixed;
+	bool tune = !(env->flags & (PF_ENV_DOUBLE | PF_ENV_NO_AUTOTUNE));
+	uint64_t out_pixels = 0;
+	bool any_auto = false;
+	for (size_t i = 0; i < n_models && tune; i++) {
+		out_pixels += (uint64_t)models[i].width * models[i].height;
+		any_auto |= models[i].convolver == PF_CONV_AUTO && models[i].psf_offset >= 0 && models[i].psf_w > 0;
 	}
-	*batch = b;
-	return PF_OK;
+	tune = tune && any_auto && out_pixels >= (1ull << 22);
+	if (!tune) return create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, fixed, batch);
+
+	// The autotuner (single precision, PF_CONV_AUTO, large batches): the batch
+	// built with every automatic model on the direct convolution, each block
+	// shape timed; built again with them on the FFT, timed; per model, the
+	// method whose fitted cost is lower (cost = seconds per unit of work,
+	// crop area x PSF area for the direct convolution, M_x M_y log2(M_x M_y)
+	// for the FFT, fitted to the two timings); the fastest shape.
+	std::vector<int8_t> none(n_models, 0), all(n_models, 1);
+	ConvPlan pd, pfft;
+	pd.auto_fft = &none;
+	pfft.auto_fft = &all;
+	pf_batch *bd = nullptr, *bf = nullptr;
+	pf_status s = create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, pd, &bd);
+	if (s != PF_OK) return s;
+	float *out = nullptr;
+	if (cudaMalloc(&out, sizeof(float) * std::max<uint64_t>(1, bd->total_out)) != cudaSuccess) {
+		pf_batch_destroy(bd);
+		return fail(PF_ERR_NO_MEMORY, "pf_batch_create: autotuner output buffer");
+	}
+	cudaMemsetAsync(bd->d_conv, 0, sizeof(float) * std::max<size_t>(1, bd->draw_total), env->stream);
+	cudaMemsetAsync(bd->d_direct, 0, sizeof(float) * std::max<size_t>(1, bd->draw_total), env->stream);
+	double t_direct = -1;
+	int best_shape = bd->fwd_shape;
+	for (int sh = 0; sh < pf::conv_num_shapes<float>(); sh++) {
+		const double ms = time_forward_conv(bd, sh, false, out);
+		if (ms >= 0 && (t_direct < 0 || ms < t_direct)) {
+			t_direct = ms;
+			best_shape = sh;
+		}
+	}
+	double work_d = 0;
+	for (const auto &d : bd->mdev) {
+		work_d += (double)d.crop_w * d.crop_h * (d.conv_required ? (double)d.psf_w * d.psf_h : 1.0);
+	}
+	std::vector<int8_t> choice(n_models, 0);
+	s = create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, pfft, &bf);
+	if (s == PF_OK && bf->any_fft) {
+		cudaMemsetAsync(bf->d_conv, 0, sizeof(float) * std::max<size_t>(1, bf->draw_total), env->stream);
+		cudaMemsetAsync(bf->d_direct, 0, sizeof(float) * std::max<size_t>(1, bf->draw_total), env->stream);
+		const double t_fft = time_forward_conv(bf, 0, true, out);
+		double work_f = 0;
+		for (const auto &d : bf->mdev) {
+			if (d.use_fft) work_f += (double)d.fft_mx * d.fft_my * std::log2((double)d.fft_mx * d.fft_my);
+		}
+		if (t_fft > 0 && t_direct > 0 && work_f > 0 && work_d > 0) {
+			const double cf = t_fft / work_f, cd = t_direct / work_d;
+			for (size_t i = 0; i < n_models; i++) {
+				const pf::ModelDev &d = bf->mdev[i];
+				if (!d.use_fft) continue;
+				choice[i] = cf * d.fft_mx * d.fft_my * std::log2((double)d.fft_mx * d.fft_my) <
+				            cd * (double)d.crop_w * d.crop_h * d.psf_w * d.psf_h;
+			}
+		}
+	}
+	if (bf) pf_batch_destroy(bf);
+	cudaFree(out);
+	pf_batch_destroy(bd);
+	ConvPlan fin;
+	fin.shape = best_shape;
+	fin.auto_fft = &choice;
+	return create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, fin, batch);
 }
 
 pf_status pf_batch_layout(const pf_batch *b, uint64_t *offsets, uint32_t *dims, uint64_t *total_pixels)
@@ -820,6 +1048,7 @@ pf_status pf_batch_set_params_dev(pf_batch *b, const double *params_dev, void *s
 		b->params_dirty = false;
 	}
 	pf::launch_set_params(b->d_profiles, (int)b->profiles.size(), params_dev, stream);
+	b->kernel_launches++;
 	PF_CUDA_TRY(cudaGetLastError());
 	return PF_OK;
 }
@@ -893,16 +1122,28 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 		pf::launch_conv<float>(0, b->fwd_shape, b->d_models, n_models, b->d_psf32, (const float *)b->d_conv,
 		                       (const float *)b->d_direct, (float *)images_dev, b->d_tile_base_out, b->n_out_tiles,
 		                       b->finish_smem, b->env->n_sm, stream);
-		for (int p = 0; b->any_fft && p <= 2; p++) {
-			pf::launch_fft_pass<float>(p, b->d_models, b->d_fft_jobs[p], b->fft_njobs[p], (const float *)b->d_conv,
-			                           nullptr, b->d_fft_work, b->d_fft_spec, (const float *)b->d_direct,
-			                           (float *)images_dev, b->d_fft_tw, b->fft_nmax, b->fft_smem_bytes, stream);
+		for (int pass = 0; b->any_fft && pass < 3; pass++) {
+			for (const auto &j : b->f32_jobs[0][pass]) {
+				pf::launch_fft32(pass, 0, j.n, j.d_jobs, j.n_jobs, b->d_models, (const float *)b->d_conv, nullptr,
+				                 b->d_fft_work, b->d_fft_spec, (const float *)b->d_direct, (float *)images_dev,
+				                 b->d_fft_tw, stream);
+			}
 		}
 		stage_end(b, t, stream);
 	}
 	b->forward_calls++;
+	{
+		uint64_t k = (n_profiles > 0 ? 2 : 1) + 1;  // setup (solves, profiles), evaluation
+		if (b->dbl) k += 1 + (b->any_fft ? 3 : 0);   // finish, FFT passes
+		else {
+			k += b->n_out_tiles > 0 ? 1 : 0;
+			for (int pass = 0; b->any_fft && pass < 3; pass++) k += b->f32_jobs[0][pass].size();
+		}
+		b->kernel_launches += k;
+	}
 	if (flux_dev) {
 		pf::launch_flux_sum(b->d_models, n_models, images_dev, b->dbl ? 1 : 0, flux_dev, stream);
+		b->kernel_launches++;
 	}
 	PF_CUDA_TRY(cudaGetLastError());
 	return PF_OK;
@@ -966,7 +1207,7 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	unsigned int max_kw = 1, max_kh = 1;
 	std::vector<std::pair<unsigned int, unsigned int>> conv_dims;
 	for (const auto &m : b->mdev) {
-		if (m.conv_required) conv_dims.push_back({m.draw_w, m.draw_h});
+		if (m.conv_required && (b->dbl || !m.use_fft)) conv_dims.push_back({m.draw_w, m.draw_h});
 	}
 	b->adj_shape = b->dbl ? best_conv_shape<double>(conv_dims) : best_conv_shape<float>(conv_dims);
 	for (size_t i = 0; i < n_models; i++) {
@@ -977,7 +1218,7 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 		}
 		max_h = std::max(max_h, m.draw_h);
 		adj_tile_base[i] = tiles;
-		if (m.conv_required) {
+		if (m.conv_required && (b->dbl || !m.use_fft)) {
 			tiles += b->dbl ? pf::conv_tiles<double>(m.draw_w, m.draw_h, b->adj_shape)
 			                : pf::conv_tiles<float>(m.draw_w, m.draw_h, b->adj_shape);
 			max_kw = std::max(max_kw, m.psf_w);
@@ -1037,9 +1278,19 @@ pf_status pf_backward(pf_batch *b, const void *images_dev, const void *data_dev,
 		if (b->dbl) pf::launch_conv<double>(1, b->adj_shape, b->d_models, n_models, b->d_psf_norm, (const double *)b->d_gout,
 		                                    nullptr, (double *)b->d_gsrc, b->d_adj_tile_base, b->n_adj_tiles,
 		                                    b->adj_smem, b->env->n_sm, stream);
-		else pf::launch_conv<float>(1, b->adj_shape, b->d_models, n_models, b->d_psf32, (const float *)b->d_gout, nullptr,
-		                            (float *)b->d_gsrc, b->d_adj_tile_base, b->n_adj_tiles, b->adj_smem,
-		                            b->env->n_sm, stream);
+		else {
+			if (b->n_adj_tiles > 0) {
+				pf::launch_conv<float>(1, b->adj_shape, b->d_models, n_models, b->d_psf32, (const float *)b->d_gout,
+				                       nullptr, (float *)b->d_gsrc, b->d_adj_tile_base, b->n_adj_tiles, b->adj_smem,
+				                       b->env->n_sm, stream);
+			}
+			for (int pass = 0; b->any_fft && pass < 3; pass++) {
+				for (const auto &j : b->f32_jobs[1][pass]) {
+					pf::launch_fft32(pass, 1, j.n, j.d_jobs, j.n_jobs, b->d_models, (const float *)b->d_gout, nullptr,
+					                 b->d_fft_work, b->d_fft_spec, nullptr, (float *)b->d_gsrc, b->d_fft_tw, stream);
+				}
+			}
+		}
 		stage_end(b, t, stream);
 	}
 	t = stage_begin(b, ST_BACKWARD, stream);
@@ -1052,6 +1303,17 @@ pf_status pf_backward(pf_batch *b, const void *images_dev, const void *data_dev,
 	                                b->env->n_sm, stream);
 	stage_end(b, t, stream);
 	b->backward_calls++;
+	{
+		uint64_t k = 1 + (n_profiles > 0 ? 2 : 0);  // chi^2, backward, gradient reduction
+		if (any_conv) {
+			if (b->dbl) k += 1;
+			else {
+				k += b->n_adj_tiles > 0 ? 1 : 0;
+				for (int pass = 0; b->any_fft && pass < 3; pass++) k += b->f32_jobs[1][pass].size();
+			}
+		}
+		b->kernel_launches += k;
+	}
 	PF_CUDA_TRY(cudaGetLastError());
 	return PF_OK;
 }
@@ -1069,9 +1331,11 @@ pf_status pf_batch_stats(pf_batch *b, pf_stage_times *times, int reset)
 	times->backward_ms = b->stage_ms[ST_BACKWARD];
 	times->forward_calls = b->forward_calls;
 	times->backward_calls = b->backward_calls;
+	times->kernel_launches = b->kernel_launches;
 	if (reset) {
 		for (double &v : b->stage_ms) v = 0;
 		b->forward_calls = b->backward_calls = 0;
+		b->kernel_launches = 0;
 	}
 	return PF_OK;
 }
@@ -1082,6 +1346,73 @@ pf_status pf_forward_backward(pf_batch *b, void *images_dev, const void *data_de
 	pf_status s = pf_forward(b, images_dev, nullptr, stream);
 	if (s != PF_OK) return s;
 	return pf_backward(b, images_dev, data_dev, sigma_dev, nullptr, chi2_dev, grad_dev, stream);
+}
+
+pf_status pf_step_graph(pf_batch *b, const double *params_dev, void *images_dev, const void *data_dev,
+                        const void *sigma_dev, double *chi2_dev, double *grad_dev, void *stream_ptr)
+{
+	if (!b) return fail(PF_ERR_INVALID_PARAMETER, "batch is NULL");
+	if (!b->adjoint) return fail(PF_ERR_INVALID_PARAMETER, "pf_batch_enable_adjoint has not been called");
+	if (!images_dev || !data_dev || !grad_dev) return fail(PF_ERR_INVALID_PARAMETER, "pf_step_graph: NULL argument");
+	cudaStream_t stream = stream_ptr ? (cudaStream_t)stream_ptr : b->env->stream;
+	if (stream == cudaStreamLegacy || stream == cudaStreamPerThread) {
+		return fail(PF_ERR_INVALID_PARAMETER, "pf_step_graph: a graph is captured on a created stream, not the default one");
+	}
+	PF_CUDA_TRY(cudaSetDevice(b->env->device));
+	// parameters set on the host since the last step go up outside the graph
+	if (b->params_dirty) {
+		PF_CUDA_TRY(cudaMemcpyAsync(b->d_profiles, b->h_profiles,
+		                            sizeof(pf::ProfileDev) * std::max<size_t>(1, b->profiles.size()),
+		                            cudaMemcpyHostToDevice, stream));
+		b->params_dirty = false;
+	}
+	pf_batch::GraphKey key;
+	key.params = params_dev;
+	key.images = images_dev;
+	key.data = data_dev;
+	key.sigma = sigma_dev;
+	key.chi2 = chi2_dev;
+	key.grad = grad_dev;
+	key.stream = stream;
+	key.record = b->record;
+	bool captured = false;
+	if (!b->graph || !(key == b->graph_key)) {
+		if (b->graph) {
+			cudaGraphExecDestroy(b->graph);
+			b->graph = nullptr;
+		}
+		PF_CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+		b->capturing = true;
+		const uint64_t k0 = b->kernel_launches;
+		pf_status s = PF_OK;
+		if (params_dev) s = pf_batch_set_params_dev(b, params_dev, stream);
+		if (s == PF_OK) s = pf_forward(b, images_dev, nullptr, stream);
+		if (s == PF_OK) s = pf_backward(b, images_dev, data_dev, sigma_dev, nullptr, chi2_dev, grad_dev, stream);
+		b->capturing = false;
+		cudaGraph_t g = nullptr;
+		const cudaError_t e = cudaStreamEndCapture(stream, &g);
+		if (s != PF_OK) {
+			if (g) cudaGraphDestroy(g);
+			return s;
+		}
+		if (e != cudaSuccess) return fail(PF_ERR_CUDA, std::string("pf_step_graph: capture: ") + cudaGetErrorString(e));
+		const cudaError_t ei = cudaGraphInstantiate(&b->graph, g, 0);
+		cudaGraphDestroy(g);
+		if (ei != cudaSuccess) {
+			b->graph = nullptr;
+			return fail(PF_ERR_CUDA, std::string("pf_step_graph: instantiate: ") + cudaGetErrorString(ei));
+		}
+		b->graph_key = key;
+		b->graph_kernels = b->kernel_launches - k0;
+		captured = true;
+	}
+	PF_CUDA_TRY(cudaGraphLaunch(b->graph, stream));
+	if (!captured) {  // the capture counted the first call
+		b->forward_calls++;
+		b->backward_calls++;
+		b->kernel_launches += b->graph_kernels;
+	}
+	return PF_OK;
 }
 
 pf_status pf_model_evaluate(pf_env *env, const pf_model_desc *model, const pf_profile_desc *profiles,

@@ -102,7 +102,7 @@ def fd(problem, oracle_lib):
     return _fd(oracle_lib, psf, profiles, data, sigma)
 
 
-def _gpu_grad(problem, use_double):
+def _gpu_grad(problem, use_double, convolver=None):
     import torch
     import __graft_entry__
     __graft_entry__.build_cuda()
@@ -111,6 +111,8 @@ def _gpu_grad(problem, use_double):
     psf, profiles, data, sigma = problem
     env = pg.get_cuda_environment(0, use_double=use_double)
     m = W.to_model(dict(width=64, height=64, psf=psf, profiles=profiles, magzero=MAGZERO), env)
+    if convolver:
+        m.set_convolver(convolver)
     b = pg.Batch([m], env)
     b.enable_adjoint()
     dt = torch.float64 if use_double else torch.float32
@@ -124,10 +126,10 @@ def _gpu_grad(problem, use_double):
     return chi2.item(), grad.cpu().numpy().reshape(len(profiles), 12)
 
 
-@pytest.mark.parametrize("use_double", [True, False])
-def test_gradient_matches_finite_differences(problem, fd, oracle_lib, use_double):
+@pytest.mark.parametrize("use_double,convolver", [(True, None), (False, None), (False, "fft")])
+def test_gradient_matches_finite_differences(problem, fd, oracle_lib, use_double, convolver):
     psf, profiles, data, sigma = problem
-    chi2, grad = _gpu_grad(problem, use_double)
+    chi2, grad = _gpu_grad(problem, use_double, convolver)
     chi2_ref, _ = _chi2(oracle_lib, psf, profiles, data, sigma)
     assert abs(chi2 - chi2_ref) <= (1e-10 if use_double else 1e-4) * chi2_ref
     rtol, floor = (1e-4, 1e-9) if use_double else (1e-3, 1e-6)
@@ -169,3 +171,15 @@ def test_cotangent_vjp(problem, oracle_lib):
         im, _, _ = O.evaluate(O.Case(64, 64, _with(profiles, i, k, v - h), psf=psf, magzero=MAGZERO))
         want = float(np.sum(cot * (ip - im)) / (2 * h))
         assert abs(g[i, SLOT[k]] - want) <= 1e-4 * abs(want) + 1e-8, (k, g[i, SLOT[k]], want)
+
+
+def test_fft_adjoint_matches_direct(problem):
+    """FP32 path: the FFT convolution's adjoint (the cotangent correlated with
+    the PSF through the spectrum) against the direct convolution's adjoint on
+    the same model and data: chi^2 within 1e-6, every gradient within
+    1e-4 relative (plus 1e-7 of the largest)."""
+    chi2_d, g_d = _gpu_grad(problem, False, "brute")
+    chi2_f, g_f = _gpu_grad(problem, False, "fft")
+    assert abs(chi2_f - chi2_d) <= 1e-6 * chi2_d
+    scale = np.abs(g_d).max()
+    np.testing.assert_allclose(g_f, g_d, rtol=1e-4, atol=1e-7 * scale)
