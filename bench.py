@@ -223,6 +223,8 @@ def run_reference(args, world, rank):
 # op weighted 8, its issue cost against the FMA pipe: 128 vs 16 per SM-clock).
 FLOP_EVAL = 2 * 7 + 5 + 3 * 8        # coordinates + base + rf + exp: 43
 FLOP_GRAD = FLOP_EVAL + 40 + 4 * 8   # + the derivative chain (sersic_grad): 115
+# DRAM bytes per model of the adjoint direct convolution's launch (ncu, 256-model copy of the workload)
+ADJ_CONV_TRAFFIC_PER_MODEL = None
 
 
 def run_ours(args, world, rank, local):
@@ -364,16 +366,30 @@ def run_ours(args, world, rank, local):
     dom = max(per_step, key=per_step.get)
     sm_mhz = clk.get("sm_mhz") or 2070.0
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s at the sampled clock
-    work = {"eval_ms": evals * FLOP_EVAL, "backward_ms": evals * FLOP_GRAD}
+    # direct convolution: 2 flop per output pixel and PSF tap (forward over the
+    # crop, adjoint over the drawing area)
+    taps = [s["psf"].shape[0] * s["psf"].shape[1] for s in specs]
+    conv_fwd = sum(2.0 * w * h * t for (w, h), t in zip(batch.dims, taps))
+    conv_adj = sum(2.0 * (w + s["psf"].shape[1] // 2 * 2) * (h + s["psf"].shape[0] // 2 * 2) * t
+                   for (w, h), t, s in zip(batch.dims, taps, specs))
+    work = {"eval_ms": evals * FLOP_EVAL, "backward_ms": evals * FLOP_GRAD, "finish_ms": conv_fwd,
+            "adjoint_conv_ms": conv_adj}
+    # DRAM bytes per launch, per model of this workload: ncu dram__bytes_read.sum +
+    # dram__bytes_write.sum of each kernel on the 256-model copy of the workload
+    # (profiles/*_256x256*.md), divided by 256
+    traffic_per_model = {"eval_ms": 106.6e6 / 256, "backward_ms": 83.1e6 / 256, "finish_ms": 193.4e6 / 256,
+                         "adjoint_conv_ms": ADJ_CONV_TRAFFIC_PER_MODEL}
+    roof = {"bound": "fp32", "kernel": dom.replace("_ms", ""), "achieved": None, "peak": fp32_peak,
+            "unit": "TFLOP/s", "frac": None, "traffic": None,
+            "peak_note": "nominal FP32 FMA peak (152 SMs x 128 lanes x 2 flop) at the sampled median SM clock; "
+                         "no measured FP32 peak exists for this pool"}
     if dom in work:
         achieved = work[dom] / (per_step[dom] / 1000.0) / 1e12
-        roof = {"bound": "fp32", "kernel": dom.replace("_ms", ""), "achieved": achieved, "peak": fp32_peak,
-                "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
-                "evals_per_step": evals, "flop_per_eval": FLOP_EVAL if dom == "eval_ms" else FLOP_GRAD,
-                "peak_note": "nominal FP32 FMA peak at the sampled median SM clock (no measured FP32 peak)"}
-    else:
-        roof = {"bound": "fp32", "kernel": dom.replace("_ms", ""), "achieved": None, "peak": fp32_peak,
-                "unit": "TFLOP/s", "frac": None, "traffic": None}
+        tpm = traffic_per_model.get(dom)
+        roof.update({"achieved": achieved, "frac": achieved / fp32_peak,
+                     "traffic": tpm * n_models if tpm else None, "flop_per_step": work[dom]})
+        if dom in ("eval_ms", "backward_ms"):
+            roof.update({"evals_per_step": evals, "flop_per_eval": FLOP_EVAL if dom == "eval_ms" else FLOP_GRAD})
 
     cpu = None
     if not args.no_cpu_baseline:
