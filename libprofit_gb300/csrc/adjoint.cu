@@ -88,7 +88,9 @@ __global__ void chi2_kernel(const ModelDev *__restrict__ models, const T *__rest
 {
 	const ModelDev &m = models[blockIdx.x];
 	const long long n = (long long)m.out_w * m.out_h;
-	double s = 0;
+	// per thread: a compensated (Kahan) sum in T, so that single precision
+	// costs no FP64 work per pixel; across threads: FP64
+	T s = 0, comp = 0;
 	for (long long i = threadIdx.x; i < n; i += blockDim.x) {
 		const long long g = m.out_off + i;
 		if (cot) {
@@ -97,12 +99,16 @@ __global__ void chi2_kernel(const ModelDev *__restrict__ models, const T *__rest
 		else {
 			const T r = img[g] - data[g];
 			const T w = sigma ? (T)1 / (sigma[g] * sigma[g]) : (T)1;
-			s += (double)w * (double)r * (double)r;
-			gout[g] = (T)2 * w * r;
+			const T wr = w * r;
+			const T y = wr * r - comp;
+			const T t = s + y;
+			comp = (t - s) - y;
+			s = t;
+			gout[g] = (T)2 * wr;
 		}
 	}
 	__shared__ double part[256];
-	part[threadIdx.x] = s;
+	part[threadIdx.x] = (double)s - (double)comp;
 	__syncthreads();
 	for (int w = blockDim.x / 2; w > 0; w >>= 1) {
 		if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];

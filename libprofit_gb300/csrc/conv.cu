@@ -32,15 +32,18 @@ namespace {
 //   float  0: 16 x 16 x 8 -> 64 x 128 outputs
 //   float  1: 14 x 14 x 5 -> 56 x 70
 //   float  2: 16 x 12 x 8 -> 64 x 96
+//   float  3: 14 x 10 x 7 -> 56 x 70
 //   double 0: 16 x 8 x 4  -> 64 x 32
 // The host picks, per batch and direction, the shape that wastes the least
-// tile area over the images it convolves.
+// tile area over the images it convolves, or, for large single-precision
+// batches, the one the autotuner timed fastest.
 struct Shape {
 	int tx, ty, r;
 };
 __host__ __device__ constexpr Shape shape_of(bool dbl, int id)
 {
-	return dbl ? Shape{16, 8, 4} : (id == 1 ? Shape{14, 14, 5} : (id == 2 ? Shape{16, 12, 8} : Shape{16, 16, 8}));
+	return dbl ? Shape{16, 8, 4}
+	           : (id == 1 ? Shape{14, 14, 5} : (id == 2 ? Shape{16, 12, 8} : (id == 3 ? Shape{14, 10, 7} : Shape{16, 16, 8})));
 }
 
 template <typename T>
@@ -74,6 +77,31 @@ __device__ __forceinline__ T cot_at(const ModelDev &m, const T *gout, int x, int
 	if (cx < 0 || cy < 0 || cx >= (int)m.crop_w || cy >= (int)m.crop_h) return (T)0;
 	if (m.fs > 1 && !m.return_fs) return gout[m.out_off + (size_t)(cy / m.fs) * m.out_w + cx / m.fs];
 	return gout[m.out_off + (size_t)cy * m.out_w + cx];
+}
+
+// The multiply-adds of one source row (srow, this thread's 4 + 4 columns) into
+// output rows r0..r1 (kernel row s - r); with r0 and r1 known at compile time
+// after unrolling, the row loop carries no tests.
+template <typename T, int R>
+__device__ __forceinline__ void conv_rows(const T *srow, const T *s_k, int s, int kwp, int r0, int r1,
+                                          T (&acc)[R][4])
+{
+	using V4 = typename Vec4<T>::type;
+	for (int kb = 0; kb < kwp; kb += 4) {
+		const V4 w0 = *reinterpret_cast<const V4 *>(srow + kb);
+		const V4 w1 = *reinterpret_cast<const V4 *>(srow + kb + 4);
+		const T w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+		for (int r = 0; r < R; r++) {
+			if (r < r0 || r > r1) continue;
+			const V4 kv4 = *reinterpret_cast<const V4 *>(s_k + (s - r) * kwp + kb);
+			const T kv[4] = {kv4.x, kv4.y, kv4.z, kv4.w};
+#pragma unroll
+			for (int c = 0; c < 4; c++)
+#pragma unroll
+				for (int q = 0; q < 4; q++) acc[r][c] = fma(w[c + q], kv[q], acc[r][c]);
+		}
+	}
 }
 
 template <typename T, int MODE, int TX, int TY, int R>
@@ -140,24 +168,22 @@ conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restri
 			}
 			__syncthreads();
 			const int xb = tx * 4, yb = ty * R;
-			for (int s = 0; s < R + kh - 1; s++) {
-				const T *srow = s_src + (yb + s) * pw + xb;
-				for (int kb = 0; kb < kwp; kb += 4) {
-					const V4 w0 = *reinterpret_cast<const V4 *>(srow + kb);
-					const V4 w1 = *reinterpret_cast<const V4 *>(srow + kb + 4);
-					const T w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+			if (kh >= R) {
+				// source row s feeds output rows r with kernel row l = s - r in
+				// [0, kh): rows 0..s while s < R - 1, all rows up to s = kh - 1,
+				// rows s - kh + 1 .. R - 1 after; the ramps are unrolled so that no
+				// row test is left in the multiply-add stream
 #pragma unroll
-					for (int r = 0; r < R; r++) {
-						const int l = s - r;
-						if (l >= 0 && l < kh) {
-							const V4 kv4 = *reinterpret_cast<const V4 *>(s_k + l * kwp + kb);
-							const T kv[4] = {kv4.x, kv4.y, kv4.z, kv4.w};
+				for (int s0 = 0; s0 < R - 1; s0++) conv_rows<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, 0, s0, acc);
+				for (int s0 = R - 1; s0 < kh; s0++) conv_rows<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, 0, R - 1, acc);
 #pragma unroll
-							for (int c = 0; c < 4; c++)
-#pragma unroll
-								for (int q = 0; q < 4; q++) acc[r][c] = fma(w[c + q], kv[q], acc[r][c]);
-						}
-					}
+				for (int d = 0; d < R - 1; d++) {
+					conv_rows<T, R>(s_src + (yb + kh + d) * pw + xb, s_k, kh + d, kwp, d + 1, R - 1, acc);
+				}
+			}
+			else {
+				for (int s0 = 0; s0 < R + kh - 1; s0++) {
+					conv_rows<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, max(0, s0 - kh + 1), min(R - 1, s0), acc);
 				}
 			}
 			__syncthreads();
@@ -189,7 +215,7 @@ conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restri
 template <typename T>
 int conv_num_shapes()
 {
-	return std::is_same<T, double>::value ? 1 : 3;
+	return std::is_same<T, double>::value ? 1 : 4;
 }
 
 template <typename T>
@@ -242,6 +268,7 @@ cudaError_t conv_configure<float>(size_t smem, int shape)
 {
 	if (shape == 1) return configure_shape<float, 14, 14, 5>(smem);
 	if (shape == 2) return configure_shape<float, 16, 12, 8>(smem);
+	if (shape == 3) return configure_shape<float, 14, 10, 7>(smem);
 	return configure_shape<float, 16, 16, 8>(smem);
 }
 
@@ -258,6 +285,7 @@ void launch_conv<float>(int mode, int shape, const ModelDev *models, int n_model
 {
 	if (shape == 1) launch_shape<float, 14, 14, 5>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
 	else if (shape == 2) launch_shape<float, 16, 12, 8>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
+	else if (shape == 3) launch_shape<float, 14, 10, 7>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
 	else launch_shape<float, 16, 16, 8>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
 }
 

@@ -918,6 +918,49 @@ static double time_forward_conv(pf_batch *b, int shape, bool fft, float *out)
 	return cudaGetLastError() == cudaSuccess ? best : -1;
 }
 
+// Autotuner timing (ms, best of three after a warm-up) of the adjoint direct
+// convolution of a batch with block shape `shape`, into its drawing-area
+// cotangent buffer.
+static double time_adjoint_conv(pf_batch *b, int shape)
+{
+	cudaStream_t st = b->env->stream;
+	const int n_models = (int)b->mdev.size();
+	std::vector<long long> base(std::max<size_t>(1, b->mdev.size()), 0);
+	long long t = 0;
+	unsigned int max_kw = 1, max_kh = 1;
+	for (size_t i = 0; i < b->mdev.size(); i++) {
+		const pf::ModelDev &m = b->mdev[i];
+		base[i] = t;
+		if (!m.conv_required || m.use_fft) continue;
+		t += pf::conv_tiles<float>(m.draw_w, m.draw_h, shape);
+		max_kw = std::max(max_kw, m.psf_w);
+		max_kh = std::max(max_kh, m.psf_h);
+	}
+	const size_t smem = pf::conv_smem<float>(max_kw, max_kh, shape);
+	long long *d_base = nullptr;
+	if (t == 0 || smem > 227 * 1024 || cudaMalloc(&d_base, sizeof(long long) * base.size()) != cudaSuccess) return -1;
+	cudaMemcpy(d_base, base.data(), sizeof(long long) * base.size(), cudaMemcpyHostToDevice);
+	pf::conv_configure<float>(smem, shape);
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	double best = -1;
+	for (int rep = 0; rep < 4; rep++) {
+		cudaEventRecord(e0, st);
+		pf::launch_conv<float>(1, shape, b->d_models, n_models, b->d_psf32, (const float *)b->d_gout, nullptr,
+		                       (float *)b->d_gsrc, d_base, t, smem, b->env->n_sm, st);
+		cudaEventRecord(e1, st);
+		cudaEventSynchronize(e1);
+		float ms = 0;
+		cudaEventElapsedTime(&ms, e0, e1);
+		if (rep > 0 && (best < 0 || ms < best)) best = ms;
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(d_base);
+	return cudaGetLastError() == cudaSuccess ? best : -1;
+}
+
 pf_status pf_batch_create(pf_env *env, const pf_model_desc *models, size_t n_models, const pf_profile_desc *profiles,
                           size_t n_profiles, const double *psf_pool, size_t psf_pool_len, pf_batch **batch)
 {
@@ -1246,8 +1289,33 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	                       cudaMemcpyHostToDevice));
 	PF_CUDA_TRY(b->dbl ? pf::conv_configure<double>(b->adj_smem, b->adj_shape)
 	                   : pf::conv_configure<float>(b->adj_smem, b->adj_shape));
-	if (b->dbl && !b->d_psf_norm) {
-		// no PSF anywhere: the adjoint convolution is never launched
+	if (!b->dbl && !(b->env->flags & PF_ENV_NO_AUTOTUNE) && b->total_out >= (1ull << 22) && tiles > 0) {
+		// the autotuner, adjoint convolution: each block shape timed over the
+		// batch's directly convolved models (zero cotangents), the fastest kept
+		PF_CUDA_TRY(cudaMemsetAsync(b->d_gout, 0, sizeof(float) * std::max<uint64_t>(1, b->total_out), b->env->stream));
+		double best = -1;
+		int best_shape = b->adj_shape;
+		for (int sh = 0; sh < pf::conv_num_shapes<float>(); sh++) {
+			const double ms = time_adjoint_conv(b, sh);
+			if (ms >= 0 && (best < 0 || ms < best)) {
+				best = ms;
+				best_shape = sh;
+			}
+		}
+		if (best_shape != b->adj_shape) {
+			long long t = 0;
+			for (size_t i = 0; i < n_models; i++) {
+				const pf::ModelDev &m = b->mdev[i];
+				adj_tile_base[i] = t;
+				if (m.conv_required && !m.use_fft) t += pf::conv_tiles<float>(m.draw_w, m.draw_h, best_shape);
+			}
+			b->adj_shape = best_shape;
+			b->n_adj_tiles = t;
+			b->adj_smem = pf::conv_smem<float>(max_kw, max_kh, best_shape);
+			PF_CUDA_TRY(cudaMemcpy(b->d_adj_tile_base, adj_tile_base.data(), sizeof(long long) * adj_tile_base.size(),
+			                       cudaMemcpyHostToDevice));
+		}
+		PF_CUDA_TRY(pf::conv_configure<float>(b->adj_smem, b->adj_shape));
 	}
 	b->adjoint = true;
 	return PF_OK;
