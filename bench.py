@@ -224,7 +224,7 @@ def run_reference(args, world, rank):
 FLOP_EVAL = 2 * 7 + 5 + 3 * 8        # coordinates + base + rf + exp: 43
 FLOP_GRAD = FLOP_EVAL + 40 + 4 * 8   # + the derivative chain (sersic_grad): 115
 # DRAM bytes per model of the adjoint direct convolution's launch (ncu, 256-model copy of the workload)
-ADJ_CONV_TRAFFIC_PER_MODEL = None
+ADJ_CONV_TRAFFIC_PER_MODEL = (67.9e6 + 25.0e6) / 256
 
 
 def run_ours(args, world, rank, local):
@@ -377,7 +377,7 @@ def run_ours(args, world, rank, local):
     # DRAM bytes per launch, per model of this workload: ncu dram__bytes_read.sum +
     # dram__bytes_write.sum of each kernel on the 256-model copy of the workload
     # (profiles/*_256x256*.md), divided by 256
-    traffic_per_model = {"eval_ms": 106.6e6 / 256, "backward_ms": 83.1e6 / 256, "finish_ms": 193.4e6 / 256,
+    traffic_per_model = {"eval_ms": 106.6e6 / 256, "backward_ms": 83.1e6 / 256, "finish_ms": 192.3e6 / 256,
                          "adjoint_conv_ms": ADJ_CONV_TRAFFIC_PER_MODEL}
     roof = {"bound": "fp32", "kernel": dom.replace("_ms", ""), "achieved": None, "peak": fp32_peak,
             "unit": "TFLOP/s", "frac": None, "traffic": None,

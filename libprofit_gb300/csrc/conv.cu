@@ -33,6 +33,7 @@ namespace {
 //   float  1: 14 x 14 x 5 -> 56 x 70
 //   float  2: 16 x 12 x 8 -> 64 x 96
 //   float  3: 14 x 10 x 7 -> 56 x 70
+//   float  4: 35 x 7 x 8  -> 140 x 56
 //   double 0: 16 x 8 x 4  -> 64 x 32
 // The host picks, per batch and direction, the shape that wastes the least
 // tile area over the images it convolves, or, for large single-precision
@@ -43,7 +44,8 @@ struct Shape {
 __host__ __device__ constexpr Shape shape_of(bool dbl, int id)
 {
 	return dbl ? Shape{16, 8, 4}
-	           : (id == 1 ? Shape{14, 14, 5} : (id == 2 ? Shape{16, 12, 8} : (id == 3 ? Shape{14, 10, 7} : Shape{16, 16, 8})));
+	           : (id == 1 ? Shape{14, 14, 5}
+	              : (id == 2 ? Shape{16, 12, 8} : (id == 3 ? Shape{14, 10, 7} : (id == 4 ? Shape{35, 7, 8} : Shape{16, 16, 8}))));
 }
 
 template <typename T>
@@ -215,7 +217,7 @@ conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restri
 template <typename T>
 int conv_num_shapes()
 {
-	return std::is_same<T, double>::value ? 1 : 4;
+	return std::is_same<T, double>::value ? 1 : 5;
 }
 
 template <typename T>
@@ -269,6 +271,7 @@ cudaError_t conv_configure<float>(size_t smem, int shape)
 	if (shape == 1) return configure_shape<float, 14, 14, 5>(smem);
 	if (shape == 2) return configure_shape<float, 16, 12, 8>(smem);
 	if (shape == 3) return configure_shape<float, 14, 10, 7>(smem);
+	if (shape == 4) return configure_shape<float, 35, 7, 8>(smem);
 	return configure_shape<float, 16, 16, 8>(smem);
 }
 
@@ -286,6 +289,7 @@ void launch_conv<float>(int mode, int shape, const ModelDev *models, int n_model
 	if (shape == 1) launch_shape<float, 14, 14, 5>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
 	else if (shape == 2) launch_shape<float, 16, 12, 8>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
 	else if (shape == 3) launch_shape<float, 14, 10, 7>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
+	else if (shape == 4) launch_shape<float, 35, 7, 8>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
 	else launch_shape<float, 16, 16, 8>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
 }
 
