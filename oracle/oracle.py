@@ -66,7 +66,7 @@ class OrcModel(ctypes.Structure):
                 ("psf", ctypes.POINTER(ctypes.c_double)), ("psf_w", ctypes.c_uint),
                 ("psf_h", ctypes.c_uint), ("psf_scale_x", ctypes.c_double),
                 ("psf_scale_y", ctypes.c_double), ("mask", ctypes.POINTER(ctypes.c_ubyte)),
-                ("convolver", ctypes.c_int), ("omp_threads", ctypes.c_int)]
+                ("adjust_mask", ctypes.c_int), ("convolver", ctypes.c_int), ("omp_threads", ctypes.c_int)]
 
 
 class OrcConstants(ctypes.Structure):
@@ -153,7 +153,7 @@ class Case:
 
     def __init__(self, width, height, profiles, psf=None, scale=(1.0, 1.0), magzero=0.0,
                  finesampling=1, return_finesampled=True, convolver="brute", psf_scale=(1.0, 1.0),
-                 mask=None):
+                 mask=None, adjust_mask=True):
         self.width, self.height = width, height
         self.profiles = profiles
         self.psf = None if psf is None else np.ascontiguousarray(psf, dtype=np.float64)
@@ -163,7 +163,10 @@ class Case:
         self.return_finesampled = return_finesampled
         self.convolver = convolver
         self.psf_scale = psf_scale
+        # adjust_mask (the reference's default): mask of the model's dimensions,
+        # adjusted as Model::evaluate does; otherwise of the drawing dimensions
         self.mask = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        self.adjust_mask = adjust_mask
 
     def c_model(self, threads=1):
         m = OrcModel()
@@ -178,6 +181,7 @@ class Case:
         m.psf_scale_x, m.psf_scale_y = self.psf_scale
         if self.mask is not None:
             m.mask = self.mask.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte))
+        m.adjust_mask = int(bool(self.adjust_mask))
         m.convolver = 1 if self.convolver == "brute_old" else 0
         m.omp_threads = threads
         return m

@@ -705,8 +705,97 @@ int orc_profile_constants(const orc_model *m, const orc_profile *pp, orc_constan
 	return 0;
 }
 
-/* Model::analyze_inputs / analyze_expansion_requirements without an
- * adjustable mask (src/model.cpp:152-219) */
+/* Model::analyze_expansion_requirements (src/model.cpp:152-184): the PSF
+ * padding, and what the mask needs. With an adjustable mask and convolution,
+ * the padding is needed only if the mask's bounding box (times the
+ * finesampling) lies closer than half the PSF to an edge. */
+typedef struct {
+	unsigned int pad_x, pad_y;
+	int mask_needs_convolution, mask_needs_psf_padding, mask_needs_adjustment;
+} expansion_t;
+
+static expansion_t analyze_expansion(const orc_model *m, int conv, unsigned int fs)
+{
+	expansion_t e = {0, 0, 0, 0, 0};
+	int needs_padding = conv;
+	if (m->mask && m->adjust_mask && conv) {
+		/* Surface::bounding_box (include/profit/image.h:472-501): [lb, ub) of
+		 * the non-zero pixels, empty (all zero) for an all-zero mask */
+		unsigned int lbx = m->width, lby = m->height, ubx = 0, uby = 0, i, j;
+		int any = 0;
+		for (j = 0; j < m->height; j++) {
+			for (i = 0; i < m->width; i++) {
+				if (!m->mask[i + (size_t)j * m->width]) continue;
+				if (i < lbx) lbx = i;
+				if (j < lby) lby = j;
+				if (i + 1 > ubx) ubx = i + 1;
+				if (j + 1 > uby) uby = j + 1;
+				any = 1;
+			}
+		}
+		if (!any) lbx = lby = ubx = uby = 0;
+		{
+			const unsigned int lowx = lbx * fs, lowy = lby * fs;
+			const unsigned int upx = m->width * fs - ubx * fs, upy = m->height * fs - uby * fs;
+			const unsigned int nx = m->psf_w / 2, ny = m->psf_h / 2;
+			needs_padding = !(lowx >= nx && lowy >= ny) || !(upx >= nx && upy >= ny);
+		}
+		e.mask_needs_convolution = 1;
+		e.mask_needs_psf_padding = needs_padding;
+	}
+	if (needs_padding) {
+		e.pad_x = m->psf_w / 2;
+		e.pad_y = m->psf_h / 2;
+	}
+	/* Model::needs_adjustment (src/model.cpp:221-228) */
+	e.mask_needs_adjustment = m->mask && m->adjust_mask &&
+	                          (e.mask_needs_convolution || e.mask_needs_psf_padding || fs > 1);
+	return e;
+}
+
+/* Model::adjust (src/model.cpp:230-246): the mask upsampled by the
+ * finesampling (Mask::upsample, src/image.cpp:51-65), extended by the PSF
+ * padding (Surface::extend) and expanded by half the PSF (Mask::expand_by,
+ * src/image.cpp:112-160: a drawing pixel is set if any mask pixel within
+ * half the PSF is). Returns a new dw x dh mask. */
+static unsigned char *adjusted_mask(const orc_model *m, const expansion_t *e, unsigned int fs, unsigned int dw,
+                                    unsigned int dh)
+{
+	const unsigned int uw = m->width * fs, uh = m->height * fs;
+	unsigned char *a = (unsigned char *)calloc((size_t)dw * dh, 1), *b;
+	unsigned int i, j;
+	for (j = 0; j < uh; j++) {
+		for (i = 0; i < uw; i++) {
+			a[(i + e->pad_x) + (size_t)(j + e->pad_y) * dw] = m->mask[i / fs + (size_t)(j / fs) * m->width] != 0;
+		}
+	}
+	if (!e->mask_needs_convolution) return a;
+	b = (unsigned char *)calloc((size_t)dw * dh, 1);
+	{
+		const unsigned int px = m->psf_w / 2, py = m->psf_h / 2;
+		for (j = 0; j < dh; j++) {
+			for (i = 0; i < dw; i++) {
+				const unsigned int y0 = j >= py ? j - py : 0, y1 = j + py < dh ? j + py : dh - 1;
+				const unsigned int x0 = i >= px ? i - px : 0, x1 = i + px < dw ? i + px : dw - 1;
+				unsigned int x, y;
+				int set = a[i + (size_t)j * dw];
+				for (y = y0; y <= y1 && !set; y++) {
+					for (x = x0; x <= x1; x++) {
+						if (a[x + (size_t)y * dw]) {
+							set = 1;
+							break;
+						}
+					}
+				}
+				b[i + (size_t)j * dw] = (unsigned char)set;
+			}
+		}
+	}
+	free(a);
+	return b;
+}
+
+/* Model::analyze_inputs (src/model.cpp:186-219) */
 int orc_output_dims(const orc_model *m, const orc_profile *profiles, int n_profiles,
                     unsigned int *out_w, unsigned int *out_h, unsigned int *draw_w, unsigned int *draw_h)
 {
@@ -725,9 +814,10 @@ int orc_output_dims(const orc_model *m, const orc_profile *profiles, int n_profi
 	for (i = 0; i < n_profiles; i++) {
 		if (validate_profile(&profiles[i], m)) return -1;
 	}
-	if (conv) {
-		pad_x = m->psf_w / 2;
-		pad_y = m->psf_h / 2;
+	{
+		const expansion_t e = analyze_expansion(m, conv, fs);
+		pad_x = e.pad_x;
+		pad_y = e.pad_y;
 	}
 	*draw_w = m->width * fs + 2 * pad_x;
 	*draw_h = m->height * fs + 2 * pad_y;
@@ -748,6 +838,8 @@ int orc_evaluate(const orc_model *m, const orc_profile *profiles, int n_profiles
 	unsigned int ow, oh, dw, dh, pad_x = 0, pad_y = 0, fs = m->finesampling ? m->finesampling : 1;
 	int i, conv = 0;
 	size_t npix;
+	const unsigned char *mask = NULL;
+	unsigned char *adj = NULL;
 	double *model_image, *to_convolve = NULL, *psf = NULL;
 	double sx, sy;
 	int threads = m->omp_threads;
@@ -758,9 +850,15 @@ int orc_evaluate(const orc_model *m, const orc_profile *profiles, int n_profiles
 	for (i = 0; i < n_profiles; i++) {
 		conv |= profiles[i].convolve != 0;
 	}
-	if (conv) {
-		pad_x = m->psf_w / 2;
-		pad_y = m->psf_h / 2;
+	{
+		const expansion_t e = analyze_expansion(m, conv, fs);
+		pad_x = e.pad_x;
+		pad_y = e.pad_y;
+		/* the mask the profiles and the convolution see: adjusted (Model::evaluate,
+		 * src/model.cpp:269-286), as given, or none */
+		if (m->mask && m->adjust_mask && e.mask_needs_adjustment) mask = adj = adjusted_mask(m, &e, fs, dw, dh);
+		else if (m->mask && m->adjust_mask) mask = m->mask;  /* no adjustment: model = drawing dims */
+		else mask = m->mask;
 	}
 	npix = (size_t)dw * dh;
 	model_image = (double *)calloc(npix, sizeof(double));
@@ -774,9 +872,6 @@ int orc_evaluate(const orc_model *m, const orc_profile *profiles, int n_profiles
 		psf = (double *)malloc(sizeof(double) * np);
 		for (q = 0; q < np; q++) sum += m->psf[q];
 		for (q = 0; q < np; q++) psf[q] = sum > 0 ? m->psf[q] / sum : m->psf[q];
-	}
-	if (m->mask) {
-		/* the mask is taken as already adjusted to the drawing dimensions */
 	}
 	sx = m->scale_x / fs;
 	sy = m->scale_y / fs;
@@ -795,7 +890,7 @@ int orc_evaluate(const orc_model *m, const orc_profile *profiles, int n_profiles
 			r.yc = r.ycen + pad_y * sy;
 			r.depth = depth ? depth + (size_t)i * npix : NULL;
 			r.depth_w = dw;
-			evaluate_radial(&r, target, dw, dh, m->mask, sx, sy, threads);
+			evaluate_radial(&r, target, dw, dh, mask, sx, sy, threads);
 			if (level_counts) {
 				memcpy(level_counts + (size_t)i * 32, r.counts, sizeof(r.counts));
 			}
@@ -804,7 +899,7 @@ int orc_evaluate(const orc_model *m, const orc_profile *profiles, int n_profiles
 			double bg = pp->par[6] / (fs * fs);
 			size_t q;
 			for (q = 0; q < npix; q++) {
-				if (m->mask && !m->mask[q]) continue;
+				if (mask && !mask[q]) continue;
 				target[q] += bg;
 			}
 		}
@@ -826,9 +921,9 @@ int orc_evaluate(const orc_model *m, const orc_profile *profiles, int n_profiles
 			unsigned char *emask = NULL;
 			unsigned int a, b;
 			for (b = 0; b < dh; b++) for (a = 0; a < dw; a++) ext[a + (size_t)b * nx] = to_convolve[a + (size_t)b * dw];
-			if (m->mask) {
+			if (mask) {
 				emask = (unsigned char *)calloc((size_t)nx * ny, 1);
-				for (b = 0; b < dh; b++) for (a = 0; a < dw; a++) emask[a + (size_t)b * nx] = m->mask[a + (size_t)b * dw];
+				for (b = 0; b < dh; b++) for (a = 0; a < dw; a++) emask[a + (size_t)b * nx] = mask[a + (size_t)b * dw];
 			}
 			orc_convolve_brute(ext, nx, ny, psf, m->psf_w, m->psf_h, emask, res, m->convolver == 1, threads);
 			for (b = 0; b < dh; b++) for (a = 0; a < dw; a++) to_convolve[a + (size_t)b * dw] = res[a + (size_t)b * nx];
@@ -839,7 +934,7 @@ int orc_evaluate(const orc_model *m, const orc_profile *profiles, int n_profiles
 		}
 		else {
 			conv_out = (double *)malloc(sizeof(double) * npix);
-			orc_convolve_brute(to_convolve, dw, dh, psf, m->psf_w, m->psf_h, m->mask, conv_out, m->convolver == 1, threads);
+			orc_convolve_brute(to_convolve, dw, dh, psf, m->psf_w, m->psf_h, mask, conv_out, m->convolver == 1, threads);
 			free(to_convolve);
 			to_convolve = conv_out;
 		}
@@ -870,10 +965,24 @@ int orc_evaluate(const orc_model *m, const orc_profile *profiles, int n_profiles
 			}
 		}
 	}
+	/* image &= mask after an adjustment (src/model.cpp:313-317): the model's
+	 * own mask over the output. (For finesampled output the reference's
+	 * element-wise product runs past the smaller mask, undefined; here output
+	 * pixel (x, y) takes mask pixel (x / fs, y / fs).) */
+	if (adj) {
+		unsigned int a, b;
+		const unsigned int f = (fs > 1 && m->return_finesampled) ? fs : 1;
+		for (b = 0; b < oh; b++) {
+			for (a = 0; a < ow; a++) {
+				if (!m->mask[a / f + (size_t)(b / f) * m->width]) out[a + (size_t)b * ow] = 0;
+			}
+		}
+	}
 	*out_w = ow;
 	*out_h = oh;
 	free(model_image);
 	free(to_convolve);
 	free(psf);
+	free(adj);
 	return 0;
 }

@@ -81,8 +81,14 @@ typedef struct {
 	const double *psf;
 	unsigned int psf_w, psf_h;
 	double psf_scale_x, psf_scale_y;
-	/* optional calculation mask of drawing dimensions (1 = evaluate), or NULL */
+	/* optional calculation mask (non-zero = evaluate), or NULL. With
+	 * adjust_mask (the reference's default, Model::set_adjust_mask) it has the
+	 * model's dimensions and is adjusted as Model::evaluate does
+	 * (src/model.cpp:152-257: padding decided by its bounding box, upsampled,
+	 * extended, expanded by half the PSF) and the final image is masked by it;
+	 * without, it has the drawing dimensions and is used as given. */
 	const unsigned char *mask;
+	int adjust_mask;
 	/* 0: BRUTE (associative row dot products), 1: BRUTE_OLD */
 	int convolver;
 	int omp_threads;

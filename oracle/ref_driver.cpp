@@ -122,6 +122,18 @@ extern "C" int ref_evaluate(const orc_model *m, const orc_profile *profiles, int
 			auto p = model.add_profile(kind_name(profiles[i].kind));
 			set_params(p, profiles[i]);
 		}
+		if (m->mask) {
+			// Model::set_mask with the model's dimensions (the reference's
+			// adjustable mask); a mask of drawing dimensions is not driven here
+			if (!m->adjust_mask) {
+				std::strncpy(err, "the driver takes adjustable masks only", err_len);
+				return -3;
+			}
+			std::vector<bool> mk((size_t)m->width * m->height);
+			for (size_t q = 0; q < mk.size(); q++) mk[q] = m->mask[q] != 0;
+			model.set_mask(profit::Mask(mk, m->width, m->height));
+			model.set_adjust_mask(true);
+		}
 		profit::Image image = model.evaluate();
 		auto dims = image.getDimensions();
 		if ((size_t)dims.x * dims.y > out_cap) {

@@ -83,6 +83,41 @@ def golden_cases():
         ("king", dict(xcen=25.5, ycen=24.5, rc=2.0, rt=12.0, convolve=True))])
     c["conv_even_psf"] = dict(width=45, height=50, psf=[[0.0, 1.0], [2.0, 3.0]], profiles=[
         ("sersic", dict(xcen=30.0, ycen=10.0, re=16.0, convolve=True))])
+    # calculation masks (Model::set_mask, adjusted by Model::evaluate,
+    # src/model.cpp:152-257): far from the edges (no PSF padding needed), on
+    # an edge (padding needed), without convolution, finesampled and
+    # SUM-downsampled, with sky and psf profiles, all zero, and random
+    rng = np.random.default_rng(77)
+    central = np.zeros((60, 60), np.uint8)
+    central[15:45, 12:48] = 1
+    c["mask_central_conv"] = dict(width=60, height=60, psf="psf15_moffat", mask=central.tolist(), profiles=[
+        ("sersic", dict(xcen=30.3, ycen=29.6, mag=16, re=6, nser=3.5, ang=20, axrat=0.7, convolve=True))])
+    edge = np.zeros((50, 60), np.uint8)
+    edge[0:21, 30:60] = 1
+    c["mask_edge_conv"] = dict(width=60, height=50, psf="psf15_moffat", mask=edge.tolist(), profiles=[
+        ("sersic", dict(xcen=44.2, ycen=10.7, mag=16, re=5, nser=2.2, ang=60, axrat=0.5, convolve=True))])
+    c["mask_nopsf"] = dict(width=50, height=50, mask=(rng.random((50, 50)) < 0.7).astype(np.uint8).tolist(),
+                           profiles=[("sersic", dict(xcen=24.6, ycen=25.3, re=4.0, nser=2.5))])
+    fsm = np.zeros((30, 40), np.uint8)
+    fsm[8:24, 10:33] = 1
+    c["mask_fs_downsampled"] = dict(width=40, height=30, finesampling=2, return_finesampled=False,
+                                    psf="psf15_moffat", mask=fsm.tolist(), profiles=[
+        ("moffat", dict(xcen=21.0, ycen=13.5, fwhm=3.0, con=2.2, convolve=True))])
+    sky = np.ones((40, 50), np.uint8)
+    sky[:, :9] = 0
+    sky[31:, :] = 0
+    c["mask_sky_psf_profile"] = dict(width=50, height=40, psf="psf15_moffat", mask=sky.tolist(), profiles=[
+        ("sersic", dict(xcen=25.5, ycen=19.0, mag=17, re=4, nser=1.5, convolve=True)),
+        ("sky", dict(bg=2e-3)),
+        ("psf", dict(xcen=40.2, ycen=12.6, mag=18))])
+    c["mask_all_zero"] = dict(width=30, height=30, psf="psf15_moffat", mask=np.zeros((30, 30), np.uint8).tolist(),
+                              profiles=[("sersic", dict(xcen=15.0, ycen=15.0, re=4, convolve=True))])
+    c["mask_random_conv"] = dict(width=64, height=56, psf="psf15_moffat",
+                                 mask=(rng.random((56, 64)) < 0.5).astype(np.uint8).tolist(), profiles=[
+        ("sersic", dict(xcen=30.1, ycen=25.9, mag=16, re=8, nser=4, ang=35, axrat=0.6, convolve=True)),
+        ("sersic", dict(xcen=36.4, ycen=30.2, mag=15.5, re=14, nser=1, ang=110, axrat=0.4, box=0.1,
+                        convolve=True)),
+        ("sky", dict(bg=1e-3))])
     return c
 
 

@@ -31,4 +31,5 @@ def to_case(O, entry):
                   scale=spec.get("scale", (1.0, 1.0)), magzero=spec.get("magzero", 0.0),
                   finesampling=spec.get("finesampling", 1),
                   return_finesampled=spec.get("return_finesampled", True),
-                  convolver=spec.get("convolver", "brute"))
+                  convolver=spec.get("convolver", "brute"),
+                  mask=None if spec.get("mask") is None else np.asarray(spec["mask"], dtype=np.uint8))
