@@ -123,6 +123,19 @@ typedef struct pf_model_desc {
 	double psf_scale_x, psf_scale_y;  /* set_psf_pixel_scale */
 	int32_t convolver;                /* pf_convolver */
 	int32_t reserved;
+	/* Calculation mask (Model::set_mask, include/profit/model.h:219-246): one
+	 * byte per pixel, non-zero = evaluate, at this offset in the mask pool of
+	 * pf_batch_create_masked (-1: none; pf_batch_create ignores it).
+	 * adjust_mask 1 (the reference's default): the mask has the model's
+	 * width x height and is adjusted as Model::evaluate does (PSF padding only
+	 * when the mask's bounding box needs it, upsampled by the finesampling,
+	 * expanded by half the PSF; the output image masked by it at the end,
+	 * src/model.cpp:152-257); 0: the mask has the drawing dimensions
+	 * (width x height times the finesampling, plus half the PSF on each side
+	 * when a profile is convolved) and is used as given. */
+	int64_t mask_offset;
+	int32_t adjust_mask;
+	int32_t reserved2;
 } pf_model_desc;
 
 typedef struct pf_env pf_env;
@@ -170,6 +183,11 @@ PF_API pf_status pf_model_output_dims(const pf_model_desc *model, const pf_profi
                                uint32_t *out_w, uint32_t *out_h);
 PF_API pf_status pf_model_evaluate(pf_env *env, const pf_model_desc *model, const pf_profile_desc *profiles,
                             const double *psf, double *image, uint32_t *out_w, uint32_t *out_h);
+/* The same with a calculation mask (host bytes; dimensions as the model's
+ * adjust_mask says; NULL: none). */
+PF_API pf_status pf_model_evaluate_masked(pf_env *env, const pf_model_desc *model, const pf_profile_desc *profiles,
+                                   const double *psf, const uint8_t *mask, double *image, uint32_t *out_w,
+                                   uint32_t *out_h);
 
 /*
  * Convolver::convolve with ConvolverType::CUDA and crop = true
@@ -225,6 +243,12 @@ PF_API pf_status pf_convolve_noalloc(pf_env *env, const double *src, uint32_t w,
 PF_API pf_status pf_batch_create(pf_env *env, const pf_model_desc *models, size_t n_models,
                           const pf_profile_desc *profiles, size_t n_profiles,
                           const double *psf_pool, size_t psf_pool_len, pf_batch **batch);
+/* pf_batch_create with calculation masks: each model's mask_offset (if not
+ * -1) points into mask_pool (host, mask_pool_len bytes). */
+PF_API pf_status pf_batch_create_masked(pf_env *env, const pf_model_desc *models, size_t n_models,
+                                 const pf_profile_desc *profiles, size_t n_profiles, const double *psf_pool,
+                                 size_t psf_pool_len, const uint8_t *mask_pool, size_t mask_pool_len,
+                                 pf_batch **batch);
 PF_API void pf_batch_destroy(pf_batch *batch);
 PF_API pf_status pf_batch_layout(const pf_batch *batch, uint64_t *offsets, uint32_t *dims,
                           uint64_t *total_pixels);
@@ -299,6 +323,10 @@ PF_API pf_status pf_batch_check(pf_batch *batch, void *stream);
 PF_API pf_status pf_batch_record_depth(pf_batch *batch, int enable);
 PF_API pf_status pf_batch_depth(pf_batch *batch, int8_t *depth, size_t depth_len,
                          int64_t *level_counts /* n_profiles * 32 */);
+/* Per model the drawing area (width, height) the depth maps cover: the model's
+ * dimensions times the finesampling plus the PSF padding, which an adjustable
+ * mask far enough from the edges leaves out. `dims` holds 2 * n_models. */
+PF_API pf_status pf_batch_drawing_dims(pf_batch *batch, uint32_t *dims);
 
 #ifdef __cplusplus
 }

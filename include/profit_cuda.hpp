@@ -305,6 +305,11 @@ public:
 	void set_psf(const Image &psf) { m_psf = psf; }
 	void set_cuda_env(const CUDAEnvPtr &env) { m_env = env; }
 	CUDAEnvPtr get_cuda_env() const { return m_env; }
+	/* Model::set_mask / set_adjust_mask (include/profit/model.h:219-246): one
+	 * byte per pixel, non-zero = evaluate; model dimensions when adjusted
+	 * (the default), the drawing dimensions otherwise. Empty: no mask. */
+	void set_mask(const std::vector<uint8_t> &mask) { m_mask = mask; }
+	void set_adjust_mask(bool adjust) { m_adjust_mask = adjust; }
 
 	Image evaluate()
 	{
@@ -315,8 +320,8 @@ public:
 		uint32_t w = 0, h = 0;
 		check(pf_model_output_dims(&m, profs.data(), &w, &h));
 		Image out(w, h);
-		check(pf_model_evaluate(m_env->get(), &m, profs.data(), m_psf.size() ? m_psf.data() : nullptr, out.data(),
-		                        &w, &h));
+		check(pf_model_evaluate_masked(m_env->get(), &m, profs.data(), m_psf.size() ? m_psf.data() : nullptr,
+		                               m_mask.empty() ? nullptr : m_mask.data(), out.data(), &w, &h));
 		return out;
 	}
 
@@ -338,6 +343,8 @@ public:
 		m.psf_scale_x = m_psf_scale.first;
 		m.psf_scale_y = m_psf_scale.second;
 		m.convolver = PF_CONV_AUTO;
+		m.mask_offset = m_mask.empty() ? -1 : 0;
+		m.adjust_mask = m_adjust_mask ? 1 : 0;
 		return m;
 	}
 
@@ -347,6 +354,8 @@ private:
 	double m_magzero = 0.0;
 	unsigned int m_finesampling = 1;
 	bool m_return_finesampled = true;
+	bool m_adjust_mask = true;
+	std::vector<uint8_t> m_mask;
 	Image m_psf;
 	CUDAEnvPtr m_env;
 	std::vector<ProfilePtr> m_profiles;

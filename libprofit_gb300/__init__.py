@@ -271,6 +271,8 @@ class Model:
         self.return_finesampled = True
         self.env = None
         self.convolver = _ffi.PF_CONV_AUTO
+        self.mask = None
+        self.adjust_mask = True
 
     def add_profile(self, name):
         p = Profile(name)
@@ -303,6 +305,16 @@ class Model:
     def set_cuda_env(self, env):
         self.env = env
 
+    def set_mask(self, mask):
+        """Model::set_mask: a boolean (height, width) calculation mask (True =
+        evaluate), of the model's dimensions (or of the drawing dimensions when
+        set_adjust_mask(False)); None removes it."""
+        self.mask = None if mask is None else np.ascontiguousarray(np.asarray(mask) != 0, dtype=np.uint8)
+
+    def set_adjust_mask(self, adjust):
+        """Model::set_adjust_mask (default True)."""
+        self.adjust_mask = bool(adjust)
+
     def set_convolver(self, convolver):
         """A Convolver from create_convolver, or "auto", "brute" or "fft"."""
         names = {"auto": _ffi.PF_CONV_AUTO, "brute": _ffi.PF_CONV_BRUTE, "cuda": _ffi.PF_CONV_BRUTE,
@@ -316,7 +328,7 @@ class Model:
         else:
             self.convolver = int(convolver)
 
-    def _descs(self, first_profile=0, psf_offset=None):
+    def _descs(self, first_profile=0, psf_offset=None, mask_offset=None):
         m = _ffi.ModelDesc()
         m.width, m.height = self.width, self.height
         m.scale_x, m.scale_y = self.scale
@@ -332,6 +344,8 @@ class Model:
             m.psf_offset = -1
         m.psf_scale_x, m.psf_scale_y = self.psf_scale
         m.convolver = self.convolver
+        m.mask_offset = -1 if self.mask is None else (0 if mask_offset is None else mask_offset)
+        m.adjust_mask = int(self.adjust_mask)
         profs = (_ffi.ProfileDesc * max(1, len(self.profiles)))()
         for i, p in enumerate(self.profiles):
             profs[i] = p.desc
@@ -351,9 +365,10 @@ class Model:
         out = np.zeros(w * h, dtype=np.float64)
         ow, oh = ctypes.c_uint32(), ctypes.c_uint32()
         psf_ptr = None if self.psf is None else self.psf.ctypes.data_as(ctypes.c_void_p)
-        _check(_ffi.load().pf_model_evaluate(env.handle, ctypes.byref(m), profs, psf_ptr,
-                                             out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ow),
-                                             ctypes.byref(oh)))
+        mask_ptr = None if self.mask is None else self.mask.ctypes.data_as(ctypes.c_void_p)
+        _check(_ffi.load().pf_model_evaluate_masked(env.handle, ctypes.byref(m), profs, psf_ptr, mask_ptr,
+                                                    out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ow),
+                                                    ctypes.byref(oh)))
         return out.reshape(oh.value, ow.value)
 
 
@@ -396,10 +411,11 @@ class Batch:
         n_prof = sum(len(m.profiles) for m in self.models)
         mds = (_ffi.ModelDesc * max(1, len(self.models)))()
         pds = (_ffi.ProfileDesc * max(1, n_prof))()
-        psfs = []
-        first, psf_off = 0, 0
+        psfs, masks = [], []
+        first, psf_off, mask_off = 0, 0, 0
         for i, m in enumerate(self.models):
-            md, pd = m._descs(first_profile=first, psf_offset=psf_off if m.psf is not None else None)
+            md, pd = m._descs(first_profile=first, psf_offset=psf_off if m.psf is not None else None,
+                              mask_offset=mask_off if m.mask is not None else None)
             mds[i] = md
             for j in range(len(m.profiles)):
                 pds[first + j] = pd[j]
@@ -407,13 +423,19 @@ class Batch:
             if m.psf is not None:
                 psfs.append(m.psf.ravel())
                 psf_off += m.psf.size
+            if m.mask is not None:
+                masks.append(m.mask.ravel())
+                mask_off += m.mask.size
         self.psf_pool = np.ascontiguousarray(np.concatenate(psfs) if psfs else np.zeros(0), dtype=np.float64)
+        self.mask_pool = np.ascontiguousarray(np.concatenate(masks) if masks else np.zeros(0), dtype=np.uint8)
         self.n_profiles = n_prof
         h = ctypes.c_void_p()
         lib = _ffi.load()
-        _check(lib.pf_batch_create(self.env.handle, mds, len(self.models), pds, n_prof,
-                                   self.psf_pool.ctypes.data_as(ctypes.c_void_p) if self.psf_pool.size else None,
-                                   self.psf_pool.size, ctypes.byref(h)))
+        _check(lib.pf_batch_create_masked(
+            self.env.handle, mds, len(self.models), pds, n_prof,
+            self.psf_pool.ctypes.data_as(ctypes.c_void_p) if self.psf_pool.size else None, self.psf_pool.size,
+            self.mask_pool.ctypes.data_as(ctypes.c_void_p) if self.mask_pool.size else None, self.mask_pool.size,
+            ctypes.byref(h)))
         self._h = h
         n = len(self.models)
         offs = (ctypes.c_uint64 * (n + 1))()
@@ -480,9 +502,11 @@ class Batch:
 
     def depth(self):
         """Per profile: (depth map over its model's drawing area, 32 level counts)."""
+        dims = np.zeros(2 * max(1, len(self.models)), dtype=np.uint32)
+        _check(_ffi.load().pf_batch_drawing_dims(self._h, dims.ctypes.data_as(ctypes.c_void_p)))
         sizes = []
         for m_idx, m in enumerate(self.models):
-            w, h = _drawing_dims(m)
+            w, h = int(dims[2 * m_idx]), int(dims[2 * m_idx + 1])
             sizes += [(h, w)] * len(m.profiles)
         total = sum(h * w for h, w in sizes)
         buf = np.zeros(max(1, total), dtype=np.int8)
@@ -527,10 +551,3 @@ def _stream_arg(stream):
     if hasattr(stream, "cuda_stream"):
         stream = stream.cuda_stream
     return ctypes.c_void_p(stream if stream else _CUDA_STREAM_LEGACY)
-
-
-def _drawing_dims(model):
-    conv = any(p.desc.convolve for p in model.profiles)
-    px = model.psf.shape[1] // 2 if (conv and model.psf is not None) else 0
-    py = model.psf.shape[0] // 2 if (conv and model.psf is not None) else 0
-    return model.width * model.finesampling + 2 * px, model.height * model.finesampling + 2 * py

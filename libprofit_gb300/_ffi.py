@@ -47,7 +47,8 @@ class ModelDesc(ctypes.Structure):
                 ("n_profiles", ctypes.c_uint32), ("psf_offset", ctypes.c_int64),
                 ("psf_w", ctypes.c_uint32), ("psf_h", ctypes.c_uint32),
                 ("psf_scale_x", ctypes.c_double), ("psf_scale_y", ctypes.c_double),
-                ("convolver", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("convolver", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("mask_offset", ctypes.c_int64), ("adjust_mask", ctypes.c_int32), ("reserved2", ctypes.c_int32)]
 
 
 class StageTimes(ctypes.Structure):
@@ -71,6 +72,9 @@ _SIGNATURES = {
                                             ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]),
     "pf_model_evaluate": (ctypes.c_int, [_P, ctypes.POINTER(ModelDesc), ctypes.POINTER(ProfileDesc), _P, _P,
                                          ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]),
+    "pf_model_evaluate_masked": (ctypes.c_int, [_P, ctypes.POINTER(ModelDesc), ctypes.POINTER(ProfileDesc), _P,
+                                                _P, _P, ctypes.POINTER(ctypes.c_uint32),
+                                                ctypes.POINTER(ctypes.c_uint32)]),
     "pf_convolve": (ctypes.c_int, [_P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_uint32,
                                    ctypes.c_uint32, _P, _P]),
     "pf_convolve_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_uint32,
@@ -78,6 +82,9 @@ _SIGNATURES = {
     "pf_batch_create": (ctypes.c_int, [_P, ctypes.POINTER(ModelDesc), ctypes.c_size_t,
                                        ctypes.POINTER(ProfileDesc), ctypes.c_size_t, _P, ctypes.c_size_t,
                                        ctypes.POINTER(_P)]),
+    "pf_batch_create_masked": (ctypes.c_int, [_P, ctypes.POINTER(ModelDesc), ctypes.c_size_t,
+                                              ctypes.POINTER(ProfileDesc), ctypes.c_size_t, _P, ctypes.c_size_t,
+                                              _P, ctypes.c_size_t, ctypes.POINTER(_P)]),
     "pf_batch_destroy": (None, [_P]),
     "pf_batch_layout": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(ctypes.c_uint64)]),
     "pf_batch_set_params": (ctypes.c_int, [_P, _P]),
@@ -90,6 +97,7 @@ _SIGNATURES = {
     "pf_step_graph": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "pf_batch_record_depth": (ctypes.c_int, [_P, ctypes.c_int]),
     "pf_batch_depth": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
+    "pf_batch_drawing_dims": (ctypes.c_int, [_P, _P]),
 }
 
 _lib = None

@@ -93,8 +93,10 @@ __global__ void chi2_kernel(const ModelDev *__restrict__ models, const T *__rest
 	T s = 0, comp = 0;
 	for (long long i = threadIdx.x; i < n; i += blockDim.x) {
 		const long long g = m.out_off + i;
+		// output pixels the final masking zeroes do not depend on the parameters
+		const bool live = kept(m, (int)(i % m.out_w), (int)(i / m.out_w));
 		if (cot) {
-			gout[g] = cot[g];
+			gout[g] = live ? cot[g] : (T)0;
 		}
 		else {
 			const T r = img[g] - data[g];
@@ -104,7 +106,7 @@ __global__ void chi2_kernel(const ModelDev *__restrict__ models, const T *__rest
 			const T t = s + y;
 			comp = (t - s) - y;
 			s = t;
-			gout[g] = (T)2 * wr;
+			gout[g] = live ? (T)2 * wr : (T)0;
 		}
 	}
 	__shared__ double part[256];
@@ -506,7 +508,8 @@ __device__ void backward_row(const ModelDev &m, const ProfileDev &P, int row, in
 	for (int tcol = c0; tcol <= c1; tcol++) {
 		if (tcol >= s0 && tcol <= s1) continue;
 		const int px = tcol * 32 + lane;
-		const bool active = px < (int)m.draw_w;
+		// masked drawing pixels were not evaluated: no gradient from them
+		const bool active = px < (int)m.draw_w && evaluated(m, px, row);
 		T g = 0;
 		if (active) {
 			g = gimg ? gimg[(size_t)row * m.draw_w + px] : g_direct(m, gout, px, row);

@@ -77,6 +77,7 @@ __device__ __forceinline__ T cot_at(const ModelDev &m, const T *gout, int x, int
 {
 	const int cx = x - (int)m.pad_x, cy = y - (int)m.pad_y;
 	if (cx < 0 || cy < 0 || cx >= (int)m.crop_w || cy >= (int)m.crop_h) return (T)0;
+	if (!evaluated(m, x, y)) return (T)0;  // the forward convolution is zero there
 	if (m.fs > 1 && !m.return_fs) return gout[m.out_off + (size_t)(cy / m.fs) * m.out_w + cx / m.fs];
 	return gout[m.out_off + (size_t)cy * m.out_w + cx];
 }
@@ -200,9 +201,16 @@ conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restri
 				const int x = xo + c;
 				if (x >= ow) continue;
 				if (MODE == CONV_FORWARD) {
-					const T v = direct[m.draw_off + (size_t)(yo + m.pad_y) * m.draw_w + x + m.pad_x] + acc[r][c];
-					if (m.fs > 1 && !m.return_fs) atomicAdd(&out[m.out_off + (size_t)(yo / m.fs) * m.out_w + x / m.fs], v);
-					else out[m.out_off + (size_t)yo * m.out_w + x] = v;
+					// the convolution is zero where the calculation mask is, and the
+					// output is multiplied by the model's mask at the end
+					const bool conv_here = evaluated(m, x + (int)m.pad_x, yo + (int)m.pad_y);
+					const T v = direct[m.draw_off + (size_t)(yo + m.pad_y) * m.draw_w + x + m.pad_x] +
+					            (conv_here ? acc[r][c] : (T)0);
+					if (m.fs > 1 && !m.return_fs) {
+						if (kept(m, x / (int)m.fs, yo / (int)m.fs))
+							atomicAdd(&out[m.out_off + (size_t)(yo / m.fs) * m.out_w + x / m.fs], v);
+					}
+					else out[m.out_off + (size_t)yo * m.out_w + x] = kept(m, x, yo) ? v : (T)0;
 				}
 				else {
 					out[m.draw_off + (size_t)yo * m.draw_w + x] = acc[r][c];

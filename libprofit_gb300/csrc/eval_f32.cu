@@ -315,6 +315,7 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 	const int col1 = min(col0 + 31, (int)m.draw_w - 1);
 	const unsigned int px = (unsigned int)col0 + lane;
 	const bool active = px < m.draw_w;
+	const bool in_mask = active && evaluated(m, (int)px, (int)row);  // the calculation mask (radial, sky)
 	const double *psf = m.psf_off >= 0 ? psf_pool + m.psf_off : nullptr;
 	// pixel centre (i + 1/2) * scale as an unevaluated float sum
 	const float cx = small_int_to_float(px) + 0.5f, cy = small_int_to_float(row) + 0.5f;
@@ -330,7 +331,7 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 		bool has = false;
 		if (P.kind == PF_SKY) {
 			add = P.fbg;
-			has = active;
+			has = in_mask;
 		}
 		else if (P.kind == PF_PSF) {
 			if (active && psf) has = psf_value(P, m, psf, px, row, add);
@@ -349,11 +350,12 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 			bool outside = rr > P.fswitch;
 			const bool amb = (P.frmax > 0.f && fabsf(rr - P.frmax) <= kGuardRadius * P.frmax) ||
 			                 fabsf(rr - P.fswitch) <= kGuardRadius * P.fswitch || !isfinite(rr);
-			if (amb && active) {
+			if (amb && in_mask) {
 				const unsigned int d = radius_f64(P, m, px, row);
 				beyond = (d & 1u) != 0;
 				outside = (d & 2u) != 0;
 			}
+			beyond |= !in_mask;  // masked pixels are not evaluated (src/radial.cpp:305-307)
 			float pixel_val = 0.f;
 			int depth = 0;
 			bool need_ss = false;

@@ -196,6 +196,7 @@ eval_tiles64_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 		const int col1 = min(col0 + 31, (int)m.draw_w - 1);
 		const unsigned int px = (unsigned int)col0 + lane;
 		const bool active = px < m.draw_w;
+		const bool in_mask = active && evaluated(m, (int)px, (int)row);  // the calculation mask (radial, sky)
 		const double sx = m.sx, sy = m.sy;
 		const double half_xbin = sx / 2.;
 		const double half_ybin = sy / 2.;
@@ -209,7 +210,7 @@ eval_tiles64_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 			bool has = false;
 			if (P.kind == PF_SKY) {
 				add = P.bg;
-				has = active;
+				has = in_mask;  // src/sky.cpp:42-45
 			}
 			else if (P.kind == PF_PSF) {
 				if (active && psf) {
@@ -228,7 +229,8 @@ eval_tiles64_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 				double pixel_val = 0;
 				int depth = 0;
 				bool need_ss = false;
-				if (P.rscale_max > 0 && r_prof / P.rscale > P.rscale_max) {
+				if (!in_mask || (P.rscale_max > 0 && r_prof / P.rscale > P.rscale_max)) {
+					// masked out (src/radial.cpp:305-307) or beyond rscale_max
 					pixel_val = 0.;
 					depth = -1;
 				}
@@ -323,12 +325,14 @@ __device__ __forceinline__ double conv_pixel64(const double *src, unsigned int s
 	return pixel;
 }
 
-// One drawing pixel of the final model image: model_image + convolved to_convolve.
+// One drawing pixel of the final model image: model_image + convolved
+// to_convolve, the convolution zero where the calculation mask is
+// (Convolver::convolve with a mask, src/convolve.cpp:55-99).
 __device__ __forceinline__ double drawn_pixel64(const ModelDev &m, const double *psf, const double *conv_img,
                                                 const double *direct_img, unsigned int dx, unsigned int dy)
 {
 	double v = direct_img[m.draw_off + (size_t)dy * m.draw_w + dx];
-	if (m.conv_required) {
+	if (m.conv_required && evaluated(m, (int)dx, (int)dy)) {
 		v += conv_pixel64(conv_img + m.draw_off, m.draw_w, m.draw_h, psf, m.psf_w, m.psf_h, dx, dy);
 	}
 	return v;
@@ -372,7 +376,7 @@ __global__ void finish64_kernel(const ModelDev *__restrict__ models, int n_model
 		else {
 			v = drawn_pixel64(m, psf, conv_img, direct_img, ox + m.pad_x, oy + m.pad_y);
 		}
-		out[g] = v;
+		out[g] = kept(m, (int)ox, (int)oy) ? v : 0.;  // image &= mask (src/model.cpp:313-317)
 	}
 }
 

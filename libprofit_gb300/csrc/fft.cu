@@ -217,9 +217,13 @@ __global__ void fft_irows_kernel(const ModelDev *__restrict__ models, const FftJ
 	for (int i = threadIdx.x; i < jb.count * (int)m.crop_w; i += blockDim.x) {
 		const int t = i / m.crop_w, c = i - t * m.crop_w;
 		const int r = jb.first + t;
-		const T v = direct[m.draw_off + (size_t)(r + m.pad_y) * m.draw_w + c + m.pad_x] + res[t * n + c + off_x].x * scale;
-		if (downsample) atomicAdd(&out[m.out_off + (size_t)(r / m.fs) * m.out_w + c / m.fs], v);
-		else out[m.out_off + (size_t)r * m.out_w + c] = v;
+		// the convolution zero where the calculation mask is; the model's mask at the end
+		const T conv = evaluated(m, c + (int)m.pad_x, r + (int)m.pad_y) ? res[t * n + c + off_x].x * scale : (T)0;
+		const T v = direct[m.draw_off + (size_t)(r + m.pad_y) * m.draw_w + c + m.pad_x] + conv;
+		if (downsample) {
+			if (kept(m, c / (int)m.fs, r / (int)m.fs)) atomicAdd(&out[m.out_off + (size_t)(r / m.fs) * m.out_w + c / m.fs], v);
+		}
+		else out[m.out_off + (size_t)r * m.out_w + c] = kept(m, c, r) ? v : (T)0;
 	}
 }
 

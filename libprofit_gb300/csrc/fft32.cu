@@ -169,9 +169,11 @@ struct Job {
 	int model, first, count, pad;
 };
 
-// cotangent of crop pixel (cx, cy) (SUM-downsampling aware)
+// cotangent of crop pixel (cx, cy) (SUM-downsampling aware; zero where the
+// calculation mask zeroed the forward convolution)
 __device__ __forceinline__ float cot_crop(const ModelDev &m, const float *gout, int cx, int cy)
 {
+	if (!evaluated(m, cx + (int)m.pad_x, cy + (int)m.pad_y)) return 0.f;
 	if (m.fs > 1 && !m.return_fs) return gout[m.out_off + (size_t)(cy / m.fs) * m.out_w + cx / m.fs];
 	return gout[m.out_off + (size_t)cy * m.out_w + cx];
 }
@@ -332,9 +334,15 @@ irows_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, 
 			const int r = jb.first + 2 * ff + half;
 			if (r >= jb.first + jb.count) continue;
 			const float2 z = buf[ff * PS + pidx(c + off_x)];
-			const float v = direct[m.draw_off + (size_t)(r + m.pad_y) * m.draw_w + c + m.pad_x] + (half ? z.y : z.x) * scale;
-			if (downsample) atomicAdd(&out[m.out_off + (size_t)(r / m.fs) * m.out_w + c / m.fs], v);
-			else out[m.out_off + (size_t)r * m.out_w + c] = v;
+			// the convolution is zero where the calculation mask is; the output
+			// is multiplied by the model's mask at the end
+			const float conv = evaluated(m, c + (int)m.pad_x, r + (int)m.pad_y) ? (half ? z.y : z.x) * scale : 0.f;
+			const float v = direct[m.draw_off + (size_t)(r + m.pad_y) * m.draw_w + c + m.pad_x] + conv;
+			if (downsample) {
+				if (kept(m, c / (int)m.fs, r / (int)m.fs))
+					atomicAdd(&out[m.out_off + (size_t)(r / m.fs) * m.out_w + c / m.fs], v);
+			}
+			else out[m.out_off + (size_t)r * m.out_w + c] = kept(m, c, r) ? v : 0.f;
 		}
 	}
 	else {

@@ -174,10 +174,14 @@ pf_status validate_profile(const pf_profile_desc &d, bool model_has_psf)
 struct Geometry {
 	uint32_t pad_x, pad_y, draw_w, draw_h, crop_w, crop_h, out_w, out_h;
 	bool conv;
+	// calculation mask (adjustable): what Model::evaluate does with it
+	bool mask_needs_convolution = false, mask_needs_psf_padding = false, mask_needs_adjustment = false;
 };
 
-// Model::analyze_inputs + analyze_expansion_requirements without a mask
-pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles, Geometry &g)
+// Model::analyze_inputs + analyze_expansion_requirements (src/model.cpp:152-219);
+// `mask` the model's calculation mask or null
+pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles, Geometry &g,
+                         const uint8_t *mask = nullptr)
 {
 	if (m.width == 0 || m.height == 0) return fail(PF_ERR_INVALID_PARAMETER, "Model's requested dimensions are 0");
 	if (m.scale_x <= 0) return fail(PF_ERR_INVALID_PARAMETER, "Model's scale_x cannot be negative or zero");
@@ -195,8 +199,33 @@ pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles
 		pf_status s = validate_profile(profiles[m.first_profile + i], has_psf);
 		if (s != PF_OK) return s;
 	}
-	g.pad_x = g.conv ? m.psf_w / 2 : 0;
-	g.pad_y = g.conv ? m.psf_h / 2 : 0;
+	// the PSF padding: with an adjustable mask, only when the mask's bounding
+	// box (times the finesampling) comes closer than half the PSF to an edge
+	bool padding = g.conv;
+	if (mask && m.adjust_mask && g.conv) {
+		uint32_t lbx = m.width, lby = m.height, ubx = 0, uby = 0;
+		bool any = false;
+		for (uint32_t j = 0; j < m.height; j++) {
+			for (uint32_t i = 0; i < m.width; i++) {
+				if (!mask[i + (size_t)j * m.width]) continue;
+				lbx = std::min(lbx, i);
+				lby = std::min(lby, j);
+				ubx = std::max(ubx, i + 1);
+				uby = std::max(uby, j + 1);
+				any = true;
+			}
+		}
+		if (!any) lbx = lby = ubx = uby = 0;
+		const uint32_t fs = m.finesampling, nx = m.psf_w / 2, ny = m.psf_h / 2;
+		const uint32_t lowx = lbx * fs, lowy = lby * fs, upx = (m.width - ubx) * fs, upy = (m.height - uby) * fs;
+		padding = !(lowx >= nx && lowy >= ny) || !(upx >= nx && upy >= ny);
+		g.mask_needs_convolution = true;
+		g.mask_needs_psf_padding = padding;
+	}
+	g.mask_needs_adjustment = mask && m.adjust_mask &&
+	                          (g.mask_needs_convolution || g.mask_needs_psf_padding || m.finesampling > 1);
+	g.pad_x = padding ? m.psf_w / 2 : 0;
+	g.pad_y = padding ? m.psf_h / 2 : 0;
 	g.crop_w = m.width * m.finesampling;
 	g.crop_h = m.height * m.finesampling;
 	g.draw_w = g.crop_w + 2 * g.pad_x;
@@ -208,6 +237,43 @@ pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles
 		g.out_h = (g.crop_h + m.finesampling - 1) / m.finesampling;
 	}
 	return PF_OK;
+}
+
+// The drawing-area mask the profiles and the convolution see (Model::adjust,
+// src/model.cpp:230-246): the model's mask upsampled by the finesampling
+// (Mask::upsample), extended by the PSF padding (Surface::extend) and, with
+// convolution, expanded by half the PSF (Mask::expand_by, src/image.cpp:
+// 112-160: a pixel is set if any mask pixel within half the PSF is; done here
+// as a separable box dilation, rows then columns, with running counts).
+void adjusted_mask(const pf_model_desc &m, const Geometry &g, const uint8_t *mask, std::vector<uint8_t> &out)
+{
+	const uint32_t fs = m.finesampling, dw = g.draw_w, dh = g.draw_h;
+	out.assign((size_t)dw * dh, 0);
+	for (uint32_t j = 0; j < g.crop_h; j++) {
+		for (uint32_t i = 0; i < g.crop_w; i++) {
+			out[(i + g.pad_x) + (size_t)(j + g.pad_y) * dw] = mask[i / fs + (size_t)(j / fs) * m.width] != 0;
+		}
+	}
+	if (!g.mask_needs_convolution) return;
+	const int px = (int)(m.psf_w / 2), py = (int)(m.psf_h / 2);
+	std::vector<uint8_t> rows(out.size(), 0);
+	std::vector<uint32_t> run(std::max(dw, dh) + 1);
+	for (uint32_t j = 0; j < dh; j++) {
+		run[0] = 0;
+		for (uint32_t i = 0; i < dw; i++) run[i + 1] = run[i] + out[i + (size_t)j * dw];
+		for (int i = 0; i < (int)dw; i++) {
+			const int a = std::max(0, i - px), z = std::min((int)dw - 1, i + px);
+			rows[i + (size_t)j * dw] = run[z + 1] - run[a] > 0;
+		}
+	}
+	for (uint32_t i = 0; i < dw; i++) {
+		run[0] = 0;
+		for (uint32_t j = 0; j < dh; j++) run[j + 1] = run[j] + rows[i + (size_t)j * dw];
+		for (int j = 0; j < (int)dh; j++) {
+			const int a = std::max(0, j - py), z = std::min((int)dh - 1, j + py);
+			out[i + (size_t)j * dw] = run[z + 1] - run[a] > 0;
+		}
+	}
 }
 
 }  // namespace
@@ -231,6 +297,8 @@ struct pf_batch {
 	pf::ProfileDev *d_profiles = nullptr;
 	double *d_psf_raw = nullptr;
 	double *d_psf_norm = nullptr;
+	uint8_t *d_mask_eval = nullptr;     // the models' drawing-area masks, back to back
+	uint8_t *d_mask_final = nullptr;    // the models' own masks for the final masking
 	size_t psf_len = 0;
 	void *d_conv = nullptr;
 	void *d_direct = nullptr;
@@ -408,6 +476,8 @@ void pf_batch_destroy(pf_batch *b)
 	cudaFree(b->d_models);
 	cudaFree(b->d_profiles);
 	cudaFree(b->d_psf_raw);
+	cudaFree(b->d_mask_eval);
+	cudaFree(b->d_mask_final);
 	cudaFree(b->d_psf_norm);
 	cudaFree(b->d_conv);
 	cudaFree(b->d_direct);
@@ -502,7 +572,11 @@ pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5], const double *p
 		pf::ModelDev &d = b->mdev[i];
 		d.use_fft = 0;
 		if (!d.conv_required) continue;
-		const unsigned int mx = next_pow2(d.crop_w + d.psf_w), my = next_pow2(d.crop_h + d.psf_h);
+		// the single-precision transforms start at 64 points (a larger zero
+		// padding leaves the linear convolution unchanged)
+		const unsigned int nmin = b->dbl ? 2u : 64u;
+		const unsigned int mx = std::max(nmin, next_pow2(d.crop_w + d.psf_w));
+		const unsigned int my = std::max(nmin, next_pow2(d.crop_h + d.psf_h));
 		bool fft = false;
 		if (d.convolver == PF_CONV_FFT) {
 			if (b->dbl && d.fs > 1 && !d.return_fs) {
@@ -548,6 +622,10 @@ pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5], const double *p
 				}
 			}
 			const int rpj_x = pf::fft32_rows_per_job((int)mx), cpj_y = pf::fft32_cols_per_job((int)my);
+			if (rpj_x <= 0 || cpj_y <= 0) {
+				return fail(PF_ERR_UNSUPPORTED, "model " + std::to_string(i) + ": no single-precision FFT of " +
+				                                    std::to_string(mx) + " x " + std::to_string(my) + " points");
+			}
 			auto add = [&](int mode, int pass, int n, int count, int per) {
 				for (int r = 0; r < count; r += per) f32[mode][pass][n].push_back({(int)i, r, std::min(per, count - r), 0});
 			};
@@ -599,8 +677,11 @@ extern "C" {
 
 static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, size_t n_models,
                                    const pf_profile_desc *profiles, size_t n_profiles, const double *psf_pool,
-                                   size_t psf_pool_len, pf_batch *b, const ConvPlan &plan)
+                                   size_t psf_pool_len, const uint8_t *mask_pool, size_t mask_pool_len, pf_batch *b,
+                                   const ConvPlan &plan)
 {
+	std::vector<uint8_t> mask_eval, mask_final;
+	std::vector<int64_t> eval_off(n_models, -1), final_off(n_models, -1);
 	b->env = env;
 	b->dbl = (env->flags & PF_ENV_DOUBLE) != 0;
 	b->models.assign(models, models + n_models);
@@ -617,11 +698,39 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		if (m.psf_offset >= 0 && (uint64_t)m.psf_offset + (uint64_t)m.psf_w * m.psf_h > psf_pool_len) {
 			return fail(PF_ERR_INVALID_PARAMETER, "model " + std::to_string(i) + ": PSF outside the PSF pool");
 		}
+		const uint8_t *mask = nullptr;
+		if (mask_pool && m.mask_offset >= 0) {
+			mask = mask_pool + m.mask_offset;
+			if ((uint64_t)m.mask_offset + (uint64_t)m.width * m.height > mask_pool_len) {
+				return fail(PF_ERR_INVALID_PARAMETER, "model " + std::to_string(i) + ": mask outside the mask pool");
+			}
+		}
 		Geometry g;
-		pf_status s = model_geometry(m, profiles, g);
+		pf_status s = model_geometry(m, profiles, g, mask);
 		if (s != PF_OK) {
 			g_last_error = "model " + std::to_string(i) + ": " + g_last_error;
 			return s;
+		}
+		if (mask) {
+			// the evaluation mask (drawing dimensions) and, after an adjustment,
+			// the model's own mask for the output (src/model.cpp:269-317)
+			eval_off[i] = (int64_t)mask_eval.size();
+			if (m.adjust_mask && g.mask_needs_adjustment) {
+				std::vector<uint8_t> adj;
+				adjusted_mask(m, g, mask, adj);
+				mask_eval.insert(mask_eval.end(), adj.begin(), adj.end());
+				final_off[i] = (int64_t)mask_final.size();
+				mask_final.insert(mask_final.end(), mask, mask + (size_t)m.width * m.height);
+			}
+			else {
+				// used as given: the model's dimensions without padding or
+				// finesampling (adjustable), else the drawing dimensions
+				const size_t n = (size_t)g.draw_w * g.draw_h;
+				if ((uint64_t)m.mask_offset + n > mask_pool_len) {
+					return fail(PF_ERR_INVALID_PARAMETER, "model " + std::to_string(i) + ": mask outside the mask pool");
+				}
+				mask_eval.insert(mask_eval.end(), mask, mask + n);
+			}
 		}
 		for (uint32_t q = 0; q < m.n_profiles; q++) {
 			if (owner[m.first_profile + q] != -1) {
@@ -768,6 +877,21 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		PF_CUDA_TRY(cudaMalloc(&b->d_psf_norm, sizeof(double) * psf_pool_len));
 		PF_CUDA_TRY(cudaMemcpy(b->d_psf_raw, psf_pool, sizeof(double) * psf_pool_len, cudaMemcpyHostToDevice));
 	}
+	if (!mask_eval.empty()) {
+		PF_CUDA_TRY(cudaMalloc(&b->d_mask_eval, mask_eval.size()));
+		PF_CUDA_TRY(cudaMemcpy(b->d_mask_eval, mask_eval.data(), mask_eval.size(), cudaMemcpyHostToDevice));
+	}
+	if (!mask_final.empty()) {
+		PF_CUDA_TRY(cudaMalloc(&b->d_mask_final, mask_final.size()));
+		PF_CUDA_TRY(cudaMemcpy(b->d_mask_final, mask_final.data(), mask_final.size(), cudaMemcpyHostToDevice));
+	}
+	for (size_t i = 0; i < n_models; i++) {
+		pf::ModelDev &d = b->mdev[i];
+		d.mask_eval = eval_off[i] >= 0 ? b->d_mask_eval + eval_off[i] : nullptr;
+		d.mask_final = final_off[i] >= 0 ? b->d_mask_final + final_off[i] : nullptr;
+		d.mask_final_w = models[i].width;
+		d.mask_final_div = models[i].finesampling > 1 && models[i].return_finesampled ? models[i].finesampling : 1;
+	}
 	if (n_models) {
 		PF_CUDA_TRY(cudaMemcpy(b->d_models, b->mdev.data(), sizeof(pf::ModelDev) * n_models, cudaMemcpyHostToDevice));
 	}
@@ -845,12 +969,14 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 
 static pf_status create_planned(pf_env *env, const pf_model_desc *models, size_t n_models,
                                 const pf_profile_desc *profiles, size_t n_profiles, const double *psf_pool,
-                                size_t psf_pool_len, const ConvPlan &plan, pf_batch **batch)
+                                size_t psf_pool_len, const uint8_t *mask_pool, size_t mask_pool_len,
+                                const ConvPlan &plan, pf_batch **batch)
 {
 	*batch = nullptr;
 	pf_batch *b = new (std::nothrow) pf_batch();
 	if (!b) return fail(PF_ERR_NO_MEMORY, "out of host memory");
-	pf_status s = batch_create_impl(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, b, plan);
+	pf_status s = batch_create_impl(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool,
+	                                mask_pool_len, b, plan);
 	if (s != PF_OK) {
 		b->env = env;
 		pf_batch_destroy(b);
@@ -964,7 +1090,17 @@ static double time_adjoint_conv(pf_batch *b, int shape)
 pf_status pf_batch_create(pf_env *env, const pf_model_desc *models, size_t n_models, const pf_profile_desc *profiles,
                           size_t n_profiles, const double *psf_pool, size_t psf_pool_len, pf_batch **batch)
 {
-	if (!env || !batch || (!models && n_models) || (!profiles && n_profiles) || (!psf_pool && psf_pool_len)) {
+	return pf_batch_create_masked(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, nullptr, 0,
+	                              batch);
+}
+
+pf_status pf_batch_create_masked(pf_env *env, const pf_model_desc *models, size_t n_models,
+                                 const pf_profile_desc *profiles, size_t n_profiles, const double *psf_pool,
+                                 size_t psf_pool_len, const uint8_t *mask_pool, size_t mask_pool_len,
+                                 pf_batch **batch)
+{
+	if (!env || !batch || (!models && n_models) || (!profiles && n_profiles) || (!psf_pool && psf_pool_len) ||
+	    (!mask_pool && mask_pool_len)) {
 		return fail(PF_ERR_INVALID_PARAMETER, "pf_batch_create: NULL argument");
 	}
 	*batch = nullptr;
@@ -978,7 +1114,10 @@ pf_status pf_batch_create(pf_env *env, const pf_model_desc *models, size_t n_mod
 		any_auto |= models[i].convolver == PF_CONV_AUTO && models[i].psf_offset >= 0 && models[i].psf_w > 0;
 	}
 	tune = tune && any_auto && out_pixels >= (1ull << 22);
-	if (!tune) return create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, fixed, batch);
+	if (!tune) {
+		return create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool,
+		                      mask_pool_len, fixed, batch);
+	}
 
 	// The autotuner (single precision, PF_CONV_AUTO, large batches): the batch
 	// built with every automatic model on the direct convolution, each block
@@ -991,7 +1130,8 @@ pf_status pf_batch_create(pf_env *env, const pf_model_desc *models, size_t n_mod
 	pd.auto_fft = &none;
 	pfft.auto_fft = &all;
 	pf_batch *bd = nullptr, *bf = nullptr;
-	pf_status s = create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, pd, &bd);
+	pf_status s = create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool,
+	                             mask_pool_len, pd, &bd);
 	if (s != PF_OK) return s;
 	float *out = nullptr;
 	if (cudaMalloc(&out, sizeof(float) * std::max<uint64_t>(1, bd->total_out)) != cudaSuccess) {
@@ -1014,7 +1154,8 @@ pf_status pf_batch_create(pf_env *env, const pf_model_desc *models, size_t n_mod
 		work_d += (double)d.crop_w * d.crop_h * (d.conv_required ? (double)d.psf_w * d.psf_h : 1.0);
 	}
 	std::vector<int8_t> choice(n_models, 0);
-	s = create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, pfft, &bf);
+	s = create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool, mask_pool_len,
+	                   pfft, &bf);
 	if (s == PF_OK && bf->any_fft) {
 		cudaMemsetAsync(bf->d_conv, 0, sizeof(float) * std::max<size_t>(1, bf->draw_total), env->stream);
 		cudaMemsetAsync(bf->d_direct, 0, sizeof(float) * std::max<size_t>(1, bf->draw_total), env->stream);
@@ -1039,7 +1180,8 @@ pf_status pf_batch_create(pf_env *env, const pf_model_desc *models, size_t n_mod
 	ConvPlan fin;
 	fin.shape = best_shape;
 	fin.auto_fft = &choice;
-	return create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, fin, batch);
+	return create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool,
+	                      mask_pool_len, fin, batch);
 }
 
 pf_status pf_batch_layout(const pf_batch *b, uint64_t *offsets, uint32_t *dims, uint64_t *total_pixels)
@@ -1224,6 +1366,16 @@ pf_status pf_batch_depth(pf_batch *b, int8_t *depth, size_t depth_len, int64_t *
 			                       cudaMemcpyDeviceToHost));
 		}
 		for (size_t i = 0; i < tmp.size(); i++) level_counts[i] = (int64_t)tmp[i];
+	}
+	return PF_OK;
+}
+
+pf_status pf_batch_drawing_dims(pf_batch *b, uint32_t *dims)
+{
+	if (!b || !dims) return fail(PF_ERR_INVALID_PARAMETER, "pf_batch_drawing_dims: NULL argument");
+	for (size_t i = 0; i < b->mdev.size(); i++) {
+		dims[2 * i] = b->mdev[i].draw_w;
+		dims[2 * i + 1] = b->mdev[i].draw_h;
 	}
 	return PF_OK;
 }
@@ -1486,6 +1638,13 @@ pf_status pf_step_graph(pf_batch *b, const double *params_dev, void *images_dev,
 pf_status pf_model_evaluate(pf_env *env, const pf_model_desc *model, const pf_profile_desc *profiles,
                             const double *psf, double *image, uint32_t *out_w, uint32_t *out_h)
 {
+	return pf_model_evaluate_masked(env, model, profiles, psf, nullptr, image, out_w, out_h);
+}
+
+pf_status pf_model_evaluate_masked(pf_env *env, const pf_model_desc *model, const pf_profile_desc *profiles,
+                                   const double *psf, const uint8_t *mask, double *image, uint32_t *out_w,
+                                   uint32_t *out_h)
+{
 	if (!env || !model || !image || (!profiles && model->n_profiles)) {
 		return fail(PF_ERR_INVALID_PARAMETER, "pf_model_evaluate: NULL argument");
 	}
@@ -1493,9 +1652,18 @@ pf_status pf_model_evaluate(pf_env *env, const pf_model_desc *model, const pf_pr
 	m.first_profile = 0;
 	const bool has_psf = psf && m.psf_w > 0 && m.psf_h > 0;
 	m.psf_offset = has_psf ? 0 : -1;
+	m.mask_offset = mask ? 0 : -1;
+	size_t mask_len = 0;
+	if (mask) {
+		// the adjustable mask has the model's dimensions; one used as given, the drawing dimensions
+		Geometry g;
+		pf_status gs = model_geometry(m, profiles, g);
+		if (gs != PF_OK) return gs;
+		mask_len = m.adjust_mask ? (size_t)m.width * m.height : (size_t)g.draw_w * g.draw_h;
+	}
 	pf_batch *b = nullptr;
-	pf_status s = pf_batch_create(env, &m, 1, profiles, m.n_profiles, has_psf ? psf : nullptr,
-	                              has_psf ? (size_t)m.psf_w * m.psf_h : 0, &b);
+	pf_status s = pf_batch_create_masked(env, &m, 1, profiles, m.n_profiles, has_psf ? psf : nullptr,
+	                                     has_psf ? (size_t)m.psf_w * m.psf_h : 0, mask, mask_len, &b);
 	if (s != PF_OK) return s;
 	const size_t n = b->total_out;
 	const size_t elem = b->dbl ? sizeof(double) : sizeof(float);

@@ -61,7 +61,26 @@ struct ModelDev {
 	uint32_t fft_mx, fft_my;
 	int32_t pad2;
 	int64_t fft_work_off, fft_spec_off;
+	// calculation mask (Model::evaluate, src/model.cpp:152-317): the drawing
+	// pixels the profiles and the convolution are evaluated at (null: all),
+	// and the mask the output is multiplied by at the end (null: none), of
+	// mask_final_w columns, output pixel (x, y) taking (x / div, y / div)
+	const uint8_t *mask_eval;
+	const uint8_t *mask_final;
+	uint32_t mask_final_w, mask_final_div;
 };
+
+// whether drawing pixel (x, y) of model m is evaluated (not masked out)
+__device__ __forceinline__ bool evaluated(const ModelDev &m, int x, int y)
+{
+	return !m.mask_eval || m.mask_eval[(size_t)y * m.draw_w + x] != 0;
+}
+
+// whether output pixel (x, y) of model m survives the final masking
+__device__ __forceinline__ bool kept(const ModelDev &m, int x, int y)
+{
+	return !m.mask_final || m.mask_final[(size_t)(y / m.mask_final_div) * m.mask_final_w + x / m.mask_final_div] != 0;
+}
 
 struct ProfileDev {
 	// from the descriptor (never modified on the device)

@@ -13,6 +13,8 @@ def product_model(spec, psf, env=None):
     m.set_return_finesampled(spec.get("return_finesampled", True))
     if psf is not None:
         m.set_psf(psf)
+    if spec.get("mask") is not None:
+        m.set_mask(np.asarray(spec["mask"], dtype=np.uint8))
     if env is not None:
         m.set_cuda_env(env)
     for kind, params in spec["profiles"]:

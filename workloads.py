@@ -132,6 +132,9 @@ def to_model(spec, env=None):
         m.set_convolver(spec["convolver"])
     if spec.get("psf") is not None:
         m.set_psf(spec["psf"])
+    if spec.get("mask") is not None:
+        m.set_mask(spec["mask"])
+        m.set_adjust_mask(spec.get("adjust_mask", True))
     if env is not None:
         m.set_cuda_env(env)
     for kind, params in spec["profiles"]:
@@ -145,7 +148,8 @@ def to_model(spec, env=None):
 def to_oracle_case(spec):
     from oracle import oracle as O
     return O.Case(spec["width"], spec["height"], spec["profiles"], psf=spec.get("psf"),
-                  magzero=spec.get("magzero", 0.0))
+                  magzero=spec.get("magzero", 0.0), mask=spec.get("mask"),
+                  adjust_mask=spec.get("adjust_mask", True))
 
 
 def param_matrix(specs):
