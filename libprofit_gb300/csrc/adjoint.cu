@@ -17,14 +17,21 @@
 // Per (profile, row) partial sums are written in FP64 and reduced in a fixed
 // order, so gradients and chi^2 are deterministic.
 //
-// Profiles supported by the adjoint: sersic (all eight parameters xcen, ycen,
-// mag, ang, axrat, box, re, nser; not rescale_flux) and sky (bg).
+// Profiles supported by the adjoint: the six radial profiles with all their
+// parameters (xcen, ycen, mag, ang, axrat, box and the profile's own: sersic
+// re, nser, not with rescale_flux; coresersic re, nser, rb, a, b; moffat fwhm,
+// con; ferrer rout, a, b; king rc, rt, a; brokenexp h1, h2, rb, a) and sky
+// (bg). A batch whose radial profiles are all sersics runs kernels with eight
+// gradient slots per partial (value, five geometric, re, nser); any other
+// batch runs the same kernels with twelve (value, five geometric, par[6..11]),
+// the other kinds' terms coming from profiles_grad.cuh.
 #include <cstdint>
 #include <type_traits>
 
 #include "pf_device.cuh"
 #include "profiles_f32.cuh"
 #include "profiles_f64.cuh"
+#include "profiles_grad.cuh"
 
 namespace pf {
 
@@ -77,6 +84,37 @@ __device__ __forceinline__ T warp_sum8(const T *v, int lane)
 	t += __shfl_xor_sync(0xffffffffu, t, 2);
 	t += __shfl_xor_sync(0xffffffffu, t, 1);
 	return t;
+}
+
+// Gradient slots per partial of a kernel built for the profile kinds KINDS.
+template <unsigned int KINDS>
+__host__ __device__ constexpr int slots_of()
+{
+	return KINDS == f32::kSersicOnly ? (int)kGradSlots : grad::kSlots;
+}
+
+__host__ __device__ constexpr bool is_radial_kind(int kind) { return kind >= PF_SERSIC && kind <= PF_BROKENEXP; }
+
+// Sums v[0..NS-1] over the warp (NS = 8 or 12, warp_sum8 once or twice) and
+// stores the totals to dst[0..NS-1] from the lanes that hold them.
+template <int NS, typename T, typename D>
+__device__ __forceinline__ void warp_store_slots(const T *v, int lane, D *dst)
+{
+	const T lo = warp_sum8(v, lane);
+	if constexpr (NS == 8) {
+		if ((lane & 3) == 0) dst[lane >> 2] = (D)lo;
+	}
+	else {
+		static_assert(NS > 8 && NS <= 16, "two passes of eight slots");
+		T rest[8];
+#pragma unroll
+		for (int k = 0; k < 8; k++) rest[k] = 8 + k < NS ? v[8 + k] : (T)0;
+		const T hi = warp_sum8(rest, lane);
+		if ((lane & 3) == 0) {
+			dst[lane >> 2] = (D)lo;
+			if ((lane >> 2) < NS - 8) dst[8 + (lane >> 2)] = (D)hi;
+		}
+	}
 }
 
 // ------------------------------------------------------------ chi^2, g_out
@@ -238,16 +276,16 @@ __device__ __forceinline__ float sersic_terms_f(const f32::Shape &P, float xp, f
 // A sub-pixel box as in eval_f32.cu: its corner relative to the profile
 // centre as an unevaluated sum hi + lo in T (lo stays 0 in double), its size
 // and its eight running totals.
-template <typename T>
+template <typename T, int NS>
 struct FrameG {
 	T xhi, xlo, yhi, ylo, bx, by;
-	T tot[kGradSlots];
+	T tot[NS];
 	unsigned int mask[kMaskWords];
 };
 
-template <typename T>
+template <typename T, int NS>
 struct WarpScratchG {
-	FrameG<T> fr[kMaxLevels];
+	FrameG<T, NS> fr[kMaxLevels];
 	unsigned int amb[kMaskWords];  // sub-points of the frame being evaluated whose decision is re-taken in FP64
 };
 
@@ -273,9 +311,10 @@ __device__ __forceinline__ void corner_pair_b(float i, float s_hi, float s_lo, f
 // The FP32 path's rare FP64 re-takes. They take only single-precision and
 // integer arguments, so that no double-precision work is scheduled on the
 // common path. The one of the subsampling recursion is inlined (a call there
-// costs the whole kernel registers); the adjoint's profiles are sersics.
+// costs the whole kernel registers).
 
 // accuracy test of one sub-point, the point (xhi + xlo) + ox, (yhi + ylo) + oy
+template <unsigned int KINDS>
 __device__ __forceinline__ bool test_f64b(const ProfileDev &P, float xhi, float xlo, float yhi, float ylo, float ox,
                                        float oy, float xbin, float ybin)
 {
@@ -283,9 +322,16 @@ __device__ __forceinline__ bool test_f64b(const ProfileDev &P, float xhi, float 
 	const double dy = ((double)yhi + (double)ylo) + (double)oy;
 	const double xp = dx * P.cos_ang + dy * P.sin_ang;
 	const double yp = (-dx * P.sin_ang + dy * P.cos_ang) / P.par[PF_P_AXRAT];
-	const double sv = f64::sersic(P, xp, yp);
 	const double dyp = (-(double)xbin * P.sin_ang + (double)ybin * P.cos_ang) / P.par[PF_P_AXRAT];
-	const double t = f64::sersic(P, fabs(xp), fabs(yp) + fabs(dyp));
+	double sv, t;
+	if constexpr (KINDS == f32::kSersicOnly) {
+		sv = f64::sersic(P, xp, yp);
+		t = f64::sersic(P, fabs(xp), fabs(yp) + fabs(dyp));
+	}
+	else {
+		sv = f64::evaluate_at(P, xp, yp);
+		t = f64::evaluate_at(P, fabs(xp), fabs(yp) + fabs(dyp));
+	}
 	return fabs(t / sv - 1.0) > P.acc;
 }
 
@@ -307,12 +353,40 @@ __device__ __noinline__ bool center_f64(const ProfileDev &P, const ModelDev &m, 
 	return fabs(x - P.xc) < m.scale_x && fabs(y - P.yc) < m.scale_y;
 }
 
-template <typename T>
-__device__ void eval_frame_g(const ProfileDev &P, const f32::Shape &sh, WarpScratchG<T> &ws, int L, unsigned int res,
-                             T inv_res, unsigned int max_rec, int lane)
+// The value and gradient terms of one point for a kernel built for KINDS:
+// t[0..slots_of<KINDS>() - 1]. Returns the value.
+template <typename T, unsigned int KINDS>
+__device__ __forceinline__ T point_terms(const ProfileDev &P, const f32::Shape &sh, const grad::GShape<T> &gs, T xp,
+                                         T yp, T *t)
 {
 	constexpr bool dbl = std::is_same<T, double>::value;
-	FrameG<T> &f = ws.fr[L];
+	constexpr int NS = slots_of<KINDS>();
+	if constexpr (KINDS != f32::kSersicOnly) {
+		if (P.kind != PF_SERSIC) return grad::terms<T>(gs, xp, yp, t);
+	}
+	if constexpr (NS > kGradSlots) {
+#pragma unroll
+		for (int k = kGradSlots; k < NS; k++) t[k] = (T)0;
+	}
+	if constexpr (dbl) {
+#pragma unroll
+		for (int k = 0; k < kGradSlots; k++) t[k] = (T)0;
+		sersic_grad<T>(P, xp, yp, (T)1, t);
+		return t[G_V];
+	}
+	else {
+		return sersic_terms_f(sh, xp, yp, t);
+	}
+}
+
+template <typename T, unsigned int KINDS>
+__device__ void eval_frame_g(const ProfileDev &P, const f32::Shape &sh, const grad::GShape<T> &gs,
+                             WarpScratchG<T, slots_of<KINDS>()> &ws, int L, unsigned int res, T inv_res,
+                             unsigned int max_rec, int lane)
+{
+	constexpr bool dbl = std::is_same<T, double>::value;
+	constexpr int NS = slots_of<KINDS>();
+	FrameG<T, NS> &f = ws.fr[L];
 	const T xhi = f.xhi, xlo = f.xlo, yhi = f.yhi, ylo = f.ylo;
 	const T txbin = f.bx * inv_res, tybin = f.by * inv_res;
 	const bool recurse = res > 1 && (unsigned int)L < max_rec;
@@ -322,9 +396,9 @@ __device__ void eval_frame_g(const ProfileDev &P, const f32::Shape &sh, WarpScra
 	const T acc_t = dbl ? (T)P.acc : (T)sh.acc;
 	const T tdyp = fabs((-txbin * s + tybin * c) * iq);
 	const unsigned int magic = res_magic(res);
-	T part[kGradSlots];
+	T part[NS];
 #pragma unroll
-	for (int k = 0; k < kGradSlots; k++) part[k] = 0;
+	for (int k = 0; k < NS; k++) part[k] = 0;
 	unsigned int amb_any = 0;
 	for (unsigned int base = 0; base < n; base += 32) {
 		const unsigned int idx = base + lane;
@@ -342,9 +416,14 @@ __device__ void eval_frame_g(const ProfileDev &P, const f32::Shape &sh, WarpScra
 					const T t = f64::evaluate_at(P, fabs(xp), fabs(yp) + tdyp);
 					fail = fabs(t / sv - (T)1) > acc_t;
 				}
-				if (!fail) sersic_grad<T>(P, xp, yp, (T)1, part);
+				if (!fail) {
+					T terms[NS];
+					point_terms<T, KINDS>(P, sh, gs, xp, yp, terms);
+#pragma unroll
+					for (int k = 0; k < NS; k++) part[k] += terms[k];
+				}
 			}
-			else {
+			else if constexpr (KINDS == f32::kSersicOnly) {
 				float terms[kGradSlots];
 				const float sv = sersic_terms_f(sh, xp, yp, terms);
 				if (recurse) {
@@ -356,6 +435,22 @@ __device__ void eval_frame_g(const ProfileDev &P, const f32::Shape &sh, WarpScra
 				if (!fail && !amb) {
 #pragma unroll
 					for (int k = 0; k < kGradSlots; k++) part[k] += terms[k];
+				}
+			}
+			else {
+				// the forward pass's decision from its own values, then the terms
+				if (recurse) {
+					const float sv = f32::value<KINDS>(sh, xp, yp);
+					const float t = f32::value<KINDS>(sh, fabsf(xp), fabsf(yp) + tdyp);
+					const float d = fabsf(__fdividef(t, sv) - 1.f);
+					amb = !(isfinite(d) && isfinite(sv)) || fabsf(d - acc_t) <= kGuardAccB * (acc_t + 1.f);
+					fail = !amb && d > acc_t;
+				}
+				if (!fail && !amb) {
+					float terms[NS];
+					point_terms<float, KINDS>(P, sh, gs, xp, yp, terms);
+#pragma unroll
+					for (int k = 0; k < NS; k++) part[k] += terms[k];
 				}
 			}
 		}
@@ -380,14 +475,14 @@ __device__ void eval_frame_g(const ProfileDev &P, const f32::Shape &sh, WarpScra
 					const unsigned int idx = base + lane;
 					const unsigned int i = div_res(idx, magic), j = idx - i * res;
 					const float ox = (small_int_to_float(i) + 0.5f) * txbin, oy = (small_int_to_float(j) + 0.5f) * tybin;
-					fail = test_f64b(P, xhi, xlo, yhi, ylo, ox, oy, txbin, tybin);
+					fail = test_f64b<KINDS>(P, xhi, xlo, yhi, ylo, ox, oy, txbin, tybin);
 					if (!fail) {
 						const float dx = (xhi + ox) + xlo;
 						const float dy = (yhi + oy) + ylo;
-						float terms[kGradSlots];
-						sersic_terms_f(sh, dx * c + dy * s, (dy * c - dx * s) * iq, terms);
+						float terms[NS];
+						point_terms<float, KINDS>(P, sh, gs, dx * c + dy * s, (dy * c - dx * s) * iq, terms);
 #pragma unroll
-						for (int k = 0; k < kGradSlots; k++) part[k] += terms[k];
+						for (int k = 0; k < NS; k++) part[k] += terms[k];
 					}
 				}
 				const unsigned int word = __ballot_sync(0xffffffffu, fail);
@@ -395,16 +490,16 @@ __device__ void eval_frame_g(const ProfileDev &P, const f32::Shape &sh, WarpScra
 			}
 		}
 	}
-	static_assert(kGradSlots == 8, "warp_sum8 reduces eight slots");
-	const T total = warp_sum8(part, lane);
-	if ((lane & 3) == 0) f.tot[lane >> 2] = total;
+	warp_store_slots<NS>(part, lane, f.tot);
 	__syncwarp();
 }
 
-template <typename T>
-__device__ void warp_subsample_g(const ProfileDev &P, const f32::Shape &sh, WarpScratchG<T> &ws, T xhi, T xlo, T yhi,
-                                 T ylo, T bx, T by, unsigned int res, unsigned int max_rec, int lane, T *out)
+template <typename T, unsigned int KINDS>
+__device__ void warp_subsample_g(const ProfileDev &P, const f32::Shape &sh, const grad::GShape<T> &gs,
+                                 WarpScratchG<T, slots_of<KINDS>()> &ws, T xhi, T xlo, T yhi, T ylo, T bx, T by,
+                                 unsigned int res, unsigned int max_rec, int lane, T *out)
 {
+	constexpr int NS = slots_of<KINDS>();
 	if (lane == 0) {
 		ws.fr[0].xhi = xhi;
 		ws.fr[0].xlo = xlo;
@@ -417,10 +512,10 @@ __device__ void warp_subsample_g(const ProfileDev &P, const f32::Shape &sh, Warp
 	const T inv_res = (T)1 / (T)res;
 	const T inv_res2 = (T)1 / (T)(res * res);
 	int L = 0;
-	eval_frame_g<T>(P, sh, ws, 0, res, inv_res, max_rec, lane);
+	eval_frame_g<T, KINDS>(P, sh, gs, ws, 0, res, inv_res, max_rec, lane);
 	const unsigned int nwords = (res * res + 31) / 32;
 	while (true) {
-		FrameG<T> &f = ws.fr[L];
+		FrameG<T, NS> &f = ws.fr[L];
 		int k = -1;
 		for (unsigned int w = 0; w < nwords; w++) {
 			const unsigned int mw = f.mask[w];
@@ -435,7 +530,7 @@ __device__ void warp_subsample_g(const ProfileDev &P, const f32::Shape &sh, Warp
 				const unsigned int i = div_res((unsigned int)k, res_magic(res)), j = (unsigned int)k - i * res;
 				const T cbx = f.bx * inv_res, cby = f.by * inv_res;
 				f.mask[k >> 5] &= ~(1u << (k & 31));
-				FrameG<T> &ch = ws.fr[L + 1];
+				FrameG<T, NS> &ch = ws.fr[L + 1];
 				T e;
 				two_sum_t<T>(f.xhi, (T)small_int_to_float(i) * cbx, ch.xhi, e);
 				ch.xlo = f.xlo + e;
@@ -446,16 +541,16 @@ __device__ void warp_subsample_g(const ProfileDev &P, const f32::Shape &sh, Warp
 			}
 			__syncwarp();
 			L++;
-			eval_frame_g<T>(P, sh, ws, L, res, inv_res, max_rec, lane);
+			eval_frame_g<T, KINDS>(P, sh, gs, ws, L, res, inv_res, max_rec, lane);
 		}
 		else {
 			if (L == 0) {
-				for (int s = 0; s < kGradSlots; s++) out[s] = f.tot[s] * inv_res2;
+				for (int s = 0; s < NS; s++) out[s] = f.tot[s] * inv_res2;
 				return;
 			}
 			L--;
 			if (lane == 0) {
-				for (int s = 0; s < kGradSlots; s++) ws.fr[L].tot[s] += f.tot[s] * inv_res2;
+				for (int s = 0; s < NS; s++) ws.fr[L].tot[s] += f.tot[s] * inv_res2;
 			}
 			__syncwarp();
 		}
@@ -476,7 +571,7 @@ __device__ __forceinline__ int item_row(const ProfileDev &P, const ModelDev &m, 
 		hi = (int)m.draw_h - 1;
 		centre = hi / 2;
 	}
-	else if (P.kind == PF_SERSIC) {
+	else if (is_radial_kind(P.kind)) {
 		lo = max(0, P.bby0);
 		hi = min((int)m.draw_h - 1, P.bby1);
 		centre = (int)floorf(__fdividef(P.fyc_hi, m.fsy_hi));
@@ -492,19 +587,24 @@ __device__ __forceinline__ int item_row(const ProfileDev &P, const ModelDev &m, 
 
 // Tiles [c0, c1] of drawing row `row` of one profile, except tiles [s0, s1]:
 // the cotangent-weighted value and shape derivatives of the profile summed
-// over their pixels, written as one FP64 partial (eight slots) to dst.
-template <typename T>
+// over their pixels, written as one FP64 partial (slots_of<KINDS>() slots) to dst.
+template <typename T, unsigned int KINDS>
 __device__ void backward_row(const ModelDev &m, const ProfileDev &P, int row, int c0, int c1, int s0, int s1,
-                             const T *__restrict__ gout, const T *__restrict__ gsrc, WarpScratchG<T> &ws, int lane,
-                             double *dst)
+                             const T *__restrict__ gout, const T *__restrict__ gsrc,
+                             WarpScratchG<T, slots_of<KINDS>()> &ws, int lane, double *dst)
 {
 	constexpr bool dbl = std::is_same<T, double>::value;
+	constexpr int NS = slots_of<KINDS>();
 	const bool is_sky = P.kind == PF_SKY;
 	const T *gimg = P.convolve ? gsrc + m.draw_off : nullptr;
 	const f32::Shape sh = f32::load_shape(P);
-	T acc[kGradSlots];
+	grad::GShape<T> gs;
+	if constexpr (KINDS != f32::kSersicOnly) {
+		if (!is_sky) gs = grad::make_gshape<T>(P);
+	}
+	T acc[NS];
 #pragma unroll
-	for (int k = 0; k < kGradSlots; k++) acc[k] = 0;
+	for (int k = 0; k < NS; k++) acc[k] = 0;
 	for (int tcol = c0; tcol <= c1; tcol++) {
 		if (tcol >= s0 && tcol <= s1) continue;
 		const int px = tcol * 32 + lane;
@@ -558,20 +658,10 @@ __device__ void backward_row(const ModelDev &m, const ProfileDev &P, int row, in
 		bool need_ss = false;
 		if (active && g != (T)0 && !beyond) {
 			if (P.rough || outside) {
-				if constexpr (dbl) {
-					T tmp[kGradSlots];
+				T tmp[NS];
+				point_terms<T, KINDS>(P, sh, gs, xp, yp, tmp);
 #pragma unroll
-					for (int k = 0; k < kGradSlots; k++) tmp[k] = 0;
-					sersic_grad<T>(P, xp, yp, (T)1, tmp);
-#pragma unroll
-					for (int k = 0; k < kGradSlots; k++) acc[k] += g * tmp[k];
-				}
-				else {
-					float tmp[kGradSlots];
-					sersic_terms_f(sh, xp, yp, tmp);
-#pragma unroll
-					for (int k = 0; k < kGradSlots; k++) acc[k] += g * tmp[k];
-				}
+				for (int k = 0; k < NS; k++) acc[k] += g * tmp[k];
 			}
 			else {
 				need_ss = true;
@@ -611,21 +701,20 @@ __device__ void backward_row(const ModelDev &m, const ProfileDev &P, int row, in
 				corner_pair_b(small_int_to_float((unsigned int)spx), m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
 				corner_pair_b(small_int_to_float((unsigned int)row), m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
 			}
-			T sums[kGradSlots];
-			warp_subsample_g<T>(P, sh, ws, bxh, bxl, byh, byl, dbl ? (T)m.sx : (T)m.fsx_hi,
-			                    dbl ? (T)m.sy : (T)m.fsy_hi, res, max_rec, lane, sums);
-			const T gs = __shfl_sync(0xffffffffu, g, src);
+			T sums[NS];
+			warp_subsample_g<T, KINDS>(P, sh, gs, ws, bxh, bxl, byh, byl, dbl ? (T)m.sx : (T)m.fsx_hi,
+			                           dbl ? (T)m.sy : (T)m.fsy_hi, res, max_rec, lane, sums);
+			const T gsrc_px = __shfl_sync(0xffffffffu, g, src);
 			if (lane == 0) {
 #pragma unroll
-				for (int k = 0; k < kGradSlots; k++) acc[k] += gs * sums[k];
+				for (int k = 0; k < NS; k++) acc[k] += gsrc_px * sums[k];
 			}
 		}
 	}
-	double acc64[kGradSlots];
+	double acc64[NS];
 #pragma unroll
-	for (int k = 0; k < kGradSlots; k++) acc64[k] = (double)acc[k];
-	const double total = warp_sum8(acc64, lane);
-	if ((lane & 3) == 0) dst[lane >> 2] = total;
+	for (int k = 0; k < NS; k++) acc64[k] = (double)acc[k];
+	warp_store_slots<NS>(acc64, lane, dst);
 }
 
 // Work items, taken by warps 32 at a time from a global counter (items with
@@ -638,16 +727,17 @@ __device__ void backward_row(const ModelDev &m, const ProfileDev &P, int row, in
 //   phase B, n_profiles * n_ring items: profile p's drawing row ring(l) of its
 //     bounding box, item n_a + l * n_profiles + p, every tile of the row but
 //     its ring tiles, one partial per (profile, row).
-template <typename T>
+template <typename T, unsigned int KINDS>
 __global__ void __launch_bounds__(kWarpsB * 32, PF_BACKWARD_MIN_BLOCKS)
 backward_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restrict__ profs, unsigned int n_profiles,
                 const T *__restrict__ gout, const T *__restrict__ gsrc, const long long *__restrict__ prow_base,
                 unsigned int n_ring, unsigned int *counter, double *__restrict__ partial,
                 double *__restrict__ ring_partial)
 {
-	__shared__ WarpScratchG<T> scratch[kWarpsB];
+	constexpr int NS = slots_of<KINDS>();
+	__shared__ WarpScratchG<T, NS> scratch[kWarpsB];
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	WarpScratchG<T> &ws = scratch[warp];
+	WarpScratchG<T, NS> &ws = scratch[warp];
 	const unsigned int n_a = n_profiles * (kRingRows * kRingCols);
 	const unsigned int n_items = n_a + n_ring * n_profiles;
 	while (true) {
@@ -665,9 +755,8 @@ backward_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restric
 			p = (int)(rem / kRingCols);
 			const int c = (int)(rem - (unsigned int)p * kRingCols);
 			const ProfileDev &P = profs[p];
-			if (P.kind == PF_SERSIC && !ring_tile_of(P, models[P.model], (int)l, c, row, tc)) row = -1;
-			if (P.kind != PF_SERSIC) row = -1;
-			slot = (((long long)p * kRingRows + l) * kRingCols + c) * kGradSlots;
+			if (!is_radial_kind(P.kind) || !ring_tile_of(P, models[P.model], (int)l, c, row, tc)) row = -1;
+			slot = (((long long)p * kRingRows + l) * kRingCols + c) * NS;
 		}
 		else if (k < n_items) {
 			const unsigned int kb = k - n_a;
@@ -687,7 +776,7 @@ backward_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restric
 			const ProfileDev &P = profs[ip];
 			const ModelDev &m = models[P.model];
 			if (itc >= 0) {  // phase A: one ring tile
-				backward_row<T>(m, P, irow, itc, itc, 0, -1, gout, gsrc, ws, lane, ring_partial + islot);
+				backward_row<T, KINDS>(m, P, irow, itc, itc, 0, -1, gout, gsrc, ws, lane, ring_partial + islot);
 			}
 			else {           // phase B: the row but its ring tiles
 				int c0 = 0, c1 = (int)m.tiles_per_row - 1, s0 = 0, s1 = -1;
@@ -696,8 +785,8 @@ backward_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restric
 					c1 = P.bbx1 < 0 ? -1 : min((int)m.draw_w - 1, P.bbx1) / 32;
 					ring_cols_of_row(P, m, irow, s0, s1);
 				}
-				backward_row<T>(m, P, irow, c0, c1, s0, s1, gout, gsrc, ws, lane,
-				                partial + (prow_base[ip] + irow) * (long long)kGradSlots);
+				backward_row<T, KINDS>(m, P, irow, c0, c1, s0, s1, gout, gsrc, ws, lane,
+				                       partial + (prow_base[ip] + irow) * (long long)NS);
 			}
 		}
 	}
@@ -707,6 +796,7 @@ backward_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restric
 // and ring-tile partials summed in a fixed order (lane l takes rows l, l + 32,
 // ... then ring slots l, l + 32, ...; then a fixed shuffle tree), then scaled
 // by the flux scale and its logarithmic derivatives.
+template <int NS>
 __global__ void grad_reduce_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restrict__ profs,
                                    int n_profiles, const long long *__restrict__ prow_base,
                                    const double *__restrict__ partial, const double *__restrict__ ring_partial,
@@ -719,30 +809,31 @@ __global__ void grad_reduce_kernel(const ModelDev *__restrict__ models, const Pr
 	const ModelDev &m = models[P.model];
 	double *g = grad + (size_t)i * PF_NPAR;
 	if (lane < PF_NPAR) g[lane] = 0.;
-	if (P.kind != PF_SERSIC && P.kind != PF_SKY) return;
+	const bool radial = is_radial_kind(P.kind);
+	if (!radial && P.kind != PF_SKY) return;
 	int lo = 0, hi = (int)m.draw_h - 1;
-	if (P.kind == PF_SERSIC) {
+	if (radial) {
 		lo = max(0, P.bby0);
 		hi = min(hi, P.bby1);
 	}
-	double S[kGradSlots];
-	for (int k = 0; k < kGradSlots; k++) S[k] = 0.;
+	double S[NS];
+	for (int k = 0; k < NS; k++) S[k] = 0.;
 	for (int r = lo + lane; r <= hi; r += 32) {
-		const double *src = partial + (prow_base[i] + r) * (long long)kGradSlots;
-		for (int k = 0; k < kGradSlots; k++) S[k] += src[k];
+		const double *src = partial + (prow_base[i] + r) * (long long)NS;
+		for (int k = 0; k < NS; k++) S[k] += src[k];
 	}
-	if (P.kind == PF_SERSIC) {
+	if (radial) {
 		for (int q = lane; q < kRingRows * kRingCols; q += 32) {
 			int row, tc;
 			if (!ring_tile_of(P, m, q / kRingCols, q % kRingCols, row, tc)) continue;
-			const double *src = ring_partial + ((long long)i * (kRingRows * kRingCols) + q) * kGradSlots;
-			for (int k = 0; k < kGradSlots; k++) S[k] += src[k];
+			const double *src = ring_partial + ((long long)i * (kRingRows * kRingCols) + q) * NS;
+			for (int k = 0; k < NS; k++) S[k] += src[k];
 		}
 	}
-	const double total = warp_sum8(S, lane);
-	double T8[kGradSlots];
-#pragma unroll
-	for (int k = 0; k < kGradSlots; k++) T8[k] = __shfl_sync(0xffffffffu, total, 4 * k);
+	__shared__ double tot[8][16];
+	double *T8 = tot[threadIdx.x >> 5];
+	warp_store_slots<NS>(S, lane, T8);
+	__syncwarp();
 	if (lane != 0) return;
 	if (P.kind == PF_SKY) {
 		g[6] = T8[G_V] / (m.fs * m.fs);  // d/d bg of bg / fs^2 on every pixel (src/sky.cpp:42-45)
@@ -755,8 +846,7 @@ __global__ void grad_reduce_kernel(const ModelDev *__restrict__ models, const Pr
 	g[PF_P_ANG] = fs_ * T8[G_ANG];
 	g[PF_P_AXRAT] = fs_ * (T8[G_AXRAT] + P.dlnfs[PF_P_AXRAT] * T8[G_V]);
 	g[PF_P_BOX] = fs_ * (T8[G_BOX] + P.dlnfs[PF_P_BOX] * T8[G_V]);
-	g[6] = fs_ * (T8[G_X0] + P.dlnfs[6] * T8[G_V]);
-	g[7] = fs_ * (T8[G_X1] + P.dlnfs[7] * T8[G_V]);
+	for (int k = PF_P_X0; k < NS; k++) g[k] = fs_ * (T8[k] + P.dlnfs[k] * T8[G_V]);
 }
 
 }  // namespace
@@ -773,14 +863,26 @@ void launch_chi2(const ModelDev *models, int n_models, const void *img, const vo
 template <typename T>
 void launch_backward(const ModelDev *models, const ProfileDev *profs, int n_profiles, const void *gout,
                      const void *gsrc, const long long *prow_base, unsigned int n_ring, unsigned int *counter,
-                     double *partial, double *ring_partial, double *grad, int n_sm, cudaStream_t stream)
+                     double *partial, double *ring_partial, double *grad, bool sersic_only, int n_sm,
+                     cudaStream_t stream)
 {
 	if (n_profiles <= 0) return;
-	backward_kernel<T><<<n_sm * PF_BACKWARD_MIN_BLOCKS, kWarpsB * 32, 0, stream>>>(
-	    models, profs, (unsigned int)n_profiles, (const T *)gout, (const T *)gsrc, prow_base, n_ring, counter,
-	    partial, ring_partial);
-	grad_reduce_kernel<<<(int)(((long long)n_profiles * 32 + 255) / 256), 256, 0, stream>>>(
-	    models, profs, n_profiles, prow_base, partial, ring_partial, grad);
+	const int blocks = n_sm * PF_BACKWARD_MIN_BLOCKS;
+	const int rblocks = (int)(((long long)n_profiles * 32 + 255) / 256);
+	if (sersic_only) {
+		backward_kernel<T, f32::kSersicOnly><<<blocks, kWarpsB * 32, 0, stream>>>(
+		    models, profs, (unsigned int)n_profiles, (const T *)gout, (const T *)gsrc, prow_base, n_ring, counter,
+		    partial, ring_partial);
+		grad_reduce_kernel<slots_of<f32::kSersicOnly>()><<<rblocks, 256, 0, stream>>>(
+		    models, profs, n_profiles, prow_base, partial, ring_partial, grad);
+	}
+	else {
+		backward_kernel<T, f32::kAllKinds><<<blocks, kWarpsB * 32, 0, stream>>>(
+		    models, profs, (unsigned int)n_profiles, (const T *)gout, (const T *)gsrc, prow_base, n_ring, counter,
+		    partial, ring_partial);
+		grad_reduce_kernel<slots_of<f32::kAllKinds>()><<<rblocks, 256, 0, stream>>>(
+		    models, profs, n_profiles, prow_base, partial, ring_partial, grad);
+	}
 }
 
 long long backward_items(long long n_profiles, long long n_ring)
@@ -788,7 +890,12 @@ long long backward_items(long long n_profiles, long long n_ring)
 	return n_profiles * (kRingRows * kRingCols) + n_profiles * n_ring;
 }
 
-long long backward_ring_slots() { return (long long)kRingRows * kRingCols * kGradSlots; }
+int backward_slots(bool sersic_only)
+{
+	return sersic_only ? slots_of<f32::kSersicOnly>() : slots_of<f32::kAllKinds>();
+}
+
+long long backward_ring_slots(bool sersic_only) { return (long long)kRingRows * kRingCols * backward_slots(sersic_only); }
 
 template void launch_chi2<float>(const ModelDev *, int, const void *, const void *, const void *, const void *, void *,
                                  double *, cudaStream_t);
@@ -796,9 +903,9 @@ template void launch_chi2<double>(const ModelDev *, int, const void *, const voi
                                   void *, double *, cudaStream_t);
 template void launch_backward<float>(const ModelDev *, const ProfileDev *, int, const void *, const void *,
                                      const long long *, unsigned int, unsigned int *, double *, double *, double *,
-                                     int, cudaStream_t);
+                                     bool, int, cudaStream_t);
 template void launch_backward<double>(const ModelDev *, const ProfileDev *, int, const void *, const void *,
                                       const long long *, unsigned int, unsigned int *, double *, double *, double *,
-                                      int, cudaStream_t);
+                                      bool, int, cudaStream_t);
 
 }  // namespace pf

@@ -24,7 +24,7 @@
 namespace pf {
 void launch_setup(const ModelDev *models, ProfileDev *profs, int n_profiles, int n_models,
                   unsigned int *tile_counter, unsigned int *err, const double *psf_raw, double *psf_norm,
-                  bool have_psf, double *solves, cudaStream_t stream);
+                  bool have_psf, double *solves, int want_grad, cudaStream_t stream);
 void launch_eval64(const ModelDev *models, int n_models, const ProfileDev *profs, const double *psf_pool,
                    double *conv_img, double *direct_img, long long n_tiles, unsigned int *tile_counter,
                    DebugRec dbg, int n_sm, cudaStream_t stream);
@@ -78,9 +78,11 @@ void launch_chi2(const ModelDev *models, int n_models, const void *img, const vo
 template <typename T>
 void launch_backward(const ModelDev *models, const ProfileDev *profs, int n_profiles, const void *gout,
                      const void *gsrc, const long long *prow_base, unsigned int n_ring, unsigned int *counter,
-                     double *partial, double *ring_partial, double *grad, int n_sm, cudaStream_t stream);
+                     double *partial, double *ring_partial, double *grad, bool sersic_only, int n_sm,
+                     cudaStream_t stream);
 long long backward_items(long long n_profiles, long long n_ring);
-long long backward_ring_slots();
+int backward_slots(bool sersic_only);
+long long backward_ring_slots(bool sersic_only);
 }  // namespace pf
 
 namespace {
@@ -342,8 +344,8 @@ struct pf_batch {
 	bool adjoint = false;
 	void *d_gout = nullptr;
 	void *d_gsrc = nullptr;
-	double *d_partial = nullptr;        // kGradSlots FP64 per (profile, drawing row)
-	double *d_ring_partial = nullptr;   // kGradSlots FP64 per (profile, ring tile)
+	double *d_partial = nullptr;        // backward_slots() FP64 per (profile, drawing row)
+	double *d_ring_partial = nullptr;   // backward_slots() FP64 per (profile, ring tile)
 	long long *d_prow_base = nullptr;   // first partial row of each profile
 	unsigned int *d_bwd_counter = nullptr;
 	unsigned int n_ring = 0;            // row items per profile: twice the tallest drawing area
@@ -898,7 +900,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 	if (any_psf) {
 		// PSF normalisation (Model::set_psf), once per batch
 		pf::launch_setup(b->d_models, b->d_profiles, 0, (int)n_models, b->d_counter, b->d_err, b->d_psf_raw,
-		                 b->d_psf_norm, true, b->d_solves, env->stream);
+		                 b->d_psf_norm, true, b->d_solves, 0, env->stream);
 		if (!b->dbl) {
 			PF_CUDA_TRY(cudaMalloc(&b->d_psf32, sizeof(float) * psf_pool_len));
 			pf::launch_psf_to_float(b->d_psf_norm, b->d_psf32, (long long)psf_pool_len, env->stream);
@@ -1274,7 +1276,7 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 	}
 	long t = stage_begin(b, ST_SETUP, stream);
 	pf::launch_setup(b->d_models, b->d_profiles, n_profiles, n_models, b->d_counter, b->d_err, nullptr, nullptr,
-	                 false, b->d_solves, stream);
+	                 false, b->d_solves, b->adjoint ? 1 : 0, stream);
 	stage_end(b, t, stream);
 	if (b->dbl) {
 		t = stage_begin(b, ST_EVAL, stream);
@@ -1386,10 +1388,12 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	if (b->adjoint) return PF_OK;
 	for (size_t i = 0; i < b->profiles.size(); i++) {
 		const pf_profile_desc &d = b->profiles[i];
-		const bool ok = (d.kind == PF_SERSIC && !d.rescale_flux) || d.kind == PF_SKY || d.kind == PF_NULL;
+		const bool ok = (d.kind >= PF_SERSIC && d.kind <= PF_BROKENEXP && !(d.kind == PF_SERSIC && d.rescale_flux)) ||
+		                d.kind == PF_SKY || d.kind == PF_NULL;
 		if (!ok) {
 			return fail(PF_ERR_UNSUPPORTED, "profile " + std::to_string(i) +
-			                                    ": the adjoint supports sersic (without rescale_flux), sky and null");
+			                                    ": the adjoint supports the radial profiles (a sersic without "
+			                                    "rescale_flux), sky and null");
 		}
 	}
 	PF_CUDA_TRY(cudaSetDevice(b->env->device));
@@ -1430,8 +1434,9 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	if (b->adj_smem > 227 * 1024) return fail(PF_ERR_UNSUPPORTED, "PSF too large for the adjoint convolution");
 	PF_CUDA_TRY(cudaMalloc(&b->d_gout, elem * std::max<uint64_t>(1, b->total_out)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_gsrc, elem * std::max<size_t>(1, b->draw_total)));
-	PF_CUDA_TRY(cudaMalloc(&b->d_partial, sizeof(double) * pf::kGradSlots * std::max<long long>(1, rows)));
-	PF_CUDA_TRY(cudaMalloc(&b->d_ring_partial, sizeof(double) * pf::backward_ring_slots() *
+	PF_CUDA_TRY(cudaMalloc(&b->d_partial, sizeof(double) * pf::backward_slots(b->sersic_only) *
+	                                          std::max<long long>(1, rows)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_ring_partial, sizeof(double) * pf::backward_ring_slots(b->sersic_only) *
 	                                               std::max<size_t>(1, b->profiles.size())));
 	PF_CUDA_TRY(cudaMalloc(&b->d_prow_base, sizeof(long long) * prow_base.size()));
 	PF_CUDA_TRY(cudaMalloc(&b->d_bwd_counter, sizeof(unsigned int)));
@@ -1517,10 +1522,10 @@ pf_status pf_backward(pf_batch *b, const void *images_dev, const void *data_dev,
 	PF_CUDA_TRY(cudaMemsetAsync(b->d_bwd_counter, 0, sizeof(unsigned int), stream));
 	if (b->dbl) pf::launch_backward<double>(b->d_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc,
 	                                        b->d_prow_base, b->n_ring, b->d_bwd_counter, b->d_partial,
-	                                        b->d_ring_partial, grad_dev, b->env->n_sm, stream);
+	                                        b->d_ring_partial, grad_dev, b->sersic_only, b->env->n_sm, stream);
 	else pf::launch_backward<float>(b->d_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc, b->d_prow_base,
 	                                b->n_ring, b->d_bwd_counter, b->d_partial, b->d_ring_partial, grad_dev,
-	                                b->env->n_sm, stream);
+	                                b->sersic_only, b->env->n_sm, stream);
 	stage_end(b, t, stream);
 	b->backward_calls++;
 	{

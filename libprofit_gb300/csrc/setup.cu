@@ -11,6 +11,7 @@
 
 #include "pf_device.cuh"
 #include "profiles_f64.cuh"
+#include "profiles_grad.cuh"
 #include "specfun.cuh"
 
 namespace pf {
@@ -269,29 +270,98 @@ __device__ double dbn_dn(double n, double bn)
 	return -2 * dpda / pdf;
 }
 
-__device__ void adjoint_constants(ProfileDev &p, double dbn)
+// r f(r) d ln f / d par[6 + k]: the integrand of d lumtot / d par[6 + k]
+// (divided by 2 pi) for the profiles whose lumtot is an integral
+struct LumtotDerivIntegrand {
+	const grad::GShape<double> *s;
+	int k;
+	__device__ double operator()(double r) const
+	{
+		double lnf, G, d[5] = {0., 0., 0., 0., 0.};
+		if (!grad::radial_terms<double>(*s, r, lnf, G, d)) return 0.;
+		const double f = exp(lnf);
+		return f > 0. ? r * f * d[k] : 0.;
+	}
+};
+
+// d ln flux_scale / d par[k] of the other radial profiles:
+//   ln flux_scale = const - 0.4 ln(10) mag - ln get_lumtot(shape) - ln axrat + ln r_box(box)
+// (src/radial.cpp:147-153). get_lumtot is closed-form for moffat
+// (pi rs^2 / (con - 1), src/moffat.cpp:77-79) and ferrer (pi rout^2 a B(a, 1 +
+// 2/(2-b)), src/ferrer.cpp:78-101), and 2 pi int_0^R r f(r) dr otherwise
+// (src/coresersic.cpp:92-104, src/king.cpp:87-96, src/brokenexponential.cpp:
+// 115-126), whose derivatives are the integrals of r df/dpar over the same
+// range (f vanishes at the king's R = rt), taken with the same QUADPACK
+// routines at a tighter tolerance. `lum_int` = that integral.
+__device__ void other_lumtot_derivatives(ProfileDev &p, double lum_int)
+{
+	const grad::GShape<double> s = grad::make_gshape<double>(p);
+	switch (p.kind) {
+	case PF_MOFFAT: {
+		const double fwhm = p.par[6], con = p.par[7];
+		p.dlnfs[6] = -2 / fwhm;
+		p.dlnfs[7] = 1 / (con - 1) - 2 * (double)s.k[1];
+		break;
+	}
+	case PF_FERRER: {
+		const double rout = p.par[6], a = p.par[7], b = p.par[8];
+		const double c = 1 + 2 / (2 - b);
+		p.dlnfs[6] = -2 / rout;
+		p.dlnfs[7] = -(1 / a + sf::digamma(a) - sf::digamma(a + c));
+		p.dlnfs[8] = -(sf::digamma(c) - sf::digamma(a + c)) * 2 / ((2 - b) * (2 - b));
+		break;
+	}
+	case PF_CORESERSIC:
+	case PF_KING:
+	case PF_BROKENEXP: {
+		const int n_shape = p.kind == PF_CORESERSIC ? 5 : (p.kind == PF_KING ? 3 : 4);
+		const bool infinite = p.kind != PF_KING;
+		const double upper = p.kind == PF_KING ? p.par[7] : 0.;
+		for (int k = 0; k < n_shape; k++) {
+			const double dint = sf::qag(LumtotDerivIntegrand{&s, k}, 0., upper, infinite,
+			                            1e-12 * fabs(lum_int), 1e-9, nullptr);
+			p.dlnfs[6 + k] = -dint / lum_int;
+		}
+		break;
+	}
+	default:
+		break;
+	}
+}
+
+// `lum_int` = get_lumtot / (2 pi) for the integral profiles; `want` = the
+// batch runs the adjoint (the integrals are skipped otherwise)
+__device__ void adjoint_constants(ProfileDev &p, double dbn, double lum_int, int want)
 {
 	for (int k = 0; k < PF_NPAR; k++) p.dlnfs[k] = 0.;
 	p.dbn = 0.;
 	p.grad_ok = 0;
-	if (p.kind != PF_SERSIC || p.rescale_flux) {
+	if ((p.kind == PF_SERSIC && p.rescale_flux) || p.kind < PF_SERSIC || p.kind > PF_BROKENEXP) {
 		return;
 	}
-	const double n = p.par[7], re = p.par[6], q = p.par[PF_P_AXRAT], B = p.par[PF_P_BOX] + 2;
-	p.dbn = dbn;
+	const double q = p.par[PF_P_AXRAT], B = p.par[PF_P_BOX] + 2;
 	p.dlnfs[PF_P_MAG] = -0.4 * log(10.);
 	p.dlnfs[PF_P_AXRAT] = -1 / q;
 	p.dlnfs[PF_P_BOX] = 1 / B + (2 / (B * B)) * (sf::digamma(1 / B) - sf::digamma(2 / B));
-	p.dlnfs[6] = -2 / re;
-	p.dlnfs[7] = -(1 / n + 2 * sf::digamma(2 * n) + dbn - 2 * log(p.bn) - 2 * n * dbn / p.bn);
-	p.fbn = (float)p.bn;
-	p.fdbn = (float)dbn;
-	p.fnser = (float)n;
-	p.fre = (float)re;
+	if (p.kind == PF_SERSIC) {
+		const double n = p.par[7], re = p.par[6];
+		p.dbn = dbn;
+		p.dlnfs[6] = -2 / re;
+		p.dlnfs[7] = -(1 / n + 2 * sf::digamma(2 * n) + dbn - 2 * log(p.bn) - 2 * n * dbn / p.bn);
+		p.fbn = (float)p.bn;
+		p.fdbn = (float)dbn;
+		p.fnser = (float)n;
+		p.fre = (float)re;
+	}
+	else {
+		if (p.kind == PF_CORESERSIC) p.dbn = dbn;
+		if (want) other_lumtot_derivatives(p, lum_int);
+	}
 	p.grad_ok = 1;
 }
 
-__device__ void radial_setup(ProfileDev &p, const ModelDev &m, double bn, const SersicSolves &sv, unsigned int *err)
+__device__ void radial_setup(ProfileDev &p, const ModelDev &m, double bn, const SersicSolves &sv, int want_grad,
+                             unsigned int *err)
 {
 	if (p.kind == PF_SERSIC) {
 		choose_rfactor(p);
@@ -303,7 +373,8 @@ __device__ void radial_setup(ProfileDev &p, const ModelDev &m, double bn, const 
 	const double box = p.par[PF_P_BOX], axrat = p.par[PF_P_AXRAT];
 	double b2 = box + 2;
 	double r_box = M_PI * b2 / (2 * sf::beta(1 / b2, 1 / b2));
-	double lumtot = get_lumtot(p) * axrat / r_box;
+	const double lum_raw = get_lumtot(p);
+	double lumtot = lum_raw * axrat / r_box;
 	p.lumtot = lumtot;
 	p.ie = pow(10, -0.4 * (p.par[PF_P_MAG] - m.magzero)) / lumtot;
 	if (p.adjust) {
@@ -370,7 +441,7 @@ __device__ void radial_setup(ProfileDev &p, const ModelDev &m, double bn, const 
 		}
 	}
 	fold_single_precision(p);
-	adjoint_constants(p, sv.dbn);
+	adjoint_constants(p, sv.dbn, lum_raw / (2 * M_PI), want_grad);
 	p.center_boost = p.kind == PF_SERSIC && p.adjust && p.par[7] > 1;
 	unsigned int max_res = p.resolution;
 	unsigned int max_rec = p.max_recursions;
@@ -415,7 +486,8 @@ __global__ void setup_solves_kernel(const ProfileDev *profs, int n_profiles, dou
 }
 
 __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs, int n_profiles,
-                                      const double *solves, unsigned int *tile_counter, unsigned int *err)
+                                      const double *solves, int want_grad, unsigned int *tile_counter,
+                                      unsigned int *err)
 {
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		*tile_counter = 0;
@@ -428,7 +500,7 @@ __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs,
 	const double nser = profs[t].par[7];
 	const double bn = solves[(size_t)t * 3 + 0];
 	SersicSolves sv{solves[(size_t)t * 3 + 1], solves[(size_t)t * 3 + 2], 0.};
-	if (kind == PF_SERSIC && !profs[t].rescale_flux) {
+	if ((kind == PF_SERSIC && !profs[t].rescale_flux) || (kind == PF_CORESERSIC && want_grad)) {
 		sv.dbn = dbn_dn(nser, bn);
 	}
 	ProfileDev p = profs[t];
@@ -438,7 +510,7 @@ __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs,
 	p.rscale_switch = p.rscale_switch_in;
 	p.rscale_max = p.rscale_max_in;
 	if (p.kind >= PF_SERSIC && p.kind <= PF_BROKENEXP) {
-		radial_setup(p, m, bn, sv, err);
+		radial_setup(p, m, bn, sv, want_grad, err);
 	}
 	else if (p.kind == PF_SKY) {
 		p.bg = p.par[6] / (m.fs * m.fs);  // src/sky.cpp:42-45
@@ -475,7 +547,7 @@ __global__ void normalise_psf_kernel(const ModelDev *models, const double *raw, 
 
 void launch_setup(const ModelDev *models, ProfileDev *profs, int n_profiles, int n_models,
                   unsigned int *tile_counter, unsigned int *err, const double *psf_raw, double *psf_norm,
-                  bool have_psf, double *solves, cudaStream_t stream)
+                  bool have_psf, double *solves, int want_grad, cudaStream_t stream)
 {
 	// single-warp blocks: the FP64-heavy work spreads over as many SMs as possible
 	if (n_profiles > 0) {
@@ -484,7 +556,8 @@ void launch_setup(const ModelDev *models, ProfileDev *profs, int n_profiles, int
 	}
 	int blocks = (n_profiles + 31) / 32;
 	if (blocks < 1) blocks = 1;
-	setup_profiles_kernel<<<blocks, 32, 0, stream>>>(models, profs, n_profiles, solves, tile_counter, err);
+	setup_profiles_kernel<<<blocks, 32, 0, stream>>>(models, profs, n_profiles, solves, want_grad, tile_counter,
+	                                                 err);
 	if (have_psf && n_models > 0) {
 		normalise_psf_kernel<<<n_models, 128, 0, stream>>>(models, psf_raw, psf_norm);
 	}

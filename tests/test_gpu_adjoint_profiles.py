@@ -1,0 +1,191 @@
+"""Adjoint of the coresersic, moffat, ferrer, king and brokenexp profiles
+against central finite differences of the FP64 oracle (GPU).
+
+One 64 x 64 model per profile kind (the profile convolved by a 15 x 15 Moffat
+PSF, plus a sky), round and boxy; data = the oracle's image at parameters
+perturbed by 5 % plus noise; chi^2 = sum ((model - data) / sigma)^2. Every
+parameter of the profile (xcen, ycen, mag, ang, axrat, box and the kind's own)
+and the sky's bg must match central differences of the oracle's chi^2 with
+h = 1e-6 relative, with the bars of the sersic adjoint test:
+  * FP64 path: |g - fd| <= 1e-4 |fd| + 1e-9 chi^2 / h
+  * FP32 path: |g - fd| <= 1e-3 |fd| + 1e-6 chi^2 / h
+Parameters whose finite difference is not that of a smooth function are
+excluded (at most two per case): those whose +-h changes the oracle's
+subsampling tree (level counts), which the adjoint holds fixed, and those
+whose difference quotient moves by more than 2e-5 relative when h shrinks ten
+times -- a sub-point near the cusp of a coresersic (f ~ r^-b at its centre)
+makes the h = 1e-6 quotient depart from the derivative by up to a few 1e-4,
+while the quotients of smaller steps converge to the adjoint's value.
+A batch holding all the models (and a sersic one, so that the twelve-slot
+kernels also run the sersic's terms) gives every model's gradient as the
+single-model batches do.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SIDE = 64
+MAGZERO = 25.0
+GEOM = ("xcen", "ycen", "mag", "ang", "axrat", "box")
+OWN = {
+    "coresersic": dict(re=8.0, nser=2.5, rb=2.0, a=3.0, b=0.5),
+    "moffat": dict(fwhm=6.0, con=2.5),
+    "ferrer": dict(rout=20.0, a=1.5, b=0.6),
+    "king": dict(rc=4.0, rt=25.0, a=2.0),
+    "brokenexp": dict(h1=5.0, h2=3.0, rb=10.0, a=1.0),
+}
+ORDER = {k: list(GEOM) + list(v) for k, v in OWN.items()}
+# (kind, box, overrides of OWN): round and boxy, plus a coresersic without the
+# central cusp (b = 0), whose centre derivatives the finite differences can check
+CASES = [(kind, box, None) for kind in OWN for box in (0.0, 0.2)] + [("coresersic", 0.1, dict(b=0.0))]
+IDS = ["%s-box%g%s" % (k, b, "-flat" if o else "") for k, b, o in CASES]
+
+
+def _truth(kind, box, over):
+    p = dict(xcen=31.3, ycen=29.6, mag=15.0, ang=33.0, axrat=0.7, box=box, convolve=True)
+    p.update(OWN[kind])
+    p.update(over or {})
+    return [(kind, p), ("sky", dict(bg=1.0))]
+
+
+def _with(profiles, i, k, v):
+    out = [(kind, dict(p)) for kind, p in profiles]
+    out[i][1][k] = v
+    return out
+
+
+def _problem(O, kind, box, over):
+    import workloads as W
+    rng = np.random.default_rng(sum(map(ord, kind)) * 10 + int(round(box * 10)))
+    psf = W.moffat_psf(15, 3.0, 2.5)
+    truth = _truth(kind, box, over)
+    data, _, _ = O.evaluate(O.Case(SIDE, SIDE, truth, psf=psf, magzero=MAGZERO))
+    perturbed = []
+    for k_, p in truth:
+        q = dict(p)
+        for k in q:
+            if k in ("convolve", "box") or q[k] == 0:
+                continue
+            q[k] = q[k] + 0.3 * rng.normal() if k in ("xcen", "ycen") else q[k] * (1 + 0.05 * rng.normal())
+        if k_ != "sky":
+            q["axrat"] = min(q["axrat"], 1.0)
+            q["box"] = box + (0.02 * rng.normal() if box else 0.0)
+        perturbed.append((k_, q))
+    sigma = 0.01 * data.max()
+    data = data + rng.normal(0, sigma, data.shape)
+    return psf, perturbed, data, np.full_like(data, sigma)
+
+
+def _chi2(O, psf, profiles, data, sigma):
+    img, _, counts = O.evaluate(O.Case(SIDE, SIDE, profiles, psf=psf, magzero=MAGZERO))
+    return float(np.sum(((img - data) / sigma) ** 2)), counts
+
+
+def _fd(O, psf, profiles, data, sigma):
+    chi0, counts0 = _chi2(O, psf, profiles, data, sigma)
+    out = {}
+    names = [(0, k) for k in ORDER[profiles[0][0]]] + [(1, "bg")]
+    for i, k in names:
+        v = profiles[i][1][k]
+        h = 1e-6 * max(abs(v), 1e-3)
+        cp, c_p = _chi2(O, psf, _with(profiles, i, k, v + h), data, sigma)
+        cm, c_m = _chi2(O, psf, _with(profiles, i, k, v - h), data, sigma)
+        same_tree = np.array_equal(c_p, counts0) and np.array_equal(c_m, counts0)
+        fd = (cp - cm) / (2 * h)
+        cp2, _ = _chi2(O, psf, _with(profiles, i, k, v + h / 10), data, sigma)
+        cm2, _ = _chi2(O, psf, _with(profiles, i, k, v - h / 10), data, sigma)
+        fd2 = (cp2 - cm2) / (2 * h / 10)
+        smooth = abs(fd - fd2) <= 2e-5 * abs(fd) + 1e-9 * chi0 / h
+        out[(i, k)] = (fd, same_tree and smooth, h)
+    return out
+
+
+def _slot(kind, k):
+    if k == "bg":
+        return 6
+    order = ORDER[kind]
+    return order.index(k)  # par[0..5] geometric, par[6..] the kind's own, in registration order
+
+
+@pytest.fixture(scope="module")
+def problems(oracle_lib):
+    out = {}
+    for kind, box, over in CASES:
+        psf, profiles, data, sigma = _problem(oracle_lib, kind, box, over)
+        out[(kind, box, bool(over))] = (psf, profiles, data, sigma, _fd(oracle_lib, psf, profiles, data, sigma))
+    return out
+
+
+def _models(pg, W, env, specs):
+    return [W.to_model(dict(width=SIDE, height=SIDE, psf=psf, profiles=profiles, magzero=MAGZERO), env)
+            for psf, profiles in specs]
+
+
+def _gpu_grads(specs, datas, sigmas, use_double):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build_cuda()
+    import libprofit_gb300 as pg
+    import workloads as W
+    env = pg.get_cuda_environment(0, use_double=use_double)
+    models = _models(pg, W, env, specs)
+    b = pg.Batch(models, env)
+    b.enable_adjoint()
+    dt = torch.float64 if use_double else torch.float32
+    img = torch.zeros(b.total_pixels, dtype=dt, device="cuda")
+    d = torch.tensor(np.concatenate([x.ravel() for x in datas]), dtype=dt, device="cuda")
+    s = torch.tensor(np.concatenate([x.ravel() for x in sigmas]), dtype=dt, device="cuda")
+    chi2 = torch.zeros(len(models), dtype=torch.float64, device="cuda")
+    n_prof = sum(len(p) for _, p in specs)
+    grad = torch.zeros(n_prof * 12, dtype=torch.float64, device="cuda")
+    b.forward_backward(img, d, s, chi2, grad)
+    b.check()
+    return chi2.cpu().numpy(), grad.cpu().numpy().reshape(n_prof, 12)
+
+
+@pytest.mark.parametrize("use_double", [True, False])
+@pytest.mark.parametrize("kind,box,over", CASES, ids=IDS)
+def test_profile_gradient_matches_finite_differences(problems, oracle_lib, kind, box, over, use_double):
+    psf, profiles, data, sigma, fd = problems[(kind, box, bool(over))]
+    chi2, grad = _gpu_grads([(psf, profiles)], [data], [sigma], use_double)
+    chi2_ref, _ = _chi2(oracle_lib, psf, profiles, data, sigma)
+    assert abs(chi2[0] - chi2_ref) <= (1e-10 if use_double else 1e-4) * chi2_ref
+    rtol, floor = (1e-4, 1e-9) if use_double else (1e-3, 1e-6)
+    checked = skipped = 0
+    for (i, k), (want, same_tree, h) in fd.items():
+        if not same_tree:
+            skipped += 1
+            continue
+        got = grad[i, _slot(kind, k) if i == 0 else 6]
+        atol = floor * chi2_ref / h
+        assert abs(got - want) <= rtol * abs(want) + atol, \
+            "%s box %g %s: adjoint %.8g vs fd %.8g" % (kind, box, k, got, want)
+        checked += 1
+    assert skipped <= 2 and checked >= len(fd) - 2
+
+
+@pytest.mark.parametrize("use_double", [True, False])
+def test_mixed_batch_equals_single_models(problems, use_double):
+    import tests.test_gpu_adjoint as S
+    from oracle import oracle as O
+    specs, datas, sigmas = [], [], []
+    for kind, box, over in CASES:
+        psf, profiles, data, sigma, _ = problems[(kind, box, bool(over))]
+        specs.append((psf, profiles))
+        datas.append(data)
+        sigmas.append(sigma)
+    spsf, sprof, sdata, ssig = S.make_problem(O)
+    specs.append((spsf, sprof))
+    datas.append(sdata)
+    sigmas.append(ssig)
+    chi2_all, g_all = _gpu_grads(specs, datas, sigmas, use_double)
+    row = 0
+    tol = 1e-9 if use_double else 1e-5
+    for j, (spec, data, sigma) in enumerate(zip(specs, datas, sigmas)):
+        chi2_one, g_one = _gpu_grads([spec], [data], [sigma], use_double)
+        n = len(spec[1])
+        assert abs(chi2_all[j] - chi2_one[0]) <= tol * chi2_one[0]
+        scale = np.abs(g_one).max()
+        np.testing.assert_allclose(g_all[row:row + n], g_one, rtol=tol * 100, atol=tol * scale)
+        row += n
