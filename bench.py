@@ -8,7 +8,17 @@ parameter vector, render every model (FP32 values, FP64 geometry and
 decisions), chi^2 per model and d chi^2 / d (all 16 parameters of every
 model) in FP64. Inputs are synthetic and seeded (workloads.py).
 
+Other workloads (--workload, one JSON line each, same keys):
+  cfg2  one 1000x1000 model (bulge + disk + sky, 51x51 PSF by FFT): FP32 and
+        FP64 forward, models/s, with the FP32 result's errors against FP64;
+  cfg3  4096 uneven models (1-3 of the six radial kinds, own PSFs, method by
+        the autotuner): FP32 forward of the whole batch, models/s;
+  cfg5  the 4096x4096 field with 10,000 profiles and a sky, 101x101 PSF by an
+        8192x8192 FFT: FP32 forward + chi^2 + gradients of all 10,001
+        profiles, fields/s.
+
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                       [--workload cfg4|cfg2|cfg3|cfg5]
 Under torchrun each rank renders its own copy of the workload (weak scaling,
 no collective on the data path); rank 0 prints one JSON line.
 --impl reference times the CPU oracle port of the reference's
@@ -45,6 +55,8 @@ def parse():
                     help="convolution method of the FP32 batch (auto: the library's choice)")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch the step's kernels one by one instead of replaying its CUDA graph")
+    ap.add_argument("--workload", default="cfg4", choices=["cfg4", "cfg2", "cfg3", "cfg5"],
+                    help="cfg4 (default): the batched model + VJP step; the others: see the module docstring")
     return ap.parse_args()
 
 
@@ -329,10 +341,17 @@ def run_ours(args, world, rank, local):
     batch.record_depth(False)
     evals = float(counts[30] + counts[31])
 
-    # the plain FP64 per-model path (forward + VJP, one model per launch sequence)
+    # the plain FP64 per-model path (forward + VJP, one model per launch
+    # sequence), timed on four models; on eight, its images, chi^2 and
+    # gradients against the FP32 batch's (accuracy of the timed step)
     fp64_rates = []
+    acc = {"flux": [], "pixel": [], "chi2": [], "grad": []}
+    img32 = img.cpu().numpy()
+    chi32 = chi2.cpu().numpy()
+    grad32 = grad.cpu().numpy().reshape(n_prof, 12)
+    first_prof = np.cumsum([0] + [len(s["profiles"]) for s in specs])
     if rank == 0:
-        for i in range(4):
+        for i in range(min(8, n_models)):
             spec = specs[i]
             b1 = pg.Batch([W.to_model(spec, env64)], env64)
             b1.enable_adjoint()
@@ -345,6 +364,19 @@ def run_ours(args, world, rank, local):
             with torch.cuda.stream(stream):
                 b1.forward_backward(im1, d1, s1, c1, g1, stream=sh)
             torch.cuda.synchronize()
+            ref = im1.cpu().numpy()
+            got = img32[batch.offsets[i]:batch.offsets[i + 1]].astype(np.float64)
+            peak = np.abs(ref).max()
+            bright = np.abs(ref) > 1e-9 * peak
+            acc["pixel"].append(float(np.max(np.abs(got[bright] - ref[bright]) / np.abs(ref[bright]))))
+            acc["flux"].append(abs(got.sum() - ref.sum()) / abs(ref.sum()))
+            acc["chi2"].append(abs(chi32[i] - c1.item()) / abs(c1.item()))
+            g64 = g1.cpu().numpy().reshape(-1, 12)[:, :8]
+            g32 = grad32[first_prof[i]:first_prof[i + 1], :8]
+            acc["grad"].append(float(np.max(np.abs(g32 - g64) / np.maximum(np.abs(g64), 1e-3 * np.abs(g64).max()))))
+            if i >= 4:
+                b1.close()
+                continue
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             reps = 3
@@ -356,6 +388,32 @@ def run_ours(args, world, rank, local):
             fp64_rates.append(reps / (e0.elapsed_time(e1) / 1000.0))
             b1.close()
     fp64_rate = statistics.median(fp64_rates) if fp64_rates else None
+
+    # the same step with every convolution forced to the FFT (the autotuner
+    # picks the direct convolution for this PSF size): models/s
+    fft_forced = None
+    if rank == 0 and args.convolver == "auto" and not args.no_graph:
+        models_f = [W.to_model(s, env32) for s in specs]
+        for m in models_f:
+            m.set_convolver("fft")
+        bf = pg.Batch(models_f, env32)
+        bf.enable_adjoint()
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                bf.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
+        torch.cuda.synchronize()
+        nf = max(3, args.steps // 2)
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        with torch.cuda.stream(stream):
+            for _ in range(nf):
+                bf.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        bf.check(stream=sh)
+        fms = f0.elapsed_time(f1) / nf
+        fft_forced = {"value": n_models / (fms / 1000.0), "unit": "models/s", "ms_per_step": fms, "steps": nf}
+        bf.close()
 
     if rank != 0:
         return
@@ -407,6 +465,16 @@ def run_ours(args, world, rank, local):
                    (2 * 4 * pix_per_step / 1e6)},
         "mpix_per_s": world * pix_per_step * args.steps / (ms / 1000.0) / 1e6,
         "fp64_per_model_evals_per_s": fp64_rate,
+        "accuracy": {"vs": "plain FP64 GPU path, same models and data (that path equals libprofit's CPU "
+                           "result to 1e-10 per pixel)",
+                     "models": len(acc["flux"]),
+                     "max_rel_flux_err": max(acc["flux"]) if acc["flux"] else None,
+                     "max_rel_pixel_err": max(acc["pixel"]) if acc["pixel"] else None,
+                     "pixel_floor": "pixels above 1e-9 x the model's peak",
+                     "max_rel_chi2_err": max(acc["chi2"]) if acc["chi2"] else None,
+                     "max_rel_grad_err": max(acc["grad"]) if acc["grad"] else None,
+                     "grad_floor": "1e-3 x the model's largest gradient component"},
+        "fft_forced": fft_forced,
         "ratio_vs_fp64_per_model": (value / world) / fp64_rate if fp64_rate else None,
         "stage_ms_per_step": per_step,
         "roofline": roof,
@@ -422,12 +490,188 @@ def run_ours(args, world, rank, local):
     }
     print(json.dumps(line), flush=True)
 
+def run_workload(args, world, rank, local):
+    """--workload cfg2 / cfg3 / cfg5 (module docstring)."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build_cuda()
+    import libprofit_gb300 as pg
+    import workloads as W
+
+    torch.cuda.set_device(local)
+    env64 = pg.get_cuda_environment(local, use_double=True)
+    env32 = pg.get_cuda_environment(local, use_double=False, profile=True)
+    specs = W.CONFIGS[int(args.workload[3:])]()
+    with_grad = args.workload == "cfg5"
+    models = [W.to_model(s, env32) for s in specs]
+    batch = pg.Batch(models, env32)
+    img = torch.zeros(batch.total_pixels, dtype=torch.float32, device="cuda")
+    n_models = len(specs)
+    pix = sum(w * h for (w, h) in batch.dims)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    if with_grad:
+        batch.enable_adjoint()
+        with torch.cuda.stream(stream):
+            batch.forward(img, stream=sh)
+        torch.cuda.synchronize()
+        rng = np.random.Generator(np.random.PCG64(5000 + rank))
+        ref = img.cpu().numpy().astype(np.float64)
+        sig = 0.01 * np.abs(ref).max()
+        data = torch.tensor(ref + rng.normal(0, sig, ref.shape), dtype=torch.float32, device="cuda")
+        sigma = torch.full_like(data, sig)
+        chi2 = torch.zeros(n_models, dtype=torch.float64, device="cuda")
+        grad = torch.zeros(batch.n_profiles * 12, dtype=torch.float64, device="cuda")
+        params = torch.tensor(W.param_matrix(specs).ravel(), dtype=torch.float64, device="cuda")
+
+    def step():
+        if with_grad:
+            batch.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
+        else:
+            batch.forward(img, stream=sh)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    batch.check(stream=sh)
+    batch.stats(reset=True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = max_over_ranks(world, ev0.elapsed_time(ev1))
+    clk = clocks.stop()
+    batch.check(stream=sh)
+    stages = batch.stats(reset=True)
+    launches = int(stages["kernel_launches"])
+    if with_grad:  # stage breakdown from the same steps launched one by one
+        with torch.cuda.stream(stream):
+            for _ in range(args.steps):
+                batch.set_params_dev(params, stream=sh)
+                batch.forward_backward(img, data, sigma, chi2, grad, stream=sh)
+        torch.cuda.synchronize()
+        stages = batch.stats(reset=True)
+    per_step = {k: stages[k] / max(1, args.steps) for k in
+                ("setup_ms", "eval_ms", "finish_ms", "chi2_ms", "adjoint_conv_ms", "backward_ms")}
+    value = world * n_models * args.steps / (ms / 1000.0)
+
+    # e2e through the public API: parameters in from pinned host memory, the
+    # images (forward) or chi^2 and gradients (cfg5) back, every step
+    h_par = torch.tensor(W.param_matrix(specs).ravel(), dtype=torch.float64).pin_memory()
+    d_par = torch.zeros_like(h_par, device="cuda")
+    if with_grad:
+        h_out = [torch.zeros(n_models, dtype=torch.float64).pin_memory(),
+                 torch.zeros(batch.n_profiles * 12, dtype=torch.float64).pin_memory()]
+        dev_out = [chi2, grad]
+    else:
+        h_out = [torch.zeros(batch.total_pixels, dtype=torch.float32).pin_memory()]
+        dev_out = [img]
+    e2e_steps = max(3, args.steps // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for _ in range(e2e_steps):
+            if with_grad:
+                params.copy_(h_par, non_blocking=True)
+                batch.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
+            else:
+                d_par.copy_(h_par, non_blocking=True)
+                batch.set_params_dev(d_par, stream=sh)
+                batch.forward(img, stream=sh)
+            for h, d in zip(h_out, dev_out):
+                h.copy_(d, non_blocking=True)
+            stream.synchronize()
+    e2e_value = world * n_models * e2e_steps / max_over_ranks(world, time.perf_counter() - t0)
+    if rank != 0:
+        return
+
+    # accuracy against the FP64 path on a sample of the models (cfg5: the
+    # direct convolution, the FP64 FFT stopping at 4096 points)
+    got = img.cpu().numpy().astype(np.float64)
+    pick = list(range(n_models)) if n_models <= 4 else list(range(0, n_models, 64))
+    models64 = [W.to_model(dict(specs[i], convolver="brute") if args.workload == "cfg5" else specs[i], env64)
+                for i in pick]
+    b64 = pg.Batch(models64, env64)
+    img64 = torch.zeros(b64.total_pixels, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    t64 = time.perf_counter()
+    b64.forward(img64)
+    b64.check()
+    t64 = time.perf_counter() - t64
+    o64 = img64.cpu().numpy()
+    flux_err, pix_err, abs_err = [], [], []
+    for j, i in enumerate(pick):
+        a = got[batch.offsets[i]:batch.offsets[i + 1]]
+        r = o64[b64.offsets[j]:b64.offsets[j + 1]]
+        peak = np.abs(r).max()
+        bright = np.abs(r) > 1e-3 * peak
+        flux_err.append(abs(a.sum() - r.sum()) / abs(r.sum()))
+        pix_err.append(float(np.max(np.abs(a[bright] - r[bright]) / np.abs(r[bright]))))
+        abs_err.append(float(np.max(np.abs(a - r)) / peak))
+    b64.close()
+
+    cpu = None
+    if not args.no_cpu_baseline and args.workload != "cfg5":
+        from oracle import oracle as O
+        O.build(with_ref=False)
+        threads = os.cpu_count() or 1
+        t0 = time.time()
+        done = 0
+        for spec in specs:
+            O.evaluate(W.to_oracle_case(dict(spec, convolver="brute")), threads=threads)
+            done += 1
+            if time.time() - t0 > 8.0:
+                break
+        dt = time.time() - t0
+        cpu = {"value": done / dt, "unit": "models/s", "cores": threads, "kind": "port",
+               "sample": "%d model(s) rendered (direct convolution) in %.1f s" % (done, dt)}
+    dom = max(per_step, key=per_step.get)
+    desc = {"cfg2": "one 1000x1000 model: sersic bulge + disk + sky, 51x51 Moffat PSF by FFT, forward",
+            "cfg3": "4096 models, sides 64-512, 1-3 radial profiles of six kinds, own Moffat PSFs (15-41), "
+                    "autotuned convolution, forward",
+            "cfg5": "one 4096x4096 field: 10,000 radial profiles + sky, 101x101 Moffat PSF by an 8192x8192 FFT, "
+                    "forward + chi2 + gradients of all profiles"}[args.workload]
+    line = {
+        "metric": METRIC, "value": value, "unit": "models/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": desc, "models_per_gpu": n_models, "pixels": pix,
+                   "l2": "inputs larger than L2" if pix * 4 > 129e6 else "inputs smaller than L2"},
+        "mpix_per_s": world * pix * args.steps / (ms / 1000.0) / 1e6,
+        "fp64_forward_s": t64, "fp64_models": len(pick),
+        "accuracy": {"vs": "plain FP64 GPU path", "models": len(pick), "max_rel_flux_err": max(flux_err),
+                     "max_rel_pixel_err": max(pix_err), "pixel_floor": "pixels above 1e-3 x the model's peak",
+                     "max_abs_err_of_peak": max(abs_err)},
+        "stage_ms_per_step": per_step,
+        "roofline": {"bound": "fp32" if dom in ("eval_ms", "backward_ms") else "hbm", "kernel": dom[:-3],
+                     "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None,
+                     "note": "stage breakdown only; the per-kernel roofline is measured on the default workload"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "models/s", "h2d_bytes_per_step": int(h_par.numel() * 8),
+                "d2h_bytes_per_step": int(sum(h.numel() * h.element_size() for h in h_out))},
+        "gpu_launches": launches,
+        "graph": with_grad,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
 
 def main():
     args = parse()
     world, rank, local = dist_init(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload != "cfg4":
+        run_workload(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

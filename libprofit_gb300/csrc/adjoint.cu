@@ -119,20 +119,29 @@ __device__ __forceinline__ void warp_store_slots(const T *v, int lane, D *dst)
 
 // ------------------------------------------------------------ chi^2, g_out
 
+// Block (model, c) of gridDim.y = `parts` blocks per model takes the model's
+// output pixels [c * chunk, (c + 1) * chunk). With one block per model it
+// writes chi2[model] itself; with several, each writes its FP64 partial and
+// the last block of the model to finish (a per-model counter, reset by that
+// block) adds the partials in block order, so the result does not depend on
+// the blocks' timing.
 template <typename T>
 __global__ void chi2_kernel(const ModelDev *__restrict__ models, const T *__restrict__ img, const T *__restrict__ data,
                             const T *__restrict__ sigma, const T *__restrict__ cot, T *__restrict__ gout,
-                            double *__restrict__ chi2)
+                            double *__restrict__ chi2, double *__restrict__ partial, unsigned int *__restrict__ done)
 {
 	const ModelDev &m = models[blockIdx.x];
 	const long long n = (long long)m.out_w * m.out_h;
+	const int parts = gridDim.y;
+	const long long chunk = (n + parts - 1) / parts;
+	const long long i0 = (long long)blockIdx.y * chunk, i1 = min(n, i0 + chunk);
 	// per thread: a compensated (Kahan) sum in T, so that single precision
 	// costs no FP64 work per pixel; across threads: FP64
 	T s = 0, comp = 0;
-	for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+	for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
 		const long long g = m.out_off + i;
 		// output pixels the final masking zeroes do not depend on the parameters
-		const bool live = kept(m, (int)(i % m.out_w), (int)(i / m.out_w));
+		const bool live = !m.mask_final || kept(m, (int)(i % m.out_w), (int)(i / m.out_w));
 		if (cot) {
 			gout[g] = live ? cot[g] : (T)0;
 		}
@@ -154,7 +163,20 @@ __global__ void chi2_kernel(const ModelDev *__restrict__ models, const T *__rest
 		if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
 		__syncthreads();
 	}
-	if (threadIdx.x == 0 && chi2) chi2[blockIdx.x] = cot ? 0. : part[0];
+	if (threadIdx.x != 0 || !chi2) return;
+	if (parts == 1) {
+		chi2[blockIdx.x] = cot ? 0. : part[0];
+		return;
+	}
+	partial[(size_t)blockIdx.x * parts + blockIdx.y] = part[0];
+	__threadfence();
+	if (atomicAdd(&done[blockIdx.x], 1u) + 1 != (unsigned int)parts) return;
+	__threadfence();
+	double total = 0.;
+	const volatile double *pp = partial + (size_t)blockIdx.x * parts;
+	for (int c = 0; c < parts; c++) total += pp[c];
+	chi2[blockIdx.x] = cot ? 0. : total;
+	done[blockIdx.x] = 0;
 }
 
 // cotangent of drawing pixel (x, y): the output pixel it lands in after the
@@ -853,10 +875,12 @@ __global__ void grad_reduce_kernel(const ModelDev *__restrict__ models, const Pr
 
 template <typename T>
 void launch_chi2(const ModelDev *models, int n_models, const void *img, const void *data, const void *sigma,
-                 const void *cot, void *gout, double *chi2, cudaStream_t stream)
+                 const void *cot, void *gout, double *chi2, int parts, double *partial, unsigned int *done,
+                 cudaStream_t stream)
 {
-	chi2_kernel<T><<<n_models, 256, 0, stream>>>(models, (const T *)img, (const T *)data, (const T *)sigma,
-	                                             (const T *)cot, (T *)gout, chi2);
+	if (n_models <= 0) return;
+	chi2_kernel<T><<<dim3((unsigned int)n_models, (unsigned int)parts), 256, 0, stream>>>(
+	    models, (const T *)img, (const T *)data, (const T *)sigma, (const T *)cot, (T *)gout, chi2, partial, done);
 }
 
 
@@ -898,9 +922,9 @@ int backward_slots(bool sersic_only)
 long long backward_ring_slots(bool sersic_only) { return (long long)kRingRows * kRingCols * backward_slots(sersic_only); }
 
 template void launch_chi2<float>(const ModelDev *, int, const void *, const void *, const void *, const void *, void *,
-                                 double *, cudaStream_t);
+                                 double *, int, double *, unsigned int *, cudaStream_t);
 template void launch_chi2<double>(const ModelDev *, int, const void *, const void *, const void *, const void *,
-                                  void *, double *, cudaStream_t);
+                                  void *, double *, int, double *, unsigned int *, cudaStream_t);
 template void launch_backward<float>(const ModelDev *, const ProfileDev *, int, const void *, const void *,
                                      const long long *, unsigned int, unsigned int *, double *, double *, double *,
                                      bool, int, cudaStream_t);

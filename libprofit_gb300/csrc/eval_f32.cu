@@ -324,98 +324,103 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 	const float yl = fmaf(cy, m.fsy_hi, -yh) + cy * m.fsy_lo;
 	float acc_conv = 0.f, acc_direct = 0.f;
 
-	for (int q = 0; q < m.n_profiles; q++) {
-		const int pi = m.first_profile + q;
-		const ProfileDev &P = profs[pi];
-		float add = 0.f;
-		bool has = false;
-		if (P.kind == PF_SKY) {
-			add = P.fbg;
-			has = in_mask;
-		}
-		else if (P.kind == PF_PSF) {
-			if (active && psf) has = psf_value(P, m, psf, px, row, add);
-		}
-		else if (P.kind <= PF_BROKENEXP) {
-			if ((int)row < P.bby0 || (int)row > P.bby1 || col1 < P.bbx0 || col0 > P.bbx1) {
-				continue;
+	for (int q0 = 0; q0 < m.n_profiles; q0 += 32) {
+		// 32 profiles' culling boxes tested at once, one per lane; the ones
+		// that reach this tile drawn one by one, in profile order
+		const bool reaches = profile_reaches(profs, m, q0 + lane, (int)row, col0, col1);
+		unsigned int todo = __ballot_sync(0xffffffffu, reaches);
+		while (todo) {
+			const int q = q0 + __ffs(todo) - 1;
+			todo &= todo - 1;
+			const int pi = m.first_profile + q;
+			const ProfileDev &P = profs[pi];
+			float add = 0.f;
+			bool has = false;
+			if (P.kind == PF_SKY) {
+				add = P.fbg;
+				has = in_mask;
 			}
-			const f32::Shape sh = f32::load_shape(P);
-			const float dx = (xh - P.fxc_hi) + (xl - P.fxc_lo);
-			const float dy = (yh - P.fyc_hi) + (yl - P.fyc_lo);
-			const float xp = dx * sh.cs + dy * sh.sn;
-			const float yp = (dy * sh.cs - dx * sh.sn) * sh.iq;
-			const float rr = sqrtf(xp * xp + yp * yp) * P.finv_rscale;
-			bool beyond = P.frmax > 0.f && rr > P.frmax;
-			bool outside = rr > P.fswitch;
-			const bool amb = (P.frmax > 0.f && fabsf(rr - P.frmax) <= kGuardRadius * P.frmax) ||
-			                 fabsf(rr - P.fswitch) <= kGuardRadius * P.fswitch || !isfinite(rr);
-			if (amb && in_mask) {
-				const unsigned int d = radius_f64(P, m, px, row);
-				beyond = (d & 1u) != 0;
-				outside = (d & 2u) != 0;
+			else if (P.kind == PF_PSF) {
+				if (active && psf) has = psf_value(P, m, psf, px, row, add);
 			}
-			beyond |= !in_mask;  // masked pixels are not evaluated (src/radial.cpp:305-307)
-			float pixel_val = 0.f;
-			int depth = 0;
-			bool need_ss = false;
-			if (beyond) {
-				depth = -1;
-			}
-			else if (P.rough || outside) {
-				pixel_val = f32::value<KINDS>(sh, xp, yp);
-				if (!isfinite(pixel_val)) pixel_val = value_f64<KINDS>(P, dx, 0.f, 0.f, dy, 0.f, 0.f);
-			}
-			else {
-				need_ss = true;
-			}
-			unsigned int pending = __ballot_sync(0xffffffffu, need_ss && active);
-			unsigned long long *counts = dbg.counts ? dbg.counts + (size_t)pi * kLevelCounts : nullptr;
-			if (counts) {
-				const unsigned int nd = __popc(__ballot_sync(0xffffffffu, active && !beyond && !need_ss));
-				if (lane == 0 && nd) atomicAdd(&counts[kCountDirectEvals], (unsigned long long)nd);
-			}
-			while (pending) {
-				const int src = __ffs(pending) - 1;
-				pending &= pending - 1;
-				const unsigned int spx = (unsigned int)col0 + src;
-				const float sdx = __shfl_sync(0xffffffffu, dx, src);
-				const float sdy = __shfl_sync(0xffffffffu, dy, src);
-				unsigned int res = P.resolution, max_rec = P.max_recursions;
-				if (P.center_boost) {  // src/sersic.cpp:331-347
-					bool center = fabsf(sdx) < m.fscale_x && fabsf(sdy) < m.fscale_y;
-					if (fabsf(fabsf(sdx) - m.fscale_x) <= 1e-5f * m.fscale_x ||
-					    fabsf(fabsf(sdy) - m.fscale_y) <= 1e-5f * m.fscale_y) {
-						center = center_f64(P, m, spx, row);
+			else if (P.kind <= PF_BROKENEXP) {
+				const f32::Shape sh = f32::load_shape(P);
+				const float dx = (xh - P.fxc_hi) + (xl - P.fxc_lo);
+				const float dy = (yh - P.fyc_hi) + (yl - P.fyc_lo);
+				const float xp = dx * sh.cs + dy * sh.sn;
+				const float yp = (dy * sh.cs - dx * sh.sn) * sh.iq;
+				const float rr = sqrtf(xp * xp + yp * yp) * P.finv_rscale;
+				bool beyond = P.frmax > 0.f && rr > P.frmax;
+				bool outside = rr > P.fswitch;
+				const bool amb = (P.frmax > 0.f && fabsf(rr - P.frmax) <= kGuardRadius * P.frmax) ||
+				                 fabsf(rr - P.fswitch) <= kGuardRadius * P.fswitch || !isfinite(rr);
+				if (amb && in_mask) {
+					const unsigned int d = radius_f64(P, m, px, row);
+					beyond = (d & 1u) != 0;
+					outside = (d & 2u) != 0;
+				}
+				beyond |= !in_mask;  // masked pixels are not evaluated (src/radial.cpp:305-307)
+				float pixel_val = 0.f;
+				int depth = 0;
+				bool need_ss = false;
+				if (beyond) {
+					depth = -1;
+				}
+				else if (P.rough || outside) {
+					pixel_val = f32::value<KINDS>(sh, xp, yp);
+					if (!isfinite(pixel_val)) pixel_val = value_f64<KINDS>(P, dx, 0.f, 0.f, dy, 0.f, 0.f);
+				}
+				else {
+					need_ss = true;
+				}
+				unsigned int pending = __ballot_sync(0xffffffffu, need_ss && active);
+				unsigned long long *counts = dbg.counts ? dbg.counts + (size_t)pi * kLevelCounts : nullptr;
+				if (counts) {
+					const unsigned int nd = __popc(__ballot_sync(0xffffffffu, active && !beyond && !need_ss));
+					if (lane == 0 && nd) atomicAdd(&counts[kCountDirectEvals], (unsigned long long)nd);
+				}
+				while (pending) {
+					const int src = __ffs(pending) - 1;
+					pending &= pending - 1;
+					const unsigned int spx = (unsigned int)col0 + src;
+					const float sdx = __shfl_sync(0xffffffffu, dx, src);
+					const float sdy = __shfl_sync(0xffffffffu, dy, src);
+					unsigned int res = P.resolution, max_rec = P.max_recursions;
+					if (P.center_boost) {  // src/sersic.cpp:331-347
+						bool center = fabsf(sdx) < m.fscale_x && fabsf(sdy) < m.fscale_y;
+						if (fabsf(fabsf(sdx) - m.fscale_x) <= 1e-5f * m.fscale_x ||
+						    fabsf(fabsf(sdy) - m.fscale_y) <= 1e-5f * m.fscale_y) {
+							center = center_f64(P, m, spx, row);
+						}
+						if (center) {
+							res = 8;
+							max_rec = 10;
+						}
 					}
-					if (center) {
-						res = 8;
-						max_rec = 10;
+					if (res > (unsigned int)kMaxRes) res = kMaxRes;
+					if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
+					// pixel box corner (i * scale - centre) as an exact float pair
+					float bxh, bxl, byh, byl;
+					corner_pair(small_int_to_float(spx), m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
+					corner_pair(small_int_to_float(row), m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
+					int deepest = 0;
+					const float v = warp_subsample_m<KINDS>(P, sh, ws, bxh, bxl, byh, byl, m.fsx_hi, m.fsy_hi, res,
+					                                        max_rec, lane, counts, deepest);
+					if (lane == src) {
+						pixel_val = v;
+						depth = deepest;
 					}
 				}
-				if (res > (unsigned int)kMaxRes) res = kMaxRes;
-				if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
-				// pixel box corner (i * scale - centre) as an exact float pair
-				float bxh, bxl, byh, byl;
-				corner_pair(small_int_to_float(spx), m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
-				corner_pair(small_int_to_float(row), m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
-				int deepest = 0;
-				const float v = warp_subsample_m<KINDS>(P, sh, ws, bxh, bxl, byh, byl, m.fsx_hi, m.fsy_hi, res,
-				                                        max_rec, lane, counts, deepest);
-				if (lane == src) {
-					pixel_val = v;
-					depth = deepest;
+				if (dbg.depth && active) {
+					dbg.depth[P.depth_off + (size_t)row * m.draw_w + px] = (int8_t)depth;
 				}
+				add = P.fflux_scale * pixel_val;
+				has = active;
 			}
-			if (dbg.depth && active) {
-				dbg.depth[P.depth_off + (size_t)row * m.draw_w + px] = (int8_t)depth;
+			if (has) {
+				if (P.convolve) acc_conv += add;
+				else acc_direct += add;
 			}
-			add = P.fflux_scale * pixel_val;
-			has = active;
-		}
-		if (has) {
-			if (P.convolve) acc_conv += add;
-			else acc_direct += add;
 		}
 	}
 	if (active) {

@@ -203,81 +203,86 @@ eval_tiles64_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 		const double *psf = m.psf_off >= 0 ? psf_pool + m.psf_off : nullptr;
 		double acc_conv = 0, acc_direct = 0;
 
-		for (int q = 0; q < m.n_profiles; q++) {
-			const int pi = m.first_profile + q;
-			const ProfileDev &P = profs[pi];
-			double add = 0;
-			bool has = false;
-			if (P.kind == PF_SKY) {
-				add = P.bg;
-				has = in_mask;  // src/sky.cpp:42-45
-			}
-			else if (P.kind == PF_PSF) {
-				if (active && psf) {
-					has = psf_pixel64(P, m, psf, px, row, add);
+		for (int q0 = 0; q0 < m.n_profiles; q0 += 32) {
+			// 32 profiles' culling boxes tested at once, one per lane; the ones
+			// that reach this tile drawn one by one, in profile order
+			const bool reaches = profile_reaches(profs, m, q0 + lane, (int)row, col0, col1);
+			unsigned int todo = __ballot_sync(0xffffffffu, reaches);
+			while (todo) {
+				const int q = q0 + __ffs(todo) - 1;
+				todo &= todo - 1;
+				const int pi = m.first_profile + q;
+				const ProfileDev &P = profs[pi];
+				double add = 0;
+				bool has = false;
+				if (P.kind == PF_SKY) {
+					add = P.bg;
+					has = in_mask;  // src/sky.cpp:42-45
 				}
-			}
-			else if (P.kind <= PF_BROKENEXP) {
-				if ((int)row < P.bby0 || (int)row > P.bby1 || col1 < P.bbx0 || col0 > P.bbx1) {
-					continue;
+				else if (P.kind == PF_PSF) {
+					if (active && psf) {
+						has = psf_pixel64(P, m, psf, px, row, add);
+					}
 				}
-				const double y = half_ybin + row * sy;
-				const double x = half_xbin + px * sx;
-				double xp, yp;
-				f64::to_profile(P, x, y, xp, yp);
-				const double r_prof = sqrt(xp * xp + yp * yp);
-				double pixel_val = 0;
-				int depth = 0;
-				bool need_ss = false;
-				if (!in_mask || (P.rscale_max > 0 && r_prof / P.rscale > P.rscale_max)) {
-					// masked out (src/radial.cpp:305-307) or beyond rscale_max
-					pixel_val = 0.;
-					depth = -1;
-				}
-				else if (P.rough || r_prof / P.rscale > P.rscale_switch) {
-					pixel_val = f64::evaluate_at(P, xp, yp);
-				}
-				else {
-					need_ss = true;
-				}
-				unsigned int pending = __ballot_sync(0xffffffffu, need_ss && active);
-				unsigned long long *counts = dbg.counts ? dbg.counts + (size_t)pi * kLevelCounts : nullptr;
-				if (counts) {
-					const unsigned int nd = __popc(__ballot_sync(0xffffffffu, active && depth == 0 && !need_ss));
-					if (lane == 0 && nd) atomicAdd(&counts[kCountDirectEvals], (unsigned long long)nd);
-				}
-				while (pending) {
-					const int s = __ffs(pending) - 1;
-					pending &= pending - 1;
-					const double xs = __shfl_sync(0xffffffffu, x, s);
-					const double ys = __shfl_sync(0xffffffffu, y, s);
-					unsigned int res = P.resolution, max_rec = P.max_recursions;
-					if (P.kind == PF_SERSIC) {  // src/sersic.cpp:331-347
-						const bool center_pixel = fabs(xs - P.xc) < m.scale_x && fabs(ys - P.yc) < m.scale_y;
-						if (P.adjust && center_pixel && P.par[7] > 1) {
-							res = 8;
-							max_rec = 10;
+				else if (P.kind <= PF_BROKENEXP) {
+					const double y = half_ybin + row * sy;
+					const double x = half_xbin + px * sx;
+					double xp, yp;
+					f64::to_profile(P, x, y, xp, yp);
+					const double r_prof = sqrt(xp * xp + yp * yp);
+					double pixel_val = 0;
+					int depth = 0;
+					bool need_ss = false;
+					if (!in_mask || (P.rscale_max > 0 && r_prof / P.rscale > P.rscale_max)) {
+						// masked out (src/radial.cpp:305-307) or beyond rscale_max
+						pixel_val = 0.;
+						depth = -1;
+					}
+					else if (P.rough || r_prof / P.rscale > P.rscale_switch) {
+						pixel_val = f64::evaluate_at(P, xp, yp);
+					}
+					else {
+						need_ss = true;
+					}
+					unsigned int pending = __ballot_sync(0xffffffffu, need_ss && active);
+					unsigned long long *counts = dbg.counts ? dbg.counts + (size_t)pi * kLevelCounts : nullptr;
+					if (counts) {
+						const unsigned int nd = __popc(__ballot_sync(0xffffffffu, active && depth == 0 && !need_ss));
+						if (lane == 0 && nd) atomicAdd(&counts[kCountDirectEvals], (unsigned long long)nd);
+					}
+					while (pending) {
+						const int s = __ffs(pending) - 1;
+						pending &= pending - 1;
+						const double xs = __shfl_sync(0xffffffffu, x, s);
+						const double ys = __shfl_sync(0xffffffffu, y, s);
+						unsigned int res = P.resolution, max_rec = P.max_recursions;
+						if (P.kind == PF_SERSIC) {  // src/sersic.cpp:331-347
+							const bool center_pixel = fabs(xs - P.xc) < m.scale_x && fabs(ys - P.yc) < m.scale_y;
+							if (P.adjust && center_pixel && P.par[7] > 1) {
+								res = 8;
+								max_rec = 10;
+							}
+						}
+						if (res > (unsigned int)kMaxRes) res = kMaxRes;
+						if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
+						int deepest = 0;
+						const double v = warp_subsample64(P, ws, xs - half_xbin, xs + half_xbin, ys - half_ybin,
+						                                  ys + half_ybin, res, max_rec, lane, counts, deepest);
+						if (lane == s) {
+							pixel_val = v;
+							depth = deepest;
 						}
 					}
-					if (res > (unsigned int)kMaxRes) res = kMaxRes;
-					if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
-					int deepest = 0;
-					const double v = warp_subsample64(P, ws, xs - half_xbin, xs + half_xbin, ys - half_ybin,
-					                                  ys + half_ybin, res, max_rec, lane, counts, deepest);
-					if (lane == s) {
-						pixel_val = v;
-						depth = deepest;
+					if (dbg.depth && active) {
+						dbg.depth[P.depth_off + (size_t)row * m.draw_w + px] = (int8_t)depth;
 					}
+					add = P.flux_scale * pixel_val;
+					has = active;
 				}
-				if (dbg.depth && active) {
-					dbg.depth[P.depth_off + (size_t)row * m.draw_w + px] = (int8_t)depth;
+				if (has) {
+					if (P.convolve) acc_conv += add;
+					else acc_direct += add;
 				}
-				add = P.flux_scale * pixel_val;
-				has = active;
-			}
-			if (has) {
-				if (P.convolve) acc_conv += add;
-				else acc_direct += add;
 			}
 		}
 		if (active) {

@@ -74,7 +74,8 @@ void launch_fft_pass(int pass, const ModelDev *models, const void *jobs, int n_j
                      cudaStream_t stream);
 template <typename T>
 void launch_chi2(const ModelDev *models, int n_models, const void *img, const void *data, const void *sigma,
-                 const void *cot, void *gout, double *chi2, cudaStream_t stream);
+                 const void *cot, void *gout, double *chi2, int parts, double *partial, unsigned int *done,
+                 cudaStream_t stream);
 template <typename T>
 void launch_backward(const ModelDev *models, const ProfileDev *profs, int n_profiles, const void *gout,
                      const void *gsrc, const long long *prow_base, unsigned int n_ring, unsigned int *counter,
@@ -344,6 +345,9 @@ struct pf_batch {
 	bool adjoint = false;
 	void *d_gout = nullptr;
 	void *d_gsrc = nullptr;
+	int chi2_parts = 1;                 // chi^2 blocks per model (large models split, ~64 k pixels each)
+	double *d_chi2_partial = nullptr;   // chi2_parts FP64 per model
+	unsigned int *d_chi2_done = nullptr;// per model: chi^2 blocks finished (the last one sums, resets)
 	double *d_partial = nullptr;        // backward_slots() FP64 per (profile, drawing row)
 	double *d_ring_partial = nullptr;   // backward_slots() FP64 per (profile, ring tile)
 	long long *d_prow_base = nullptr;   // first partial row of each profile
@@ -501,6 +505,8 @@ void pf_batch_destroy(pf_batch *b)
 	cudaFree(b->d_gout);
 	cudaFree(b->d_gsrc);
 	cudaFree(b->d_partial);
+	cudaFree(b->d_chi2_partial);
+	cudaFree(b->d_chi2_done);
 	cudaFree(b->d_ring_partial);
 	cudaFree(b->d_prow_base);
 	cudaFree(b->d_bwd_counter);
@@ -1433,6 +1439,12 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	                     : pf::conv_smem<float>(max_kw, max_kh, b->adj_shape);
 	if (b->adj_smem > 227 * 1024) return fail(PF_ERR_UNSUPPORTED, "PSF too large for the adjoint convolution");
 	PF_CUDA_TRY(cudaMalloc(&b->d_gout, elem * std::max<uint64_t>(1, b->total_out)));
+	uint64_t max_out = 1;
+	for (const auto &m : b->mdev) max_out = std::max<uint64_t>(max_out, (uint64_t)m.out_w * m.out_h);
+	b->chi2_parts = (int)std::min<uint64_t>(128, (max_out + 65535) / 65536);
+	PF_CUDA_TRY(cudaMalloc(&b->d_chi2_partial, sizeof(double) * b->chi2_parts * std::max<size_t>(1, n_models)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_chi2_done, sizeof(unsigned int) * std::max<size_t>(1, n_models)));
+	PF_CUDA_TRY(cudaMemset(b->d_chi2_done, 0, sizeof(unsigned int) * std::max<size_t>(1, n_models)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_gsrc, elem * std::max<size_t>(1, b->draw_total)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_partial, sizeof(double) * pf::backward_slots(b->sersic_only) *
 	                                          std::max<long long>(1, rows)));
@@ -1494,9 +1506,10 @@ pf_status pf_backward(pf_batch *b, const void *images_dev, const void *data_dev,
 	for (const auto &m : b->mdev) any_conv |= m.conv_required != 0;
 	long t = stage_begin(b, ST_CHI2, stream);
 	if (b->dbl) pf::launch_chi2<double>(b->d_models, n_models, images_dev, data_dev, sigma_dev, cotangent_dev,
-	                                    b->d_gout, chi2_dev, stream);
+	                                    b->d_gout, chi2_dev, b->chi2_parts, b->d_chi2_partial, b->d_chi2_done,
+	                                    stream);
 	else pf::launch_chi2<float>(b->d_models, n_models, images_dev, data_dev, sigma_dev, cotangent_dev, b->d_gout,
-	                            chi2_dev, stream);
+	                            chi2_dev, b->chi2_parts, b->d_chi2_partial, b->d_chi2_done, stream);
 	stage_end(b, t, stream);
 	if (any_conv) {
 		t = stage_begin(b, ST_ADJCONV, stream);

@@ -151,6 +151,20 @@ __device__ __forceinline__ float small_int_to_float(unsigned int i)
 	return __int_as_float(0x4B000000 | (int)i) - 8388608.f;
 }
 
+// Whether profile q of model m contributes to the 32-pixel row tile
+// [col0, col1] of drawing row `row`: a radial profile only within its culling
+// box, the sky and psf profiles everywhere, null profiles nowhere. The eval
+// kernels test 32 profiles at once, one per lane, and draw the ones that
+// reach the tile in profile order.
+__device__ __forceinline__ bool profile_reaches(const ProfileDev *__restrict__ profs, const ModelDev &m, int q,
+                                                int row, int col0, int col1)
+{
+	if (q >= m.n_profiles) return false;
+	const ProfileDev &P = profs[m.first_profile + q];
+	if (P.kind > PF_BROKENEXP) return P.kind == PF_SKY || P.kind == PF_PSF;
+	return !(row < P.bby0 || row > P.bby1 || col1 < P.bbx0 || col0 > P.bbx1);
+}
+
 // Costly tiles first (FP32 eval and backward). A profile's ring tiles lie in
 // its subsampling box: rows by distance from the row of its centre (ring
 // index l = 0: that row, 1: the row above, 2: the row below, ...; l <

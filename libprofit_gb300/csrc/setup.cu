@@ -406,34 +406,42 @@ __device__ void radial_setup(ProfileDev &p, const ModelDev &m, double bn, const 
 	}
 	p.flux_scale = flux_scale;
 
-	// Culling box: r_prof >= the pixel centre's distance to (xc, yc) because
-	// axrat <= 1, so a pixel whose centre is farther than rscale_max * rscale
-	// is exactly 0 (src/radial.cpp:323-325). One pixel of margin.
+	// Culling box: a pixel whose centre has r_prof > rscale_max * rscale is
+	// exactly 0 (src/radial.cpp:323-325). r_prof^2 = xp^2 + yp^2 with (xp,
+	// yp * axrat) the centre offset rotated by the position angle, so the
+	// pixels kept lie in an ellipse of semi-axes R (along (cos, sin)) and
+	// R axrat, whose half-extents are R sqrt(cos^2 + axrat^2 sin^2) in x and
+	// R sqrt(sin^2 + axrat^2 cos^2) in y. One pixel of margin.
+	const double q2 = axrat * axrat;
+	const double ex = sqrt(p.cos_ang * p.cos_ang + q2 * p.sin_ang * p.sin_ang);
+	const double ey = sqrt(p.sin_ang * p.sin_ang + q2 * p.cos_ang * p.cos_ang);
 	p.bbx0 = 0;
 	p.bby0 = 0;
 	p.bbx1 = (int)m.draw_w - 1;
 	p.bby1 = (int)m.draw_h - 1;
 	if (p.rscale_max > 0) {
-		double R = p.rscale_max * p.rscale;
-		if (R == R && R < 1e12) {
-			p.bbx0 = clamp_index(floor((p.xc - R) / m.sx - 0.5) - 1, 0, (int)m.draw_w);
-			p.bbx1 = clamp_index(ceil((p.xc + R) / m.sx - 0.5) + 1, -1, (int)m.draw_w - 1);
-			p.bby0 = clamp_index(floor((p.yc - R) / m.sy - 0.5) - 1, 0, (int)m.draw_h);
-			p.bby1 = clamp_index(ceil((p.yc + R) / m.sy - 0.5) + 1, -1, (int)m.draw_h - 1);
+		const double R = p.rscale_max * p.rscale;
+		if (R == R && R < 1e12 && axrat > 0 && axrat <= 1) {
+			const double hx = R * ex, hy = R * ey;
+			p.bbx0 = clamp_index(floor((p.xc - hx) / m.sx - 0.5) - 1, 0, (int)m.draw_w);
+			p.bbx1 = clamp_index(ceil((p.xc + hx) / m.sx - 0.5) + 1, -1, (int)m.draw_w - 1);
+			p.bby0 = clamp_index(floor((p.yc - hy) / m.sy - 0.5) - 1, 0, (int)m.draw_h);
+			p.bby1 = clamp_index(ceil((p.yc + hy) / m.sy - 0.5) + 1, -1, (int)m.draw_h - 1);
 		}
 	}
 	// Subsampling box: a pixel is subsampled only if r_prof <= rscale_switch *
-	// rscale (src/radial.cpp:327-331), so, as above, only within that distance
-	// of the centre. Used to schedule the costly tiles first.
+	// rscale (src/radial.cpp:327-331), so, as above, only within that ellipse.
+	// Used to schedule the costly tiles first.
 	p.sbx0 = p.sby0 = 0;
 	p.sbx1 = p.sby1 = -1;
 	if (p.kind <= PF_BROKENEXP && !p.rough) {
-		double R = p.rscale_switch * p.rscale;
-		if (R == R && R < 1e12) {
-			p.sbx0 = clamp_index(floor((p.xc - R) / m.sx - 0.5) - 1, 0, (int)m.draw_w);
-			p.sbx1 = clamp_index(ceil((p.xc + R) / m.sx - 0.5) + 1, -1, (int)m.draw_w - 1);
-			p.sby0 = clamp_index(floor((p.yc - R) / m.sy - 0.5) - 1, 0, (int)m.draw_h);
-			p.sby1 = clamp_index(ceil((p.yc + R) / m.sy - 0.5) + 1, -1, (int)m.draw_h - 1);
+		const double R = p.rscale_switch * p.rscale;
+		if (R == R && R < 1e12 && axrat > 0 && axrat <= 1) {
+			const double hx = R * ex, hy = R * ey;
+			p.sbx0 = clamp_index(floor((p.xc - hx) / m.sx - 0.5) - 1, 0, (int)m.draw_w);
+			p.sbx1 = clamp_index(ceil((p.xc + hx) / m.sx - 0.5) + 1, -1, (int)m.draw_w - 1);
+			p.sby0 = clamp_index(floor((p.yc - hy) / m.sy - 0.5) - 1, 0, (int)m.draw_h);
+			p.sby1 = clamp_index(ceil((p.yc + hy) / m.sy - 0.5) + 1, -1, (int)m.draw_h - 1);
 		}
 		else {
 			p.sbx1 = (int)m.draw_w - 1;
