@@ -38,12 +38,14 @@ namespace pf {
 namespace {
 
 // Warps per block and blocks per SM of the backward pass's register budget
-// (4 and 3: up to 170 registers, 12 warps per SM).
+// (4 and 4: 128 registers, 16 warps per SM; the kernel is latency-bound:
+// 2.99 ms on the 1024-model step against 3.21 ms at 12 warps and 166
+// registers without spills).
 #ifndef PF_BACKWARD_WARPS
 #define PF_BACKWARD_WARPS 4
 #endif
 #ifndef PF_BACKWARD_MIN_BLOCKS
-#define PF_BACKWARD_MIN_BLOCKS 3
+#define PF_BACKWARD_MIN_BLOCKS 4
 #endif
 constexpr int kWarpsB = PF_BACKWARD_WARPS;
 // the forward pass's guard bands (eval_f32.cu), so that both take the same decisions

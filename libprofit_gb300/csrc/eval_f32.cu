@@ -31,13 +31,14 @@ namespace pf {
 namespace {
 
 // Warps per block and blocks per SM the register allocation is sized for: 4
-// and 4, 128 registers and 16 warps per SM (measured faster than 12 warps
-// with no spills at all).
+// and 5, 96 registers and 20 warps per SM (the kernel is latency-bound;
+// measured on the 1024-model step: 3.10 ms at 16 warps and 128 registers,
+// 2.95 ms at 20 warps with 148 bytes of spills on cold paths).
 #ifndef PF_EVAL32_WARPS
 #define PF_EVAL32_WARPS 4
 #endif
 #ifndef PF_EVAL32_MIN_BLOCKS
-#define PF_EVAL32_MIN_BLOCKS 4
+#define PF_EVAL32_MIN_BLOCKS 5
 #endif
 constexpr int kWarps32 = PF_EVAL32_WARPS;
 // Half-width of the band around a threshold inside which an FP32 comparison is

@@ -508,7 +508,7 @@ __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs,
 	const double nser = profs[t].par[7];
 	const double bn = solves[(size_t)t * 3 + 0];
 	SersicSolves sv{solves[(size_t)t * 3 + 1], solves[(size_t)t * 3 + 2], 0.};
-	if ((kind == PF_SERSIC && !profs[t].rescale_flux) || (kind == PF_CORESERSIC && want_grad)) {
+	if (((kind == PF_SERSIC && !profs[t].rescale_flux) || kind == PF_CORESERSIC) && want_grad) {
 		sv.dbn = dbn_dn(nser, bn);
 	}
 	ProfileDev p = profs[t];

@@ -140,34 +140,28 @@ __device__ inline double wilson_hilferty_guess(double p, double a)
 	return a * t * t * t;
 }
 
-// Inverse of P(a, .). With a usable starting point (guess > 0) the root is
-// bracketed around it by doubling steps instead of from [0, max(a, 1)].
+// Inverse of P(a, .) by safeguarded Halley iterations on f(x) = P(a, x) - p
+// (Q(a, x) - q for p > 1/2), one evaluation of f per iteration. With a usable
+// starting point (guess > 0) the iteration starts there, the bracket [lo, hi]
+// of the root growing from (0, +inf) as the signs of f are seen; without one,
+// the root is first bracketed by doubling from max(a, 1). A step that leaves
+// the bracket is replaced by bisection (or by doubling while hi is unknown).
+// The iteration stops when a Halley step moves x by less than 1e-7 relative
+// (cubic convergence: the next step would be below 1e-20) or by less than
+// 4 eps, or when f is exactly 0.
 __device__ inline double qgamma(double p, double a, double guess = -1.)
 {
 	if (!(p > 0.)) return 0.;
 	if (p >= 1.) return CUDART_INF;
 	const bool use_q = p > 0.5;
 	const double q = 1. - p;
-	double lo = 0., hi = a > 1. ? a : 1.;
+	double lo = 0., hi = CUDART_INF;
 	double x;
 	if (guess > 0.) {
-		// f(guess) decides which side of the root the guess lies on
-		const double f0 = use_q ? (q - qgamma_upper(guess, a)) : (pgamma(guess, a) - p);
-		if (f0 < 0.) {
-			lo = guess;
-			hi = guess * (1. + 1e-3);
-			while ((use_q ? (q - qgamma_upper(hi, a)) : (pgamma(hi, a) - p)) < 0.) {
-				lo = hi;
-				hi *= 2.;
-			}
-		}
-		else {
-			hi = guess;
-			lo = 0.;  // f(0) = -p < 0
-		}
 		x = guess;
 	}
 	else {
+		hi = a > 1. ? a : 1.;
 		for (int it = 0; it < 2000; it++) {
 			bool below = use_q ? (qgamma_upper(hi, a) > q) : (pgamma(hi, a) < p);
 			if (!below) break;
@@ -175,29 +169,25 @@ __device__ inline double qgamma(double p, double a, double guess = -1.)
 			hi *= 2.;
 		}
 		x = a;
+		if (!(x > lo && x < hi)) x = 0.5 * (lo + hi);
 	}
-	if (!(x > lo && x < hi)) {
-		x = 0.5 * (lo + hi);
-	}
+	const double lga = lgamma(a);
 	for (int it = 0; it < 200; it++) {
-		double f = use_q ? (q - qgamma_upper(x, a)) : (pgamma(x, a) - p);
+		const double f = use_q ? (q - qgamma_upper(x, a)) : (pgamma(x, a) - p);
 		if (f == 0.) break;
 		if (f < 0.) lo = x; else hi = x;
-		double pdf = exp((a - 1.) * log(x) - x - lgamma(a));
+		const double pdf = exp((a - 1.) * log(x) - x - lga);
 		double dx = f / pdf;
-		double t = 0.5 * dx * ((a - 1.) / x - 1.);
-		if (fabs(t) < 0.5) {
-			dx = dx / (1. - t);
-		}
+		const double t = 0.5 * dx * ((a - 1.) / x - 1.);
+		const bool halley = fabs(t) < 0.5;
+		if (halley) dx = dx / (1. - t);
 		double xn = x - dx;
 		if (!(xn > lo && xn < hi)) {
-			xn = 0.5 * (lo + hi);
+			xn = isinf(hi) ? 2. * x : 0.5 * (lo + hi);
 		}
-		if (fabs(xn - x) <= 4. * DBL_EPSILON * xn) {
-			x = xn;
-			break;
-		}
+		const double step = fabs(xn - x);
 		x = xn;
+		if (step <= 4. * DBL_EPSILON * xn || (halley && step <= 1e-7 * xn)) break;
 	}
 	return x;
 }
