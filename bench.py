@@ -485,6 +485,7 @@ def run_ours(args, world, rank, local):
         # evaluation, convolution (direct and / or FFT passes), chi2, adjoint convolution,
         # backward, gradient reduction
         "gpu_launches": launches,
+        "conv_plan": batch.conv_info(),
         "graph": not args.no_graph,
         "clocks": clk,
     }

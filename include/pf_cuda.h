@@ -130,12 +130,21 @@ typedef struct pf_model_desc {
 	 * width x height and is adjusted as Model::evaluate does (PSF padding only
 	 * when the mask's bounding box needs it, upsampled by the finesampling,
 	 * expanded by half the PSF; the output image masked by it at the end,
-	 * src/model.cpp:152-257); 0: the mask has the drawing dimensions
-	 * (width x height times the finesampling, plus half the PSF on each side
-	 * when a profile is convolved) and is used as given. */
+	 * src/model.cpp:152-257); 0: the mask is used as given and must have the
+	 * drawing dimensions: width x height times the finesampling, plus half the
+	 * PSF on each side if the mask is larger than that in both directions
+	 * (src/model.cpp:165-167, 277-283). mask_w x mask_h: the mask's
+	 * dimensions ("Mask dimensions != model dimensions" / "!= drawing
+	 * dimensions" otherwise). */
 	int64_t mask_offset;
 	int32_t adjust_mask;
-	int32_t reserved2;
+	/* Model::set_crop(false) (include/profit/model.h:206-214): 1 = keep the
+	 * padding the convolver adds (src/model.cpp:288-306). The direct
+	 * convolutions add none (Convolver::padding is empty, src/convolve.cpp:
+	 * 50-53), so their image is the cropped one, at offset (0, 0); with
+	 * PF_CONV_FFT it is refused (PF_ERR_UNSUPPORTED). 0 (the default): crop. */
+	int32_t no_crop;
+	uint32_t mask_w, mask_h;
 } pf_model_desc;
 
 typedef struct pf_env pf_env;
@@ -328,6 +337,13 @@ PF_API pf_status pf_batch_depth(pf_batch *batch, int8_t *depth, size_t depth_len
  * dimensions times the finesampling plus the PSF padding, which an adjustable
  * mask far enough from the edges leaves out. `dims` holds 2 * n_models. */
 PF_API pf_status pf_batch_drawing_dims(pf_batch *batch, uint32_t *dims);
+
+/* The convolution plan the batch runs: the direct convolution's block shape
+ * for the forward pass and for the adjoint (-1 before
+ * pf_batch_enable_adjoint), and how many models use the FFT (chosen per model
+ * by the autotuner, or requested). Any pointer may be NULL. */
+PF_API pf_status pf_batch_conv_info(const pf_batch *batch, int32_t *forward_shape, int32_t *adjoint_shape,
+                                    uint32_t *fft_models);
 
 #ifdef __cplusplus
 }

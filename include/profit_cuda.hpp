@@ -306,10 +306,28 @@ public:
 	void set_cuda_env(const CUDAEnvPtr &env) { m_env = env; }
 	CUDAEnvPtr get_cuda_env() const { return m_env; }
 	/* Model::set_mask / set_adjust_mask (include/profit/model.h:219-246): one
-	 * byte per pixel, non-zero = evaluate; model dimensions when adjusted
-	 * (the default), the drawing dimensions otherwise. Empty: no mask. */
-	void set_mask(const std::vector<uint8_t> &mask) { m_mask = mask; }
+	 * byte per pixel, non-zero = evaluate, row-major width x height; the
+	 * model's dimensions when adjusted (the default), the drawing dimensions
+	 * otherwise. Empty: no mask. */
+	void set_mask(const std::vector<uint8_t> &mask, unsigned int width, unsigned int height)
+	{
+		if (mask.size() != (size_t)width * height) throw invalid_parameter("mask size != width x height");
+		m_mask = mask;
+		m_mask_w = width;
+		m_mask_h = height;
+	}
 	void set_adjust_mask(bool adjust) { m_adjust_mask = adjust; }
+	/* Model::set_crop: the direct convolutions add no padding, so the image
+	 * is the cropped one at offset (0, 0); FFT with crop false is refused. */
+	void set_crop(bool crop) { m_crop = crop; }
+
+	/* Model::evaluate(Point &offset_out) */
+	Image evaluate(std::pair<unsigned int, unsigned int> &offset_out)
+	{
+		Image img = evaluate();
+		offset_out = {0u, 0u};
+		return img;
+	}
 
 	Image evaluate()
 	{
@@ -345,6 +363,9 @@ public:
 		m.convolver = PF_CONV_AUTO;
 		m.mask_offset = m_mask.empty() ? -1 : 0;
 		m.adjust_mask = m_adjust_mask ? 1 : 0;
+		m.mask_w = m_mask_w;
+		m.mask_h = m_mask_h;
+		m.no_crop = m_crop ? 0 : 1;
 		return m;
 	}
 
@@ -355,7 +376,9 @@ private:
 	unsigned int m_finesampling = 1;
 	bool m_return_finesampled = true;
 	bool m_adjust_mask = true;
+	bool m_crop = true;
 	std::vector<uint8_t> m_mask;
+	unsigned int m_mask_w = 0, m_mask_h = 0;
 	Image m_psf;
 	CUDAEnvPtr m_env;
 	std::vector<ProfilePtr> m_profiles;

@@ -273,6 +273,7 @@ class Model:
         self.convolver = _ffi.PF_CONV_AUTO
         self.mask = None
         self.adjust_mask = True
+        self.crop = True
 
     def add_profile(self, name):
         p = Profile(name)
@@ -315,6 +316,12 @@ class Model:
         """Model::set_adjust_mask (default True)."""
         self.adjust_mask = bool(adjust)
 
+    def set_crop(self, crop):
+        """Model::set_crop (default True). The direct convolutions add no
+        padding, so their uncropped image is the cropped one at offset (0, 0);
+        the FFT convolution with crop False is refused (Unsupported)."""
+        self.crop = bool(crop)
+
     def set_convolver(self, convolver):
         """A Convolver from create_convolver, or "auto", "brute" or "fft"."""
         names = {"auto": _ffi.PF_CONV_AUTO, "brute": _ffi.PF_CONV_BRUTE, "cuda": _ffi.PF_CONV_BRUTE,
@@ -346,6 +353,9 @@ class Model:
         m.convolver = self.convolver
         m.mask_offset = -1 if self.mask is None else (0 if mask_offset is None else mask_offset)
         m.adjust_mask = int(self.adjust_mask)
+        if self.mask is not None:
+            m.mask_h, m.mask_w = self.mask.shape
+        m.no_crop = int(not self.crop)
         profs = (_ffi.ProfileDesc * max(1, len(self.profiles)))()
         for i, p in enumerate(self.profiles):
             profs[i] = p.desc
@@ -356,6 +366,12 @@ class Model:
         w, h = ctypes.c_uint32(), ctypes.c_uint32()
         _check(_ffi.load().pf_model_output_dims(ctypes.byref(m), profs, ctypes.byref(w), ctypes.byref(h)))
         return w.value, h.value
+
+    def evaluate_with_offset(self):
+        """Model::evaluate(Point &offset): (image, (x, y)) with the offset of
+        the requested area in an uncropped image, (0, 0) with this backend's
+        convolutions (see set_crop)."""
+        return self.evaluate(), (0, 0)
 
     def evaluate(self):
         """Model::evaluate: returns the image as a (height, width) float64 array."""
@@ -474,6 +490,13 @@ class Batch:
         t = _ffi.StageTimes()
         _check(_ffi.load().pf_batch_stats(self._h, ctypes.byref(t), int(bool(reset))))
         return {name: getattr(t, name) for name, _ in _ffi.StageTimes._fields_}
+
+    def conv_info(self):
+        """The convolution plan: {"forward_shape", "adjoint_shape" (-1 before
+        enable_adjoint), "fft_models"} (pf_batch_conv_info)."""
+        f, a, n = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_uint32()
+        _check(_ffi.load().pf_batch_conv_info(self._h, ctypes.byref(f), ctypes.byref(a), ctypes.byref(n)))
+        return {"forward_shape": f.value, "adjoint_shape": a.value, "fft_models": n.value}
 
     def enable_adjoint(self):
         """Sizes the adjoint's device buffers (pf_batch_enable_adjoint)."""

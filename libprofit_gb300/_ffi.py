@@ -48,7 +48,8 @@ class ModelDesc(ctypes.Structure):
                 ("psf_w", ctypes.c_uint32), ("psf_h", ctypes.c_uint32),
                 ("psf_scale_x", ctypes.c_double), ("psf_scale_y", ctypes.c_double),
                 ("convolver", ctypes.c_int32), ("reserved", ctypes.c_int32),
-                ("mask_offset", ctypes.c_int64), ("adjust_mask", ctypes.c_int32), ("reserved2", ctypes.c_int32)]
+                ("mask_offset", ctypes.c_int64), ("adjust_mask", ctypes.c_int32), ("no_crop", ctypes.c_int32),
+                ("mask_w", ctypes.c_uint32), ("mask_h", ctypes.c_uint32)]
 
 
 class StageTimes(ctypes.Structure):
@@ -98,6 +99,7 @@ _SIGNATURES = {
     "pf_batch_record_depth": (ctypes.c_int, [_P, ctypes.c_int]),
     "pf_batch_depth": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "pf_batch_drawing_dims": (ctypes.c_int, [_P, _P]),
+    "pf_batch_conv_info": (ctypes.c_int, [_P, _P, _P, _P]),
 }
 
 _lib = None

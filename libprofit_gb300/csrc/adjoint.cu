@@ -735,10 +735,10 @@ __device__ void backward_row(const ModelDev &m, const ProfileDev &P, int row, in
 			}
 		}
 	}
-	double acc64[NS];
-#pragma unroll
-	for (int k = 0; k < NS; k++) acc64[k] = (double)acc[k];
-	warp_store_slots<NS>(acc64, lane, dst);
+	// the lanes' sums added across the warp in T (single precision: 32 terms,
+	// a few ulp), each total stored as this item's FP64 partial; the partials
+	// are reduced in FP64 (grad_reduce_kernel)
+	warp_store_slots<NS>(acc, lane, dst);
 }
 
 // Work items, taken by warps 32 at a time from a global counter (items with

@@ -107,8 +107,23 @@ __device__ __forceinline__ void conv_rows(const T *srow, const T *s_k, int s, in
 	}
 }
 
+// Register cap per thread of the convolution kernels (0: the compiler's
+// choice), as a minimum of resident blocks per SM.
+#ifndef PF_CONV_REGS
+#define PF_CONV_REGS 0
+#endif
+__host__ __device__ constexpr int conv_min_blocks(int threads)
+{
+	return PF_CONV_REGS > 0 ? 65536 / (threads * PF_CONV_REGS) : 1;
+}
+
+#if PF_CONV_REGS > 0
+#define PF_CONV_BOUNDS(threads) __launch_bounds__(threads, conv_min_blocks(threads))
+#else
+#define PF_CONV_BOUNDS(threads) __launch_bounds__(threads)
+#endif
 template <typename T, int MODE, int TX, int TY, int R>
-__global__ void __launch_bounds__(TX * TY)
+__global__ void PF_CONV_BOUNDS(TX * TY)
 conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restrict__ psf, const T *__restrict__ in,
             const T *__restrict__ direct, T *__restrict__ out, const long long *__restrict__ tile_base,
             long long n_tiles)
@@ -149,17 +164,31 @@ conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restri
 				sy0 = y0 - (kh - 1 - kh / 2);
 			}
 			const T *src = in + (MODE == CONV_FORWARD ? m.draw_off : 0);
-			for (int i = threadIdx.x; i < pw * ph; i += blockDim.x) {
-				const int xx = sx0 + i % pw, yy = sy0 + i / pw;
-				T v = 0;
-				if (MODE == CONV_FORWARD) {
-					if (xx >= 0 && xx < (int)m.draw_w && yy >= 0 && yy < (int)m.draw_h && i % pw < BW + kw - 1)
-						v = src[(size_t)yy * m.draw_w + xx];
+			if (MODE == CONV_FORWARD) {
+				// one full warp per patch row, lanes along it (coalesced, no index
+				// division); the threads of a partial last warp take no part
+				const int lane = threadIdx.x & 31, nwarp = (TX * TY) >> 5;
+				for (int py = (int)threadIdx.x >> 5; py < ph && ((int)threadIdx.x >> 5) < nwarp; py += nwarp) {
+					const int yy = sy0 + py;
+					const bool row_in = yy >= 0 && yy < (int)m.draw_h;
+					T *dst = s_src + py * pw;
+					for (int px = lane; px < pw; px += 32) {
+						const int xx = sx0 + px;
+						T v = 0;
+						if (px < BW + kw - 1 && row_in && xx >= 0 && xx < (int)m.draw_w) {
+							v = src[(size_t)yy * m.draw_w + xx];
+						}
+						dst[px] = v;
+					}
 				}
-				else {
-					if (i % pw < BW + kw - 1) v = cot_at(m, in, xx, yy);
+			}
+			else {
+				// the cotangent placed at the crop (measured faster flattened over
+				// every thread of the block than row by row)
+				for (int i = threadIdx.x; i < pw * ph; i += blockDim.x) {
+					const int px = i % pw;
+					s_src[i] = px < BW + kw - 1 ? cot_at(m, in, sx0 + px, sy0 + i / pw) : (T)0;
 				}
-				s_src[i] = v;
 			}
 			const T *k = psf + m.psf_off;
 			const int kn = kw * kh;

@@ -193,7 +193,7 @@ __device__ void eval_frame_m(const ProfileDev &P, const f32::Shape &sh, WarpScra
 			const float sub = f32::value<KINDS>(sh, xp, yp);
 			if (recurse) {
 				const float t = f32::value<KINDS>(sh, fabsf(xp), fabsf(yp) + fdyp);
-				const float d = fabsf(t / sub - 1.f);
+				const float d = fabsf(__fdividef(t, sub) - 1.f);
 				amb = !(isfinite(d) && isfinite(sub)) || fabsf(d - facc) <= kGuardAcc * (facc + 1.f);
 				fail = !amb && d > facc;
 			}

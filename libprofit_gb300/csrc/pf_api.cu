@@ -198,14 +198,28 @@ pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles
 	if (g.conv && !has_psf) {
 		return fail(PF_ERR_INVALID_PARAMETER, "No psf provided but profile(s) requested convolution");
 	}
+	if (m.no_crop && g.conv && m.convolver == PF_CONV_FFT) {
+		// the FFT convolver's uncropped frame (FFTConvolver::padding,
+		// src/convolve.cpp:263-268) is not produced by this backend
+		return fail(PF_ERR_UNSUPPORTED, "crop = false with the FFT convolver is not supported by the CUDA backend");
+	}
 	for (uint32_t i = 0; i < m.n_profiles; i++) {
 		pf_status s = validate_profile(profiles[m.first_profile + i], has_psf);
 		if (s != PF_OK) return s;
 	}
-	// the PSF padding: with an adjustable mask, only when the mask's bounding
-	// box (times the finesampling) comes closer than half the PSF to an edge
+	// src/model.cpp:198-201
+	if (mask && m.adjust_mask && (m.mask_w != m.width || m.mask_h != m.height)) {
+		return fail(PF_ERR_INVALID_PARAMETER, "Mask dimensions != model dimensions");
+	}
+	// the PSF padding: with a mask used as given, when the mask is larger than
+	// the model (times the finesampling) in both directions; with an
+	// adjustable one, only when its bounding box (times the finesampling)
+	// comes closer than half the PSF to an edge (src/model.cpp:152-184)
 	bool padding = g.conv;
-	if (mask && m.adjust_mask && g.conv) {
+	if (mask && !m.adjust_mask) {
+		padding = m.mask_w > m.width * m.finesampling && m.mask_h > m.height * m.finesampling;
+	}
+	else if (mask && g.conv) {
 		uint32_t lbx = m.width, lby = m.height, ubx = 0, uby = 0;
 		bool any = false;
 		for (uint32_t j = 0; j < m.height; j++) {
@@ -227,8 +241,8 @@ pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles
 	}
 	g.mask_needs_adjustment = mask && m.adjust_mask &&
 	                          (g.mask_needs_convolution || g.mask_needs_psf_padding || m.finesampling > 1);
-	g.pad_x = padding ? m.psf_w / 2 : 0;
-	g.pad_y = padding ? m.psf_h / 2 : 0;
+	g.pad_x = padding && has_psf ? m.psf_w / 2 : 0;
+	g.pad_y = padding && has_psf ? m.psf_h / 2 : 0;
 	g.crop_w = m.width * m.finesampling;
 	g.crop_h = m.height * m.finesampling;
 	g.draw_w = g.crop_w + 2 * g.pad_x;
@@ -238,6 +252,12 @@ pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles
 	if (m.finesampling > 1 && !m.return_finesampled) {
 		g.out_w = (g.crop_w + m.finesampling - 1) / m.finesampling;
 		g.out_h = (g.crop_h + m.finesampling - 1) / m.finesampling;
+	}
+	// src/model.cpp:277-283
+	if (mask && !m.adjust_mask && (m.mask_w != g.draw_w || m.mask_h != g.draw_h)) {
+		return fail(PF_ERR_INVALID_PARAMETER, "Mask dimensions != drawing dimensions: [" + std::to_string(m.mask_w) +
+		                                          ", " + std::to_string(m.mask_h) + "] != [" +
+		                                          std::to_string(g.draw_w) + ", " + std::to_string(g.draw_h) + "]");
 	}
 	return PF_OK;
 }
@@ -709,7 +729,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		const uint8_t *mask = nullptr;
 		if (mask_pool && m.mask_offset >= 0) {
 			mask = mask_pool + m.mask_offset;
-			if ((uint64_t)m.mask_offset + (uint64_t)m.width * m.height > mask_pool_len) {
+			if ((uint64_t)m.mask_offset + (uint64_t)m.mask_w * m.mask_h > mask_pool_len) {
 				return fail(PF_ERR_INVALID_PARAMETER, "model " + std::to_string(i) + ": mask outside the mask pool");
 			}
 		}
@@ -1148,12 +1168,20 @@ pf_status pf_batch_create_masked(pf_env *env, const pf_model_desc *models, size_
 	}
 	cudaMemsetAsync(bd->d_conv, 0, sizeof(float) * std::max<size_t>(1, bd->draw_total), env->stream);
 	cudaMemsetAsync(bd->d_direct, 0, sizeof(float) * std::max<size_t>(1, bd->draw_total), env->stream);
+	// every shape timed in each of two rounds, the best time of each kept:
+	// a clock ramp or a slow launch early on does not decide the choice
 	double t_direct = -1;
 	int best_shape = bd->fwd_shape;
+	std::vector<double> t_shape(pf::conv_num_shapes<float>(), -1.);
+	for (int round = 0; round < 2; round++) {
+		for (int sh = 0; sh < pf::conv_num_shapes<float>(); sh++) {
+			const double ms = time_forward_conv(bd, sh, false, out);
+			if (ms >= 0 && (t_shape[sh] < 0 || ms < t_shape[sh])) t_shape[sh] = ms;
+		}
+	}
 	for (int sh = 0; sh < pf::conv_num_shapes<float>(); sh++) {
-		const double ms = time_forward_conv(bd, sh, false, out);
-		if (ms >= 0 && (t_direct < 0 || ms < t_direct)) {
-			t_direct = ms;
+		if (t_shape[sh] >= 0 && (t_direct < 0 || t_shape[sh] < t_direct)) {
+			t_direct = t_shape[sh];
 			best_shape = sh;
 		}
 	}
@@ -1388,6 +1416,20 @@ pf_status pf_batch_drawing_dims(pf_batch *b, uint32_t *dims)
 	return PF_OK;
 }
 
+pf_status pf_batch_conv_info(const pf_batch *b, int32_t *forward_shape, int32_t *adjoint_shape,
+                             uint32_t *fft_models)
+{
+	if (!b) return fail(PF_ERR_INVALID_PARAMETER, "batch is NULL");
+	if (forward_shape) *forward_shape = b->fwd_shape;
+	if (adjoint_shape) *adjoint_shape = b->adjoint ? b->adj_shape : -1;
+	if (fft_models) {
+		uint32_t n = 0;
+		for (const auto &m : b->mdev) n += m.use_fft ? 1u : 0u;
+		*fft_models = n;
+	}
+	return PF_OK;
+}
+
 pf_status pf_batch_enable_adjoint(pf_batch *b)
 {
 	if (!b) return fail(PF_ERR_INVALID_PARAMETER, "batch is NULL");
@@ -1464,10 +1506,16 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 		PF_CUDA_TRY(cudaMemsetAsync(b->d_gout, 0, sizeof(float) * std::max<uint64_t>(1, b->total_out), b->env->stream));
 		double best = -1;
 		int best_shape = b->adj_shape;
+		std::vector<double> t_shape(pf::conv_num_shapes<float>(), -1.);
+		for (int round = 0; round < 2; round++) {  // as for the forward shapes
+			for (int sh = 0; sh < pf::conv_num_shapes<float>(); sh++) {
+				const double ms = time_adjoint_conv(b, sh);
+				if (ms >= 0 && (t_shape[sh] < 0 || ms < t_shape[sh])) t_shape[sh] = ms;
+			}
+		}
 		for (int sh = 0; sh < pf::conv_num_shapes<float>(); sh++) {
-			const double ms = time_adjoint_conv(b, sh);
-			if (ms >= 0 && (best < 0 || ms < best)) {
-				best = ms;
+			if (t_shape[sh] >= 0 && (best < 0 || t_shape[sh] < best)) {
+				best = t_shape[sh];
 				best_shape = sh;
 			}
 		}
@@ -1672,13 +1720,7 @@ pf_status pf_model_evaluate_masked(pf_env *env, const pf_model_desc *model, cons
 	m.psf_offset = has_psf ? 0 : -1;
 	m.mask_offset = mask ? 0 : -1;
 	size_t mask_len = 0;
-	if (mask) {
-		// the adjustable mask has the model's dimensions; one used as given, the drawing dimensions
-		Geometry g;
-		pf_status gs = model_geometry(m, profiles, g);
-		if (gs != PF_OK) return gs;
-		mask_len = m.adjust_mask ? (size_t)m.width * m.height : (size_t)g.draw_w * g.draw_h;
-	}
+	if (mask) mask_len = (size_t)m.mask_w * m.mask_h;
 	pf_batch *b = nullptr;
 	pf_status s = pf_batch_create_masked(env, &m, 1, profiles, m.n_profiles, has_psf ? psf : nullptr,
 	                                     has_psf ? (size_t)m.psf_w * m.psf_h : 0, mask, mask_len, &b);

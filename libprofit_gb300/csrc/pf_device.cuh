@@ -103,8 +103,10 @@ struct ProfileDev {
 	int32_t bbx0, bbx1, bby0, bby1;   // drawing pixels outside are exactly zero
 	int32_t sbx0, sbx1, sby0, sby1;   // drawing pixels outside are never subsampled (empty: x1 < x0)
 	int64_t depth_off;         // offset of this profile's depth map (debug recording)
-	// single-precision copies for the FP32 path (setup kernel)
-	float fxc_hi, fxc_lo, fyc_hi, fyc_lo;  // centre as an unevaluated float sum
+	// single-precision copies for the FP32 path (setup kernel); 16-byte
+	// aligned and contiguous up to fpar[11], read as float4 vectors
+	alignas(16) float fxc_hi;
+	float fxc_lo, fyc_hi, fyc_lo;          // centre as an unevaluated float sum
 	float fcos, fsin, finv_axrat, finv_rscale;
 	float fswitch, frmax, facc, fflux_scale;
 	float fbg;

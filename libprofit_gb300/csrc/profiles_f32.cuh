@@ -17,6 +17,7 @@
 #pragma once
 
 #include <cmath>
+#include <cstddef>
 
 #include "pf_device.cuh"
 
@@ -42,17 +43,34 @@ struct Shape {
 	float bn, dbn;         // sersic bn and d bn / d nser (adjoint)
 };
 
+// The FP32 block of ProfileDev (fxc_hi .. fpar[11], 26 words from a 16-byte
+// boundary) as seven float4 loads instead of word by word.
+static_assert(offsetof(ProfileDev, fxc_hi) % 16 == 0 && sizeof(ProfileDev) % 16 == 0, "float4 block");
+static_assert(offsetof(ProfileDev, fpar) == offsetof(ProfileDev, fxc_hi) + 14 * sizeof(float), "FP32 block layout");
+
 __device__ __forceinline__ Shape load_shape(const ProfileDev &p)
 {
+	const float4 *v = reinterpret_cast<const float4 *>(&p.fxc_hi);
+	const float4 a = v[1], b = v[2], c = v[3], d = v[4], e = v[5], f = v[6];
 	Shape s;
 	s.kind = p.kind;
-	s.boxy = p.fboxy;
-#pragma unroll
-	for (int i = 0; i < 12; i++) s.c[i] = p.fpar[i];
-	s.cs = p.fcos;
-	s.sn = p.fsin;
-	s.iq = p.finv_axrat;
-	s.acc = p.facc;
+	s.cs = a.x;
+	s.sn = a.y;
+	s.iq = a.z;
+	s.acc = b.z;
+	s.boxy = __float_as_int(c.y);
+	s.c[0] = c.z;
+	s.c[1] = c.w;
+	s.c[2] = d.x;
+	s.c[3] = d.y;
+	s.c[4] = d.z;
+	s.c[5] = d.w;
+	s.c[6] = e.x;
+	s.c[7] = e.y;
+	s.c[8] = e.z;
+	s.c[9] = e.w;
+	s.c[10] = f.x;
+	s.c[11] = f.y;
 	s.bn = p.fbn;
 	s.dbn = p.fdbn;
 	return s;

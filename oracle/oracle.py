@@ -66,7 +66,8 @@ class OrcModel(ctypes.Structure):
                 ("psf", ctypes.POINTER(ctypes.c_double)), ("psf_w", ctypes.c_uint),
                 ("psf_h", ctypes.c_uint), ("psf_scale_x", ctypes.c_double),
                 ("psf_scale_y", ctypes.c_double), ("mask", ctypes.POINTER(ctypes.c_ubyte)),
-                ("adjust_mask", ctypes.c_int), ("convolver", ctypes.c_int), ("omp_threads", ctypes.c_int)]
+                ("adjust_mask", ctypes.c_int), ("mask_w", ctypes.c_uint), ("mask_h", ctypes.c_uint),
+                ("convolver", ctypes.c_int), ("omp_threads", ctypes.c_int)]
 
 
 class OrcConstants(ctypes.Structure):
@@ -164,7 +165,8 @@ class Case:
         self.convolver = convolver
         self.psf_scale = psf_scale
         # adjust_mask (the reference's default): mask of the model's dimensions,
-        # adjusted as Model::evaluate does; otherwise of the drawing dimensions
+        # adjusted as Model::evaluate does; otherwise used as given (drawing
+        # dimensions, padded only if the mask is larger than the model)
         self.mask = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
         self.adjust_mask = adjust_mask
 
@@ -181,6 +183,7 @@ class Case:
         m.psf_scale_x, m.psf_scale_y = self.psf_scale
         if self.mask is not None:
             m.mask = self.mask.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte))
+            m.mask_h, m.mask_w = self.mask.shape
         m.adjust_mask = int(bool(self.adjust_mask))
         m.convolver = 1 if self.convolver == "brute_old" else 0
         m.omp_threads = threads

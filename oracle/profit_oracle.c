@@ -718,7 +718,13 @@ static expansion_t analyze_expansion(const orc_model *m, int conv, unsigned int 
 {
 	expansion_t e = {0, 0, 0, 0, 0};
 	int needs_padding = conv;
-	if (m->mask && m->adjust_mask && conv) {
+	if (m->mask && !m->adjust_mask) {
+		/* a mask used as given: padding if it is larger than the model (times
+		 * the finesampling) in both directions, whether or not anything is
+		 * convolved (src/model.cpp:165-167) */
+		needs_padding = m->mask_w > m->width * fs && m->mask_h > m->height * fs;
+	}
+	else if (m->mask && conv) {
 		/* Surface::bounding_box (include/profit/image.h:472-501): [lb, ub) of
 		 * the non-zero pixels, empty (all zero) for an all-zero mask */
 		unsigned int lbx = m->width, lby = m->height, ubx = 0, uby = 0, i, j;
@@ -808,6 +814,10 @@ int orc_output_dims(const orc_model *m, const orc_profile *profiles, int n_profi
 	for (i = 0; i < n_profiles; i++) {
 		conv |= profiles[i].convolve != 0;
 	}
+	/* src/model.cpp:198-201 */
+	if (m->mask && m->adjust_mask && (m->mask_w != m->width || m->mask_h != m->height)) {
+		return fail("Mask dimensions != model dimensions");
+	}
 	if (conv && (!m->psf || m->psf_w == 0 || m->psf_h == 0)) {
 		return fail("No psf provided but profile(s) requested convolution");
 	}
@@ -821,6 +831,12 @@ int orc_output_dims(const orc_model *m, const orc_profile *profiles, int n_profi
 	}
 	*draw_w = m->width * fs + 2 * pad_x;
 	*draw_h = m->height * fs + 2 * pad_y;
+	/* src/model.cpp:277-283 */
+	if (m->mask && !m->adjust_mask && (m->mask_w != *draw_w || m->mask_h != *draw_h)) {
+		snprintf(g_err, sizeof g_err, "Mask dimensions != drawing dimensions: [%u, %u] != [%u, %u]", m->mask_w,
+		         m->mask_h, *draw_w, *draw_h);
+		return -1;
+	}
 	*out_w = m->width * fs;
 	*out_h = m->height * fs;
 	if (fs > 1 && !m->return_finesampled) {

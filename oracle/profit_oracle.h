@@ -86,9 +86,13 @@ typedef struct {
 	 * model's dimensions and is adjusted as Model::evaluate does
 	 * (src/model.cpp:152-257: padding decided by its bounding box, upsampled,
 	 * extended, expanded by half the PSF) and the final image is masked by it;
-	 * without, it has the drawing dimensions and is used as given. */
+	 * without, it is used as given and must have the drawing dimensions, which
+	 * include the PSF padding only if the mask is larger than the model's
+	 * dimensions times the finesampling in both directions
+	 * (src/model.cpp:165-167, 277-283). mask_w x mask_h: its dimensions. */
 	const unsigned char *mask;
 	int adjust_mask;
+	unsigned int mask_w, mask_h;
 	/* 0: BRUTE (associative row dot products), 1: BRUTE_OLD */
 	int convolver;
 	int omp_threads;

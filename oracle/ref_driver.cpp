@@ -123,16 +123,12 @@ extern "C" int ref_evaluate(const orc_model *m, const orc_profile *profiles, int
 			set_params(p, profiles[i]);
 		}
 		if (m->mask) {
-			// Model::set_mask with the model's dimensions (the reference's
-			// adjustable mask); a mask of drawing dimensions is not driven here
-			if (!m->adjust_mask) {
-				std::strncpy(err, "the driver takes adjustable masks only", err_len);
-				return -3;
-			}
-			std::vector<bool> mk((size_t)m->width * m->height);
+			// Model::set_mask with the mask's own dimensions, adjusted or used
+			// as given (Model::set_adjust_mask)
+			std::vector<bool> mk((size_t)m->mask_w * m->mask_h);
 			for (size_t q = 0; q < mk.size(); q++) mk[q] = m->mask[q] != 0;
-			model.set_mask(profit::Mask(mk, m->width, m->height));
-			model.set_adjust_mask(true);
+			model.set_mask(profit::Mask(mk, m->mask_w, m->mask_h));
+			model.set_adjust_mask(m->adjust_mask != 0);
 		}
 		profit::Image image = model.evaluate();
 		auto dims = image.getDimensions();

@@ -118,6 +118,23 @@ def golden_cases():
         ("sersic", dict(xcen=36.4, ycen=30.2, mag=15.5, re=14, nser=1, ang=110, axrat=0.4, box=0.1,
                         convolve=True)),
         ("sky", dict(bg=1e-3))])
+    # masks used as given (Model::set_adjust_mask(false)): drawing dimensions,
+    # with the PSF padding when the mask is larger than the model
+    # (src/model.cpp:165-167, 277-283), without it otherwise
+    padded = (rng.random((64, 74)) < 0.8).astype(np.uint8)
+    padded[:, :6] = 0
+    c["mask_given_padded"] = dict(width=60, height=50, psf="psf15_moffat", mask=padded.tolist(), adjust_mask=False,
+                                  profiles=[
+        ("sersic", dict(xcen=31.2, ycen=24.6, mag=15, re=6, nser=2.5, ang=40, axrat=0.6, box=0.1, convolve=True)),
+        ("sky", dict(bg=0.01))])
+    unpadded = np.ones((40, 50), np.uint8)
+    unpadded[10:20, 5:45] = 0
+    c["mask_given_unpadded"] = dict(width=50, height=40, psf="psf15_moffat", mask=unpadded.tolist(),
+                                    adjust_mask=False, profiles=[
+        ("sersic", dict(xcen=24.2, ycen=20.9, mag=15, re=7, nser=1.8, ang=100, axrat=0.8, convolve=True))])
+    fine = (rng.random((50, 60)) < 0.6).astype(np.uint8)
+    c["mask_given_finesampled"] = dict(width=30, height=25, finesampling=2, mask=fine.tolist(), adjust_mask=False,
+                                       profiles=[("king", dict(xcen=14.8, ycen=12.2, rc=2.0, rt=9.0))])
     return c
 
 

@@ -32,4 +32,5 @@ def to_case(O, entry):
                   finesampling=spec.get("finesampling", 1),
                   return_finesampled=spec.get("return_finesampled", True),
                   convolver=spec.get("convolver", "brute"),
-                  mask=None if spec.get("mask") is None else np.asarray(spec["mask"], dtype=np.uint8))
+                  mask=None if spec.get("mask") is None else np.asarray(spec["mask"], dtype=np.uint8),
+                  adjust_mask=spec.get("adjust_mask", True))

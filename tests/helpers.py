@@ -15,6 +15,7 @@ def product_model(spec, psf, env=None):
         m.set_psf(psf)
     if spec.get("mask") is not None:
         m.set_mask(np.asarray(spec["mask"], dtype=np.uint8))
+        m.set_adjust_mask(spec.get("adjust_mask", True))
     if env is not None:
         m.set_cuda_env(env)
     for kind, params in spec["profiles"]:

@@ -42,7 +42,7 @@ def test_struct_layout_matches_header():
     from libprofit_gb300 import _ffi
     # pf_profile_desc: 5 int32 + 2 uint32 (28 B, padded to 32) + 3 + 12 doubles
     assert ctypes.sizeof(_ffi.ProfileDesc) == 32 + 15 * 8
-    assert ctypes.sizeof(_ffi.ModelDesc) == 104
+    assert ctypes.sizeof(_ffi.ModelDesc) == 112
 
 
 def test_version_and_errors_without_gpu(lib):
