@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--models", type=int, default=1024)
+    ap.add_argument("--models", type=int, default=None,
+                    help="models in the batch (default: 1024 for cfg4, 4096 for cfg3)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--convolver", default="auto", choices=["auto", "brute", "fft"],
                     help="convolution method of the FP32 batch (auto: the library's choice)")
@@ -207,7 +208,7 @@ def run_reference(args, world, rank):
     if rank != 0:
         return
     import workloads as W
-    specs = W.cfg4(args.models)
+    specs = W.cfg4(args.models or 1024)
     par = W.param_matrix(specs)
     vals = []
     for _ in range(max(1, args.warmup // 3)):
@@ -222,7 +223,7 @@ def run_reference(args, world, rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": "1024 models 256x256, sersic bulge+disk, 25x25 Moffat PSF, model+VJP",
-                       "models": args.models},
+                       "models": len(specs)},
             "cpu_baseline": {"value": value, "unit": "models/s", "cores": threads, "kind": "port",
                              "sample": "models rendered + 33-point central-difference gradient until 5 s per step"},
             "e2e": {"value": value, "unit": "models/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -249,7 +250,7 @@ def run_ours(args, world, rank, local):
     torch.cuda.set_device(local)
     env64 = pg.get_cuda_environment(local, use_double=True)
     env32 = pg.get_cuda_environment(local, use_double=False, profile=True)
-    specs, par, data_np, sigma_np = make_problem(args.models, rank, env64, torch)
+    specs, par, data_np, sigma_np = make_problem(args.models or 1024, rank, env64, torch)
     n_models = len(specs)
     models32 = [W.to_model(s, env32) for s in specs]
     for m in models32:
@@ -435,7 +436,7 @@ def run_ours(args, world, rank, local):
     # DRAM bytes per launch, per model of this workload: ncu dram__bytes_read.sum +
     # dram__bytes_write.sum of each kernel on the 256-model copy of the workload
     # (profiles/*_256x256*.md), divided by 256
-    traffic_per_model = {"eval_ms": 106.6e6 / 256, "backward_ms": 83.1e6 / 256, "finish_ms": 192.3e6 / 256,
+    traffic_per_model = {"eval_ms": 118.5e6 / 256, "backward_ms": 76.3e6 / 256, "finish_ms": 192.3e6 / 256,
                          "adjoint_conv_ms": ADJ_CONV_TRAFFIC_PER_MODEL}
     roof = {"bound": "fp32", "kernel": dom.replace("_ms", ""), "achieved": None, "peak": fp32_peak,
             "unit": "TFLOP/s", "frac": None, "traffic": None,
@@ -502,7 +503,7 @@ def run_workload(args, world, rank, local):
     torch.cuda.set_device(local)
     env64 = pg.get_cuda_environment(local, use_double=True)
     env32 = pg.get_cuda_environment(local, use_double=False, profile=True)
-    specs = W.CONFIGS[int(args.workload[3:])]()
+    specs = W.cfg3(args.models or 4096) if args.workload == "cfg3" else W.CONFIGS[int(args.workload[3:])]()
     with_grad = args.workload == "cfg5"
     models = [W.to_model(s, env32) for s in specs]
     batch = pg.Batch(models, env32)
@@ -637,8 +638,8 @@ def run_workload(args, world, rank, local):
                "sample": "%d model(s) rendered (direct convolution) in %.1f s" % (done, dt)}
     dom = max(per_step, key=per_step.get)
     desc = {"cfg2": "one 1000x1000 model: sersic bulge + disk + sky, 51x51 Moffat PSF by FFT, forward",
-            "cfg3": "4096 models, sides 64-512, 1-3 radial profiles of six kinds, own Moffat PSFs (15-41), "
-                    "autotuned convolution, forward",
+            "cfg3": "%d models, sides 64-512, 1-3 radial profiles of six kinds, own Moffat PSFs (15-41), "
+                    "autotuned convolution, forward" % n_models,
             "cfg5": "one 4096x4096 field: 10,000 radial profiles + sky, 101x101 Moffat PSF by an 8192x8192 FFT, "
                     "forward + chi2 + gradients of all profiles"}[args.workload]
     line = {
