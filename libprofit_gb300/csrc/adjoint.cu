@@ -47,6 +47,12 @@ namespace {
 #ifndef PF_BACKWARD_MIN_BLOCKS
 #define PF_BACKWARD_MIN_BLOCKS 4
 #endif
+// phase-A (ring tile) items a warp claims at once (a divisor of 32): 8
+// measured best on the 1024-model step (backward 2.57 ms, against 2.87 at 32
+// and 2.68 at 2)
+#ifndef PF_BACKWARD_RING_CHUNK
+#define PF_BACKWARD_RING_CHUNK 8
+#endif
 constexpr int kWarpsB = PF_BACKWARD_WARPS;
 // the forward pass's guard bands (eval_f32.cu), so that both take the same decisions
 constexpr float kGuardAccB = 1.2e-5f;
@@ -764,15 +770,28 @@ backward_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restric
 	WarpScratchG<T, NS> &ws = scratch[warp];
 	const unsigned int n_a = n_profiles * (kRingRows * kRingCols);
 	const unsigned int n_items = n_a + n_ring * n_profiles;
+	// phase A from counter[0], PF_BACKWARD_RING_CHUNK items per claim; phase B
+	// from counter[1], 32 per claim (as the evaluation kernel)
+	bool ring = n_a > 0;
 	while (true) {
 		unsigned int chunk = 0;
-		if (lane == 0) chunk = atomicAdd(counter, 32u);
+		if (lane == 0) {
+			chunk = atomicAdd(&counter[ring ? 0 : 1], ring ? (unsigned int)PF_BACKWARD_RING_CHUNK : 32u);
+		}
 		chunk = __shfl_sync(0xffffffffu, chunk, 0);
+		if (ring && chunk >= n_a) {
+			ring = false;
+			continue;
+		}
+		if (!ring) chunk += n_a;
 		if (chunk >= n_items) break;
 		const unsigned int k = chunk + (unsigned int)lane;
 		int p = 0, row = -1, tc = -1;
 		long long slot = 0;
-		if (k < n_a) {
+		if (ring && lane >= PF_BACKWARD_RING_CHUNK) {
+			// not this claim's item
+		}
+		else if (k < n_a) {
 			const unsigned int per_ring = n_profiles * kRingCols;
 			const unsigned int l = k / per_ring;
 			const unsigned int rem = k - l * per_ring;

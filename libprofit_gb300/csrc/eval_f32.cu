@@ -40,6 +40,11 @@ namespace {
 #ifndef PF_EVAL32_MIN_BLOCKS
 #define PF_EVAL32_MIN_BLOCKS 5
 #endif
+// phase-A (ring tile) items a warp claims at once (a divisor of 32; 32, 8
+// and 2 measured within 5 % of each other on the 1024-model step)
+#ifndef PF_EVAL_RING_CHUNK
+#define PF_EVAL_RING_CHUNK 32
+#endif
 constexpr int kWarps32 = PF_EVAL32_WARPS;
 // Half-width of the band around a threshold inside which an FP32 comparison is
 // re-taken in FP64. The FP32 profile values carry at most ~3e-6 relative
@@ -455,9 +460,11 @@ __device__ __forceinline__ long long ring_tile(const ModelDev *__restrict__ mode
 }
 
 // Work items: phase A (ring_tile, n_ring_items of them, a multiple of 32),
-// then phase B, every tile in order. Warps take 32 items at a time from a
-// global counter; a tile is evaluated by the item that first sets its bit in
-// `claims` (zeroed before the launch), so each tile exactly once.
+// then phase B, every tile in order. Warps take phase-A items
+// PF_EVAL_RING_CHUNK at a time from counter[0] (the costly centre tiles of one profile are not
+// all left to one warp) and phase-B tiles 32 at a time from counter[1]; a
+// tile is evaluated by the item that first sets its bit in `claims` (zeroed
+// before the launch), so each tile exactly once.
 template <unsigned int KINDS>
 __global__ void __launch_bounds__(kWarps32 * 32, PF_EVAL32_MIN_BLOCKS)
 eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const ProfileDev *__restrict__ profs,
@@ -468,17 +475,23 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 	__shared__ WarpScratchM scratch[kWarps32];
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	WarpScratchM &ws = scratch[warp];
-	const unsigned int n_items = n_ring_items + n_tiles;
+	bool ring = n_ring_items > 0;
 	while (true) {
 		unsigned int chunk = 0;
-		if (lane == 0) chunk = atomicAdd(counter, 32u);
+		if (lane == 0) {
+			chunk = atomicAdd(&counter[ring ? 0 : 1], ring ? (unsigned int)PF_EVAL_RING_CHUNK : 32u);
+		}
 		chunk = __shfl_sync(0xffffffffu, chunk, 0);
-		if (chunk >= n_items) break;
+		if (ring && chunk >= n_ring_items) {
+			ring = false;
+			continue;
+		}
+		if (!ring && chunk >= n_tiles) break;
 		long long tile = -1;
 		unsigned int todo;
-		if (chunk >= n_ring_items) {
+		if (!ring) {
 			// phase B: 32 consecutive tiles, one claim word
-			const unsigned int t0 = chunk - n_ring_items;
+			const unsigned int t0 = chunk;
 			const unsigned int left = n_tiles - t0;
 			const unsigned int valid = left >= 32 ? 0xffffffffu : (1u << left) - 1u;
 			unsigned int old = 0;
@@ -487,7 +500,7 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 			tile = (long long)t0 + lane;
 		}
 		else {
-			tile = ring_tile(models, profs, n_profiles, chunk + (unsigned int)lane);
+			tile = lane < PF_EVAL_RING_CHUNK ? ring_tile(models, profs, n_profiles, chunk + (unsigned int)lane) : -1;
 			bool mine = false;
 			if (tile >= 0) {
 				const unsigned int bit = 1u << (tile & 31);

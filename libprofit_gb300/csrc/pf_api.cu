@@ -881,7 +881,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 
 	PF_CUDA_TRY(cudaMalloc(&b->d_models, sizeof(pf::ModelDev) * std::max<size_t>(1, n_models)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_profiles, sizeof(pf::ProfileDev) * std::max<size_t>(1, n_profiles)));
-	PF_CUDA_TRY(cudaMalloc(&b->d_counter, sizeof(unsigned int)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_counter, 2 * sizeof(unsigned int)));
 	b->sersic_only = true;
 	for (size_t i = 0; i < n_profiles; i++) {
 		const int k = b->h_profiles[i].kind;
@@ -1493,7 +1493,7 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	PF_CUDA_TRY(cudaMalloc(&b->d_ring_partial, sizeof(double) * pf::backward_ring_slots(b->sersic_only) *
 	                                               std::max<size_t>(1, b->profiles.size())));
 	PF_CUDA_TRY(cudaMalloc(&b->d_prow_base, sizeof(long long) * prow_base.size()));
-	PF_CUDA_TRY(cudaMalloc(&b->d_bwd_counter, sizeof(unsigned int)));
+	PF_CUDA_TRY(cudaMalloc(&b->d_bwd_counter, 2 * sizeof(unsigned int)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_adj_tile_base, sizeof(long long) * adj_tile_base.size()));
 	PF_CUDA_TRY(cudaMemcpy(b->d_prow_base, prow_base.data(), sizeof(long long) * prow_base.size(), cudaMemcpyHostToDevice));
 	PF_CUDA_TRY(cudaMemcpy(b->d_adj_tile_base, adj_tile_base.data(), sizeof(long long) * adj_tile_base.size(),
@@ -1580,7 +1580,7 @@ pf_status pf_backward(pf_batch *b, const void *images_dev, const void *data_dev,
 		stage_end(b, t, stream);
 	}
 	t = stage_begin(b, ST_BACKWARD, stream);
-	PF_CUDA_TRY(cudaMemsetAsync(b->d_bwd_counter, 0, sizeof(unsigned int), stream));
+	PF_CUDA_TRY(cudaMemsetAsync(b->d_bwd_counter, 0, 2 * sizeof(unsigned int), stream));
 	if (b->dbl) pf::launch_backward<double>(b->d_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc,
 	                                        b->d_prow_base, b->n_ring, b->d_bwd_counter, b->d_partial,
 	                                        b->d_ring_partial, grad_dev, b->sersic_only, b->env->n_sm, stream);

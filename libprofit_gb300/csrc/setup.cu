@@ -498,7 +498,8 @@ __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs,
                                       unsigned int *err)
 {
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
-		*tile_counter = 0;
+		tile_counter[0] = 0;  // the eval kernels' work counters (two: the FP32 one's phases)
+		tile_counter[1] = 0;
 	}
 	const int t = blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= n_profiles) {
