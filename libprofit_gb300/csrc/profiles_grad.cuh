@@ -35,9 +35,18 @@ namespace grad {
 
 constexpr int kSlots = 12;
 
-__host__ __device__ inline float g_exp(float x) { return expf(x); }
+// single precision on the device: the special-function unit's exp2 / log2
+// (a few 1e-7 relative, plus |x| eps for exp): the terms feed gradients
+// checked at 1e-3, and the value used for decisions comes from
+// profiles_f32.cuh, not from here
+#ifdef __CUDA_ARCH__
+__device__ inline float g_exp(float x) { return __expf(x); }
+__device__ inline float g_log(float x) { return __logf(x); }
+#else
+inline float g_exp(float x) { return expf(x); }
+inline float g_log(float x) { return logf(x); }
+#endif
 __host__ __device__ inline double g_exp(double x) { return exp(x); }
-__host__ __device__ inline float g_log(float x) { return logf(x); }
 __host__ __device__ inline double g_log(double x) { return log(x); }
 __host__ __device__ inline float g_log1p(float x) { return log1pf(x); }
 __host__ __device__ inline double g_log1p(double x) { return log1p(x); }
