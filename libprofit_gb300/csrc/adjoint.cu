@@ -24,7 +24,9 @@
 // (bg). A batch whose radial profiles are all sersics runs kernels with eight
 // gradient slots per partial (value, five geometric, re, nser); any other
 // batch runs the same kernels with twelve (value, five geometric, par[6..11]),
-// the other kinds' terms coming from profiles_grad.cuh.
+// the other kinds' terms coming from profiles_grad.cuh. The psf profile
+// (point source, src/psf.cpp:58-145): xcen, ycen (its stamp's overlaps are
+// piecewise linear in the centre) and mag.
 #include <cstdint>
 #include <type_traits>
 
@@ -32,6 +34,7 @@
 #include "profiles_f32.cuh"
 #include "profiles_f64.cuh"
 #include "profiles_grad.cuh"
+#include "psf_profile.cuh"
 
 namespace pf {
 
@@ -607,6 +610,11 @@ __device__ __forceinline__ int item_row(const ProfileDev &P, const ModelDev &m, 
 		centre = (int)floorf(__fdividef(P.fyc_hi, m.fsy_hi));
 		centre = min(max(centre, lo), max(lo, hi));
 	}
+	else if (P.kind == PF_PSF && m.psf_off >= 0) {
+		int x0, x1;
+		psf_stamp(P, m, x0, x1, lo, hi);
+		centre = (lo + hi) / 2;
+	}
 	else {
 		return -1;
 	}
@@ -621,11 +629,13 @@ __device__ __forceinline__ int item_row(const ProfileDev &P, const ModelDev &m, 
 template <typename T, unsigned int KINDS>
 __device__ void backward_row(const ModelDev &m, const ProfileDev &P, int row, int c0, int c1, int s0, int s1,
                              const T *__restrict__ gout, const T *__restrict__ gsrc,
-                             WarpScratchG<T, slots_of<KINDS>()> &ws, int lane, double *dst)
+                             const double *__restrict__ psf_pool, WarpScratchG<T, slots_of<KINDS>()> &ws, int lane,
+                             double *dst)
 {
 	constexpr bool dbl = std::is_same<T, double>::value;
 	constexpr int NS = slots_of<KINDS>();
 	const bool is_sky = P.kind == PF_SKY;
+	const bool is_psf = P.kind == PF_PSF;
 	const T *gimg = P.convolve ? gsrc + m.draw_off : nullptr;
 	const f32::Shape sh = f32::load_shape(P);
 	grad::GShape<T> gs;
@@ -638,14 +648,25 @@ __device__ void backward_row(const ModelDev &m, const ProfileDev &P, int row, in
 	for (int tcol = c0; tcol <= c1; tcol++) {
 		if (tcol >= s0 && tcol <= s1) continue;
 		const int px = tcol * 32 + lane;
-		// masked drawing pixels were not evaluated: no gradient from them
-		const bool active = px < (int)m.draw_w && evaluated(m, px, row);
+		// masked drawing pixels were not evaluated: no gradient from them (the
+		// psf profile is drawn whatever the mask, src/psf.cpp:58-145)
+		const bool active = px < (int)m.draw_w && (is_psf || evaluated(m, px, row));
 		T g = 0;
 		if (active) {
 			g = gimg ? gimg[(size_t)row * m.draw_w + px] : g_direct(m, gout, px, row);
 		}
 		if (is_sky) {
 			acc[G_V] += g;
+			continue;
+		}
+		if (is_psf) {
+			double v, dvx, dvy;
+			if (active && g != (T)0 &&
+			    psf_pixel_grad64(P, m, psf_pool + m.psf_off, (unsigned int)px, (unsigned int)row, v, dvx, dvy)) {
+				acc[G_V] += g * (T)v;
+				acc[G_XCEN] += g * (T)dvx;
+				acc[G_YCEN] += g * (T)dvy;
+			}
 			continue;
 		}
 		// the forward pass's decisions for this pixel (eval_f32.cu / eval_f64.cu)
@@ -760,9 +781,9 @@ __device__ void backward_row(const ModelDev &m, const ProfileDev &P, int row, in
 template <typename T, unsigned int KINDS>
 __global__ void __launch_bounds__(kWarpsB * 32, PF_BACKWARD_MIN_BLOCKS)
 backward_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restrict__ profs, unsigned int n_profiles,
-                const T *__restrict__ gout, const T *__restrict__ gsrc, const long long *__restrict__ prow_base,
-                unsigned int n_ring, unsigned int *counter, double *__restrict__ partial,
-                double *__restrict__ ring_partial)
+                const T *__restrict__ gout, const T *__restrict__ gsrc, const double *__restrict__ psf_pool,
+                const long long *__restrict__ prow_base, unsigned int n_ring, unsigned int *counter,
+                double *__restrict__ partial, double *__restrict__ ring_partial)
 {
 	constexpr int NS = slots_of<KINDS>();
 	__shared__ WarpScratchG<T, NS> scratch[kWarpsB];
@@ -819,16 +840,23 @@ backward_kernel(const ModelDev *__restrict__ models, const ProfileDev *__restric
 			const ProfileDev &P = profs[ip];
 			const ModelDev &m = models[P.model];
 			if (itc >= 0) {  // phase A: one ring tile
-				backward_row<T, KINDS>(m, P, irow, itc, itc, 0, -1, gout, gsrc, ws, lane, ring_partial + islot);
+				backward_row<T, KINDS>(m, P, irow, itc, itc, 0, -1, gout, gsrc, psf_pool, ws, lane,
+				                       ring_partial + islot);
 			}
 			else {           // phase B: the row but its ring tiles
 				int c0 = 0, c1 = (int)m.tiles_per_row - 1, s0 = 0, s1 = -1;
-				if (P.kind != PF_SKY) {
+				if (P.kind == PF_PSF) {
+					int x0, x1, y0, y1;
+					psf_stamp(P, m, x0, x1, y0, y1);
+					c0 = x0 / 32;
+					c1 = x1 / 32;
+				}
+				else if (P.kind != PF_SKY) {
 					c0 = max(0, P.bbx0) / 32;
 					c1 = P.bbx1 < 0 ? -1 : min((int)m.draw_w - 1, P.bbx1) / 32;
 					ring_cols_of_row(P, m, irow, s0, s1);
 				}
-				backward_row<T, KINDS>(m, P, irow, c0, c1, s0, s1, gout, gsrc, ws, lane,
+				backward_row<T, KINDS>(m, P, irow, c0, c1, s0, s1, gout, gsrc, psf_pool, ws, lane,
 				                       partial + (prow_base[ip] + irow) * (long long)NS);
 			}
 		}
@@ -853,11 +881,16 @@ __global__ void grad_reduce_kernel(const ModelDev *__restrict__ models, const Pr
 	double *g = grad + (size_t)i * PF_NPAR;
 	if (lane < PF_NPAR) g[lane] = 0.;
 	const bool radial = is_radial_kind(P.kind);
-	if (!radial && P.kind != PF_SKY) return;
+	const bool psf = P.kind == PF_PSF && m.psf_off >= 0;
+	if (!radial && !psf && P.kind != PF_SKY) return;
 	int lo = 0, hi = (int)m.draw_h - 1;
 	if (radial) {
 		lo = max(0, P.bby0);
 		hi = min(hi, P.bby1);
+	}
+	else if (psf) {
+		int x0, x1;
+		psf_stamp(P, m, x0, x1, lo, hi);
 	}
 	double S[NS];
 	for (int k = 0; k < NS; k++) S[k] = 0.;
@@ -880,6 +913,13 @@ __global__ void grad_reduce_kernel(const ModelDev *__restrict__ models, const Pr
 	if (lane != 0) return;
 	if (P.kind == PF_SKY) {
 		g[6] = T8[G_V] / (m.fs * m.fs);  // d/d bg of bg / fs^2 on every pixel (src/sky.cpp:42-45)
+		return;
+	}
+	if (psf) {  // value x 10^(-0.4 (mag - magzero)) (src/psf.cpp:66, 141)
+		const double sc = P.psf_mag_scale;
+		g[PF_P_XCEN] = sc * T8[G_XCEN];
+		g[PF_P_YCEN] = sc * T8[G_YCEN];
+		g[PF_P_MAG] = -0.4 * log(10.) * sc * T8[G_V];
 		return;
 	}
 	const double fs_ = P.flux_scale;
@@ -907,24 +947,24 @@ void launch_chi2(const ModelDev *models, int n_models, const void *img, const vo
 
 template <typename T>
 void launch_backward(const ModelDev *models, const ProfileDev *profs, int n_profiles, const void *gout,
-                     const void *gsrc, const long long *prow_base, unsigned int n_ring, unsigned int *counter,
-                     double *partial, double *ring_partial, double *grad, bool sersic_only, int n_sm,
-                     cudaStream_t stream)
+                     const void *gsrc, const double *psf_pool, const long long *prow_base, unsigned int n_ring,
+                     unsigned int *counter, double *partial, double *ring_partial, double *grad, bool sersic_only,
+                     int n_sm, cudaStream_t stream)
 {
 	if (n_profiles <= 0) return;
 	const int blocks = n_sm * PF_BACKWARD_MIN_BLOCKS;
 	const int rblocks = (int)(((long long)n_profiles * 32 + 255) / 256);
 	if (sersic_only) {
 		backward_kernel<T, f32::kSersicOnly><<<blocks, kWarpsB * 32, 0, stream>>>(
-		    models, profs, (unsigned int)n_profiles, (const T *)gout, (const T *)gsrc, prow_base, n_ring, counter,
-		    partial, ring_partial);
+		    models, profs, (unsigned int)n_profiles, (const T *)gout, (const T *)gsrc, psf_pool, prow_base, n_ring,
+		    counter, partial, ring_partial);
 		grad_reduce_kernel<slots_of<f32::kSersicOnly>()><<<rblocks, 256, 0, stream>>>(
 		    models, profs, n_profiles, prow_base, partial, ring_partial, grad);
 	}
 	else {
 		backward_kernel<T, f32::kAllKinds><<<blocks, kWarpsB * 32, 0, stream>>>(
-		    models, profs, (unsigned int)n_profiles, (const T *)gout, (const T *)gsrc, prow_base, n_ring, counter,
-		    partial, ring_partial);
+		    models, profs, (unsigned int)n_profiles, (const T *)gout, (const T *)gsrc, psf_pool, prow_base, n_ring,
+		    counter, partial, ring_partial);
 		grad_reduce_kernel<slots_of<f32::kAllKinds>()><<<rblocks, 256, 0, stream>>>(
 		    models, profs, n_profiles, prow_base, partial, ring_partial, grad);
 	}
@@ -947,10 +987,10 @@ template void launch_chi2<float>(const ModelDev *, int, const void *, const void
 template void launch_chi2<double>(const ModelDev *, int, const void *, const void *, const void *, const void *,
                                   void *, double *, int, double *, unsigned int *, cudaStream_t);
 template void launch_backward<float>(const ModelDev *, const ProfileDev *, int, const void *, const void *,
-                                     const long long *, unsigned int, unsigned int *, double *, double *, double *,
-                                     bool, int, cudaStream_t);
+                                     const double *, const long long *, unsigned int, unsigned int *, double *,
+                                     double *, double *, bool, int, cudaStream_t);
 template void launch_backward<double>(const ModelDev *, const ProfileDev *, int, const void *, const void *,
-                                      const long long *, unsigned int, unsigned int *, double *, double *, double *,
-                                      bool, int, cudaStream_t);
+                                      const double *, const long long *, unsigned int, unsigned int *, double *,
+                                      double *, double *, bool, int, cudaStream_t);
 
 }  // namespace pf

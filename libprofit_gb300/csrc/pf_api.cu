@@ -78,9 +78,9 @@ void launch_chi2(const ModelDev *models, int n_models, const void *img, const vo
                  cudaStream_t stream);
 template <typename T>
 void launch_backward(const ModelDev *models, const ProfileDev *profs, int n_profiles, const void *gout,
-                     const void *gsrc, const long long *prow_base, unsigned int n_ring, unsigned int *counter,
-                     double *partial, double *ring_partial, double *grad, bool sersic_only, int n_sm,
-                     cudaStream_t stream);
+                     const void *gsrc, const double *psf_pool, const long long *prow_base, unsigned int n_ring,
+                     unsigned int *counter, double *partial, double *ring_partial, double *grad, bool sersic_only,
+                     int n_sm, cudaStream_t stream);
 long long backward_items(long long n_profiles, long long n_ring);
 int backward_slots(bool sersic_only);
 long long backward_ring_slots(bool sersic_only);
@@ -1437,11 +1437,11 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	for (size_t i = 0; i < b->profiles.size(); i++) {
 		const pf_profile_desc &d = b->profiles[i];
 		const bool ok = (d.kind >= PF_SERSIC && d.kind <= PF_BROKENEXP && !(d.kind == PF_SERSIC && d.rescale_flux)) ||
-		                d.kind == PF_SKY || d.kind == PF_NULL;
+		                d.kind == PF_SKY || d.kind == PF_PSF || d.kind == PF_NULL;
 		if (!ok) {
 			return fail(PF_ERR_UNSUPPORTED, "profile " + std::to_string(i) +
 			                                    ": the adjoint supports the radial profiles (a sersic without "
-			                                    "rescale_flux), sky and null");
+			                                    "rescale_flux), sky, psf and null");
 		}
 	}
 	PF_CUDA_TRY(cudaSetDevice(b->env->device));
@@ -1582,11 +1582,11 @@ pf_status pf_backward(pf_batch *b, const void *images_dev, const void *data_dev,
 	t = stage_begin(b, ST_BACKWARD, stream);
 	PF_CUDA_TRY(cudaMemsetAsync(b->d_bwd_counter, 0, 2 * sizeof(unsigned int), stream));
 	if (b->dbl) pf::launch_backward<double>(b->d_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc,
-	                                        b->d_prow_base, b->n_ring, b->d_bwd_counter, b->d_partial,
+	                                        b->d_psf_norm, b->d_prow_base, b->n_ring, b->d_bwd_counter, b->d_partial,
 	                                        b->d_ring_partial, grad_dev, b->sersic_only, b->env->n_sm, stream);
-	else pf::launch_backward<float>(b->d_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc, b->d_prow_base,
-	                                b->n_ring, b->d_bwd_counter, b->d_partial, b->d_ring_partial, grad_dev,
-	                                b->sersic_only, b->env->n_sm, stream);
+	else pf::launch_backward<float>(b->d_models, b->d_profiles, n_profiles, b->d_gout, b->d_gsrc, b->d_psf_norm,
+	                                b->d_prow_base, b->n_ring, b->d_bwd_counter, b->d_partial, b->d_ring_partial,
+	                                grad_dev, b->sersic_only, b->env->n_sm, stream);
 	stage_end(b, t, stream);
 	b->backward_calls++;
 	{

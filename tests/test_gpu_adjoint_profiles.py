@@ -189,3 +189,45 @@ def test_mixed_batch_equals_single_models(problems, use_double):
         scale = np.abs(g_one).max()
         np.testing.assert_allclose(g_all[row:row + n], g_one, rtol=tol * 100, atol=tol * scale)
         row += n
+
+
+# The psf profile (a point source, src/psf.cpp:58-145): its stamp's overlaps
+# with the image pixels are piecewise linear in the centre, so its xcen and
+# ycen gradients are those of the overlap lengths; mag scales it. A sersic
+# (convolved) plus two point sources, one convolved and one not, plus a sky.
+def _psf_problem(O):
+    import workloads as W
+    rng = np.random.default_rng(31)
+    psf = W.moffat_psf(15, 3.0, 2.5)
+    truth = [("sersic", dict(xcen=30.2, ycen=33.7, mag=16.0, re=5.0, nser=2.0, ang=20.0, axrat=0.6, convolve=True)),
+             ("psf", dict(xcen=20.37, ycen=22.81, mag=17.0)),
+             ("psf", dict(xcen=44.62, ycen=17.29, mag=16.5, convolve=True)),
+             ("sky", dict(bg=0.5))]
+    data, _, _ = O.evaluate(O.Case(SIDE, SIDE, truth, psf=psf, magzero=MAGZERO))
+    perturbed = [(k, dict(p)) for k, p in truth]
+    perturbed[1][1].update(xcen=20.61, ycen=22.55, mag=17.2)
+    perturbed[2][1].update(xcen=44.43, ycen=17.48, mag=16.3)
+    sigma = 0.01 * data.max()
+    data = data + rng.normal(0, sigma, data.shape)
+    return psf, perturbed, data, np.full_like(data, sigma)
+
+
+@pytest.mark.parametrize("use_double", [True, False])
+def test_psf_profile_gradient_matches_finite_differences(oracle_lib, use_double):
+    O = oracle_lib
+    psf, profiles, data, sigma = _psf_problem(O)
+    chi2, grad = _gpu_grads([(psf, profiles)], [data], [sigma], use_double)
+    chi2_ref, _ = _chi2(O, psf, profiles, data, sigma)
+    assert abs(chi2[0] - chi2_ref) <= (1e-10 if use_double else 1e-4) * chi2_ref
+    rtol, floor = (1e-4, 1e-9) if use_double else (1e-3, 1e-6)
+    slots = {"xcen": 0, "ycen": 1, "mag": 2}
+    for i in (1, 2):
+        for k in ("xcen", "ycen", "mag"):
+            v = profiles[i][1][k]
+            h = 1e-6 * max(abs(v), 1e-3)
+            cp, _ = _chi2(O, psf, _with(profiles, i, k, v + h), data, sigma)
+            cm, _ = _chi2(O, psf, _with(profiles, i, k, v - h), data, sigma)
+            want = (cp - cm) / (2 * h)
+            got = grad[i, slots[k]]
+            atol = floor * chi2_ref / h
+            assert abs(got - want) <= rtol * abs(want) + atol, "psf %d %s: adjoint %.8g vs fd %.8g" % (i, k, got, want)
