@@ -292,7 +292,7 @@ PF_API pf_status pf_forward(pf_batch *batch, void *images_dev, double *flux_dev,
  * data/sigma/cotangent have the images' layout and precision. The
  * subsampling tree of every pixel is recomputed, not stored, and held fixed.
  * Supported: the six radial profiles with all their parameters (a sersic
- * without rescale_flux), sky (bg), psf (xcen, ycen, mag), null.
+ * with rescale_flux too), sky (bg), psf (xcen, ycen, mag), null.
  * pf_forward_backward = pf_forward followed by pf_backward.
  */
 PF_API pf_status pf_batch_enable_adjoint(pf_batch *batch);

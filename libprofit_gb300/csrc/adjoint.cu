@@ -19,7 +19,7 @@
 //
 // Profiles supported by the adjoint: the six radial profiles with all their
 // parameters (xcen, ycen, mag, ang, axrat, box and the profile's own: sersic
-// re, nser, not with rescale_flux; coresersic re, nser, rb, a, b; moffat fwhm,
+// re, nser (rescale_flux included); coresersic re, nser, rb, a, b; moffat fwhm,
 // con; ferrer rout, a, b; king rc, rt, a; brokenexp h1, h2, rb, a) and sky
 // (bg). A batch whose radial profiles are all sersics runs kernels with eight
 // gradient slots per partial (value, five geometric, re, nser); any other

@@ -1436,12 +1436,10 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	if (b->adjoint) return PF_OK;
 	for (size_t i = 0; i < b->profiles.size(); i++) {
 		const pf_profile_desc &d = b->profiles[i];
-		const bool ok = (d.kind >= PF_SERSIC && d.kind <= PF_BROKENEXP && !(d.kind == PF_SERSIC && d.rescale_flux)) ||
-		                d.kind == PF_SKY || d.kind == PF_PSF || d.kind == PF_NULL;
+		const bool ok = (d.kind >= PF_SERSIC && d.kind <= PF_BROKENEXP) || d.kind == PF_SKY || d.kind == PF_PSF ||
+		                d.kind == PF_NULL;
 		if (!ok) {
-			return fail(PF_ERR_UNSUPPORTED, "profile " + std::to_string(i) +
-			                                    ": the adjoint supports the radial profiles (a sersic without "
-			                                    "rescale_flux), sky, psf and null");
+			return fail(PF_ERR_UNSUPPORTED, "profile " + std::to_string(i) + ": no adjoint for this profile kind");
 		}
 	}
 	PF_CUDA_TRY(cudaSetDevice(b->env->device));

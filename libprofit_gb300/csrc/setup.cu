@@ -336,7 +336,7 @@ __device__ void adjoint_constants(ProfileDev &p, double dbn, double lum_int, int
 	for (int k = 0; k < PF_NPAR; k++) p.dlnfs[k] = 0.;
 	p.dbn = 0.;
 	p.grad_ok = 0;
-	if ((p.kind == PF_SERSIC && p.rescale_flux) || p.kind < PF_SERSIC || p.kind > PF_BROKENEXP) {
+	if (p.kind < PF_SERSIC || p.kind > PF_BROKENEXP) {
 		return;
 	}
 	const double q = p.par[PF_P_AXRAT], B = p.par[PF_P_BOX] + 2;
@@ -348,6 +348,19 @@ __device__ void adjoint_constants(ProfileDev &p, double dbn, double lum_int, int
 		p.dbn = dbn;
 		p.dlnfs[6] = -2 / re;
 		p.dlnfs[7] = -(1 / n + 2 * sf::digamma(2 * n) + dbn - 2 * log(p.bn) - 2 * n * dbn / p.bn);
+		if (p.adjust && p.rescale_flux && want) {
+			// flux_scale also divides by P(2n, x), x = bn (rscale_max / re)^(1/n)
+			// (src/sersic.cpp:302-311); rscale_max, when derived, moves in steps
+			// (a ceiling) and contributes nothing between them
+			const double lr = log(p.rscale_max) - log(re);
+			const double x = p.bn * exp(lr / n);
+			const double a = 2 * n, d = 1e-4 * a;
+			const double P = sf::pgamma(x, a);
+			const double dPda = (sf::pgamma(x, a + d) - sf::pgamma(x, a - d)) / (2 * d);
+			const double px = exp((a - 1.) * log(x) - x - lgamma(a)) * x;  // x p(x; a)
+			p.dlnfs[6] -= px * (-1 / (n * re)) / P;
+			p.dlnfs[7] -= (2 * dPda + px * (dbn / p.bn - lr / (n * n))) / P;
+		}
 		p.fbn = (float)p.bn;
 		p.fdbn = (float)dbn;
 		p.fnser = (float)n;
@@ -509,7 +522,7 @@ __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs,
 	const double nser = profs[t].par[7];
 	const double bn = solves[(size_t)t * 3 + 0];
 	SersicSolves sv{solves[(size_t)t * 3 + 1], solves[(size_t)t * 3 + 2], 0.};
-	if (((kind == PF_SERSIC && !profs[t].rescale_flux) || kind == PF_CORESERSIC) && want_grad) {
+	if ((kind == PF_SERSIC || kind == PF_CORESERSIC) && want_grad) {
 		sv.dbn = dbn_dn(nser, bn);
 	}
 	ProfileDev p = profs[t];

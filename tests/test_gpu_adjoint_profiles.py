@@ -231,3 +231,40 @@ def test_psf_profile_gradient_matches_finite_differences(oracle_lib, use_double)
             got = grad[i, slots[k]]
             atol = floor * chi2_ref / h
             assert abs(got - want) <= rtol * abs(want) + atol, "psf %d %s: adjoint %.8g vs fd %.8g" % (i, k, got, want)
+
+
+# A Sersic with rescale_flux (src/sersic.cpp:302-325): the flux scale divides
+# by P(2n, bn (rscale_max / re)^(1/n)), with rscale_max given (so it moves
+# with re and nser through x) and derived by adjust (a ceiling: constant
+# between its steps).
+@pytest.mark.parametrize("use_double", [True, False])
+@pytest.mark.parametrize("rscale_max", [6.0, 0.0])
+def test_rescale_flux_gradient_matches_finite_differences(oracle_lib, use_double, rscale_max):
+    import workloads as W
+    O = oracle_lib
+    rng = np.random.default_rng(57)
+    psf = W.moffat_psf(15, 3.0, 2.5)
+    sersic = dict(xcen=31.1, ycen=30.4, mag=16.0, re=6.0, nser=2.6, ang=35.0, axrat=0.65, box=0.05, convolve=True,
+                  rescale_flux=True, rscale_max=rscale_max)
+    truth = [("sersic", sersic), ("sky", dict(bg=0.3))]
+    data, _, _ = O.evaluate(O.Case(SIDE, SIDE, truth, psf=psf, magzero=MAGZERO))
+    profiles = _with(_with(_with(truth, 0, "re", 6.4), 0, "nser", 2.4), 0, "xcen", 31.5)
+    sigma = np.full_like(data, 0.01 * data.max())
+    data = data + rng.normal(0, sigma[0, 0], data.shape)
+    chi2, grad = _gpu_grads([(psf, profiles)], [data], [sigma], use_double)
+    chi2_ref, counts0 = _chi2(O, psf, profiles, data, sigma)
+    assert abs(chi2[0] - chi2_ref) <= (1e-10 if use_double else 1e-4) * chi2_ref
+    rtol, floor = (1e-4, 1e-9) if use_double else (1e-3, 1e-6)
+    checked = 0
+    for k, slot in (("xcen", 0), ("mag", 2), ("axrat", 4), ("re", 6), ("nser", 7)):
+        v = profiles[0][1][k]
+        h = 1e-6 * max(abs(v), 1e-3)
+        cp, c_p = _chi2(O, psf, _with(profiles, 0, k, v + h), data, sigma)
+        cm, c_m = _chi2(O, psf, _with(profiles, 0, k, v - h), data, sigma)
+        if not (np.array_equal(c_p, counts0) and np.array_equal(c_m, counts0)):
+            continue
+        want = (cp - cm) / (2 * h)
+        got = grad[0, slot]
+        assert abs(got - want) <= rtol * abs(want) + floor * chi2_ref / h, "%s: adjoint %.8g vs fd %.8g" % (k, got, want)
+        checked += 1
+    assert checked >= 4
