@@ -357,24 +357,29 @@ __global__ void convolve64_kernel(const double *__restrict__ src, unsigned int w
 	}
 }
 
+// fft_fine 0: every model on the direct convolution (the FFT's last pass
+// writes the others); 1: the SUM-downsampled FFT models, whose fine pixels
+// that pass left in conv_img at their drawing positions.
 __global__ void finish64_kernel(const ModelDev *__restrict__ models, int n_models, const double *__restrict__ psf_pool,
                                 const double *__restrict__ conv_img, const double *__restrict__ direct_img,
-                                double *__restrict__ out, long long total_out)
+                                double *__restrict__ out, long long total_out, int fft_fine)
 {
 	for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total_out;
 	     g += (long long)gridDim.x * blockDim.x) {
 		const int mi = find_model_out(models, n_models, g);
 		const ModelDev &m = models[mi];
-		if (m.use_fft) continue;  // written by the FFT convolution's last pass
+		const bool downsample = m.fs > 1 && !m.return_fs;
+		if (fft_fine ? !(m.use_fft && downsample) : (bool)m.use_fft) continue;
 		const long long local = g - m.out_off;
 		const unsigned int ox = (unsigned int)(local % m.out_w), oy = (unsigned int)(local / m.out_w);
 		const double *psf = m.psf_off >= 0 ? psf_pool + m.psf_off : nullptr;
 		double v;
-		if (m.fs > 1 && !m.return_fs) {
+		if (downsample) {
 			v = 0;
 			for (unsigned int r = oy * m.fs; r < min((oy + 1) * m.fs, m.crop_h); r++) {
 				for (unsigned int c = ox * m.fs; c < min((ox + 1) * m.fs, m.crop_w); c++) {
-					v += drawn_pixel64(m, psf, conv_img, direct_img, c + m.pad_x, r + m.pad_y);
+					v += fft_fine ? conv_img[m.draw_off + (size_t)(r + m.pad_y) * m.draw_w + c + m.pad_x]
+					              : drawn_pixel64(m, psf, conv_img, direct_img, c + m.pad_x, r + m.pad_y);
 				}
 			}
 		}
@@ -409,13 +414,15 @@ void launch_convolve64(const double *src, unsigned int w, unsigned int h, const 
 }
 
 void launch_finish64(const ModelDev *models, int n_models, const double *psf_pool, const double *conv_img,
-                     const double *direct_img, double *out, long long total_out, int n_sm, cudaStream_t stream)
+                     const double *direct_img, double *out, long long total_out, int fft_fine, int n_sm,
+                     cudaStream_t stream)
 {
 	int threads = 256;
 	long long need = (total_out + threads - 1) / threads;
 	int blocks = (int)(need < (long long)n_sm * 16 ? need : (long long)n_sm * 16);
 	if (blocks < 1) blocks = 1;
-	finish64_kernel<<<blocks, threads, 0, stream>>>(models, n_models, psf_pool, conv_img, direct_img, out, total_out);
+	finish64_kernel<<<blocks, threads, 0, stream>>>(models, n_models, psf_pool, conv_img, direct_img, out, total_out,
+	                                                fft_fine);
 }
 
 }  // namespace pf

@@ -16,7 +16,9 @@
 //                     kept (in place);
 //   pass 3 (rows):    each kept row, Hermitian-completed, inverse FFT, the
 //                     crop's columns scaled by 1/(M_x M_y), plus the direct
-//                     image, written to the output (SUM-downsampled if asked).
+//                     image, written to the output (SUM-downsampled if asked:
+//                     the fine pixels are left in the source buffer and summed
+//                     in the reference's order by a last finishing pass).
 // The PSF spectrum is made once per batch by passes 1-2 without the product.
 // Every transform is a radix-2 Stockham FFT in shared memory (natural-order
 // output, ping-pong buffers), several transforms per block when they are
@@ -182,11 +184,15 @@ __global__ void fft_cols_kernel(const ModelDev *__restrict__ models, const FftJo
 	}
 }
 
-// pass 3: kept rows, inverse, crop, scale, plus the direct image
+// pass 3: kept rows, inverse, crop, scale, plus the direct image. A model
+// SUM-downsampled: with `fine` given, each fine pixel's value is stored there
+// at its drawing position, and the downsampling sums them afterwards in the
+// reference's order (finish64_kernel); without, added to its output pixel.
 template <typename T>
 __global__ void fft_irows_kernel(const ModelDev *__restrict__ models, const FftJob *__restrict__ jobs,
                                  const typename Cx<T>::t *__restrict__ work, const T *__restrict__ direct,
-                                 T *__restrict__ out, const typename Cx<T>::t *__restrict__ tw, int nmax)
+                                 T *__restrict__ out, T *__restrict__ fine, const typename Cx<T>::t *__restrict__ tw,
+                                 int nmax)
 {
 	using C = typename Cx<T>::t;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -220,7 +226,10 @@ __global__ void fft_irows_kernel(const ModelDev *__restrict__ models, const FftJ
 		// the convolution zero where the calculation mask is; the model's mask at the end
 		const T conv = evaluated(m, c + (int)m.pad_x, r + (int)m.pad_y) ? res[t * n + c + off_x].x * scale : (T)0;
 		const T v = direct[m.draw_off + (size_t)(r + m.pad_y) * m.draw_w + c + m.pad_x] + conv;
-		if (downsample) {
+		if (downsample && fine) {
+			fine[m.draw_off + (size_t)(r + m.pad_y) * m.draw_w + c + m.pad_x] = v;
+		}
+		else if (downsample) {
 			if (kept(m, c / (int)m.fs, r / (int)m.fs)) atomicAdd(&out[m.out_off + (size_t)(r / m.fs) * m.out_w + c / m.fs], v);
 		}
 		else out[m.out_off + (size_t)r * m.out_w + c] = kept(m, c, r) ? v : (T)0;
@@ -269,7 +278,7 @@ void launch_twiddles(void *tw, int nmax, cudaStream_t stream)
 // spectrum), 4 columns (PSF spectrum)
 template <typename T>
 void launch_fft_pass(int pass, const ModelDev *models, const void *jobs, int n_jobs, const T *src, const T *psf,
-                     void *work, void *spec, const T *direct, T *out, const void *tw, int nmax, size_t smem,
+                     void *work, void *spec, const T *direct, T *out, T *fine, const void *tw, int nmax, size_t smem,
                      cudaStream_t stream)
 {
 	using C = typename Cx<T>::t;
@@ -284,8 +293,8 @@ void launch_fft_pass(int pass, const ModelDev *models, const void *jobs, int n_j
 		fft_cols_kernel<T><<<n_jobs, threads, smem, stream>>>(models, j, (C *)work, (C *)spec, (const C *)tw, nmax, 0);
 		break;
 	case 2:
-		fft_irows_kernel<T><<<n_jobs, threads, smem, stream>>>(models, j, (const C *)work, direct, out, (const C *)tw,
-		                                                        nmax);
+		fft_irows_kernel<T><<<n_jobs, threads, smem, stream>>>(models, j, (const C *)work, direct, out, fine,
+		                                                        (const C *)tw, nmax);
 		break;
 	case 3:
 		fft_rows_kernel<T><<<n_jobs, threads, smem, stream>>>(models, j, src, psf, (C *)spec, (const C *)tw, nmax, 1);
@@ -303,9 +312,10 @@ template cudaError_t fft_configure<double>(size_t);
 template void launch_twiddles<float>(void *, int, cudaStream_t);
 template void launch_twiddles<double>(void *, int, cudaStream_t);
 template void launch_fft_pass<float>(int, const ModelDev *, const void *, int, const float *, const float *, void *,
-                                     void *, const float *, float *, const void *, int, size_t, cudaStream_t);
+                                     void *, const float *, float *, float *, const void *, int, size_t,
+                                     cudaStream_t);
 template void launch_fft_pass<double>(int, const ModelDev *, const void *, int, const double *, const double *,
-                                      void *, void *, const double *, double *, const void *, int, size_t,
+                                      void *, void *, const double *, double *, double *, const void *, int, size_t,
                                       cudaStream_t);
 
 }  // namespace pf

@@ -29,7 +29,8 @@ void launch_eval64(const ModelDev *models, int n_models, const ProfileDev *profs
                    double *conv_img, double *direct_img, long long n_tiles, unsigned int *tile_counter,
                    DebugRec dbg, int n_sm, cudaStream_t stream);
 void launch_finish64(const ModelDev *models, int n_models, const double *psf_pool, const double *conv_img,
-                     const double *direct_img, double *out, long long total_out, int n_sm, cudaStream_t stream);
+                     const double *direct_img, double *out, long long total_out, int fft_fine, int n_sm,
+                     cudaStream_t stream);
 void launch_convolve64(const double *src, unsigned int w, unsigned int h, const double *krn, unsigned int kw,
                        unsigned int kh, const uint8_t *mask, double *out, int n_sm, cudaStream_t stream);
 void launch_flux_sum(const ModelDev *models, int n_models, const void *images, int is_double, double *flux,
@@ -70,7 +71,7 @@ template <typename T>
 void launch_twiddles(void *tw, int nmax, cudaStream_t stream);
 template <typename T>
 void launch_fft_pass(int pass, const ModelDev *models, const void *jobs, int n_jobs, const T *src, const T *psf,
-                     void *work, void *spec, const T *direct, T *out, const void *tw, int nmax, size_t smem,
+                     void *work, void *spec, const T *direct, T *out, T *fine, const void *tw, int nmax, size_t smem,
                      cudaStream_t stream);
 template <typename T>
 void launch_chi2(const ModelDev *models, int n_models, const void *img, const void *data, const void *sigma,
@@ -343,6 +344,7 @@ struct pf_batch {
 	long long n_out_tiles = 0;
 	size_t finish_smem = 0;
 	bool any_downsample = false;
+	bool any_fft_downsample = false;    // FP64: an FFT model SUM-downsampled (one more finishing pass)
 	int fwd_shape = 0, adj_shape = 0;  // convolution block shapes (conv.cu)
 	// FFT convolution
 	bool any_fft = false;
@@ -607,10 +609,6 @@ pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5], const double *p
 		const unsigned int my = std::max(nmin, next_pow2(d.crop_h + d.psf_h));
 		bool fft = false;
 		if (d.convolver == PF_CONV_FFT) {
-			if (b->dbl && d.fs > 1 && !d.return_fs) {
-				return fail(PF_ERR_UNSUPPORTED, "model " + std::to_string(i) +
-				                                    ": FFT convolution with SUM downsampling needs the single-precision path");
-			}
 			if ((int)mx > nmax || (int)my > nmax) {
 				return fail(PF_ERR_UNSUPPORTED, "model " + std::to_string(i) + ": FFT size above " +
 				                                    std::to_string(nmax) + " in this precision");
@@ -631,6 +629,7 @@ pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5], const double *p
 		}
 		if (!fft) continue;
 		d.use_fft = 1;
+		if (b->dbl && d.fs > 1 && !d.return_fs) b->any_fft_downsample = true;
 		d.fft_mx = mx;
 		d.fft_my = my;
 		const int64_t nb = mx / 2 + 1;
@@ -961,8 +960,8 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 			pf::launch_twiddles<double>(b->d_fft_tw, b->fft_nmax, env->stream);
 			for (int p = 3; p <= 4; p++) {
 				pf::launch_fft_pass<double>(p, b->d_models, b->d_fft_jobs[p], b->fft_njobs[p], nullptr, b->d_psf_norm,
-				                            b->d_fft_work, b->d_fft_spec, nullptr, nullptr, b->d_fft_tw, b->fft_nmax,
-				                            b->fft_smem_bytes, env->stream);
+				                            b->d_fft_work, b->d_fft_spec, nullptr, nullptr, nullptr, b->d_fft_tw,
+				                            b->fft_nmax, b->fft_smem_bytes, env->stream);
 			}
 		}
 		else {
@@ -1319,12 +1318,19 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 		stage_end(b, t, stream);
 		t = stage_begin(b, ST_FINISH, stream);
 		pf::launch_finish64(b->d_models, n_models, b->d_psf_norm, (const double *)b->d_conv,
-		                    (const double *)b->d_direct, (double *)images_dev, (long long)b->total_out,
+		                    (const double *)b->d_direct, (double *)images_dev, (long long)b->total_out, 0,
 		                    b->env->n_sm, stream);
 		for (int p = 0; b->any_fft && p <= 2; p++) {
 			pf::launch_fft_pass<double>(p, b->d_models, b->d_fft_jobs[p], b->fft_njobs[p], (const double *)b->d_conv,
 			                            nullptr, b->d_fft_work, b->d_fft_spec, (const double *)b->d_direct,
-			                            (double *)images_dev, b->d_fft_tw, b->fft_nmax, b->fft_smem_bytes, stream);
+			                            (double *)images_dev, (double *)b->d_conv, b->d_fft_tw, b->fft_nmax,
+			                            b->fft_smem_bytes, stream);
+		}
+		if (b->any_fft_downsample) {
+			// the SUM downsampling of the FFT models' fine pixels, in the reference's order
+			pf::launch_finish64(b->d_models, n_models, b->d_psf_norm, (const double *)b->d_conv,
+			                    (const double *)b->d_direct, (double *)images_dev, (long long)b->total_out, 1,
+			                    b->env->n_sm, stream);
 		}
 		stage_end(b, t, stream);
 	}
@@ -1355,7 +1361,7 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 	b->forward_calls++;
 	{
 		uint64_t k = (n_profiles > 0 ? 2 : 1) + 1;  // setup (solves, profiles), evaluation
-		if (b->dbl) k += 1 + (b->any_fft ? 3 : 0);   // finish, FFT passes
+		if (b->dbl) k += 1 + (b->any_fft ? 3 : 0) + (b->any_fft_downsample ? 1 : 0);  // finish, FFT passes
 		else {
 			k += b->n_out_tiles > 0 ? 1 : 0;
 			for (int pass = 0; b->any_fft && pass < 3; pass++) k += b->f32_jobs[0][pass].size();

@@ -48,8 +48,6 @@ def _check(img, ref, abs_tol, rel_tol, floor=1e-3):
 def test_fft_fp64_matches_reference(envs, name):
     env64, _ = envs
     entry = GOLDEN[name]
-    if entry["spec"].get("finesampling", 1) > 1 and not entry["spec"].get("return_finesampled", True):
-        pytest.skip("SUM downsampling with FFT runs in the single-precision path")
     m = product_model(entry["spec"], entry["psf"], env64)
     m.set_convolver("fft")
     _check(m.evaluate(), entry["image"], 1e-12, 1e-10)
