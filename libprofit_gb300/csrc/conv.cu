@@ -112,12 +112,8 @@ __device__ __forceinline__ void conv_rows(const T *srow, const T *s_k, int s, in
 #ifndef PF_CONV_REGS
 #define PF_CONV_REGS 0
 #endif
-__host__ __device__ constexpr int conv_min_blocks(int threads)
-{
-	return PF_CONV_REGS > 0 ? 65536 / (threads * PF_CONV_REGS) : 1;
-}
-
 #if PF_CONV_REGS > 0
+__host__ __device__ constexpr int conv_min_blocks(int threads) { return 65536 / (threads * PF_CONV_REGS); }
 #define PF_CONV_BOUNDS(threads) __launch_bounds__(threads, conv_min_blocks(threads))
 #else
 #define PF_CONV_BOUNDS(threads) __launch_bounds__(threads)
