@@ -186,7 +186,8 @@ PF_API void pf_env_destroy(pf_env *env);
  * validates like analyze_inputs, draws every profile into the padded drawing
  * area, convolves the profiles with convolve=1 by the model's PSF, adds,
  * crops the PSF padding, optionally downsamples. `image` receives
- * out_w * out_h doubles (query the size with pf_model_output_dims).
+ * out_w * out_h doubles (query the size with pf_model_output_dims, which
+ * also checks a mask's declared dimensions: mask_offset >= 0, mask_w x mask_h).
  */
 PF_API pf_status pf_model_output_dims(const pf_model_desc *model, const pf_profile_desc *profiles,
                                uint32_t *out_w, uint32_t *out_h);

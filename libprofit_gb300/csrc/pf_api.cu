@@ -183,10 +183,13 @@ struct Geometry {
 };
 
 // Model::analyze_inputs + analyze_expansion_requirements (src/model.cpp:152-219);
-// `mask` the model's calculation mask or null
+// `mask` the model's calculation mask or null; `mask_declared`: a mask of the
+// descriptor's mask_w x mask_h is set even if its bytes are not given (its
+// dimension checks and, used as given, its padding rule need only those)
 pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles, Geometry &g,
-                         const uint8_t *mask = nullptr)
+                         const uint8_t *mask = nullptr, bool mask_declared = false)
 {
+	const bool has_mask = mask != nullptr || mask_declared;
 	if (m.width == 0 || m.height == 0) return fail(PF_ERR_INVALID_PARAMETER, "Model's requested dimensions are 0");
 	if (m.scale_x <= 0) return fail(PF_ERR_INVALID_PARAMETER, "Model's scale_x cannot be negative or zero");
 	if (m.scale_y <= 0) return fail(PF_ERR_INVALID_PARAMETER, "Model's scale_y cannot be negative or zero");
@@ -209,7 +212,7 @@ pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles
 		if (s != PF_OK) return s;
 	}
 	// src/model.cpp:198-201
-	if (mask && m.adjust_mask && (m.mask_w != m.width || m.mask_h != m.height)) {
+	if (has_mask && m.adjust_mask && (m.mask_w != m.width || m.mask_h != m.height)) {
 		return fail(PF_ERR_INVALID_PARAMETER, "Mask dimensions != model dimensions");
 	}
 	// the PSF padding: with a mask used as given, when the mask is larger than
@@ -217,7 +220,7 @@ pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles
 	// adjustable one, only when its bounding box (times the finesampling)
 	// comes closer than half the PSF to an edge (src/model.cpp:152-184)
 	bool padding = g.conv;
-	if (mask && !m.adjust_mask) {
+	if (has_mask && !m.adjust_mask) {
 		padding = m.mask_w > m.width * m.finesampling && m.mask_h > m.height * m.finesampling;
 	}
 	else if (mask && g.conv) {
@@ -255,7 +258,7 @@ pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles
 		g.out_h = (g.crop_h + m.finesampling - 1) / m.finesampling;
 	}
 	// src/model.cpp:277-283
-	if (mask && !m.adjust_mask && (m.mask_w != g.draw_w || m.mask_h != g.draw_h)) {
+	if (has_mask && !m.adjust_mask && (m.mask_w != g.draw_w || m.mask_h != g.draw_h)) {
 		return fail(PF_ERR_INVALID_PARAMETER, "Mask dimensions != drawing dimensions: [" + std::to_string(m.mask_w) +
 		                                          ", " + std::to_string(m.mask_h) + "] != [" +
 		                                          std::to_string(g.draw_w) + ", " + std::to_string(g.draw_h) + "]");
@@ -489,7 +492,7 @@ pf_status pf_model_output_dims(const pf_model_desc *model, const pf_profile_desc
 	pf_model_desc m = *model;
 	m.first_profile = 0;
 	Geometry g;
-	pf_status s = model_geometry(m, profiles, g);
+	pf_status s = model_geometry(m, profiles, g, nullptr, m.mask_offset >= 0 && m.mask_w > 0 && m.mask_h > 0);
 	if (s != PF_OK) return s;
 	if (out_w) *out_w = g.out_w;
 	if (out_h) *out_h = g.out_h;

@@ -1,0 +1,84 @@
+"""Parameter validation and model checks on the host (no GPU needed).
+
+pf_model_output_dims runs the same validation as Model::evaluate (the
+profiles' validate() methods, src/*.cpp, and analyze_inputs,
+src/model.cpp:186-219) before any device work. Every invalid case must raise
+InvalidParameter with the message the oracle restatement gives and, when the
+reference compiled here (oracle/_ref), the message the reference itself
+throws.
+"""
+import os
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+CASES = [
+    ("sersic", dict(axrat=0.0), "axrat <= 0, must have axrat > 0"),
+    ("sersic", dict(axrat=1.5), "axrat > 1, must have axrat <= 1"),
+    ("moffat", dict(box=-2.0), "box <= -2, must have box > -2"),
+    ("sersic", dict(re=0.0), "re <= 0, must have re > 0"),
+    ("sersic", dict(nser=-1.0), "nser <= 0, must have nser > 0"),
+    ("coresersic", dict(rb=0.0), "rb <= 0, must have rb > 0"),
+    ("coresersic", dict(a=0.0), "a <= 0, must have a > 0"),
+    ("coresersic", dict(b=2.5), "b > 1.999, must have b < 1.999"),
+    ("moffat", dict(fwhm=0.0), "fwhm <= 0, must have fwhm > 0"),
+    ("moffat", dict(con=-0.5), "con < 0, must have con >= 0"),
+    ("ferrer", dict(rout=0.0), "rout <= 0, must have rout >= 0"),
+    ("ferrer", dict(a=-1.0), "a < 0, must have a >= 0"),
+    ("ferrer", dict(b=2.5), "b > 2, must have b <= 2"),
+    ("king", dict(rc=0.0), "rc <= 0, must have rc > 0"),
+    ("king", dict(rt=-1.0), "rt <= 0, must have rt > 0"),
+    ("king", dict(a=-1.0), "a < 0, must have a >=0"),
+    ("brokenexp", dict(h1=0.0), "h1 <= 0, must have h1 > 0"),
+    ("brokenexp", dict(h2=0.0), "h2 <= 0, must have h2 > 0"),
+    ("brokenexp", dict(rb=0.0), "rb <= 0, must have rb > 0"),
+]
+
+
+def _gpu_message(width, height, profiles, psf=None, mask=None, adjust_mask=True):
+    import libprofit_gb300 as pg
+    m = pg.Model(width, height)
+    if psf is not None:
+        m.set_psf(psf)
+    if mask is not None:
+        m.set_mask(mask)
+        m.set_adjust_mask(adjust_mask)
+    for kind, params in profiles:
+        p = m.add_profile(kind)
+        for k, v in params.items():
+            p.parameter(k, bool(v) if k == "convolve" else float(v))
+    with pytest.raises(pg.InvalidParameter) as e:
+        m.output_dims()
+    return str(e.value)
+
+
+def _ref_available():
+    return os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libprofit_ref.so"))
+
+
+@pytest.mark.parametrize("kind,params,msg", CASES, ids=["%s-%s" % (c[0], list(c[1])[0]) for c in CASES])
+def test_profile_validation_messages(oracle_lib, kind, params, msg):
+    O = oracle_lib
+    got = _gpu_message(10, 10, [(kind, params)])
+    assert got == msg
+    with pytest.raises(O.OracleError) as e:
+        O.evaluate(O.Case(10, 10, [(kind, params)]))
+    assert str(e.value) == msg
+    if _ref_available():
+        with pytest.raises(O.OracleError) as e:
+            O.evaluate_reference(O.Case(10, 10, [(kind, params)]))
+        assert str(e.value) == msg
+
+
+def test_model_checks(oracle_lib):
+    O = oracle_lib
+    assert _gpu_message(0, 10, [("sersic", {})]) == "Model's requested dimensions are 0"
+    assert _gpu_message(10, 10, [("sersic", dict(convolve=True))]) == \
+        "No psf provided but profile(s) requested convolution"
+    assert _gpu_message(10, 10, [("psf", {})]) == "No psf present in the model, cannot produce a psf profile"
+    mask = np.ones((9, 10), np.uint8)
+    assert _gpu_message(10, 10, [("sersic", {})], mask=mask) == "Mask dimensions != model dimensions"
+    with pytest.raises(O.OracleError, match="Mask dimensions != model dimensions"):
+        O.evaluate(O.Case(10, 10, [("sersic", {})], mask=mask))
