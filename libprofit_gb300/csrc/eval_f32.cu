@@ -45,6 +45,11 @@ namespace {
 #ifndef PF_EVAL_RING_CHUNK
 #define PF_EVAL_RING_CHUNK 32
 #endif
+// phase-B tiles a warp claims at once (a divisor of 32; 8 and 2 measured no
+// better on the 1024-model step or the 4096 uneven models)
+#ifndef PF_EVAL_TILE_CHUNK
+#define PF_EVAL_TILE_CHUNK 32
+#endif
 constexpr int kWarps32 = PF_EVAL32_WARPS;
 // Half-width of the band around a threshold inside which an FP32 comparison is
 // re-taken in FP64. The FP32 profile values carry at most ~3e-6 relative
@@ -479,7 +484,8 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 	while (true) {
 		unsigned int chunk = 0;
 		if (lane == 0) {
-			chunk = atomicAdd(&counter[ring ? 0 : 1], ring ? (unsigned int)PF_EVAL_RING_CHUNK : 32u);
+			chunk = atomicAdd(&counter[ring ? 0 : 1],
+			                  ring ? (unsigned int)PF_EVAL_RING_CHUNK : (unsigned int)PF_EVAL_TILE_CHUNK);
 		}
 		chunk = __shfl_sync(0xffffffffu, chunk, 0);
 		if (ring && chunk >= n_ring_items) {
@@ -490,13 +496,15 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 		long long tile = -1;
 		unsigned int todo;
 		if (!ring) {
-			// phase B: 32 consecutive tiles, one claim word
+			// phase B: PF_EVAL_TILE_CHUNK consecutive tiles, within one claim word
 			const unsigned int t0 = chunk;
 			const unsigned int left = n_tiles - t0;
-			const unsigned int valid = left >= 32 ? 0xffffffffu : (1u << left) - 1u;
+			const unsigned int n = left < (unsigned int)PF_EVAL_TILE_CHUNK ? left : (unsigned int)PF_EVAL_TILE_CHUNK;
+			const unsigned int sh = t0 & 31;
+			const unsigned int bits = n >= 32 ? 0xffffffffu : ((1u << n) - 1u) << sh;
 			unsigned int old = 0;
-			if (lane == 0) old = atomicOr(&claims[t0 >> 5], valid);
-			todo = valid & ~__shfl_sync(0xffffffffu, old, 0);
+			if (lane == 0) old = atomicOr(&claims[t0 >> 5], bits);
+			todo = (bits & ~__shfl_sync(0xffffffffu, old, 0)) >> sh;
 			tile = (long long)t0 + lane;
 		}
 		else {
