@@ -61,16 +61,23 @@ def parse():
     return ap.parse_args()
 
 
-def dist_init(args):
+def dist_init(args, backend=None):
+    """One process per GPU (torchrun's RANK / LOCAL_RANK / WORLD_SIZE): the
+    ranks render independent replicas of the workload; the process group only
+    carries the timing barrier and the max over ranks (NCCL on GPUs, gloo
+    without). The reference arm, CPU only, starts none: rank 0 alone works."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
+    if world > 1 and getattr(args, "impl", "ours") != "reference":
         import torch
         import torch.distributed as dist
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend is None:
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     return world, rank, local
 
 
@@ -85,7 +92,8 @@ def max_over_ranks(world, value):
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    on_gpu = dist.get_backend() == "nccl"
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if on_gpu else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -676,7 +684,7 @@ def main():
         run_workload(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
-    if world > 1:
+    if world > 1 and args.impl != "reference":
         import torch.distributed as dist
         dist.destroy_process_group()
 
