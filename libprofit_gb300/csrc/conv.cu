@@ -83,14 +83,15 @@ __device__ __forceinline__ T cot_at(const ModelDev &m, const T *gout, int x, int
 }
 
 // The multiply-adds of one source row (srow, this thread's 4 + 4 columns) into
-// output rows r0..r1 (kernel row s - r); with r0 and r1 known at compile time
-// after unrolling, the row loop carries no tests.
+// output rows r0..r1 (kernel row s - r), over the kw4 = 4 floor(kw / 4) taps
+// of whole groups of four; with r0 and r1 known at compile time after
+// unrolling, the row loop carries no tests.
 template <typename T, int R>
-__device__ __forceinline__ void conv_rows(const T *srow, const T *s_k, int s, int kwp, int r0, int r1,
+__device__ __forceinline__ void conv_rows(const T *srow, const T *s_k, int s, int kwp, int kw4, int r0, int r1,
                                           T (&acc)[R][4])
 {
 	using V4 = typename Vec4<T>::type;
-	for (int kb = 0; kb < kwp; kb += 4) {
+	for (int kb = 0; kb < kw4; kb += 4) {
 		const V4 w0 = *reinterpret_cast<const V4 *>(srow + kb);
 		const V4 w1 = *reinterpret_cast<const V4 *>(srow + kb + 4);
 		const T w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
@@ -103,6 +104,31 @@ __device__ __forceinline__ void conv_rows(const T *srow, const T *s_k, int s, in
 			for (int c = 0; c < 4; c++)
 #pragma unroll
 				for (int q = 0; q < 4; q++) acc[r][c] = fma(w[c + q], kv[q], acc[r][c]);
+		}
+	}
+}
+
+// The kw mod 4 taps past kw4 (tail of them), one by one, in a pass of their
+// own after every source row's whole groups: fewer multiply-adds than a
+// zero-padded group (measured 2.75 -> 2.68 ms for the adjoint of 1024 models
+// of 280 x 280 with a 25 x 25 PSF, the forward unchanged).
+template <typename T, int R>
+__device__ __forceinline__ void conv_tail(const T *srow, const T *s_k, int s, int kwp, int kw4, int tail, int r0,
+                                          int r1, T (&acc)[R][4])
+{
+	using V4 = typename Vec4<T>::type;
+	const V4 w0 = *reinterpret_cast<const V4 *>(srow + kw4);
+	const V4 w1 = *reinterpret_cast<const V4 *>(srow + kw4 + 4);
+	const T w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+	for (int q = 0; q < 3; q++) {
+		if (q >= tail) break;
+#pragma unroll
+		for (int r = 0; r < R; r++) {
+			if (r < r0 || r > r1) continue;
+			const T kv = s_k[(s - r) * kwp + kw4 + q];
+#pragma unroll
+			for (int c = 0; c < 4; c++) acc[r][c] = fma(w[c + q], kv, acc[r][c]);
 		}
 	}
 }
@@ -196,22 +222,32 @@ conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restri
 			}
 			__syncthreads();
 			const int xb = tx * 4, yb = ty * R;
+			const int kw4 = kw & ~3, tail = kw & 3;
 			if (kh >= R) {
 				// source row s feeds output rows r with kernel row l = s - r in
 				// [0, kh): rows 0..s while s < R - 1, all rows up to s = kh - 1,
 				// rows s - kh + 1 .. R - 1 after; the ramps are unrolled so that no
 				// row test is left in the multiply-add stream
 #pragma unroll
-				for (int s0 = 0; s0 < R - 1; s0++) conv_rows<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, 0, s0, acc);
-				for (int s0 = R - 1; s0 < kh; s0++) conv_rows<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, 0, R - 1, acc);
+				for (int s0 = 0; s0 < R - 1; s0++)
+					conv_rows<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, kw4, 0, s0, acc);
+				for (int s0 = R - 1; s0 < kh; s0++)
+					conv_rows<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, kw4, 0, R - 1, acc);
 #pragma unroll
 				for (int d = 0; d < R - 1; d++) {
-					conv_rows<T, R>(s_src + (yb + kh + d) * pw + xb, s_k, kh + d, kwp, d + 1, R - 1, acc);
+					conv_rows<T, R>(s_src + (yb + kh + d) * pw + xb, s_k, kh + d, kwp, kw4, d + 1, R - 1, acc);
 				}
 			}
 			else {
 				for (int s0 = 0; s0 < R + kh - 1; s0++) {
-					conv_rows<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, max(0, s0 - kh + 1), min(R - 1, s0), acc);
+					conv_rows<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, kw4, max(0, s0 - kh + 1),
+					                min(R - 1, s0), acc);
+				}
+			}
+			if (tail) {
+				for (int s0 = 0; s0 < R + kh - 1; s0++) {
+					conv_tail<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, kw4, tail, max(0, s0 - kh + 1),
+					                min(R - 1, s0), acc);
 				}
 			}
 			__syncthreads();
