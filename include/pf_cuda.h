@@ -52,7 +52,8 @@ typedef enum pf_status {
 	PF_ERR_NO_MEMORY = 4,
 	PF_ERR_DEVICE_LIMIT = 5,      /* a bounded device-side resource was exceeded */
 	PF_ERR_UNSUPPORTED = 6,
-	PF_ERR_INTERNAL = 7
+	PF_ERR_INTERNAL = 7,
+	PF_ERR_INVALID_FILE = 8       /* profit::invalid_file */
 } pf_status;
 
 /* Profile kinds, by the names Model::add_profile accepts (src/model.cpp:103-135). */
@@ -345,6 +346,31 @@ PF_API pf_status pf_batch_drawing_dims(pf_batch *batch, uint32_t *dims);
  * by the autotuner, or requested). Any pointer may be NULL. */
 PF_API pf_status pf_batch_conv_info(const pf_batch *batch, int32_t *forward_shape, int32_t *adjoint_shape,
                                     uint32_t *fft_models);
+
+/* FITS images on either side of the path (host only, no device work): the
+ * PSFs a caller reads in and the images it writes out.
+ *
+ * pf_fits_write is profit::to_fits (src/fits_utils.cpp:150-205): a primary
+ * HDU of BITPIX -64, NAXIS 2 (NAXIS1 = width), the pixel scale as CDELT1/2 and
+ * the origin's offset (whole pixels, the reference's unsigned Point,
+ * include/profit/image.h:47-61) as CRVAL1/2 = (0.5 - offset) * scale, big-endian
+ * doubles in row-major order, header and data each padded after their end
+ * to the 2880-byte block (a whole block when they already end on one), and
+ * ".fits" appended to `filename` unless it ends in it. The bytes written are
+ * the reference's.
+ *
+ * pf_fits_read is profit::from_fits (src/fits_utils.cpp:60-126): 80-byte
+ * header cards up to END, NAXIS1/NAXIS2/CDELT1/CDELT2 taken when present
+ * (scale 1 by default), BITPIX taken to be -64, the data starting at the
+ * 2880-byte block after END's card (a whole block further when END ends on
+ * one, as the reference reads). With `image` NULL only the dimensions and
+ * scale are reported; otherwise `image_len` must hold width * height.
+ * A file that cannot be opened or read returns PF_ERR_INVALID_FILE with the
+ * reference's messages (and a failed write with its own). */
+PF_API pf_status pf_fits_write(const char *filename, const double *image, uint32_t width, uint32_t height,
+                               uint32_t offset_x, uint32_t offset_y, double scale_x, double scale_y);
+PF_API pf_status pf_fits_read(const char *filename, double *image, size_t image_len, uint32_t *width,
+                              uint32_t *height, double *scale_x, double *scale_y);
 
 #ifdef __cplusplus
 }

@@ -11,9 +11,11 @@
  *   Model::set_opencl_env         -> Model::set_cuda_env      (include/profit/model.h:305-311)
  *   create_convolver(type, prefs) -> create_convolver("cuda") (src/convolve.cpp:521-584)
  *   Convolver::convolve           -> Convolver::convolve      (include/profit/convolve.h:98-99)
- *   invalid_parameter, unknown_parameter, opencl_error
- *                                 -> invalid_parameter, unknown_parameter, cuda_error
- *                                    (include/profit/exceptions.h:41-104)
+ *   from_fits, to_fits            -> from_fits, to_fits       (src/fits_utils.cpp:60-205)
+ *   invalid_parameter, unknown_parameter, opencl_error, invalid_file
+ *                                 -> invalid_parameter, unknown_parameter, cuda_error, invalid_file
+ *                                    (include/profit/exceptions.h:41-104,
+ *                                    include/profit/fits_utils.h:34-43)
  * Parameter names, types, defaults and validation messages are the
  * reference's; errors become exceptions of the same categories.
  */
@@ -58,6 +60,11 @@ public:
 	explicit cuda_error(const std::string &what) : exception(what) {}
 };
 
+class invalid_file : public exception {
+public:
+	explicit invalid_file(const std::string &what) : exception(what) {}
+};
+
 inline void check(pf_status s)
 {
 	if (s == PF_OK) return;
@@ -65,6 +72,7 @@ inline void check(pf_status s)
 	if (s == PF_ERR_INVALID_PARAMETER) throw invalid_parameter(msg);
 	if (s == PF_ERR_UNKNOWN_PARAMETER) throw unknown_parameter(msg);
 	if (s == PF_ERR_CUDA || s == PF_ERR_NO_MEMORY) throw cuda_error(msg);
+	if (s == PF_ERR_INVALID_FILE) throw invalid_file(msg);
 	throw exception(msg);
 }
 
@@ -406,6 +414,33 @@ inline ConvolverPtr create_convolver(const std::string &type, CUDAEnvPtr env = n
 {
 	if (type != "cuda") throw invalid_parameter("Unsupported convolver type: " + type);
 	return std::make_shared<Convolver>(env ? env : get_cuda_environment(0, true));
+}
+
+/* The reference's Point (whole pixels) and PixelScale (include/profit/image.h:47-61, 823). */
+typedef std::pair<double, double> PixelScale;
+struct Point {
+	unsigned int x = 0, y = 0;
+};
+
+/* profit::from_fits (src/fits_utils.cpp:60-126): the image of a FITS file and
+ * its pixel scale (CDELT1, CDELT2). */
+inline Image from_fits(const std::string &filename, PixelScale &pixel_scale)
+{
+	uint32_t w = 0, h = 0;
+	double sx = 1, sy = 1;
+	check(pf_fits_read(filename.c_str(), nullptr, 0, &w, &h, &sx, &sy));
+	Image img(w, h);
+	check(pf_fits_read(filename.c_str(), img.data(), img.size(), &w, &h, &sx, &sy));
+	pixel_scale = {sx, sy};
+	return img;
+}
+
+/* profit::to_fits (src/fits_utils.cpp:150-205): ".fits" is appended to the
+ * name unless it ends in it. */
+inline void to_fits(const Image &image, const Point &offset, const PixelScale &pixel_scale, std::string fname)
+{
+	check(pf_fits_write(fname.c_str(), image.data(), image.getWidth(), image.getHeight(), offset.x, offset.y,
+	                    pixel_scale.first, pixel_scale.second));
 }
 
 }  // namespace profit_cuda

@@ -17,6 +17,7 @@ Everything computes on the GPU through the C ABI of include/pf_cuda.h
 (libpfcuda.so); Batch exposes the batched path (many models per launch).
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -24,7 +25,8 @@ from . import _ffi
 from ._ffi import KINDS, NPAR
 
 __all__ = ["Model", "Profile", "CUDAEnv", "get_cuda_environment", "create_convolver", "Batch",
-           "ProfitError", "InvalidParameter", "UnknownParameter", "CudaError", "version"]
+           "from_fits", "to_fits",
+           "ProfitError", "InvalidParameter", "UnknownParameter", "CudaError", "InvalidFile", "version"]
 
 
 class ProfitError(RuntimeError):
@@ -51,6 +53,10 @@ class Unsupported(ProfitError):
     """A parameter combination the CUDA backend does not support."""
 
 
+class InvalidFile(ProfitError):
+    """profit::invalid_file (include/profit/fits_utils.h:34-43)"""
+
+
 _ERRORS = {
     _ffi.PF_ERR_INVALID_PARAMETER: InvalidParameter,
     _ffi.PF_ERR_UNKNOWN_PARAMETER: UnknownParameter,
@@ -59,6 +65,7 @@ _ERRORS = {
     _ffi.PF_ERR_DEVICE_LIMIT: DeviceLimit,
     _ffi.PF_ERR_UNSUPPORTED: Unsupported,
     _ffi.PF_ERR_INTERNAL: ProfitError,
+    _ffi.PF_ERR_INVALID_FILE: InvalidFile,
 }
 
 
@@ -413,6 +420,40 @@ def create_convolver(kind="cuda", env=None):
     if kind not in names:
         raise InvalidParameter("Unsupported convolver type: %s" % kind)
     return Convolver(names[kind], env)
+
+
+def from_fits(filename):
+    """profit::from_fits (src/fits_utils.cpp:60-126) through pf_fits_read:
+    the image of a FITS file written as to_fits writes (BITPIX -64, NAXIS 2)
+    as a float64 array of shape (height, width), and its pixel scale
+    (CDELT1, CDELT2; 1 where absent). Raises InvalidFile with the
+    reference's messages."""
+    lib = _ffi.load()
+    name = os.fsencode(filename)
+    w, h = ctypes.c_uint32(), ctypes.c_uint32()
+    sx, sy = ctypes.c_double(), ctypes.c_double()
+    _check(lib.pf_fits_read(name, None, 0, ctypes.byref(w), ctypes.byref(h), ctypes.byref(sx), ctypes.byref(sy)))
+    img = np.zeros((h.value, w.value), dtype=np.float64)
+    _check(lib.pf_fits_read(name, img.ctypes.data_as(ctypes.c_void_p), img.size, ctypes.byref(w),
+                            ctypes.byref(h), ctypes.byref(sx), ctypes.byref(sy)))
+    return img, (sx.value, sy.value)
+
+
+def to_fits(image, offset, pixel_scale, filename):
+    """profit::to_fits (src/fits_utils.cpp:150-205) through pf_fits_write:
+    writes `image` (2-D, rows = height) with the origin's `offset` (x, y;
+    whole pixels, as Model.evaluate_with_offset returns it) and `pixel_scale`
+    (x, y) into `filename`, ".fits" appended unless it ends in it; the bytes
+    are the reference's."""
+    img = np.ascontiguousarray(image, dtype=np.float64)
+    if img.ndim != 2:
+        raise InvalidParameter("to_fits: the image must be 2-D")
+    ox, oy = (int(v) for v in offset)
+    if ox != offset[0] or oy != offset[1] or ox < 0 or oy < 0 or max(ox, oy) >= 1 << 32:
+        raise InvalidParameter("to_fits: the offset must be a pair of non-negative whole pixels")
+    h, w = img.shape
+    _check(_ffi.load().pf_fits_write(os.fsencode(filename), img.ctypes.data_as(ctypes.c_void_p), w, h, ox, oy,
+                                     float(pixel_scale[0]), float(pixel_scale[1])))
 
 
 class Batch:

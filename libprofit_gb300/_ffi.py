@@ -20,6 +20,7 @@ PF_ERR_NO_MEMORY = 4
 PF_ERR_DEVICE_LIMIT = 5
 PF_ERR_UNSUPPORTED = 6
 PF_ERR_INTERNAL = 7
+PF_ERR_INVALID_FILE = 8
 
 PF_ENV_DOUBLE = 0x1
 
@@ -100,6 +101,9 @@ _SIGNATURES = {
     "pf_batch_depth": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "pf_batch_drawing_dims": (ctypes.c_int, [_P, _P]),
     "pf_batch_conv_info": (ctypes.c_int, [_P, _P, _P, _P]),
+    "pf_fits_write": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                     ctypes.c_uint32, ctypes.c_double, ctypes.c_double]),
+    "pf_fits_read": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.c_size_t, _P, _P, _P, _P]),
 }
 
 _lib = None

@@ -97,6 +97,16 @@ pf_status fail(pf_status s, const std::string &msg)
 	return s;
 }
 
+}  // namespace
+
+namespace pf {
+// the calling thread's pf_last_error message, for the host-only entry points
+// of other translation units (fits.cu)
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace pf
+
+namespace {
+
 #define PF_CUDA_TRY(call)                                                                              \
 	do {                                                                                               \
 		cudaError_t e_ = (call);                                                                       \

@@ -118,6 +118,32 @@ def ref():
     return _ref
 
 
+def ref_to_fits(image, offset, scale, fname):
+    """profit::to_fits of the compiled reference (oracle/_ref)."""
+    R = ref()
+    img = np.ascontiguousarray(image, dtype=np.float64)
+    err = ctypes.create_string_buffer(512)
+    rc = R.ref_to_fits(img.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint(img.shape[1]), ctypes.c_uint(img.shape[0]),
+                       ctypes.c_uint(offset[0]), ctypes.c_uint(offset[1]), ctypes.c_double(scale[0]),
+                       ctypes.c_double(scale[1]), os.fsencode(fname), err, 512)
+    if rc != 0:
+        raise OracleError(err.value.decode())
+
+
+def ref_from_fits(fname, cap=1 << 22):
+    """profit::from_fits of the compiled reference: (image (h, w), (sx, sy))."""
+    R = ref()
+    out = np.zeros(cap, dtype=np.float64)
+    w, h = ctypes.c_uint(), ctypes.c_uint()
+    sx, sy = ctypes.c_double(), ctypes.c_double()
+    err = ctypes.create_string_buffer(512)
+    rc = R.ref_from_fits(os.fsencode(fname), out.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(cap),
+                         ctypes.byref(w), ctypes.byref(h), ctypes.byref(sx), ctypes.byref(sy), err, 512)
+    if rc != 0:
+        raise OracleError(err.value.decode())
+    return out[:w.value * h.value].reshape(h.value, w.value).copy(), (sx.value, sy.value)
+
+
 def make_profile(kind, **params):
     """Builds an OrcProfile with the reference defaults, overridden by params."""
     p = OrcProfile()

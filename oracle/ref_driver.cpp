@@ -6,13 +6,15 @@
  * public C++ API exactly as a user would: profit::Model, add_profile,
  * Profile::parameter, set_psf, set_convolver(create_convolver(...)),
  * Model::evaluate (include/profit/model.h, include/profit/profile.h,
- * include/profit/convolve.h).
+ * include/profit/convolve.h), and profit::from_fits / to_fits
+ * (include/profit/fits_utils.h) for the FITS fixtures.
  */
 #include <cstring>
 #include <exception>
 #include <string>
 #include <vector>
 
+#include "profit/fits_utils.h"
 #include "profit/profit.h"
 #include "profit_oracle.h"
 
@@ -159,6 +161,50 @@ extern "C" int ref_evaluate(const orc_model *m, const orc_profile *profiles, int
 #else
 		(void)level_counts;
 #endif
+		return 0;
+	}
+	catch (const std::exception &e) {
+		std::strncpy(err, e.what(), err_len - 1);
+		err[err_len - 1] = 0;
+		return -1;
+	}
+}
+
+// profit::to_fits (src/fits_utils.cpp:150-205) on a row-major image.
+extern "C" int ref_to_fits(const double *image, unsigned int w, unsigned int h, unsigned int offset_x,
+                           unsigned int offset_y, double scale_x, double scale_y, const char *fname, char *err,
+                           int err_len)
+{
+	try {
+		std::vector<double> data(image, image + (size_t)w * h);
+		profit::Point offset(offset_x, offset_y);
+		profit::to_fits(profit::Image(data, w, h), offset, {scale_x, scale_y}, fname);
+		return 0;
+	}
+	catch (const std::exception &e) {
+		std::strncpy(err, e.what(), err_len - 1);
+		err[err_len - 1] = 0;
+		return -1;
+	}
+}
+
+// profit::from_fits (src/fits_utils.cpp:60-126): dimensions and scale, and the
+// pixels when they fit in `cap` values.
+extern "C" int ref_from_fits(const char *fname, double *out, size_t cap, unsigned int *w, unsigned int *h,
+                             double *scale_x, double *scale_y, char *err, int err_len)
+{
+	try {
+		profit::PixelScale scale;
+		profit::Image image = profit::from_fits(fname, scale);
+		*w = image.getWidth();
+		*h = image.getHeight();
+		*scale_x = scale.first;
+		*scale_y = scale.second;
+		if (image.size() > cap) {
+			std::strncpy(err, "output buffer too small", err_len);
+			return -2;
+		}
+		std::memcpy(out, image.data(), sizeof(double) * image.size());
 		return 0;
 	}
 	catch (const std::exception &e) {
