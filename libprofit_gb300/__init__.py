@@ -507,10 +507,20 @@ class Batch:
     def handle(self):
         return self._h
 
+    def _check_buffers(self, params=None, images=None, data=None, sigma=None, cotangent=None, chi2=None,
+                       grad=None):
+        pix = 8 if self.env.use_double else 4
+        _need(params, self.n_profiles * NPAR, 8, "params")
+        for name, buf in (("images", images), ("data", data), ("sigma", sigma), ("cotangent", cotangent)):
+            _need(buf, self.total_pixels, pix, name)
+        _need(chi2, len(self.models), 8, "chi2")
+        _need(grad, self.n_profiles * NPAR, 8, "grad")
+
     def forward(self, images, flux=None, stream=None):
         """Renders into `images` (device buffer of total_pixels elements,
         float64 for a use_double environment), on `stream` (a cudaStream_t
         handle; by default torch's current stream)."""
+        self._check_buffers(images=images)
         _check(_ffi.load().pf_forward(self._h, ctypes.c_void_p(images.data_ptr()),
                                       None if flux is None else ctypes.c_void_p(flux.data_ptr()),
                                       _stream_arg(stream)))
@@ -523,6 +533,7 @@ class Batch:
         _check(_ffi.load().pf_batch_set_params(self._h, p.ctypes.data_as(ctypes.c_void_p)))
 
     def set_params_dev(self, params, stream=None):
+        self._check_buffers(params=params)
         _check(_ffi.load().pf_batch_set_params_dev(self._h, ctypes.c_void_p(params.data_ptr()),
                                                    _stream_arg(stream)))
 
@@ -546,11 +557,13 @@ class Batch:
     def backward(self, images, data=None, sigma=None, cotangent=None, chi2=None, grad=None, stream=None):
         """chi^2 per model and d chi^2 / d par (or, with a cotangent, the
         vector-Jacobian product of the images) into the given device buffers."""
+        self._check_buffers(images=images, data=data, sigma=sigma, cotangent=cotangent, chi2=chi2, grad=grad)
         _check(_ffi.load().pf_backward(self._h, _ptr(images), _ptr(data), _ptr(sigma), _ptr(cotangent),
                                        _ptr(chi2), _ptr(grad), _stream_arg(stream)))
 
     def forward_backward(self, images, data, sigma=None, chi2=None, grad=None, stream=None):
         """One model + VJP evaluation: render, then chi^2 and its gradient."""
+        self._check_buffers(images=images, data=data, sigma=sigma, chi2=chi2, grad=grad)
         _check(_ffi.load().pf_forward_backward(self._h, _ptr(images), _ptr(data), _ptr(sigma), _ptr(chi2),
                                                _ptr(grad), _stream_arg(stream)))
 
@@ -558,6 +571,7 @@ class Batch:
         """set_params_dev(params) (if given) + forward_backward, captured once
         into a CUDA graph and replayed (pf_step_graph); `stream` must be a
         created stream (torch.cuda.Stream().cuda_stream)."""
+        self._check_buffers(params=params, images=images, data=data, sigma=sigma, chi2=chi2, grad=grad)
         _check(_ffi.load().pf_step_graph(self._h, _ptr(params), _ptr(images), _ptr(data), _ptr(sigma),
                                          _ptr(chi2), _ptr(grad), _stream_arg(stream)))
 
@@ -600,6 +614,17 @@ _CUDA_STREAM_LEGACY = 0x1  # cudaStreamLegacy
 
 def _ptr(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _need(buf, count, itemsize, what):
+    """The C ABI takes raw device pointers and reads or writes `count`
+    elements through them: a tensor that is smaller, or of another element
+    size, is refused here instead of being overrun on the device."""
+    if buf is None or not hasattr(buf, "numel"):
+        return
+    if buf.element_size() != itemsize or buf.numel() < count:
+        raise InvalidParameter("%s: %d elements of %d bytes needed, the buffer has %d of %d" %
+                               (what, count, itemsize, buf.numel(), buf.element_size()))
 
 
 def _stream_arg(stream):

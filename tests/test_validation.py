@@ -82,3 +82,29 @@ def test_model_checks(oracle_lib):
     assert _gpu_message(10, 10, [("sersic", {})], mask=mask) == "Mask dimensions != model dimensions"
     with pytest.raises(O.OracleError, match="Mask dimensions != model dimensions"):
         O.evaluate(O.Case(10, 10, [("sersic", {})], mask=mask))
+
+
+def test_device_buffer_sizes_checked_on_the_host():
+    """The C ABI takes raw device pointers; the Python Batch methods refuse a
+    buffer with too few elements or another element size before any launch
+    (a parameter vector of one row per model instead of one per profile would
+    otherwise be read past its end)."""
+    import libprofit_gb300 as pg
+
+    class Buf:
+        def __init__(self, n, size):
+            self.n, self.size = n, size
+
+        def numel(self):
+            return self.n
+
+        def element_size(self):
+            return self.size
+
+    pg._need(Buf(384, 8), 384, 8, "params")
+    pg._need(Buf(400, 8), 384, 8, "params")
+    pg._need(None, 384, 8, "params")
+    with pytest.raises(pg.InvalidParameter, match="params: 384 elements of 8 bytes needed, the buffer has 192 of 8"):
+        pg._need(Buf(192, 8), 384, 8, "params")
+    with pytest.raises(pg.InvalidParameter, match="images"):
+        pg._need(Buf(1000, 8), 1000, 4, "images")
