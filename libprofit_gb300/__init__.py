@@ -394,6 +394,31 @@ class Model:
                                                     ctypes.byref(oh)))
         return out.reshape(oh.value, ow.value)
 
+    def get_profile_integrations(self):
+        """Model::get_profile_integrations (src/model.cpp:370-381, a
+        PROFIT_DEBUG build): per radial profile name, {recursion level:
+        subsample_pixel calls at that level} for one evaluation of the model
+        (src/radial.cpp:71-79); a later profile of the same name replaces an
+        earlier one, as in the reference's map. Evaluates the model once
+        through a one-model batch with depth recording on."""
+        import torch
+        env = _env_or_default(self.env)
+        b = Batch([self], env)
+        try:
+            b.record_depth(True)
+            out = torch.zeros(b.total_pixels, dtype=torch.float64 if env.use_double else torch.float32,
+                              device="cuda:%d" % env.device)
+            b.forward(out)
+            b.check()
+            res = {}
+            for prof, (_, counts) in zip(self.profiles, b.depth()):
+                if prof.kind in _RADIAL:
+                    # slots 0-15 of the depth recording's counts are the levels
+                    res[prof.kind] = {lvl: int(c) for lvl, c in enumerate(counts[:16]) if c > 0}
+            return res
+        finally:
+            b.close()
+
 
 class Convolver:
     """A ConvolverType::CUDA convolver (create_convolver, src/convolve.cpp:521-584)."""
@@ -579,7 +604,10 @@ class Batch:
         _check(_ffi.load().pf_batch_record_depth(self._h, int(bool(enable))))
 
     def depth(self):
-        """Per profile: (depth map over its model's drawing area, 32 level counts)."""
+        """Per profile: (depth map over its model's drawing area, 32 counts:
+        slots 0-15 the subsample_pixel calls per recursion level, slot 30 the
+        evaluate_at calls on pixel centres, slot 31 those inside
+        subsample_pixel)."""
         dims = np.zeros(2 * max(1, len(self.models)), dtype=np.uint32)
         _check(_ffi.load().pf_batch_drawing_dims(self._h, dims.ctypes.data_as(ctypes.c_void_p)))
         sizes = []

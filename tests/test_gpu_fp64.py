@@ -146,3 +146,16 @@ def test_convolver_matches_reference_brute(env, oracle_lib):
     # height is refused, as Surface::extend refuses it
     with pytest.raises(pg.InvalidParameter):
         conv.convolve(rng.random((40, 10)), rng.random((15, 15)))
+
+
+@pytest.mark.parametrize("name", sorted(n for n in GOLDEN if _radial_single(n))[::4])
+def test_model_profile_integrations(env, name):
+    """Model.get_profile_integrations against the reference's PROFIT_DEBUG
+    n_integrations (src/model.cpp:370-381): {level: count} of the levels the
+    reference counted, keyed by the profile's name."""
+    entry = GOLDEN[name]
+    m = product_model(entry["spec"], entry["psf"], env)
+    got = m.get_profile_integrations()
+    kind = entry["spec"]["profiles"][0][0]
+    want = {lvl: int(c) for lvl, c in enumerate(entry["counts"][0][:16]) if c > 0}
+    assert got == {kind: want}
