@@ -449,7 +449,7 @@ def run_ours(args, world, rank, local):
             "adjoint_conv_ms": conv_adj}
     # DRAM bytes per launch, per model of this workload: ncu dram__bytes_read.sum +
     # dram__bytes_write.sum of each kernel on the 256-model copy of the workload
-    # (profiles/*_256x256*.md), divided by 256
+    # (one ncu capture per kernel), divided by 256
     traffic_per_model = {"eval_ms": 118.5e6 / 256, "backward_ms": 76.3e6 / 256, "finish_ms": 192.3e6 / 256,
                          "adjoint_conv_ms": ADJ_CONV_TRAFFIC_PER_MODEL}
     roof = {"bound": "fp32", "kernel": dom.replace("_ms", ""), "achieved": None, "peak": fp32_peak,
