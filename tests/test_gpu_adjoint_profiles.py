@@ -6,9 +6,9 @@ PSF, plus a sky), round and boxy; data = the oracle's image at parameters
 perturbed by 5 % plus noise; chi^2 = sum ((model - data) / sigma)^2. Every
 parameter of the profile (xcen, ycen, mag, ang, axrat, box and the kind's own)
 and the sky's bg must match central differences of the oracle's chi^2 with
-h = 1e-6 relative, with the bars of the sersic adjoint test:
-  * FP64 path: |g - fd| <= 1e-4 |fd| + 1e-9 chi^2 / h
-  * FP32 path: |g - fd| <= 1e-3 |fd| + 1e-6 chi^2 / h
+h = 1e-6 relative, by the criterion of tests/helpers.py (that of the sersic
+adjoint test):
+  |g - fd| <= 1e-4 |fd| + 1e-14 sum|c m| / h (+ 2e-6 sum|c dm/dpar| in FP32)
 Parameters whose finite difference is not that of a smooth function are
 excluded (at most two per case): those whose +-h changes the oracle's
 subsampling tree (level counts), which the adjoint holds fixed, and those
@@ -50,9 +50,8 @@ def _truth(kind, box, over):
 
 
 def _with(profiles, i, k, v):
-    out = [(kind, dict(p)) for kind, p in profiles]
-    out[i][1][k] = v
-    return out
+    from tests.helpers import with_param
+    return with_param(profiles, i, k, v)
 
 
 def _problem(O, kind, box, over):
@@ -82,23 +81,17 @@ def _chi2(O, psf, profiles, data, sigma):
     return float(np.sum(((img - data) / sigma) ** 2)), counts
 
 
+def _render(O, psf):
+    def render(p):
+        img, _, counts = O.evaluate(O.Case(SIDE, SIDE, p, psf=psf, magzero=MAGZERO))
+        return img, counts
+    return render
+
+
 def _fd(O, psf, profiles, data, sigma):
-    chi0, counts0 = _chi2(O, psf, profiles, data, sigma)
-    out = {}
+    from tests.helpers import fd_gradients
     names = [(0, k) for k in ORDER[profiles[0][0]]] + [(1, "bg")]
-    for i, k in names:
-        v = profiles[i][1][k]
-        h = 1e-6 * max(abs(v), 1e-3)
-        cp, c_p = _chi2(O, psf, _with(profiles, i, k, v + h), data, sigma)
-        cm, c_m = _chi2(O, psf, _with(profiles, i, k, v - h), data, sigma)
-        same_tree = np.array_equal(c_p, counts0) and np.array_equal(c_m, counts0)
-        fd = (cp - cm) / (2 * h)
-        cp2, _ = _chi2(O, psf, _with(profiles, i, k, v + h / 10), data, sigma)
-        cm2, _ = _chi2(O, psf, _with(profiles, i, k, v - h / 10), data, sigma)
-        fd2 = (cp2 - cm2) / (2 * h / 10)
-        smooth = abs(fd - fd2) <= 2e-5 * abs(fd) + 1e-9 * chi0 / h
-        out[(i, k)] = (fd, same_tree and smooth, h)
-    return out
+    return fd_gradients(_render(O, psf), profiles, names, data, sigma, smooth=True)[1]
 
 
 def _slot(kind, k):
@@ -150,17 +143,13 @@ def test_profile_gradient_matches_finite_differences(problems, oracle_lib, kind,
     psf, profiles, data, sigma, fd = problems[(kind, box, bool(over))]
     chi2, grad = _gpu_grads([(psf, profiles)], [data], [sigma], use_double)
     chi2_ref, _ = _chi2(oracle_lib, psf, profiles, data, sigma)
-    assert abs(chi2[0] - chi2_ref) <= (1e-10 if use_double else 1e-4) * chi2_ref
-    rtol, floor = (1e-4, 1e-9) if use_double else (1e-3, 1e-6)
+    assert abs(chi2[0] - chi2_ref) <= (1e-10 if use_double else 1e-5) * chi2_ref
     checked = skipped = 0
-    for (i, k), (want, same_tree, h) in fd.items():
-        if not same_tree:
+    for (i, k), r in fd.items():
+        if not r.usable:
             skipped += 1
             continue
-        got = grad[i, _slot(kind, k) if i == 0 else 6]
-        atol = floor * chi2_ref / h
-        assert abs(got - want) <= rtol * abs(want) + atol, \
-            "%s box %g %s: adjoint %.8g vs fd %.8g" % (kind, box, k, got, want)
+        r.check(grad[i, _slot(kind, k) if i == 0 else 6], not use_double, "%s box %g %s" % (kind, box, k))
         checked += 1
     assert skipped <= 2 and checked >= len(fd) - 2
 
@@ -218,19 +207,13 @@ def test_psf_profile_gradient_matches_finite_differences(oracle_lib, use_double)
     psf, profiles, data, sigma = _psf_problem(O)
     chi2, grad = _gpu_grads([(psf, profiles)], [data], [sigma], use_double)
     chi2_ref, _ = _chi2(O, psf, profiles, data, sigma)
-    assert abs(chi2[0] - chi2_ref) <= (1e-10 if use_double else 1e-4) * chi2_ref
-    rtol, floor = (1e-4, 1e-9) if use_double else (1e-3, 1e-6)
+    assert abs(chi2[0] - chi2_ref) <= (1e-10 if use_double else 1e-5) * chi2_ref
+    from tests.helpers import fd_gradients
     slots = {"xcen": 0, "ycen": 1, "mag": 2}
-    for i in (1, 2):
-        for k in ("xcen", "ycen", "mag"):
-            v = profiles[i][1][k]
-            h = 1e-6 * max(abs(v), 1e-3)
-            cp, _ = _chi2(O, psf, _with(profiles, i, k, v + h), data, sigma)
-            cm, _ = _chi2(O, psf, _with(profiles, i, k, v - h), data, sigma)
-            want = (cp - cm) / (2 * h)
-            got = grad[i, slots[k]]
-            atol = floor * chi2_ref / h
-            assert abs(got - want) <= rtol * abs(want) + atol, "psf %d %s: adjoint %.8g vs fd %.8g" % (i, k, got, want)
+    names = [(i, k) for i in (1, 2) for k in ("xcen", "ycen", "mag")]
+    _, fd = fd_gradients(_render(O, psf), profiles, names, data, sigma)
+    for (i, k), r in fd.items():
+        r.check(grad[i, slots[k]], not use_double, "psf %d %s" % (i, k))
 
 
 # A Sersic with rescale_flux (src/sersic.cpp:302-325): the flux scale divides
@@ -252,19 +235,15 @@ def test_rescale_flux_gradient_matches_finite_differences(oracle_lib, use_double
     sigma = np.full_like(data, 0.01 * data.max())
     data = data + rng.normal(0, sigma[0, 0], data.shape)
     chi2, grad = _gpu_grads([(psf, profiles)], [data], [sigma], use_double)
-    chi2_ref, counts0 = _chi2(O, psf, profiles, data, sigma)
-    assert abs(chi2[0] - chi2_ref) <= (1e-10 if use_double else 1e-4) * chi2_ref
-    rtol, floor = (1e-4, 1e-9) if use_double else (1e-3, 1e-6)
+    chi2_ref, _ = _chi2(O, psf, profiles, data, sigma)
+    assert abs(chi2[0] - chi2_ref) <= (1e-10 if use_double else 1e-5) * chi2_ref
+    from tests.helpers import fd_gradients
+    slots = {"xcen": 0, "mag": 2, "axrat": 4, "re": 6, "nser": 7}
+    _, fd = fd_gradients(_render(O, psf), profiles, [(0, k) for k in slots], data, sigma)
     checked = 0
-    for k, slot in (("xcen", 0), ("mag", 2), ("axrat", 4), ("re", 6), ("nser", 7)):
-        v = profiles[0][1][k]
-        h = 1e-6 * max(abs(v), 1e-3)
-        cp, c_p = _chi2(O, psf, _with(profiles, 0, k, v + h), data, sigma)
-        cm, c_m = _chi2(O, psf, _with(profiles, 0, k, v - h), data, sigma)
-        if not (np.array_equal(c_p, counts0) and np.array_equal(c_m, counts0)):
+    for (_, k), r in fd.items():
+        if not r.usable:
             continue
-        want = (cp - cm) / (2 * h)
-        got = grad[0, slot]
-        assert abs(got - want) <= rtol * abs(want) + floor * chi2_ref / h, "%s: adjoint %.8g vs fd %.8g" % (k, got, want)
+        r.check(grad[0, slots[k]], not use_double, k)
         checked += 1
     assert checked >= 4

@@ -164,3 +164,56 @@ def param_matrix(specs):
                     p.parameter(k, float(v))
             rows.append([p.desc.par[i] for i in range(12)])
     return np.array(rows, dtype=np.float64)
+
+
+def gradient_scales(specs, par, images, data, sigma, env64, h_rel=1e-6, n_par=8):
+    """The scale of each chi^2 gradient component: sum_p |c_p dm_p / dpar|,
+    c = 2 (m - d) / sigma^2 at the parameters `par` (n_profiles x 12, batch
+    order of `specs`), dm/dpar by central differences (h = h_rel x |par|,
+    at least h_rel x 1e-3) of the plain FP64 path. `images`, `data`, `sigma`:
+    the models' output images back to back (numpy, float64). An FP32
+    gradient carries rounding of a few units of 2^-24 on this scale, whatever
+    the component's own size.
+
+    Returns (scale, same_tree), both n_profiles x n_par: same_tree is False
+    where the +-h images of a parameter do not keep the subsampling tree
+    (per-level counts differ from the unperturbed model's), so that the
+    difference is not a derivative there."""
+    import torch
+    import libprofit_gb300 as pg
+    first = np.cumsum([0] + [len(s["profiles"]) for s in specs])
+    scale = np.zeros((int(first[-1]), n_par))
+    same = np.ones((int(first[-1]), n_par), dtype=bool)
+    out_off = np.cumsum([0] + [s["width"] * s["height"] for s in specs])
+    for i, s in enumerate(specs):
+        n = len(s["profiles"])
+        p0 = par[first[i]:first[i + 1]]
+        rows, hs = [p0], []
+        for j in range(n):
+            for k in range(n_par):
+                h = h_rel * max(abs(p0[j, k]), 1e-3)
+                hs.append(h)
+                for sgn in (1.0, -1.0):
+                    q = p0.copy()
+                    q[j, k] += sgn * h
+                    rows.append(q)
+        b = pg.Batch([to_model(s, env64) for _ in rows], env64)
+        b.set_params(np.concatenate(rows))
+        b.record_depth(True)
+        img = torch.zeros(b.total_pixels, dtype=torch.float64, device="cuda")
+        b.forward(img)
+        b.check()
+        im = img.cpu().numpy().reshape(len(rows), -1)
+        counts = [c for _, c in b.depth()]
+        b.close()
+        a, z = out_off[i], out_off[i + 1]
+        cot = 2 * (images[a:z] - data[a:z]) / sigma[a:z] ** 2
+        q = 0
+        for j in range(n):
+            for k in range(n_par):
+                up, dn = 1 + 2 * q, 2 + 2 * q
+                scale[first[i] + j, k] = np.sum(np.abs(cot * (im[up] - im[dn]) / (2 * hs[q])))
+                same[first[i] + j, k] = all(np.array_equal(counts[r * n + jj], counts[jj])
+                                            for r in (up, dn) for jj in range(n))
+                q += 1
+    return scale, same
