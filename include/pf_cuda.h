@@ -211,8 +211,8 @@ PF_API pf_status pf_convolve(pf_env *env, const double *src, uint32_t w, uint32_
                       double *out);
 
 /*
- * pf_convolve_noalloc: pf_convolve without allocating memory of any kind. No
- * counterpart in the reference.
+ * pf_convolve_noalloc: pf_convolve that allocates no device memory after its
+ * first call on a device. No counterpart in the reference.
  *
  * For callers that cannot allocate device memory at the moment they convolve:
  * a fitting loop running beside a caching allocator that holds almost all of
@@ -231,12 +231,14 @@ PF_API pf_status pf_convolve(pf_env *env, const double *src, uint32_t w, uint32_
  * element it reads.
  *
  * The first call on each device looks up the scratch's address, which can
- * load this library's device code onto that device; make that first call
- * before any stream capture. All calls on one device share the one scratch:
- * calls that overlap in time on the same device (from several threads, or
- * through several environments) race and give wrong results; serialise them.
- * On success nothing is allocated; a failure records its message for
- * pf_last_error as every entry point does.
+ * load this library's device code onto that device and so reserve the array;
+ * make that first call before any stream capture. The address is kept for the
+ * life of the process: after a cudaDeviceReset of that device this entry
+ * point must not be called again. All calls on one device share the one
+ * scratch: calls that overlap in time on the same device (from several
+ * threads, or through several environments) race and give wrong results;
+ * serialise them. A failure records its message for pf_last_error, as every
+ * entry point does (that message is host memory).
  */
 #define PF_NOALLOC_MAX_PIXELS (1u << 20)
 #define PF_NOALLOC_MAX_KERNEL_PIXELS (1u << 16)

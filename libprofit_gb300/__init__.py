@@ -535,17 +535,19 @@ class Batch:
     def _check_buffers(self, params=None, images=None, data=None, sigma=None, cotangent=None, chi2=None,
                        grad=None):
         pix = 8 if self.env.use_double else 4
-        _need(params, self.n_profiles * NPAR, 8, "params")
+        dev = self.env.device
+        _need(params, self.n_profiles * NPAR, 8, "params", dev)
         for name, buf in (("images", images), ("data", data), ("sigma", sigma), ("cotangent", cotangent)):
-            _need(buf, self.total_pixels, pix, name)
-        _need(chi2, len(self.models), 8, "chi2")
-        _need(grad, self.n_profiles * NPAR, 8, "grad")
+            _need(buf, self.total_pixels, pix, name, dev)
+        _need(chi2, len(self.models), 8, "chi2", dev)
+        _need(grad, self.n_profiles * NPAR, 8, "grad", dev)
 
     def forward(self, images, flux=None, stream=None):
         """Renders into `images` (device buffer of total_pixels elements,
         float64 for a use_double environment), on `stream` (a cudaStream_t
         handle; by default torch's current stream)."""
         self._check_buffers(images=images)
+        _need(flux, len(self.models), 8, "flux", self.env.device)
         _check(_ffi.load().pf_forward(self._h, ctypes.c_void_p(images.data_ptr()),
                                       None if flux is None else ctypes.c_void_p(flux.data_ptr()),
                                       _stream_arg(stream)))
@@ -644,15 +646,25 @@ def _ptr(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
 
-def _need(buf, count, itemsize, what):
+def _need(buf, count, itemsize, what, device=None):
     """The C ABI takes raw device pointers and reads or writes `count`
-    elements through them: a tensor that is smaller, or of another element
-    size, is refused here instead of being overrun on the device."""
+    elements through them as one dense array on the environment's device: a
+    tensor that is smaller, of another element size, not contiguous, in host
+    memory or on another device is refused here instead of being overrun or
+    misread on the device."""
     if buf is None or not hasattr(buf, "numel"):
         return
     if buf.element_size() != itemsize or buf.numel() < count:
         raise InvalidParameter("%s: %d elements of %d bytes needed, the buffer has %d of %d" %
                                (what, count, itemsize, buf.numel(), buf.element_size()))
+    if hasattr(buf, "is_cuda"):
+        if not buf.is_cuda:
+            raise InvalidParameter("%s: a device (CUDA) buffer is needed, the tensor is in host memory" % what)
+        if device is not None and buf.device.index is not None and buf.device.index != device:
+            raise InvalidParameter("%s: the buffer is on device %d, the environment on device %d" %
+                                   (what, buf.device.index, device))
+    if hasattr(buf, "is_contiguous") and not buf.is_contiguous():
+        raise InvalidParameter("%s: the buffer must be contiguous" % what)
 
 
 def _stream_arg(stream):

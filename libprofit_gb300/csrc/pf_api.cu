@@ -1914,6 +1914,10 @@ pf_status pf_convolve_noalloc(pf_env *env, const double *src, uint32_t w, uint32
 		                                     std::to_string(PF_NOALLOC_MAX_KERNEL_PIXELS) + "; use pf_convolve");
 	}
 	PF_CUDA_TRY(cudaSetDevice(env->device));
+	// an earlier failed runtime call of the process (a cudaMalloc that found the
+	// device full) leaves its error for cudaGetLastError: cleared here, so that
+	// the check after the launch below reports this call's launch only
+	(void)cudaGetLastError();
 	unsigned char *base = nullptr;
 	pf_status s = convolve_scratch(env->device, &base);
 	if (s != PF_OK) return s;

@@ -78,11 +78,12 @@ class OrcConstants(ctypes.Structure):
 
 
 def build(with_ref=None):
-    """Compiles liboracle.so (always) and the reference library (when the
-    reference tree is present, or when with_ref is True)."""
+    """Compiles liboracle.so (always) and the reference library when the
+    environment variable PF_REFERENCE_DIR names a libprofit source tree
+    (with_ref None), or must (with_ref True)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    ref_dir = os.environ.get("PF_REFERENCE_DIR", "/root/reference")
-    if with_ref or (with_ref is None and os.path.isdir(os.path.join(ref_dir, "src"))):
+    ref_dir = os.environ.get("PF_REFERENCE_DIR", "")
+    if with_ref or (with_ref is None and ref_dir and os.path.isdir(os.path.join(ref_dir, "src"))):
         subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "REF=" + ref_dir], check=True)
 
 

@@ -108,3 +108,36 @@ def test_device_buffer_sizes_checked_on_the_host():
         pg._need(Buf(192, 8), 384, 8, "params")
     with pytest.raises(pg.InvalidParameter, match="images"):
         pg._need(Buf(1000, 8), 1000, 4, "images")
+
+
+def test_batch_refuses_host_foreign_and_strided_buffers():
+    """A tensor in host memory, on another device than the environment's, or
+    not contiguous is refused: the C ABI would read or write its data pointer
+    as one dense array on the environment's device."""
+    import torch
+    import libprofit_gb300 as pg
+
+    class Dev:
+        def __init__(self, index):
+            self.index = index
+
+    class Buf:
+        def __init__(self, n, cuda=True, index=0, contiguous=True):
+            self.n, self.is_cuda, self.device, self.c = n, cuda, Dev(index), contiguous
+
+        def numel(self):
+            return self.n
+
+        def element_size(self):
+            return 8
+
+        def is_contiguous(self):
+            return self.c
+
+    pg._need(Buf(16), 16, 8, "grad", 0)
+    with pytest.raises(pg.InvalidParameter, match="grad: a device .* host memory"):
+        pg._need(torch.zeros(16, dtype=torch.float64), 16, 8, "grad", 0)
+    with pytest.raises(pg.InvalidParameter, match="chi2: the buffer is on device 1, the environment on device 0"):
+        pg._need(Buf(16, index=1), 16, 8, "chi2", 0)
+    with pytest.raises(pg.InvalidParameter, match="flux: the buffer must be contiguous"):
+        pg._need(Buf(16, contiguous=False), 16, 8, "flux", 0)

@@ -6,6 +6,9 @@ both alone and after every other test has used the device. Each case makes two
 calls in a row on different inputs, so a result that depended on what an
 earlier call left in the shared scratch would show. Tolerance: 1e-13 relative,
 as for pf_convolve against the brute-force oracle (both run the same kernel).
+Two tests check the property the entry point exists for: 100 calls leave the
+device's free memory unchanged, and with the device's memory taken by
+torch's caching allocator (pf_convolve then fails) the call still succeeds.
 """
 import ctypes
 
@@ -83,3 +86,56 @@ def test_noalloc_refuses_beyond_scratch(abi):
     st, got = _call(lib, "pf_convolve_noalloc", env, src, krn)
     assert st == ffi.PF_OK
     np.testing.assert_allclose(got, ref, rtol=RTOL, atol=0)
+
+
+def test_noalloc_allocates_no_device_memory(abi):
+    """The property the entry point exists for. After a first call on the
+    device (which may load the library's device code), 100 calls leave the
+    device's free memory exactly as it was."""
+    import torch
+    ffi, lib, env = abi
+    rng = np.random.default_rng(11)
+    src, krn = rng.random((512, 512)), rng.random((25, 25))
+    mask = (rng.random(src.shape) > 0.2).astype(np.uint8)
+    st, first = _call(lib, "pf_convolve_noalloc", env, src, krn, mask)
+    assert st == ffi.PF_OK, lib.pf_last_error()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    for _ in range(100):
+        st, out = _call(lib, "pf_convolve_noalloc", env, src, krn, mask)
+        assert st == ffi.PF_OK, lib.pf_last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0
+    np.testing.assert_array_equal(out, first)
+
+
+def test_noalloc_works_on_a_full_device(abi):
+    """A caller whose caching allocator holds nearly all of the device's
+    memory: pf_convolve cannot allocate its buffers there, while
+    pf_convolve_noalloc still gives the same result as on an empty device."""
+    import torch
+    ffi, lib, env = abi
+    rng = np.random.default_rng(12)
+    src, krn = rng.random((1024, 1024)), rng.random((15, 15))
+    st, want = _call(lib, "pf_convolve_noalloc", env, src, krn)
+    assert st == ffi.PF_OK, lib.pf_last_error()
+    held = []
+    try:
+        # take the device's memory through torch until 8 to 10 MiB are free
+        # (pf_convolve needs 2 x 8 MiB for this image)
+        for chunk in (1 << 34, 1 << 30, 1 << 26, 1 << 21):
+            while torch.cuda.mem_get_info(0)[0] > chunk + (8 << 20):
+                try:
+                    held.append(torch.empty(chunk, dtype=torch.uint8, device="cuda:0"))
+                except torch.cuda.OutOfMemoryError:
+                    break
+        assert torch.cuda.mem_get_info(0)[0] < 16 << 20
+        st_alloc, _ = _call(lib, "pf_convolve", env, src, krn)
+        assert st_alloc != ffi.PF_OK
+        st, got = _call(lib, "pf_convolve_noalloc", env, src, krn)
+        assert st == ffi.PF_OK, lib.pf_last_error()
+        np.testing.assert_array_equal(got, want)
+    finally:
+        del held
+        torch.cuda.empty_cache()
