@@ -258,23 +258,26 @@ def gradient_accuracy(specs, par, img64, data, sigma, g32, g64, env64):
     """The FP32 batch's gradients (n_profiles x 8) against the plain FP64
     path's on the same models and data: the largest relative error with no
     floor, the share of components within 1e-4 relative, and the check
-    |g32 - g64| <= 1e-4 |g64| + 2e-6 sum_p |c_p dm_p/dpar| (the scale of the
-    sum each component is, from central differences of the FP64 path), over
-    the components whose differences keep the subsampling tree."""
+    |g32 - g64| <= 1e-4 |g64| + 2e-6 sum_p |c_p dm_p/dpar| + 2e-6 sum_p
+    2 |m_p dm_p/dpar| / sigma_p^2 (the scale of the sum each component is, and
+    its sensitivity to the FP32 image's relative error; central differences
+    of the FP64 path), over the components whose differences keep the
+    subsampling tree."""
     import workloads as W
-    scale, same = W.gradient_scales(specs, par, img64, data, sigma, env64)
+    scale_c, scale_m, same = W.gradient_scales(specs, par, img64, data, sigma, env64)
     err = np.abs(g32 - g64)
     rel = err / np.abs(g64)
-    bound = 1e-4 * np.abs(g64) + 2e-6 * scale
+    bound = 1e-4 * np.abs(g64) + 2e-6 * scale_c + 2e-6 * scale_m
     worst = np.unravel_index(np.argmax(rel), rel.shape)
     return {"models": len(specs), "components": int(rel.size),
             "max_rel_err": float(rel.max()),
             "median_rel_err": float(np.median(rel)),
             "frac_within_1e-4": float((rel <= 1e-4).mean()),
             "worst": {"g64": float(g64[worst]), "g32": float(g32[worst]),
-                      "scale_sum_abs_c_dm": float(scale[worst])},
-            "max_err_over_scale": float((err / scale)[same].max()),
-            "bound": "1e-4 |g64| + 2e-6 sum_p |c_p dm_p/dpar|",
+                      "sum_abs_c_dm": float(scale_c[worst]), "sum_abs_2m_dm_over_sigma2": float(scale_m[worst])},
+            "max_err_over_sum_abs_c_dm": float((err / scale_c)[same].max()),
+            "max_err_over_sum_abs_2m_dm_over_sigma2": float((err / scale_m)[same].max()),
+            "bound": "1e-4 |g64| + 2e-6 sum_p |c_p dm_p/dpar| + 2e-6 sum_p 2 |m_p dm_p/dpar| / sigma_p^2",
             "max_err_over_bound": float((err / bound)[same].max()),
             "components_checked": int(same.sum())}
 

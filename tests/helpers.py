@@ -44,7 +44,8 @@ def rel_err(a, b, floor=0.0):
 # The adjoint is checked against central differences of the FP64 oracle's
 # chi^2 = sum ((m - d) / sigma)^2, step h = FD_STEP x |parameter|. A gradient
 # g passes when
-#   |g - fd| <= GRAD_RTOL |fd| + noise (+ FP32_COND x cond for FP32 results)
+#   |g - fd| <= GRAD_RTOL |fd| + noise
+#               (+ FP32_COND x cond + FP32_IMAGE x sens for FP32 results)
 # where
 #   noise = FD_NOISE x sum_p |c_p m_p| / h, c = 2 (m - d) / sigma^2: the
 #           rounding of the two chi^2 values the difference divides by 2h
@@ -55,28 +56,34 @@ def rel_err(a, b, floor=0.0):
 #           the scale of the sum the gradient is. An FP32 result carries
 #           rounding of a few units of 2^-24 on that scale, whatever the
 #           gradient's own size; a component that nearly cancels (|g| much
-#           smaller than cond) can hold no more relative precision than that.
+#           smaller than cond) can hold no more relative precision than that;
+#   sens  = sum_p 2 |m_p dm_p / dtheta| / sigma_p^2: the gradient's
+#           sensitivity to relative errors of the image m, which an FP32
+#           image carries at ~1e-7 (a few 1e-6 at most, on faint pixels).
 # Parameters whose +-h changes the oracle's subsampling tree (per-level
 # counts) are not checked: the adjoint holds the tree fixed.
 FD_STEP = 1e-6
 FD_NOISE = 1e-14
 FP32_COND = 2e-6
+FP32_IMAGE = 2e-6
 GRAD_RTOL = 1e-4
 
 
 class FD:
     """One parameter's central difference and the floors of its check."""
 
-    def __init__(self, fd, usable, h, noise, cond):
-        self.fd, self.usable, self.h, self.noise, self.cond = fd, usable, h, noise, cond
+    def __init__(self, fd, usable, h, noise, cond, sens):
+        self.fd, self.usable, self.h, self.noise, self.cond, self.sens = fd, usable, h, noise, cond, sens
 
     def bound(self, single):
-        return GRAD_RTOL * abs(self.fd) + self.noise + (FP32_COND * self.cond if single else 0.0)
+        fp32 = FP32_COND * self.cond + FP32_IMAGE * self.sens if single else 0.0
+        return GRAD_RTOL * abs(self.fd) + self.noise + fp32
 
     def check(self, got, single, what=""):
         err = abs(got - self.fd)
         assert err <= self.bound(single), "%s: adjoint %.10g vs fd %.10g (err %.3g, 1e-4|fd| %.3g, noise %.3g, " \
-            "cond %.3g)" % (what, got, self.fd, err, GRAD_RTOL * abs(self.fd), self.noise, self.cond)
+            "cond %.3g, sens %.3g)" % (what, got, self.fd, err, GRAD_RTOL * abs(self.fd), self.noise, self.cond,
+                                       self.sens)
 
 
 def fd_gradients(render, profiles, names, data, sigma, smooth=False):
@@ -90,6 +97,7 @@ def fd_gradients(render, profiles, names, data, sigma, smooth=False):
     cot = 2 * (img0 - data) / sigma ** 2
     chi0 = float(np.sum(((img0 - data) / sigma) ** 2))
     scale = float(np.sum(np.abs(cot * img0)))
+    msens = 2 * np.abs(img0) / sigma ** 2
 
     def chi(img):
         return float(np.sum(((img - data) / sigma) ** 2))
@@ -101,7 +109,9 @@ def fd_gradients(render, profiles, names, data, sigma, smooth=False):
         ip, cp = render(with_param(profiles, i, k, v + h))
         im, cm = render(with_param(profiles, i, k, v - h))
         fd = (chi(ip) - chi(im)) / (2 * h)
-        cond = float(np.sum(np.abs(cot * (ip - im) / (2 * h))))
+        dm = np.abs(ip - im) / (2 * h)
+        cond = float(np.sum(np.abs(cot) * dm))
+        sens = float(np.sum(msens * dm))
         usable = np.array_equal(cp, counts0) and np.array_equal(cm, counts0)
         noise = FD_NOISE * scale / h
         if smooth and usable:
@@ -109,7 +119,7 @@ def fd_gradients(render, profiles, names, data, sigma, smooth=False):
             im2, _ = render(with_param(profiles, i, k, v - h / 10))
             fd2 = (chi(ip2) - chi(im2)) / (2 * h / 10)
             usable = abs(fd - fd2) <= 2e-5 * abs(fd) + 10 * noise
-        out[(i, k)] = FD(fd, usable, h, noise, cond)
+        out[(i, k)] = FD(fd, usable, h, noise, cond, sens)
     return chi0, out
 
 

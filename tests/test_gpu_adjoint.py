@@ -6,9 +6,11 @@ data = the oracle's image at parameters perturbed by 5 %, plus noise. The
 gradient with respect to all 17 parameters (8 per sersic, bg) must match
 central differences of the oracle's chi^2 with h = 1e-6 relative, by the
 criterion of tests/helpers.py:
-  |g - fd| <= 1e-4 |fd| + 1e-14 sum|c m| / h (+ 2e-6 sum|c dm/dpar| in FP32)
-(the second term the differences' own rounding, the third the scale of the
-sum an FP32 gradient is; c = 2 (m - d) / sigma^2).
+  |g - fd| <= 1e-4 |fd| + 1e-14 sum|c m| / h
+              (+ 2e-6 sum|c dm/dpar| + 2e-6 sum 2|m dm/dpar| / sigma^2 in FP32)
+(the second term the differences' own rounding, the others the scale of the
+sum an FP32 gradient is and its sensitivity to the FP32 image's relative
+error; c = 2 (m - d) / sigma^2).
 Parameters whose finite difference changes the oracle's subsampling tree
 (level counts at +-h differ) are excluded, as the adjoint holds the tree
 fixed; the test asserts that at least 15 of the 17 remain.

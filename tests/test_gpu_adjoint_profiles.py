@@ -8,7 +8,8 @@ parameter of the profile (xcen, ycen, mag, ang, axrat, box and the kind's own)
 and the sky's bg must match central differences of the oracle's chi^2 with
 h = 1e-6 relative, by the criterion of tests/helpers.py (that of the sersic
 adjoint test):
-  |g - fd| <= 1e-4 |fd| + 1e-14 sum|c m| / h (+ 2e-6 sum|c dm/dpar| in FP32)
+  |g - fd| <= 1e-4 |fd| + 1e-14 sum|c m| / h
+              (+ 2e-6 sum|c dm/dpar| + 2e-6 sum 2|m dm/dpar| / sigma^2 in FP32)
 Parameters whose finite difference is not that of a smooth function are
 excluded (at most two per case): those whose +-h changes the oracle's
 subsampling tree (level counts), which the adjoint holds fixed, and those

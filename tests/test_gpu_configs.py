@@ -12,9 +12,12 @@ would take hours, so the size-independent properties are checked here:
   * cfg4: 1024 models of 256 x 256 (sersic bulge + disk, 25 x 25 PSF), one
     FP32 batch with the adjoint: flux, pixels, chi^2 and all 16 gradients of
     every 32nd model against the FP64 path: |g32 - g64| <= 1e-4 |g64| +
-    2e-6 sum_p |c_p dm_p/dpar| (the scale of the sum the gradient is, from
-    central differences of the FP64 path; c = 2 (m - d) / sigma^2), for every
-    parameter whose +-1e-6 differences keep the subsampling tree;
+    2e-6 sum_p |c_p dm_p/dpar| + 2e-6 sum_p 2 |m_p dm_p/dpar| / sigma_p^2 (the
+    scale of the sum the gradient is, and its sensitivity to the FP32 image's
+    relative error, from central differences of the FP64 path; c = 2 (m - d)
+    / sigma^2), for every parameter whose +-1e-6 differences keep the
+    subsampling tree (the data here are the FP32 images with 1 % noise, so
+    the residuals are small and the second floor is the larger);
   * cfg5: the 4096 x 4096 crowded field (10,000 profiles and a sky, 101 x 101
     PSF by an 8192 x 8192 FP32 FFT) against the FP64 path with the direct
     convolution: flux <= 1e-5, pixels above 1e-3 x peak <= 1e-4, every pixel
@@ -24,6 +27,11 @@ import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+# FP32 gradient floors (tests/helpers.py): on the scale of the gradient's sum
+# and on its sensitivity to the FP32 image's relative error
+FP32_C = 2e-6
+FP32_M = 2e-6
 
 
 @pytest.fixture(scope="module")
@@ -115,19 +123,27 @@ def test_cfg4_full_batch_with_gradients(envs):
     i32, i64 = img32.cpu().numpy().astype(np.float64), img64.cpu().numpy()
     G32, G64 = g32.cpu().numpy().reshape(-1, 12), g64.cpu().numpy().reshape(-1, 12)
     c32, c64 = chi32.cpu().numpy(), chi64.cpu().numpy()
-    scale, same = W.gradient_scales([specs[i] for i in pick], W.param_matrix([specs[i] for i in pick]), i64,
-                                    data[sel], sigma[sel], env64)
+    scale_c, scale_m, same = W.gradient_scales([specs[i] for i in pick], W.param_matrix([specs[i] for i in pick]),
+                                               i64, data[sel], sigma[sel], env64)
     assert same.mean() >= 0.85  # +-1e-6 changes the tree of ~7 % of the parameters here
+    G32p = np.concatenate([G32[2 * i:2 * i + 2, :8] for i in pick])
+    G64p = G64[:, :8]
+    err = np.abs(G32p - G64p)
+    print("cfg4 gradients: err/scale_c max %.3g, err/scale_m max %.3g, err/(1e-4|g|) max %.3g" % (
+        (err / scale_c)[same].max(), (err / scale_m)[same].max(), (err / (1e-4 * np.abs(G64p)))[same].max()))
     for j, i in enumerate(pick):
         a = i32[b32.offsets[i]:b32.offsets[i + 1]]
         r = i64[b64.offsets[j]:b64.offsets[j + 1]]
         _check(a, r, "model %d" % i)
-        assert abs(c32[i] - c64[j]) <= 1e-5 * c64[j]
+        # chi^2 is ~0.3 here (residuals of 1 % of the image against sigma = 1 % of
+        # the peak), so its relative error is the FP32 image's, not the 1e-5 of
+        # the fitting workload
+        assert abs(c32[i] - c64[j]) <= 1e-4 * c64[j]
         ga, gr = G32[2 * i:2 * i + 2, :8], G64[2 * j:2 * j + 2, :8]
-        sc, ok = scale[2 * j:2 * j + 2], same[2 * j:2 * j + 2]
-        bound = 1e-4 * np.abs(gr) + 2e-6 * sc
+        sc, sm, ok = scale_c[2 * j:2 * j + 2], scale_m[2 * j:2 * j + 2], same[2 * j:2 * j + 2]
+        bound = 1e-4 * np.abs(gr) + FP32_C * sc + FP32_M * sm
         bad = ok & (np.abs(ga - gr) > bound)
-        assert not bad.any(), "model %d: %s vs %s (scale %s)" % (i, ga[bad], gr[bad], sc[bad])
+        assert not bad.any(), "model %d: %s vs %s (scales %s, %s)" % (i, ga[bad], gr[bad], sc[bad], sm[bad])
 
 
 def test_cfg5_crowded_field(envs):

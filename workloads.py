@@ -167,22 +167,26 @@ def param_matrix(specs):
 
 
 def gradient_scales(specs, par, images, data, sigma, env64, h_rel=1e-6, n_par=8):
-    """The scale of each chi^2 gradient component: sum_p |c_p dm_p / dpar|,
-    c = 2 (m - d) / sigma^2 at the parameters `par` (n_profiles x 12, batch
-    order of `specs`), dm/dpar by central differences (h = h_rel x |par|,
-    at least h_rel x 1e-3) of the plain FP64 path. `images`, `data`, `sigma`:
-    the models' output images back to back (numpy, float64). An FP32
-    gradient carries rounding of a few units of 2^-24 on this scale, whatever
-    the component's own size.
+    """Two scales of each chi^2 gradient component, from central differences
+    (h = h_rel x |par|, at least h_rel x 1e-3) of the plain FP64 path at the
+    parameters `par` (n_profiles x 12, batch order of `specs`):
+      sum_p |c_p dm_p/dpar|, c = 2 (m - d) / sigma^2: the sum the gradient is;
+      sum_p 2 |m_p dm_p/dpar| / sigma_p^2: its sensitivity to relative errors
+      of the model image m itself.
+    An FP32 gradient carries rounding of a few units of 2^-24 on the first
+    (its own arithmetic) and on the second times the FP32 image's relative
+    error, whatever the component's own size. `images`, `data`, `sigma`: the
+    models' FP64 output images back to back (numpy, float64).
 
-    Returns (scale, same_tree), both n_profiles x n_par: same_tree is False
-    where the +-h images of a parameter do not keep the subsampling tree
-    (per-level counts differ from the unperturbed model's), so that the
+    Returns (scale_c, scale_m, same_tree), each n_profiles x n_par: same_tree
+    is False where the +-h images of a parameter do not keep the subsampling
+    tree (per-level counts differ from the unperturbed model's), so that the
     difference is not a derivative there."""
     import torch
     import libprofit_gb300 as pg
     first = np.cumsum([0] + [len(s["profiles"]) for s in specs])
-    scale = np.zeros((int(first[-1]), n_par))
+    scale_c = np.zeros((int(first[-1]), n_par))
+    scale_m = np.zeros((int(first[-1]), n_par))
     same = np.ones((int(first[-1]), n_par), dtype=bool)
     out_off = np.cumsum([0] + [s["width"] * s["height"] for s in specs])
     for i, s in enumerate(specs):
@@ -208,12 +212,15 @@ def gradient_scales(specs, par, images, data, sigma, env64, h_rel=1e-6, n_par=8)
         b.close()
         a, z = out_off[i], out_off[i + 1]
         cot = 2 * (images[a:z] - data[a:z]) / sigma[a:z] ** 2
+        msens = 2 * np.abs(images[a:z]) / sigma[a:z] ** 2
         q = 0
         for j in range(n):
             for k in range(n_par):
                 up, dn = 1 + 2 * q, 2 + 2 * q
-                scale[first[i] + j, k] = np.sum(np.abs(cot * (im[up] - im[dn]) / (2 * hs[q])))
+                dm = np.abs(im[up] - im[dn]) / (2 * hs[q])
+                scale_c[first[i] + j, k] = np.sum(np.abs(cot) * dm)
+                scale_m[first[i] + j, k] = np.sum(msens * dm)
                 same[first[i] + j, k] = all(np.array_equal(counts[r * n + jj], counts[jj])
                                             for r in (up, dn) for jj in range(n))
                 q += 1
-    return scale, same
+    return scale_c, scale_m, same
