@@ -158,6 +158,9 @@ typedef struct pf_batch pf_batch;
 #define PF_ENV_NO_AUTOTUNE 0x4u  /* single precision, PF_CONV_AUTO: choose brute force or FFT and
                                     the direct block shape by the fixed cost model, never by
                                     timing candidates on the device (reproducible choices) */
+#define PF_ENV_NO_SPLIT 0x8u     /* single precision: walk every subsampled pixel's tree in the
+                                    warp that meets it, none split off to other warps (the
+                                    images then sum each pixel's profiles strictly in order) */
 
 /* Per-stage device times accumulated since the last reset (PF_ENV_PROFILE). */
 typedef struct pf_stage_times {

@@ -219,13 +219,15 @@ class CUDAEnv:
     """A CUDA environment (get_opencl_environment analogue). use_double selects
     the plain FP64 path (the reference's arithmetic and subsampling decisions);
     profile, per-stage CUDA-event timing; autotune=False, the fixed cost model
-    for the automatic convolution choice of large single-precision batches."""
+    for the automatic convolution choice of large single-precision batches;
+    split=False, every subsampled pixel's tree walked by the warp that meets
+    it (single precision; PF_ENV_NO_SPLIT)."""
 
-    def __init__(self, device=0, use_double=True, profile=False, autotune=True):
+    def __init__(self, device=0, use_double=True, profile=False, autotune=True, split=True):
         lib = _ffi.load()
         h = ctypes.c_void_p()
         flags = (_ffi.PF_ENV_DOUBLE if use_double else 0) | (_ffi.PF_ENV_PROFILE if profile else 0) | \
-            (0 if autotune else _ffi.PF_ENV_NO_AUTOTUNE)
+            (0 if autotune else _ffi.PF_ENV_NO_AUTOTUNE) | (0 if split else _ffi.PF_ENV_NO_SPLIT)
         _check(lib.pf_env_create(int(device), flags, ctypes.byref(h)))
         self._h = h
         self.device = device
@@ -247,8 +249,8 @@ class CUDAEnv:
             pass
 
 
-def get_cuda_environment(device=0, use_double=True, profile=False, autotune=True):
-    return CUDAEnv(device, use_double, profile, autotune)
+def get_cuda_environment(device=0, use_double=True, profile=False, autotune=True, split=True):
+    return CUDAEnv(device, use_double, profile, autotune, split)
 
 
 _default_env = None

@@ -62,6 +62,7 @@ class StageTimes(ctypes.Structure):
 
 PF_ENV_PROFILE = 0x2
 PF_ENV_NO_AUTOTUNE = 0x4
+PF_ENV_NO_SPLIT = 0x8
 
 _P = ctypes.c_void_p
 _SIGNATURES = {

@@ -246,26 +246,19 @@ __device__ void eval_frame_m(const ProfileDev &P, const f32::Shape &sh, WarpScra
 	__syncwarp();
 }
 
-// subsample_pixel on a box given relative to the profile centre
+// The depth-first walk of subsample_pixel below frame L0 of the warp's
+// scratch, which has been evaluated (its total holds its accepted sub-points,
+// its mask the failing ones): each failing sub-point's box evaluated and
+// walked in ascending order, its value added to the frame's total. Returns
+// the frame's value, total / res^2; `deepest`: the deepest level + 1 reached.
 template <unsigned int KINDS>
-__device__ float warp_subsample_m(const ProfileDev &P, const f32::Shape &sh, WarpScratchM &ws, float xhi, float xlo,
-                                  float yhi, float ylo, float bx, float by, unsigned int res, unsigned int max_rec,
-                                  int lane, unsigned long long *counts, int &deepest)
+__device__ float warp_walk_m(const ProfileDev &P, const f32::Shape &sh, WarpScratchM &ws, int L0, unsigned int res,
+                             unsigned int max_rec, int lane, unsigned long long *counts, int &deepest)
 {
-	if (lane == 0) {
-		ws.fr[0].xhi = xhi;
-		ws.fr[0].xlo = xlo;
-		ws.fr[0].yhi = yhi;
-		ws.fr[0].ylo = ylo;
-		ws.fr[0].bx = bx;
-		ws.fr[0].by = by;
-	}
-	__syncwarp();
 	const float inv_res = __frcp_rn((float)res);
 	const float inv_res2 = __frcp_rn((float)(res * res));
-	int L = 0;
-	deepest = 1;
-	eval_frame_m<KINDS>(P, sh, ws, 0, res, inv_res, max_rec, lane, counts);
+	int L = L0;
+	deepest = L0 + 1;
 	const unsigned int nwords = (res * res + 31) / 32;
 	while (true) {
 		FrameM &f = ws.fr[L];
@@ -299,7 +292,7 @@ __device__ float warp_subsample_m(const ProfileDev &P, const f32::Shape &sh, War
 		}
 		else {
 			const float v = f.total * inv_res2;
-			if (L == 0) {
+			if (L == L0) {
 				return v;
 			}
 			L--;
@@ -309,6 +302,133 @@ __device__ float warp_subsample_m(const ProfileDev &P, const f32::Shape &sh, War
 	}
 }
 
+// Frame L of the warp's scratch set to a box relative to the profile centre
+__device__ __forceinline__ void set_frame(WarpScratchM &ws, int L, float xhi, float xlo, float yhi, float ylo, float bx,
+                                          float by, int lane)
+{
+	if (lane == 0) {
+		ws.fr[L].xhi = xhi;
+		ws.fr[L].xlo = xlo;
+		ws.fr[L].yhi = yhi;
+		ws.fr[L].ylo = ylo;
+		ws.fr[L].bx = bx;
+		ws.fr[L].by = by;
+	}
+	__syncwarp();
+}
+
+// Exports the failing sub-points of the evaluated level-0 frame of a
+// subsampled drawing pixel as level-1 boxes of the split pool (SplitPool in
+// pf_device.cuh). Returns false, having exported nothing, when fewer than
+// pool.min_fail sub-points fail or the pool has no room; the caller then walks
+// the tree itself. Warp-uniform; lane `src` holds the pixel, whose split
+// record (prec) and last split root (plast) are updated.
+__device__ bool split_root(const SplitPool &pool, const ProfileDev &P, int pi, const ModelDev &m, WarpScratchM &ws,
+                           unsigned int res, unsigned int max_rec, int lane, int src, long long canvas_idx,
+                           long long depth_idx, int &prec, int &plast)
+{
+	const FrameM &f = ws.fr[0];
+	const unsigned int nwords = (res * res + 31) / 32;
+	unsigned int nf = 0;
+	for (unsigned int w = 0; w < nwords; w++) nf += __popc(f.mask[w]);
+	if (nf == 0 || nf < pool.min_fail) return false;
+	const int old_prec = __shfl_sync(0xffffffffu, prec, src), old_last = __shfl_sync(0xffffffffu, plast, src);
+	int p = old_prec, r = -1;
+	unsigned int b0 = 0, ok = 1;
+	if (lane == 0) {
+		if (p < 0) {
+			const unsigned int q = atomicAdd(&pool.cnt[2], 1u);
+			if (q < pool.cap_pix) p = (int)q;
+			else ok = 0;
+		}
+		if (ok) {
+			const unsigned int q = atomicAdd(&pool.cnt[1], 1u);
+			if (q < pool.cap_root) r = (int)q;
+			else ok = 0;
+		}
+		if (ok) {
+			// room for nf boxes, taken without passing the capacity (a lock-free
+			// retry: each failed exchange means another warp took room)
+			ok = 0;
+			unsigned int old = *(volatile unsigned int *)&pool.cnt[0];
+			for (int tries = 0; tries < (1 << 16) && old <= pool.cap_box && pool.cap_box - old >= nf; tries++) {
+				const unsigned int got = atomicCAS(&pool.cnt[0], old, old + nf);
+				if (got == old) {
+					b0 = old;
+					ok = 1;
+					break;
+				}
+				old = got;
+			}
+		}
+		if (!ok) atomicAdd(&pool.cnt[4], 1u);
+	}
+	if (!__shfl_sync(0xffffffffu, ok, 0)) return false;
+	p = __shfl_sync(0xffffffffu, p, 0);
+	r = __shfl_sync(0xffffffffu, r, 0);
+	b0 = __shfl_sync(0xffffffffu, b0, 0);
+	if (lane == 0) {
+		SplitRoot &R = pool.root[r];
+		R.accepted = f.total;
+		R.first_box = b0;
+		R.n_boxes = nf;
+		R.pending = nf;
+		R.profile = pi;
+		R.pixel = p;
+		R.next = -1;
+		R.depth = 1;
+		R.res = res;
+		R.fflux = P.fflux_scale;
+		R.convolve = P.convolve;
+		R.value = 0.f;
+		R.depth_idx = depth_idx;
+		SplitPixel &X = pool.pix[p];
+		if (old_prec < 0) {
+			X.idx = canvas_idx;
+			X.s_conv = X.s_direct = 0.f;
+			X.first_root = r;
+			X.pending = 1;
+			X.conv_required = m.conv_required;
+		}
+		else {
+			pool.root[old_last].next = r;
+			X.pending += 1;
+		}
+	}
+	// the boxes in ascending sub-point order, placed as the walk would place
+	// its child frames
+	const float inv_res = __frcp_rn((float)res);
+	const float cbx = f.bx * inv_res, cby = f.by * inv_res;
+	const unsigned int magic = res_magic(res);
+	const uint32_t meta = res | (1u << 8) | (max_rec << 16);
+	unsigned int rank = 0;
+	for (unsigned int w = 0; w < nwords; w++) {
+		const unsigned int bits = f.mask[w];
+		if ((bits >> lane) & 1u) {
+			const unsigned int k = w * 32 + (unsigned int)lane;
+			const unsigned int i = div_res(k, magic), j = k - i * res;
+			SplitBox bx;
+			float e;
+			two_sum(f.xhi, small_int_to_float(i) * cbx, bx.xhi, e);
+			bx.xlo = f.xlo + e;
+			two_sum(f.yhi, small_int_to_float(j) * cby, bx.yhi, e);
+			bx.ylo = f.ylo + e;
+			bx.bx = cbx;
+			bx.by = cby;
+			bx.root = r;
+			bx.meta = meta;
+			pool.box[b0 + rank + __popc(bits & ((1u << lane) - 1u))] = bx;
+		}
+		rank += __popc(bits);
+	}
+	__syncwarp();
+	if (lane == src) {
+		prec = p;
+		plast = r;
+	}
+	return true;
+}
+
 // One 32-pixel row tile of a model's drawing area: every profile of the model
 // in order, summed into the conv / direct images. KINDS: the radial profile
 // kinds of the batch.
@@ -316,7 +436,7 @@ template <unsigned int KINDS>
 __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, int n_models,
                                           const ProfileDev *__restrict__ profs, const double *__restrict__ psf_pool,
                                           float *__restrict__ conv_img, float *__restrict__ direct_img, long long tile,
-                                          WarpScratchM &ws, int lane, const DebugRec &dbg)
+                                          WarpScratchM &ws, int lane, const DebugRec &dbg, const SplitPool &pool)
 {
 	const int mi = find_model(models, n_models, tile);
 	const ModelDev &m = models[mi];
@@ -334,6 +454,10 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 	const float xl = fmaf(cx, m.fsx_hi, -xh) + cx * m.fsx_lo;
 	const float yl = fmaf(cy, m.fsy_hi, -yh) + cy * m.fsy_lo;
 	float acc_conv = 0.f, acc_direct = 0.f;
+	// this lane's pixel: its split record once a profile's subtrees are split
+	// off (SplitPool), and the last split profile's root
+	int prec = -1, plast = -1;
+	const long long canvas_idx = (long long)m.draw_off + (long long)row * m.draw_w + px;
 
 	for (int q0 = 0; q0 < m.n_profiles; q0 += 32) {
 		// 32 profiles' culling boxes tested at once, one per lane; the ones
@@ -373,7 +497,7 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 				beyond |= !in_mask;  // masked pixels are not evaluated (src/radial.cpp:305-307)
 				float pixel_val = 0.f;
 				int depth = 0;
-				bool need_ss = false;
+				bool need_ss = false, split = false;
 				if (beyond) {
 					depth = -1;
 				}
@@ -414,19 +538,30 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 					float bxh, bxl, byh, byl;
 					corner_pair(small_int_to_float(spx), m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
 					corner_pair(small_int_to_float(row), m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
+					// the level-0 box; its failing sub-points' subtrees split off to
+					// other warps, or walked here
+					set_frame(ws, 0, bxh, bxl, byh, byl, m.fsx_hi, m.fsy_hi, lane);
+					eval_frame_m<KINDS>(P, sh, ws, 0, res, __frcp_rn((float)res), max_rec, lane, counts);
+					const long long didx =
+					    dbg.depth ? P.depth_off + (long long)row * m.draw_w + (long long)spx : -1;
+					if (pool.box && split_root(pool, P, pi, m, ws, res, max_rec, lane, src,
+					                           (long long)m.draw_off + (long long)row * m.draw_w + spx, didx,
+					                           prec, plast)) {
+						if (lane == src) split = true;
+						continue;
+					}
 					int deepest = 0;
-					const float v = warp_subsample_m<KINDS>(P, sh, ws, bxh, bxl, byh, byl, m.fsx_hi, m.fsy_hi, res,
-					                                        max_rec, lane, counts, deepest);
+					const float v = warp_walk_m<KINDS>(P, sh, ws, 0, res, max_rec, lane, counts, deepest);
 					if (lane == src) {
 						pixel_val = v;
 						depth = deepest;
 					}
 				}
-				if (dbg.depth && active) {
+				if (dbg.depth && active && !split) {
 					dbg.depth[P.depth_off + (size_t)row * m.draw_w + px] = (int8_t)depth;
 				}
 				add = P.fflux_scale * pixel_val;
-				has = active;
+				has = active && !split;  // a split profile's value is added when its boxes finish
 			}
 			if (has) {
 				if (P.convolve) acc_conv += add;
@@ -435,9 +570,16 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 		}
 	}
 	if (active) {
-		const size_t idx = (size_t)m.draw_off + (size_t)row * m.draw_w + px;
-		if (m.conv_required) conv_img[idx] = acc_conv;
-		direct_img[idx] = acc_direct;
+		if (prec >= 0) {
+			// the split profiles' values are still to come: the warp that
+			// finishes the last of them writes the canvas
+			pool.pix[prec].s_conv = acc_conv;
+			pool.pix[prec].s_direct = acc_direct;
+		}
+		else {
+			if (m.conv_required) conv_img[canvas_idx] = acc_conv;
+			direct_img[canvas_idx] = acc_direct;
+		}
 	}
 }
 
@@ -475,7 +617,7 @@ __global__ void __launch_bounds__(kWarps32 * 32, PF_EVAL32_MIN_BLOCKS)
 eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const ProfileDev *__restrict__ profs,
                     unsigned int n_profiles, const double *__restrict__ psf_pool, float *__restrict__ conv_img,
                     float *__restrict__ direct_img, unsigned int n_tiles, unsigned int n_ring_items,
-                    unsigned int *counter, unsigned int *claims, DebugRec dbg)
+                    unsigned int *counter, unsigned int *claims, DebugRec dbg, SplitPool pool)
 {
 	__shared__ WarpScratchM scratch[kWarps32];
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -520,8 +662,74 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 			const int src = __ffs(todo) - 1;
 			todo &= todo - 1;
 			const long long t = __shfl_sync(0xffffffffu, tile, src);
-			eval_tile<KINDS>(models, n_models, profs, psf_pool, conv_img, direct_img, t, ws, lane, dbg);
+			eval_tile<KINDS>(models, n_models, profs, psf_pool, conv_img, direct_img, t, ws, lane, dbg, pool);
 		}
+	}
+}
+
+// Lane 0, box b of root r finished with value v (deepest level + 1 reached:
+// deepest): its value stored; the warp that finishes the root's last box forms
+// the pixel value in the walk's order (the level-0 box's accepted points, then
+// the boxes in ascending sub-point order) and, if it finishes the pixel's last
+// split profile, writes the pixel's canvas values.
+__device__ void finish_split_box(const SplitPool &pool, unsigned int b, int r, float v, int deepest,
+                                 float *__restrict__ conv_img, float *__restrict__ direct_img, const DebugRec &dbg)
+{
+	pool.box_val[b] = v;
+	SplitRoot &R = pool.root[r];
+	atomicMax(&R.depth, deepest);
+	__threadfence();
+	if (atomicSub(&R.pending, 1u) != 1u) return;
+	__threadfence();
+	const volatile float *vals = pool.box_val + R.first_box;
+	float total = R.accepted;
+	for (unsigned int j = 0; j < R.n_boxes; j++) total += vals[j];
+	const float value = R.fflux * (total * __frcp_rn((float)(R.res * R.res)));
+	*(volatile float *)&R.value = value;
+	if (R.depth_idx >= 0) dbg.depth[R.depth_idx] = (int8_t)atomicAdd(&R.depth, 0);
+	__threadfence();
+	SplitPixel &X = pool.pix[R.pixel];
+	if (atomicSub(&X.pending, 1u) != 1u) return;
+	__threadfence();
+	float c = X.s_conv, d = X.s_direct;
+	for (int q = X.first_root; q >= 0; q = pool.root[q].next) {
+		const float val = *(volatile const float *)&pool.root[q].value;
+		if (pool.root[q].convolve) c += val;
+		else d += val;
+	}
+	if (X.conv_required) conv_img[X.idx] = c;
+	direct_img[X.idx] = d;
+}
+
+// The split-off boxes (SplitPool), one per warp, each walked depth first
+// below its level; taken one at a time from the pool's work counter.
+template <unsigned int KINDS>
+__global__ void __launch_bounds__(kWarps32 * 32, PF_EVAL32_MIN_BLOCKS)
+split_boxes32_kernel(const ProfileDev *__restrict__ profs, float *__restrict__ conv_img,
+                     float *__restrict__ direct_img, SplitPool pool, DebugRec dbg)
+{
+	__shared__ WarpScratchM scratch[kWarps32];
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	WarpScratchM &ws = scratch[warp];
+	// final: the evaluation kernel, launched before, allocated them
+	const unsigned int n_boxes = min(*(volatile unsigned int *)&pool.cnt[0], pool.cap_box);
+	while (true) {
+		unsigned int b = 0;
+		if (lane == 0) b = atomicAdd(&pool.cnt[3], 1u);
+		b = __shfl_sync(0xffffffffu, b, 0);
+		if (b >= n_boxes) break;
+		const SplitBox bx = pool.box[b];
+		const int pi = pool.root[bx.root].profile;
+		const ProfileDev &P = profs[pi];
+		const f32::Shape sh = f32::load_shape(P);
+		const unsigned int res = bx.meta & 0xffu, level = (bx.meta >> 8) & 0xffu, max_rec = bx.meta >> 16;
+		unsigned long long *counts = dbg.counts ? dbg.counts + (size_t)pi * kLevelCounts : nullptr;
+		set_frame(ws, (int)level, bx.xhi, bx.xlo, bx.yhi, bx.ylo, bx.bx, bx.by, lane);
+		eval_frame_m<KINDS>(P, sh, ws, (int)level, res, __frcp_rn((float)res), max_rec, lane, counts);
+		int deepest = 0;
+		const float v = warp_walk_m<KINDS>(P, sh, ws, (int)level, res, max_rec, lane, counts, deepest);
+		if (lane == 0) finish_split_box(pool, b, bx.root, v, deepest, conv_img, direct_img, dbg);
+		__syncwarp();
 	}
 }
 
@@ -535,19 +743,28 @@ __global__ void psf_to_float_kernel(const double *in, float *out, long long n)
 
 void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs, int n_profiles,
                    const double *psf_pool, float *conv_img, float *direct_img, long long n_tiles,
-                   unsigned int *counter, unsigned int *claims, DebugRec dbg, bool sersic_only, int n_sm,
-                   cudaStream_t stream)
+                   unsigned int *counter, unsigned int *claims, DebugRec dbg, const SplitPool &pool, bool sersic_only,
+                   int n_sm, cudaStream_t stream)
 {
 	const unsigned int n_ring = (unsigned int)n_profiles * kRingRows * kRingCols;
+	const int blocks = n_sm * PF_EVAL32_MIN_BLOCKS;
 	if (sersic_only) {
-		eval_tiles32_kernel<f32::kSersicOnly><<<n_sm * PF_EVAL32_MIN_BLOCKS, kWarps32 * 32, 0, stream>>>(
+		eval_tiles32_kernel<f32::kSersicOnly><<<blocks, kWarps32 * 32, 0, stream>>>(
 		    models, n_models, profs, (unsigned int)n_profiles, psf_pool, conv_img, direct_img, (unsigned int)n_tiles,
-		    n_ring, counter, claims, dbg);
+		    n_ring, counter, claims, dbg, pool);
+		if (pool.box) {
+			split_boxes32_kernel<f32::kSersicOnly><<<blocks, kWarps32 * 32, 0, stream>>>(profs, conv_img, direct_img,
+			                                                                             pool, dbg);
+		}
 	}
 	else {
-		eval_tiles32_kernel<f32::kAllKinds><<<n_sm * PF_EVAL32_MIN_BLOCKS, kWarps32 * 32, 0, stream>>>(
+		eval_tiles32_kernel<f32::kAllKinds><<<blocks, kWarps32 * 32, 0, stream>>>(
 		    models, n_models, profs, (unsigned int)n_profiles, psf_pool, conv_img, direct_img, (unsigned int)n_tiles,
-		    n_ring, counter, claims, dbg);
+		    n_ring, counter, claims, dbg, pool);
+		if (pool.box) {
+			split_boxes32_kernel<f32::kAllKinds><<<blocks, kWarps32 * 32, 0, stream>>>(profs, conv_img, direct_img,
+			                                                                          pool, dbg);
+		}
 	}
 }
 

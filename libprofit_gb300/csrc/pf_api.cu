@@ -38,7 +38,7 @@ void launch_flux_sum(const ModelDev *models, int n_models, const void *images, i
 void launch_set_params(ProfileDev *profs, int n_profiles, const double *params, cudaStream_t stream);
 void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs, int n_profiles,
                    const double *psf_pool, float *conv_img, float *direct_img, long long n_tiles,
-                   unsigned int *counter, unsigned int *claims, DebugRec dbg, bool sersic_only, int n_sm,
+                   unsigned int *counter, unsigned int *claims, DebugRec dbg, const SplitPool &pool, bool sersic_only, int n_sm,
                    cudaStream_t stream);
 long long eval32_items(long long n_profiles, long long n_tiles);
 int fft32_rows_per_job(int n);
@@ -342,6 +342,9 @@ struct pf_batch {
 	size_t draw_total = 0;
 	unsigned int *d_counter = nullptr;
 	unsigned int *d_claims = nullptr;   // FP32 eval: one bit per tile, set by the warp that evaluates it
+	// FP32 eval: sub-pixel boxes split off to other warps (pf::SplitPool); no
+	// pool (box == nullptr) for FP64 batches and PF_ENV_NO_SPLIT
+	pf::SplitPool split{};
 	bool sersic_only = false;           // every radial profile is a sersic: the FP32 kernels drop the other kinds
 	unsigned int *d_err = nullptr;
 	double *d_solves = nullptr;  // per profile: the inverse-gamma solves of the setup
@@ -419,6 +422,13 @@ struct pf_batch {
 };
 
 namespace {
+
+// Failing level-0 sub-points from which a subsampled pixel's subtrees are split
+// off to other warps (FP32 evaluation)
+#ifndef PF_SPLIT_MIN_FAIL
+#define PF_SPLIT_MIN_FAIL 1
+#endif
+constexpr unsigned int kSplitMinFail = PF_SPLIT_MIN_FAIL;
 
 enum Stage { ST_SETUP = 0, ST_EVAL, ST_FINISH, ST_CHI2, ST_ADJCONV, ST_BACKWARD };
 
@@ -524,6 +534,10 @@ void pf_batch_destroy(pf_batch *b)
 	cudaFree(b->d_direct);
 	cudaFree(b->d_counter);
 	cudaFree(b->d_claims);
+	cudaFree(b->split.box);
+	cudaFree(b->split.box_val);
+	cudaFree(b->split.root);
+	cudaFree(b->split.pix);
 	cudaFree(b->d_err);
 	cudaFree(b->d_solves);
 	cudaFree(b->d_depth);
@@ -893,7 +907,8 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 
 	PF_CUDA_TRY(cudaMalloc(&b->d_models, sizeof(pf::ModelDev) * std::max<size_t>(1, n_models)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_profiles, sizeof(pf::ProfileDev) * std::max<size_t>(1, n_profiles)));
-	PF_CUDA_TRY(cudaMalloc(&b->d_counter, 2 * sizeof(unsigned int)));
+	// the eval kernels' two work counters, then the split pool's (reset by the setup kernel)
+	PF_CUDA_TRY(cudaMalloc(&b->d_counter, (2 + pf::kSplitCounters) * sizeof(unsigned int)));
 	b->sersic_only = true;
 	for (size_t i = 0; i < n_profiles; i++) {
 		const int k = b->h_profiles[i].kind;
@@ -904,6 +919,21 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 			return fail(PF_ERR_UNSUPPORTED, "batch too large for one single-precision evaluation pass");
 		}
 		PF_CUDA_TRY(cudaMalloc(&b->d_claims, sizeof(unsigned int) * (size_t)std::max<long long>(1, (b->n_tiles + 31) / 32)));
+		if (!(env->flags & PF_ENV_NO_SPLIT)) {
+			// room for a split record per drawing pixel up to 2^21 and 16 boxes per
+			// record up to 2^23 (about 470 MB at most); a split that finds no room
+			// is walked by the warp that meets it instead
+			pf::SplitPool &sp = b->split;
+			sp.cap_pix = (unsigned int)std::min<size_t>(std::max<size_t>(1, b->draw_total), 1u << 21);
+			sp.cap_root = sp.cap_pix;
+			sp.cap_box = (unsigned int)std::min<size_t>(std::max<size_t>(16 * (size_t)sp.cap_root, 1u << 16), 1u << 23);
+			sp.min_fail = kSplitMinFail;
+			PF_CUDA_TRY(cudaMalloc(&sp.box, sizeof(pf::SplitBox) * sp.cap_box));
+			PF_CUDA_TRY(cudaMalloc(&sp.box_val, sizeof(float) * sp.cap_box));
+			PF_CUDA_TRY(cudaMalloc(&sp.root, sizeof(pf::SplitRoot) * sp.cap_root));
+			PF_CUDA_TRY(cudaMalloc(&sp.pix, sizeof(pf::SplitPixel) * sp.cap_pix));
+			sp.cnt = b->d_counter + 2;
+		}
 	}
 	PF_CUDA_TRY(cudaMalloc(&b->d_err, sizeof(unsigned int)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_solves, sizeof(double) * 3 * std::max<size_t>(1, n_profiles)));
@@ -1352,7 +1382,7 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 		PF_CUDA_TRY(cudaMemsetAsync(b->d_claims, 0, sizeof(unsigned int) * (size_t)std::max<long long>(1, (b->n_tiles + 31) / 32),
 		                            stream));
 		pf::launch_eval32(b->d_models, n_models, b->d_profiles, n_profiles, b->d_psf_norm, (float *)b->d_conv,
-		                  (float *)b->d_direct, b->n_tiles, b->d_counter, b->d_claims, dbg, b->sersic_only,
+		                  (float *)b->d_direct, b->n_tiles, b->d_counter, b->d_claims, dbg, b->split, b->sersic_only,
 		                  b->env->n_sm, stream);
 		stage_end(b, t, stream);
 		t = stage_begin(b, ST_FINISH, stream);
@@ -1376,6 +1406,7 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 		uint64_t k = (n_profiles > 0 ? 2 : 1) + 1;  // setup (solves, profiles), evaluation
 		if (b->dbl) k += 1 + (b->any_fft ? 3 : 0) + (b->any_fft_downsample ? 1 : 0);  // finish, FFT passes
 		else {
+			k += b->split.box ? 1 : 0;  // the split boxes
 			k += b->n_out_tiles > 0 ? 1 : 0;
 			for (int pass = 0; b->any_fft && pass < 3; pass++) k += b->f32_jobs[0][pass].size();
 		}

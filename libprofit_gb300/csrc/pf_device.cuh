@@ -137,6 +137,62 @@ enum FParSlot : int {
 	FP_E_RB = 2, FP_E_A = 3, FP_E_INV_A = 4, FP_E_INV_H1 = 5, FP_E_EXPO = 6,
 };
 
+// Sub-pixel boxes split off the subsampling trees (FP32 path). A subsampled
+// pixel whose level-0 box (subsample_pixel's first call, src/radial.cpp:55-135)
+// fails the accuracy test at some sub-points does not walk their subtrees in
+// the warp that meets it: it exports them as level-1 boxes, which a later
+// kernel takes one per warp. The pixel's value is then formed as the
+// depth-first walk forms it -- the level-0 box's accepted points, then each
+// failing sub-point's subtree in ascending order -- by whichever warp
+// finishes the pixel's last box, and the pixel's canvas value (the tile's sum
+// of its other profiles, then the split profiles in profile order) by the
+// warp that finishes its last split profile. Counters, never waits.
+struct SplitBox {
+	float xhi, xlo, yhi, ylo;  // corner relative to the profile centre (unevaluated sums)
+	float bx, by;              // size
+	int32_t root;              // the SplitRoot it belongs to
+	uint32_t meta;             // res | level << 8 | max_rec << 16
+};
+
+struct SplitRoot {
+	float accepted;            // the level-0 box's accepted sub-points (warp sum)
+	uint32_t first_box, n_boxes;
+	uint32_t pending;          // boxes not finished
+	int32_t profile;
+	int32_t pixel;             // the SplitPixel of its drawing pixel
+	int32_t next;              // the pixel's next split profile (profile order), -1 none
+	int32_t depth;             // deepest level + 1 (depth map)
+	uint32_t res;
+	float fflux;               // the profile's flux scale
+	int32_t convolve;
+	float value;               // fflux x the pixel value, once complete
+	int64_t depth_idx;         // index into the depth maps, -1 when not recording
+};
+
+struct SplitPixel {
+	int64_t idx;               // canvas index (the model's draw_off + row x draw_w + column)
+	float s_conv, s_direct;    // the tile's sums of the profiles not split
+	int32_t first_root;        // split profiles, in profile order
+	uint32_t pending;          // split profiles not complete
+	int32_t conv_required;
+	int32_t pad;
+};
+
+// The device pool (sized at batch creation; box == nullptr: no splitting).
+// cnt: [0] boxes, [1] roots, [2] pixels allocated, [3] the box kernel's work
+// counter, [4] splits refused for lack of room (the tree then walked in place);
+// reset by the setup kernel.
+struct SplitPool {
+	SplitBox *box;
+	float *box_val;
+	SplitRoot *root;
+	SplitPixel *pix;
+	unsigned int *cnt;
+	unsigned int cap_box, cap_root, cap_pix;
+	unsigned int min_fail;     // failing level-0 sub-points for a split
+};
+constexpr int kSplitCounters = 8;
+
 struct DebugRec {
 	int8_t *depth;             // per profile drawing-area depth maps, or nullptr
 	unsigned long long *counts;// n_profiles * kLevelCounts, or nullptr

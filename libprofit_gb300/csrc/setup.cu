@@ -511,8 +511,9 @@ __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs,
                                       unsigned int *err)
 {
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
-		tile_counter[0] = 0;  // the eval kernels' work counters (two: the FP32 one's phases)
-		tile_counter[1] = 0;
+		// the eval kernels' work counters (two: the FP32 one's phases), then the
+		// FP32 path's split-box pool counters (SplitPool::cnt)
+		for (int i = 0; i < 2 + kSplitCounters; i++) tile_counter[i] = 0;
 	}
 	const int t = blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= n_profiles) {
