@@ -352,6 +352,15 @@ PF_API pf_status pf_batch_drawing_dims(pf_batch *batch, uint32_t *dims);
 PF_API pf_status pf_batch_conv_info(const pf_batch *batch, int32_t *forward_shape, int32_t *adjoint_shape,
                                     uint32_t *fft_models);
 
+/* No counterpart: how the last single-precision forward pass spread its
+ * subsampling trees. boxes: sub-pixel boxes split off to other warps; roots:
+ * (profile, pixel) trees they came from; pixels: drawing pixels with at least
+ * one; refused: splits walked in place for lack of room in the batch's pool.
+ * Synchronises the batch's stream (stream as in pf_forward). All zero for
+ * PF_ENV_DOUBLE and PF_ENV_NO_SPLIT environments. Any argument may be NULL. */
+PF_API pf_status pf_batch_split_info(pf_batch *batch, void *stream, uint32_t *boxes, uint32_t *roots,
+                                     uint32_t *pixels, uint32_t *refused);
+
 /* FITS images on either side of the path (host only, no device work): the
  * PSFs a caller reads in and the images it writes out.
  *

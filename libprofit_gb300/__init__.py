@@ -579,6 +579,13 @@ class Batch:
         _check(_ffi.load().pf_batch_conv_info(self._h, ctypes.byref(f), ctypes.byref(a), ctypes.byref(n)))
         return {"forward_shape": f.value, "adjoint_shape": a.value, "fft_models": n.value}
 
+    def split_info(self, stream=None):
+        """How the last single-precision forward pass spread its subsampling
+        trees: {"boxes", "roots", "pixels", "refused"} (pf_batch_split_info)."""
+        v = [ctypes.c_uint32() for _ in range(4)]
+        _check(_ffi.load().pf_batch_split_info(self._h, _stream_arg(stream), *[ctypes.byref(x) for x in v]))
+        return dict(zip(("boxes", "roots", "pixels", "refused"), (x.value for x in v)))
+
     def enable_adjoint(self):
         """Sizes the adjoint's device buffers (pf_batch_enable_adjoint)."""
         _check(_ffi.load().pf_batch_enable_adjoint(self._h))

@@ -909,6 +909,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 	PF_CUDA_TRY(cudaMalloc(&b->d_profiles, sizeof(pf::ProfileDev) * std::max<size_t>(1, n_profiles)));
 	// the eval kernels' two work counters, then the split pool's (reset by the setup kernel)
 	PF_CUDA_TRY(cudaMalloc(&b->d_counter, (2 + pf::kSplitCounters) * sizeof(unsigned int)));
+	PF_CUDA_TRY(cudaMemset(b->d_counter, 0, (2 + pf::kSplitCounters) * sizeof(unsigned int)));
 	b->sersic_only = true;
 	for (size_t i = 0; i < n_profiles; i++) {
 		const int k = b->h_profiles[i].kind;
@@ -1477,6 +1478,26 @@ pf_status pf_batch_conv_info(const pf_batch *b, int32_t *forward_shape, int32_t 
 		for (const auto &m : b->mdev) n += m.use_fft ? 1u : 0u;
 		*fft_models = n;
 	}
+	return PF_OK;
+}
+
+pf_status pf_batch_split_info(pf_batch *b, void *stream_ptr, uint32_t *boxes, uint32_t *roots, uint32_t *pixels,
+                              uint32_t *refused)
+{
+	if (!b) return fail(PF_ERR_INVALID_PARAMETER, "batch is NULL");
+	uint32_t c[pf::kSplitCounters] = {};
+	if (b->split.box) {
+		cudaStream_t stream = stream_ptr ? (cudaStream_t)stream_ptr : b->env->stream;
+		PF_CUDA_TRY(cudaSetDevice(b->env->device));
+		PF_CUDA_TRY(cudaStreamSynchronize(stream));
+		PF_CUDA_TRY(cudaMemcpy(c, b->split.cnt, sizeof(c), cudaMemcpyDeviceToHost));
+		c[1] = std::min(c[1], b->split.cap_root);  // failed allocations counted past the capacity
+		c[2] = std::min(c[2], b->split.cap_pix);
+	}
+	if (boxes) *boxes = c[0];
+	if (roots) *roots = c[1];
+	if (pixels) *pixels = c[2];
+	if (refused) *refused = c[4];
 	return PF_OK;
 }
 
