@@ -356,8 +356,10 @@ PF_API pf_status pf_batch_conv_info(const pf_batch *batch, int32_t *forward_shap
  * subsampling trees. boxes: sub-pixel boxes split off to other warps; roots:
  * (profile, pixel) trees they came from; pixels: drawing pixels with at least
  * one; refused: splits walked in place for lack of room in the batch's pool.
- * Synchronises the batch's stream (stream as in pf_forward). All zero for
- * PF_ENV_DOUBLE and PF_ENV_NO_SPLIT environments. Any argument may be NULL. */
+ * Synchronises the batch's stream (stream as in pf_forward). All zero when
+ * the batch does not split its trees: PF_ENV_DOUBLE and PF_ENV_NO_SPLIT
+ * environments, and large automatic batches whose evaluation the autotuner
+ * timed faster with every tree walked where met. Any argument may be NULL. */
 PF_API pf_status pf_batch_split_info(pf_batch *batch, void *stream, uint32_t *boxes, uint32_t *roots,
                                      uint32_t *pixels, uint32_t *refused);
 

@@ -581,6 +581,7 @@ struct HostFftJob {
 struct ConvPlan {
 	int shape = -1;                         // direct convolution block shape; -1: least tile area
 	const std::vector<int8_t> *auto_fft = nullptr;  // per model, PF_CONV_AUTO: 1 FFT, 0 direct
+	bool split = true;                      // single precision: a split pool unless PF_ENV_NO_SPLIT
 };
 
 // The convolution block shape covering the given images with the least tile area.
@@ -920,7 +921,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 			return fail(PF_ERR_UNSUPPORTED, "batch too large for one single-precision evaluation pass");
 		}
 		PF_CUDA_TRY(cudaMalloc(&b->d_claims, sizeof(unsigned int) * (size_t)std::max<long long>(1, (b->n_tiles + 31) / 32)));
-		if (!(env->flags & PF_ENV_NO_SPLIT)) {
+		if (!(env->flags & PF_ENV_NO_SPLIT) && plan.split) {
 			// room for a split record per drawing pixel up to 2^21 and 16 boxes per
 			// record up to 2^23 (about 470 MB at most); a split that finds no room
 			// is walked by the warp that meets it instead
@@ -1115,6 +1116,43 @@ static double time_forward_conv(pf_batch *b, int shape, bool fft, float *out)
 	return cudaGetLastError() == cudaSuccess ? best : -1;
 }
 
+// Autotuner timing (ms, best of three after a warm-up) of a single-precision
+// batch's setup and evaluation passes, with its subsampling trees split off
+// to other warps (split) or walked where met.
+static double time_eval(pf_batch *b, bool split)
+{
+	cudaStream_t st = b->env->stream;
+	const int n_models = (int)b->mdev.size(), n_profiles = (int)b->profiles.size();
+	if (b->params_dirty) {
+		if (cudaMemcpyAsync(b->d_profiles, b->h_profiles, sizeof(pf::ProfileDev) * std::max(1, n_profiles),
+		                    cudaMemcpyHostToDevice, st) != cudaSuccess) return -1;
+		b->params_dirty = false;
+	}
+	const pf::SplitPool pool = split ? b->split : pf::SplitPool{};
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	double best = -1;
+	for (int rep = 0; rep < 4; rep++) {
+		cudaEventRecord(e0, st);
+		pf::launch_setup(b->d_models, b->d_profiles, n_profiles, n_models, b->d_counter, b->d_err, nullptr, nullptr,
+		                 false, b->d_solves, b->adjoint ? 1 : 0, st);
+		cudaMemsetAsync(b->d_claims, 0, sizeof(unsigned int) * (size_t)std::max<long long>(1, (b->n_tiles + 31) / 32),
+		                st);
+		pf::launch_eval32(b->d_models, n_models, b->d_profiles, n_profiles, b->d_psf_norm, (float *)b->d_conv,
+		                  (float *)b->d_direct, b->n_tiles, b->d_counter, b->d_claims, pf::DebugRec{nullptr, nullptr},
+		                  pool, b->sersic_only, b->env->n_sm, st);
+		cudaEventRecord(e1, st);
+		cudaEventSynchronize(e1);
+		float ms = 0;
+		cudaEventElapsedTime(&ms, e0, e1);
+		if (rep > 0 && (best < 0 || ms < best)) best = ms;
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	return cudaGetLastError() == cudaSuccess ? best : -1;
+}
+
 // Autotuner timing (ms, best of three after a warm-up) of the adjoint direct
 // convolution of a batch with block shape `shape`, into its drawing-area
 // cotangent buffer.
@@ -1195,11 +1233,14 @@ pf_status pf_batch_create_masked(pf_env *env, const pf_model_desc *models, size_
 	// shape timed; built again with them on the FFT, timed; per model, the
 	// method whose fitted cost is lower (cost = seconds per unit of work,
 	// crop area x PSF area for the direct convolution, M_x M_y log2(M_x M_y)
-	// for the FFT, fitted to the two timings); the fastest shape.
+	// for the FFT, fitted to the two timings); the fastest shape; the
+	// evaluation's subsampling trees split off to other warps or not, whichever
+	// was faster.
 	std::vector<int8_t> none(n_models, 0), all(n_models, 1);
 	ConvPlan pd, pfft;
 	pd.auto_fft = &none;
 	pfft.auto_fft = &all;
+	pfft.split = false;  // only its FFT passes are timed
 	pf_batch *bd = nullptr, *bf = nullptr;
 	pf_status s = create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool,
 	                             mask_pool_len, pd, &bd);
@@ -1211,6 +1252,14 @@ pf_status pf_batch_create_masked(pf_env *env, const pf_model_desc *models, size_
 	}
 	cudaMemsetAsync(bd->d_conv, 0, sizeof(float) * std::max<size_t>(1, bd->draw_total), env->stream);
 	cudaMemsetAsync(bd->d_direct, 0, sizeof(float) * std::max<size_t>(1, bd->draw_total), env->stream);
+	// splitting the subsampling trees off to other warps pays where a few
+	// pixels' trees would set the pass's end, and costs a little where the
+	// work is spread already: the evaluation timed both ways
+	bool split = bd->split.box != nullptr;
+	if (split) {
+		const double t_split = time_eval(bd, true), t_walk = time_eval(bd, false);
+		split = !(t_walk > 0 && t_split > 0 && t_walk < t_split);
+	}
 	// every shape timed in each of two rounds, the best time of each kept:
 	// a clock ramp or a slow launch early on does not decide the choice
 	double t_direct = -1;
@@ -1259,6 +1308,7 @@ pf_status pf_batch_create_masked(pf_env *env, const pf_model_desc *models, size_
 	ConvPlan fin;
 	fin.shape = best_shape;
 	fin.auto_fft = &choice;
+	fin.split = split;
 	return create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool,
 	                      mask_pool_len, fin, batch);
 }
