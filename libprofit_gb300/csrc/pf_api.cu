@@ -125,42 +125,9 @@ pf_status validate_profile(const pf_profile_desc &d, bool model_has_psf)
 	if (d.kind < PF_SERSIC || d.kind > PF_NULL) {
 		return fail(PF_ERR_INVALID_PARAMETER, "Unknown profile kind " + std::to_string(d.kind));
 	}
-	if (is_radial(d.kind)) {  // src/radial.cpp:204-214
-		if (v[PF_P_AXRAT] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "axrat <= 0, must have axrat > 0");
-		if (v[PF_P_AXRAT] > 1) return fail(PF_ERR_INVALID_PARAMETER, "axrat > 1, must have axrat <= 1");
-		if (v[PF_P_BOX] <= -2) return fail(PF_ERR_INVALID_PARAMETER, "box <= -2, must have box > -2");
-	}
+	const int rule = pf::param_rule(d.kind, v);  // src/radial.cpp:204-214 and each kind's validate()
+	if (rule != pf::PR_OK) return fail(PF_ERR_INVALID_PARAMETER, pf::param_rule_message(rule));
 	switch (d.kind) {
-	case PF_SERSIC:  // src/sersic.cpp:207-218
-		if (v[6] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "re <= 0, must have re > 0");
-		if (v[7] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "nser <= 0, must have nser > 0");
-		break;
-	case PF_CORESERSIC:  // src/coresersic.cpp:61-82
-		if (v[6] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "re <= 0, must have re > 0");
-		if (v[8] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "rb <= 0, must have rb > 0");
-		if (v[7] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "nser <= 0, must have nser > 0");
-		if (v[9] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "a <= 0, must have a > 0");
-		if (v[10] > 1.999) return fail(PF_ERR_INVALID_PARAMETER, "b > 1.999, must have b < 1.999");
-		break;
-	case PF_MOFFAT:  // src/moffat.cpp:60-71
-		if (v[6] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "fwhm <= 0, must have fwhm > 0");
-		if (v[7] < 0) return fail(PF_ERR_INVALID_PARAMETER, "con < 0, must have con >= 0");
-		break;
-	case PF_FERRER:  // src/ferrer.cpp:62-76
-		if (v[6] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "rout <= 0, must have rout >= 0");
-		if (v[7] < 0) return fail(PF_ERR_INVALID_PARAMETER, "a < 0, must have a >= 0");
-		if (v[8] > 2) return fail(PF_ERR_INVALID_PARAMETER, "b > 2, must have b <= 2");
-		break;
-	case PF_KING:  // src/king.cpp:61-74
-		if (v[6] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "rc <= 0, must have rc > 0");
-		if (v[7] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "rt <= 0, must have rt > 0");
-		if (v[8] < 0) return fail(PF_ERR_INVALID_PARAMETER, "a < 0, must have a >=0");
-		break;
-	case PF_BROKENEXP:  // src/brokenexponential.cpp:96-109
-		if (v[6] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "h1 <= 0, must have h1 > 0");
-		if (v[7] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "h2 <= 0, must have h2 > 0");
-		if (v[8] <= 0) return fail(PF_ERR_INVALID_PARAMETER, "rb <= 0, must have rb > 0");
-		break;
 	case PF_PSF:  // src/psf.cpp:39-45
 		if (!model_has_psf) {
 			return fail(PF_ERR_INVALID_PARAMETER, "No psf present in the model, cannot produce a psf profile");
@@ -937,9 +904,11 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 			sp.cnt = b->d_counter + 2;
 		}
 	}
-	PF_CUDA_TRY(cudaMalloc(&b->d_err, sizeof(unsigned int)));
+	// [0] device-limit flags, [1] the last pass's first invalid profile (index << 5 | rule)
+	PF_CUDA_TRY(cudaMalloc(&b->d_err, 2 * sizeof(unsigned int)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_solves, sizeof(double) * 3 * std::max<size_t>(1, n_profiles)));
 	PF_CUDA_TRY(cudaMemset(b->d_err, 0, sizeof(unsigned int)));
+	PF_CUDA_TRY(cudaMemset(b->d_err + 1, 0xff, sizeof(unsigned int)));
 	const size_t elem = b->dbl ? sizeof(double) : sizeof(float);
 	PF_CUDA_TRY(cudaMalloc(&b->d_conv, elem * std::max<size_t>(1, b->draw_total)));
 	PF_CUDA_TRY(cudaMalloc(&b->d_direct, elem * std::max<size_t>(1, b->draw_total)));
@@ -1477,8 +1446,15 @@ pf_status pf_batch_check(pf_batch *b, void *stream_ptr)
 	cudaStream_t stream = stream_ptr ? (cudaStream_t)stream_ptr : b->env->stream;
 	PF_CUDA_TRY(cudaSetDevice(b->env->device));
 	PF_CUDA_TRY(cudaStreamSynchronize(stream));
-	unsigned int err = 0;
-	PF_CUDA_TRY(cudaMemcpy(&err, b->d_err, sizeof(err), cudaMemcpyDeviceToHost));
+	unsigned int errs[2] = {0, 0xffffffffu};
+	PF_CUDA_TRY(cudaMemcpy(errs, b->d_err, sizeof(errs), cudaMemcpyDeviceToHost));
+	const unsigned int err = errs[0];
+	if (errs[1] != 0xffffffffu) {
+		// parameters written on the device that the reference's validate()
+		// refuses (its message); the profile drew nothing in that pass
+		return fail(PF_ERR_INVALID_PARAMETER, std::string(pf::param_rule_message((int)(errs[1] & 31u))) +
+		                                          " (profile " + std::to_string(errs[1] >> 5) + " of the batch)");
+	}
 	if (err & (pf::ERR_LEVELS | pf::ERR_RES)) {
 		return fail(PF_ERR_DEVICE_LIMIT, "a profile needed more sub-pixel levels or a finer resolution than the "
 		                                 "device supports; its pixels were clamped");

@@ -70,6 +70,89 @@ struct ModelDev {
 	uint32_t mask_final_w, mask_final_div;
 };
 
+// The reference's parameter validation of the radial profiles, in its order:
+// RadialProfile::validate (src/radial.cpp:204-214), then each kind's own
+// (src/sersic.cpp:207-218, src/coresersic.cpp:61-82, src/moffat.cpp:60-71,
+// src/ferrer.cpp:62-76, src/king.cpp:61-74, src/brokenexponential.cpp:96-109).
+// Returns the first rule the parameters break (param_rule_message gives the
+// reference's text), 0 if none. Comparisons as the reference's: a NaN passes.
+enum ParamRule : int {
+	PR_OK = 0, PR_AXRAT_LE0, PR_AXRAT_GT1, PR_BOX, PR_RE, PR_NSER, PR_RB, PR_CORE_A, PR_CORE_B, PR_FWHM, PR_CON,
+	PR_ROUT, PR_FERRER_A, PR_FERRER_B, PR_RC, PR_RT, PR_KING_A, PR_H1, PR_H2, PR_EXP_RB, PR_COUNT
+};
+
+__host__ __device__ inline int param_rule(int kind, const double *v)
+{
+	if (kind >= PF_SERSIC && kind <= PF_BROKENEXP) {
+		if (v[PF_P_AXRAT] <= 0) return PR_AXRAT_LE0;
+		if (v[PF_P_AXRAT] > 1) return PR_AXRAT_GT1;
+		if (v[PF_P_BOX] <= -2) return PR_BOX;
+	}
+	switch (kind) {
+	case PF_SERSIC:
+		if (v[6] <= 0) return PR_RE;
+		if (v[7] <= 0) return PR_NSER;
+		break;
+	case PF_CORESERSIC:
+		if (v[6] <= 0) return PR_RE;
+		if (v[8] <= 0) return PR_RB;
+		if (v[7] <= 0) return PR_NSER;
+		if (v[9] <= 0) return PR_CORE_A;
+		if (v[10] > 1.999) return PR_CORE_B;
+		break;
+	case PF_MOFFAT:
+		if (v[6] <= 0) return PR_FWHM;
+		if (v[7] < 0) return PR_CON;
+		break;
+	case PF_FERRER:
+		if (v[6] <= 0) return PR_ROUT;
+		if (v[7] < 0) return PR_FERRER_A;
+		if (v[8] > 2) return PR_FERRER_B;
+		break;
+	case PF_KING:
+		if (v[6] <= 0) return PR_RC;
+		if (v[7] <= 0) return PR_RT;
+		if (v[8] < 0) return PR_KING_A;
+		break;
+	case PF_BROKENEXP:
+		if (v[6] <= 0) return PR_H1;
+		if (v[7] <= 0) return PR_H2;
+		if (v[8] <= 0) return PR_EXP_RB;
+		break;
+	default:
+		break;
+	}
+	return PR_OK;
+}
+
+// the reference's invalid_parameter message of each rule
+inline const char *param_rule_message(int rule)
+{
+	static const char *const msg[PR_COUNT] = {
+	    "",
+	    "axrat <= 0, must have axrat > 0",
+	    "axrat > 1, must have axrat <= 1",
+	    "box <= -2, must have box > -2",
+	    "re <= 0, must have re > 0",
+	    "nser <= 0, must have nser > 0",
+	    "rb <= 0, must have rb > 0",
+	    "a <= 0, must have a > 0",
+	    "b > 1.999, must have b < 1.999",
+	    "fwhm <= 0, must have fwhm > 0",
+	    "con < 0, must have con >= 0",
+	    "rout <= 0, must have rout >= 0",
+	    "a < 0, must have a >= 0",
+	    "b > 2, must have b <= 2",
+	    "rc <= 0, must have rc > 0",
+	    "rt <= 0, must have rt > 0",
+	    "a < 0, must have a >=0",
+	    "h1 <= 0, must have h1 > 0",
+	    "h2 <= 0, must have h2 > 0",
+	    "rb <= 0, must have rb > 0",
+	};
+	return rule > 0 && rule < PR_COUNT ? msg[rule] : "";
+}
+
 // whether drawing pixel (x, y) of model m is evaluated (not masked out)
 __device__ __forceinline__ bool evaluated(const ModelDev &m, int x, int y)
 {

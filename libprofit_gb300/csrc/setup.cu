@@ -483,9 +483,10 @@ __device__ void radial_setup(ProfileDev &p, const ModelDev &m, double bn, const 
 //   task 0  bn = P^-1(1/2, 2n)                 (sersic, coresersic)
 //   task 1  P^-1(1 - n^2/2000, 2n)             (sersic switch radius, adjust)
 //   task 2  P^-1(0.9999, 2n)                   (sersic rscale_max, adjust, rscale_max = 0)
-__global__ void setup_solves_kernel(const ProfileDev *profs, int n_profiles, double *solves)
+__global__ void setup_solves_kernel(const ProfileDev *profs, int n_profiles, double *solves, unsigned int *err)
 {
 	const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+	if (t == 0) err[1] = 0xffffffffu;  // this pass's first invalid profile: none yet
 	if (t >= 3LL * n_profiles) {
 		return;
 	}
@@ -493,7 +494,10 @@ __global__ void setup_solves_kernel(const ProfileDev *profs, int n_profiles, dou
 	const int kind = profs[i].kind;
 	const double nser = profs[i].par[7];
 	double v = 0.;
-	if (task == 0 && (kind == PF_SERSIC || kind == PF_CORESERSIC)) {
+	if (param_rule(kind, profs[i].par) != PR_OK) {
+		// invalid parameters (written on the device): the profile is not set up
+	}
+	else if (task == 0 && (kind == PF_SERSIC || kind == PF_CORESERSIC)) {
 		v = sf::qgamma(0.5, 2 * nser, sf::bn_guess(nser));
 	}
 	else if (task == 1 && kind == PF_SERSIC && profs[i].adjust) {
@@ -532,7 +536,22 @@ __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs,
 	p.acc = p.acc_in;
 	p.rscale_switch = p.rscale_switch_in;
 	p.rscale_max = p.rscale_max_in;
-	if (p.kind >= PF_SERSIC && p.kind <= PF_BROKENEXP) {
+	const int rule = param_rule(p.kind, p.par);
+	if (rule != PR_OK) {
+		// Parameters the reference's validate() refuses, written on the device
+		// (pf_batch_set_params_dev, pf_step_graph): the first such profile is
+		// recorded for pf_batch_check, and this one draws nothing and gets no
+		// gradient (empty culling and subsampling boxes, zero flux scale).
+		atomicMin(&err[1], ((unsigned int)t << 5) | (unsigned int)rule);
+		p.bbx0 = p.bby0 = p.sbx0 = p.sby0 = 0;
+		p.bbx1 = p.bby1 = p.sbx1 = p.sby1 = -1;
+		p.flux_scale = 0.;
+		p.fflux_scale = 0.f;
+		for (int k = 0; k < PF_NPAR; k++) p.dlnfs[k] = 0.;
+		p.grad_ok = 0;
+		p.center_boost = 0;
+	}
+	else if (p.kind >= PF_SERSIC && p.kind <= PF_BROKENEXP) {
 		radial_setup(p, m, bn, sv, want_grad, err);
 	}
 	else if (p.kind == PF_SKY) {
@@ -575,7 +594,7 @@ void launch_setup(const ModelDev *models, ProfileDev *profs, int n_profiles, int
 	// single-warp blocks: the FP64-heavy work spreads over as many SMs as possible
 	if (n_profiles > 0) {
 		const long long tasks = 3LL * n_profiles;
-		setup_solves_kernel<<<(unsigned int)((tasks + 31) / 32), 32, 0, stream>>>(profs, n_profiles, solves);
+		setup_solves_kernel<<<(unsigned int)((tasks + 31) / 32), 32, 0, stream>>>(profs, n_profiles, solves, err);
 	}
 	int blocks = (n_profiles + 31) / 32;
 	if (blocks < 1) blocks = 1;
