@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -287,6 +288,9 @@ struct pf_env {
 	uint32_t flags = 0;
 	int n_sm = 1;
 	cudaStream_t stream = nullptr;
+	// the caller's handle plus one per live batch: the environment (its stream)
+	// is released with the last of them, whatever order they are destroyed in
+	std::atomic<int> refs{1};
 };
 
 struct pf_batch {
@@ -399,6 +403,21 @@ constexpr unsigned int kSplitMinFail = PF_SPLIT_MIN_FAIL;
 
 enum Stage { ST_SETUP = 0, ST_EVAL, ST_FINISH, ST_CHI2, ST_ADJCONV, ST_BACKWARD };
 
+// Drops one reference to an environment; the last frees it.
+void env_release(pf_env *env)
+{
+	if (env->refs.fetch_sub(1) != 1) return;
+	cudaSetDevice(env->device);
+	if (env->stream) cudaStreamDestroy(env->stream);
+	delete env;
+}
+
+// Entry points that check cudaGetLastError() after their launches first clear
+// an error an earlier, unrelated runtime call of the process left there (a
+// failed cudaMalloc, say), so that the check reports their own launches only.
+// Sticky errors (a faulted context) are not cleared by this and still show.
+void clear_stale_error() { (void)cudaGetLastError(); }
+
 void fold_stage_times(pf_batch *b)
 {
 	for (size_t i = 0; i < b->ev_used; i++) {
@@ -467,9 +486,7 @@ pf_status pf_env_create(int device, uint32_t flags, pf_env **env)
 void pf_env_destroy(pf_env *env)
 {
 	if (!env) return;
-	cudaSetDevice(env->device);
-	if (env->stream) cudaStreamDestroy(env->stream);
-	delete env;
+	env_release(env);
 }
 
 pf_status pf_model_output_dims(const pf_model_desc *model, const pf_profile_desc *profiles, uint32_t *out_w,
@@ -532,7 +549,9 @@ void pf_batch_destroy(pf_batch *b)
 		cudaEventDestroy(p.b);
 	}
 	cudaFreeHost(b->h_profiles);
+	pf_env *env = b->env;
 	delete b;
+	if (env) env_release(env);
 }
 
 }  // extern "C"
@@ -1016,10 +1035,12 @@ static pf_status create_planned(pf_env *env, const pf_model_desc *models, size_t
 	*batch = nullptr;
 	pf_batch *b = new (std::nothrow) pf_batch();
 	if (!b) return fail(PF_ERR_NO_MEMORY, "out of host memory");
+	b->env = env;
+	env->refs.fetch_add(1);
+	clear_stale_error();
 	pf_status s = batch_create_impl(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool,
 	                                mask_pool_len, b, plan);
 	if (s != PF_OK) {
-		b->env = env;
 		pf_batch_destroy(b);
 		return s;
 	}
@@ -1323,6 +1344,7 @@ pf_status pf_batch_set_params_dev(pf_batch *b, const double *params_dev, void *s
 	if (!b || !params_dev) return fail(PF_ERR_INVALID_PARAMETER, "pf_batch_set_params_dev: NULL argument");
 	cudaStream_t stream = stream_ptr ? (cudaStream_t)stream_ptr : b->env->stream;
 	PF_CUDA_TRY(cudaSetDevice(b->env->device));
+	clear_stale_error();
 	if (b->params_dirty) {
 		// descriptors first, so that the device copy is complete before the scatter
 		PF_CUDA_TRY(cudaMemcpyAsync(b->d_profiles, b->h_profiles,
@@ -1354,6 +1376,7 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 	if (!b || (!images_dev && b->total_out)) return fail(PF_ERR_INVALID_PARAMETER, "pf_forward: NULL argument");
 	cudaStream_t stream = stream_ptr ? (cudaStream_t)stream_ptr : b->env->stream;
 	PF_CUDA_TRY(cudaSetDevice(b->env->device));
+	clear_stale_error();
 	const int n_models = (int)b->mdev.size();
 	const int n_profiles = (int)b->profiles.size();
 	if (n_models == 0) return PF_OK;
@@ -1643,6 +1666,7 @@ pf_status pf_backward(pf_batch *b, const void *images_dev, const void *data_dev,
 	}
 	cudaStream_t stream = stream_ptr ? (cudaStream_t)stream_ptr : b->env->stream;
 	PF_CUDA_TRY(cudaSetDevice(b->env->device));
+	clear_stale_error();
 	const int n_models = (int)b->mdev.size(), n_profiles = (int)b->profiles.size();
 	if (n_models == 0) return PF_OK;
 	bool any_conv = false;
@@ -1740,6 +1764,7 @@ pf_status pf_step_graph(pf_batch *b, const double *params_dev, void *images_dev,
 		return fail(PF_ERR_INVALID_PARAMETER, "pf_step_graph: a graph is captured on a created stream, not the default one");
 	}
 	PF_CUDA_TRY(cudaSetDevice(b->env->device));
+	clear_stale_error();
 	// parameters set on the host since the last step go up outside the graph
 	if (b->params_dirty) {
 		PF_CUDA_TRY(cudaMemcpyAsync(b->d_profiles, b->h_profiles,
@@ -1856,6 +1881,7 @@ pf_status pf_convolve(pf_env *env, const double *src, uint32_t w, uint32_t h, co
 	if (!env || !src || !krn || !out) return fail(PF_ERR_INVALID_PARAMETER, "pf_convolve: NULL argument");
 	if (w == 0 || h == 0 || kw == 0 || kh == 0) return fail(PF_ERR_INVALID_PARAMETER, "pf_convolve: empty image");
 	PF_CUDA_TRY(cudaSetDevice(env->device));
+	clear_stale_error();
 	// Convolver::convolve: an image smaller than the kernel is first extended
 	// to max(src, krn), whose y component repeats the x maximum
 	// (include/profit/image.h:204-207), and the result cropped back.

@@ -128,3 +128,32 @@ def test_invalid_parameters_in_step_graph():
     torch.cuda.synchronize()
     b.step_graph(pstep, img, data, sigma, chi2, grad, stream=stream)
     b.check(stream=stream)
+
+
+def test_environment_released_after_its_batches():
+    """An environment closed while a batch still uses it (as garbage
+    collection may order it) stays alive until that batch is destroyed: the
+    batch still renders, and nothing is left behind for later calls."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build_cuda()
+    import libprofit_gb300 as pg
+    import workloads as W
+    specs = _specs("sersic")
+    env = pg.get_cuda_environment(0, use_double=False)
+    b = pg.Batch([W.to_model(s, env) for s in specs], env)
+    img = torch.zeros(b.total_pixels, dtype=torch.float32, device="cuda")
+    b.forward(img)
+    b.check()
+    first = img.cpu().numpy().copy()
+    env.close()
+    img.zero_()
+    b.forward(img)
+    b.check()
+    np.testing.assert_array_equal(img.cpu().numpy(), first)
+    b.close()
+    env2 = pg.get_cuda_environment(0, use_double=False)
+    b2 = pg.Batch([W.to_model(s, env2) for s in specs], env2)
+    b2.forward(img)
+    b2.check()
+    np.testing.assert_array_equal(img.cpu().numpy(), first)
