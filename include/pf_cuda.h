@@ -192,6 +192,15 @@ PF_API void pf_env_destroy(pf_env *env);
  * crops the PSF padding, optionally downsamples. `image` receives
  * out_w * out_h doubles (query the size with pf_model_output_dims, which
  * also checks a mask's declared dimensions: mask_offset >= 0, mask_w x mask_h).
+ *
+ * The environment keeps the device state of its last call: a model that
+ * differs from the previous one in parameter values only (a fitting loop's
+ * Model::evaluate) reuses it and allocates nothing -- its parameters are
+ * validated as a new model's would be, uploaded, and its constants
+ * recomputed on the device. Any other change (dimensions, profiles and their
+ * flags, PSF or mask contents) builds the state anew. Calls on one
+ * environment are serialised (a mutex), as the reference's Model::evaluate
+ * is not re-entrant either.
  */
 PF_API pf_status pf_model_output_dims(const pf_model_desc *model, const pf_profile_desc *profiles,
                                uint32_t *out_w, uint32_t *out_h);
@@ -212,6 +221,24 @@ PF_API pf_status pf_model_evaluate_masked(pf_env *env, const pf_model_desc *mode
 PF_API pf_status pf_convolve(pf_env *env, const double *src, uint32_t w, uint32_t h,
                       const double *krn, uint32_t kw, uint32_t kh, const uint8_t *mask,
                       double *out);
+
+/*
+ * Convolver::convolve(src, krn, mask, crop, offset_out) with ConvolverType::CUDA
+ * (include/profit/convolve.h:65-97): pf_convolve plus the crop flag and the
+ * offset of the cropped image in the returned one. The CUDA convolver is a
+ * direct convolution, which adds no padding (Convolver::padding is empty,
+ * src/convolve.cpp:50-53, as for BRUTE): crop = 0 returns the same w*h image
+ * and offset (0, 0), as mask_and_crop does (src/convolve.cpp:81-99).
+ * offset_x / offset_y may be NULL (the reference's NO_OFFSET).
+ *
+ * pf_convolve and pf_convolve_crop keep their device buffers in the
+ * environment, growing them only when an image larger than any before comes:
+ * repeated calls allocate nothing after the first. Calls on one environment
+ * are serialised (a mutex).
+ */
+PF_API pf_status pf_convolve_crop(pf_env *env, const double *src, uint32_t w, uint32_t h,
+                                  const double *krn, uint32_t kw, uint32_t kh, const uint8_t *mask,
+                                  int crop, double *out, uint32_t *offset_x, uint32_t *offset_y);
 
 /*
  * pf_convolve_noalloc: pf_convolve that allocates no device memory after its

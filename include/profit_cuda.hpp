@@ -393,15 +393,21 @@ private:
 };
 
 /* ConvolverType::CUDA: a direct convolution on the GPU with the reference's
- * semantics (src/convolve.cpp:55-79, crop = true). */
+ * semantics (Convolver::convolve, src/convolve.cpp:55-99). It adds no
+ * padding, so crop = false returns the same image and offset (0, 0);
+ * offset_out (x, y) may be null, the reference's NO_OFFSET. */
 class Convolver {
 public:
 	explicit Convolver(CUDAEnvPtr env) : m_env(std::move(env)) {}
-	Image convolve(const Image &src, const Image &krn, const std::vector<uint8_t> &mask = {})
+	Image convolve(const Image &src, const Image &krn, const std::vector<uint8_t> &mask = {}, bool crop = true,
+	               std::pair<unsigned int, unsigned int> *offset_out = nullptr)
 	{
 		Image out(src.getWidth(), src.getHeight());
-		check(pf_convolve(m_env->get(), src.data(), src.getWidth(), src.getHeight(), krn.data(), krn.getWidth(),
-		                  krn.getHeight(), mask.empty() ? nullptr : mask.data(), out.data()));
+		uint32_t ox = 0, oy = 0;
+		check(pf_convolve_crop(m_env->get(), src.data(), src.getWidth(), src.getHeight(), krn.data(),
+		                       krn.getWidth(), krn.getHeight(), mask.empty() ? nullptr : mask.data(), crop ? 1 : 0,
+		                       out.data(), &ox, &oy));
+		if (offset_out) *offset_out = {ox, oy};
 		return out;
 	}
 

@@ -429,16 +429,23 @@ class Convolver:
         self.kind = kind
         self.env = env
 
-    def convolve(self, src, krn, mask=None):
+    def convolve(self, src, krn, mask=None, crop=True, offset_out=None):
+        """Convolver::convolve (include/profit/convolve.h:65-99). The CUDA
+        convolver adds no padding: crop=False gives the same image, and
+        offset_out (a list, optional) receives the offset [0, 0]."""
         env = _env_or_default(self.env)
         src = np.ascontiguousarray(src, dtype=np.float64)
         krn = np.ascontiguousarray(krn, dtype=np.float64)
         out = np.zeros_like(src)
         mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
-        _check(_ffi.load().pf_convolve(env.handle, src.ctypes.data_as(ctypes.c_void_p), src.shape[1],
-                                       src.shape[0], krn.ctypes.data_as(ctypes.c_void_p), krn.shape[1],
-                                       krn.shape[0], None if mk is None else mk.ctypes.data_as(ctypes.c_void_p),
-                                       out.ctypes.data_as(ctypes.c_void_p)))
+        ox, oy = ctypes.c_uint32(), ctypes.c_uint32()
+        _check(_ffi.load().pf_convolve_crop(env.handle, src.ctypes.data_as(ctypes.c_void_p), src.shape[1],
+                                            src.shape[0], krn.ctypes.data_as(ctypes.c_void_p), krn.shape[1],
+                                            krn.shape[0], None if mk is None else mk.ctypes.data_as(ctypes.c_void_p),
+                                            int(bool(crop)), out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ox),
+                                            ctypes.byref(oy)))
+        if offset_out is not None:
+            offset_out[:] = [ox.value, oy.value]
         return out
 
 

@@ -80,6 +80,8 @@ _SIGNATURES = {
                                                 ctypes.POINTER(ctypes.c_uint32)]),
     "pf_convolve": (ctypes.c_int, [_P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_uint32,
                                    ctypes.c_uint32, _P, _P]),
+    "pf_convolve_crop": (ctypes.c_int, [_P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_uint32,
+                                        ctypes.c_uint32, _P, ctypes.c_int, _P, _P, _P]),
     "pf_convolve_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_uint32,
                                            ctypes.c_uint32, _P, _P]),
     "pf_batch_create": (ctypes.c_int, [_P, ctypes.POINTER(ModelDesc), ctypes.c_size_t,

@@ -291,6 +291,24 @@ struct pf_env {
 	// the caller's handle plus one per live batch: the environment (its stream)
 	// is released with the last of them, whatever order they are destroyed in
 	std::atomic<int> refs{1};
+	// Model::evaluate's state across calls (pf_model_evaluate*, pf_convolve):
+	// the last model's batch, reused while only parameter values change, and
+	// device buffers that only grow
+	struct Cache {
+		std::mutex mu;
+		pf_batch *batch = nullptr;
+		pf_model_desc model{};
+		std::vector<pf_profile_desc> profiles;  // parameter values not part of the key
+		std::vector<double> psf;
+		std::vector<uint8_t> mask;
+		bool has_mask = false;
+		void *d_out = nullptr;
+		size_t out_bytes = 0;
+		std::vector<double> params;
+		std::vector<float> host32;
+		void *d_conv = nullptr;                 // pf_convolve: source, output, kernel, mask
+		size_t conv_bytes = 0;
+	} cache;
 };
 
 struct pf_batch {
@@ -453,6 +471,29 @@ void stage_end(pf_batch *b, long slot, cudaStream_t s)
 
 }  // namespace
 
+namespace {
+
+// Whether two model descriptions give the same batch layout (every field).
+bool same_model(const pf_model_desc &a, const pf_model_desc &b)
+{
+	return a.width == b.width && a.height == b.height && a.scale_x == b.scale_x && a.scale_y == b.scale_y &&
+	       a.magzero == b.magzero && a.finesampling == b.finesampling && a.return_finesampled == b.return_finesampled &&
+	       a.first_profile == b.first_profile && a.n_profiles == b.n_profiles && a.psf_offset == b.psf_offset &&
+	       a.psf_w == b.psf_w && a.psf_h == b.psf_h && a.psf_scale_x == b.psf_scale_x &&
+	       a.psf_scale_y == b.psf_scale_y && a.convolver == b.convolver && a.mask_offset == b.mask_offset &&
+	       a.adjust_mask == b.adjust_mask && a.no_crop == b.no_crop && a.mask_w == b.mask_w && a.mask_h == b.mask_h;
+}
+
+// Whether two profiles differ at most in their parameter values.
+bool same_profile_layout(const pf_profile_desc &a, const pf_profile_desc &b)
+{
+	return a.kind == b.kind && a.convolve == b.convolve && a.rough == b.rough && a.adjust == b.adjust &&
+	       a.rescale_flux == b.rescale_flux && a.resolution == b.resolution && a.max_recursions == b.max_recursions &&
+	       a.acc == b.acc && a.rscale_switch == b.rscale_switch && a.rscale_max == b.rscale_max;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *pf_last_error(void) { return g_last_error.c_str(); }
@@ -486,6 +527,15 @@ pf_status pf_env_create(int device, uint32_t flags, pf_env **env)
 void pf_env_destroy(pf_env *env)
 {
 	if (!env) return;
+	{
+		std::lock_guard<std::mutex> lock(env->cache.mu);
+		cudaSetDevice(env->device);
+		if (env->cache.batch) pf_batch_destroy(env->cache.batch);  // drops its reference
+		env->cache.batch = nullptr;
+		cudaFree(env->cache.d_out);
+		cudaFree(env->cache.d_conv);
+		env->cache.d_out = env->cache.d_conv = nullptr;
+	}
 	env_release(env);
 }
 
@@ -1839,44 +1889,86 @@ pf_status pf_model_evaluate_masked(pf_env *env, const pf_model_desc *model, cons
 	const bool has_psf = psf && m.psf_w > 0 && m.psf_h > 0;
 	m.psf_offset = has_psf ? 0 : -1;
 	m.mask_offset = mask ? 0 : -1;
-	size_t mask_len = 0;
-	if (mask) mask_len = (size_t)m.mask_w * m.mask_h;
-	pf_batch *b = nullptr;
-	pf_status s = pf_batch_create_masked(env, &m, 1, profiles, m.n_profiles, has_psf ? psf : nullptr,
-	                                     has_psf ? (size_t)m.psf_w * m.psf_h : 0, mask, mask_len, &b);
-	if (s != PF_OK) return s;
+	const size_t psf_len = has_psf ? (size_t)m.psf_w * m.psf_h : 0;
+	const size_t mask_len = mask ? (size_t)m.mask_w * m.mask_h : 0;
+	PF_CUDA_TRY(cudaSetDevice(env->device));
+	pf_env::Cache &c = env->cache;
+	std::lock_guard<std::mutex> lock(c.mu);
+	// The batch of the previous call is reused when the model differs from it
+	// in parameter values only (Model::evaluate in a fitting loop): its
+	// constants are recomputed on the device from the new values, nothing is
+	// allocated.
+	bool hit = c.batch && same_model(c.model, m) && c.profiles.size() == m.n_profiles &&
+	           c.psf.size() == psf_len && (!psf_len || std::memcmp(c.psf.data(), psf, sizeof(double) * psf_len) == 0) &&
+	           c.has_mask == (mask != nullptr) && c.mask.size() == mask_len &&
+	           (!mask_len || std::memcmp(c.mask.data(), mask, mask_len) == 0);
+	for (uint32_t i = 0; hit && i < m.n_profiles; i++) hit = same_profile_layout(c.profiles[i], profiles[i]);
+	pf_status s = PF_OK;
+	if (hit) {
+		// the reference's validate() of each profile, as a new batch would run it
+		for (uint32_t i = 0; i < m.n_profiles; i++) {
+			s = validate_profile(profiles[i], has_psf);
+			if (s != PF_OK) return s;
+		}
+		c.params.resize((size_t)m.n_profiles * PF_NPAR);
+		for (uint32_t i = 0; i < m.n_profiles; i++) {
+			std::memcpy(&c.params[(size_t)i * PF_NPAR], profiles[i].par, sizeof(double) * PF_NPAR);
+		}
+		s = pf_batch_set_params(c.batch, c.params.data());
+		if (s != PF_OK) return s;
+	}
+	else {
+		if (c.batch) pf_batch_destroy(c.batch);
+		c.batch = nullptr;
+		s = pf_batch_create_masked(env, &m, 1, profiles, m.n_profiles, has_psf ? psf : nullptr, psf_len, mask,
+		                           mask_len, &c.batch);
+		if (s != PF_OK) return s;
+		c.model = m;
+		c.profiles.assign(profiles, profiles + m.n_profiles);
+		c.psf.assign(psf, psf + psf_len);
+		c.has_mask = mask != nullptr;
+		c.mask.assign(mask, mask + mask_len);
+	}
+	pf_batch *b = c.batch;
 	const size_t n = b->total_out;
 	const size_t elem = b->dbl ? sizeof(double) : sizeof(float);
-	void *d_out = nullptr;
-	cudaError_t e = cudaMalloc(&d_out, elem * std::max<size_t>(1, n));
-	if (e != cudaSuccess) {
-		pf_batch_destroy(b);
-		return fail(PF_ERR_NO_MEMORY, std::string("pf_model_evaluate: ") + cudaGetErrorString(e));
+	if (c.out_bytes < elem * std::max<size_t>(1, n)) {
+		cudaFree(c.d_out);
+		c.d_out = nullptr;
+		c.out_bytes = 0;
+		const cudaError_t e = cudaMalloc(&c.d_out, elem * std::max<size_t>(1, n));
+		if (e != cudaSuccess) return fail(PF_ERR_NO_MEMORY, std::string("pf_model_evaluate: ") + cudaGetErrorString(e));
+		c.out_bytes = elem * std::max<size_t>(1, n);
 	}
-	s = pf_forward(b, d_out, nullptr, nullptr);
+	s = pf_forward(b, c.d_out, nullptr, nullptr);
 	if (s == PF_OK) s = pf_batch_check(b, nullptr);
-	if (s == PF_OK) {
-		if (b->dbl) {
-			e = cudaMemcpy(image, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost);
-		}
-		else {
-			std::vector<float> tmp(n);
-			e = cudaMemcpy(tmp.data(), d_out, sizeof(float) * n, cudaMemcpyDeviceToHost);
-			for (size_t i = 0; i < n; i++) image[i] = tmp[i];
-		}
-		if (e != cudaSuccess) s = fail(PF_ERR_CUDA, std::string("pf_model_evaluate: ") + cudaGetErrorString(e));
+	if (s != PF_OK) return s;
+	cudaError_t e;
+	if (b->dbl) {
+		e = cudaMemcpyAsync(image, c.d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, env->stream);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(env->stream);
 	}
-	if (s == PF_OK) {
-		if (out_w) *out_w = b->mdev[0].out_w;
-		if (out_h) *out_h = b->mdev[0].out_h;
+	else {
+		c.host32.resize(n);
+		e = cudaMemcpyAsync(c.host32.data(), c.d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, env->stream);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(env->stream);
+		for (size_t i = 0; e == cudaSuccess && i < n; i++) image[i] = c.host32[i];
 	}
-	cudaFree(d_out);
-	pf_batch_destroy(b);
-	return s;
+	if (e != cudaSuccess) return fail(PF_ERR_CUDA, std::string("pf_model_evaluate: ") + cudaGetErrorString(e));
+	if (out_w) *out_w = b->mdev[0].out_w;
+	if (out_h) *out_h = b->mdev[0].out_h;
+	return PF_OK;
 }
 
 pf_status pf_convolve(pf_env *env, const double *src, uint32_t w, uint32_t h, const double *krn, uint32_t kw,
                       uint32_t kh, const uint8_t *mask, double *out)
+{
+	return pf_convolve_crop(env, src, w, h, krn, kw, kh, mask, 1, out, nullptr, nullptr);
+}
+
+pf_status pf_convolve_crop(pf_env *env, const double *src, uint32_t w, uint32_t h, const double *krn, uint32_t kw,
+                           uint32_t kh, const uint8_t *mask, int crop, double *out, uint32_t *offset_x,
+                           uint32_t *offset_y)
 {
 	if (!env || !src || !krn || !out) return fail(PF_ERR_INVALID_PARAMETER, "pf_convolve: NULL argument");
 	if (w == 0 || h == 0 || kw == 0 || kh == 0) return fail(PF_ERR_INVALID_PARAMETER, "pf_convolve: empty image");
@@ -1892,54 +1984,61 @@ pf_status pf_convolve(pf_env *env, const double *src, uint32_t w, uint32_t h, co
 	}
 	// Surface::extend refuses a smaller height (include/profit/image.h:305-311)
 	if (eh < h) return fail(PF_ERR_INVALID_PARAMETER, "pf_convolve: new_height should be >= height");
+	// crop = false: a direct convolver adds no padding (Convolver::padding is
+	// empty, src/convolve.cpp:50-53), so the image is the cropped one and its
+	// offset (0, 0) (mask_and_crop, src/convolve.cpp:81-99)
+	(void)crop;
+	if (offset_x) *offset_x = 0;
+	if (offset_y) *offset_y = 0;
 	const size_t n = (size_t)ew * eh, kn = (size_t)kw * kh;
-	std::vector<double> ext;
-	std::vector<uint8_t> emask;
-	const double *s_host = src;
-	const uint8_t *m_host = mask;
-	if (ew != w || eh != h) {
-		ext.assign(n, 0.0);
-		for (uint32_t y = 0; y < h && y < eh; y++) std::memcpy(&ext[(size_t)y * ew], src + (size_t)y * w, sizeof(double) * w);
-		s_host = ext.data();
-		if (mask) {
-			emask.assign(n, 0);
-			for (uint32_t y = 0; y < h && y < eh; y++) std::memcpy(&emask[(size_t)y * ew], mask + (size_t)y * w, w);
-			m_host = emask.data();
-		}
+	// the environment's scratch (grown when too small, else reused): source,
+	// output, kernel, mask, each on a 256-byte boundary
+	auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+	const size_t o_out = up(sizeof(double) * n), o_krn = o_out + up(sizeof(double) * n);
+	const size_t o_mask = o_krn + up(sizeof(double) * kn), bytes = o_mask + up(mask ? n : 1);
+	pf_env::Cache &c = env->cache;
+	std::lock_guard<std::mutex> lock(c.mu);
+	if (c.conv_bytes < bytes) {
+		cudaFree(c.d_conv);
+		c.d_conv = nullptr;
+		c.conv_bytes = 0;
+		const cudaError_t e = cudaMalloc(&c.d_conv, bytes);
+		if (e != cudaSuccess) return fail(PF_ERR_NO_MEMORY, std::string("pf_convolve: ") + cudaGetErrorString(e));
+		c.conv_bytes = bytes;
 	}
-	double *d_src = nullptr, *d_krn = nullptr, *d_out = nullptr;
-	uint8_t *d_mask = nullptr;
-	pf_status s = PF_OK;
-	cudaError_t e = cudaMalloc(&d_src, sizeof(double) * n);
-	if (e == cudaSuccess) e = cudaMalloc(&d_out, sizeof(double) * n);
-	if (e == cudaSuccess) e = cudaMalloc(&d_krn, sizeof(double) * kn);
-	if (e == cudaSuccess && m_host) e = cudaMalloc(&d_mask, n);
-	// on the kernel's stream: a pageable copy may return before its DMA ends
-	if (e == cudaSuccess) e = cudaMemcpyAsync(d_src, s_host, sizeof(double) * n, cudaMemcpyHostToDevice, env->stream);
-	if (e == cudaSuccess) e = cudaMemcpyAsync(d_krn, krn, sizeof(double) * kn, cudaMemcpyHostToDevice, env->stream);
-	if (e == cudaSuccess && m_host) e = cudaMemcpyAsync(d_mask, m_host, n, cudaMemcpyHostToDevice, env->stream);
+	unsigned char *base = static_cast<unsigned char *>(c.d_conv);
+	double *d_src = reinterpret_cast<double *>(base), *d_out = reinterpret_cast<double *>(base + o_out);
+	double *d_krn = reinterpret_cast<double *>(base + o_krn);
+	uint8_t *d_mask = mask ? base + o_mask : nullptr;
+	cudaStream_t st = env->stream;
+	const bool extended = ew != w || eh != h;
+	const size_t row = sizeof(double) * w, erow = sizeof(double) * ew;
+	cudaError_t e = cudaSuccess;
+	if (extended) {
+		// zero extension, the original at the top left (Surface::extend, start 0)
+		e = cudaMemsetAsync(d_src, 0, sizeof(double) * n, st);
+		if (e == cudaSuccess) e = cudaMemcpy2DAsync(d_src, erow, src, row, row, h, cudaMemcpyHostToDevice, st);
+		if (e == cudaSuccess && mask) e = cudaMemsetAsync(d_mask, 0, n, st);
+		if (e == cudaSuccess && mask) e = cudaMemcpy2DAsync(d_mask, ew, mask, w, w, h, cudaMemcpyHostToDevice, st);
+	}
+	else {
+		e = cudaMemcpyAsync(d_src, src, sizeof(double) * n, cudaMemcpyHostToDevice, st);
+		if (e == cudaSuccess && mask) e = cudaMemcpyAsync(d_mask, mask, n, cudaMemcpyHostToDevice, st);
+	}
+	if (e == cudaSuccess) e = cudaMemcpyAsync(d_krn, krn, sizeof(double) * kn, cudaMemcpyHostToDevice, st);
 	if (e == cudaSuccess) {
-		pf::launch_convolve64(d_src, ew, eh, d_krn, kw, kh, d_mask, d_out, env->n_sm, env->stream);
+		pf::launch_convolve64(d_src, ew, eh, d_krn, kw, kh, d_mask, d_out, env->n_sm, st);
 		e = cudaGetLastError();
 	}
-	if (e == cudaSuccess) e = cudaStreamSynchronize(env->stream);
+	// cropped back to the original size (result.crop(dims - diff), top-left aligned)
 	if (e == cudaSuccess) {
-		if (ew == w && eh == h) {
-			e = cudaMemcpy(out, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost);
-		}
-		else {
-			// crop back to the original size (result.crop(dims - diff), top-left aligned)
-			std::vector<double> tmp(n);
-			e = cudaMemcpy(tmp.data(), d_out, sizeof(double) * n, cudaMemcpyDeviceToHost);
-			for (uint32_t y = 0; y < h; y++) std::memcpy(out + (size_t)y * w, &tmp[(size_t)y * ew], sizeof(double) * w);
-		}
+		e = extended ? cudaMemcpy2DAsync(out, row, d_out, erow, row, h, cudaMemcpyDeviceToHost, st)
+		             : cudaMemcpyAsync(out, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
 	}
-	if (e != cudaSuccess) s = fail(PF_ERR_CUDA, std::string("pf_convolve: ") + cudaGetErrorString(e));
-	cudaFree(d_src);
-	cudaFree(d_krn);
-	cudaFree(d_out);
-	cudaFree(d_mask);
-	return s;
+	const cudaError_t sync = cudaStreamSynchronize(st);
+	if (e == cudaSuccess) e = sync;
+	if (e != cudaSuccess) return fail(PF_ERR_CUDA, std::string("pf_convolve: ") + cudaGetErrorString(e));
+	return PF_OK;
 }
 
 }  // extern "C"
