@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--models", type=int, default=None,
                     help="models in the batch (default: 1024 for cfg4, 4096 for cfg3)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-dropin", action="store_true", help="skip the one-model-per-call drop-in timings")
     ap.add_argument("--convolver", default="auto", choices=["auto", "brute", "fft"],
                     help="convolution method of the FP32 batch (auto: the library's choice)")
     ap.add_argument("--no-graph", action="store_true",
@@ -250,6 +251,49 @@ def run_reference(args, world, rank):
 # op weighted 8, its issue cost against the FMA pipe: 128 vs 16 per SM-clock).
 FLOP_EVAL = 2 * 7 + 5 + 3 * 8        # coordinates + base + rf + exp: 43
 FLOP_GRAD = FLOP_EVAL + 40 + 4 * 8   # + the derivative chain (sersic_grad): 115
+def dropin_rates(env64, env32, budget_s=2.0):
+    """The drop-in path: Model.evaluate (pf_model_evaluate, host buffers in
+    and out) on one model per call, the sersic's xcen changed between calls
+    as a fitter changes parameters, for the one-model workloads (cfg1:
+    100x100, 15x15 PSF, direct convolution; cfg2: 1000x1000 bulge + disk +
+    sky, 51x51 PSF by FFT), in the plain FP64 and the FP32 environments; and
+    the CPU oracle port (all host threads) on the same models. Calls per
+    second, each leg timed for about budget_s after three warm-up calls."""
+    from oracle import oracle as O
+    import workloads as W
+    O.build(with_ref=False)
+    threads = os.cpu_count() or 1
+    out = {"calls": "Model.evaluate through pf_model_evaluate with host buffers, one model per call",
+           "cpu_threads": threads}
+    for name, spec in (("cfg1", W.cfg1()[0]), ("cfg2", W.cfg2()[0])):
+        row = {}
+        for label, env in (("fp64", env64), ("fp32", env32)):
+            m = W.to_model(spec, env)
+            p = m.profiles[0]
+            x0 = spec["profiles"][0][1]["xcen"]
+            k = 0
+            for _ in range(3):
+                p.parameter("xcen", x0 + 0.01 * (k % 7))
+                m.evaluate()
+                k += 1
+            n, t0 = 0, time.perf_counter()
+            while time.perf_counter() - t0 < budget_s or n < 3:
+                p.parameter("xcen", x0 + 0.01 * (k % 7))
+                m.evaluate()
+                n += 1
+                k += 1
+            row[label + "_calls_per_s"] = n / (time.perf_counter() - t0)
+        case = W.to_oracle_case(spec)
+        O.evaluate(case, threads=threads)
+        n, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < budget_s or n < 1:
+            O.evaluate(case, threads=threads)
+            n += 1
+        row["cpu_port_calls_per_s"] = n / (time.perf_counter() - t0)
+        out[name] = row
+    return out
+
+
 # models whose images, chi^2 and gradients are checked against the plain FP64 path
 ACC_MODELS = 32
 
@@ -509,6 +553,8 @@ def run_ours(args, world, rank, local):
                                                 "frac": work[k] / (per_step[k] / 1000.0) / 1e12 / fp32_peak}
                          for k in work if per_step.get(k)}
 
+    dropin = dropin_rates(env64, pg.get_cuda_environment(local, use_double=False)) if not args.no_dropin else None
+
     cpu = None
     if not args.no_cpu_baseline:
         v, threads, done, dt = cpu_baseline_sample(specs, par, budget_s=8.0)
@@ -534,6 +580,7 @@ def run_ours(args, world, rank, local):
                      "max_rel_chi2_err": max(acc["chi2"]) if acc["chi2"] else None,
                      "grad": grad_acc},
         "fft_forced": fft_forced,
+        "drop_in": dropin,
         "ratio_vs_fp64_per_model": (value / world) / fp64_rate if fp64_rate else None,
         "stage_ms_per_step": per_step,
         "roofline": roof,
