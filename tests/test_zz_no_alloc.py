@@ -8,7 +8,8 @@ earlier call left in the shared scratch would show. Tolerance: 1e-13 relative,
 as for pf_convolve against the brute-force oracle (both run the same kernel).
 Two tests check the property the entry point exists for: 100 calls leave the
 device's free memory unchanged, and with the device's memory taken by
-torch's caching allocator (pf_convolve then fails) the call still succeeds.
+torch's caching allocator (pf_convolve on a new environment, which must
+allocate its buffers, then fails) the call still succeeds.
 """
 import ctypes
 
@@ -112,14 +113,17 @@ def test_noalloc_allocates_no_device_memory(abi):
 
 def test_noalloc_works_on_a_full_device(abi):
     """A caller whose caching allocator holds nearly all of the device's
-    memory: pf_convolve cannot allocate its buffers there, while
-    pf_convolve_noalloc still gives the same result as on an empty device."""
+    memory: pf_convolve on an environment that has not yet grown its buffers
+    cannot allocate them there, while pf_convolve_noalloc still gives the
+    same result as on an empty device."""
     import torch
+    import libprofit_gb300 as pg
     ffi, lib, env = abi
     rng = np.random.default_rng(12)
     src, krn = rng.random((1024, 1024)), rng.random((15, 15))
     st, want = _call(lib, "pf_convolve_noalloc", env, src, krn)
     assert st == ffi.PF_OK, lib.pf_last_error()
+    fresh = pg.get_cuda_environment(0, use_double=True)  # no convolution buffers yet
     held = []
     try:
         # take the device's memory through torch until 8 to 10 MiB are free
@@ -131,7 +135,7 @@ def test_noalloc_works_on_a_full_device(abi):
                 except torch.cuda.OutOfMemoryError:
                     break
         assert torch.cuda.mem_get_info(0)[0] < 16 << 20
-        st_alloc, _ = _call(lib, "pf_convolve", env, src, krn)
+        st_alloc, _ = _call(lib, "pf_convolve", fresh, src, krn)
         assert st_alloc != ffi.PF_OK
         st, got = _call(lib, "pf_convolve_noalloc", env, src, krn)
         assert st == ffi.PF_OK, lib.pf_last_error()
@@ -139,3 +143,4 @@ def test_noalloc_works_on_a_full_device(abi):
     finally:
         del held
         torch.cuda.empty_cache()
+        fresh.close()
