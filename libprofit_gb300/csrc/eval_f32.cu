@@ -432,7 +432,7 @@ __device__ bool split_root(const SplitPool &pool, const ProfileDev &P, int pi, c
 // One 32-pixel row tile of a model's drawing area: every profile of the model
 // in order, summed into the conv / direct images. KINDS: the radial profile
 // kinds of the batch.
-template <unsigned int KINDS>
+template <unsigned int KINDS, bool SPLIT>
 __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, int n_models,
                                           const ProfileDev *__restrict__ profs, const double *__restrict__ psf_pool,
                                           float *__restrict__ conv_img, float *__restrict__ direct_img, long long tile,
@@ -544,7 +544,7 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 					eval_frame_m<KINDS>(P, sh, ws, 0, res, __frcp_rn((float)res), max_rec, lane, counts);
 					const long long didx =
 					    dbg.depth ? P.depth_off + (long long)row * m.draw_w + (long long)spx : -1;
-					if (pool.box && split_root(pool, P, pi, m, ws, res, max_rec, lane, src,
+					if (SPLIT && split_root(pool, P, pi, m, ws, res, max_rec, lane, src,
 					                           (long long)m.draw_off + (long long)row * m.draw_w + spx, didx,
 					                           prec, plast)) {
 						if (lane == src) split = true;
@@ -570,7 +570,7 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 		}
 	}
 	if (active) {
-		if (prec >= 0) {
+		if (SPLIT && prec >= 0) {
 			// the split profiles' values are still to come: the warp that
 			// finishes the last of them writes the canvas
 			pool.pix[prec].s_conv = acc_conv;
@@ -612,7 +612,7 @@ __device__ __forceinline__ long long ring_tile(const ModelDev *__restrict__ mode
 // all left to one warp) and phase-B tiles 32 at a time from counter[1]; a
 // tile is evaluated by the item that first sets its bit in `claims` (zeroed
 // before the launch), so each tile exactly once.
-template <unsigned int KINDS>
+template <unsigned int KINDS, bool SPLIT>
 __global__ void __launch_bounds__(kWarps32 * 32, PF_EVAL32_MIN_BLOCKS)
 eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const ProfileDev *__restrict__ profs,
                     unsigned int n_profiles, const double *__restrict__ psf_pool, float *__restrict__ conv_img,
@@ -662,7 +662,7 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 			const int src = __ffs(todo) - 1;
 			todo &= todo - 1;
 			const long long t = __shfl_sync(0xffffffffu, tile, src);
-			eval_tile<KINDS>(models, n_models, profs, psf_pool, conv_img, direct_img, t, ws, lane, dbg, pool);
+			eval_tile<KINDS, SPLIT>(models, n_models, profs, psf_pool, conv_img, direct_img, t, ws, lane, dbg, pool);
 		}
 	}
 }
@@ -748,22 +748,34 @@ void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs
 {
 	const unsigned int n_ring = (unsigned int)n_profiles * kRingRows * kRingCols;
 	const int blocks = n_sm * PF_EVAL32_MIN_BLOCKS;
+	// kernels without the split path where the batch does not split: it costs
+	// the walk registers (measured 2.79 against 3.10 ms for the 1024-model step)
 	if (sersic_only) {
-		eval_tiles32_kernel<f32::kSersicOnly><<<blocks, kWarps32 * 32, 0, stream>>>(
-		    models, n_models, profs, (unsigned int)n_profiles, psf_pool, conv_img, direct_img, (unsigned int)n_tiles,
-		    n_ring, counter, claims, dbg, pool);
 		if (pool.box) {
+			eval_tiles32_kernel<f32::kSersicOnly, true><<<blocks, kWarps32 * 32, 0, stream>>>(
+			    models, n_models, profs, (unsigned int)n_profiles, psf_pool, conv_img, direct_img,
+			    (unsigned int)n_tiles, n_ring, counter, claims, dbg, pool);
 			split_boxes32_kernel<f32::kSersicOnly><<<blocks, kWarps32 * 32, 0, stream>>>(profs, conv_img, direct_img,
 			                                                                             pool, dbg);
 		}
+		else {
+			eval_tiles32_kernel<f32::kSersicOnly, false><<<blocks, kWarps32 * 32, 0, stream>>>(
+			    models, n_models, profs, (unsigned int)n_profiles, psf_pool, conv_img, direct_img,
+			    (unsigned int)n_tiles, n_ring, counter, claims, dbg, pool);
+		}
 	}
 	else {
-		eval_tiles32_kernel<f32::kAllKinds><<<blocks, kWarps32 * 32, 0, stream>>>(
-		    models, n_models, profs, (unsigned int)n_profiles, psf_pool, conv_img, direct_img, (unsigned int)n_tiles,
-		    n_ring, counter, claims, dbg, pool);
 		if (pool.box) {
+			eval_tiles32_kernel<f32::kAllKinds, true><<<blocks, kWarps32 * 32, 0, stream>>>(
+			    models, n_models, profs, (unsigned int)n_profiles, psf_pool, conv_img, direct_img,
+			    (unsigned int)n_tiles, n_ring, counter, claims, dbg, pool);
 			split_boxes32_kernel<f32::kAllKinds><<<blocks, kWarps32 * 32, 0, stream>>>(profs, conv_img, direct_img,
 			                                                                          pool, dbg);
+		}
+		else {
+			eval_tiles32_kernel<f32::kAllKinds, false><<<blocks, kWarps32 * 32, 0, stream>>>(
+			    models, n_models, profs, (unsigned int)n_profiles, psf_pool, conv_img, direct_img,
+			    (unsigned int)n_tiles, n_ring, counter, claims, dbg, pool);
 		}
 	}
 }
