@@ -302,6 +302,26 @@ __device__ float warp_walk_m(const ProfileDev &P, const f32::Shape &sh, WarpScra
 	}
 }
 
+// subsample_pixel on a box given relative to the profile centre: its frame
+// evaluated and walked (the kernels that split no trees)
+template <unsigned int KINDS>
+__device__ float warp_subsample_m(const ProfileDev &P, const f32::Shape &sh, WarpScratchM &ws, float xhi, float xlo,
+                                  float yhi, float ylo, float bx, float by, unsigned int res, unsigned int max_rec,
+                                  int lane, unsigned long long *counts, int &deepest)
+{
+	if (lane == 0) {
+		ws.fr[0].xhi = xhi;
+		ws.fr[0].xlo = xlo;
+		ws.fr[0].yhi = yhi;
+		ws.fr[0].ylo = ylo;
+		ws.fr[0].bx = bx;
+		ws.fr[0].by = by;
+	}
+	__syncwarp();
+	eval_frame_m<KINDS>(P, sh, ws, 0, res, __frcp_rn((float)res), max_rec, lane, counts);
+	return warp_walk_m<KINDS>(P, sh, ws, 0, res, max_rec, lane, counts, deepest);
+}
+
 // Frame L of the warp's scratch set to a box relative to the profile centre
 __device__ __forceinline__ void set_frame(WarpScratchM &ws, int L, float xhi, float xlo, float yhi, float ylo, float bx,
                                           float by, int lane)
@@ -457,7 +477,6 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 	// this lane's pixel: its split record once a profile's subtrees are split
 	// off (SplitPool), and the last split profile's root
 	int prec = -1, plast = -1;
-	const long long canvas_idx = (long long)m.draw_off + (long long)row * m.draw_w + px;
 
 	for (int q0 = 0; q0 < m.n_profiles; q0 += 32) {
 		// 32 profiles' culling boxes tested at once, one per lane; the ones
@@ -538,20 +557,26 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 					float bxh, bxl, byh, byl;
 					corner_pair(small_int_to_float(spx), m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
 					corner_pair(small_int_to_float(row), m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
-					// the level-0 box; its failing sub-points' subtrees split off to
-					// other warps, or walked here
-					set_frame(ws, 0, bxh, bxl, byh, byl, m.fsx_hi, m.fsy_hi, lane);
-					eval_frame_m<KINDS>(P, sh, ws, 0, res, __frcp_rn((float)res), max_rec, lane, counts);
-					const long long didx =
-					    dbg.depth ? P.depth_off + (long long)row * m.draw_w + (long long)spx : -1;
-					if (SPLIT && split_root(pool, P, pi, m, ws, res, max_rec, lane, src,
-					                           (long long)m.draw_off + (long long)row * m.draw_w + spx, didx,
-					                           prec, plast)) {
-						if (lane == src) split = true;
-						continue;
-					}
 					int deepest = 0;
-					const float v = warp_walk_m<KINDS>(P, sh, ws, 0, res, max_rec, lane, counts, deepest);
+					float v = 0.f;
+					if constexpr (SPLIT) {
+						// the level-0 box; its failing sub-points' subtrees split off
+						// to other warps, or walked here
+						set_frame(ws, 0, bxh, bxl, byh, byl, m.fsx_hi, m.fsy_hi, lane);
+						eval_frame_m<KINDS>(P, sh, ws, 0, res, __frcp_rn((float)res), max_rec, lane, counts);
+						const long long didx =
+						    dbg.depth ? P.depth_off + (long long)row * m.draw_w + (long long)spx : -1;
+						if (split_root(pool, P, pi, m, ws, res, max_rec, lane, src,
+						               (long long)m.draw_off + (long long)row * m.draw_w + spx, didx, prec, plast)) {
+							if (lane == src) split = true;
+							continue;
+						}
+						v = warp_walk_m<KINDS>(P, sh, ws, 0, res, max_rec, lane, counts, deepest);
+					}
+					else {
+						v = warp_subsample_m<KINDS>(P, sh, ws, bxh, bxl, byh, byl, m.fsx_hi, m.fsy_hi, res, max_rec,
+						                            lane, counts, deepest);
+					}
 					if (lane == src) {
 						pixel_val = v;
 						depth = deepest;
@@ -570,6 +595,7 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 		}
 	}
 	if (active) {
+		const size_t canvas_idx = (size_t)m.draw_off + (size_t)row * m.draw_w + px;
 		if (SPLIT && prec >= 0) {
 			// the split profiles' values are still to come: the warp that
 			// finishes the last of them writes the canvas
