@@ -142,8 +142,10 @@ typedef struct pf_model_desc {
 	/* Model::set_crop(false) (include/profit/model.h:206-214): 1 = keep the
 	 * padding the convolver adds (src/model.cpp:288-306). The direct
 	 * convolutions add none (Convolver::padding is empty, src/convolve.cpp:
-	 * 50-53), so their image is the cropped one, at offset (0, 0); with
-	 * PF_CONV_FFT it is refused (PF_ERR_UNSUPPORTED). 0 (the default): crop. */
+	 * 50-53), so their image is the cropped one, at offset (0, 0); PF_CONV_FFT
+	 * gives the FFT convolver's uncropped frame with only the PSF padding
+	 * removed (pf_model_output_dims / pf_model_output_offset give its size
+	 * and offset; double precision only). 0 (the default): crop. */
 	int32_t no_crop;
 	uint32_t mask_w, mask_h;
 } pf_model_desc;
@@ -204,6 +206,12 @@ PF_API void pf_env_destroy(pf_env *env);
  */
 PF_API pf_status pf_model_output_dims(const pf_model_desc *model, const pf_profile_desc *profiles,
                                uint32_t *out_w, uint32_t *out_h);
+/* The offset Model::evaluate(Point &offset_out) reports (src/model.cpp:259-320):
+ * where the requested area lies in the returned image. (0, 0) unless crop = 0
+ * (no_crop) with the FFT convolver, whose uncropped frame the image is then
+ * (double precision only; not with SUM downsampling or an adjustable mask). */
+PF_API pf_status pf_model_output_offset(const pf_model_desc *model, const pf_profile_desc *profiles,
+                                        uint32_t *offset_x, uint32_t *offset_y);
 PF_API pf_status pf_model_evaluate(pf_env *env, const pf_model_desc *model, const pf_profile_desc *profiles,
                             const double *psf, double *image, uint32_t *out_w, uint32_t *out_h);
 /* The same with a calculation mask (host bytes; dimensions as the model's

@@ -326,14 +326,21 @@ public:
 	}
 	void set_adjust_mask(bool adjust) { m_adjust_mask = adjust; }
 	/* Model::set_crop: the direct convolutions add no padding, so the image
-	 * is the cropped one at offset (0, 0); FFT with crop false is refused. */
+	 * is the cropped one at offset (0, 0); with the FFT convolver (double
+	 * precision) crop false keeps its uncropped frame less the PSF padding. */
 	void set_crop(bool crop) { m_crop = crop; }
 
-	/* Model::evaluate(Point &offset_out) */
+	/* Model::evaluate(Point &offset_out): the offset of the requested area in
+	 * the returned image */
 	Image evaluate(std::pair<unsigned int, unsigned int> &offset_out)
 	{
 		Image img = evaluate();
-		offset_out = {0u, 0u};
+		pf_model_desc m = desc();
+		std::vector<pf_profile_desc> profs;
+		for (auto &p : m_profiles) profs.push_back(p->desc());
+		uint32_t x = 0, y = 0;
+		check(pf_model_output_offset(&m, profs.data(), &x, &y));
+		offset_out = {x, y};
 		return img;
 	}
 

@@ -328,7 +328,9 @@ class Model:
     def set_crop(self, crop):
         """Model::set_crop (default True). The direct convolutions add no
         padding, so their uncropped image is the cropped one at offset (0, 0);
-        the FFT convolution with crop False is refused (Unsupported)."""
+        the FFT convolution with crop False gives its uncropped frame less the
+        PSF padding, and the offset of the requested area in it
+        (evaluate_with_offset; double precision only)."""
         self.crop = bool(crop)
 
     def set_convolver(self, convolver):
@@ -376,11 +378,18 @@ class Model:
         _check(_ffi.load().pf_model_output_dims(ctypes.byref(m), profs, ctypes.byref(w), ctypes.byref(h)))
         return w.value, h.value
 
+    def output_offset(self):
+        """The offset Model::evaluate reports (pf_model_output_offset): (0, 0)
+        unless set_crop(False) with the FFT convolver."""
+        m, profs = self._descs()
+        x, y = ctypes.c_uint32(), ctypes.c_uint32()
+        _check(_ffi.load().pf_model_output_offset(ctypes.byref(m), profs, ctypes.byref(x), ctypes.byref(y)))
+        return x.value, y.value
+
     def evaluate_with_offset(self):
         """Model::evaluate(Point &offset): (image, (x, y)) with the offset of
-        the requested area in an uncropped image, (0, 0) with this backend's
-        convolutions (see set_crop)."""
-        return self.evaluate(), (0, 0)
+        the requested area in the returned image (see set_crop)."""
+        return self.evaluate(), self.output_offset()
 
     def evaluate(self):
         """Model::evaluate: returns the image as a (height, width) float64 array."""

@@ -73,6 +73,8 @@ _SIGNATURES = {
     "pf_env_destroy": (None, [_P]),
     "pf_model_output_dims": (ctypes.c_int, [ctypes.POINTER(ModelDesc), ctypes.POINTER(ProfileDesc),
                                             ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]),
+    "pf_model_output_offset": (ctypes.c_int, [ctypes.POINTER(ModelDesc), ctypes.POINTER(ProfileDesc),
+                                              ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]),
     "pf_model_evaluate": (ctypes.c_int, [_P, ctypes.POINTER(ModelDesc), ctypes.POINTER(ProfileDesc), _P, _P,
                                          ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]),
     "pf_model_evaluate_masked": (ctypes.c_int, [_P, ctypes.POINTER(ModelDesc), ctypes.POINTER(ProfileDesc), _P,

@@ -177,10 +177,19 @@ __global__ void fft_cols_kernel(const ModelDev *__restrict__ models, const FftJo
 	__syncthreads();
 	C *other = res == x ? y : x;
 	res = stockham(res, other, n, jb.count, tw, nmax, true);
-	const int off_y = (int)m.pad_y + (int)m.psf_h - 1 - (int)m.psf_h / 2;
-	for (int i = threadIdx.x; i < jb.count * (int)m.crop_h; i += blockDim.x) {
+	// the output rows: the crop's, from its offset in the linear convolution;
+	// with the uncropped frame, its own rows (zero where the convolution is)
+	const int off_y = m.uncropped ? m.ufy0 : (int)m.pad_y + (int)m.psf_h - 1 - (int)m.psf_h / 2;
+	const int rows_out = m.uncropped ? (int)m.out_h : (int)m.crop_h;
+	const int full_h = (int)m.draw_h + (int)m.psf_h - 1;
+	for (int i = threadIdx.x; i < jb.count * rows_out; i += blockDim.x) {
 		const int r = i / jb.count, t = i - r * jb.count;
-		col[(size_t)r * nb + jb.first + t] = res[t * n + r + off_y];
+		const int ry = r + off_y;
+		C v;
+		v.x = 0;
+		v.y = 0;
+		if (ry >= 0 && ry < full_h && ry < n) v = res[t * n + ry];
+		col[(size_t)r * nb + jb.first + t] = v;
 	}
 }
 
@@ -220,6 +229,24 @@ __global__ void fft_irows_kernel(const ModelDev *__restrict__ models, const FftJ
 	const T scale = (T)1 / ((T)m.fft_mx * (T)m.fft_my);
 	const int off_x = (int)m.pad_x + (int)m.psf_w - 1 - (int)m.psf_w / 2;
 	const bool downsample = m.fs > 1 && !m.return_fs;
+	if (m.uncropped) {
+		// the uncropped frame (Model::evaluate with crop = false): the linear
+		// convolution at (c + ufx0, row), the direct image at drawing pixel
+		// (c + udx0, r + udy0); the convolution masked by the calculation mask
+		// extended over the frame (mask_and_crop, src/convolve.cpp:81-94)
+		const int full_w = (int)m.draw_w + (int)m.psf_w - 1;
+		for (int i = threadIdx.x; i < jb.count * (int)m.out_w; i += blockDim.x) {
+			const int t = i / m.out_w, c = i - t * m.out_w;
+			const int r = jb.first + t;
+			const int fx = c + m.ufx0, dxp = c + m.udx0, dyp = r + m.udy0;
+			const bool in_draw = dxp >= 0 && dyp >= 0 && dxp < (int)m.draw_w && dyp < (int)m.draw_h;
+			T conv = fx >= 0 && fx < full_w && fx < n ? res[t * n + fx].x * scale : (T)0;
+			if (m.mask_eval && !(in_draw && evaluated(m, dxp, dyp))) conv = (T)0;
+			const T dir = in_draw ? direct[m.draw_off + (size_t)dyp * m.draw_w + dxp] : (T)0;
+			out[m.out_off + (size_t)r * m.out_w + c] = dir + conv;
+		}
+		return;
+	}
 	for (int i = threadIdx.x; i < jb.count * (int)m.crop_w; i += blockDim.x) {
 		const int t = i / m.crop_w, c = i - t * m.crop_w;
 		const int r = jb.first + t;

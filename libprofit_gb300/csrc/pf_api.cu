@@ -156,9 +156,80 @@ pf_status validate_profile(const pf_profile_desc &d, bool model_has_psf)
 struct Geometry {
 	uint32_t pad_x, pad_y, draw_w, draw_h, crop_w, crop_h, out_w, out_h;
 	bool conv;
+	// crop = false with the FFT convolver: the output window in the FFT's
+	// uncropped frame (ModelDev::ufx0..udy0) and the offset Model::evaluate
+	// reports (offset_out); 0 otherwise
+	bool uncropped = false;
+	int32_t ufx0 = 0, ufy0 = 0, udx0 = 0, udy0 = 0;
+	uint32_t off_x = 0, off_y = 0;
 	// calculation mask (adjustable): what Model::evaluate does with it
 	bool mask_needs_convolution = false, mask_needs_psf_padding = false, mask_needs_adjustment = false;
 };
+
+// crop = false with the FFT convolver (Model::evaluate, src/model.cpp:288-317):
+// the convolution returns its uncropped frame E = 2 max(D, K) (D the drawing
+// dimensions, K the PSF's; the x component of max() for both sides,
+// include/profit/image.h:204-207), the source at offset_after_convolution(D, K)
+// in it (src/convolve.cpp:270-281), the linear convolution shifted by the
+// kernel's start (D - K) / 2; the direct image is extended to E at that
+// offset and added; then only the PSF padding is removed, by the difference
+// between FFTConvolver::padding of D and of D - 2 x padding
+// (src/convolve.cpp:263-268). Unsigned arithmetic as the reference's: the
+// per-axis sum offset_diff + dim_diff is max(D, K).x - max(D - 2p, K).x.
+pf_status uncropped_fft_geometry(const pf_model_desc &m, Geometry &g)
+{
+	if (m.finesampling > 1 && !m.return_finesampled) {
+		return fail(PF_ERR_UNSUPPORTED, "crop = false with the FFT convolver and a SUM-downsampled image is not "
+		                                "supported by the CUDA backend");
+	}
+	if (g.mask_needs_adjustment) {
+		// the reference masks the larger uncropped image with the model's own
+		// mask (src/model.cpp:312-314) and reads past the mask's end
+		return fail(PF_ERR_UNSUPPORTED, "crop = false with the FFT convolver and an adjustable calculation mask "
+		                                "is not supported by the CUDA backend (the reference's result is undefined)");
+	}
+	const int64_t dx = g.draw_w, dy = g.draw_h, kx = m.psf_w, ky = m.psf_h;
+	if (dx < kx || dy < ky) {
+		return fail(PF_ERR_UNSUPPORTED, "crop = false with the FFT convolver and a PSF larger than the drawing area "
+		                                "is not supported by the CUDA backend");
+	}
+	auto off = [&](int64_t a, int64_t k) { return a / 2 - ((a % 2 == 0 || k % 2 == 0) ? 1 : 0); };
+	const int64_t px = g.pad_x, py = g.pad_y;
+	const int64_t mx = std::max(dx, kx), e = 2 * mx;
+	// the reference transforms the flattened frame as one sequence: when the
+	// linear convolution's rows (the kernel starting (dy - ky) / 2 down) pass
+	// the frame's e rows, they wrap into its first rows
+	if (dy + (dy - ky) / 2 + ky - 1 > e) {
+		return fail(PF_ERR_UNSUPPORTED, "crop = false with the FFT convolver: the reference's frame wraps around "
+		                                "for an image this much taller than wide");
+	}
+	const int64_t odx = off(dx, kx), ody = off(dy, ky);
+	int64_t cox = 0, coy = 0, cw = e, ch = e, rx = odx, ry = ody;
+	if (px > 0 && py > 0) {  // Dimensions' bool: both components (include/profit/image.h:92-94)
+		const int64_t d2x = dx - 2 * px, d2y = dy - 2 * py;
+		const int64_t o2x = off(d2x, kx), o2y = off(d2y, ky);
+		const int64_t shrink = mx - std::max(d2x, kx);
+		cw = e - 2 * px - shrink;
+		ch = e - 2 * py - shrink;
+		cox = px + (odx - o2x);
+		coy = py + (ody - o2y);
+		rx = o2x;
+		ry = o2y;
+	}
+	if (odx < 0 || ody < 0 || rx < 0 || ry < 0 || cw <= 0 || ch <= 0) {
+		return fail(PF_ERR_UNSUPPORTED, "crop = false with the FFT convolver: an image too small for its PSF");
+	}
+	g.uncropped = true;
+	g.out_w = (uint32_t)cw;
+	g.out_h = (uint32_t)ch;
+	g.ufx0 = (int32_t)(cox - (dx - kx) / 2);
+	g.ufy0 = (int32_t)(coy - (dy - ky) / 2);
+	g.udx0 = (int32_t)(cox - odx);
+	g.udy0 = (int32_t)(coy - ody);
+	g.off_x = (uint32_t)rx;
+	g.off_y = (uint32_t)ry;
+	return PF_OK;
+}
 
 // Model::analyze_inputs + analyze_expansion_requirements (src/model.cpp:152-219);
 // `mask` the model's calculation mask or null; `mask_declared`: a mask of the
@@ -179,11 +250,6 @@ pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles
 	}
 	if (g.conv && !has_psf) {
 		return fail(PF_ERR_INVALID_PARAMETER, "No psf provided but profile(s) requested convolution");
-	}
-	if (m.no_crop && g.conv && m.convolver == PF_CONV_FFT) {
-		// the FFT convolver's uncropped frame (FFTConvolver::padding,
-		// src/convolve.cpp:263-268) is not produced by this backend
-		return fail(PF_ERR_UNSUPPORTED, "crop = false with the FFT convolver is not supported by the CUDA backend");
 	}
 	for (uint32_t i = 0; i < m.n_profiles; i++) {
 		pf_status s = validate_profile(profiles[m.first_profile + i], has_psf);
@@ -241,6 +307,7 @@ pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles
 		                                          ", " + std::to_string(m.mask_h) + "] != [" +
 		                                          std::to_string(g.draw_w) + ", " + std::to_string(g.draw_h) + "]");
 	}
+	if (m.no_crop && g.conv && m.convolver == PF_CONV_FFT) return uncropped_fft_geometry(m, g);
 	return PF_OK;
 }
 
@@ -539,6 +606,20 @@ void pf_env_destroy(pf_env *env)
 	env_release(env);
 }
 
+pf_status pf_model_output_offset(const pf_model_desc *model, const pf_profile_desc *profiles, uint32_t *offset_x,
+                                 uint32_t *offset_y)
+{
+	if (!model || (!profiles && model->n_profiles)) return fail(PF_ERR_INVALID_PARAMETER, "NULL model or profiles");
+	pf_model_desc m = *model;
+	m.first_profile = 0;
+	Geometry g;
+	pf_status s = model_geometry(m, profiles, g, nullptr, m.mask_offset >= 0 && m.mask_w > 0 && m.mask_h > 0);
+	if (s != PF_OK) return s;
+	if (offset_x) *offset_x = g.off_x;
+	if (offset_y) *offset_y = g.off_y;
+	return PF_OK;
+}
+
 pf_status pf_model_output_dims(const pf_model_desc *model, const pf_profile_desc *profiles, uint32_t *out_w,
                                uint32_t *out_h)
 {
@@ -669,8 +750,10 @@ pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5], const double *p
 		// the single-precision transforms start at 64 points (a larger zero
 		// padding leaves the linear convolution unchanged)
 		const unsigned int nmin = b->dbl ? 2u : 64u;
-		const unsigned int mx = std::max(nmin, next_pow2(d.crop_w + d.psf_w));
-		const unsigned int my = std::max(nmin, next_pow2(d.crop_h + d.psf_h));
+		// the cropped outputs need no wrap-around below crop + psf; the
+		// uncropped frame takes the whole linear convolution, draw + psf - 1
+		const unsigned int mx = std::max(nmin, next_pow2((d.uncropped ? d.draw_w : d.crop_w) + d.psf_w));
+		const unsigned int my = std::max(nmin, next_pow2((d.uncropped ? d.draw_h : d.crop_h) + d.psf_h));
 		bool fft = false;
 		if (d.convolver == PF_CONV_FFT) {
 			if ((int)mx > nmax || (int)my > nmax) {
@@ -698,7 +781,9 @@ pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5], const double *p
 		d.fft_my = my;
 		const int64_t nb = mx / 2 + 1;
 		d.fft_work_off = work;
-		work += (int64_t)d.draw_h * nb;
+		// the source rows in, the output rows out (in place)
+		const unsigned int rows_out = d.uncropped ? d.out_h : d.crop_h;
+		work += (int64_t)std::max(d.draw_h, rows_out) * nb;
 		used_nmax = std::max(used_nmax, (int)std::max(mx, my));
 		if (!b->dbl) {
 			// models with the same PSF values and transform sizes share one spectrum
@@ -741,7 +826,7 @@ pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5], const double *p
 		const int cc = std::max(1, std::min(16, per_block / (int)my));
 		for (unsigned int r = 0; r < d.draw_h; r += cr) jobs[0].push_back({(int)i, (int)r, (int)std::min<unsigned int>(cr, d.draw_h - r), 0});
 		for (int c = 0; c < nb; c += cc) jobs[1].push_back({(int)i, c, (int)std::min<int64_t>(cc, nb - c), 0});
-		for (unsigned int r = 0; r < d.crop_h; r += cr) jobs[2].push_back({(int)i, (int)r, (int)std::min<unsigned int>(cr, d.crop_h - r), 0});
+		for (unsigned int r = 0; r < rows_out; r += cr) jobs[2].push_back({(int)i, (int)r, (int)std::min<unsigned int>(cr, rows_out - r), 0});
 		for (unsigned int r = 0; r < d.psf_h; r += cr) jobs[3].push_back({(int)i, (int)r, (int)std::min<unsigned int>(cr, d.psf_h - r), 0});
 		for (int c = 0; c < nb; c += cc) jobs[4].push_back({(int)i, c, (int)std::min<int64_t>(cc, nb - c), 0});
 		b->any_fft = true;
@@ -844,6 +929,17 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		d.crop_h = g.crop_h;
 		d.out_w = g.out_w;
 		d.out_h = g.out_h;
+		if (g.uncropped) {
+			if (!b->dbl) {
+				return fail(PF_ERR_UNSUPPORTED, "crop = false with the FFT convolver is supported in the double "
+				                                "precision environment only");
+			}
+			d.uncropped = 1;
+			d.ufx0 = g.ufx0;
+			d.ufy0 = g.ufy0;
+			d.udx0 = g.udx0;
+			d.udy0 = g.udy0;
+		}
 		d.scale_x = m.scale_x;
 		d.scale_y = m.scale_y;
 		d.sx = m.scale_x / m.finesampling;
@@ -1610,6 +1706,12 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 		                d.kind == PF_NULL;
 		if (!ok) {
 			return fail(PF_ERR_UNSUPPORTED, "profile " + std::to_string(i) + ": no adjoint for this profile kind");
+		}
+	}
+	for (size_t i = 0; i < b->mdev.size(); i++) {
+		if (b->mdev[i].uncropped) {
+			return fail(PF_ERR_UNSUPPORTED, "model " + std::to_string(i) + ": no adjoint of the FFT convolver's "
+			                                "uncropped image (crop = false)");
 		}
 	}
 	PF_CUDA_TRY(cudaSetDevice(b->env->device));

@@ -68,6 +68,14 @@ struct ModelDev {
 	const uint8_t *mask_eval;
 	const uint8_t *mask_final;
 	uint32_t mask_final_w, mask_final_div;
+	// crop = false with the FFT convolver (double precision): output pixel
+	// (c, r) takes the linear convolution (source * PSF) at (c + ufx0, r + ufy0)
+	// and the direct image at drawing pixel (c + udx0, r + udy0), each zero
+	// outside its area (Model::evaluate, src/model.cpp:288-306, on the
+	// FFTConvolver's uncropped frame, src/convolve.cpp:263-312)
+	int32_t uncropped;
+	int32_t ufx0, ufy0, udx0, udy0;
+	int32_t pad3;
 };
 
 // The reference's parameter validation of the radial profiles, in its order:

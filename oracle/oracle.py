@@ -316,6 +316,80 @@ def fft_convolve_reference_math(src, krn):
     return res[oy:oy + sh, ox:ox + sw]
 
 
+def fft_convolve_uncropped(src, krn, mask=None):
+    """The FFTConvolver's uncropped result (crop = false): the whole ext frame
+    of fft_convolve_reference_math, masked by the mask extended over it at
+    the offset (mask_and_crop, src/convolve.cpp:81-94), and that offset."""
+    sh, sw = src.shape
+    kh, kw = krn.shape
+    m = max(sw, kw)
+    ext_w, ext_h = 2 * m, 2 * m
+    ext_src = np.zeros((ext_h, ext_w))
+    ext_src[:sh, :sw] = src
+    ext_krn = np.zeros((ext_h, ext_w))
+    ky, kx = (sh - kh) // 2, (sw - kw) // 2
+    ext_krn[ky:ky + kh, kx:kx + kw] = krn
+    n = ext_w * ext_h
+    res = np.fft.irfft(np.fft.rfft(ext_src.ravel()) * np.fft.rfft(ext_krn.ravel()), n=n).reshape(ext_h, ext_w)
+    ox = sw // 2 - (1 if (sw % 2 == 0 or kw % 2 == 0) else 0)
+    oy = sh // 2 - (1 if (sh % 2 == 0 or kh % 2 == 0) else 0)
+    if mask is not None:
+        ext_mask = np.zeros((ext_h, ext_w), dtype=bool)
+        ext_mask[oy:oy + sh, ox:ox + sw] = np.asarray(mask) != 0
+        res = np.where(ext_mask, res, 0.0)
+    return res, (ox, oy)
+
+
+def evaluate_uncropped_fft(case):
+    """Model::evaluate with set_crop(false) and the FFT convolver
+    (src/model.cpp:259-360), finesampling 1 and no calculation mask: the
+    profiles drawn on the padded drawing area (the oracle's own drawing, the
+    centres moved by the PSF padding as RadialProfile::evaluate moves them),
+    the convolved ones through fft_convolve_uncropped, the others extended to
+    its frame at its offset and added, then only the PSF padding removed with
+    FFTConvolver::padding's offset and dimension differences (the x component
+    of max() for both sides, include/profit/image.h:204-207). Returns (image,
+    (offset_x, offset_y)) as Model::evaluate(Point &) does."""
+    psf = np.asarray(case.psf, dtype=np.float64)
+    psf = psf / psf.sum()
+    kh, kw = psf.shape
+    conv = [(k, p) for k, p in case.profiles if p.get("convolve", False)]
+    rest = [(k, p) for k, p in case.profiles if not p.get("convolve", False)]
+    px, py = kw // 2, kh // 2
+    sx, sy = case.scale if hasattr(case, "scale") else (1.0, 1.0)
+    dw, dh = case.width + 2 * px, case.height + 2 * py
+
+    def draw(profiles):
+        if not profiles:
+            return np.zeros((dh, dw))
+        moved = []
+        for k, p in profiles:
+            q = dict(p, convolve=False)
+            if "xcen" in q:
+                q["xcen"] = q["xcen"] + px * sx
+                q["ycen"] = q["ycen"] + py * sy
+            moved.append((k, q))
+        img, _, _ = evaluate(Case(dw, dh, moved, scale=(sx, sy), magzero=case.magzero))
+        return img
+
+    conv_img, (ox, oy) = fft_convolve_uncropped(draw(conv), psf)
+    direct = np.zeros_like(conv_img)
+    direct[oy:oy + dh, ox:ox + dw] = draw(rest)
+    image = direct + conv_img
+    e = conv_img.shape[0]
+
+    def off(a, k):
+        return a // 2 - (1 if (a % 2 == 0 or k % 2 == 0) else 0)
+
+    if px > 0 and py > 0:
+        d2w, d2h = dw - 2 * px, dh - 2 * py
+        shrink = max(dw, kw) - max(d2w, kw)
+        cw, ch = e - 2 * px - shrink, e - 2 * py - shrink
+        cx, cy = px + off(dw, kw) - off(d2w, kw), py + off(dh, kh) - off(d2h, kh)
+        return image[cy:cy + ch, cx:cx + cw], (off(d2w, kw), off(d2h, kh))
+    return image, (ox, oy)
+
+
 def moffat_psf(size, fwhm, con, threads=1):
     """A size x size Moffat PSF rendered by the oracle's moffat profile,
     centred, normalised to unit sum (as Model::set_psf does)."""

@@ -141,3 +141,21 @@ def test_batch_refuses_host_foreign_and_strided_buffers():
         pg._need(Buf(16, index=1), 16, 8, "chi2", 0)
     with pytest.raises(pg.InvalidParameter, match="flux: the buffer must be contiguous"):
         pg._need(Buf(16, contiguous=False), 16, 8, "flux", 0)
+
+
+def test_uncropped_fft_dimensions_and_offset(oracle_lib):
+    """The dimensions and offset of Model::evaluate with crop = false and the
+    FFT convolver (pf_model_output_dims / pf_model_output_offset, no GPU
+    needed) equal those of the oracle's restatement of the reference's
+    arithmetic (src/model.cpp:288-306, src/convolve.cpp:263-281)."""
+    import workloads as W
+    import libprofit_gb300 as pg
+    for w, h, k in [(40, 40, 9), (41, 37, 8), (60, 30, 10), (33, 30, 15), (12, 12, 9), (30, 34, 7), (64, 20, 16)]:
+        profs = [("sersic", dict(xcen=w / 2, ycen=h / 2, mag=15.0, re=3.0, convolve=True))]
+        spec = dict(width=w, height=h, psf=W.moffat_psf(k, 2.5, 2.5), profiles=profs)
+        m = W.to_model(spec)
+        m.set_convolver("fft")
+        m.set_crop(False)
+        ref, ref_off = oracle_lib.evaluate_uncropped_fft(oracle_lib.Case(w, h, profs, psf=spec["psf"]))
+        assert m.output_dims() == (ref.shape[1], ref.shape[0])
+        assert m.output_offset() == ref_off
