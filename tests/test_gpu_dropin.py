@@ -13,6 +13,8 @@ state and reuses it while only parameter values change:
   * pf_convolve's scratch is kept the same way, and crop = false returns the
     same image at offset (0, 0), as the reference's direct convolvers do.
 """
+import gc
+
 import numpy as np
 import pytest
 
@@ -51,8 +53,6 @@ def test_repeated_evaluate_reuses_state(use_double):
     env = pg.get_cuda_environment(0, use_double=use_double)
     rng = np.random.default_rng(7)
     _model(pg, env, _params(rng), psf).evaluate()  # builds the state
-    torch.cuda.synchronize()
-    free0 = torch.cuda.mem_get_info(0)[0]
     for _ in range(20):
         par = _params(rng)
         got = _model(pg, env, par, psf).evaluate()
@@ -60,9 +60,10 @@ def test_repeated_evaluate_reuses_state(use_double):
         want = _model(pg, fresh_env, par, psf).evaluate()
         fresh_env.close()
         np.testing.assert_array_equal(got, want)
-    # the fresh environments have been released: the loop's own calls
-    # allocated nothing
+    # a fitting loop's calls allocate nothing
+    gc.collect()  # earlier objects freed now, not during the measurement
     torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(0)[0]
     for _ in range(20):
         _model(pg, env, _params(rng), psf).evaluate()
     torch.cuda.synchronize()
@@ -116,6 +117,7 @@ def test_convolve_scratch_and_crop():
     rng = np.random.default_rng(10)
     src, krn = rng.random((300, 280)), rng.random((25, 25))
     want = conv.convolve(src, krn)
+    gc.collect()  # earlier objects freed now, not during the measurement
     torch.cuda.synchronize()
     free0 = torch.cuda.mem_get_info(0)[0]
     for _ in range(20):

@@ -13,6 +13,8 @@ allocate its buffers, then fails) the call still succeeds.
 """
 import ctypes
 
+import gc
+
 import numpy as np
 import pytest
 
@@ -100,6 +102,7 @@ def test_noalloc_allocates_no_device_memory(abi):
     mask = (rng.random(src.shape) > 0.2).astype(np.uint8)
     st, first = _call(lib, "pf_convolve_noalloc", env, src, krn, mask)
     assert st == ffi.PF_OK, lib.pf_last_error()
+    gc.collect()  # earlier objects freed now, not during the measurement
     torch.cuda.synchronize()
     free0, _ = torch.cuda.mem_get_info(0)
     for _ in range(100):
