@@ -214,6 +214,18 @@ PF_API pf_status pf_model_output_offset(const pf_model_desc *model, const pf_pro
                                         uint32_t *offset_x, uint32_t *offset_y);
 PF_API pf_status pf_model_evaluate(pf_env *env, const pf_model_desc *model, const pf_profile_desc *profiles,
                             const double *psf, double *image, uint32_t *out_w, uint32_t *out_h);
+/* The statistics of the last pf_model_evaluate* call on env, for
+ * Model::get_stats (src/model.cpp:362-368, the ProfileStats of
+ * include/profit/profile.h:46-73). With PF_ENV_PROFILE: that call's stage
+ * times (setup, evaluation, convolution: the fused passes of all its
+ * profiles, timed with CUDA events), and per profile 32 counts as
+ * pf_batch_depth gives them -- subsample_pixel calls per recursion level in
+ * [0, 16), evaluate_at calls on pixel centres [30] and inside
+ * subsample_pixel [31] -- by which a caller can attribute the evaluation
+ * time to its profiles. Without it, all zero. level_counts: n_profiles x 32,
+ * or NULL. */
+PF_API pf_status pf_env_last_model_stats(pf_env *env, pf_stage_times *times, int64_t *level_counts,
+                                         size_t n_profiles);
 /* The same with a calculation mask (host bytes; dimensions as the model's
  * adjust_mask says; NULL: none). */
 PF_API pf_status pf_model_evaluate_masked(pf_env *env, const pf_model_desc *model, const pf_profile_desc *profiles,

@@ -106,12 +106,13 @@ private:
 };
 
 /* A CUDA environment (OpenCLEnv analogue). use_double selects the plain FP64
- * path that reproduces the reference's arithmetic. */
+ * path that reproduces the reference's arithmetic; profile, the stage timing
+ * and counts of Model::get_stats. */
 class CUDAEnv {
 public:
-	CUDAEnv(int device, bool use_double) : m_env(nullptr)
+	CUDAEnv(int device, bool use_double, bool profile = false) : m_env(nullptr)
 	{
-		check(pf_env_create(device, use_double ? PF_ENV_DOUBLE : 0u, &m_env));
+		check(pf_env_create(device, (use_double ? PF_ENV_DOUBLE : 0u) | (profile ? PF_ENV_PROFILE : 0u), &m_env));
 	}
 	~CUDAEnv() { pf_env_destroy(m_env); }
 	CUDAEnv(const CUDAEnv &) = delete;
@@ -123,12 +124,33 @@ private:
 };
 typedef std::shared_ptr<CUDAEnv> CUDAEnvPtr;
 
-inline CUDAEnvPtr get_cuda_environment(int device = 0, bool use_double = true)
+inline CUDAEnvPtr get_cuda_environment(int device = 0, bool use_double = true, bool profile = false)
 {
-	return std::make_shared<CUDAEnv>(device, use_double);
+	return std::make_shared<CUDAEnv>(device, use_double, profile);
 }
 
 class Model;
+
+/* Model::get_stats (include/profit/profile.h:46-73, src/model.cpp:362-368),
+ * for an environment with PF_ENV_PROFILE (CUDAEnv(device, use_double,
+ * profile = true)). This backend evaluates all of a model's profiles in fused
+ * passes timed as a whole: cuda_times holds those passes' device times, and
+ * `total` the profile's share -- the setup pass split evenly, the evaluation
+ * pass by the profile's evaluate_at calls. */
+typedef long long nsecs_t;
+struct CUDA_times {
+	nsecs_t setup = 0, evaluation = 0, convolution = 0;
+};
+class ProfileStats {
+public:
+	virtual ~ProfileStats() {}
+	nsecs_t total = 0;
+};
+struct RadialProfileStats : ProfileStats {
+	CUDA_times cuda_times;
+	unsigned long long evaluations = 0;        // evaluate_at calls
+	std::map<int, unsigned long long> integrations;  // subsample_pixel calls per recursion level
+};
 
 /* A profile of a Model (include/profit/profile.h:78-260). */
 class Profile {
@@ -301,6 +323,8 @@ public:
 
 	void set_dimensions(unsigned int w, unsigned int h) { m_width = w, m_height = h; }
 	void set_image_pixel_scale(const std::pair<double, double> &s) { m_scale = s; }
+	std::pair<double, double> get_image_pixel_scale() const { return m_scale; }
+	bool has_profiles() const { return !m_profiles.empty(); }
 	void set_psf_pixel_scale(const std::pair<double, double> &s) { m_psf_scale = s; }
 	void set_magzero(double magzero) { m_magzero = magzero; }
 	void set_finesampling(unsigned int fs)
@@ -329,6 +353,17 @@ public:
 	 * is the cropped one at offset (0, 0); with the FFT convolver (double
 	 * precision) crop false keeps its uncropped frame less the PSF padding. */
 	void set_crop(bool crop) { m_crop = crop; }
+	/* The convolver of create_convolver's string form (src/convolve.cpp:
+	 * 562-584) on this backend: "brute" / "cuda" the direct convolution, "fft"
+	 * / "cuda-fft" the FFT convolution, "auto" (the default) the library's
+	 * choice. */
+	void set_convolver(const std::string &type)
+	{
+		if (type == "brute" || type == "cuda") m_convolver = PF_CONV_BRUTE;
+		else if (type == "fft" || type == "cuda-fft") m_convolver = PF_CONV_FFT;
+		else if (type == "auto") m_convolver = PF_CONV_AUTO;
+		else throw invalid_parameter("Convolver of type " + type + " is not supported");
+	}
 
 	/* Model::evaluate(Point &offset_out): the offset of the requested area in
 	 * the returned image */
@@ -358,6 +393,35 @@ public:
 		return out;
 	}
 
+	/* Model::get_stats: {profile name: stats} of the last evaluate() (keyed
+	 * by name as the reference's map: a later profile of the same name
+	 * replaces an earlier one); empty without PF_ENV_PROFILE. */
+	std::map<std::string, std::shared_ptr<ProfileStats>> get_stats() const
+	{
+		std::map<std::string, std::shared_ptr<ProfileStats>> out;
+		if (!m_env || m_profiles.empty()) return out;
+		pf_stage_times t = pf_stage_times();
+		std::vector<int64_t> counts(m_profiles.size() * 32, 0);
+		check(pf_env_last_model_stats(m_env->get(), &t, counts.data(), m_profiles.size()));
+		if (t.forward_calls == 0) return out;
+		unsigned long long all = 0;
+		for (size_t i = 0; i < m_profiles.size(); i++) all += counts[i * 32 + 30] + counts[i * 32 + 31];
+		for (size_t i = 0; i < m_profiles.size(); i++) {
+			auto st = std::make_shared<RadialProfileStats>();
+			st->cuda_times.setup = (nsecs_t)(t.setup_ms * 1e6);
+			st->cuda_times.evaluation = (nsecs_t)(t.eval_ms * 1e6);
+			st->cuda_times.convolution = (nsecs_t)(t.finish_ms * 1e6);
+			st->evaluations = (unsigned long long)(counts[i * 32 + 30] + counts[i * 32 + 31]);
+			for (int l = 0; l < 16; l++) {
+				if (counts[i * 32 + l]) st->integrations[l] = (unsigned long long)counts[i * 32 + l];
+			}
+			const double share = all ? (double)st->evaluations / all : 1.0 / m_profiles.size();
+			st->total = (nsecs_t)((t.setup_ms / m_profiles.size() + t.eval_ms * share) * 1e6);
+			out[m_profiles[i]->get_name()] = st;
+		}
+		return out;
+	}
+
 	pf_model_desc desc() const
 	{
 		pf_model_desc m = pf_model_desc();
@@ -375,7 +439,7 @@ public:
 		m.psf_h = m_psf.getHeight();
 		m.psf_scale_x = m_psf_scale.first;
 		m.psf_scale_y = m_psf_scale.second;
-		m.convolver = PF_CONV_AUTO;
+		m.convolver = m_convolver;
 		m.mask_offset = m_mask.empty() ? -1 : 0;
 		m.adjust_mask = m_adjust_mask ? 1 : 0;
 		m.mask_w = m_mask_w;
@@ -392,6 +456,7 @@ private:
 	bool m_return_finesampled = true;
 	bool m_adjust_mask = true;
 	bool m_crop = true;
+	int32_t m_convolver = PF_CONV_AUTO;
 	std::vector<uint8_t> m_mask;
 	unsigned int m_mask_w = 0, m_mask_h = 0;
 	Image m_psf;

@@ -405,6 +405,40 @@ class Model:
                                                     ctypes.byref(oh)))
         return out.reshape(oh.value, ow.value)
 
+    def get_stats(self):
+        """Model::get_stats (src/model.cpp:362-368): {profile name: stats} of
+        the last evaluate() on this model's environment, keyed by name as the
+        reference's map is (a later profile of the same name replaces an
+        earlier one). Needs an environment created with profile=True (an
+        empty dict otherwise). This backend evaluates all of a model's
+        profiles in fused passes timed as a whole, so each entry holds the
+        passes' device times ("pass_*_ms") and the profile's own counts --
+        subsample_pixel calls per recursion level ("integrations", as
+        get_profile_integrations) and evaluate_at calls ("evaluations") --
+        and "total_ms", the setup pass split evenly plus the evaluation pass
+        split by evaluations (pf_env_last_model_stats)."""
+        env = _env_or_default(self.env)
+        n = len(self.profiles)
+        t = _ffi.StageTimes()
+        counts = np.zeros(max(1, n) * 32, dtype=np.int64)
+        _check(_ffi.load().pf_env_last_model_stats(env.handle, ctypes.byref(t),
+                                                    counts.ctypes.data_as(ctypes.c_void_p), n))
+        if t.forward_calls == 0 or n == 0:
+            return {}
+        counts = counts.reshape(-1, 32)[:n]
+        evals = counts[:, 30] + counts[:, 31]
+        all_evals = int(evals.sum())
+        out = {}
+        for i, p in enumerate(self.profiles):
+            share = evals[i] / all_evals if all_evals else 1.0 / n
+            out[p.name] = {
+                "total_ms": t.setup_ms / n + t.eval_ms * share,
+                "pass_setup_ms": t.setup_ms, "pass_evaluation_ms": t.eval_ms, "pass_convolution_ms": t.finish_ms,
+                "evaluations": int(evals[i]),
+                "integrations": {lvl: int(c) for lvl, c in enumerate(counts[i, :16]) if c},
+            }
+        return out
+
     def get_profile_integrations(self):
         """Model::get_profile_integrations (src/model.cpp:370-381, a
         PROFIT_DEBUG build): per radial profile name, {recursion level:

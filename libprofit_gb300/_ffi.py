@@ -106,6 +106,7 @@ _SIGNATURES = {
     "pf_batch_depth": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "pf_batch_drawing_dims": (ctypes.c_int, [_P, _P]),
     "pf_batch_conv_info": (ctypes.c_int, [_P, _P, _P, _P]),
+    "pf_env_last_model_stats": (ctypes.c_int, [_P, _P, _P, ctypes.c_size_t]),
     "pf_batch_split_info": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     "pf_fits_write": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                      ctypes.c_uint32, ctypes.c_double, ctypes.c_double]),

@@ -17,6 +17,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpfcuda.so")
+CLI_SRC = os.path.join(HERE, "cli", "profit_cli.cpp")
+CLI = os.path.join(HERE, "profit-cli")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
@@ -68,9 +70,26 @@ def _compile(src, extra):
     return obj, r.stderr
 
 
+def build_cli():
+    """profit-cli for this backend (cli/profit_cli.cpp on include/profit_cuda.hpp),
+    next to the library."""
+    if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(
+            os.path.getmtime(p) for p in (LIB, CLI_SRC, os.path.join(ROOT, "include", "profit_cuda.hpp"))):
+        return CLI
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++11", "-O2", "-Wall", "-I" + os.path.join(ROOT, "include"), CLI_SRC,
+           "-o", CLI + ".tmp", "-L" + HERE, "-lpfcuda", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("profit-cli build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(CLI + ".tmp", CLI)
+    return CLI
+
+
 def build(force=False, verbose=False, extra=None):
-    """Compiles every CUDA translation unit for sm_103a and links the library."""
+    """Compiles every CUDA translation unit for sm_103a and links the library
+    (and profit-cli on it)."""
     if not force and up_to_date():
+        build_cli()
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     extra = list(extra or [])
@@ -88,6 +107,7 @@ def build(force=False, verbose=False, extra=None):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, LIB)
+    build_cli()
     return LIB
 
 

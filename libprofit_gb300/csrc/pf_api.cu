@@ -375,6 +375,9 @@ struct pf_env {
 		std::vector<float> host32;
 		void *d_conv = nullptr;                 // pf_convolve: source, output, kernel, mask
 		size_t conv_bytes = 0;
+		// the last model's statistics (PF_ENV_PROFILE): stage times, per-level counts
+		pf_stage_times last_times{};
+		std::vector<unsigned long long> last_counts;
 	} cache;
 };
 
@@ -407,6 +410,7 @@ struct pf_batch {
 	long long n_tiles = 0;
 	uint64_t total_out = 0;
 	bool record = false;
+	bool count_only = false;            // per-level counts recorded without the depth maps
 	int8_t *d_depth = nullptr;
 	size_t depth_total = 0;
 	unsigned long long *d_counts = nullptr;
@@ -1532,6 +1536,11 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 		b->params_dirty = false;
 	}
 	pf::DebugRec dbg{nullptr, nullptr};
+	if (b->count_only && !b->record) {
+		PF_CUDA_TRY(cudaMemsetAsync(b->d_counts, 0, sizeof(unsigned long long) * pf::kLevelCounts *
+		                                               std::max(1, n_profiles), stream));
+		dbg.counts = b->d_counts;
+	}
 	if (b->record) {
 		PF_CUDA_TRY(cudaMemsetAsync(b->d_depth, 0xff, std::max<size_t>(1, b->depth_total), stream));
 		PF_CUDA_TRY(cudaMemsetAsync(b->d_counts, 0, sizeof(unsigned long long) * pf::kLevelCounts *
@@ -2025,6 +2034,14 @@ pf_status pf_model_evaluate_masked(pf_env *env, const pf_model_desc *model, cons
 		s = pf_batch_create_masked(env, &m, 1, profiles, m.n_profiles, has_psf ? psf : nullptr, psf_len, mask,
 		                           mask_len, &c.batch);
 		if (s != PF_OK) return s;
+		if (env->flags & PF_ENV_PROFILE) {
+			// Model::get_stats: the profiling environment counts each profile's
+			// subsample_pixel calls and evaluations (pf_env_last_model_stats)
+			c.batch->count_only = true;
+			const cudaError_t e = cudaMalloc(&c.batch->d_counts, sizeof(unsigned long long) * pf::kLevelCounts *
+			                                                          std::max<size_t>(1, m.n_profiles));
+			if (e != cudaSuccess) return fail(PF_ERR_NO_MEMORY, std::string("pf_model_evaluate: ") + cudaGetErrorString(e));
+		}
 		c.model = m;
 		c.profiles.assign(profiles, profiles + m.n_profiles);
 		c.psf.assign(psf, psf + psf_len);
@@ -2059,6 +2076,31 @@ pf_status pf_model_evaluate_masked(pf_env *env, const pf_model_desc *model, cons
 	if (e != cudaSuccess) return fail(PF_ERR_CUDA, std::string("pf_model_evaluate: ") + cudaGetErrorString(e));
 	if (out_w) *out_w = b->mdev[0].out_w;
 	if (out_h) *out_h = b->mdev[0].out_h;
+	if (env->flags & PF_ENV_PROFILE) {
+		s = pf_batch_stats(b, &c.last_times, 1);
+		if (s != PF_OK) return s;
+		c.last_counts.assign((size_t)pf::kLevelCounts * m.n_profiles, 0);
+		if (m.n_profiles && b->d_counts) {
+			e = cudaMemcpy(c.last_counts.data(), b->d_counts, sizeof(unsigned long long) * c.last_counts.size(),
+			               cudaMemcpyDeviceToHost);
+			if (e != cudaSuccess) return fail(PF_ERR_CUDA, std::string("pf_model_evaluate: ") + cudaGetErrorString(e));
+		}
+	}
+	return PF_OK;
+}
+
+pf_status pf_env_last_model_stats(pf_env *env, pf_stage_times *times, int64_t *level_counts, size_t n_profiles)
+{
+	if (!env) return fail(PF_ERR_INVALID_PARAMETER, "env is NULL");
+	pf_env::Cache &c = env->cache;
+	std::lock_guard<std::mutex> lock(c.mu);
+	if (times) *times = c.last_times;
+	if (level_counts) {
+		const size_t have = c.last_counts.size() / pf::kLevelCounts;
+		for (size_t i = 0; i < n_profiles * pf::kLevelCounts; i++) {
+			level_counts[i] = i / pf::kLevelCounts < have ? (int64_t)c.last_counts[i] : 0;
+		}
+	}
 	return PF_OK;
 }
 
