@@ -130,3 +130,29 @@ def test_convolve_scratch_and_crop():
     got = conv.convolve(src, krn, crop=False, offset_out=off)
     np.testing.assert_array_equal(got, want)
     assert off == [0, 0]
+
+
+def test_get_stats():
+    """Model::get_stats (src/model.cpp:362-368) in a profiling environment:
+    one entry per profile name (a later profile of the same name replacing an
+    earlier one, as in the reference's map), the last evaluation's pass
+    times, and the profile's subsample_pixel calls per level, which equal
+    get_profile_integrations' (the reference's PROFIT_DEBUG counts)."""
+    import __graft_entry__
+    __graft_entry__.build_cuda()
+    import libprofit_gb300 as pg
+    import workloads as W
+    psf = W.moffat_psf(15, 3.0, 2.5)
+    env = pg.get_cuda_environment(0, use_double=True, profile=True)
+    m = _model(pg, env, _params(np.random.default_rng(11)), psf)
+    assert m.get_stats() == {}  # nothing evaluated yet
+    m.evaluate()
+    st = m.get_stats()
+    assert set(st) == {"sersic", "sky"}
+    s = st["sersic"]
+    assert s["pass_evaluation_ms"] > 0 and s["total_ms"] > 0 and s["evaluations"] > 0
+    assert s["integrations"] == {k: v for k, v in m.get_profile_integrations()["sersic"].items() if v}
+    plain = pg.get_cuda_environment(0, use_double=True)
+    m.set_cuda_env(plain)
+    m.evaluate()
+    assert m.get_stats() == {}
