@@ -66,7 +66,9 @@ enum pf_profile_kind {
 	PF_BROKENEXP = 5,
 	PF_SKY = 6,
 	PF_PSF = 7,
-	PF_NULL = 8
+	PF_NULL = 8,
+	PF_USER = 9   /* the user-defined radial profile compiled into the library, if any
+	                 (pf_user_profile_info; libprofit_gb300/user_profiles/example_moffat.cuh) */
 };
 
 /* Parameter slots of pf_profile_desc.par. Slots 0-5 are the radial
@@ -175,6 +177,15 @@ typedef struct pf_stage_times {
 	uint64_t forward_calls, backward_calls;
 	uint64_t kernel_launches;  /* this library's kernels launched (graph replays included) */
 } pf_stage_times;
+
+/* The user-defined radial profile compiled into this library (the CUDA
+ * counterpart of a RadialProfile subclass added to libprofit,
+ * docs/new_profile.rst): its Model::add_profile name and its own parameters
+ * (slots 6, 7, ... of pf_profile_desc.par) with their defaults.
+ * PF_ERR_UNSUPPORTED when the library was built without one. Profiles of
+ * kind PF_USER are evaluated in PF_ENV_DOUBLE environments only. */
+PF_API pf_status pf_user_profile_info(const char **name, const char *const **param_names,
+                                      const double **param_defaults, uint32_t *n_params);
 
 /* Last error message of the calling thread. */
 PF_API const char *pf_last_error(void);

@@ -178,6 +178,14 @@ public:
 		case PF_SERSIC: set_slots({1.0, 1.0}); break;
 		case PF_CORESERSIC: set_slots({1.0, 4.0, 1.0, 1.0, 1.0}); break;
 		case PF_MOFFAT: set_slots({3.0, 2.0}); break;
+		case PF_USER: {
+			const double *defaults = nullptr;
+			uint32_t count = 0;
+			if (pf_user_profile_info(nullptr, nullptr, &defaults, &count) == PF_OK) {
+				for (uint32_t i = 0; i < count; i++) m_desc.par[PF_P_X0 + i] = defaults[i];
+			}
+			break;
+		}
 		case PF_FERRER: set_slots({3.0, 1.0, 1.0}); break;
 		case PF_KING: set_slots({1.0, 3.0, 2.0}); break;
 		case PF_BROKENEXP: set_slots({1.0, 1.0, 1.0, 1.0}); break;
@@ -235,7 +243,10 @@ public:
 	}
 
 private:
-	bool is_radial() const { return m_desc.kind >= PF_SERSIC && m_desc.kind <= PF_BROKENEXP; }
+	bool is_radial() const
+	{
+		return (m_desc.kind >= PF_SERSIC && m_desc.kind <= PF_BROKENEXP) || m_desc.kind == PF_USER;
+	}
 
 	void set_slots(std::initializer_list<double> vals)
 	{
@@ -294,6 +305,14 @@ private:
 			for (size_t i = 0; i < it->second.size(); i++)
 				if (n == it->second[i]) return &m_desc.par[PF_P_X0 + i];
 		}
+		if (m_desc.kind == PF_USER) {  // the compiled-in user profile's own parameters
+			const char *const *names = nullptr;
+			uint32_t count = 0;
+			if (pf_user_profile_info(nullptr, &names, nullptr, &count) == PF_OK) {
+				for (uint32_t i = 0; i < count; i++)
+					if (n == names[i]) return &m_desc.par[PF_P_X0 + i];
+			}
+		}
 		return nullptr;
 	}
 
@@ -316,8 +335,13 @@ public:
 		    {"brokenexp", PF_BROKENEXP}, {"sky", PF_SKY},        {"psf", PF_PSF},
 		    {"null", PF_NULL}};
 		auto it = kinds.find(name);
-		if (it == kinds.end()) throw invalid_parameter("Unknown profile name: " + name);
-		m_profiles.push_back(std::make_shared<Profile>(name, it->second));
+		int kind = it == kinds.end() ? -1 : it->second;
+		const char *user = nullptr;  // the user-defined profile compiled into the library, if any
+		if (kind < 0 && pf_user_profile_info(&user, nullptr, nullptr, nullptr) == PF_OK && name == user) {
+			kind = PF_USER;
+		}
+		if (kind < 0) throw invalid_parameter("Unknown profile name: " + name);
+		m_profiles.push_back(std::make_shared<Profile>(name, kind));
 		return m_profiles.back();
 	}
 

@@ -105,7 +105,26 @@ _DEFAULTS = {
     "psf": {"xcen": 0.0, "ycen": 0.0, "mag": 0.0},
     "null": {},
 }
-_RADIAL = ("sersic", "coresersic", "moffat", "ferrer", "king", "brokenexp")
+_RADIAL = ["sersic", "coresersic", "moffat", "ferrer", "king", "brokenexp"]
+PF_USER = 9
+
+
+def _user_profile():
+    """The user-defined radial profile compiled into the loaded library
+    (pf_user_profile_info): registered under its name, with its parameters
+    and defaults, the first time an unknown profile name is asked for."""
+    name, names, defaults, n = ctypes.c_char_p(), ctypes.POINTER(ctypes.c_char_p)(), \
+        ctypes.POINTER(ctypes.c_double)(), ctypes.c_uint32()
+    if _ffi.load().pf_user_profile_info(ctypes.byref(name), ctypes.byref(names), ctypes.byref(defaults),
+                                        ctypes.byref(n)) != _ffi.PF_OK:
+        return None
+    kind = name.value.decode()
+    if kind not in KINDS:
+        KINDS[kind] = PF_USER
+        _SPECIFIC[kind] = {names[i].decode(): 6 + i for i in range(n.value)}
+        _DEFAULTS[kind] = {names[i].decode(): defaults[i] for i in range(n.value)}
+        _RADIAL.append(kind)
+    return kind
 
 
 class Profile:
@@ -113,7 +132,7 @@ class Profile:
 
     def __init__(self, name):
         kind = "ferrer" if name == "ferrers" else name
-        if kind not in KINDS:
+        if kind not in KINDS and _user_profile() != kind:
             raise InvalidParameter("Unknown profile name: %s" % name)
         self.name = name
         self.kind = kind

@@ -8,7 +8,9 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libpfcuda.so")
+# PF_CUDA_LIBRARY: another build of the library to load (one with a
+# user-defined profile compiled in, libprofit_gb300/build.py --out)
+LIB_PATH = os.environ.get("PF_CUDA_LIBRARY") or os.path.join(HERE, "libpfcuda.so")
 
 NPAR = 12
 
@@ -106,6 +108,10 @@ _SIGNATURES = {
     "pf_batch_depth": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "pf_batch_drawing_dims": (ctypes.c_int, [_P, _P]),
     "pf_batch_conv_info": (ctypes.c_int, [_P, _P, _P, _P]),
+    "pf_user_profile_info": (ctypes.c_int, [ctypes.POINTER(ctypes.c_char_p),
+                                            ctypes.POINTER(ctypes.POINTER(ctypes.c_char_p)),
+                                            ctypes.POINTER(ctypes.POINTER(ctypes.c_double)),
+                                            ctypes.POINTER(ctypes.c_uint32)]),
     "pf_env_last_model_stats": (ctypes.c_int, [_P, _P, _P, ctypes.c_size_t]),
     "pf_batch_split_info": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     "pf_fits_write": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,

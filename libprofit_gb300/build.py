@@ -51,15 +51,16 @@ def _deps():
     return out
 
 
-def up_to_date():
-    if not os.path.exists(LIB):
+def up_to_date(lib=LIB, user_profile=None):
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
-    return all(os.path.getmtime(p) <= t for p in _deps())
+    t = os.path.getmtime(lib)
+    deps = _deps() + ([user_profile] if user_profile else [])
+    return all(os.path.getmtime(p) <= t for p in deps)
 
 
-def _compile(src, extra):
-    obj = os.path.join(BUILD, src[:-3] + ".o")
+def _compile(src, extra, build_dir=BUILD):
+    obj = os.path.join(build_dir, src[:-3] + ".o")
     cmd = [nvcc()] + ARCH + COMMON + extra
     if src in NO_FMAD:
         cmd += ["-fmad=false"]
@@ -85,33 +86,53 @@ def build_cli():
     return CLI
 
 
-def build(force=False, verbose=False, extra=None):
+def build(force=False, verbose=False, extra=None, user_profile=None, out_dir=None):
     """Compiles every CUDA translation unit for sm_103a and links the library
-    (and profit-cli on it)."""
-    if not force and up_to_date():
-        build_cli()
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+    (and profit-cli on it). user_profile: a user-defined radial profile file
+    to compile in (csrc/user_profile.cuh), out_dir: where that library goes
+    (its own directory: libpfcuda.so and _build/), instead of next to this
+    file."""
+    lib, build_dir = LIB, BUILD
+    if out_dir:
+        lib, build_dir = os.path.join(out_dir, "libpfcuda.so"), os.path.join(out_dir, "_build")
+    if user_profile:
+        user_profile = os.path.abspath(user_profile)
+        if not os.path.exists(user_profile):
+            raise RuntimeError("user profile file not found: %s" % user_profile)
+    if not force and up_to_date(lib, user_profile):
+        if lib == LIB:
+            build_cli()
+        return lib
+    os.makedirs(build_dir, exist_ok=True)
     extra = list(extra or [])
+    if user_profile:
+        extra.append('-DPF_USER_PROFILE_FILE="%s"' % user_profile)
     srcs = sources()
     with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        results = list(ex.map(lambda s: _compile(s, extra), srcs))
+        results = list(ex.map(lambda s: _compile(s, extra, build_dir), srcs))
     objs = [o for o, _ in results]
     if verbose:
         for _, err in results:
             if err.strip():
                 sys.stderr.write(err)
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
-    os.replace(tmp, LIB)
-    build_cli()
-    return LIB
+    os.replace(tmp, lib)
+    if lib == LIB:
+        build_cli()
+    return lib
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose=True,
-          extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else None)
-    print(LIB)
+    import argparse
+    ap = argparse.ArgumentParser(description="builds libpfcuda.so (sm_103a) and profit-cli")
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("--ptxas", action="store_true", help="print ptxas register and spill figures")
+    ap.add_argument("--user-profile", help="a user-defined radial profile file to compile in")
+    ap.add_argument("--out", help="directory of the library built (default: next to this file)")
+    a = ap.parse_args()
+    print(build(force=a.force, verbose=True, extra=["-Xptxas", "-v"] if a.ptxas else None,
+                user_profile=a.user_profile, out_dir=a.out))

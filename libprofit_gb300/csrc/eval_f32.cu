@@ -497,7 +497,7 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 			else if (P.kind == PF_PSF) {
 				if (active && psf) has = psf_value(P, m, psf, px, row, add);
 			}
-			else if (P.kind <= PF_BROKENEXP) {
+			else if (is_radial(P.kind)) {
 				const f32::Shape sh = f32::load_shape(P);
 				const float dx = (xh - P.fxc_hi) + (xl - P.fxc_lo);
 				const float dy = (yh - P.fyc_hi) + (yl - P.fyc_lo);

@@ -224,7 +224,7 @@ eval_tiles64_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 						has = psf_pixel64(P, m, psf, px, row, add);
 					}
 				}
-				else if (P.kind <= PF_BROKENEXP) {
+				else if (is_radial(P.kind)) {
 					const double y = half_ybin + row * sy;
 					const double x = half_xbin + px * sx;
 					double xp, yp;

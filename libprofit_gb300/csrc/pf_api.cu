@@ -117,13 +117,13 @@ namespace {
 		}                                                                                              \
 	} while (0)
 
-bool is_radial(int kind) { return kind >= PF_SERSIC && kind <= PF_BROKENEXP; }
+using pf::is_radial;
 
 // Profile::validate of every kind, with the reference's messages.
 pf_status validate_profile(const pf_profile_desc &d, bool model_has_psf)
 {
 	const double *v = d.par;
-	if (d.kind < PF_SERSIC || d.kind > PF_NULL) {
+	if (d.kind < PF_SERSIC || d.kind > PF_USER || (d.kind == PF_USER && !pf::user::available)) {
 		return fail(PF_ERR_INVALID_PARAMETER, "Unknown profile kind " + std::to_string(d.kind));
 	}
 	const int rule = pf::param_rule(d.kind, v);  // src/radial.cpp:204-214 and each kind's validate()
@@ -568,6 +568,19 @@ bool same_profile_layout(const pf_profile_desc &a, const pf_profile_desc &b)
 extern "C" {
 
 const char *pf_last_error(void) { return g_last_error.c_str(); }
+
+pf_status pf_user_profile_info(const char **name, const char *const **param_names, const double **param_defaults,
+                               uint32_t *n_params)
+{
+	if (!pf::user::available) {
+		return fail(PF_ERR_UNSUPPORTED, "this library was built without a user-defined profile");
+	}
+	if (name) *name = pf::user::name();
+	if (param_names) *param_names = pf::user::param_names();
+	if (param_defaults) *param_defaults = pf::user::param_defaults();
+	if (n_params) *n_params = (uint32_t)pf::user::n_params;
+	return PF_OK;
+}
 
 const char *pf_version(void) { return "0.1.0 (libprofit 1.9.3 image path, sm_103a)"; }
 
@@ -1050,7 +1063,11 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 	b->sersic_only = true;
 	for (size_t i = 0; i < n_profiles; i++) {
 		const int k = b->h_profiles[i].kind;
-		if (k <= PF_BROKENEXP && k != PF_SERSIC) b->sersic_only = false;
+		if (k == PF_USER && !b->dbl) {
+			return fail(PF_ERR_UNSUPPORTED, "profile " + std::to_string(i) + ": the user-defined profile " +
+			                                    pf::user::name() + " is evaluated in double precision only");
+		}
+		if (is_radial(k) && k != PF_SERSIC) b->sersic_only = false;
 	}
 	if (!b->dbl) {
 		if (pf::eval32_items((long long)n_profiles, b->n_tiles) >= (1ll << 31)) {

@@ -15,6 +15,7 @@
 #include <cstdint>
 
 #include "../../include/pf_cuda.h"
+#include "user_profile.cuh"
 
 namespace pf {
 
@@ -78,6 +79,13 @@ struct ModelDev {
 	int32_t pad3;
 };
 
+// The radial profile kinds: the six of the reference and a user-defined one
+// compiled in (user_profile.cuh)
+__host__ __device__ constexpr bool is_radial(int kind)
+{
+	return (kind >= PF_SERSIC && kind <= PF_BROKENEXP) || (kind == PF_USER && user::available);
+}
+
 // The reference's parameter validation of the radial profiles, in its order:
 // RadialProfile::validate (src/radial.cpp:204-214), then each kind's own
 // (src/sersic.cpp:207-218, src/coresersic.cpp:61-82, src/moffat.cpp:60-71,
@@ -88,10 +96,13 @@ enum ParamRule : int {
 	PR_OK = 0, PR_AXRAT_LE0, PR_AXRAT_GT1, PR_BOX, PR_RE, PR_NSER, PR_RB, PR_CORE_A, PR_CORE_B, PR_FWHM, PR_CON,
 	PR_ROUT, PR_FERRER_A, PR_FERRER_B, PR_RC, PR_RT, PR_KING_A, PR_H1, PR_H2, PR_EXP_RB, PR_COUNT
 };
+// a user profile's validate() result k >= 1 is rule PR_COUNT - 1 + k (rules fit
+// in 5 bits: at most 11 user messages)
+static_assert(PR_COUNT + 11 <= 32, "rule numbers fit in 5 bits");
 
 __host__ __device__ inline int param_rule(int kind, const double *v)
 {
-	if (kind >= PF_SERSIC && kind <= PF_BROKENEXP) {
+	if (is_radial(kind)) {
 		if (v[PF_P_AXRAT] <= 0) return PR_AXRAT_LE0;
 		if (v[PF_P_AXRAT] > 1) return PR_AXRAT_GT1;
 		if (v[PF_P_BOX] <= -2) return PR_BOX;
@@ -127,6 +138,11 @@ __host__ __device__ inline int param_rule(int kind, const double *v)
 		if (v[7] <= 0) return PR_H2;
 		if (v[8] <= 0) return PR_EXP_RB;
 		break;
+	case PF_USER: {
+		const int k = user::validate(v);
+		if (k > 0 && k <= 11) return PR_COUNT - 1 + k;
+		break;
+	}
 	default:
 		break;
 	}
@@ -158,6 +174,7 @@ inline const char *param_rule_message(int rule)
 	    "h2 <= 0, must have h2 > 0",
 	    "rb <= 0, must have rb > 0",
 	};
+	if (rule >= PR_COUNT && user::available) return user::message(rule - PR_COUNT);
 	return rule > 0 && rule < PR_COUNT ? msg[rule] : "";
 }
 
@@ -310,7 +327,7 @@ __device__ __forceinline__ bool profile_reaches(const ProfileDev *__restrict__ p
 {
 	if (q >= m.n_profiles) return false;
 	const ProfileDev &P = profs[m.first_profile + q];
-	if (P.kind > PF_BROKENEXP) return P.kind == PF_SKY || P.kind == PF_PSF;
+	if (!is_radial(P.kind)) return P.kind == PF_SKY || P.kind == PF_PSF;
 	return !(row < P.bby0 || row > P.bby1 || col1 < P.bbx0 || col0 > P.bbx1);
 }
 

@@ -114,6 +114,8 @@ __device__ __forceinline__ double evaluate_at(const ProfileDev &p, double x, dou
 		return king_r(p, boxy_r(box, x, y));
 	case PF_BROKENEXP:
 		return broken_exponential(boxy_r(box, x, y), p.par[6], p.par[7], p.par[8], p.par[9]);
+	case PF_USER:
+		return user::evaluate_at(p.par, p.rscale, x, y);
 	}
 	return 0;
 }

@@ -56,6 +56,7 @@ __device__ double get_rscale(const ProfileDev &p)
 	case PF_FERRER: return p.par[6];
 	case PF_KING: return p.par[7];
 	case PF_BROKENEXP: return p.par[6] * 4;
+	case PF_USER: return user::get_rscale(p.par);
 	}
 	return 0;
 }
@@ -81,6 +82,8 @@ __device__ double get_lumtot(ProfileDev &p)
 		return 2 * M_PI * sf::qag(KingIntegrand{&p}, 0., p.par[7], false, 1e-4, 1e-4, nullptr);
 	case PF_BROKENEXP:  // src/brokenexponential.cpp:115-126
 		return 2 * M_PI * sf::qag(BrokenExpIntegrand{&p}, 0., 0., true, 1e-4, 1e-4, nullptr);
+	case PF_USER:
+		return user::get_lumtot(p.par, p.rscale);
 	}
 	return 0;
 }
@@ -121,6 +124,7 @@ __device__ double adjust_rscale_switch(const ProfileDev &p, const SersicSolves &
 	case PF_FERRER: return 0.5;       // src/ferrer.cpp:103-105
 	case PF_KING: return 0.5;         // src/king.cpp:98-100
 	case PF_BROKENEXP: return 1;      // src/brokenexponential.cpp:128-130
+	case PF_USER: return user::adjust_rscale_switch(p.par, p.rscale);
 	}
 	return 1;
 }
@@ -134,6 +138,7 @@ __device__ double adjust_rscale_max(const ProfileDev &p, const SersicSolves &sv)
 	case PF_FERRER: return 1;
 	case PF_KING: return 1.5;
 	case PF_BROKENEXP: return 100;
+	case PF_USER: return user::adjust_rscale_max(p.par, p.rscale);
 	}
 	return 0;
 }
@@ -146,6 +151,8 @@ __device__ double adjust_acc(const ProfileDev &p, double acc)
 		return sf::dmax(0.1, acc) / p.par[PF_P_AXRAT];
 	case PF_MOFFAT:  // src/moffat.cpp:97-99
 		return 0.1 / p.par[PF_P_AXRAT];
+	case PF_USER:
+		return user::adjust_acc(p.par, acc);
 	}
 	return acc;
 }
@@ -447,7 +454,7 @@ __device__ void radial_setup(ProfileDev &p, const ModelDev &m, double bn, const 
 	// Used to schedule the costly tiles first.
 	p.sbx0 = p.sby0 = 0;
 	p.sbx1 = p.sby1 = -1;
-	if (p.kind <= PF_BROKENEXP && !p.rough) {
+	if (is_radial(p.kind) && !p.rough) {
 		const double R = p.rscale_switch * p.rscale;
 		if (R == R && R < 1e12 && axrat > 0 && axrat <= 1) {
 			const double hx = R * ex, hy = R * ey;
@@ -551,7 +558,7 @@ __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs,
 		p.grad_ok = 0;
 		p.center_boost = 0;
 	}
-	else if (p.kind >= PF_SERSIC && p.kind <= PF_BROKENEXP) {
+	else if (is_radial(p.kind)) {
 		radial_setup(p, m, bn, sv, want_grad, err);
 	}
 	else if (p.kind == PF_SKY) {

@@ -159,3 +159,15 @@ def test_uncropped_fft_dimensions_and_offset(oracle_lib):
         ref, ref_off = oracle_lib.evaluate_uncropped_fft(oracle_lib.Case(w, h, profs, psf=spec["psf"]))
         assert m.output_dims() == (ref.shape[1], ref.shape[0])
         assert m.output_offset() == ref_off
+
+
+def test_no_user_profile_in_the_default_build():
+    """The default library has no user-defined profile compiled in: the C ABI
+    says so, and its name is unknown to Model.add_profile."""
+    import ctypes
+    import libprofit_gb300 as pg
+    from libprofit_gb300 import _ffi
+    name = ctypes.c_char_p()
+    assert _ffi.load().pf_user_profile_info(ctypes.byref(name), None, None, None) == _ffi.PF_ERR_UNSUPPORTED
+    with pytest.raises(pg.InvalidParameter, match="Unknown profile name: usermoffat"):
+        pg.Model(10, 10).add_profile("usermoffat")
