@@ -71,8 +71,9 @@ try:
 except pg.InvalidParameter as e:
     assert str(e) == "fwhm <= 0, must have fwhm > 0 (profile 0 of the batch)", str(e)
 # single precision and the adjoint refuse it
+env32 = pg.get_cuda_environment(0, use_double=False)
 try:
-    pg.Batch([W.to_model(spec, pg.get_cuda_environment(0, use_double=False))])
+    pg.Batch([W.to_model(spec, env32)], env32)
     raise SystemExit("single precision accepted")
 except pg.Unsupported as e:
     assert "double precision only" in str(e)
