@@ -162,9 +162,10 @@ typedef struct pf_batch pf_batch;
 #define PF_ENV_NO_AUTOTUNE 0x4u  /* single precision, PF_CONV_AUTO: choose brute force or FFT and
                                     the direct block shape by the fixed cost model, never by
                                     timing candidates on the device (reproducible choices) */
-#define PF_ENV_NO_SPLIT 0x8u     /* single precision: walk every subsampled pixel's tree in the
-                                    warp that meets it, none split off to other warps (the
-                                    images then sum each pixel's profiles strictly in order) */
+#define PF_ENV_NO_SPLIT 0x8u     /* walk every subsampled pixel's tree in the warp that meets
+                                    it: in single precision none split off to other warps, in
+                                    double precision no level-by-level evaluation (the images
+                                    then sum each pixel's profiles strictly in order) */
 
 /* Per-stage device times accumulated since the last reset (PF_ENV_PROFILE). */
 typedef struct pf_stage_times {
@@ -410,13 +411,16 @@ PF_API pf_status pf_batch_drawing_dims(pf_batch *batch, uint32_t *dims);
 PF_API pf_status pf_batch_conv_info(const pf_batch *batch, int32_t *forward_shape, int32_t *adjoint_shape,
                                     uint32_t *fft_models);
 
-/* No counterpart: how the last single-precision forward pass spread its
- * subsampling trees. boxes: sub-pixel boxes split off to other warps; roots:
- * (profile, pixel) trees they came from; pixels: drawing pixels with at least
- * one; refused: splits walked in place for lack of room in the batch's pool.
+/* No counterpart: how the last forward pass spread its subsampling trees.
+ * Single precision: boxes, sub-pixel boxes split off to other warps; roots,
+ * the (profile, pixel) trees they came from; pixels, drawing pixels with at
+ * least one; refused, splits walked in place for lack of room in the batch's
+ * pool. Double precision: boxes, the boxes evaluated level by level (level 0
+ * included); roots, the (profile, pixel) trees; pixels, drawing pixels with
+ * at least one; refused, trees or subtrees walked in place for lack of room.
  * Synchronises the batch's stream (stream as in pf_forward). All zero when
- * the batch does not split its trees: PF_ENV_DOUBLE and PF_ENV_NO_SPLIT
- * environments, and large automatic batches whose evaluation the autotuner
+ * the batch does not spread its trees: PF_ENV_NO_SPLIT environments, and
+ * large automatic single-precision batches whose evaluation the autotuner
  * timed faster with every tree walked where met. Any argument may be NULL. */
 PF_API pf_status pf_batch_split_info(pf_batch *batch, void *stream, uint32_t *boxes, uint32_t *roots,
                                      uint32_t *pixels, uint32_t *refused);

@@ -240,7 +240,7 @@ class CUDAEnv:
     profile, per-stage CUDA-event timing; autotune=False, the fixed cost model
     for the automatic convolution choice of large single-precision batches;
     split=False, every subsampled pixel's tree walked by the warp that meets
-    it (single precision; PF_ENV_NO_SPLIT)."""
+    it (PF_ENV_NO_SPLIT)."""
 
     def __init__(self, device=0, use_double=True, profile=False, autotune=True, split=True):
         lib = _ffi.load()
@@ -649,8 +649,8 @@ class Batch:
         return {"forward_shape": f.value, "adjoint_shape": a.value, "fft_models": n.value}
 
     def split_info(self, stream=None):
-        """How the last single-precision forward pass spread its subsampling
-        trees: {"boxes", "roots", "pixels", "refused"} (pf_batch_split_info)."""
+        """How the last forward pass spread its subsampling trees: {"boxes",
+        "roots", "pixels", "refused"} (pf_batch_split_info)."""
         v = [ctypes.c_uint32() for _ in range(4)]
         _check(_ffi.load().pf_batch_split_info(self._h, _stream_arg(stream), *[ctypes.byref(x) for x in v]))
         return dict(zip(("boxes", "roots", "pixels", "refused"), (x.value for x in v)))

@@ -12,6 +12,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -28,7 +29,7 @@ void launch_setup(const ModelDev *models, ProfileDev *profs, int n_profiles, int
                   bool have_psf, double *solves, int want_grad, cudaStream_t stream);
 void launch_eval64(const ModelDev *models, int n_models, const ProfileDev *profs, const double *psf_pool,
                    double *conv_img, double *direct_img, long long n_tiles, unsigned int *tile_counter,
-                   DebugRec dbg, int n_sm, cudaStream_t stream);
+                   DebugRec dbg, const LevelPool64 &pool, int n_levels, int n_sm, cudaStream_t stream);
 void launch_finish64(const ModelDev *models, int n_models, const double *psf_pool, const double *conv_img,
                      const double *direct_img, double *out, long long total_out, int fft_fine, int n_sm,
                      cudaStream_t stream);
@@ -404,6 +405,10 @@ struct pf_batch {
 	// FP32 eval: sub-pixel boxes split off to other warps (pf::SplitPool); no
 	// pool (box == nullptr) for FP64 batches and PF_ENV_NO_SPLIT
 	pf::SplitPool split{};
+	// FP64 eval: the subsampling trees level by level (pf::LevelPool64), over
+	// levels64 recursion levels; no pool for PF_ENV_NO_SPLIT
+	pf::LevelPool64 level64{};
+	int levels64 = 0;
 	bool sersic_only = false;           // every radial profile is a sersic: the FP32 kernels drop the other kinds
 	unsigned int *d_err = nullptr;
 	double *d_solves = nullptr;  // per profile: the inverse-gamma solves of the setup
@@ -670,6 +675,10 @@ void pf_batch_destroy(pf_batch *b)
 	cudaFree(b->split.box_val);
 	cudaFree(b->split.root);
 	cudaFree(b->split.pix);
+	cudaFree(b->level64.box);
+	cudaFree(b->level64.val);
+	cudaFree(b->level64.root);
+	cudaFree(b->level64.pix);
 	cudaFree(b->d_err);
 	cudaFree(b->d_solves);
 	cudaFree(b->d_depth);
@@ -1088,6 +1097,39 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 			PF_CUDA_TRY(cudaMalloc(&sp.root, sizeof(pf::SplitRoot) * sp.cap_root));
 			PF_CUDA_TRY(cudaMalloc(&sp.pix, sizeof(pf::SplitPixel) * sp.cap_pix));
 			sp.cnt = b->d_counter + 2;
+		}
+	}
+	if (b->dbl && !(env->flags & PF_ENV_NO_SPLIT)) {
+		// the recursion levels a tree can reach: max_recursions, 10 for a
+		// sersic's central pixel (src/sersic.cpp:339-345), at most kMaxLevels - 1
+		int top = -1;
+		for (size_t i = 0; i < n_profiles; i++) {
+			const pf::ProfileDev &d = b->h_profiles[i];
+			if (!is_radial(d.kind) || d.rough) continue;
+			unsigned int rec = d.max_recursions;
+			if (d.kind == PF_SERSIC && d.adjust) rec = std::max(rec, 10u);
+			top = std::max(top, (int)std::min<unsigned int>(rec, pf::kMaxLevels - 1));
+		}
+		if (top >= 0) {
+			// room for a subsampled profile per drawing pixel up to 2^21, twice
+			// as many boxes within [2^15, 2^20] and 64 sub-point values per box
+			// (about 640 MB at most); a tree that finds no room is walked by the
+			// warp that meets it instead
+			pf::LevelPool64 &lp = b->level64;
+			lp.cap_pix = (unsigned int)std::min<size_t>(std::max<size_t>(1, b->draw_total), 1u << 21);
+			lp.cap_root = lp.cap_pix;
+			lp.cap_box = (unsigned int)std::min<size_t>(std::max<size_t>(2 * (size_t)lp.cap_root, 1u << 15), 1u << 20);
+			if (const char *cap = std::getenv("PF_LEVEL_POOL_BOXES")) {
+				// a smaller pool, for exercising the walks that a full pool falls back to
+				lp.cap_box = (unsigned int)std::max(1l, std::min(std::atol(cap), (long)lp.cap_box));
+			}
+			lp.cap_val = 64ull * lp.cap_box;
+			PF_CUDA_TRY(cudaMalloc(&lp.box, sizeof(pf::LevelBox64) * lp.cap_box));
+			PF_CUDA_TRY(cudaMalloc(&lp.val, sizeof(double) * lp.cap_val));
+			PF_CUDA_TRY(cudaMalloc(&lp.root, sizeof(pf::LevelRoot64) * lp.cap_root));
+			PF_CUDA_TRY(cudaMalloc(&lp.pix, sizeof(pf::LevelPixel64) * lp.cap_pix));
+			lp.cnt = b->d_counter + 2;
+			b->levels64 = top + 1;
 		}
 	}
 	// [0] device-limit flags, [1] the last pass's first invalid profile (index << 5 | rule)
@@ -1572,7 +1614,8 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 	if (b->dbl) {
 		t = stage_begin(b, ST_EVAL, stream);
 		pf::launch_eval64(b->d_models, n_models, b->d_profiles, b->d_psf_norm, (double *)b->d_conv,
-		                  (double *)b->d_direct, b->n_tiles, b->d_counter, dbg, b->env->n_sm, stream);
+		                  (double *)b->d_direct, b->n_tiles, b->d_counter, dbg, b->level64, b->levels64,
+		                  b->env->n_sm, stream);
 		stage_end(b, t, stream);
 		t = stage_begin(b, ST_FINISH, stream);
 		pf::launch_finish64(b->d_models, n_models, b->d_psf_norm, (const double *)b->d_conv,
@@ -1619,7 +1662,10 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 	b->forward_calls++;
 	{
 		uint64_t k = (n_profiles > 0 ? 2 : 1) + 1;  // setup (solves, profiles), evaluation
-		if (b->dbl) k += 1 + (b->any_fft ? 3 : 0) + (b->any_fft_downsample ? 1 : 0);  // finish, FFT passes
+		if (b->dbl) {
+			k += 1 + (b->any_fft ? 3 : 0) + (b->any_fft_downsample ? 1 : 0);  // finish, FFT passes
+			k += b->level64.box ? b->levels64 : 0;  // the recursion levels
+		}
 		else {
 			k += b->split.box ? 1 : 0;  // the split boxes
 			k += b->n_out_tiles > 0 ? 1 : 0;
@@ -1714,6 +1760,17 @@ pf_status pf_batch_split_info(pf_batch *b, void *stream_ptr, uint32_t *boxes, ui
 		PF_CUDA_TRY(cudaMemcpy(c, b->split.cnt, sizeof(c), cudaMemcpyDeviceToHost));
 		c[1] = std::min(c[1], b->split.cap_root);  // failed allocations counted past the capacity
 		c[2] = std::min(c[2], b->split.cap_pix);
+	}
+	else if (b->level64.box) {
+		cudaStream_t stream = stream_ptr ? (cudaStream_t)stream_ptr : b->env->stream;
+		PF_CUDA_TRY(cudaSetDevice(b->env->device));
+		PF_CUDA_TRY(cudaStreamSynchronize(stream));
+		uint32_t l[pf::kSplitCounters] = {};
+		PF_CUDA_TRY(cudaMemcpy(l, b->level64.cnt, sizeof(l), cudaMemcpyDeviceToHost));
+		c[0] = std::min(l[pf::LC_BOX], b->level64.cap_box);
+		c[1] = std::min(l[pf::LC_ROOT], b->level64.cap_root);
+		c[2] = std::min(l[pf::LC_PIX], b->level64.cap_pix);
+		c[4] = l[pf::LC_REFUSED];
 	}
 	if (boxes) *boxes = c[0];
 	if (roots) *roots = c[1];

@@ -299,7 +299,72 @@ struct SplitPool {
 	unsigned int cap_box, cap_root, cap_pix;
 	unsigned int min_fail;     // failing level-0 sub-points for a split
 };
-constexpr int kSplitCounters = 8;
+// The FP64 path's subsampling trees, one recursion level at a time
+// (eval_f64.cu). A subsampled drawing pixel of a profile becomes a level-0
+// box (subsample_pixel's first call, src/radial.cpp:55-135); the level-L
+// kernel evaluates every level-L box's res x res sub-points, 16 per warp, and
+// the warp that evaluates a box's last sub-points sums its accepted values in
+// index order and allocates its failing sub-points' boxes at level L + 1 in
+// ascending order. A box whose children are all complete forms its value as
+// the depth-first walk does (the accepted sum, then the children's values in
+// ascending order, over res^2) in the warp that completed its last child, up
+// to the pixel. Counters, never waits.
+struct LevelBox64 {
+	double x0, x1, y0, y1;     // subsample_pixel's box
+	double accepted;           // the accepted sub-points' values, summed in index order
+	double value;              // (accepted + the children's values) / res^2, once complete
+	int32_t profile;
+	int32_t parent;            // -1: a drawing pixel's level-0 box
+	uint32_t rank;             // the parent's failing sub-point it refines (in ascending order)
+	uint32_t meta;             // res | level << 8 | max_rec << 16; kDeadBox: allocated without room
+	uint32_t pending;          // chunks not evaluated, then children not complete
+	uint32_t first_child, n_children;
+	int32_t root;              // its LevelRoot64
+	unsigned long long val_off;  // its res^2 sub-point values in LevelPool64::val
+	uint32_t mask[kMaskWords]; // the failing sub-points
+};
+constexpr uint32_t kDeadBox = 0xffffffffu;
+constexpr int kChunk64 = 16;  // sub-points per warp (a lane pair each: value, test)
+
+struct LevelRoot64 {
+	double flux_scale;
+	double value;              // flux_scale x the pixel value, once complete
+	int32_t pixel;             // its LevelPixel64
+	int32_t next;              // the pixel's next subsampled profile (profile order), -1 none
+	int32_t convolve;
+	int32_t deepest;           // deepest level + 1 (depth map)
+	int64_t depth_idx;         // index into the depth maps, -1 when not recording
+};
+
+struct LevelPixel64 {
+	int64_t idx;               // canvas index
+	double s_conv, s_direct;   // the tile's sums of the profiles not subsampled
+	int32_t first_root;
+	uint32_t pending;          // subsampled profiles not complete
+	int32_t conv_required;
+	int32_t pad;
+};
+
+// cnt: the LevelCnt words, reset by the setup kernel. bound[L] .. bound[L+1]
+// are the level-L boxes (bound[L+1] written by the last block of the kernel
+// that allocated them); done[k] counts the finished blocks of the tile kernel
+// (k = 0) and of the level-(k-1) kernel.
+enum LevelCnt : int {
+	LC_BOX = 0, LC_ROOT = 1, LC_VAL = 2 /* and 3: 64 bits */, LC_PIX = 4, LC_REFUSED = 5,
+	LC_BOUND = 8, LC_DONE = LC_BOUND + kMaxLevels + 2, LC_END = LC_DONE + kMaxLevels + 1,
+};
+
+struct LevelPool64 {
+	LevelBox64 *box;           // nullptr: no level pool (the tile warps walk the trees)
+	double *val;
+	LevelRoot64 *root;
+	LevelPixel64 *pix;
+	unsigned int *cnt;
+	unsigned int cap_box, cap_root, cap_pix;
+	unsigned long long cap_val;
+};
+
+constexpr int kSplitCounters = LC_END;  // the FP32 pool's 5 counters or the FP64 pool's LevelCnt words
 
 struct DebugRec {
 	int8_t *depth;             // per profile drawing-area depth maps, or nullptr

@@ -523,7 +523,8 @@ __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs,
 {
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		// the eval kernels' work counters (two: the FP32 one's phases), then the
-		// FP32 path's split-box pool counters (SplitPool::cnt)
+		// FP32 path's split-box pool counters (SplitPool::cnt) or the FP64
+		// path's level pool counters (LevelPool64::cnt)
 		for (int i = 0; i < 2 + kSplitCounters; i++) tile_counter[i] = 0;
 	}
 	const int t = blockIdx.x * blockDim.x + threadIdx.x;

@@ -159,3 +159,48 @@ def test_model_profile_integrations(env, name):
     kind = entry["spec"]["profiles"][0][0]
     want = {lvl: int(c) for lvl, c in enumerate(entry["counts"][0][:16]) if c > 0}
     assert got == {kind: want}
+
+
+def _forward_depth(m, env):
+    import torch
+    import libprofit_gb300 as pg
+    b = pg.Batch([m], env)
+    b.record_depth(True)
+    out = torch.zeros(b.total_pixels, dtype=torch.float64, device="cuda")
+    b.forward(out)
+    b.check()
+    maps = b.depth()
+    depth = [d for d, _ in maps]
+    counts = np.array([c for _, c in maps])
+    return out.cpu().numpy(), depth, counts, b.split_info()
+
+
+@pytest.mark.parametrize("pool_boxes", [None, "40"])
+def test_level_pool_equals_tile_walk(env, pool_boxes, monkeypatch):
+    """The subsampling trees evaluated level by level over the whole GPU give
+    the depth-first walk's results: the same depth maps and per-level counts,
+    and the same image bits for one-profile models (each box's sum is formed
+    in the walk's order; a pixel's subsampled profiles are added after its
+    other profiles, so several-profile pixels may differ by rounding). With
+    a pool of 40 boxes most trees find no room and are walked in place, at
+    level 0 by the tile's warp or deeper by the level kernel's."""
+    import libprofit_gb300 as pg
+    if pool_boxes:
+        monkeypatch.setenv("PF_LEVEL_POOL_BOXES", pool_boxes)
+    walk = pg.CUDAEnv(0, use_double=True, split=False)
+    roots = refused = 0
+    for name in sorted(GOLDEN):
+        entry = GOLDEN[name]
+        a, da, ca, info = _forward_depth(product_model(entry["spec"], entry["psf"], env), env)
+        w, dw, cw, winfo = _forward_depth(product_model(entry["spec"], entry["psf"], walk), walk)
+        assert winfo == {"boxes": 0, "roots": 0, "pixels": 0, "refused": 0}
+        roots += info["roots"]
+        refused += info["refused"]
+        assert len(da) == len(dw) and all(np.array_equal(x, y) for x, y in zip(da, dw)), name
+        assert np.array_equal(ca, cw), name
+        if len(entry["spec"]["profiles"]) == 1:
+            assert np.array_equal(a, w), name
+        else:
+            np.testing.assert_allclose(a, w, rtol=1e-14, atol=0, err_msg=name)
+    assert roots > 0
+    assert (refused > 0) == bool(pool_boxes)
