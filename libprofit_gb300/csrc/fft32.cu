@@ -1,429 +1,51 @@
-// FFT convolution of the single-precision batched path: forward (the
-// reference's FFTConvolver, src/convolve.cpp:233-312, restated as a 2-D real
-// convolution) and its adjoint (the cotangent correlated with the PSF).
-//
-// Per model, with M_x, M_y powers of two >= crop + psf (no wrap-around reaches
-// a kept output):
-//   forward  out  = crop(IFFT(FFT(src) * S)) / (M_x M_y) + direct
-//   adjoint  gsrc = drawing(IFFT(FFT(embed(gout)) * conj(S))) / (M_x M_y)
-// where S is the PSF's spectrum (made once per batch) and embed places the
-// cotangent where the forward crop takes its outputs. Three passes:
-//   rows    two real rows per complex transform (z = a + i b), bins 0..M_x/2
-//           of both unpacked from Z(k) and conj(Z(M_x - k));
-//   columns 16 bin columns per block (fewer when long), forward transform,
-//           product with the spectrum, inverse transform, the kept rows back
-//           in place;
-//   rows    two Hermitian rows per inverse transform (Z = A + i B), the real
-//           and imaginary parts the two output rows.
-// Transforms: Stockham autosort radix-8 (radix-4 / -2 last) stages in shared
-// memory, N / 8 threads per transform each holding eight values in
-// registers (formulation of Govindaraju et al., "High performance discrete
-// Fourier transforms on graphics processors", SC 2008); twiddles from a table
-// of exp(-2 pi i k / 8192) computed in FP64. Shared-memory element i of a
-// transform sits at i + i / 8, so the stride-8 stores of the first stages hit
-// distinct banks.
-#include <cstdint>
-
-#include "pf_device.cuh"
+// FFT convolution of the single-precision batched path (kernels in
+// fft32.cuh): the lengths, the twiddle tables, the launches of the first
+// group of lengths and the dispatch to the other groups' translation units.
+#include "fft32.cuh"
 
 namespace pf {
 
 namespace {
 
-constexpr int kTwN = 8192;  // twiddle table length: exp(-2 pi i k / kTwN)
+__constant__ int c_sizes[kNumSizes] = {PF_FFT32_SIZES(PF_FFT32_LIST)};
 
-enum { F_FORWARD = 0, F_ADJOINT = 1, F_SPECTRUM = 2 };
-
-__device__ __forceinline__ float2 cmulf(float2 a, float2 b)
-{
-	return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ float2 caddf(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csubf(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-// a * (-i) (forward) or a * (+i) (inverse)
-template <bool INV>
-__device__ __forceinline__ float2 rot90(float2 a)
-{
-	return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
-}
-
-__device__ __forceinline__ int pidx(int i) { return i + (i >> 3); }
-
-template <bool INV>
-__device__ __forceinline__ float2 twiddle(const float2 *__restrict__ table, int k)
-{
-	float2 w = __ldg(table + k);
-	if (INV) w.y = -w.y;
-	return w;
-}
-
-template <bool INV>
-__device__ __forceinline__ void dft2(float2 *v)
-{
-	const float2 a = v[0], b = v[1];
-	v[0] = caddf(a, b);
-	v[1] = csubf(a, b);
-}
-
-template <bool INV>
-__device__ __forceinline__ void dft4(float2 *v)
-{
-	const float2 p0 = caddf(v[0], v[2]), p1 = csubf(v[0], v[2]);
-	const float2 p2 = caddf(v[1], v[3]), p3 = rot90<INV>(csubf(v[1], v[3]));
-	v[0] = caddf(p0, p2);
-	v[2] = csubf(p0, p2);
-	v[1] = caddf(p1, p3);
-	v[3] = csubf(p1, p3);
-}
-
-// 8-point DFT, natural order in and out (decimation in frequency)
-template <bool INV>
-__device__ __forceinline__ void dft8(float2 *v)
-{
-	constexpr float h = 0.70710678118654752f;
-	float2 u[4], w[4];
-#pragma unroll
-	for (int n = 0; n < 4; n++) {
-		u[n] = caddf(v[n], v[n + 4]);
-		w[n] = csubf(v[n], v[n + 4]);
-	}
-	// w[n] *= exp(-+ 2 pi i n / 8)
-	w[1] = INV ? make_float2(h * (w[1].x - w[1].y), h * (w[1].x + w[1].y))
-	           : make_float2(h * (w[1].x + w[1].y), h * (w[1].y - w[1].x));
-	w[2] = rot90<INV>(w[2]);
-	w[3] = INV ? make_float2(-h * (w[3].x + w[3].y), h * (w[3].x - w[3].y))
-	           : make_float2(h * (w[3].y - w[3].x), -h * (w[3].x + w[3].y));
-	dft4<INV>(u);
-	dft4<INV>(w);
-#pragma unroll
-	for (int k = 0; k < 4; k++) {
-		v[2 * k] = u[k];
-		v[2 * k + 1] = w[k];
-	}
-}
-
-template <int R, bool INV>
-__device__ __forceinline__ void dft(float2 *v)
-{
-	if constexpr (R == 8) dft8<INV>(v);
-	else if constexpr (R == 4) dft4<INV>(v);
-	else dft2<INV>(v);
-}
-
-// One radix-R Stockham stage over the N points of buf (padded layout) by
-// thread t < N / 8 of the transform. All threads of the block take part.
-template <int N, int R, int NS, bool INV>
-__device__ __forceinline__ void stage(float2 *buf, int t, const float2 *__restrict__ table)
-{
-	constexpr int G = 8 / R;  // butterfly groups per thread
-	float2 v[8];
-#pragma unroll
-	for (int q = 0; q < G; q++) {
-		const int j = t + q * (N / 8);
-#pragma unroll
-		for (int r = 0; r < R; r++) v[q * R + r] = buf[pidx(j + r * (N / R))];
-	}
-	__syncthreads();
-#pragma unroll
-	for (int q = 0; q < G; q++) {
-		const int j = t + q * (N / 8);
-		const int jm = j & (NS - 1);
-		if constexpr (NS > 1) {
-#pragma unroll
-			for (int r = 1; r < R; r++) v[q * R + r] = cmulf(v[q * R + r], twiddle<INV>(table, jm * r * (kTwN / (NS * R))));
-		}
-		dft<R, INV>(v + q * R);
-		const int base = (j - jm) * R + jm;
-#pragma unroll
-		for (int r = 0; r < R; r++) buf[pidx(base + r * NS)] = v[q * R + r];
-	}
-	__syncthreads();
-}
-
-// In-place FFT of the N points of buf (natural order in and out).
-template <int N, bool INV>
-__device__ __forceinline__ void fft(float2 *buf, int t, const float2 *__restrict__ table)
-{
-	static_assert(N >= 64 && N <= 8192 && (N & (N - 1)) == 0, "power of two in [64, 8192]");
-	stage<N, 8, 1, INV>(buf, t, table);
-	stage<N, 8, 8, INV>(buf, t, table);
-	if constexpr (N == 128) stage<N, 2, 64, INV>(buf, t, table);
-	if constexpr (N == 256) stage<N, 4, 64, INV>(buf, t, table);
-	if constexpr (N >= 512) stage<N, 8, 64, INV>(buf, t, table);
-	if constexpr (N == 1024) stage<N, 2, 512, INV>(buf, t, table);
-	if constexpr (N == 2048) stage<N, 4, 512, INV>(buf, t, table);
-	if constexpr (N >= 4096) stage<N, 8, 512, INV>(buf, t, table);
-	if constexpr (N == 8192) stage<N, 2, 4096, INV>(buf, t, table);
-}
-
-template <int N>
-__host__ __device__ constexpr int row_ffts() { return (N / 8) >= 256 ? 1 : 256 / (N / 8); }  // transforms per row block
-template <int N>
-__host__ __device__ constexpr int col_ffts() { return (N / 8) >= 64 ? 1024 / (N / 8) < 16 ? 1024 / (N / 8) : 16 : 16; }
-template <int N>
-__host__ __device__ constexpr int row_stride() { return N + N / 8; }                     // padded length
-template <int N>
-__host__ __device__ constexpr int col_stride() { return N + N / 8 + 1; }                 // = 1 or 9 mod 16: columns on distinct banks
-
-struct Job {
-	int model, first, count, pad;
-};
-
-// cotangent of crop pixel (cx, cy) (SUM-downsampling aware; zero where the
-// calculation mask zeroed the forward convolution)
-__device__ __forceinline__ float cot_crop(const ModelDev &m, const float *gout, int cx, int cy)
-{
-	if (!evaluated(m, cx + (int)m.pad_x, cy + (int)m.pad_y)) return 0.f;
-	if (m.fs > 1 && !m.return_fs) return gout[m.out_off + (size_t)(cy / m.fs) * m.out_w + cx / m.fs];
-	return gout[m.out_off + (size_t)cy * m.out_w + cx];
-}
-
-// Pass 1: rows. Job rows first .. first + count - 1 (of the source image,
-// the cotangent or the PSF), two per transform; bins 0..N/2 to dst rows.
-template <int N, int MODE>
-__global__ void __launch_bounds__(row_ffts<N>() * (N / 8))
-rows_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, const float *__restrict__ src,
-            const float *__restrict__ psf, float2 *__restrict__ work, float2 *__restrict__ spec,
-            const float2 *__restrict__ table)
-{
-	constexpr int F = row_ffts<N>(), PS = row_stride<N>(), NB = N / 2 + 1;
-	extern __shared__ float2 fsm[];
-	float2 *buf = fsm;
-	const Job jb = jobs[blockIdx.x];
-	const ModelDev &m = models[jb.model];
-	const int f = threadIdx.x / (N / 8), t = threadIdx.x % (N / 8);
-	// source columns and their offset in the transform
-	int w, xoff = 0;
-	if (MODE == F_FORWARD) w = (int)m.draw_w;
-	else if (MODE == F_ADJOINT) {
-		w = (int)m.crop_w;
-		xoff = (int)m.pad_x + (int)m.psf_w - 1 - (int)m.psf_w / 2;
-	}
-	else w = (int)m.psf_w;
-	for (int i = threadIdx.x; i < F * N; i += blockDim.x) {
-		const int ff = i / N, c = i % N;
-		const int r0 = jb.first + 2 * ff, r1 = r0 + 1;
-		const int x = c - xoff;
-		float2 v = make_float2(0.f, 0.f);
-		if (x >= 0 && x < w) {
-			if (MODE == F_FORWARD) {
-				const float *s = src + m.draw_off;
-				if (r0 < jb.first + jb.count) v.x = s[(size_t)r0 * m.draw_w + x];
-				if (r1 < jb.first + jb.count) v.y = s[(size_t)r1 * m.draw_w + x];
-			}
-			else if (MODE == F_ADJOINT) {
-				if (r0 < jb.first + jb.count) v.x = cot_crop(m, src, x, r0);
-				if (r1 < jb.first + jb.count) v.y = cot_crop(m, src, x, r1);
-			}
-			else {
-				const float *k = psf + m.psf_off;
-				if (r0 < jb.first + jb.count) v.x = k[(size_t)r0 * m.psf_w + x];
-				if (r1 < jb.first + jb.count) v.y = k[(size_t)r1 * m.psf_w + x];
-			}
-		}
-		buf[ff * PS + pidx(c)] = v;
-	}
-	__syncthreads();
-	fft<N, false>(buf + f * PS, t, table);
-	// unpack: A(k) = (Z(k) + conj Z(N-k)) / 2, B(k) = (Z(k) - conj Z(N-k)) / (2 i)
-	float2 *dst = MODE == F_SPECTRUM ? spec + m.fft_spec_off : work + m.fft_work_off;
-	const int nbr = (int)m.fft_mx / 2 + 1;  // = NB
-	for (int i = threadIdx.x; i < F * NB; i += blockDim.x) {
-		const int ff = i / NB, k = i % NB;
-		const int r0 = jb.first + 2 * ff;
-		const float2 z = buf[ff * PS + pidx(k)], zm = buf[ff * PS + pidx((N - k) & (N - 1))];
-		if (r0 < jb.first + jb.count) dst[(size_t)r0 * nbr + k] = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
-		if (r0 + 1 < jb.first + jb.count) dst[(size_t)(r0 + 1) * nbr + k] = make_float2(0.5f * (z.y + zm.y), 0.5f * (zm.x - z.x));
-	}
-}
-
-// Pass 2: columns of bins. Job: bin columns first .. first + count - 1.
-template <int N, int MODE>
-__global__ void __launch_bounds__(col_ffts<N>() * (N / 8))
-cols_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, float2 *__restrict__ work,
-            float2 *__restrict__ spec, const float2 *__restrict__ table)
-{
-	constexpr int F = col_ffts<N>(), PS = col_stride<N>();
-	extern __shared__ float2 fsm[];
-	float2 *cbuf = fsm;
-	const Job jb = jobs[blockIdx.x];
-	const ModelDev &m = models[jb.model];
-	const int nb = (int)m.fft_mx / 2 + 1;
-	const int f = threadIdx.x / (N / 8), t = threadIdx.x % (N / 8);
-	float2 *col = MODE == F_SPECTRUM ? spec + m.fft_spec_off : work + m.fft_work_off;
-	// rows present in the input and their place in the transform
-	int rows_in, yoff = 0;
-	if (MODE == F_FORWARD) rows_in = (int)m.draw_h;
-	else if (MODE == F_ADJOINT) {
-		rows_in = (int)m.crop_h;
-		yoff = (int)m.pad_y + (int)m.psf_h - 1 - (int)m.psf_h / 2;
-	}
-	else rows_in = (int)m.psf_h;
-	for (int i = threadIdx.x; i < F * N; i += blockDim.x) {
-		const int rg = i / F, ff = i % F;  // transform row, column within the job
-		const int r = rg - yoff;
-		float2 v = make_float2(0.f, 0.f);
-		if (ff < jb.count && r >= 0 && r < rows_in) v = col[(size_t)r * nb + jb.first + ff];
-		cbuf[ff * PS + pidx(rg)] = v;
-	}
-	__syncthreads();
-	fft<N, false>(cbuf + f * PS, t, table);
-	if (MODE == F_SPECTRUM) {
-		for (int i = threadIdx.x; i < F * N; i += blockDim.x) {
-			const int rg = i / F, ff = i % F;
-			if (ff < jb.count) col[(size_t)rg * nb + jb.first + ff] = cbuf[ff * PS + pidx(rg)];
-		}
-		return;
-	}
-	const float2 *sp = spec + m.fft_spec_off;
-	for (int i = threadIdx.x; i < F * N; i += blockDim.x) {
-		const int rg = i / F, ff = i % F;
-		if (ff >= jb.count) continue;
-		float2 s = sp[(size_t)rg * nb + jb.first + ff];
-		if (MODE == F_ADJOINT) s.y = -s.y;
-		cbuf[ff * PS + pidx(rg)] = cmulf(cbuf[ff * PS + pidx(rg)], s);
-	}
-	__syncthreads();
-	fft<N, true>(cbuf + f * PS, t, table);
-	// kept rows: forward, the crop's (from its offset); adjoint, the drawing area's
-	const int rows_out = MODE == F_FORWARD ? (int)m.crop_h : (int)m.draw_h;
-	const int keep = MODE == F_FORWARD ? (int)m.pad_y + (int)m.psf_h - 1 - (int)m.psf_h / 2 : 0;
-	for (int i = threadIdx.x; i < F * rows_out; i += blockDim.x) {
-		const int r = i / F, ff = i % F;
-		if (ff < jb.count) col[(size_t)r * nb + jb.first + ff] = cbuf[ff * PS + pidx(r + keep)];
-	}
-}
-
-// Pass 3: inverse rows. Job rows first .. first + count - 1 of the kept rows,
-// two per transform: Z(k) = A(k) + i B(k) over all k, A and B Hermitian.
-template <int N, int MODE>
-__global__ void __launch_bounds__(row_ffts<N>() * (N / 8))
-irows_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, const float2 *__restrict__ work,
-             const float *__restrict__ direct, float *__restrict__ out, const float2 *__restrict__ table)
-{
-	constexpr int F = row_ffts<N>(), PS = row_stride<N>();
-	extern __shared__ float2 fsm[];
-	float2 *buf = fsm;
-	const Job jb = jobs[blockIdx.x];
-	const ModelDev &m = models[jb.model];
-	const int nb = (int)m.fft_mx / 2 + 1;
-	const int f = threadIdx.x / (N / 8), t = threadIdx.x % (N / 8);
-	const float2 *src = work + m.fft_work_off;
-	for (int i = threadIdx.x; i < F * N; i += blockDim.x) {
-		const int ff = i / N, k = i % N;
-		const int r0 = jb.first + 2 * ff, r1 = r0 + 1;
-		const int kk = k <= N / 2 ? k : N - k;
-		float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
-		if (r0 < jb.first + jb.count) a = src[(size_t)r0 * nb + kk];
-		if (r1 < jb.first + jb.count) b = src[(size_t)r1 * nb + kk];
-		if (k > N / 2) {
-			a.y = -a.y;
-			b.y = -b.y;
-		}
-		buf[ff * PS + pidx(k)] = make_float2(a.x - b.y, a.y + b.x);
-	}
-	__syncthreads();
-	fft<N, true>(buf + f * PS, t, table);
-	const float scale = 1.f / ((float)m.fft_mx * (float)m.fft_my);
-	if (MODE == F_FORWARD) {
-		const int off_x = (int)m.pad_x + (int)m.psf_w - 1 - (int)m.psf_w / 2;
-		const bool downsample = m.fs > 1 && !m.return_fs;
-		const int cw = (int)m.crop_w;
-		for (int i = threadIdx.x; i < F * 2 * cw; i += blockDim.x) {
-			const int ff = i / (2 * cw), rem = i % (2 * cw), half = rem / cw, c = rem % cw;
-			const int r = jb.first + 2 * ff + half;
-			if (r >= jb.first + jb.count) continue;
-			const float2 z = buf[ff * PS + pidx(c + off_x)];
-			// the convolution is zero where the calculation mask is; the output
-			// is multiplied by the model's mask at the end
-			const float conv = evaluated(m, c + (int)m.pad_x, r + (int)m.pad_y) ? (half ? z.y : z.x) * scale : 0.f;
-			const float v = direct[m.draw_off + (size_t)(r + m.pad_y) * m.draw_w + c + m.pad_x] + conv;
-			if (downsample) {
-				if (kept(m, c / (int)m.fs, r / (int)m.fs))
-					atomicAdd(&out[m.out_off + (size_t)(r / m.fs) * m.out_w + c / m.fs], v);
-			}
-			else out[m.out_off + (size_t)r * m.out_w + c] = kept(m, c, r) ? v : 0.f;
-		}
-	}
-	else {
-		const int dw = (int)m.draw_w;
-		for (int i = threadIdx.x; i < F * 2 * dw; i += blockDim.x) {
-			const int ff = i / (2 * dw), rem = i % (2 * dw), half = rem / dw, c = rem % dw;
-			const int r = jb.first + 2 * ff + half;
-			if (r >= jb.first + jb.count) continue;
-			const float2 z = buf[ff * PS + pidx(c)];
-			out[m.draw_off + (size_t)r * m.draw_w + c] = (half ? z.y : z.x) * scale;
-		}
-	}
-}
-
+// every length's table: tw[tw_offset(n) + k] = exp(-2 pi i k / n)
 __global__ void twiddle32_kernel(float2 *tw)
 {
-	const int k = blockIdx.x * blockDim.x + threadIdx.x;
-	if (k >= kTwN) return;
+	int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= kTwTotal) return;
+	float2 *out = tw + k;
+	int n = 0;
+	for (int i = 0; i < kNumSizes; i++) {
+		n = c_sizes[i];
+		if (k < n) break;
+		k -= n;
+	}
 	double s, c;
-	sincospi(-2.0 * k / kTwN, &s, &c);
-	tw[k] = make_float2((float)c, (float)s);
+	sincospi(-2.0 * k / n, &s, &c);
+	*out = make_float2((float)c, (float)s);
 }
 
-template <int N>
-constexpr size_t rows_smem() { return sizeof(float2) * row_ffts<N>() * row_stride<N>(); }
-template <int N>
-constexpr size_t cols_smem() { return sizeof(float2) * col_ffts<N>() * col_stride<N>(); }
-
-template <int N>
-cudaError_t configure_n()
+bool fft32_launch_a(int pass, int mode, int n, int n_jobs, const ModelDev *models, const Job *jobs, const float *src,
+                    const float *psf, float2 *work, float2 *spec, const float *direct, float *out, const float2 *tw,
+                    cudaStream_t stream)
 {
-	const int rs = (int)rows_smem<N>(), cs = (int)cols_smem<N>();
-	const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-	cudaError_t e = cudaFuncSetAttribute(rows_kernel<N, F_FORWARD>, a, rs);
-	if (e == cudaSuccess) e = cudaFuncSetAttribute(rows_kernel<N, F_ADJOINT>, a, rs);
-	if (e == cudaSuccess) e = cudaFuncSetAttribute(rows_kernel<N, F_SPECTRUM>, a, rs);
-	if (e == cudaSuccess) e = cudaFuncSetAttribute(irows_kernel<N, F_FORWARD>, a, rs);
-	if (e == cudaSuccess) e = cudaFuncSetAttribute(irows_kernel<N, F_ADJOINT>, a, rs);
-	if (e == cudaSuccess) e = cudaFuncSetAttribute(cols_kernel<N, F_FORWARD>, a, cs);
-	if (e == cudaSuccess) e = cudaFuncSetAttribute(cols_kernel<N, F_ADJOINT>, a, cs);
-	if (e == cudaSuccess) e = cudaFuncSetAttribute(cols_kernel<N, F_SPECTRUM>, a, cs);
-	return e;
-}
-
-template <int N>
-void launch_n(int pass, int mode, int n_jobs, const ModelDev *models, const Job *jobs, const float *src,
-              const float *psf, float2 *work, float2 *spec, const float *direct, float *out, const float2 *tw,
-              cudaStream_t stream)
-{
-	const int rthreads = row_ffts<N>() * (N / 8), cthreads = col_ffts<N>() * (N / 8);
-	const size_t rsmem = rows_smem<N>(), csmem = cols_smem<N>();
-	if (pass == 0) {
-		if (mode == F_FORWARD) rows_kernel<N, F_FORWARD><<<n_jobs, rthreads, rsmem, stream>>>(models, jobs, src, psf, work, spec, tw);
-		else if (mode == F_ADJOINT) rows_kernel<N, F_ADJOINT><<<n_jobs, rthreads, rsmem, stream>>>(models, jobs, src, psf, work, spec, tw);
-		else rows_kernel<N, F_SPECTRUM><<<n_jobs, rthreads, rsmem, stream>>>(models, jobs, src, psf, work, spec, tw);
+	switch (n) {
+		PF_FFT32_SIZES_A(PF_FFT32_GROUP_LAUNCH)
 	}
-	else if (pass == 1) {
-		if (mode == F_FORWARD) cols_kernel<N, F_FORWARD><<<n_jobs, cthreads, csmem, stream>>>(models, jobs, work, spec, tw);
-		else if (mode == F_ADJOINT) cols_kernel<N, F_ADJOINT><<<n_jobs, cthreads, csmem, stream>>>(models, jobs, work, spec, tw);
-		else cols_kernel<N, F_SPECTRUM><<<n_jobs, cthreads, csmem, stream>>>(models, jobs, work, spec, tw);
-	}
-	else {
-		if (mode == F_FORWARD) irows_kernel<N, F_FORWARD><<<n_jobs, rthreads, rsmem, stream>>>(models, jobs, work, direct, out, tw);
-		else irows_kernel<N, F_ADJOINT><<<n_jobs, rthreads, rsmem, stream>>>(models, jobs, work, direct, out, tw);
-	}
+	return false;
 }
 
 }  // namespace
 
-// Rows per row-pass job and bin columns per column-pass job for transforms of n points.
+// Rows per row-pass job and bin columns per column-pass job for transforms of
+// n points (0: no transform of that length).
 int fft32_rows_per_job(int n)
 {
 	switch (n) {
-	case 64: return 2 * row_ffts<64>();
-	case 128: return 2 * row_ffts<128>();
-	case 256: return 2 * row_ffts<256>();
-	case 512: return 2 * row_ffts<512>();
-	case 1024: return 2 * row_ffts<1024>();
-	case 2048: return 2 * row_ffts<2048>();
-	case 4096: return 2 * row_ffts<4096>();
-	case 8192: return 2 * row_ffts<8192>();
+#define PF_FFT32_ROWS(N) \
+	case N: return 2 * row_ffts<N>();
+		PF_FFT32_SIZES(PF_FFT32_ROWS)
 	}
 	return 0;
 }
@@ -431,34 +53,35 @@ int fft32_rows_per_job(int n)
 int fft32_cols_per_job(int n)
 {
 	switch (n) {
-	case 64: return col_ffts<64>();
-	case 128: return col_ffts<128>();
-	case 256: return col_ffts<256>();
-	case 512: return col_ffts<512>();
-	case 1024: return col_ffts<1024>();
-	case 2048: return col_ffts<2048>();
-	case 4096: return col_ffts<4096>();
-	case 8192: return col_ffts<8192>();
+#define PF_FFT32_COLS(N) \
+	case N: return col_ffts<N>();
+		PF_FFT32_SIZES(PF_FFT32_COLS)
 	}
 	return 0;
 }
 
+// the smallest transform length >= n (0: none)
+int fft32_size_at_least(int n)
+{
+	for (int i = 0; i < kNumSizes; i++)
+		if (kSizes[i] >= n) return kSizes[i];
+	return 0;
+}
+
+int fft32_twiddle_len() { return kTwTotal; }
+
 cudaError_t fft32_configure()
 {
-	cudaError_t e = configure_n<64>();
-	if (e == cudaSuccess) e = configure_n<128>();
-	if (e == cudaSuccess) e = configure_n<256>();
-	if (e == cudaSuccess) e = configure_n<512>();
-	if (e == cudaSuccess) e = configure_n<1024>();
-	if (e == cudaSuccess) e = configure_n<2048>();
-	if (e == cudaSuccess) e = configure_n<4096>();
-	if (e == cudaSuccess) e = configure_n<8192>();
+	cudaError_t e = cudaSuccess;
+	PF_FFT32_SIZES_A(PF_FFT32_GROUP_CONF)
+	if (e == cudaSuccess) e = fft32_configure_b();
+	if (e == cudaSuccess) e = fft32_configure_c();
 	return e;
 }
 
 void launch_fft32_twiddles(void *tw, cudaStream_t stream)
 {
-	twiddle32_kernel<<<kTwN / 256, 256, 0, stream>>>((float2 *)tw);
+	twiddle32_kernel<<<(kTwTotal + 255) / 256, 256, 0, stream>>>((float2 *)tw);
 }
 
 // pass 0 rows, 1 columns, 2 inverse rows; mode 0 forward, 1 adjoint, 2 PSF
@@ -472,16 +95,9 @@ void launch_fft32(int pass, int mode, int n, const void *jobs, int n_jobs, const
 	const Job *j = (const Job *)jobs;
 	float2 *w = (float2 *)work, *s = (float2 *)spec;
 	const float2 *t = (const float2 *)tw;
-	switch (n) {
-	case 64: launch_n<64>(pass, mode, n_jobs, models, j, src, psf, w, s, direct, out, t, stream); break;
-	case 128: launch_n<128>(pass, mode, n_jobs, models, j, src, psf, w, s, direct, out, t, stream); break;
-	case 256: launch_n<256>(pass, mode, n_jobs, models, j, src, psf, w, s, direct, out, t, stream); break;
-	case 512: launch_n<512>(pass, mode, n_jobs, models, j, src, psf, w, s, direct, out, t, stream); break;
-	case 1024: launch_n<1024>(pass, mode, n_jobs, models, j, src, psf, w, s, direct, out, t, stream); break;
-	case 2048: launch_n<2048>(pass, mode, n_jobs, models, j, src, psf, w, s, direct, out, t, stream); break;
-	case 4096: launch_n<4096>(pass, mode, n_jobs, models, j, src, psf, w, s, direct, out, t, stream); break;
-	case 8192: launch_n<8192>(pass, mode, n_jobs, models, j, src, psf, w, s, direct, out, t, stream); break;
-	}
+	if (fft32_launch_b(pass, mode, n, n_jobs, models, j, src, psf, w, s, direct, out, t, stream)) return;
+	if (fft32_launch_c(pass, mode, n, n_jobs, models, j, src, psf, w, s, direct, out, t, stream)) return;
+	fft32_launch_a(pass, mode, n, n_jobs, models, j, src, psf, w, s, direct, out, t, stream);
 }
 
 }  // namespace pf

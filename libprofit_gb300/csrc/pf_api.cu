@@ -45,6 +45,8 @@ void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs
 long long eval32_items(long long n_profiles, long long n_tiles);
 int fft32_rows_per_job(int n);
 int fft32_cols_per_job(int n);
+int fft32_size_at_least(int n);
+int fft32_twiddle_len();
 cudaError_t fft32_configure();
 void launch_fft32_twiddles(void *tw, cudaStream_t stream);
 void launch_fft32(int pass, int mode, int n, const void *jobs, int n_jobs, const ModelDev *models, const float *src,
@@ -773,13 +775,24 @@ pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5], const double *p
 		pf::ModelDev &d = b->mdev[i];
 		d.use_fft = 0;
 		if (!d.conv_required) continue;
-		// the single-precision transforms start at 64 points (a larger zero
-		// padding leaves the linear convolution unchanged)
-		const unsigned int nmin = b->dbl ? 2u : 64u;
 		// the cropped outputs need no wrap-around below crop + psf; the
-		// uncropped frame takes the whole linear convolution, draw + psf - 1
-		const unsigned int mx = std::max(nmin, next_pow2((d.uncropped ? d.draw_w : d.crop_w) + d.psf_w));
-		const unsigned int my = std::max(nmin, next_pow2((d.uncropped ? d.draw_h : d.crop_h) + d.psf_h));
+		// uncropped frame takes the whole linear convolution, draw + psf - 1.
+		// Double precision: powers of two; single precision: the smallest of
+		// its lengths (2^a from 64 and 3, 5, 9 x 2^a), a larger zero padding
+		// leaving the linear convolution unchanged (0: none long enough)
+		const unsigned int need_x = (d.uncropped ? d.draw_w : d.crop_w) + d.psf_w;
+		const unsigned int need_y = (d.uncropped ? d.draw_h : d.crop_h) + d.psf_h;
+		unsigned int mx, my;
+		if (b->dbl) {
+			mx = next_pow2(need_x);
+			my = next_pow2(need_y);
+		}
+		else {
+			const int fx = pf::fft32_size_at_least((int)std::min<unsigned int>(need_x, 1u << 30));
+			const int fy = pf::fft32_size_at_least((int)std::min<unsigned int>(need_y, 1u << 30));
+			mx = fx > 0 ? (unsigned int)fx : next_pow2(need_x);
+			my = fy > 0 ? (unsigned int)fy : next_pow2(need_y);
+		}
 		bool fft = false;
 		if (d.convolver == PF_CONV_FFT) {
 			if ((int)mx > nmax || (int)my > nmax) {
@@ -1187,7 +1200,8 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		const size_t celem = b->dbl ? 2 * sizeof(double) : 2 * sizeof(float);
 		PF_CUDA_TRY(cudaMalloc(&b->d_fft_work, celem * std::max<int64_t>(1, b->fft_work_elems)));
 		PF_CUDA_TRY(cudaMalloc(&b->d_fft_spec, celem * std::max<int64_t>(1, b->fft_spec_elems)));
-		PF_CUDA_TRY(cudaMalloc(&b->d_fft_tw, b->dbl ? celem * (b->fft_nmax / 2) : sizeof(float) * 2 * 8192));
+		PF_CUDA_TRY(cudaMalloc(&b->d_fft_tw, b->dbl ? celem * (b->fft_nmax / 2)
+		                                            : sizeof(float) * 2 * (size_t)pf::fft32_twiddle_len()));
 		for (int p = 0; p < 5; p++) {
 			b->fft_njobs[p] = (int)fft_jobs[p].size();
 			PF_CUDA_TRY(cudaMalloc(&b->d_fft_jobs[p], sizeof(HostFftJob) * std::max<size_t>(1, fft_jobs[p].size())));

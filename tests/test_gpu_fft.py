@@ -64,6 +64,30 @@ def test_fft_fp32_matches_direct(envs, name):
     _check(a.evaluate(), b.evaluate(), 2e-6, 1e-4)
 
 
+FFT32_LENGTHS = [64, 96, 128, 160, 192, 256, 288, 320, 384, 512, 576, 640, 768, 1024, 1152, 1280, 1536, 2048,
+                 2304, 2560, 3072, 4096, 4608, 5120, 6144, 8192]
+
+
+@pytest.mark.parametrize("n", FFT32_LENGTHS)
+def test_fft32_every_length(envs, n):
+    """Every single-precision transform length (2^a, 3, 5, 9 x 2^a): a model
+    of width (or height) n - 15 with a 15 x 15 PSF needs exactly n points
+    (crop + psf) and gets that length; its FFT convolution against the direct
+    one, at the FP32 FFT bars. Lengths up to 2304 square, longer ones on thin
+    models along either axis."""
+    import workloads as W
+    _, env32 = envs
+    k = 15
+    shapes = [(n - k, n - k)] if n <= 2304 else [(n - k, 40), (40, n - k)]
+    for w, h in shapes:
+        spec = dict(width=w, height=h, psf=W.moffat_psf(k, 3.0, 2.5), profiles=[
+            ("sersic", dict(xcen=0.4 * w, ycen=0.55 * h, mag=15.0, re=max(3.0, min(w, h) / 8), nser=2.5, ang=30.0,
+                            axrat=0.7, box=0.0, convolve=True))])
+        a = W.to_model(dict(spec, convolver="fft"), env32)
+        b = W.to_model(dict(spec, convolver="brute"), env32)
+        _check(a.evaluate(), b.evaluate(), 2e-6, 1e-4)
+
+
 def test_fft_batch_mixed_methods(envs):
     """Models with FFT and direct convolution in one batch render as alone."""
     import torch
