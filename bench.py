@@ -152,6 +152,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def fft_length(n):
+    """The single-precision FFT's transform length for n points: the smallest
+    of 2^a (64 .. 8192) and 3, 5, 9 x 2^a (2^a >= 32) that is >= n."""
+    lengths = sorted({1 << a for a in range(6, 14)} |
+                     {f << a for f, top in ((3, 6144), (5, 5120), (9, 4608)) for a in range(5, 14) if f << a <= top})
+    return next(x for x in lengths if x >= n)
+
+
+def hbm_peak():
+    """The measured copy bandwidth (MEASURED_PEAKS.json next to this file), or
+    the 6.8 TB/s fallback."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return {"gbs": float(json.load(f)["hbm_gbs"]), "note": "of measured"}
+    except (OSError, KeyError, ValueError):
+        return {"gbs": 6800.0, "note": "of fallback"}
+
+
 def make_problem(models, seed_offset, env64, torch):
     """Workload specs, the batch parameter matrix and the data (rendered by
     the FP64 path at perturbed parameters, plus noise)."""
@@ -436,7 +454,7 @@ def run_ours(args, world, rank, local):
     # sequence), timed on four models; on 32, its images, chi^2 and
     # gradients against the FP32 batch's (accuracy of the timed step)
     fp64_rates = []
-    acc = {"flux": [], "pixel": [], "chi2": []}
+    acc = {"flux": [], "pixel": [], "pixel3": [], "abs": [], "chi2": []}
     img32 = img.cpu().numpy()
     chi32 = chi2.cpu().numpy()
     grad32 = grad.cpu().numpy().reshape(n_prof, 12)
@@ -463,6 +481,9 @@ def run_ours(args, world, rank, local):
             peak = np.abs(ref).max()
             bright = np.abs(ref) > 1e-9 * peak
             acc["pixel"].append(float(np.max(np.abs(got[bright] - ref[bright]) / np.abs(ref[bright]))))
+            bright3 = np.abs(ref) > 1e-3 * peak
+            acc["pixel3"].append(float(np.max(np.abs(got[bright3] - ref[bright3]) / np.abs(ref[bright3]))))
+            acc["abs"].append(float(np.max(np.abs(got - ref)) / peak))
             acc["flux"].append(abs(got.sum() - ref.sum()) / abs(ref.sum()))
             acc["chi2"].append(abs(chi32[i] - c1.item()) / abs(c1.item()))
             g64_all.append(g1.cpu().numpy().reshape(-1, 12)[:, :8])
@@ -487,31 +508,32 @@ def run_ours(args, world, rank, local):
                                      np.concatenate(g32_all), np.concatenate(g64_all), env64)
     fp64_rate = statistics.median(fp64_rates) if fp64_rates else None
 
-    # the same step with every convolution forced to the FFT (the autotuner
-    # picks the direct convolution for this PSF size): models/s
-    fft_forced = None
+    # the same step with every convolution forced to the FFT, and to the
+    # direct convolution (the autotuner picks per model by timing): models/s
+    forced = {"fft": None, "brute": None}
     if rank == 0 and args.convolver == "auto" and not args.no_graph:
-        models_f = [W.to_model(s, env32) for s in specs]
-        for m in models_f:
-            m.set_convolver("fft")
-        bf = pg.Batch(models_f, env32)
-        bf.enable_adjoint()
-        with torch.cuda.stream(stream):
-            for _ in range(2):
-                bf.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
-        torch.cuda.synchronize()
-        nf = max(3, args.steps // 2)
-        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        with torch.cuda.stream(stream):
-            for _ in range(nf):
-                bf.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
-        f1.record(stream)
-        torch.cuda.synchronize()
-        bf.check(stream=sh)
-        fms = f0.elapsed_time(f1) / nf
-        fft_forced = {"value": n_models / (fms / 1000.0), "unit": "models/s", "ms_per_step": fms, "steps": nf}
-        bf.close()
+        for how in forced:
+            models_f = [W.to_model(s, env32) for s in specs]
+            for m in models_f:
+                m.set_convolver(how)
+            bf = pg.Batch(models_f, env32)
+            bf.enable_adjoint()
+            with torch.cuda.stream(stream):
+                for _ in range(2):
+                    bf.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
+            torch.cuda.synchronize()
+            nf = max(3, args.steps // 2)
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            with torch.cuda.stream(stream):
+                for _ in range(nf):
+                    bf.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
+            f1.record(stream)
+            torch.cuda.synchronize()
+            bf.check(stream=sh)
+            fms = f0.elapsed_time(f1) / nf
+            forced[how] = {"value": n_models / (fms / 1000.0), "unit": "models/s", "ms_per_step": fms, "steps": nf}
+            bf.close()
 
     if rank != 0:
         return
@@ -530,6 +552,21 @@ def run_ours(args, world, rank, local):
                    for (w, h), t, s in zip(batch.dims, taps, specs))
     work = {"eval_ms": evals * FLOP_EVAL, "backward_ms": evals * FLOP_GRAD, "finish_ms": conv_fwd,
             "adjoint_conv_ms": conv_adj}
+    # the FFT convolution (when the plan takes it for every model) is bound by
+    # HBM: its algorithmic bytes per model (the three passes' reads and
+    # writes, the PSF spectrum shared and read from L2), against the measured
+    # copy bandwidth
+    plan = batch.conv_info()
+    fft_bytes = None
+    if plan["fft_models"] == n_models:
+        fwd_b = adj_b = 0.0
+        for (cw, ch), s in zip(batch.dims, specs):
+            kh, kw = s["psf"].shape
+            dw, dh = cw + kw // 2 * 2, ch + kh // 2 * 2
+            nb = fft_length(cw + kw) // 2 + 1
+            fwd_b += 4.0 * dw * dh + 16.0 * nb * (dh + ch) + 8.0 * cw * ch
+            adj_b += 4.0 * cw * ch + 16.0 * nb * (ch + dh) + 4.0 * dw * dh
+        fft_bytes = {"finish_ms": fwd_b, "adjoint_conv_ms": adj_b}
     # DRAM bytes per launch, per model of this workload: ncu dram__bytes_read.sum +
     # dram__bytes_write.sum of each kernel on the 256-model copy of the workload
     # (one ncu capture per kernel), divided by 256
@@ -550,8 +587,22 @@ def run_ours(args, world, rank, local):
     # changes with run-to-run noise: they are within ~6 % of each other)
     roof["by_kernel"] = {k.replace("_ms", ""): {"ms_per_step": per_step[k],
                                                 "achieved": work[k] / (per_step[k] / 1000.0) / 1e12,
+                                                "unit": "TFLOP/s",
                                                 "frac": work[k] / (per_step[k] / 1000.0) / 1e12 / fp32_peak}
                          for k in work if per_step.get(k)}
+    if fft_bytes:
+        hbm = hbm_peak()
+        for k, nbytes in fft_bytes.items():
+            if per_step.get(k):
+                gbs = nbytes / (per_step[k] / 1000.0) / 1e9
+                roof["by_kernel"][k.replace("_ms", "")] = {
+                    "ms_per_step": per_step[k], "method": "fft", "achieved": gbs, "unit": "GB/s",
+                    "peak": hbm["gbs"], "peak_note": hbm["note"], "frac": gbs / hbm["gbs"],
+                    "algorithmic_bytes_per_step": nbytes}
+        if dom in fft_bytes:
+            e = roof["by_kernel"][dom.replace("_ms", "")]
+            roof.update({"bound": "hbm", "achieved": e["achieved"], "peak": e["peak"], "unit": "GB/s",
+                         "frac": e["frac"], "traffic": None, "peak_note": e["peak_note"]})
 
     dropin = dropin_rates(env64, pg.get_cuda_environment(local, use_double=False)) if not args.no_dropin else None
 
@@ -577,9 +628,14 @@ def run_ours(args, world, rank, local):
                      "max_rel_flux_err": max(acc["flux"]) if acc["flux"] else None,
                      "max_rel_pixel_err": max(acc["pixel"]) if acc["pixel"] else None,
                      "pixel_floor": "pixels above 1e-9 x the model's peak",
+                     "max_rel_pixel_err_above_1e-3_peak": max(acc["pixel3"]) if acc["pixel3"] else None,
+                     "max_abs_err_of_peak": max(acc["abs"]) if acc["abs"] else None,
+                     "convolution": "FFT for %d of %d models (the FFT's rounding is absolute, relative to the "
+                                    "peak: faint pixels carry it)" % (plan["fft_models"], n_models),
                      "max_rel_chi2_err": max(acc["chi2"]) if acc["chi2"] else None,
                      "grad": grad_acc},
-        "fft_forced": fft_forced,
+        "fft_forced": forced["fft"],
+        "direct_forced": forced["brute"],
         "drop_in": dropin,
         "ratio_vs_fp64_per_model": (value / world) / fp64_rate if fp64_rate else None,
         "stage_ms_per_step": per_step,

@@ -246,8 +246,20 @@ __device__ __forceinline__ void fft(float2 *buf, int t, const float2 *__restrict
 
 template <int N>
 __host__ __device__ constexpr int row_ffts() { return (N / 8) >= 256 ? 1 : 256 / (N / 8); }  // transforms per row block
+// Column-pass blocks: at most PF_FFT_COL_THREADS threads (16 transforms at
+// most), PF_FFT_COL_MINB blocks per SM for the launch bounds when they have
+// at most 576 threads.
+#ifndef PF_FFT_COL_THREADS
+#define PF_FFT_COL_THREADS 288
+#endif
+#ifndef PF_FFT_COL_MINB
+#define PF_FFT_COL_MINB 2
+#endif
 template <int N>
-__host__ __device__ constexpr int col_ffts() { return (N / 8) >= 64 ? 1024 / (N / 8) < 16 ? 1024 / (N / 8) : 16 : 16; }
+__host__ __device__ constexpr int col_ffts()
+{
+	return PF_FFT_COL_THREADS / (N / 8) < 1 ? 1 : PF_FFT_COL_THREADS / (N / 8) > 16 ? 16 : PF_FFT_COL_THREADS / (N / 8);
+}
 template <int N>
 __host__ __device__ constexpr int row_stride() { return N + N / 8; }                     // padded length
 template <int N>
@@ -285,28 +297,37 @@ rows_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, c
 		xoff = (int)m.pad_x + (int)m.psf_w - 1 - (int)m.psf_w / 2;
 	}
 	else w = (int)m.psf_w;
-	for (int i = threadIdx.x; i < F * N; i += blockDim.x) {
+	// the block has F * N / 8 threads: eight points each, all loads issued
+	// before the shared-memory stores
+	float2 v[8];
+#pragma unroll
+	for (int q = 0; q < 8; q++) {
+		const int i = (int)threadIdx.x + q * (F * (N / 8));
 		const int ff = i / N, c = i % N;
 		const int r0 = jb.first + 2 * ff, r1 = r0 + 1;
 		const int x = c - xoff;
-		float2 v = make_float2(0.f, 0.f);
+		v[q] = make_float2(0.f, 0.f);
 		if (x >= 0 && x < w) {
 			if (MODE == F_FORWARD) {
 				const float *s = src + m.draw_off;
-				if (r0 < jb.first + jb.count) v.x = s[(size_t)r0 * m.draw_w + x];
-				if (r1 < jb.first + jb.count) v.y = s[(size_t)r1 * m.draw_w + x];
+				if (r0 < jb.first + jb.count) v[q].x = s[(size_t)r0 * m.draw_w + x];
+				if (r1 < jb.first + jb.count) v[q].y = s[(size_t)r1 * m.draw_w + x];
 			}
 			else if (MODE == F_ADJOINT) {
-				if (r0 < jb.first + jb.count) v.x = cot_crop(m, src, x, r0);
-				if (r1 < jb.first + jb.count) v.y = cot_crop(m, src, x, r1);
+				if (r0 < jb.first + jb.count) v[q].x = cot_crop(m, src, x, r0);
+				if (r1 < jb.first + jb.count) v[q].y = cot_crop(m, src, x, r1);
 			}
 			else {
 				const float *k = psf + m.psf_off;
-				if (r0 < jb.first + jb.count) v.x = k[(size_t)r0 * m.psf_w + x];
-				if (r1 < jb.first + jb.count) v.y = k[(size_t)r1 * m.psf_w + x];
+				if (r0 < jb.first + jb.count) v[q].x = k[(size_t)r0 * m.psf_w + x];
+				if (r1 < jb.first + jb.count) v[q].y = k[(size_t)r1 * m.psf_w + x];
 			}
 		}
-		buf[ff * PS + pidx(c)] = v;
+	}
+#pragma unroll
+	for (int q = 0; q < 8; q++) {
+		const int i = (int)threadIdx.x + q * (F * (N / 8));
+		buf[(i / N) * PS + pidx(i % N)] = v[q];
 	}
 	__syncthreads();
 	fft<N, false>(buf + f * PS, t, table);
@@ -323,8 +344,11 @@ rows_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, c
 }
 
 // Pass 2: columns of bins. Job: bin columns first .. first + count - 1.
+template <int N>
+__host__ __device__ constexpr int col_min_blocks() { return col_ffts<N>() * (N / 8) <= 576 ? PF_FFT_COL_MINB : 1; }
+
 template <int N, int MODE>
-__global__ void __launch_bounds__(col_ffts<N>() * (N / 8))
+__global__ void __launch_bounds__(col_ffts<N>() * (N / 8), col_min_blocks<N>())
 cols_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, float2 *__restrict__ work,
             float2 *__restrict__ spec, const float2 *__restrict__ table)
 {
@@ -344,12 +368,21 @@ cols_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, f
 		yoff = (int)m.pad_y + (int)m.psf_h - 1 - (int)m.psf_h / 2;
 	}
 	else rows_in = (int)m.psf_h;
-	for (int i = threadIdx.x; i < F * N; i += blockDim.x) {
+	// the block has F * N / 8 threads: eight points each, all loads issued
+	// before the shared-memory stores
+	float2 v[8];
+#pragma unroll
+	for (int q = 0; q < 8; q++) {
+		const int i = (int)threadIdx.x + q * (F * (N / 8));
 		const int rg = i / F, ff = i % F;  // transform row, column within the job
 		const int r = rg - yoff;
-		float2 v = make_float2(0.f, 0.f);
-		if (ff < jb.count && r >= 0 && r < rows_in) v = col[(size_t)r * nb + jb.first + ff];
-		cbuf[ff * PS + pidx(rg)] = v;
+		v[q] = make_float2(0.f, 0.f);
+		if (ff < jb.count && r >= 0 && r < rows_in) v[q] = col[(size_t)r * nb + jb.first + ff];
+	}
+#pragma unroll
+	for (int q = 0; q < 8; q++) {
+		const int i = (int)threadIdx.x + q * (F * (N / 8));
+		cbuf[(i % F) * PS + pidx(i / F)] = v[q];
 	}
 	__syncthreads();
 	fft<N, false>(cbuf + f * PS, t, table);
@@ -361,18 +394,27 @@ cols_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, f
 		return;
 	}
 	const float2 *sp = spec + m.fft_spec_off;
-	for (int i = threadIdx.x; i < F * N; i += blockDim.x) {
+#pragma unroll
+	for (int q = 0; q < 8; q++) {
+		const int i = (int)threadIdx.x + q * (F * (N / 8));
+		const int rg = i / F, ff = i % F;
+		v[q] = ff < jb.count ? sp[(size_t)rg * nb + jb.first + ff] : make_float2(0.f, 0.f);
+	}
+#pragma unroll
+	for (int q = 0; q < 8; q++) {
+		const int i = (int)threadIdx.x + q * (F * (N / 8));
 		const int rg = i / F, ff = i % F;
 		if (ff >= jb.count) continue;
-		float2 s = sp[(size_t)rg * nb + jb.first + ff];
-		if (MODE == F_ADJOINT) s.y = -s.y;
-		cbuf[ff * PS + pidx(rg)] = cmulf(cbuf[ff * PS + pidx(rg)], s);
+		float2 sq = v[q];
+		if (MODE == F_ADJOINT) sq.y = -sq.y;
+		cbuf[ff * PS + pidx(rg)] = cmulf(cbuf[ff * PS + pidx(rg)], sq);
 	}
 	__syncthreads();
 	fft<N, true>(cbuf + f * PS, t, table);
 	// kept rows: forward, the crop's (from its offset); adjoint, the drawing area's
 	const int rows_out = MODE == F_FORWARD ? (int)m.crop_h : (int)m.draw_h;
 	const int keep = MODE == F_FORWARD ? (int)m.pad_y + (int)m.psf_h - 1 - (int)m.psf_h / 2 : 0;
+#pragma unroll 4
 	for (int i = threadIdx.x; i < F * rows_out; i += blockDim.x) {
 		const int r = i / F, ff = i % F;
 		if (ff < jb.count) col[(size_t)r * nb + jb.first + ff] = cbuf[ff * PS + pidx(r + keep)];
@@ -394,18 +436,28 @@ irows_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, 
 	const int nb = (int)m.fft_mx / 2 + 1;
 	const int f = threadIdx.x / (N / 8), t = threadIdx.x % (N / 8);
 	const float2 *src = work + m.fft_work_off;
-	for (int i = threadIdx.x; i < F * N; i += blockDim.x) {
+	// the block has F * N / 8 threads: eight points each, all loads issued
+	// before the shared-memory stores
+	float2 a[8], b[8];
+#pragma unroll
+	for (int q = 0; q < 8; q++) {
+		const int i = (int)threadIdx.x + q * (F * (N / 8));
 		const int ff = i / N, k = i % N;
 		const int r0 = jb.first + 2 * ff, r1 = r0 + 1;
 		const int kk = k <= N / 2 ? k : N - k;
-		float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
-		if (r0 < jb.first + jb.count) a = src[(size_t)r0 * nb + kk];
-		if (r1 < jb.first + jb.count) b = src[(size_t)r1 * nb + kk];
+		a[q] = b[q] = make_float2(0.f, 0.f);
+		if (r0 < jb.first + jb.count) a[q] = src[(size_t)r0 * nb + kk];
+		if (r1 < jb.first + jb.count) b[q] = src[(size_t)r1 * nb + kk];
+	}
+#pragma unroll
+	for (int q = 0; q < 8; q++) {
+		const int i = (int)threadIdx.x + q * (F * (N / 8));
+		const int ff = i / N, k = i % N;
 		if (k > N / 2) {
-			a.y = -a.y;
-			b.y = -b.y;
+			a[q].y = -a[q].y;
+			b[q].y = -b[q].y;
 		}
-		buf[ff * PS + pidx(k)] = make_float2(a.x - b.y, a.y + b.x);
+		buf[ff * PS + pidx(k)] = make_float2(a[q].x - b[q].y, a[q].y + b[q].x);
 	}
 	__syncthreads();
 	fft<N, true>(buf + f * PS, t, table);
@@ -414,6 +466,7 @@ irows_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, 
 		const int off_x = (int)m.pad_x + (int)m.psf_w - 1 - (int)m.psf_w / 2;
 		const bool downsample = m.fs > 1 && !m.return_fs;
 		const int cw = (int)m.crop_w;
+#pragma unroll 4
 		for (int i = threadIdx.x; i < F * 2 * cw; i += blockDim.x) {
 			const int ff = i / (2 * cw), rem = i % (2 * cw), half = rem / cw, c = rem % cw;
 			const int r = jb.first + 2 * ff + half;

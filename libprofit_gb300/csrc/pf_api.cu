@@ -750,6 +750,13 @@ int best_conv_shape(const std::vector<std::pair<unsigned int, unsigned int>> &di
 	return best;
 }
 
+// PF_CONV_AUTO in single precision takes the FFT for a model only where it
+// at least halves the convolution's time: its FP32 rounding is absolute
+// (about 1e-7 x the image peak at every pixel) where the direct
+// convolution's is relative, which faint pixels and the gradients they carry
+// feel; PF_CONV_FFT takes it regardless.
+constexpr double kFftGain = 0.5;
+
 unsigned int next_pow2(unsigned int v)
 {
 	unsigned int p = 2;
@@ -761,9 +768,10 @@ unsigned int next_pow2(unsigned int v)
 // job lists. An explicit PF_CONV_BRUTE / PF_CONV_FFT is obeyed; PF_CONV_AUTO
 // keeps the plain FP64 path on the direct convolution (the reference's
 // default BRUTE convolver and summation order) and, for the FP32 path, takes
-// the cheaper of the two by a cost model of this GPU: direct = 2 P^2 flop per
-// output pixel at 35 TFLOP/s; FFT = its HBM bytes at 3 TB/s plus
-// 5 N log2 N flop per transform at 10 TFLOP/s.
+// the FFT where it costs at most kFftGain of the direct convolution by a cost
+// model of this GPU: direct = 2 P^2 flop per output pixel at 35 TFLOP/s;
+// FFT = its HBM bytes at 3 TB/s plus 5 N log2 N flop per transform at
+// 10 TFLOP/s (large batches: by the autotuner's timings instead).
 pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5], const double *psf_pool,
                    std::map<int, std::vector<HostFftJob>> f32[3][3], const ConvPlan &plan)
 {
@@ -811,7 +819,7 @@ pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5], const double *p
 			                     4.0 * ((double)d.draw_w * d.draw_h + 2.0 * d.crop_w * d.crop_h);
 			const double flops = 5.0 * (d.draw_h * mx * std::log2((double)mx) + 2 * nb * my * std::log2((double)my) +
 			                            d.crop_h * mx * std::log2((double)mx));
-			fft = bytes / 3e12 + flops / 10e12 < direct_s;
+			fft = bytes / 3e12 + flops / 10e12 < kFftGain * direct_s;
 		}
 		if (!fft) continue;
 		d.use_fft = 1;
@@ -1332,6 +1340,18 @@ static double time_forward_conv(pf_batch *b, int shape, bool fft, float *out)
 // Autotuner timing (ms, best of three after a warm-up) of a single-precision
 // batch's setup and evaluation passes, with its subsampling trees split off
 // to other warps (split) or walked where met.
+static double time_eval(pf_batch *b, bool split);
+
+// The batch's split pool given back: its trees walked where met from now on.
+static void release_split_pool(pf_batch *b)
+{
+	cudaFree(b->split.box);
+	cudaFree(b->split.box_val);
+	cudaFree(b->split.root);
+	cudaFree(b->split.pix);
+	b->split = pf::SplitPool{};
+}
+
 static double time_eval(pf_batch *b, bool split)
 {
 	cudaStream_t st = b->env->stream;
@@ -1435,10 +1455,18 @@ pf_status pf_batch_create_masked(pf_env *env, const pf_model_desc *models, size_
 		out_pixels += (uint64_t)models[i].width * models[i].height;
 		any_auto |= models[i].convolver == PF_CONV_AUTO && models[i].psf_offset >= 0 && models[i].psf_w > 0;
 	}
-	tune = tune && any_auto && out_pixels >= (1ull << 22);
+	const bool tune_split = tune && out_pixels >= (1ull << 22);
+	tune = tune_split && any_auto;
 	if (!tune) {
-		return create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool,
-		                      mask_pool_len, fixed, batch);
+		pf_status s = create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool,
+		                             mask_pool_len, fixed, batch);
+		if (s == PF_OK && tune_split && (*batch)->split.box) {
+			// every convolution requested explicitly: the evaluation still timed
+			// with and without its subsampling trees split off (below)
+			const double t_split = time_eval(*batch, true), t_walk = time_eval(*batch, false);
+			if (t_walk > 0 && t_split > 0 && t_walk < t_split) release_split_pool(*batch);
+		}
+		return s;
 	}
 
 	// The autotuner (single precision, PF_CONV_AUTO, large batches): the batch
@@ -1511,7 +1539,7 @@ pf_status pf_batch_create_masked(pf_env *env, const pf_model_desc *models, size_
 				const pf::ModelDev &d = bf->mdev[i];
 				if (!d.use_fft) continue;
 				choice[i] = cf * d.fft_mx * d.fft_my * std::log2((double)d.fft_mx * d.fft_my) <
-				            cd * (double)d.crop_w * d.crop_h * d.psf_w * d.psf_h;
+				            kFftGain * cd * (double)d.crop_w * d.crop_h * d.psf_w * d.psf_h;
 			}
 		}
 	}

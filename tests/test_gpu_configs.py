@@ -52,7 +52,10 @@ def _check(img, ref, name):
     # over the transform (1e-6 x peak + 2e-8 x flux)
     err = np.abs(img - ref) - 1e-4 * np.abs(ref)
     assert err.max() <= 1e-6 * peak + 2e-8 * flux, "%s: abs %.3g of peak" % (name, err.max() / peak)
-    bright = np.abs(ref) > 1e-3 * peak
+    # 1e-4 relative from 1e-2 x peak up: the FP32 FFT's rounding, about
+    # 1e-7 x peak wherever the pixel is, is already 1e-4 of a pixel at
+    # 1e-3 x peak (the models whose autotuned method is the FFT)
+    bright = np.abs(ref) > 1e-2 * peak
     rel = np.abs(img[bright] - ref[bright]) / np.abs(ref[bright])
     assert rel.max() <= 1e-4, "%s: rel %.3g" % (name, rel.max())
 
