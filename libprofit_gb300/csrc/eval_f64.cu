@@ -584,7 +584,13 @@ level64_kernel(const ProfileDev *__restrict__ profs, double *__restrict__ conv_i
 	WarpScratch64 &ws = scratch[warp];
 	const unsigned int lo = *(volatile unsigned int *)&pool.cnt[LC_BOUND + level];
 	const unsigned int hi = *(volatile unsigned int *)&pool.cnt[LC_BOUND + level + 1];
-	const long long n_items = hi > lo ? (long long)(hi - lo) * kSlots : 0;
+	if (hi <= lo) {
+		// no box at this level, so none deeper: the next level's (empty)
+		// range recorded without the blocks' completion count
+		if (blockIdx.x == 0 && threadIdx.x == 0) pool.cnt[LC_BOUND + level + 2] = hi;
+		return;
+	}
+	const long long n_items = (long long)(hi - lo) * kSlots;
 	for (long long item = (long long)blockIdx.x * kWarps64 + warp; item < n_items;
 	     item += (long long)gridDim.x * kWarps64) {
 		const unsigned int b = lo + (unsigned int)(item / kSlots);

@@ -1155,7 +1155,9 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 	}
 	// [0] device-limit flags, [1] the last pass's first invalid profile (index << 5 | rule)
 	PF_CUDA_TRY(cudaMalloc(&b->d_err, 2 * sizeof(unsigned int)));
-	PF_CUDA_TRY(cudaMalloc(&b->d_solves, sizeof(double) * 3 * std::max<size_t>(1, n_profiles)));
+	// per profile the three solves, then the nser each was made for (NaN: none yet)
+	PF_CUDA_TRY(cudaMalloc(&b->d_solves, sizeof(double) * 6 * std::max<size_t>(1, n_profiles)));
+	PF_CUDA_TRY(cudaMemset(b->d_solves, 0xff, sizeof(double) * 6 * std::max<size_t>(1, n_profiles)));
 	PF_CUDA_TRY(cudaMemset(b->d_err, 0, sizeof(unsigned int)));
 	PF_CUDA_TRY(cudaMemset(b->d_err + 1, 0xff, sizeof(unsigned int)));
 	const size_t elem = b->dbl ? sizeof(double) : sizeof(float);

@@ -500,8 +500,14 @@ __global__ void setup_solves_kernel(const ProfileDev *profs, int n_profiles, dou
 	const int task = (int)(t / n_profiles), i = (int)(t % n_profiles);
 	const int kind = profs[i].kind;
 	const double nser = profs[i].par[7];
+	// a valid profile's solve depends on nser alone (kind and flags are fixed
+	// per batch): kept while nser is (the keys, after the 3 n_profiles
+	// values, start NaN; an invalid profile's stays NaN)
+	double *key = solves + 3LL * n_profiles + (size_t)i * 3 + task;
+	if (*key == nser) return;
 	double v = 0.;
-	if (param_rule(kind, profs[i].par) != PR_OK) {
+	const bool valid = param_rule(kind, profs[i].par) == PR_OK;
+	if (!valid) {
 		// invalid parameters (written on the device): the profile is not set up
 	}
 	else if (task == 0 && (kind == PF_SERSIC || kind == PF_CORESERSIC)) {
@@ -515,6 +521,7 @@ __global__ void setup_solves_kernel(const ProfileDev *profs, int n_profiles, dou
 		v = sf::qgamma(0.9999, 2 * nser, sf::wilson_hilferty_guess(0.9999, 2 * nser));
 	}
 	solves[(size_t)i * 3 + task] = v;
+	*key = valid ? nser : CUDART_NAN;
 }
 
 __global__ void setup_profiles_kernel(const ModelDev *models, ProfileDev *profs, int n_profiles,

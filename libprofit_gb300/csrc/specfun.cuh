@@ -66,40 +66,78 @@ __device__ inline double digamma(double x)
 	return acc + log(x) - 0.5 * r - series;
 }
 
-constexpr double kFpMin = 1e-300;
-
+// P(a, x) = x^a e^-x / Gamma(a + 1) sum_n x^n / ((a + 1) ... (a + n)): the
+// terms' ratios x / (a + n) taken four at a time, so that their divisions
+// (hundreds of cycles each in FP64 on this GPU) run side by side instead of
+// on the running product's dependency chain; the terms, the sum and the stop
+// are the one-at-a-time loop's, in its order.
 __device__ inline double pgamma_series(double a, double x)
 {
 	double ap = a, term = 1., sum = 1.;
-	for (int n = 1; n < 2000; n++) {
-		ap += 1.;
-		term *= x / ap;
-		sum += term;
-		if (fabs(term) < fabs(sum) * DBL_EPSILON) {
-			break;
+	int n = 1;
+	while (n < 2000) {
+		double ratio[4];
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			ap += 1.;
+			ratio[q] = x / ap;
 		}
+		bool done = false;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			term *= ratio[q];
+			sum += term;
+			n++;
+			if (fabs(term) < fabs(sum) * DBL_EPSILON || n >= 2000) {
+				done = true;
+				break;
+			}
+		}
+		if (done) break;
 	}
 	return exp(a * log(x) - x - lgamma(a + 1.)) * sum;
 }
 
+// Q(a, x) = x^a e^-x / Gamma(a) / (b_0 + a_1 / (b_1 + a_2 / (b_2 + ...))),
+// b_i = x + 2i + 1 - a, a_i = -i (i - a), for x >= a + 1. The continued
+// fraction by the three-term recurrence of its convergents A_i / B_i
+// (A_i = b_i A_{i-1} + a_i A_{i-2}, the same for B; the Wallis form),
+// rescaled by exact powers of two against overflow: two multiply-adds per
+// term on the dependency chain instead of two divisions; converged when four
+// more terms move B / A by less than 2 eps relative.
 __device__ inline double qgamma_cf(double a, double x)
 {
-	double b = x + 1. - a, c = 1. / kFpMin, d = 1. / b, h = d;
-	for (int i = 1; i < 2000; i++) {
-		double an = -i * (i - a);
-		b += 2.;
-		d = an * d + b;
-		if (fabs(d) < kFpMin) d = kFpMin;
-		c = b + an / c;
-		if (fabs(c) < kFpMin) c = kFpMin;
-		d = 1. / d;
-		double del = d * c;
-		h *= del;
-		if (fabs(del - 1.) < DBL_EPSILON) {
+	double b = x + 1. - a;
+	double A2 = 1., A1 = b, B2 = 0., B1 = 1.;  // A_{i-2}, A_{i-1}, B_{i-2}, B_{i-1}
+	double f = B1 / A1;
+	for (int i = 1; i < 2000; i += 4) {
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			const double an = -(double)(i + q) * ((double)(i + q) - a);
+			b += 2.;
+			const double A = b * A1 + an * A2, B = b * B1 + an * B2;
+			A2 = A1;
+			A1 = A;
+			B2 = B1;
+			B1 = B;
+		}
+		// both convergents' pairs scaled by the same power of two: exact
+		int e;
+		frexp(A1, &e);
+		if (e > 600 || e < -600) {
+			A1 = ldexp(A1, -e);
+			A2 = ldexp(A2, -e);
+			B1 = ldexp(B1, -e);
+			B2 = ldexp(B2, -e);
+		}
+		const double fn = B1 / A1;
+		if (fabs(fn - f) <= 2. * DBL_EPSILON * fabs(fn)) {
+			f = fn;
 			break;
 		}
+		f = fn;
 	}
-	return exp(a * log(x) - x - lgamma(a)) * h;
+	return exp(a * log(x) - x - lgamma(a)) * f;
 }
 
 __device__ inline double pgamma(double x, double a)
