@@ -57,7 +57,7 @@ def parse():
                     help="convolution method of the FP32 batch (auto: the library's choice)")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch the step's kernels one by one instead of replaying its CUDA graph")
-    ap.add_argument("--workload", default="cfg4", choices=["cfg4", "cfg2", "cfg3", "cfg5"],
+    ap.add_argument("--workload", default="cfg4", choices=["cfg4", "cfg2", "cfg3", "cfg5", "dropin"],
                     help="cfg4 (default): the batched model + VJP step; the others: see the module docstring")
     return ap.parse_args()
 
@@ -269,17 +269,19 @@ def run_reference(args, world, rank):
 # op weighted 8, its issue cost against the FMA pipe: 128 vs 16 per SM-clock).
 FLOP_EVAL = 2 * 7 + 5 + 3 * 8        # coordinates + base + rf + exp: 43
 FLOP_GRAD = FLOP_EVAL + 40 + 4 * 8   # + the derivative chain (sersic_grad): 115
-def dropin_rates(env64, env32, budget_s=2.0):
+def dropin_rates(env64, env32, budget_s=2.0, cpu=True):
     """The drop-in path: Model.evaluate (pf_model_evaluate, host buffers in
-    and out) on one model per call, the sersic's xcen changed between calls
-    as a fitter changes parameters, for the one-model workloads (cfg1:
-    100x100, 15x15 PSF, direct convolution; cfg2: 1000x1000 bulge + disk +
-    sky, 51x51 PSF by FFT), in the plain FP64 and the FP32 environments; and
-    the CPU oracle port (all host threads) on the same models. Calls per
-    second, each leg timed for about budget_s after three warm-up calls."""
-    from oracle import oracle as O
+    and out) on one model per call, the first sersic's xcen and nser changed
+    between calls as a fitter changes parameters (so that the setup's solves
+    are redone every call), for the one-model workloads (cfg1: 100x100,
+    15x15 PSF, direct convolution; cfg2: 1000x1000 bulge + disk + sky, 51x51
+    PSF by FFT), in the plain FP64 and the FP32 environments; and the CPU
+    oracle port (all host threads) on the same models. Calls per second, each
+    leg timed for about budget_s after three warm-up calls."""
     import workloads as W
-    O.build(with_ref=False)
+    if cpu:
+        from oracle import oracle as O
+        O.build(with_ref=False)
     threads = os.cpu_count() or 1
     out = {"calls": "Model.evaluate through pf_model_evaluate with host buffers, one model per call",
            "cpu_threads": threads}
@@ -288,19 +290,25 @@ def dropin_rates(env64, env32, budget_s=2.0):
         for label, env in (("fp64", env64), ("fp32", env32)):
             m = W.to_model(spec, env)
             p = m.profiles[0]
-            x0 = spec["profiles"][0][1]["xcen"]
+            x0, n0 = spec["profiles"][0][1]["xcen"], spec["profiles"][0][1]["nser"]
+
+            def call(k):
+                p.parameter("xcen", x0 + 0.01 * (k % 7))
+                p.parameter("nser", n0 * (1 + 1e-6 * (k % 5)))
+                m.evaluate()
             k = 0
             for _ in range(3):
-                p.parameter("xcen", x0 + 0.01 * (k % 7))
-                m.evaluate()
+                call(k)
                 k += 1
             n, t0 = 0, time.perf_counter()
             while time.perf_counter() - t0 < budget_s or n < 3:
-                p.parameter("xcen", x0 + 0.01 * (k % 7))
-                m.evaluate()
+                call(k)
                 n += 1
                 k += 1
             row[label + "_calls_per_s"] = n / (time.perf_counter() - t0)
+        out[name] = row
+        if not cpu:
+            continue
         case = W.to_oracle_case(spec)
         O.evaluate(case, threads=threads)
         n, t0 = 0, time.perf_counter()
@@ -372,10 +380,20 @@ def run_ours(args, world, rank, local):
     chi2 = torch.zeros(n_models, dtype=torch.float64, device="cuda")
     grad = torch.zeros(n_prof * 12, dtype=torch.float64, device="cuda")
     params = torch.tensor(par.ravel(), dtype=torch.float64, device="cuda")
+    # consecutive steps alternate between the parameters and a copy moved by
+    # ~1e-6 relative in every entry (nser included), as an optimiser's steps
+    # are: nothing the setup caches across unchanged parameters carries over
+    alt_np = par * (1 + 1e-6 * np.random.Generator(np.random.PCG64(6000 + rank)).standard_normal(par.shape))
+    alt_np[:, 4] = np.minimum(alt_np[:, 4], 1.0)  # axrat stays <= 1
+    p_alt = [params.clone(), torch.tensor(alt_np.ravel(), dtype=torch.float64, device="cuda")]
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
+    n_step = [0]
 
     def step():
+        with torch.cuda.stream(stream):
+            params.copy_(p_alt[n_step[0] & 1], non_blocking=True)
+        n_step[0] += 1
         if args.no_graph:
             batch.set_params_dev(params, stream=sh)
             batch.forward_backward(img, data, sigma, chi2, grad, stream=sh)
@@ -409,7 +427,8 @@ def run_ours(args, world, rank, local):
         # graph launches record no stage times: the breakdown comes from the
         # same steps launched one by one (CUDA events around each stage)
         with torch.cuda.stream(stream):
-            for _ in range(args.steps):
+            for k in range(args.steps):
+                params.copy_(p_alt[k & 1], non_blocking=True)
                 batch.set_params_dev(params, stream=sh)
                 batch.forward_backward(img, data, sigma, chi2, grad, stream=sh)
         torch.cuda.synchronize()
@@ -421,7 +440,9 @@ def run_ours(args, world, rank, local):
 
     # e2e through the public API with host buffers: parameters in from pinned
     # host memory, chi^2 and gradients back to pinned host memory, every step
-    h_par = torch.tensor(par.ravel(), dtype=torch.float64).pin_memory()
+    h_alt = [torch.tensor(par.ravel(), dtype=torch.float64).pin_memory(),
+             torch.tensor(alt_np.ravel(), dtype=torch.float64).pin_memory()]
+    h_par = h_alt[0]
     h_chi2 = torch.zeros(n_models, dtype=torch.float64).pin_memory()
     h_grad = torch.zeros(n_prof * 12, dtype=torch.float64).pin_memory()
     e2e_steps = max(3, args.steps // 2)
@@ -429,8 +450,13 @@ def run_ours(args, world, rank, local):
     t0 = time.perf_counter()
     with torch.cuda.stream(stream):
         for _ in range(e2e_steps):
-            params.copy_(h_par, non_blocking=True)
-            step()
+            params.copy_(h_alt[n_step[0] & 1], non_blocking=True)
+            n_step[0] += 1
+            if args.no_graph:
+                batch.set_params_dev(params, stream=sh)
+                batch.forward_backward(img, data, sigma, chi2, grad, stream=sh)
+            else:
+                batch.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
             h_chi2.copy_(chi2, non_blocking=True)
             h_grad.copy_(grad, non_blocking=True)
             stream.synchronize()
@@ -438,6 +464,12 @@ def run_ours(args, world, rank, local):
     e2e_value = world * n_models * e2e_steps / max_over_ranks(world, e2e_s)
     batch.stats(reset=True)
 
+    # back to the parameters themselves for the counts and the accuracy checks
+    with torch.cuda.stream(stream):
+        params.copy_(p_alt[0], non_blocking=True)
+        batch.set_params_dev(params, stream=sh)
+        batch.forward_backward(img, data, sigma, chi2, grad, stream=sh)
+    torch.cuda.synchronize()
     # evaluate_at calls per step (the tree's algorithmic work), from one
     # recorded forward pass
     batch.record_depth(True)
@@ -519,14 +551,16 @@ def run_ours(args, world, rank, local):
             bf = pg.Batch(models_f, env32)
             bf.enable_adjoint()
             with torch.cuda.stream(stream):
-                for _ in range(2):
+                for k in range(2):
+                    params.copy_(p_alt[k & 1], non_blocking=True)
                     bf.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
             torch.cuda.synchronize()
             nf = max(3, args.steps // 2)
             f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             f0.record(stream)
             with torch.cuda.stream(stream):
-                for _ in range(nf):
+                for k in range(nf):
+                    params.copy_(p_alt[k & 1], non_blocking=True)
                     bf.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
             f1.record(stream)
             torch.cuda.synchronize()
@@ -685,12 +719,23 @@ def run_workload(args, world, rank, local):
         sigma = torch.full_like(data, sig)
         chi2 = torch.zeros(n_models, dtype=torch.float64, device="cuda")
         grad = torch.zeros(batch.n_profiles * 12, dtype=torch.float64, device="cuda")
-        params = torch.tensor(W.param_matrix(specs).ravel(), dtype=torch.float64, device="cuda")
+    # consecutive steps alternate between the parameters and a copy moved by
+    # ~1e-6 relative in every entry, as an optimiser's steps are
+    par_w = W.param_matrix(specs)
+    alt_w = par_w * (1 + 1e-6 * np.random.Generator(np.random.PCG64(6000 + rank)).standard_normal(par_w.shape))
+    alt_w[:, 4] = np.minimum(alt_w[:, 4], 1.0)  # axrat stays <= 1
+    p_alt = [torch.tensor(par_w.ravel(), dtype=torch.float64, device="cuda"),
+             torch.tensor(alt_w.ravel(), dtype=torch.float64, device="cuda")]
+    params = p_alt[0].clone()
+    n_step = [0]
 
-    def step():
+    def step():  # on `stream`
+        params.copy_(p_alt[n_step[0] & 1], non_blocking=True)
+        n_step[0] += 1
         if with_grad:
             batch.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
         else:
+            batch.set_params_dev(params, stream=sh)
             batch.forward(img, stream=sh)
 
     with torch.cuda.stream(stream):
@@ -718,7 +763,8 @@ def run_workload(args, world, rank, local):
     launches = int(stages["kernel_launches"])
     if with_grad:  # stage breakdown from the same steps launched one by one
         with torch.cuda.stream(stream):
-            for _ in range(args.steps):
+            for k in range(args.steps):
+                params.copy_(p_alt[k & 1], non_blocking=True)
                 batch.set_params_dev(params, stream=sh)
                 batch.forward_backward(img, data, sigma, chi2, grad, stream=sh)
         torch.cuda.synchronize()
@@ -729,7 +775,9 @@ def run_workload(args, world, rank, local):
 
     # e2e through the public API: parameters in from pinned host memory, the
     # images (forward) or chi^2 and gradients (cfg5) back, every step
-    h_par = torch.tensor(W.param_matrix(specs).ravel(), dtype=torch.float64).pin_memory()
+    h_alt = [torch.tensor(par_w.ravel(), dtype=torch.float64).pin_memory(),
+             torch.tensor(alt_w.ravel(), dtype=torch.float64).pin_memory()]
+    h_par = h_alt[0]
     d_par = torch.zeros_like(h_par, device="cuda")
     if with_grad:
         h_out = [torch.zeros(n_models, dtype=torch.float64).pin_memory(),
@@ -742,12 +790,12 @@ def run_workload(args, world, rank, local):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     with torch.cuda.stream(stream):
-        for _ in range(e2e_steps):
+        for k in range(e2e_steps):
             if with_grad:
-                params.copy_(h_par, non_blocking=True)
+                params.copy_(h_alt[k & 1], non_blocking=True)
                 batch.step_graph(params, img, data, sigma, chi2, grad, stream=sh)
             else:
-                d_par.copy_(h_par, non_blocking=True)
+                d_par.copy_(h_alt[k & 1], non_blocking=True)
                 batch.set_params_dev(d_par, stream=sh)
                 batch.forward(img, stream=sh)
             for h, d in zip(h_out, dev_out):
@@ -756,6 +804,11 @@ def run_workload(args, world, rank, local):
     e2e_value = world * n_models * e2e_steps / max_over_ranks(world, time.perf_counter() - t0)
     if rank != 0:
         return
+    # the image at the parameters themselves, for the accuracy check
+    with torch.cuda.stream(stream):
+        batch.set_params_dev(p_alt[0], stream=sh)
+        batch.forward(img, stream=sh)
+    torch.cuda.synchronize()
 
     # accuracy against the FP64 path on a sample of the models (cfg5: the
     # direct convolution, the FP64 FFT stopping at 4096 points)
@@ -828,11 +881,38 @@ def run_workload(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_dropin(args, rank, local):
+    """--workload dropin: the drop-in Model::evaluate path alone (cfg1 and
+    cfg2 through pf_model_evaluate, host buffers in and out, one model per
+    call, FP64 and FP32), with the CPU oracle port on the same models unless
+    --no-cpu-baseline. value = cfg1's double-precision calls/s."""
+    import __graft_entry__
+    __graft_entry__.build_cuda()
+    import libprofit_gb300 as pg
+    if rank != 0:
+        return
+    env64 = pg.get_cuda_environment(local, use_double=True)
+    env32 = pg.get_cuda_environment(local, use_double=False)
+    clocks = ClockSampler(local)
+    clocks.start()
+    rates = dropin_rates(env64, env32, cpu=not args.no_cpu_baseline)
+    clk = clocks.stop()
+    line = {"metric": "drop-in Model::evaluate calls/s (one model per call, host buffers)",
+            "value": rates["cfg1"]["fp64_calls_per_s"], "unit": "calls/s", "n_gpus": 1, "steps": None,
+            "warmup": 3, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "cfg1: one 100x100 sersic, 15x15 PSF, direct convolution (value); cfg2: one "
+                                   "1000x1000 bulge + disk + sky, 51x51 PSF by FFT"},
+            "drop_in": rates, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_init(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "dropin":
+        run_dropin(args, rank, local)
     elif args.workload != "cfg4":
         run_workload(args, world, rank, local)
     else:

@@ -8,11 +8,11 @@
 //   adjoint  g_src(q) = sum_{k,l} G(q + (k,l) - h') psf(k,l), h' = size - 1 - h,
 //            over the drawing area, G = the output cotangent placed at the crop.
 // A block stages a source patch and the (reversed or not) PSF, zero-padded to
-// a multiple of 4 columns, in shared memory. Each thread owns a 4-wide by
-// R-tall block of outputs; it reads every source row of its patch once, as
-// 16-byte vectors, and applies it to all the kernel rows that touch it,
+// a multiple of 4 columns, in shared memory. Each thread owns a C-wide (4 or
+// 8) by R-tall block of outputs; it reads every source row of its patch once,
+// as 16-byte vectors, and applies it to all the kernel rows that touch it,
 // taking four kernel taps per 16-byte broadcast read, so that a shared-memory
-// read feeds up to 4 R FMAs.
+// read feeds up to C R FMAs.
 #include <cstdint>
 #include <type_traits>
 
@@ -28,24 +28,29 @@ void launch_conv(int mode, int shape, const ModelDev *models, int n_models, cons
 
 namespace {
 
-// Block shapes: TX x TY threads, each 4 columns by R rows of outputs.
-//   float  0: 16 x 16 x 8 -> 64 x 128 outputs
-//   float  1: 14 x 14 x 5 -> 56 x 70
-//   float  2: 16 x 12 x 8 -> 64 x 96
-//   float  3: 14 x 10 x 7 -> 56 x 70
-//   float  4: 35 x 7 x 8  -> 140 x 56
-//   double 0: 16 x 8 x 4  -> 64 x 32
+// Block shapes: TX x TY threads, each C columns by R rows of outputs.
+//   float  0: 16 x 16, 4 x 8 -> 64 x 128 outputs
+//   float  1: 14 x 14, 4 x 5 -> 56 x 70
+//   float  2: 16 x 12, 4 x 8 -> 64 x 96
+//   float  3: 14 x 10, 4 x 7 -> 56 x 70
+//   float  4: 35 x 7, 4 x 8  -> 140 x 56
+//   double 0: 16 x 8, 4 x 4  -> 64 x 32
+// (8 columns per thread, 64 x 128 and 128 x 64 tiles, measured slower in
+// both directions on the 1024-model step.)
 // The host picks, per batch and direction, the shape that wastes the least
 // tile area over the images it convolves, or, for large single-precision
 // batches, the one the autotuner timed fastest.
 struct Shape {
-	int tx, ty, r;
+	int tx, ty, r, c;
 };
 __host__ __device__ constexpr Shape shape_of(bool dbl, int id)
 {
-	return dbl ? Shape{16, 8, 4}
-	           : (id == 1 ? Shape{14, 14, 5}
-	              : (id == 2 ? Shape{16, 12, 8} : (id == 3 ? Shape{14, 10, 7} : (id == 4 ? Shape{35, 7, 8} : Shape{16, 16, 8}))));
+	return dbl ? Shape{16, 8, 4, 4}
+	           : id == 1 ? Shape{14, 14, 5, 4}
+	           : id == 2 ? Shape{16, 12, 8, 4}
+	           : id == 3 ? Shape{14, 10, 7, 4}
+	           : id == 4 ? Shape{35, 7, 8, 4}
+	                     : Shape{16, 16, 8, 4};
 }
 
 template <typename T>
@@ -82,26 +87,40 @@ __device__ __forceinline__ T cot_at(const ModelDev &m, const T *gout, int x, int
 	return gout[m.out_off + (size_t)cy * m.out_w + cx];
 }
 
-// The multiply-adds of one source row (srow, this thread's 4 + 4 columns) into
-// output rows r0..r1 (kernel row s - r), over the kw4 = 4 floor(kw / 4) taps
-// of whole groups of four; with r0 and r1 known at compile time after
+// C + 4 source values from srow: the thread's C columns and the next 4
+template <typename T, int C>
+__device__ __forceinline__ void load_src(const T *srow, T (&w)[C + 4])
+{
+	using V4 = typename Vec4<T>::type;
+#pragma unroll
+	for (int v = 0; v < C / 4 + 1; v++) {
+		const V4 x = *reinterpret_cast<const V4 *>(srow + 4 * v);
+		w[4 * v] = x.x;
+		w[4 * v + 1] = x.y;
+		w[4 * v + 2] = x.z;
+		w[4 * v + 3] = x.w;
+	}
+}
+
+// The multiply-adds of one source row (srow, this thread's C + 4 columns)
+// into output rows r0..r1 (kernel row s - r), over the kw4 = 4 floor(kw / 4)
+// taps of whole groups of four; with r0 and r1 known at compile time after
 // unrolling, the row loop carries no tests.
-template <typename T, int R>
+template <typename T, int R, int C>
 __device__ __forceinline__ void conv_rows(const T *srow, const T *s_k, int s, int kwp, int kw4, int r0, int r1,
-                                          T (&acc)[R][4])
+                                          T (&acc)[R][C])
 {
 	using V4 = typename Vec4<T>::type;
 	for (int kb = 0; kb < kw4; kb += 4) {
-		const V4 w0 = *reinterpret_cast<const V4 *>(srow + kb);
-		const V4 w1 = *reinterpret_cast<const V4 *>(srow + kb + 4);
-		const T w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+		T w[C + 4];
+		load_src<T, C>(srow + kb, w);
 #pragma unroll
 		for (int r = 0; r < R; r++) {
 			if (r < r0 || r > r1) continue;
 			const V4 kv4 = *reinterpret_cast<const V4 *>(s_k + (s - r) * kwp + kb);
 			const T kv[4] = {kv4.x, kv4.y, kv4.z, kv4.w};
 #pragma unroll
-			for (int c = 0; c < 4; c++)
+			for (int c = 0; c < C; c++)
 #pragma unroll
 				for (int q = 0; q < 4; q++) acc[r][c] = fma(w[c + q], kv[q], acc[r][c]);
 		}
@@ -112,14 +131,12 @@ __device__ __forceinline__ void conv_rows(const T *srow, const T *s_k, int s, in
 // own after every source row's whole groups: fewer multiply-adds than a
 // zero-padded group (measured 2.75 -> 2.68 ms for the adjoint of 1024 models
 // of 280 x 280 with a 25 x 25 PSF, the forward unchanged).
-template <typename T, int R>
+template <typename T, int R, int C>
 __device__ __forceinline__ void conv_tail(const T *srow, const T *s_k, int s, int kwp, int kw4, int tail, int r0,
-                                          int r1, T (&acc)[R][4])
+                                          int r1, T (&acc)[R][C])
 {
-	using V4 = typename Vec4<T>::type;
-	const V4 w0 = *reinterpret_cast<const V4 *>(srow + kw4);
-	const V4 w1 = *reinterpret_cast<const V4 *>(srow + kw4 + 4);
-	const T w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+	T w[C + 4];
+	load_src<T, C>(srow + kw4, w);
 #pragma unroll
 	for (int q = 0; q < 3; q++) {
 		if (q >= tail) break;
@@ -128,7 +145,7 @@ __device__ __forceinline__ void conv_tail(const T *srow, const T *s_k, int s, in
 			if (r < r0 || r > r1) continue;
 			const T kv = s_k[(s - r) * kwp + kw4 + q];
 #pragma unroll
-			for (int c = 0; c < 4; c++) acc[r][c] = fma(w[c + q], kv, acc[r][c]);
+			for (int c = 0; c < C; c++) acc[r][c] = fma(w[c + q], kv, acc[r][c]);
 		}
 	}
 }
@@ -144,13 +161,13 @@ __host__ __device__ constexpr int conv_min_blocks(int threads) { return 65536 / 
 #else
 #define PF_CONV_BOUNDS(threads) __launch_bounds__(threads)
 #endif
-template <typename T, int MODE, int TX, int TY, int R>
+template <typename T, int MODE, int TX, int TY, int R, int C>
 __global__ void PF_CONV_BOUNDS(TX * TY)
 conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restrict__ psf, const T *__restrict__ in,
             const T *__restrict__ direct, T *__restrict__ out, const long long *__restrict__ tile_base,
             long long n_tiles)
 {
-	constexpr int BW = TX * 4, BH = TY * R;  // outputs per block
+	constexpr int BW = TX * C, BH = TY * R;  // outputs per block
 	using V4 = typename Vec4<T>::type;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	T *smem = reinterpret_cast<T *>(smem_raw);
@@ -164,11 +181,11 @@ conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restri
 		const int oh = MODE == CONV_FORWARD ? (int)m.crop_h : (int)m.draw_h;
 		const int tiles_x = (ow + BW - 1) / BW;
 		const int x0 = (int)(local % tiles_x) * BW, y0 = (int)(local / tiles_x) * BH;
-		T acc[R][4];
+		T acc[R][C];
 #pragma unroll
 		for (int r = 0; r < R; r++)
 #pragma unroll
-			for (int c = 0; c < 4; c++) acc[r][c] = 0;
+			for (int c = 0; c < C; c++) acc[r][c] = 0;
 		if (m.conv_required) {
 			const int kw = (int)m.psf_w, kh = (int)m.psf_h;
 			const int kwp = (kw + 3) & ~3;
@@ -221,7 +238,7 @@ conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restri
 				s_k[i] = v;
 			}
 			__syncthreads();
-			const int xb = tx * 4, yb = ty * R;
+			const int xb = tx * C, yb = ty * R;
 			const int kw4 = kw & ~3, tail = kw & 3;
 			if (kh >= R) {
 				// source row s feeds output rows r with kernel row l = s - r in
@@ -230,35 +247,35 @@ conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restri
 				// row test is left in the multiply-add stream
 #pragma unroll
 				for (int s0 = 0; s0 < R - 1; s0++)
-					conv_rows<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, kw4, 0, s0, acc);
+					conv_rows<T, R, C>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, kw4, 0, s0, acc);
 				for (int s0 = R - 1; s0 < kh; s0++)
-					conv_rows<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, kw4, 0, R - 1, acc);
+					conv_rows<T, R, C>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, kw4, 0, R - 1, acc);
 #pragma unroll
 				for (int d = 0; d < R - 1; d++) {
-					conv_rows<T, R>(s_src + (yb + kh + d) * pw + xb, s_k, kh + d, kwp, kw4, d + 1, R - 1, acc);
+					conv_rows<T, R, C>(s_src + (yb + kh + d) * pw + xb, s_k, kh + d, kwp, kw4, d + 1, R - 1, acc);
 				}
 			}
 			else {
 				for (int s0 = 0; s0 < R + kh - 1; s0++) {
-					conv_rows<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, kw4, max(0, s0 - kh + 1),
-					                min(R - 1, s0), acc);
+					conv_rows<T, R, C>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, kw4, max(0, s0 - kh + 1),
+					                   min(R - 1, s0), acc);
 				}
 			}
 			if (tail) {
 				for (int s0 = 0; s0 < R + kh - 1; s0++) {
-					conv_tail<T, R>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, kw4, tail, max(0, s0 - kh + 1),
-					                min(R - 1, s0), acc);
+					conv_tail<T, R, C>(s_src + (yb + s0) * pw + xb, s_k, s0, kwp, kw4, tail, max(0, s0 - kh + 1),
+					                   min(R - 1, s0), acc);
 				}
 			}
 			__syncthreads();
 		}
-		const int xo = x0 + tx * 4;
+		const int xo = x0 + tx * C;
 #pragma unroll
 		for (int r = 0; r < R; r++) {
 			const int yo = y0 + ty * R + r;
 			if (yo >= oh) continue;
 #pragma unroll
-			for (int c = 0; c < 4; c++) {
+			for (int c = 0; c < C; c++) {
 				const int x = xo + c;
 				if (x >= ow) continue;
 				if (MODE == CONV_FORWARD) {
@@ -293,7 +310,7 @@ template <typename T>
 long long conv_tiles(unsigned int w, unsigned int h, int shape)
 {
 	const Shape sh = shape_of(std::is_same<T, double>::value, shape);
-	const unsigned int bw = sh.tx * 4, bh = sh.ty * sh.r;
+	const unsigned int bw = sh.tx * sh.c, bh = sh.ty * sh.r;
 	return (long long)((w + bw - 1) / bw) * ((h + bh - 1) / bh);
 }
 
@@ -301,35 +318,35 @@ template <typename T>
 size_t conv_smem(unsigned int kw, unsigned int kh, int shape)
 {
 	const Shape sh = shape_of(std::is_same<T, double>::value, shape);
-	const size_t bw = sh.tx * 4, bh = sh.ty * sh.r;
+	const size_t bw = sh.tx * sh.c, bh = sh.ty * sh.r;
 	const size_t kwp = (kw + 3) & ~3u;
 	return sizeof(T) * ((bw + kwp) * (bh + kh - 1) + kwp * kh);
 }
 
 namespace {
 
-template <typename T, int TX, int TY, int R>
+template <typename T, int TX, int TY, int R, int C>
 cudaError_t configure_shape(size_t smem)
 {
-	cudaError_t e = cudaFuncSetAttribute(conv_kernel<T, CONV_FORWARD, TX, TY, R>,
+	cudaError_t e = cudaFuncSetAttribute(conv_kernel<T, CONV_FORWARD, TX, TY, R, C>,
 	                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
-	return cudaFuncSetAttribute(conv_kernel<T, CONV_ADJOINT, TX, TY, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	                            (int)smem);
+	return cudaFuncSetAttribute(conv_kernel<T, CONV_ADJOINT, TX, TY, R, C>,
+	                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-template <typename T, int TX, int TY, int R>
+template <typename T, int TX, int TY, int R, int C>
 void launch_shape(int mode, const ModelDev *models, int n_models, const T *psf, const T *in, const T *direct, T *out,
                   const long long *tile_base, long long n_tiles, size_t smem, int n_sm, cudaStream_t stream)
 {
 	int blocks = (int)(n_tiles < (long long)n_sm * 8 ? n_tiles : (long long)n_sm * 8);
 	if (blocks < 1) blocks = 1;
 	if (mode == CONV_FORWARD)
-		conv_kernel<T, CONV_FORWARD, TX, TY, R><<<blocks, TX * TY, smem, stream>>>(models, n_models, psf, in, direct,
-		                                                                          out, tile_base, n_tiles);
+		conv_kernel<T, CONV_FORWARD, TX, TY, R, C><<<blocks, TX * TY, smem, stream>>>(models, n_models, psf, in,
+		                                                                             direct, out, tile_base, n_tiles);
 	else
-		conv_kernel<T, CONV_ADJOINT, TX, TY, R><<<blocks, TX * TY, smem, stream>>>(models, n_models, psf, in, direct,
-		                                                                          out, tile_base, n_tiles);
+		conv_kernel<T, CONV_ADJOINT, TX, TY, R, C><<<blocks, TX * TY, smem, stream>>>(models, n_models, psf, in,
+		                                                                             direct, out, tile_base, n_tiles);
 }
 
 }  // namespace
@@ -337,17 +354,17 @@ void launch_shape(int mode, const ModelDev *models, int n_models, const T *psf, 
 template <>
 cudaError_t conv_configure<float>(size_t smem, int shape)
 {
-	if (shape == 1) return configure_shape<float, 14, 14, 5>(smem);
-	if (shape == 2) return configure_shape<float, 16, 12, 8>(smem);
-	if (shape == 3) return configure_shape<float, 14, 10, 7>(smem);
-	if (shape == 4) return configure_shape<float, 35, 7, 8>(smem);
-	return configure_shape<float, 16, 16, 8>(smem);
+	if (shape == 1) return configure_shape<float, 14, 14, 5, 4>(smem);
+	if (shape == 2) return configure_shape<float, 16, 12, 8, 4>(smem);
+	if (shape == 3) return configure_shape<float, 14, 10, 7, 4>(smem);
+	if (shape == 4) return configure_shape<float, 35, 7, 8, 4>(smem);
+	return configure_shape<float, 16, 16, 8, 4>(smem);
 }
 
 template <>
 cudaError_t conv_configure<double>(size_t smem, int)
 {
-	return configure_shape<double, 16, 8, 4>(smem);
+	return configure_shape<double, 16, 8, 4, 4>(smem);
 }
 
 template <>
@@ -355,11 +372,14 @@ void launch_conv<float>(int mode, int shape, const ModelDev *models, int n_model
                         const float *direct, float *out, const long long *tile_base, long long n_tiles, size_t smem,
                         int n_sm, cudaStream_t stream)
 {
-	if (shape == 1) launch_shape<float, 14, 14, 5>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
-	else if (shape == 2) launch_shape<float, 16, 12, 8>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
-	else if (shape == 3) launch_shape<float, 14, 10, 7>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
-	else if (shape == 4) launch_shape<float, 35, 7, 8>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
-	else launch_shape<float, 16, 16, 8>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
+#define PF_CONV_SHAPE(TX, TY, R, C) \
+	launch_shape<float, TX, TY, R, C>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream)
+	if (shape == 1) PF_CONV_SHAPE(14, 14, 5, 4);
+	else if (shape == 2) PF_CONV_SHAPE(16, 12, 8, 4);
+	else if (shape == 3) PF_CONV_SHAPE(14, 10, 7, 4);
+	else if (shape == 4) PF_CONV_SHAPE(35, 7, 8, 4);
+	else PF_CONV_SHAPE(16, 16, 8, 4);
+#undef PF_CONV_SHAPE
 }
 
 template <>
@@ -367,14 +387,14 @@ void launch_conv<double>(int mode, int, const ModelDev *models, int n_models, co
                          const double *direct, double *out, const long long *tile_base, long long n_tiles, size_t smem,
                          int n_sm, cudaStream_t stream)
 {
-	launch_shape<double, 16, 8, 4>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
+	launch_shape<double, 16, 8, 4, 4>(mode, models, n_models, psf, in, direct, out, tile_base, n_tiles, smem, n_sm, stream);
 }
 
 template <typename T>
 void conv_tile_dims(int shape, int *bw, int *bh)
 {
 	const Shape sh = shape_of(std::is_same<T, double>::value, shape);
-	*bw = sh.tx * 4;
+	*bw = sh.tx * sh.c;
 	*bh = sh.ty * sh.r;
 }
 

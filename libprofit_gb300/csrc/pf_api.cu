@@ -729,6 +729,17 @@ struct ConvPlan {
 	bool split = true;                      // single precision: a split pool unless PF_ENV_NO_SPLIT
 };
 
+// PF_CONV_SHAPE: a single-precision direct-convolution block shape to use in
+// both directions instead of the chosen one, for exercising every shape
+// (-1: none)
+static int forced_conv_shape()
+{
+	const char *v = std::getenv("PF_CONV_SHAPE");
+	if (!v || !*v) return -1;
+	const int s = std::atoi(v);
+	return s >= 0 && s < pf::conv_num_shapes<float>() ? s : -1;
+}
+
 // The convolution block shape covering the given images with the least tile area.
 template <typename T>
 int best_conv_shape(const std::vector<std::pair<unsigned int, unsigned int>> &dims)
@@ -1036,6 +1047,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 			if (!d.use_fft) conv_dims.push_back({d.crop_w, d.crop_h});
 		}
 		b->fwd_shape = plan.shape >= 0 ? plan.shape : best_conv_shape<float>(conv_dims);
+		if (forced_conv_shape() >= 0) b->fwd_shape = forced_conv_shape();
 		long long t = 0;
 		for (size_t i = 0; i < n_models; i++) {
 			const pf::ModelDev &d = b->mdev[i];
@@ -1854,6 +1866,7 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 		if (m.conv_required && (b->dbl || !m.use_fft)) conv_dims.push_back({m.draw_w, m.draw_h});
 	}
 	b->adj_shape = b->dbl ? best_conv_shape<double>(conv_dims) : best_conv_shape<float>(conv_dims);
+	if (!b->dbl && forced_conv_shape() >= 0) b->adj_shape = forced_conv_shape();
 	for (size_t i = 0; i < n_models; i++) {
 		const pf::ModelDev &m = b->mdev[i];
 		for (int q = 0; q < m.n_profiles; q++) {
@@ -1897,7 +1910,8 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	                       cudaMemcpyHostToDevice));
 	PF_CUDA_TRY(b->dbl ? pf::conv_configure<double>(b->adj_smem, b->adj_shape)
 	                   : pf::conv_configure<float>(b->adj_smem, b->adj_shape));
-	if (!b->dbl && !(b->env->flags & PF_ENV_NO_AUTOTUNE) && b->total_out >= (1ull << 22) && tiles > 0) {
+	if (!b->dbl && !(b->env->flags & PF_ENV_NO_AUTOTUNE) && b->total_out >= (1ull << 22) && tiles > 0 &&
+	    forced_conv_shape() < 0) {
 		// the autotuner, adjoint convolution: each block shape timed over the
 		// batch's directly convolved models (zero cotangents), the fastest kept
 		PF_CUDA_TRY(cudaMemsetAsync(b->d_gout, 0, sizeof(float) * std::max<uint64_t>(1, b->total_out), b->env->stream));

@@ -119,6 +119,34 @@ def test_direct_convolution_shapes(envs, kw, kh, w, h):
     assert np.all(np.abs(g32 - g64) <= 1e-3 * np.abs(g64) + 1e-4 * scale), np.abs(g32 - g64).max() / scale
 
 
+N_SHAPES = 5
+
+
+@pytest.mark.parametrize("shape", range(N_SHAPES))
+def test_every_block_shape(envs, shape, monkeypatch):
+    """Each single-precision block shape (the autotuner may pick any, the
+    least-area rule never picks shape 3), forced with PF_CONV_SHAPE, in both directions on
+    a ragged image with a 25 x 25 and a 7 x 6 PSF, against the plain FP64
+    path as above."""
+    env64, env32 = envs
+    monkeypatch.setenv("PF_CONV_SHAPE", str(shape))
+    w, h = 131, 77
+    y, x = np.mgrid[0:h, 0:w]
+    cot = 1.0 + 0.5 * np.sin(x / 7.0) * np.cos(y / 5.0)
+    for kw, kh in ((25, 25), (7, 6)):
+        psf = _psf(kw, kh)
+        profiles = _profiles(w, h)
+        img64, g64, _ = _run(env64, True, w, h, psf, profiles, cot)
+        img32, g32, info = _run(env32, False, w, h, psf, profiles, cot)
+        assert info["forward_shape"] == shape and info["adjoint_shape"] == shape
+        assert abs(img32.sum() - img64.sum()) <= 1e-5 * abs(img64.sum())
+        peak = np.abs(img64).max()
+        bright = np.abs(img64) > 1e-3 * peak
+        assert np.max(np.abs(img32[bright] - img64[bright]) / np.abs(img64[bright])) <= 1e-4
+        scale = np.abs(g64).max()
+        assert np.all(np.abs(g32 - g64) <= 1e-3 * np.abs(g64) + 1e-4 * scale), np.abs(g32 - g64).max() / scale
+
+
 def test_block_shapes_covered():
     """The image sizes above select at least four of the five block shapes
     (shape 3 has shape 1's tile, so the least-area rule never picks it)."""
