@@ -590,11 +590,15 @@ level64_kernel(const ProfileDev *__restrict__ profs, double *__restrict__ conv_i
 		if (blockIdx.x == 0 && threadIdx.x == 0) pool.cnt[LC_BOUND + level + 2] = hi;
 		return;
 	}
-	const long long n_items = (long long)(hi - lo) * kSlots;
+	// chunk-major items (every box's chunk 0, then every box's chunk 1, ...):
+	// the real chunks (res^2 / 16 of a box's kSlots) come first and fill the
+	// grid's warps in one pass
+	const unsigned int nb = hi - lo;
+	const long long n_items = (long long)nb * kSlots;
 	for (long long item = (long long)blockIdx.x * kWarps64 + warp; item < n_items;
 	     item += (long long)gridDim.x * kWarps64) {
-		const unsigned int b = lo + (unsigned int)(item / kSlots);
-		const unsigned int c = (unsigned int)(item % kSlots);
+		const unsigned int b = lo + (unsigned int)(item % nb);
+		const unsigned int c = (unsigned int)(item / nb);
 		LevelBox64 &B = pool.box[b];
 		const uint32_t meta = B.meta;
 		if (meta == kDeadBox) continue;

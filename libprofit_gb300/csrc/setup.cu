@@ -486,18 +486,20 @@ __device__ void radial_setup(ProfileDev &p, const ModelDev &m, double bn, const 
 }  // namespace
 
 // The independent inverse-gamma solves of the sersic-like profiles, one per
-// thread, task-major so that each warp runs one kind of solve:
+// thread, the task in blockIdx.y so that each warp runs one kind of solve:
 //   task 0  bn = P^-1(1/2, 2n)                 (sersic, coresersic)
 //   task 1  P^-1(1 - n^2/2000, 2n)             (sersic switch radius, adjust)
 //   task 2  P^-1(0.9999, 2n)                   (sersic rscale_max, adjust, rscale_max = 0)
 __global__ void setup_solves_kernel(const ProfileDev *profs, int n_profiles, double *solves, unsigned int *err)
 {
+	// task blockIdx.y, profile i: each warp runs one kind of solve (a warp
+	// mixing them would run their iterations one after another)
 	const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-	if (t == 0) err[1] = 0xffffffffu;  // this pass's first invalid profile: none yet
-	if (t >= 3LL * n_profiles) {
+	if (t == 0 && blockIdx.y == 0) err[1] = 0xffffffffu;  // this pass's first invalid profile: none yet
+	if (t >= n_profiles) {
 		return;
 	}
-	const int task = (int)(t / n_profiles), i = (int)(t % n_profiles);
+	const int task = (int)blockIdx.y, i = (int)t;
 	const int kind = profs[i].kind;
 	const double nser = profs[i].par[7];
 	// a valid profile's solve depends on nser alone (kind and flags are fixed
@@ -608,8 +610,8 @@ void launch_setup(const ModelDev *models, ProfileDev *profs, int n_profiles, int
 {
 	// single-warp blocks: the FP64-heavy work spreads over as many SMs as possible
 	if (n_profiles > 0) {
-		const long long tasks = 3LL * n_profiles;
-		setup_solves_kernel<<<(unsigned int)((tasks + 31) / 32), 32, 0, stream>>>(profs, n_profiles, solves, err);
+		setup_solves_kernel<<<dim3((unsigned int)((n_profiles + 31) / 32), 3), 32, 0, stream>>>(profs, n_profiles,
+		                                                                                        solves, err);
 	}
 	int blocks = (n_profiles + 31) / 32;
 	if (blocks < 1) blocks = 1;

@@ -71,7 +71,7 @@ __device__ inline double digamma(double x)
 // (hundreds of cycles each in FP64 on this GPU) run side by side instead of
 // on the running product's dependency chain; the terms, the sum and the stop
 // are the one-at-a-time loop's, in its order.
-__device__ inline double pgamma_series(double a, double x)
+__device__ inline double pgamma_series(double a, double x, double lga1)
 {
 	double ap = a, term = 1., sum = 1.;
 	int n = 1;
@@ -95,8 +95,10 @@ __device__ inline double pgamma_series(double a, double x)
 		}
 		if (done) break;
 	}
-	return exp(a * log(x) - x - lgamma(a + 1.)) * sum;
+	return exp(a * log(x) - x - lga1) * sum;
 }
+
+__device__ inline double pgamma_series(double a, double x) { return pgamma_series(a, x, lgamma(a + 1.)); }
 
 // Q(a, x) = x^a e^-x / Gamma(a) / (b_0 + a_1 / (b_1 + a_2 / (b_2 + ...))),
 // b_i = x + 2i + 1 - a, a_i = -i (i - a), for x >= a + 1. The continued
@@ -105,7 +107,7 @@ __device__ inline double pgamma_series(double a, double x)
 // rescaled by exact powers of two against overflow: two multiply-adds per
 // term on the dependency chain instead of two divisions; converged when four
 // more terms move B / A by less than 2 eps relative.
-__device__ inline double qgamma_cf(double a, double x)
+__device__ inline double qgamma_cf(double a, double x, double lga)
 {
 	double b = x + 1. - a;
 	double A2 = 1., A1 = b, B2 = 0., B1 = 1.;  // A_{i-2}, A_{i-1}, B_{i-2}, B_{i-1}
@@ -137,8 +139,10 @@ __device__ inline double qgamma_cf(double a, double x)
 		}
 		f = fn;
 	}
-	return exp(a * log(x) - x - lgamma(a)) * f;
+	return exp(a * log(x) - x - lga) * f;
 }
+
+__device__ inline double qgamma_cf(double a, double x) { return qgamma_cf(a, x, lgamma(a)); }
 
 __device__ inline double pgamma(double x, double a)
 {
@@ -209,9 +213,16 @@ __device__ inline double qgamma(double p, double a, double guess = -1.)
 		x = a;
 		if (!(x > lo && x < hi)) x = 0.5 * (lo + hi);
 	}
-	const double lga = lgamma(a);
+	// log Gamma(a) and log Gamma(a + 1) once for all the iterations' P and Q
+	// (each from lgamma itself: the solves feed ceilings, src/sersic.cpp:
+	// 262-276, so they stay as close to the reference's values as lgamma is)
+	const double lga = lgamma(a), lga1 = lgamma(a + 1.);
 	for (int it = 0; it < 200; it++) {
-		const double f = use_q ? (q - qgamma_upper(x, a)) : (pgamma(x, a) - p);
+		double f;
+		if (!(x > 0.)) f = use_q ? q - 1. : -p;
+		else if (isinf(x)) f = use_q ? q : 1. - p;
+		else if (x < a + 1.) f = use_q ? (q - (1. - pgamma_series(a, x, lga1))) : (pgamma_series(a, x, lga1) - p);
+		else f = use_q ? (q - qgamma_cf(a, x, lga)) : ((1. - qgamma_cf(a, x, lga)) - p);
 		if (f == 0.) break;
 		if (f < 0.) lo = x; else hi = x;
 		const double pdf = exp((a - 1.) * log(x) - x - lga);
