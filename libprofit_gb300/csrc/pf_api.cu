@@ -729,6 +729,16 @@ struct ConvPlan {
 	bool split = true;                      // single precision: a split pool unless PF_ENV_NO_SPLIT
 };
 
+// PF_SPLIT: 1 splits the single-precision subsampling trees off to other
+// warps, 0 walks them where met, instead of the timed choice, for exercising
+// both (-1: not set)
+static int forced_split()
+{
+	const char *v = std::getenv("PF_SPLIT");
+	if (!v || !*v) return -1;
+	return std::atoi(v) != 0 ? 1 : 0;
+}
+
 // PF_CONV_SHAPE: a single-precision direct-convolution block shape to use in
 // both directions instead of the chosen one, for exercising every shape
 // (-1: none)
@@ -1461,7 +1471,9 @@ pf_status pf_batch_create_masked(pf_env *env, const pf_model_desc *models, size_
 	}
 	*batch = nullptr;
 	PF_CUDA_TRY(cudaSetDevice(env->device));
-	const ConvPlan fixed;
+	ConvPlan fixed;
+	const int fsplit = forced_split();
+	if (fsplit == 0) fixed.split = false;
 	bool tune = !(env->flags & (PF_ENV_DOUBLE | PF_ENV_NO_AUTOTUNE));
 	uint64_t out_pixels = 0;
 	bool any_auto = false;
@@ -1469,8 +1481,11 @@ pf_status pf_batch_create_masked(pf_env *env, const pf_model_desc *models, size_
 		out_pixels += (uint64_t)models[i].width * models[i].height;
 		any_auto |= models[i].convolver == PF_CONV_AUTO && models[i].psf_offset >= 0 && models[i].psf_w > 0;
 	}
-	const bool tune_split = tune && out_pixels >= (1ull << 22);
-	tune = tune_split && any_auto;
+	// the split of the subsampling trees is timed for every single-precision
+	// batch (it loses on some small ones, e.g. one 1000 x 1000 model); the
+	// convolution methods and shapes only from 2^22 output pixels up
+	const bool tune_split = tune && fsplit < 0;
+	tune = tune && out_pixels >= (1ull << 22) && any_auto;
 	if (!tune) {
 		pf_status s = create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool,
 		                             mask_pool_len, fixed, batch);
@@ -1511,7 +1526,8 @@ pf_status pf_batch_create_masked(pf_env *env, const pf_model_desc *models, size_
 	// pixels' trees would set the pass's end, and costs a little where the
 	// work is spread already: the evaluation timed both ways
 	bool split = bd->split.box != nullptr;
-	if (split) {
+	if (fsplit >= 0) split = split && fsplit == 1;
+	else if (split) {
 		const double t_split = time_eval(bd, true), t_walk = time_eval(bd, false);
 		split = !(t_walk > 0 && t_split > 0 && t_walk < t_split);
 	}

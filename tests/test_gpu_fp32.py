@@ -76,9 +76,14 @@ def test_fp32_tree_equals_oracle(env32, oracle_lib, name):
     assert np.array_equal(counts[:16], ocounts[0][:16])
 
 
-def test_fp32_batch_equals_single(env32):
+def test_fp32_batch_equals_single():
+    """Models packed in one batch render as they do alone, bit for bit, in an
+    environment without timed choices (PF_ENV_NO_AUTOTUNE: the timed split
+    of the subsampling trees may add a multi-profile pixel's values in
+    another order, which can move its last bit)."""
     import torch
     import libprofit_gb300 as pg
+    env32 = pg.CUDAEnv(0, use_double=False, autotune=False)
     names = ["cfg1_sersic_brute", "king_rotated", "mixed_conv_sky_psf", "finesampled", "brokenexp_shaped"]
     models = [product_model(GOLDEN[n]["spec"], GOLDEN[n]["psf"], env32) for n in names]
     b = pg.Batch(models, env32)
@@ -93,3 +98,39 @@ def test_fp32_batch_equals_single(env32):
         assert np.array_equal(img.astype(np.float64), models[i].evaluate())
         check_fp32(img.astype(np.float64), GOLDEN[n]["image"], n)
         assert abs(flux[i].item() - img.astype(np.float64).sum()) <= 1e-6 * abs(img.sum())
+
+
+def _forward32(m, env):
+    import torch
+    import libprofit_gb300 as pg
+    b = pg.Batch([m], env)
+    b.record_depth(True)
+    out = torch.zeros(b.total_pixels, dtype=torch.float32, device="cuda")
+    b.forward(out)
+    b.check()
+    maps = b.depth()
+    return out.cpu().numpy(), [d for d, _ in maps], np.array([c for _, c in maps]), b.split_info()
+
+
+def test_fp32_split_equals_walk(env32, monkeypatch):
+    """The subsampling trees split off to other warps (PF_SPLIT=1) or walked
+    where met (PF_SPLIT=0; the batch otherwise times both): the same depth
+    maps and per-level counts, the same image bits for one-profile models,
+    and several-profile pixels within the last bit (addition order)."""
+    used = 0
+    for name in sorted(GOLDEN):
+        entry = GOLDEN[name]
+        runs = []
+        for mode in ("1", "0"):
+            monkeypatch.setenv("PF_SPLIT", mode)
+            runs.append(_forward32(product_model(entry["spec"], entry["psf"], env32), env32))
+        (a, da, ca, info), (w, dw, cw, winfo) = runs
+        assert winfo["boxes"] == 0
+        used += info["boxes"]
+        assert len(da) == len(dw) and all(np.array_equal(x, y) for x, y in zip(da, dw)), name
+        assert np.array_equal(ca, cw), name
+        if len(entry["spec"]["profiles"]) == 1:
+            assert np.array_equal(a, w), name
+        else:
+            np.testing.assert_allclose(a, w, rtol=1e-6, atol=0, err_msg=name)
+    assert used > 0
