@@ -14,7 +14,7 @@ Other workloads (--workload, one JSON line each, same keys):
   cfg3  4096 uneven models (1-3 of the six radial kinds, own PSFs, method by
         the autotuner): FP32 forward of the whole batch, models/s;
   cfg5  the 4096x4096 field with 10,000 profiles and a sky, 101x101 PSF by an
-        8192x8192 FFT: FP32 forward + chi^2 + gradients of all 10,001
+        4608x4608 FFT: FP32 forward + chi^2 + gradients of all 10,001
         profiles, fields/s.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -854,7 +854,7 @@ def run_workload(args, world, rank, local):
     desc = {"cfg2": "one 1000x1000 model: sersic bulge + disk + sky, 51x51 Moffat PSF by FFT, forward",
             "cfg3": "%d models, sides 64-512, 1-3 radial profiles of six kinds, own Moffat PSFs (15-41), "
                     "autotuned convolution, forward" % n_models,
-            "cfg5": "one 4096x4096 field: 10,000 radial profiles + sky, 101x101 Moffat PSF by an 8192x8192 FFT, "
+            "cfg5": "one 4096x4096 field: 10,000 radial profiles + sky, 101x101 Moffat PSF by a 4608x4608 FFT, "
                     "forward + chi2 + gradients of all profiles"}[args.workload]
     line = {
         "metric": METRIC, "value": value, "unit": "models/s", "n_gpus": world, "steps": args.steps,
