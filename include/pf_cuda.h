@@ -240,6 +240,20 @@ PF_API pf_status pf_model_evaluate(pf_env *env, const pf_model_desc *model, cons
  * or NULL. */
 PF_API pf_status pf_env_last_model_stats(pf_env *env, pf_stage_times *times, int64_t *level_counts,
                                          size_t n_profiles);
+
+/* The autotuner's decisions (single precision: the convolution method per
+ * model and the block shapes of large PF_CONV_AUTO batches, whether the
+ * subsampling trees split off to other warps) are kept by the environment,
+ * keyed by the GPU and the batch's layout (dimensions, PSF sizes, convolvers,
+ * masks, profile kinds and subsampling controls; not parameter values): a
+ * batch of a layout seen before is created without timing anything, as
+ * FFTW reuses a plan. With the environment variable PF_AUTOTUNE_CACHE naming
+ * a file when the environment is created, the decisions are read from it
+ * and new ones appended to it (one text line each), so that they outlive the
+ * process, as FFTW's wisdom does (include/profit/library.h, src/library.cpp:
+ * 69-165). timed: decisions made by timing in this environment; reused:
+ * decisions taken from the cache. Either pointer may be NULL. */
+PF_API pf_status pf_env_autotune_counts(pf_env *env, uint64_t *timed, uint64_t *reused);
 /* The same with a calculation mask (host bytes; dimensions as the model's
  * adjust_mask says; NULL: none). */
 PF_API pf_status pf_model_evaluate_masked(pf_env *env, const pf_model_desc *model, const pf_profile_desc *profiles,

@@ -256,6 +256,15 @@ class CUDAEnv:
     def handle(self):
         return self._h
 
+    def autotune_counts(self):
+        """{"timed", "reused"}: the autotuner's decisions made by timing in
+        this environment and those taken from its cache (the same batch
+        layout seen before, or the PF_AUTOTUNE_CACHE file read at its
+        creation) (pf_env_autotune_counts)."""
+        t, r = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(_ffi.load().pf_env_autotune_counts(self._h, ctypes.byref(t), ctypes.byref(r)))
+        return {"timed": t.value, "reused": r.value}
+
     def close(self):
         if self._h:
             _ffi.load().pf_env_destroy(self._h)

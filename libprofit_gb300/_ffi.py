@@ -113,6 +113,7 @@ _SIGNATURES = {
                                             ctypes.POINTER(ctypes.POINTER(ctypes.c_double)),
                                             ctypes.POINTER(ctypes.c_uint32)]),
     "pf_env_last_model_stats": (ctypes.c_int, [_P, _P, _P, ctypes.c_size_t]),
+    "pf_env_autotune_counts": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "pf_batch_split_info": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     "pf_fits_write": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                      ctypes.c_uint32, ctypes.c_double, ctypes.c_double]),

@@ -353,6 +353,14 @@ void adjusted_mask(const pf_model_desc &m, const Geometry &g, const uint8_t *mas
 
 }  // namespace
 
+// One batch layout's autotuned decisions (-1 / empty: not decided yet).
+struct TuneEntry {
+	int fwd_shape = -1;         // forward direct-convolution block shape
+	int split = -1;             // subsampling trees split off to other warps
+	int adj_shape = -1;         // adjoint direct-convolution block shape
+	std::vector<int8_t> fft;    // per model: the FFT (PF_CONV_AUTO models)
+};
+
 struct pf_env {
 	int device = 0;
 	uint32_t flags = 0;
@@ -382,10 +390,21 @@ struct pf_env {
 		pf_stage_times last_times{};
 		std::vector<unsigned long long> last_counts;
 	} cache;
+	// The autotuner's decisions (the analogue of FFTW's plans and wisdom), by
+	// batch layout: kept for the environment's life and, with PF_AUTOTUNE_CACHE
+	// naming a file at its creation, read from and appended to that file.
+	struct Tune {
+		std::mutex mu;
+		std::map<uint64_t, TuneEntry> entries;
+		std::string file;
+		std::string gpu;                   // device name and SM count: part of every key
+		uint64_t timed = 0, reused = 0;    // decisions timed, decisions taken from the cache
+	} tune;
 };
 
 struct pf_batch {
 	pf_env *env = nullptr;
+	uint64_t tune_key = 0;              // its layout's key in env->tune (0: not tuned)
 	bool dbl = true;
 	std::vector<pf_model_desc> models;
 	std::vector<pf_profile_desc> profiles;
@@ -572,6 +591,105 @@ bool same_profile_layout(const pf_profile_desc &a, const pf_profile_desc &b)
 
 }  // namespace
 
+// ---- the autotuner's decision cache
+
+static uint64_t fnv1a(uint64_t h, const void *data, size_t n)
+{
+	const unsigned char *p = static_cast<const unsigned char *>(data);
+	for (size_t i = 0; i < n; i++) {
+		h ^= p[i];
+		h *= 1099511628211ull;
+	}
+	return h;
+}
+
+// The key of a batch layout: the GPU, every model's geometry, PSF size,
+// convolver, mask and crop settings, and every profile's kind and subsampling
+// controls; not the parameter values. Never 0.
+static uint64_t tune_key(const pf_env *env, const pf_model_desc *models, size_t n_models,
+                         const pf_profile_desc *profiles, size_t n_profiles)
+{
+	uint64_t h = fnv1a(1469598103934665603ull, env->tune.gpu.data(), env->tune.gpu.size());
+	h = fnv1a(h, &n_models, sizeof(n_models));
+	for (size_t i = 0; i < n_models; i++) {
+		const pf_model_desc &m = models[i];
+		const uint32_t f[] = {m.width, m.height, m.finesampling, (uint32_t)m.return_finesampled, m.first_profile,
+		                      m.n_profiles, (uint32_t)(m.psf_offset >= 0), m.psf_w, m.psf_h, (uint32_t)m.convolver,
+		                      (uint32_t)(m.mask_offset >= 0), (uint32_t)m.adjust_mask, (uint32_t)m.no_crop,
+		                      m.mask_w, m.mask_h};
+		h = fnv1a(h, f, sizeof(f));
+	}
+	h = fnv1a(h, &n_profiles, sizeof(n_profiles));
+	for (size_t i = 0; i < n_profiles; i++) {
+		const pf_profile_desc &d = profiles[i];
+		const int32_t f[] = {d.kind, d.convolve, d.rough, d.adjust, (int32_t)d.resolution, (int32_t)d.max_recursions};
+		h = fnv1a(h, f, sizeof(f));
+	}
+	return h ? h : 1;
+}
+
+// One line per entry: "pfcuda-tune 1 <key> <fwd> <split> <adj> <fft: one digit per model, or ->";
+// a later line for a key replaces an earlier one. Lines that do not parse are skipped.
+static void tune_load(pf_env *e)
+{
+	std::FILE *f = std::fopen(e->tune.file.c_str(), "r");
+	if (!f) return;
+	std::string line;
+	char buf[4096];
+	while (std::fgets(buf, sizeof(buf), f)) {
+		line += buf;
+		if (line.empty() || line.back() != '\n') {
+			if (!std::feof(f)) continue;
+		}
+		unsigned long long key = 0;
+		int fwd = -1, split = -1, adj = -1, used = 0;
+		if (std::sscanf(line.c_str(), "pfcuda-tune 1 %llx %d %d %d %n", &key, &fwd, &split, &adj, &used) == 4 &&
+		    used > 0) {
+			TuneEntry t;
+			t.fwd_shape = fwd;
+			t.split = split;
+			t.adj_shape = adj;
+			for (size_t i = (size_t)used; i < line.size() && (line[i] == '0' || line[i] == '1'); i++)
+				t.fft.push_back((int8_t)(line[i] - '0'));
+			e->tune.entries[key] = t;
+		}
+		line.clear();
+	}
+	std::fclose(f);
+}
+
+// the entry of `key` (a copy); false if none
+static bool tune_lookup(pf_env *e, uint64_t key, TuneEntry *out)
+{
+	std::lock_guard<std::mutex> lock(e->tune.mu);
+	auto it = e->tune.entries.find(key);
+	if (it == e->tune.entries.end()) return false;
+	*out = it->second;
+	return true;
+}
+
+// entry `key` updated by `update` and, with a cache file, appended to it
+template <typename F>
+static void tune_store(pf_env *e, uint64_t key, F update)
+{
+	std::lock_guard<std::mutex> lock(e->tune.mu);
+	TuneEntry &t = e->tune.entries[key];
+	update(t);
+	e->tune.timed++;
+	if (e->tune.file.empty()) return;
+	std::string line = "pfcuda-tune 1 ";
+	char head[96];
+	std::snprintf(head, sizeof(head), "%llx %d %d %d ", (unsigned long long)key, t.fwd_shape, t.split, t.adj_shape);
+	line += head;
+	if (t.fft.empty()) line += "-";
+	for (int8_t v : t.fft) line += v ? '1' : '0';
+	line += "\n";
+	if (std::FILE *f = std::fopen(e->tune.file.c_str(), "a")) {
+		std::fputs(line.c_str(), f);
+		std::fclose(f);
+	}
+}
+
 extern "C" {
 
 const char *pf_last_error(void) { return g_last_error.c_str(); }
@@ -591,6 +709,15 @@ pf_status pf_user_profile_info(const char **name, const char *const **param_name
 
 const char *pf_version(void) { return "0.1.0 (libprofit 1.9.3 image path, sm_103a)"; }
 
+pf_status pf_env_autotune_counts(pf_env *env, uint64_t *timed, uint64_t *reused)
+{
+	if (!env) return fail(PF_ERR_INVALID_PARAMETER, "env is NULL");
+	std::lock_guard<std::mutex> lock(env->tune.mu);
+	if (timed) *timed = env->tune.timed;
+	if (reused) *reused = env->tune.reused;
+	return PF_OK;
+}
+
 pf_status pf_env_create(int device, uint32_t flags, pf_env **env)
 {
 	if (!env) return fail(PF_ERR_INVALID_PARAMETER, "env is NULL");
@@ -607,9 +734,16 @@ pf_status pf_env_create(int device, uint32_t flags, pf_env **env)
 	e->flags = flags;
 	cudaError_t err = cudaDeviceGetAttribute(&e->n_sm, cudaDevAttrMultiProcessorCount, device);
 	if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+	cudaDeviceProp prop{};
+	if (err == cudaSuccess) err = cudaGetDeviceProperties(&prop, device);
 	if (err != cudaSuccess) {
 		delete e;
 		return fail(PF_ERR_CUDA, std::string("pf_env_create: ") + cudaGetErrorString(err));
+	}
+	e->tune.gpu = std::string(prop.name) + "/" + std::to_string(e->n_sm) + "/" + pf_version();
+	if (const char *f = std::getenv("PF_AUTOTUNE_CACHE")) {
+		e->tune.file = f;
+		tune_load(e);
 	}
 	*env = e;
 	return PF_OK;
@@ -1485,15 +1619,44 @@ pf_status pf_batch_create_masked(pf_env *env, const pf_model_desc *models, size_
 	// batch (it loses on some small ones, e.g. one 1000 x 1000 model); the
 	// convolution methods and shapes only from 2^22 output pixels up
 	const bool tune_split = tune && fsplit < 0;
+	const uint64_t key = tune ? tune_key(env, models, n_models, profiles, n_profiles) : 0;
 	tune = tune && out_pixels >= (1ull << 22) && any_auto;
+	TuneEntry known;
+	const bool have = key && tune_lookup(env, key, &known);
 	if (!tune) {
 		pf_status s = create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool,
 		                             mask_pool_len, fixed, batch);
+		if (s == PF_OK && key) (*batch)->tune_key = key;
 		if (s == PF_OK && tune_split && (*batch)->split.box) {
-			// every convolution requested explicitly: the evaluation still timed
-			// with and without its subsampling trees split off (below)
-			const double t_split = time_eval(*batch, true), t_walk = time_eval(*batch, false);
-			if (t_walk > 0 && t_split > 0 && t_walk < t_split) release_split_pool(*batch);
+			// the evaluation timed with and without its subsampling trees split
+			// off (below), or the decision taken from the cache
+			bool walk;
+			if (have && known.split >= 0) {
+				walk = known.split == 0;
+				std::lock_guard<std::mutex> lock(env->tune.mu);
+				env->tune.reused++;
+			}
+			else {
+				const double t_split = time_eval(*batch, true), t_walk = time_eval(*batch, false);
+				walk = t_walk > 0 && t_split > 0 && t_walk < t_split;
+				tune_store(env, key, [&](TuneEntry &t) { t.split = walk ? 0 : 1; });
+			}
+			if (walk) release_split_pool(*batch);
+		}
+		return s;
+	}
+	if (have && known.fwd_shape >= 0 && known.split >= 0 && known.fft.size() == n_models) {
+		// this layout's decisions, taken before (in this environment or from its cache file)
+		ConvPlan fin;
+		fin.shape = known.fwd_shape;
+		fin.auto_fft = &known.fft;
+		fin.split = fsplit >= 0 ? fsplit == 1 : known.split == 1;
+		pf_status s = create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool,
+		                             mask_pool_len, fin, batch);
+		if (s == PF_OK) {
+			(*batch)->tune_key = key;
+			std::lock_guard<std::mutex> lock(env->tune.mu);
+			env->tune.reused++;
 		}
 		return s;
 	}
@@ -1580,8 +1743,17 @@ pf_status pf_batch_create_masked(pf_env *env, const pf_model_desc *models, size_
 	fin.shape = best_shape;
 	fin.auto_fft = &choice;
 	fin.split = split;
-	return create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool,
-	                      mask_pool_len, fin, batch);
+	if (fsplit < 0) {
+		tune_store(env, key, [&](TuneEntry &t) {
+			t.fwd_shape = best_shape;
+			t.split = split ? 1 : 0;
+			t.fft = choice;
+		});
+	}
+	s = create_planned(env, models, n_models, profiles, n_profiles, psf_pool, psf_pool_len, mask_pool, mask_pool_len,
+	                   fin, batch);
+	if (s == PF_OK) (*batch)->tune_key = key;
+	return s;
 }
 
 pf_status pf_batch_layout(const pf_batch *b, uint64_t *offsets, uint32_t *dims, uint64_t *total_pixels)
@@ -1929,22 +2101,34 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	if (!b->dbl && !(b->env->flags & PF_ENV_NO_AUTOTUNE) && b->total_out >= (1ull << 22) && tiles > 0 &&
 	    forced_conv_shape() < 0) {
 		// the autotuner, adjoint convolution: each block shape timed over the
-		// batch's directly convolved models (zero cotangents), the fastest kept
-		PF_CUDA_TRY(cudaMemsetAsync(b->d_gout, 0, sizeof(float) * std::max<uint64_t>(1, b->total_out), b->env->stream));
-		double best = -1;
+		// batch's directly convolved models (zero cotangents), the fastest kept;
+		// or the shape this layout was given before
 		int best_shape = b->adj_shape;
-		std::vector<double> t_shape(pf::conv_num_shapes<float>(), -1.);
-		for (int round = 0; round < 2; round++) {  // as for the forward shapes
-			for (int sh = 0; sh < pf::conv_num_shapes<float>(); sh++) {
-				const double ms = time_adjoint_conv(b, sh);
-				if (ms >= 0 && (t_shape[sh] < 0 || ms < t_shape[sh])) t_shape[sh] = ms;
-			}
+		TuneEntry known;
+		if (b->tune_key && tune_lookup(b->env, b->tune_key, &known) && known.adj_shape >= 0 &&
+		    known.adj_shape < pf::conv_num_shapes<float>()) {
+			best_shape = known.adj_shape;
+			std::lock_guard<std::mutex> lock(b->env->tune.mu);
+			b->env->tune.reused++;
 		}
-		for (int sh = 0; sh < pf::conv_num_shapes<float>(); sh++) {
-			if (t_shape[sh] >= 0 && (best < 0 || t_shape[sh] < best)) {
-				best = t_shape[sh];
-				best_shape = sh;
+		else {
+			PF_CUDA_TRY(cudaMemsetAsync(b->d_gout, 0, sizeof(float) * std::max<uint64_t>(1, b->total_out),
+			                            b->env->stream));
+			double best = -1;
+			std::vector<double> t_shape(pf::conv_num_shapes<float>(), -1.);
+			for (int round = 0; round < 2; round++) {  // as for the forward shapes
+				for (int sh = 0; sh < pf::conv_num_shapes<float>(); sh++) {
+					const double ms = time_adjoint_conv(b, sh);
+					if (ms >= 0 && (t_shape[sh] < 0 || ms < t_shape[sh])) t_shape[sh] = ms;
+				}
 			}
+			for (int sh = 0; sh < pf::conv_num_shapes<float>(); sh++) {
+				if (t_shape[sh] >= 0 && (best < 0 || t_shape[sh] < best)) {
+					best = t_shape[sh];
+					best_shape = sh;
+				}
+			}
+			if (b->tune_key) tune_store(b->env, b->tune_key, [&](TuneEntry &t) { t.adj_shape = best_shape; });
 		}
 		if (best_shape != b->adj_shape) {
 			long long t = 0;
