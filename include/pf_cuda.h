@@ -111,7 +111,9 @@ enum pf_convolver {
 	                       the FFT only where it at least halves the convolution's time, its
 	                       rounding being absolute, about 1e-7 x the image peak) */
 	PF_CONV_BRUTE = 1,  /* shared-memory-tiled direct convolution */
-	PF_CONV_FFT = 2     /* Stockham FFT convolution */
+	PF_CONV_FFT = 2     /* Stockham FFT convolution (a model whose transforms would exceed 8192
+	                       points per side in single precision, 4096 in double, takes the
+	                       direct convolution: the same cropped image, exactly) */
 };
 
 /* One model: Model(width, height) with its setters (include/profit/model.h:130-330). */

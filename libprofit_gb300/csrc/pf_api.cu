@@ -905,6 +905,15 @@ int best_conv_shape(const std::vector<std::pair<unsigned int, unsigned int>> &di
 	return best;
 }
 
+// Whether a single-precision direct convolution with a kw x kh PSF fits the
+// shared memory of a block in some block shape, both directions.
+static bool direct_fits(unsigned int kw, unsigned int kh)
+{
+	for (int sh = 0; sh < pf::conv_num_shapes<float>(); sh++)
+		if (pf::conv_smem<float>(kw, kh, sh) <= 227 * 1024) return true;
+	return false;
+}
+
 // PF_CONV_AUTO in single precision takes the FFT for a model only where it
 // at least halves the convolution's time: its FP32 rounding is absolute
 // (about 1e-7 x the image peak at every pixel) where the direct
@@ -959,10 +968,20 @@ pf_status plan_fft(pf_batch *b, std::vector<HostFftJob> jobs[5], const double *p
 		bool fft = false;
 		if (d.convolver == PF_CONV_FFT) {
 			if ((int)mx > nmax || (int)my > nmax) {
-				return fail(PF_ERR_UNSUPPORTED, "model " + std::to_string(i) + ": FFT size above " +
-				                                    std::to_string(nmax) + " in this precision");
+				// longer than this precision's transforms: the cropped image is the
+				// linear convolution, which the direct convolution gives (exactly,
+				// more slowly); the uncropped FFT frame has no such stand-in
+				if (d.uncropped) {
+					return fail(PF_ERR_UNSUPPORTED, "model " + std::to_string(i) + ": crop = false with an FFT "
+					                                    "above " + std::to_string(nmax) + " points in this precision");
+				}
+				continue;
 			}
 			fft = true;
+		}
+		else if (d.convolver == PF_CONV_AUTO && !b->dbl && (int)mx <= nmax && (int)my <= nmax &&
+		         !direct_fits(d.psf_w, d.psf_h)) {
+			fft = true;  // a PSF too large for the shared-memory direct convolution
 		}
 		else if (d.convolver == PF_CONV_AUTO && !b->dbl && (int)mx <= nmax && (int)my <= nmax && plan.auto_fft) {
 			fft = (*plan.auto_fft)[i] != 0;
@@ -1192,23 +1211,34 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		}
 		b->fwd_shape = plan.shape >= 0 ? plan.shape : best_conv_shape<float>(conv_dims);
 		if (forced_conv_shape() >= 0) b->fwd_shape = forced_conv_shape();
+		for (size_t i = 0; i < n_models; i++) {
+			const pf::ModelDev &d = b->mdev[i];
+			if (!d.use_fft && d.conv_required) {
+				max_kw = std::max(max_kw, d.psf_w);
+				max_kh = std::max(max_kh, d.psf_h);
+			}
+		}
+		if (pf::conv_smem<float>(max_kw, max_kh, b->fwd_shape) > 227 * 1024 && forced_conv_shape() < 0) {
+			// the chosen block shape's patch too large for this PSF: the first one that fits
+			for (int sh = 0; sh < pf::conv_num_shapes<float>(); sh++) {
+				if (pf::conv_smem<float>(max_kw, max_kh, sh) <= 227 * 1024) {
+					b->fwd_shape = sh;
+					break;
+				}
+			}
+		}
 		long long t = 0;
 		for (size_t i = 0; i < n_models; i++) {
 			const pf::ModelDev &d = b->mdev[i];
 			tile_base_out[i] = t;
-			if (!d.use_fft) {  // models convolved by FFT are finished by its last pass
-				t += pf::conv_tiles<float>(d.crop_w, d.crop_h, b->fwd_shape);
-				if (d.conv_required) {
-					max_kw = std::max(max_kw, d.psf_w);
-					max_kh = std::max(max_kh, d.psf_h);
-				}
-			}
+			if (!d.use_fft) t += pf::conv_tiles<float>(d.crop_w, d.crop_h, b->fwd_shape);  // FFT models: their last pass
 			b->any_downsample |= d.fs > 1 && !d.return_fs;
 		}
 		b->n_out_tiles = t;
 		b->finish_smem = pf::conv_smem<float>(max_kw, max_kh, b->fwd_shape);
 		if (b->finish_smem > 227 * 1024) {
-			return fail(PF_ERR_UNSUPPORTED, "PSF too large for the shared-memory direct convolution");
+			return fail(PF_ERR_UNSUPPORTED, "PSF too large for the single-precision direct convolution's shared "
+			                                "memory: request the FFT convolver or double precision");
 		}
 	}
 
@@ -2055,6 +2085,21 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	}
 	b->adj_shape = b->dbl ? best_conv_shape<double>(conv_dims) : best_conv_shape<float>(conv_dims);
 	if (!b->dbl && forced_conv_shape() >= 0) b->adj_shape = forced_conv_shape();
+	for (const auto &m : b->mdev) {
+		if (m.conv_required && (b->dbl || !m.use_fft)) {
+			max_kw = std::max(max_kw, m.psf_w);
+			max_kh = std::max(max_kh, m.psf_h);
+		}
+	}
+	if (!b->dbl && pf::conv_smem<float>(max_kw, max_kh, b->adj_shape) > 227 * 1024 && forced_conv_shape() < 0) {
+		// the chosen block shape's patch too large for this PSF: the first one that fits
+		for (int sh = 0; sh < pf::conv_num_shapes<float>(); sh++) {
+			if (pf::conv_smem<float>(max_kw, max_kh, sh) <= 227 * 1024) {
+				b->adj_shape = sh;
+				break;
+			}
+		}
+	}
 	for (size_t i = 0; i < n_models; i++) {
 		const pf::ModelDev &m = b->mdev[i];
 		for (int q = 0; q < m.n_profiles; q++) {
@@ -2066,8 +2111,6 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 		if (m.conv_required && (b->dbl || !m.use_fft)) {
 			tiles += b->dbl ? pf::conv_tiles<double>(m.draw_w, m.draw_h, b->adj_shape)
 			                : pf::conv_tiles<float>(m.draw_w, m.draw_h, b->adj_shape);
-			max_kw = std::max(max_kw, m.psf_w);
-			max_kh = std::max(max_kh, m.psf_h);
 		}
 	}
 	if (pf::backward_items((long long)std::max<size_t>(1, b->profiles.size()), 2ll * max_h) >= (1ll << 31)) {

@@ -153,3 +153,61 @@ def test_block_shapes_covered():
     if len(_SHAPES) == 0:
         pytest.skip("runs after the shape cases")
     assert {0, 1, 2, 4} <= _SHAPES, _SHAPES
+
+
+def test_large_psf_takes_a_block_shape_that_fits(envs):
+    """A 121 x 121 PSF: the least-area block shape's patch does not fit in
+    shared memory, a smaller one does and is taken, forward and adjoint; the
+    image against the FP64 path, the gradients against the same model's FFT
+    convolution."""
+    import torch
+    import libprofit_gb300 as pg
+    import workloads as W
+    env64, env32 = envs
+    w, h = 256, 256
+    psf = W.moffat_psf(121, 4.0, 2.5)
+    profiles = _profiles(w, h)
+
+    def run(env, conv, dt):
+        m = W.to_model(dict(width=w, height=h, psf=psf, profiles=profiles), env)
+        m.set_convolver(conv)
+        b = pg.Batch([m], env)
+        img = torch.zeros(b.total_pixels, dtype=dt, device="cuda")
+        b.forward(img)
+        b.check()
+        out = img.cpu().numpy().astype(np.float64).reshape(h, w)
+        g = None
+        if dt == torch.float32:
+            b.enable_adjoint()
+            y, x = np.mgrid[0:h, 0:w]
+            cot = torch.tensor((1.0 + 0.5 * np.sin(x / 7.0) * np.cos(y / 5.0)).ravel(), dtype=dt, device="cuda")
+            grad = torch.zeros(len(profiles) * 12, dtype=torch.float64, device="cuda")
+            b.backward(img, cotangent=cot, grad=grad)
+            b.check()
+            g = grad.cpu().numpy()
+        return out, g, b.conv_info()
+
+    ref, _, _ = run(env64, "brute", torch.float64)
+    img, g, info = run(env32, "brute", torch.float32)
+    assert info["fft_models"] == 0
+    assert abs(img.sum() - ref.sum()) <= 1e-5 * abs(ref.sum())
+    peak = np.abs(ref).max()
+    bright = np.abs(ref) > 1e-3 * peak
+    assert np.max(np.abs(img[bright] - ref[bright]) / np.abs(ref[bright])) <= 1e-4
+    _, gf, _ = run(env32, "fft", torch.float32)
+    scale = np.abs(gf).max()
+    assert np.all(np.abs(g - gf) <= 1e-4 * np.abs(gf) + 1e-6 * scale)
+
+
+def test_psf_beyond_direct_takes_fft_automatically(envs):
+    """A 181 x 181 PSF fits no direct block shape's shared memory: the
+    automatic choice takes the FFT whatever the cost model says; the image
+    against the FP64 path (direct) at the FFT's bars."""
+    import workloads as W
+    env64, env32 = envs
+    spec = dict(width=200, height=180, psf=W.moffat_psf(181, 5.0, 2.5), profiles=_profiles(200, 180))
+    ref = W.to_model(dict(spec, convolver="brute"), env64).evaluate()
+    img = W.to_model(dict(spec, convolver="auto"), env32).evaluate()
+    assert abs(img.sum() - ref.sum()) <= 1e-5 * abs(ref.sum())
+    peak = np.abs(ref).max()
+    assert np.max(np.abs(img - ref)) <= 2e-6 * peak

@@ -121,3 +121,19 @@ def test_large_psf_auto_fft(envs):
     img = W.to_model(spec, env32).evaluate()
     assert abs(img.sum() - ref.sum()) <= 1e-5 * abs(ref.sum())
     _check(img, ref, 2e-6, 1e-4)
+
+
+@pytest.mark.parametrize("use_double,width", [(True, 4100), (False, 8190)])
+def test_fft_longer_than_transforms_takes_direct(envs, use_double, width):
+    """A model whose FFT would exceed the longest transform (4096 points per
+    side in double precision, 8192 in single) is convolved directly: the
+    same cropped image as requesting the direct convolution, bit for bit."""
+    import workloads as W
+    env = envs[0] if use_double else envs[1]
+    spec = dict(width=width, height=40, psf=W.moffat_psf(15, 3.0, 2.5), profiles=[
+        ("sersic", dict(xcen=0.3 * width, ycen=20.0, mag=15.0, re=12.0, nser=2.0, ang=20.0, axrat=0.6, box=0.0,
+                        convolve=True))])
+    a = W.to_model(dict(spec, convolver="fft"), env).evaluate()
+    b = W.to_model(dict(spec, convolver="brute"), env).evaluate()
+    assert np.array_equal(a, b)
+    assert a.max() > 0
