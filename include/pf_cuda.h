@@ -108,7 +108,7 @@ typedef struct pf_profile_desc {
 
 enum pf_convolver {
 	PF_CONV_AUTO = 0,   /* autotuner choice (direct for the double mode; in single precision
-	                       the FFT only where it at least halves the convolution's time, its
+	                       the FFT only where it cuts the convolution's time fourfold, its
 	                       rounding being absolute, about 1e-7 x the image peak) */
 	PF_CONV_BRUTE = 1,  /* shared-memory-tiled direct convolution */
 	PF_CONV_FFT = 2     /* Stockham FFT convolution (a model whose transforms would exceed 8192

@@ -255,9 +255,18 @@ __host__ __device__ constexpr int row_ffts() { return (N / 8) >= 256 ? 1 : 256 /
 #ifndef PF_FFT_COL_MINB
 #define PF_FFT_COL_MINB 2
 #endif
+// Lengths whose column pass runs as warp transforms (cols_w_kernel): N = 32 P
+// with P points per lane, P one of the register DFTs' sizes.
+template <int N>
+__host__ __device__ constexpr bool warp_cols()
+{
+	return N == 64 || N == 96 || N == 128 || N == 160 || N == 256 || N == 288 || N == 512;
+}
+
 template <int N>
 __host__ __device__ constexpr int col_ffts()
 {
+	if (warp_cols<N>()) return 8;  // one warp per bin column, 8 per block
 	return PF_FFT_COL_THREADS / (N / 8) < 1 ? 1 : PF_FFT_COL_THREADS / (N / 8) > 16 ? 16 : PF_FFT_COL_THREADS / (N / 8);
 }
 template <int N>
@@ -332,7 +341,7 @@ rows_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, c
 	__syncthreads();
 	fft<N, false>(buf + f * PS, t, table);
 	// unpack: A(k) = (Z(k) + conj Z(N-k)) / 2, B(k) = (Z(k) - conj Z(N-k)) / (2 i)
-	float2 *dst = MODE == F_SPECTRUM ? spec + m.fft_spec_off : work + m.fft_work_off;
+	float2 *dst = work + m.fft_work_off;  // the PSF's row spectra too: the column pass writes the spectrum
 	const int nbr = (int)m.fft_mx / 2 + 1;  // = NB
 	for (int i = threadIdx.x; i < F * NB; i += blockDim.x) {
 		const int ff = i / NB, k = i % NB;
@@ -359,7 +368,7 @@ cols_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, f
 	const ModelDev &m = models[jb.model];
 	const int nb = (int)m.fft_mx / 2 + 1;
 	const int f = threadIdx.x / (N / 8), t = threadIdx.x % (N / 8);
-	float2 *col = MODE == F_SPECTRUM ? spec + m.fft_spec_off : work + m.fft_work_off;
+	float2 *col = work + m.fft_work_off;
 	// rows present in the input and their place in the transform
 	int rows_in, yoff = 0;
 	if (MODE == F_FORWARD) rows_in = (int)m.draw_h;
@@ -387,9 +396,10 @@ cols_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, f
 	__syncthreads();
 	fft<N, false>(cbuf + f * PS, t, table);
 	if (MODE == F_SPECTRUM) {
+		float2 *sp_out = spec + m.fft_spec_off;
 		for (int i = threadIdx.x; i < F * N; i += blockDim.x) {
 			const int rg = i / F, ff = i % F;
-			if (ff < jb.count) col[(size_t)rg * nb + jb.first + ff] = cbuf[ff * PS + pidx(rg)];
+			if (ff < jb.count) sp_out[(size_t)rg * nb + jb.first + ff] = cbuf[ff * PS + pidx(rg)];
 		}
 		return;
 	}
@@ -418,6 +428,198 @@ cols_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, f
 	for (int i = threadIdx.x; i < F * rows_out; i += blockDim.x) {
 		const int r = i / F, ff = i % F;
 		if (ff < jb.count) col[(size_t)r * nb + jb.first + ff] = cbuf[ff * PS + pidx(r + keep)];
+	}
+}
+
+// ---- the column pass as warp transforms (lengths N = 32 P, warp_cols<N>())
+//
+// One warp per bin column, lane l holding points l + 32 p (p < P). With
+// n = 32 n1 + n2 and k = k1 + P k2 (Cooley-Tukey, N = P x 32):
+//   forward  a P-point DFT in registers over n1, the twiddle W_N^(l k1), and
+//            a 32-point decimation-in-frequency DFT across the lanes (shuffles),
+//            which leaves X[k1 + P bitrev5(l)] in lane l's k1-th register;
+//   product  with the PSF spectrum stored in that same order (the spectrum pass
+//            runs the same forward transform), so no permutation is needed;
+//   inverse  the lane network undone stage by stage, the conjugate twiddle and
+//            the inverse register DFT: back to natural order, unnormalised.
+
+// exp(-2 pi i m / P) (forward; conjugated for the inverse) for the register
+// DFTs of 9 and 16 points, m < 10
+template <int P, bool INV>
+__device__ __forceinline__ float2 small_twiddle(int m)
+{
+	constexpr float c9[5] = {1.f, 0.76604444311897804f, 0.17364817766693035f, -0.5f, -0.93969262078590838f};
+	constexpr float s9[5] = {0.f, 0.64278760968653933f, 0.98480775301220802f, 0.86602540378443865f,
+	                         0.34202014332566873f};
+	constexpr float c16[10] = {1.f, 0.92387953251128674f, 0.70710678118654752f, 0.38268343236508978f, 0.f,
+	                           -0.38268343236508978f, -0.70710678118654752f, -0.92387953251128674f, -1.f,
+	                           -0.92387953251128674f};
+	constexpr float s16[10] = {0.f, 0.38268343236508978f, 0.70710678118654752f, 0.92387953251128674f, 1.f,
+	                           0.92387953251128674f, 0.70710678118654752f, 0.38268343236508978f, 0.f,
+	                           -0.38268343236508978f};
+	const float c = P == 9 ? c9[m] : c16[m], sn = P == 9 ? s9[m] : s16[m];
+	return make_float2(c, INV ? sn : -sn);
+}
+
+// A B-point DFT in registers, natural order in and out (Cooley-Tukey A x B):
+// A-point DFTs of the stride-B subsequences, twiddles W_(AB)^(n2 k1), B-point
+// DFTs across them.
+template <int A, int B, bool INV>
+__device__ __forceinline__ void dft_ct(float2 *v)
+{
+	constexpr int P = A * B;
+	float2 y[P];
+#pragma unroll
+	for (int n2 = 0; n2 < B; n2++) {
+		float2 t[A];
+#pragma unroll
+		for (int n1 = 0; n1 < A; n1++) t[n1] = v[B * n1 + n2];
+		dft<A, INV>(t);
+#pragma unroll
+		for (int k1 = 0; k1 < A; k1++) y[n2 * A + k1] = n2 * k1 ? cmulf(t[k1], small_twiddle<P, INV>(n2 * k1)) : t[k1];
+	}
+#pragma unroll
+	for (int k1 = 0; k1 < A; k1++) {
+		float2 t[B];
+#pragma unroll
+		for (int n2 = 0; n2 < B; n2++) t[n2] = y[n2 * A + k1];
+		dft<B, INV>(t);
+#pragma unroll
+		for (int k2 = 0; k2 < B; k2++) v[k1 + A * k2] = t[k2];
+	}
+}
+
+template <int P, bool INV>
+__device__ __forceinline__ void dft_reg(float2 *v)
+{
+	if constexpr (P == 9) dft_ct<3, 3, INV>(v);
+	else if constexpr (P == 16) dft_ct<4, 4, INV>(v);
+	else dft<P, INV>(v);
+}
+
+__device__ __forceinline__ float2 shfl_xor2(float2 v, int m)
+{
+	return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+
+// forward: v[p] = x[lane + 32 p] in, X[k1 + P bitrev5(lane)] in v[k1] out
+template <int N>
+__device__ __forceinline__ void warp_fft_forward(float2 (&v)[N / 32], int lane, const float2 *__restrict__ table)
+{
+	constexpr int P = N / 32;
+	dft_reg<P, false>(v);
+#pragma unroll
+	for (int k1 = 1; k1 < P; k1++) v[k1] = cmulf(v[k1], twiddle<false>(table, tw_offset(N) + lane * k1));
+#pragma unroll
+	for (int h = 16; h >= 1; h >>= 1) {
+		const bool upper = lane & h;
+		const float2 w = twiddle<false>(table, tw_offset(N) + (lane & (h - 1)) * (N / (2 * h)));
+#pragma unroll
+		for (int k1 = 0; k1 < P; k1++) {
+			const float2 o = shfl_xor2(v[k1], h);
+			v[k1] = upper ? cmulf(csubf(o, v[k1]), w) : caddf(v[k1], o);
+		}
+	}
+}
+
+// inverse of warp_fft_forward times N (the unnormalised inverse DFT)
+template <int N>
+__device__ __forceinline__ void warp_fft_inverse(float2 (&v)[N / 32], int lane, const float2 *__restrict__ table)
+{
+	constexpr int P = N / 32;
+#pragma unroll
+	for (int h = 1; h <= 16; h <<= 1) {
+		const bool upper = lane & h;
+		const float2 w = twiddle<true>(table, tw_offset(N) + (lane & (h - 1)) * (N / (2 * h)));
+#pragma unroll
+		for (int k1 = 0; k1 < P; k1++) {
+			const float2 o = shfl_xor2(v[k1], h);
+			// lower lane: its own sum term, the partner's difference term; upper: the reverse
+			const float2 t = cmulf(upper ? v[k1] : o, w);
+			v[k1] = upper ? csubf(o, t) : caddf(v[k1], t);
+		}
+	}
+#pragma unroll
+	for (int k1 = 1; k1 < P; k1++) v[k1] = cmulf(v[k1], twiddle<true>(table, tw_offset(N) + lane * k1));
+	dft_reg<P, true>(v);
+}
+
+// Pass 2 for warp_cols<N>() lengths: 8 bin columns per block, one per warp.
+// The spectrum pass (F_SPECTRUM) stores its columns' transforms in the
+// warps' own order (column c at spec[c N + 32 k1 + lane]).
+template <int N, int MODE>
+__global__ void __launch_bounds__(256)
+cols_w_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, float2 *__restrict__ work,
+              float2 *__restrict__ spec, const float2 *__restrict__ table)
+{
+	constexpr int F = 8, P = N / 32, PS = N + 1;
+	extern __shared__ float2 fsm[];
+	float2 *cbuf = fsm;
+	const Job jb = jobs[blockIdx.x];
+	const ModelDev &m = models[jb.model];
+	const int nb = (int)m.fft_mx / 2 + 1;
+	const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+	float2 *col = work + m.fft_work_off;
+	int rows_in, yoff = 0;
+	if (MODE == F_FORWARD) rows_in = (int)m.draw_h;
+	else if (MODE == F_ADJOINT) {
+		rows_in = (int)m.crop_h;
+		yoff = (int)m.pad_y + (int)m.psf_h - 1 - (int)m.psf_h / 2;
+	}
+	else rows_in = (int)m.psf_h;
+	// coalesced loads of the job's columns (F x 8 bytes per row), P per thread,
+	// all issued before the shared-memory stores
+	float2 v[P];
+#pragma unroll
+	for (int q = 0; q < P; q++) {
+		const int i = (int)threadIdx.x + q * 256;
+		const int rg = i / F, ff = i % F;
+		const int r = rg - yoff;
+		v[q] = make_float2(0.f, 0.f);
+		if (ff < jb.count && r >= 0 && r < rows_in) v[q] = col[(size_t)r * nb + jb.first + ff];
+	}
+#pragma unroll
+	for (int q = 0; q < P; q++) {
+		const int i = (int)threadIdx.x + q * 256;
+		cbuf[(i % F) * PS + i / F] = v[q];
+	}
+	__syncthreads();
+	const bool live = warp < jb.count;
+	const int c = jb.first + warp;
+	float2 x[P];
+#pragma unroll
+	for (int p = 0; p < P; p++) x[p] = cbuf[warp * PS + lane + 32 * p];
+	warp_fft_forward<N>(x, lane, table);
+	if (MODE == F_SPECTRUM) {
+		if (live) {
+			float2 *sp = spec + m.fft_spec_off + (size_t)c * N;
+#pragma unroll
+			for (int k1 = 0; k1 < P; k1++) sp[32 * k1 + lane] = x[k1];
+		}
+		return;
+	}
+	if (live) {
+		const float2 *sp = spec + m.fft_spec_off + (size_t)c * N;
+		float2 sv[P];
+#pragma unroll
+		for (int k1 = 0; k1 < P; k1++) sv[k1] = sp[32 * k1 + lane];
+#pragma unroll
+		for (int k1 = 0; k1 < P; k1++) {
+			if (MODE == F_ADJOINT) sv[k1].y = -sv[k1].y;
+			x[k1] = cmulf(x[k1], sv[k1]);
+		}
+	}
+	warp_fft_inverse<N>(x, lane, table);
+#pragma unroll
+	for (int p = 0; p < P; p++) cbuf[warp * PS + lane + 32 * p] = x[p];
+	__syncthreads();
+	// kept rows: forward, the crop's (from its offset); adjoint, the drawing area's
+	const int rows_out = MODE == F_FORWARD ? (int)m.crop_h : (int)m.draw_h;
+	const int keep = MODE == F_FORWARD ? (int)m.pad_y + (int)m.psf_h - 1 - (int)m.psf_h / 2 : 0;
+#pragma unroll 4
+	for (int i = threadIdx.x; i < F * rows_out; i += blockDim.x) {
+		const int r = i / F, ff = i % F;
+		if (ff < jb.count) col[(size_t)r * nb + jb.first + ff] = cbuf[ff * PS + r + keep];
 	}
 }
 
@@ -498,7 +700,10 @@ irows_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, 
 template <int N>
 constexpr size_t rows_smem() { return sizeof(float2) * row_ffts<N>() * row_stride<N>(); }
 template <int N>
-constexpr size_t cols_smem() { return sizeof(float2) * col_ffts<N>() * col_stride<N>(); }
+constexpr size_t cols_smem()
+{
+	return warp_cols<N>() ? sizeof(float2) * 8 * (N + 1) : sizeof(float2) * col_ffts<N>() * col_stride<N>();
+}
 
 template <int N>
 cudaError_t configure_n()
@@ -510,9 +715,16 @@ cudaError_t configure_n()
 	if (e == cudaSuccess) e = cudaFuncSetAttribute(rows_kernel<N, F_SPECTRUM>, a, rs);
 	if (e == cudaSuccess) e = cudaFuncSetAttribute(irows_kernel<N, F_FORWARD>, a, rs);
 	if (e == cudaSuccess) e = cudaFuncSetAttribute(irows_kernel<N, F_ADJOINT>, a, rs);
-	if (e == cudaSuccess) e = cudaFuncSetAttribute(cols_kernel<N, F_FORWARD>, a, cs);
-	if (e == cudaSuccess) e = cudaFuncSetAttribute(cols_kernel<N, F_ADJOINT>, a, cs);
-	if (e == cudaSuccess) e = cudaFuncSetAttribute(cols_kernel<N, F_SPECTRUM>, a, cs);
+	if constexpr (warp_cols<N>()) {
+		if (e == cudaSuccess) e = cudaFuncSetAttribute(cols_w_kernel<N, F_FORWARD>, a, cs);
+		if (e == cudaSuccess) e = cudaFuncSetAttribute(cols_w_kernel<N, F_ADJOINT>, a, cs);
+		if (e == cudaSuccess) e = cudaFuncSetAttribute(cols_w_kernel<N, F_SPECTRUM>, a, cs);
+	}
+	else {
+		if (e == cudaSuccess) e = cudaFuncSetAttribute(cols_kernel<N, F_FORWARD>, a, cs);
+		if (e == cudaSuccess) e = cudaFuncSetAttribute(cols_kernel<N, F_ADJOINT>, a, cs);
+		if (e == cudaSuccess) e = cudaFuncSetAttribute(cols_kernel<N, F_SPECTRUM>, a, cs);
+	}
 	return e;
 }
 
@@ -529,9 +741,16 @@ void launch_n(int pass, int mode, int n_jobs, const ModelDev *models, const Job 
 		else rows_kernel<N, F_SPECTRUM><<<n_jobs, rthreads, rsmem, stream>>>(models, jobs, src, psf, work, spec, tw);
 	}
 	else if (pass == 1) {
-		if (mode == F_FORWARD) cols_kernel<N, F_FORWARD><<<n_jobs, cthreads, csmem, stream>>>(models, jobs, work, spec, tw);
-		else if (mode == F_ADJOINT) cols_kernel<N, F_ADJOINT><<<n_jobs, cthreads, csmem, stream>>>(models, jobs, work, spec, tw);
-		else cols_kernel<N, F_SPECTRUM><<<n_jobs, cthreads, csmem, stream>>>(models, jobs, work, spec, tw);
+		if constexpr (warp_cols<N>()) {
+			if (mode == F_FORWARD) cols_w_kernel<N, F_FORWARD><<<n_jobs, 256, csmem, stream>>>(models, jobs, work, spec, tw);
+			else if (mode == F_ADJOINT) cols_w_kernel<N, F_ADJOINT><<<n_jobs, 256, csmem, stream>>>(models, jobs, work, spec, tw);
+			else cols_w_kernel<N, F_SPECTRUM><<<n_jobs, 256, csmem, stream>>>(models, jobs, work, spec, tw);
+		}
+		else {
+			if (mode == F_FORWARD) cols_kernel<N, F_FORWARD><<<n_jobs, cthreads, csmem, stream>>>(models, jobs, work, spec, tw);
+			else if (mode == F_ADJOINT) cols_kernel<N, F_ADJOINT><<<n_jobs, cthreads, csmem, stream>>>(models, jobs, work, spec, tw);
+			else cols_kernel<N, F_SPECTRUM><<<n_jobs, cthreads, csmem, stream>>>(models, jobs, work, spec, tw);
+		}
 	}
 	else {
 		if (mode == F_FORWARD) irows_kernel<N, F_FORWARD><<<n_jobs, rthreads, rsmem, stream>>>(models, jobs, work, direct, out, tw);

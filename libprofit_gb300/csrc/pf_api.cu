@@ -915,11 +915,12 @@ static bool direct_fits(unsigned int kw, unsigned int kh)
 }
 
 // PF_CONV_AUTO in single precision takes the FFT for a model only where it
-// at least halves the convolution's time: its FP32 rounding is absolute
-// (about 1e-7 x the image peak at every pixel) where the direct
-// convolution's is relative, which faint pixels and the gradients they carry
-// feel; PF_CONV_FFT takes it regardless.
-constexpr double kFftGain = 0.5;
+// cuts the convolution's time at least fourfold (large PSFs): its FP32
+// rounding is absolute (about 1e-7 x the image peak at every pixel) where the
+// direct convolution's is relative, which faint pixels and the gradients
+// they carry feel; PF_CONV_FFT takes it regardless. (The bench workload's
+// 25 x 25 PSF: FFT 1.06 against 2.24 ms, kept direct.)
+constexpr double kFftGain = 0.25;
 
 unsigned int next_pow2(unsigned int v)
 {
