@@ -638,28 +638,29 @@ irows_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, 
 	const int nb = (int)m.fft_mx / 2 + 1;
 	const int f = threadIdx.x / (N / 8), t = threadIdx.x % (N / 8);
 	const float2 *src = work + m.fft_work_off;
-	// the block has F * N / 8 threads: eight points each, all loads issued
-	// before the shared-memory stores
-	float2 a[8], b[8];
+	// each stored bin k <= N/2 of the two rows loaded once (all loads issued
+	// before the shared-memory stores), Z(k) = A(k) + i B(k) written at k and,
+	// from A(N-k) = conj A(k), B(N-k) = conj B(k), at N - k
+	constexpr int NB = N / 2 + 1, T = F * (N / 8), Q = (F * NB + T - 1) / T;
+	float2 a[Q], b[Q];
 #pragma unroll
-	for (int q = 0; q < 8; q++) {
-		const int i = (int)threadIdx.x + q * (F * (N / 8));
-		const int ff = i / N, k = i % N;
+	for (int q = 0; q < Q; q++) {
+		const int i = (int)threadIdx.x + q * T;
+		const int ff = i / NB, k = i % NB;
 		const int r0 = jb.first + 2 * ff, r1 = r0 + 1;
-		const int kk = k <= N / 2 ? k : N - k;
 		a[q] = b[q] = make_float2(0.f, 0.f);
-		if (r0 < jb.first + jb.count) a[q] = src[(size_t)r0 * nb + kk];
-		if (r1 < jb.first + jb.count) b[q] = src[(size_t)r1 * nb + kk];
+		if (i < F * NB) {
+			if (r0 < jb.first + jb.count) a[q] = src[(size_t)r0 * nb + k];
+			if (r1 < jb.first + jb.count) b[q] = src[(size_t)r1 * nb + k];
+		}
 	}
 #pragma unroll
-	for (int q = 0; q < 8; q++) {
-		const int i = (int)threadIdx.x + q * (F * (N / 8));
-		const int ff = i / N, k = i % N;
-		if (k > N / 2) {
-			a[q].y = -a[q].y;
-			b[q].y = -b[q].y;
-		}
+	for (int q = 0; q < Q; q++) {
+		const int i = (int)threadIdx.x + q * T;
+		if (i >= F * NB) continue;
+		const int ff = i / NB, k = i % NB;
 		buf[ff * PS + pidx(k)] = make_float2(a[q].x - b[q].y, a[q].y + b[q].x);
+		if (k > 0 && k < N - k) buf[ff * PS + pidx(N - k)] = make_float2(a[q].x + b[q].y, b[q].x - a[q].y);
 	}
 	__syncthreads();
 	fft<N, true>(buf + f * PS, t, table);
