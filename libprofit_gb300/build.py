@@ -2,7 +2,8 @@
 include/pf_cuda.h, for sm_103a only.
 
 Each translation unit is compiled in parallel with nvcc; the ones that must
-keep the reference's FP64 arithmetic (no fused multiply-add) get -fmad=false.
+round alike wherever they are inlined (the reference's FP64 arithmetic, the
+single-precision evaluation) get -fmad=false.
 Objects go to libprofit_gb300/_build/, the library next to this file. The
 build is skipped when the library is newer than every source.
 """
@@ -23,8 +24,12 @@ CLI = os.path.join(HERE, "profit-cli")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
           "-I" + os.path.join(ROOT, "include")]
-# translation units that reproduce the reference's double-precision arithmetic
-NO_FMAD = {"setup.cu", "eval_f64.cu"}
+# translation units built without the compiler's multiply-add contraction:
+# the two that reproduce the reference's double-precision arithmetic, and the
+# single-precision evaluation, whose multiply-adds are explicit fmaf calls so
+# that every kernel instance rounds alike (its FP64 re-takes then round as the
+# double-precision path does)
+NO_FMAD = {"setup.cu", "eval_f64.cu", "eval_f32.cu"}
 
 
 def nvcc():

@@ -131,25 +131,60 @@ __device__ __forceinline__ void warp_store_slots(const T *v, int lane, D *dst)
 // ------------------------------------------------------------ chi^2, g_out
 
 // Block (model, c) of gridDim.y = `parts` blocks per model takes the model's
-// output pixels [c * chunk, (c + 1) * chunk). With one block per model it
-// writes chi2[model] itself; with several, each writes its FP64 partial and
-// the last block of the model to finish (a per-model counter, reset by that
-// block) adds the partials in block order, so the result does not depend on
-// the blocks' timing.
+// output pixels [c * chunk, (c + 1) * chunk), chunk a multiple of 4. With one
+// block per model it writes chi2[model] itself; with several, each writes its
+// FP64 partial and the last block of the model to finish (a per-model counter,
+// reset by that block) adds the partials in block order, so the result does
+// not depend on the blocks' timing. `vec`: every buffer starts on a 16-byte
+// boundary, so that single-precision models whose pixels do too (and that have
+// no final mask) are read and written four pixels at a time (16-byte
+// accesses: twice the bytes in flight of one pixel per thread, which left the
+// pass at about 3 TB/s).
 template <typename T>
 __global__ void chi2_kernel(const ModelDev *__restrict__ models, const T *__restrict__ img, const T *__restrict__ data,
                             const T *__restrict__ sigma, const T *__restrict__ cot, T *__restrict__ gout,
-                            double *__restrict__ chi2, double *__restrict__ partial, unsigned int *__restrict__ done)
+                            double *__restrict__ chi2, double *__restrict__ partial, unsigned int *__restrict__ done,
+                            bool vec)
 {
 	const ModelDev &m = models[blockIdx.x];
 	const long long n = (long long)m.out_w * m.out_h;
 	const int parts = gridDim.y;
-	const long long chunk = (n + parts - 1) / parts;
-	const long long i0 = (long long)blockIdx.y * chunk, i1 = min(n, i0 + chunk);
+	const long long chunk = ((n + parts - 1) / parts + 3) & ~3ll;
+	const long long i0 = min(n, (long long)blockIdx.y * chunk), i1 = min(n, i0 + chunk);
 	// per thread: a compensated (Kahan) sum in T, so that single precision
 	// costs no FP64 work per pixel; across threads: FP64
 	T s = 0, comp = 0;
-	for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+	long long first = i0;  // the pixels from here on go one at a time
+	if constexpr (std::is_same<T, float>::value) {
+		if (vec && !cot && !m.mask_final && (m.out_off & 3) == 0) {
+			const long long nq = (i1 - i0) >> 2;
+			const long long g0 = (m.out_off + i0) >> 2;
+			const float4 *img4 = reinterpret_cast<const float4 *>(img) + g0;
+			const float4 *data4 = reinterpret_cast<const float4 *>(data) + g0;
+			const float4 *sig4 = sigma ? reinterpret_cast<const float4 *>(sigma) + g0 : nullptr;
+			float4 *gout4 = reinterpret_cast<float4 *>(gout) + g0;
+			for (long long q = threadIdx.x; q < nq; q += blockDim.x) {
+				const float4 a = img4[q], d = data4[q];
+				const float4 sg = sig4 ? sig4[q] : make_float4(1.f, 1.f, 1.f, 1.f);
+				const float av[4] = {a.x, a.y, a.z, a.w}, dv[4] = {d.x, d.y, d.z, d.w};
+				const float sv[4] = {sg.x, sg.y, sg.z, sg.w};
+				float gv[4];
+#pragma unroll
+				for (int k = 0; k < 4; k++) {
+					const float r = av[k] - dv[k];
+					const float wr = (sig4 ? 1.f / (sv[k] * sv[k]) : 1.f) * r;
+					const float y = wr * r - comp;
+					const float t = s + y;
+					comp = (t - s) - y;
+					s = t;
+					gv[k] = 2.f * wr;
+				}
+				gout4[q] = make_float4(gv[0], gv[1], gv[2], gv[3]);
+			}
+			first = i0 + 4 * nq;
+		}
+	}
+	for (long long i = first + threadIdx.x; i < i1; i += blockDim.x) {
 		const long long g = m.out_off + i;
 		// output pixels the final masking zeroes do not depend on the parameters
 		const bool live = !m.mask_final || kept(m, (int)(i % m.out_w), (int)(i / m.out_w));
@@ -940,8 +975,11 @@ void launch_chi2(const ModelDev *models, int n_models, const void *img, const vo
                  cudaStream_t stream)
 {
 	if (n_models <= 0) return;
+	const auto a16 = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
+	const bool vec = a16(img) && a16(data) && a16(sigma) && a16(gout);
 	chi2_kernel<T><<<dim3((unsigned int)n_models, (unsigned int)parts), 256, 0, stream>>>(
-	    models, (const T *)img, (const T *)data, (const T *)sigma, (const T *)cot, (T *)gout, chi2, partial, done);
+	    models, (const T *)img, (const T *)data, (const T *)sigma, (const T *)cot, (T *)gout, chi2, partial, done,
+	    vec);
 }
 
 

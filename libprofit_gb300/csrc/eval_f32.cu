@@ -31,14 +31,15 @@ namespace pf {
 namespace {
 
 // Warps per block and blocks per SM the register allocation is sized for: 4
-// and 5, 96 registers and 20 warps per SM (the kernel is latency-bound;
-// measured on the 1024-model step: 3.10 ms at 16 warps and 128 registers,
-// 2.95 ms at 20 warps with 148 bytes of spills on cold paths).
+// and 4, 128 registers and 16 warps per SM (measured on the 1024-model step
+// with the row segments below: 2.41 ms, against 2.82 ms at 20 warps and 96
+// registers, whose spills fall in the subsampling walk, and 3.21 ms at 24
+// warps).
 #ifndef PF_EVAL32_WARPS
 #define PF_EVAL32_WARPS 4
 #endif
 #ifndef PF_EVAL32_MIN_BLOCKS
-#define PF_EVAL32_MIN_BLOCKS 5
+#define PF_EVAL32_MIN_BLOCKS 4
 #endif
 // phase-A (ring tile) items a warp claims at once (a divisor of 32; 32, 8
 // and 2 measured within 5 % of each other on the 1024-model step)
@@ -83,7 +84,7 @@ __device__ __forceinline__ void corner_pair(float i, float s_hi, float s_lo, flo
                                             float &lo)
 {
 	const float p = i * s_hi;
-	const float ep = fmaf(i, s_hi, -p) + i * s_lo;
+	const float ep = fmaf(i, s_lo, fmaf(i, s_hi, -p));
 	float e;
 	two_sum(p, -c_hi, hi, e);
 	lo = (e + ep) - c_lo;
@@ -182,7 +183,7 @@ __device__ void eval_frame_m(const ProfileDev &P, const f32::Shape &sh, WarpScra
 	const bool recurse = res > 1 && (unsigned int)L < max_rec;
 	const unsigned int n = res * res;
 	const float c = sh.cs, s = sh.sn, iq = sh.iq, facc = sh.acc;
-	const float fdyp = fabsf((-fxbin * s + fybin * c) * iq);
+	const float fdyp = fabsf(fmaf(fybin, c, -(fxbin * s)) * iq);
 	if (counts && lane == 0 && L < kLevelCounts) {
 		atomicAdd(&counts[L], 1ull);
 		atomicAdd(&counts[kCountSubEvals], (unsigned long long)(recurse ? 2 * n : n));
@@ -198,8 +199,8 @@ __device__ void eval_frame_m(const ProfileDev &P, const f32::Shape &sh, WarpScra
 			const float ox = (small_int_to_float(i) + 0.5f) * fxbin, oy = (small_int_to_float(j) + 0.5f) * fybin;
 			const float dx = (xhi + ox) + xlo;
 			const float dy = (yhi + oy) + ylo;
-			const float xp = dx * c + dy * s;
-			const float yp = (dy * c - dx * s) * iq;
+			const float xp = fmaf(dx, c, dy * s);
+			const float yp = fmaf(dy, c, -(dx * s)) * iq;
 			const float sub = f32::value<KINDS>(sh, xp, yp);
 			if (recurse) {
 				const float t = f32::value<KINDS>(sh, fabsf(xp), fabsf(yp) + fdyp);
@@ -449,102 +450,185 @@ __device__ bool split_root(const SplitPool &pool, const ProfileDev &P, int pi, c
 	return true;
 }
 
-// One 32-pixel row tile of a model's drawing area: every profile of the model
-// in order, summed into the conv / direct images. KINDS: the radial profile
+// Tiles a phase-B work item evaluates together: consecutive 32-pixel tiles of
+// one drawing row, each profile's constants loaded once for all of them
+// (measured on the 1024-model step with every profile rough: 1.54 ms one tile
+// at a time, the profile and model data loaded for each tile).
+#ifndef PF_EVAL_SEG_TILES
+#define PF_EVAL_SEG_TILES 8
+#endif
+constexpr int kSegTiles = PF_EVAL_SEG_TILES;
+// a claim of ring items starts a profile's ring row: its lanes 4g .. 4g + 3
+// are one row's kRingCols tiles
+static_assert(PF_EVAL_RING_CHUNK % kRingCols == 0, "ring claims hold whole ring rows");
+
+// A warp's per-pixel running sums over a segment's tiles, lane-major in shared
+// memory: the conv and direct image values, and (split kernels) the pixel's
+// split record and last split root.
+template <bool SPLIT>
+struct SegScratch {
+	float conv[kSegTiles][32], direct[kSegTiles][32];
+	int prec[SPLIT ? kSegTiles : 1][32], plast[SPLIT ? kSegTiles : 1][32];
+	unsigned int pend[kSegTiles];  // the current profile's subsampled pixels, a bit per lane
+};
+
+// Tiles tc0 .. tc0 + nt - 1 (nt <= kSegTiles; the ones whose bit is set in
+// `own`) of drawing row `row` of model mi: every profile of the model in
+// order, summed into the conv / direct images. A pixel's sum is formed in
+// profile order, as one tile at a time forms it. KINDS: the radial profile
 // kinds of the batch.
 template <unsigned int KINDS, bool SPLIT>
-__device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, int n_models,
-                                          const ProfileDev *__restrict__ profs, const double *__restrict__ psf_pool,
-                                          float *__restrict__ conv_img, float *__restrict__ direct_img, long long tile,
-                                          WarpScratchM &ws, int lane, const DebugRec &dbg, const SplitPool &pool)
+__device__ __forceinline__ void eval_seg(const ModelDev *__restrict__ models, int mi,
+                                         const ProfileDev *__restrict__ profs, const double *__restrict__ psf_pool,
+                                         float *__restrict__ conv_img, float *__restrict__ direct_img, int row,
+                                         int tc0, int nt, unsigned int own, WarpScratchM &ws, SegScratch<SPLIT> &ss,
+                                         int lane, const DebugRec &dbg, const SplitPool &pool)
 {
-	const int mi = find_model(models, n_models, tile);
 	const ModelDev &m = models[mi];
-	const long long local = tile - m.tile_base;
-	const unsigned int row = (unsigned int)local / m.tiles_per_row;
-	const int col0 = (int)((unsigned int)local - row * m.tiles_per_row) * 32;
-	const int col1 = min(col0 + 31, (int)m.draw_w - 1);
-	const unsigned int px = (unsigned int)col0 + lane;
-	const bool active = px < m.draw_w;
-	const bool in_mask = active && evaluated(m, (int)px, (int)row);  // the calculation mask (radial, sky)
+	const int col0 = tc0 * 32;
+	const int col1 = min((tc0 + nt) * 32 - 1, (int)m.draw_w - 1);
 	const double *psf = m.psf_off >= 0 ? psf_pool + m.psf_off : nullptr;
-	// pixel centre (i + 1/2) * scale as an unevaluated float sum
-	const float cx = small_int_to_float(px) + 0.5f, cy = small_int_to_float(row) + 0.5f;
-	const float xh = cx * m.fsx_hi, yh = cy * m.fsy_hi;
-	const float xl = fmaf(cx, m.fsx_hi, -xh) + cx * m.fsx_lo;
-	const float yl = fmaf(cy, m.fsy_hi, -yh) + cy * m.fsy_lo;
-	float acc_conv = 0.f, acc_direct = 0.f;
-	// this lane's pixel: its split record once a profile's subtrees are split
-	// off (SplitPool), and the last split profile's root
-	int prec = -1, plast = -1;
+	for (int j = 0; j < nt; j++) {
+		ss.conv[j][lane] = 0.f;
+		ss.direct[j][lane] = 0.f;
+		if constexpr (SPLIT) {
+			ss.prec[j][lane] = -1;
+			ss.plast[j][lane] = -1;
+		}
+	}
+	// pixel centre (i + 1/2) * scale as an unevaluated float sum (y: the row's)
+	const float cy = small_int_to_float((unsigned int)row) + 0.5f;
+	const float yh = cy * m.fsy_hi;
+	const float yl = fmaf(cy, m.fsy_lo, fmaf(cy, m.fsy_hi, -yh));
 
 	for (int q0 = 0; q0 < m.n_profiles; q0 += 32) {
 		// 32 profiles' culling boxes tested at once, one per lane; the ones
-		// that reach this tile drawn one by one, in profile order
-		const bool reaches = profile_reaches(profs, m, q0 + lane, (int)row, col0, col1);
+		// that reach the segment drawn one by one, in profile order
+		const bool reaches = profile_reaches(profs, m, q0 + lane, row, col0, col1);
 		unsigned int todo = __ballot_sync(0xffffffffu, reaches);
 		while (todo) {
 			const int q = q0 + __ffs(todo) - 1;
 			todo &= todo - 1;
 			const int pi = m.first_profile + q;
 			const ProfileDev &P = profs[pi];
-			float add = 0.f;
-			bool has = false;
-			if (P.kind == PF_SKY) {
-				add = P.fbg;
-				has = in_mask;
+			const int kind = P.kind;
+			const bool conv = P.convolve != 0;
+			if (kind == PF_SKY || kind == PF_PSF) {
+				const float fbg = P.fbg;
+				for (int j = 0; j < nt; j++) {
+					if (!((own >> j) & 1u)) continue;
+					const unsigned int px = (unsigned int)(col0 + 32 * j + lane);
+					const bool active = px < m.draw_w;
+					float add = 0.f;
+					bool has;
+					if (kind == PF_SKY) {
+						add = fbg;
+						has = active && evaluated(m, (int)px, row);
+					}
+					else {
+						has = active && psf && psf_value(P, m, psf, px, (unsigned int)row, add);
+					}
+					if (has) {
+						if (conv) ss.conv[j][lane] += add;
+						else ss.direct[j][lane] += add;
+					}
+				}
+				continue;
 			}
-			else if (P.kind == PF_PSF) {
-				if (active && psf) has = psf_value(P, m, psf, px, row, add);
-			}
-			else if (is_radial(P.kind)) {
-				const f32::Shape sh = f32::load_shape(P);
-				const float dx = (xh - P.fxc_hi) + (xl - P.fxc_lo);
-				const float dy = (yh - P.fyc_hi) + (yl - P.fyc_lo);
-				const float xp = dx * sh.cs + dy * sh.sn;
-				const float yp = (dy * sh.cs - dx * sh.sn) * sh.iq;
-				const float rr = sqrtf(xp * xp + yp * yp) * P.finv_rscale;
-				bool beyond = P.frmax > 0.f && rr > P.frmax;
-				bool outside = rr > P.fswitch;
-				const bool amb = (P.frmax > 0.f && fabsf(rr - P.frmax) <= kGuardRadius * P.frmax) ||
-				                 fabsf(rr - P.fswitch) <= kGuardRadius * P.fswitch || !isfinite(rr);
+			if (!is_radial(kind)) continue;
+			const f32::Shape sh = f32::load_shape(P);
+			const float fxc_hi = P.fxc_hi, fxc_lo = P.fxc_lo;
+			const float dy = (yh - P.fyc_hi) + (yl - P.fyc_lo);
+			const float inv_rscale = P.finv_rscale, frmax = P.frmax, fswitch = P.fswitch;
+			const bool rough = P.rough != 0;
+			const float fflux = P.fflux_scale;
+			// the segment's tiles that the profile's culling box reaches
+			const int jlo = max(0, (max(P.bbx0, col0) >> 5) - tc0);
+			const int jhi = min(nt - 1, (min(P.bbx1, col1) >> 5) - tc0);
+			unsigned long long *counts = dbg.counts ? dbg.counts + (size_t)pi * kLevelCounts : nullptr;
+			// the pixels evaluated directly, tile by tile; the subsampled ones
+			// marked, then walked tile by tile (no calls in the first loop, so
+			// that its values stay in registers). Each pixel gets one addition
+			// per profile, in profile order.
+			unsigned int any_ss = 0;
+			for (int j = jlo; j <= jhi; j++) {
+				if (!((own >> j) & 1u)) continue;
+				const unsigned int px = (unsigned int)(col0 + 32 * j + lane);
+				const bool active = px < m.draw_w;
+				const bool in_mask = active && evaluated(m, (int)px, row);  // the calculation mask
+				const float cx = small_int_to_float(px) + 0.5f;
+				const float xh = cx * m.fsx_hi;
+				const float xl = fmaf(cx, m.fsx_lo, fmaf(cx, m.fsx_hi, -xh));
+				const float dx = (xh - fxc_hi) + (xl - fxc_lo);
+				const float xp = fmaf(dx, sh.cs, dy * sh.sn);
+				const float yp = fmaf(dy, sh.cs, -(dx * sh.sn)) * sh.iq;
+				const float rr = sqrtf(fmaf(xp, xp, yp * yp)) * inv_rscale;
+				bool beyond = frmax > 0.f && rr > frmax;
+				bool outside = rr > fswitch;
+				const bool amb = (frmax > 0.f && fabsf(rr - frmax) <= kGuardRadius * frmax) ||
+				                 fabsf(rr - fswitch) <= kGuardRadius * fswitch || !isfinite(rr);
 				if (amb && in_mask) {
-					const unsigned int d = radius_f64(P, m, px, row);
+					const unsigned int d = radius_f64(P, m, px, (unsigned int)row);
 					beyond = (d & 1u) != 0;
 					outside = (d & 2u) != 0;
 				}
 				beyond |= !in_mask;  // masked pixels are not evaluated (src/radial.cpp:305-307)
 				float pixel_val = 0.f;
-				int depth = 0;
-				bool need_ss = false, split = false;
+				bool need_ss = false;
 				if (beyond) {
-					depth = -1;
 				}
-				else if (P.rough || outside) {
+				else if (rough || outside) {
 					pixel_val = f32::value<KINDS>(sh, xp, yp);
 					if (!isfinite(pixel_val)) pixel_val = value_f64<KINDS>(P, dx, 0.f, 0.f, dy, 0.f, 0.f);
 				}
 				else {
 					need_ss = true;
 				}
-				unsigned int pending = __ballot_sync(0xffffffffu, need_ss && active);
-				unsigned long long *counts = dbg.counts ? dbg.counts + (size_t)pi * kLevelCounts : nullptr;
+				const unsigned int pending = __ballot_sync(0xffffffffu, need_ss && active);
+				if (lane == 0) ss.pend[j] = pending;
+				any_ss |= pending;
 				if (counts) {
 					const unsigned int nd = __popc(__ballot_sync(0xffffffffu, active && !beyond && !need_ss));
 					if (lane == 0 && nd) atomicAdd(&counts[kCountDirectEvals], (unsigned long long)nd);
 				}
+				if (active && !need_ss) {
+					if (dbg.depth) dbg.depth[P.depth_off + (size_t)row * m.draw_w + px] = (int8_t)(beyond ? -1 : 0);
+					const float add = fflux * pixel_val;
+					if (conv) ss.conv[j][lane] += add;
+					else ss.direct[j][lane] += add;
+				}
+			}
+			if (!any_ss) continue;
+			__syncwarp();
+			for (int j = jlo; j <= jhi; j++) {
+				unsigned int pending = ss.pend[j];
+				if (!((own >> j) & 1u) || !pending) continue;
+				const bool mine = (pending >> lane) & 1u;
+				const int tcol0 = col0 + 32 * j;
+				// the pixel's split record and last split root, while trees are split
+				int prec = -1, plast = -1;
+				if constexpr (SPLIT) {
+					prec = ss.prec[j][lane];
+					plast = ss.plast[j][lane];
+				}
+				float pixel_val = 0.f;
+				int depth = 0;
+				bool split = false;
 				while (pending) {
 					const int src = __ffs(pending) - 1;
 					pending &= pending - 1;
-					const unsigned int spx = (unsigned int)col0 + src;
-					const float sdx = __shfl_sync(0xffffffffu, dx, src);
-					const float sdy = __shfl_sync(0xffffffffu, dy, src);
+					const unsigned int spx = (unsigned int)tcol0 + src;
 					unsigned int res = P.resolution, max_rec = P.max_recursions;
 					if (P.center_boost) {  // src/sersic.cpp:331-347
-						bool center = fabsf(sdx) < m.fscale_x && fabsf(sdy) < m.fscale_y;
+						// the pixel's x offset from the centre, as the first loop formed it
+						const float scx = small_int_to_float(spx) + 0.5f;
+						const float sxh = scx * m.fsx_hi;
+						const float sxl = fmaf(scx, m.fsx_lo, fmaf(scx, m.fsx_hi, -sxh));
+						const float sdx = (sxh - fxc_hi) + (sxl - fxc_lo);
+						bool center = fabsf(sdx) < m.fscale_x && fabsf(dy) < m.fscale_y;
 						if (fabsf(fabsf(sdx) - m.fscale_x) <= 1e-5f * m.fscale_x ||
-						    fabsf(fabsf(sdy) - m.fscale_y) <= 1e-5f * m.fscale_y) {
-							center = center_f64(P, m, spx, row);
+						    fabsf(fabsf(dy) - m.fscale_y) <= 1e-5f * m.fscale_y) {
+							center = center_f64(P, m, spx, (unsigned int)row);
 						}
 						if (center) {
 							res = 8;
@@ -555,8 +639,9 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 					if (max_rec > (unsigned int)kMaxLevels - 1) max_rec = kMaxLevels - 1;
 					// pixel box corner (i * scale - centre) as an exact float pair
 					float bxh, bxl, byh, byl;
-					corner_pair(small_int_to_float(spx), m.fsx_hi, m.fsx_lo, P.fxc_hi, P.fxc_lo, bxh, bxl);
-					corner_pair(small_int_to_float(row), m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh, byl);
+					corner_pair(small_int_to_float(spx), m.fsx_hi, m.fsx_lo, fxc_hi, fxc_lo, bxh, bxl);
+					corner_pair(small_int_to_float((unsigned int)row), m.fsy_hi, m.fsy_lo, P.fyc_hi, P.fyc_lo, byh,
+					            byl);
 					int deepest = 0;
 					float v = 0.f;
 					if constexpr (SPLIT) {
@@ -582,31 +667,40 @@ __device__ __forceinline__ void eval_tile(const ModelDev *__restrict__ models, i
 						depth = deepest;
 					}
 				}
-				if (dbg.depth && active && !split) {
-					dbg.depth[P.depth_off + (size_t)row * m.draw_w + px] = (int8_t)depth;
+				if constexpr (SPLIT) {
+					ss.prec[j][lane] = prec;
+					ss.plast[j][lane] = plast;
 				}
-				add = P.fflux_scale * pixel_val;
-				has = active && !split;  // a split profile's value is added when its boxes finish
+				// a split profile's value is added when its boxes finish
+				if (mine && !split) {
+					if (dbg.depth) dbg.depth[P.depth_off + (size_t)row * m.draw_w + tcol0 + lane] = (int8_t)depth;
+					const float add = fflux * pixel_val;
+					if (conv) ss.conv[j][lane] += add;
+					else ss.direct[j][lane] += add;
+				}
 			}
-			if (has) {
-				if (P.convolve) acc_conv += add;
-				else acc_direct += add;
-			}
+			__syncwarp();
 		}
 	}
-	if (active) {
+	for (int j = 0; j < nt; j++) {
+		if (!((own >> j) & 1u)) continue;
+		const unsigned int px = (unsigned int)(col0 + 32 * j + lane);
+		if (px >= m.draw_w) continue;
 		const size_t canvas_idx = (size_t)m.draw_off + (size_t)row * m.draw_w + px;
-		if (SPLIT && prec >= 0) {
+		const float c = ss.conv[j][lane], d = ss.direct[j][lane];
+		if (SPLIT && ss.prec[j][lane] >= 0) {
 			// the split profiles' values are still to come: the warp that
 			// finishes the last of them writes the canvas
-			pool.pix[prec].s_conv = acc_conv;
-			pool.pix[prec].s_direct = acc_direct;
+			const int prec = ss.prec[j][lane];
+			pool.pix[prec].s_conv = c;
+			pool.pix[prec].s_direct = d;
 		}
 		else {
-			if (m.conv_required) conv_img[canvas_idx] = acc_conv;
-			direct_img[canvas_idx] = acc_direct;
+			if (m.conv_required) conv_img[canvas_idx] = c;
+			direct_img[canvas_idx] = d;
 		}
 	}
+	__syncwarp();
 }
 
 // Phase A item k (k < n_profiles * kRingRows * kRingCols): tile column
@@ -646,9 +740,12 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
                     unsigned int *counter, unsigned int *claims, DebugRec dbg, SplitPool pool)
 {
 	__shared__ WarpScratchM scratch[kWarps32];
+	__shared__ SegScratch<SPLIT> segs[kWarps32];
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	WarpScratchM &ws = scratch[warp];
+	SegScratch<SPLIT> &ss = segs[warp];
 	bool ring = n_ring_items > 0;
+	int mi = 0;  // the model of the warp's last tile
 	while (true) {
 		unsigned int chunk = 0;
 		if (lane == 0) {
@@ -686,9 +783,32 @@ eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const Pro
 		}
 		while (todo) {
 			const int src = __ffs(todo) - 1;
-			todo &= todo - 1;
 			const long long t = __shfl_sync(0xffffffffu, tile, src);
-			eval_tile<KINDS, SPLIT>(models, n_models, profs, psf_pool, conv_img, direct_img, t, ws, lane, dbg, pool);
+			mi = find_model_from(models, n_models, t, mi);
+			const ModelDev &m = models[mi];
+			const unsigned int local = (unsigned int)(t - m.tile_base);
+			const int row = (int)(local / m.tiles_per_row);
+			const int tc = (int)(local - (unsigned int)row * m.tiles_per_row);
+			int nt = 1;
+			unsigned int own = 1u;
+			if (!ring) {
+				// phase B: with it, the claim's next tiles of the same row (the
+				// claim's tiles are consecutive), up to kSegTiles, those it owns
+				const int span = min(min(kSegTiles, (int)m.tiles_per_row - tc), 32 - src);
+				own = (todo >> src) & (span >= 32 ? 0xffffffffu : ((1u << span) - 1u));
+				nt = 32 - __clz(own);
+				todo &= ~(own << src);
+			}
+			else {
+				// phase A: with it, the same item's next ring tiles (lanes 4g ..
+				// 4g + 3 hold one profile's ring row, consecutive tile columns)
+				const int span = min(kRingCols - src % kRingCols, kSegTiles);
+				own = (todo >> src) & ((1u << span) - 1u);
+				nt = 32 - __clz(own);
+				todo &= ~(own << src);
+			}
+			eval_seg<KINDS, SPLIT>(models, mi, profs, psf_pool, conv_img, direct_img, row, tc, nt, own, ws, ss, lane,
+			                       dbg, pool);
 		}
 	}
 }

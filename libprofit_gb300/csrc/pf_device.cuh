@@ -12,6 +12,7 @@
 // one warp per tile, tiles of all models numbered consecutively.
 #pragma once
 
+#include <climits>
 #include <cstdint>
 
 #include "../../include/pf_cuda.h"
@@ -451,6 +452,17 @@ __device__ __forceinline__ int find_model(const ModelDev *models, int n_models, 
 		if (models[mid].tile_base <= tile) lo = mid; else hi = mid - 1;
 	}
 	return lo;
+}
+
+// find_model, tried first at the model `hint` and the one after it
+__device__ __forceinline__ int find_model_from(const ModelDev *models, int n_models, long long tile, int hint)
+{
+	const long long b0 = models[hint].tile_base;
+	const long long b1 = hint + 1 < n_models ? models[hint + 1].tile_base : LLONG_MAX;
+	const long long b2 = hint + 2 < n_models ? models[hint + 2].tile_base : LLONG_MAX;
+	if (b0 <= tile && tile < b1) return hint;
+	if (b1 <= tile && tile < b2) return hint + 1;
+	return find_model(models, n_models, tile);
 }
 
 }  // namespace pf

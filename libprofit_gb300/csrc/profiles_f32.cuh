@@ -10,6 +10,11 @@
 // every decision that could flip because of it is re-taken in FP64 by the
 // caller (see eval_f32.cu).
 //
+// Every multiply-add is written as fmaf, so that the rounding is the same in
+// every kernel these are compiled into (eval_f32.cu is built without the
+// compiler's own contraction: a batch and a single model, drawn by kernels
+// built for different kinds, give the same bits).
+//
 // The kernels copy a profile's constants once into a Shape, held in
 // registers, and evaluate through value<KINDS>(), where KINDS is the set of
 // profile kinds the kernel is built for: a batch of sersic profiles only runs
@@ -80,7 +85,7 @@ __device__ __forceinline__ Shape load_shape(const ProfileDev &p)
 __device__ __forceinline__ float boxy_r(const Shape &s, float x, float y)
 {
 	if (!s.boxy) {
-		return sqrtf(x * x + y * y);
+		return sqrtf(fmaf(x, x, y * y));
 	}
 	const float B = s.c[FP_B], invB = s.c[FP_INVB];
 	return ex2(invB * lg2(powabs(x, B) + powabs(y, B)));
@@ -91,7 +96,7 @@ __device__ __forceinline__ float sersic(const Shape &s, float x, float y)
 	const float *c = s.c;
 	float base, e;
 	if (!s.boxy) {
-		base = (x * x + y * y) * c[FP_S_INV_RE2];  // (r/re)^2
+		base = fmaf(x, x, y * y) * c[FP_S_INV_RE2];  // (r/re)^2
 		e = c[FP_S_HALF_INV_N];                     // 1 / (2 n)
 	}
 	else {
@@ -99,7 +104,7 @@ __device__ __forceinline__ float sersic(const Shape &s, float x, float y)
 		e = c[FP_S_INV_NB];                          // 1 / (n B)
 	}
 	const float rf = ex2(e * lg2(base));
-	return ex2(c[FP_S_K] - c[FP_S_K] * rf);          // exp(-bn (rf - 1)), K = bn log2(e)
+	return ex2(fmaf(-c[FP_S_K], rf, c[FP_S_K]));     // exp(-bn (rf - 1)), K = bn log2(e)
 }
 
 __device__ __forceinline__ float coresersic(const Shape &s, float x, float y)
@@ -117,7 +122,7 @@ __device__ __forceinline__ float moffat(const Shape &s, float x, float y)
 	const float *c = s.c;
 	float r2;
 	if (!s.boxy) {
-		r2 = (x * x + y * y) * c[FP_M_INV_RS2];
+		r2 = fmaf(x, x, y * y) * c[FP_M_INV_RS2];
 	}
 	else {
 		const float rf = boxy_r(s, x, y) * c[FP_M_INV_RS];
@@ -146,7 +151,7 @@ __device__ __forceinline__ float king(const Shape &s, float x, float y)
 	const float rt = c[FP_K_RT];
 	if (r < rt) {
 		const float q = r * c[FP_K_INV_RC];
-		const float u = 1.f + q * q;
+		const float u = fmaf(q, q, 1.f);
 		const float w = (rt - r) * (rt + r) * (c[FP_K_INV_RC] * c[FP_K_INV_RC]) / u;
 		const float diff = c[FP_K_TEMP] * expm1f(c[FP_K_INV_A] * log1pf(w));
 		return ex2(c[FP_K_A] * lg2(diff));
@@ -163,7 +168,7 @@ __device__ __forceinline__ float brokenexp(const Shape &s, float x, float y)
 	if (ab < 40.f) {
 		base = log1pf(__expf(ab)) * c[FP_E_INV_A];
 	}
-	return __expf(-r * c[FP_E_INV_H1] + c[FP_E_EXPO] * base);
+	return __expf(fmaf(-r, c[FP_E_INV_H1], c[FP_E_EXPO] * base));
 }
 
 // The profile value at profile coordinates (x, y), for a kernel built for the
