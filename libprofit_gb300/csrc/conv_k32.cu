@@ -1,0 +1,9 @@
+// Single-precision direct convolution kernels with a PSF row stride of 32
+// floats compiled in (conv.cuh).
+#include "conv.cuh"
+
+namespace pf {
+
+PF_CONV_FIXED_DEF(32)
+
+}  // namespace pf

@@ -61,10 +61,12 @@ long long conv_tiles(unsigned int w, unsigned int h, int shape);
 template <typename T>
 size_t conv_smem(unsigned int kw, unsigned int kh, int shape);
 template <typename T>
-cudaError_t conv_configure(size_t smem, int shape);
+cudaError_t conv_configure(size_t smem, int shape, int kwp);
 template <typename T>
-void launch_conv(int mode, int shape, const ModelDev *models, int n_models, const T *psf, const T *in, const T *direct,
-                 T *out, const long long *tile_base, long long n_tiles, size_t smem, int n_sm, cudaStream_t stream);
+void launch_conv(int mode, int shape, int kwp, const ModelDev *models, int n_models, const T *psf, const T *in,
+                 const T *direct, T *out, const long long *tile_base, long long n_tiles, size_t smem, int n_sm,
+                 cudaStream_t stream);
+bool conv_stride_fixed(int kwp);
 void launch_psf_to_float(const double *in, float *out, long long n, cudaStream_t stream);
 int fft_job_size();
 template <typename T>
@@ -445,6 +447,7 @@ struct pf_batch {
 	long long *d_tile_base_out = nullptr;
 	long long n_out_tiles = 0;
 	size_t finish_smem = 0;
+	int conv_kwp = 0;                   // PSF row stride compiled into the direct convolution (0: read per model)
 	bool any_downsample = false;
 	bool any_fft_downsample = false;    // FP64: an FFT model SUM-downsampled (one more finishing pass)
 	int fwd_shape = 0, adj_shape = 0;  // convolution block shapes (conv.cu)
@@ -873,6 +876,26 @@ static int forced_split()
 	return std::atoi(v) != 0 ? 1 : 0;
 }
 
+// The PSF row stride (4 ceil(kw / 4) floats) shared by every model that the
+// single-precision direct convolution convolves, when kernels with that
+// stride compiled in exist (conv_k*.cu), else 0: the kernels that read it per
+// model. PF_CONV_STRIDE=0 always takes the latter, for exercising both.
+static int shared_conv_stride(const pf_batch *b)
+{
+	if (b->dbl) return 0;
+	if (const char *v = std::getenv("PF_CONV_STRIDE")) {
+		if (*v && std::atoi(v) == 0) return 0;
+	}
+	int k = -1;
+	for (const auto &d : b->mdev) {
+		if (!d.conv_required || d.use_fft) continue;
+		const int w = (int)((d.psf_w + 3) & ~3u);
+		if (k >= 0 && w != k) return 0;
+		k = w;
+	}
+	return k > 0 && pf::conv_stride_fixed(k) ? k : 0;
+}
+
 // PF_CONV_SHAPE: a single-precision direct-convolution block shape to use in
 // both directions instead of the chosen one, for exercising every shape
 // (-1: none)
@@ -1237,6 +1260,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		}
 		b->n_out_tiles = t;
 		b->finish_smem = pf::conv_smem<float>(max_kw, max_kh, b->fwd_shape);
+		b->conv_kwp = shared_conv_stride(b);
 		if (b->finish_smem > 227 * 1024) {
 			return fail(PF_ERR_UNSUPPORTED, "PSF too large for the single-precision direct convolution's shared "
 			                                "memory: request the FFT convolver or double precision");
@@ -1389,7 +1413,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		PF_CUDA_TRY(cudaMalloc(&b->d_tile_base_out, sizeof(long long) * tile_base_out.size()));
 		PF_CUDA_TRY(cudaMemcpy(b->d_tile_base_out, tile_base_out.data(), sizeof(long long) * tile_base_out.size(),
 		                       cudaMemcpyHostToDevice));
-		PF_CUDA_TRY(pf::conv_configure<float>(b->finish_smem, b->fwd_shape));
+		PF_CUDA_TRY(pf::conv_configure<float>(b->finish_smem, b->fwd_shape, b->conv_kwp));
 	}
 	if (b->any_fft) {
 		// FFT buffers, twiddles and, once per batch, the PSF spectra
@@ -1489,11 +1513,12 @@ static double time_forward_conv(pf_batch *b, int shape, bool fft, float *out)
 		}
 	}
 	const size_t smem = pf::conv_smem<float>(max_kw, max_kh, shape);
+	const int kwp = shared_conv_stride(b);
 	long long *d_base = nullptr;
 	if (!fft && (smem > 227 * 1024 || cudaMalloc(&d_base, sizeof(long long) * base.size()) != cudaSuccess)) return -1;
 	if (!fft) {
 		cudaMemcpy(d_base, base.data(), sizeof(long long) * base.size(), cudaMemcpyHostToDevice);
-		pf::conv_configure<float>(smem, shape);
+		pf::conv_configure<float>(smem, shape, kwp);
 	}
 	cudaEvent_t e0, e1;
 	cudaEventCreate(&e0);
@@ -1510,7 +1535,7 @@ static double time_forward_conv(pf_batch *b, int shape, bool fft, float *out)
 			}
 		}
 		else if (t > 0) {
-			pf::launch_conv<float>(0, shape, b->d_models, n_models, b->d_psf32, (const float *)b->d_conv,
+			pf::launch_conv<float>(0, shape, kwp, b->d_models, n_models, b->d_psf32, (const float *)b->d_conv,
 			                       (const float *)b->d_direct, out, d_base, t, smem, b->env->n_sm, st);
 		}
 		cudaEventRecord(e1, st);
@@ -1522,7 +1547,7 @@ static double time_forward_conv(pf_batch *b, int shape, bool fft, float *out)
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
 	cudaFree(d_base);
-	if (!fft) pf::conv_configure<float>(b->finish_smem, b->fwd_shape);
+	if (!fft) pf::conv_configure<float>(b->finish_smem, b->fwd_shape, b->conv_kwp);
 	return cudaGetLastError() == cudaSuccess ? best : -1;
 }
 
@@ -1597,14 +1622,15 @@ static double time_adjoint_conv(pf_batch *b, int shape)
 	long long *d_base = nullptr;
 	if (t == 0 || smem > 227 * 1024 || cudaMalloc(&d_base, sizeof(long long) * base.size()) != cudaSuccess) return -1;
 	cudaMemcpy(d_base, base.data(), sizeof(long long) * base.size(), cudaMemcpyHostToDevice);
-	pf::conv_configure<float>(smem, shape);
+	const int kwp = shared_conv_stride(b);
+	pf::conv_configure<float>(smem, shape, kwp);
 	cudaEvent_t e0, e1;
 	cudaEventCreate(&e0);
 	cudaEventCreate(&e1);
 	double best = -1;
 	for (int rep = 0; rep < 4; rep++) {
 		cudaEventRecord(e0, st);
-		pf::launch_conv<float>(1, shape, b->d_models, n_models, b->d_psf32, (const float *)b->d_gout, nullptr,
+		pf::launch_conv<float>(1, shape, kwp, b->d_models, n_models, b->d_psf32, (const float *)b->d_gout, nullptr,
 		                       (float *)b->d_gsrc, d_base, t, smem, b->env->n_sm, st);
 		cudaEventRecord(e1, st);
 		cudaEventSynchronize(e1);
@@ -1922,9 +1948,9 @@ pf_status pf_forward(pf_batch *b, void *images_dev, double *flux_dev, void *stre
 		if (b->any_downsample) {
 			PF_CUDA_TRY(cudaMemsetAsync(images_dev, 0, sizeof(float) * b->total_out, stream));
 		}
-		pf::launch_conv<float>(0, b->fwd_shape, b->d_models, n_models, b->d_psf32, (const float *)b->d_conv,
-		                       (const float *)b->d_direct, (float *)images_dev, b->d_tile_base_out, b->n_out_tiles,
-		                       b->finish_smem, b->env->n_sm, stream);
+		pf::launch_conv<float>(0, b->fwd_shape, b->conv_kwp, b->d_models, n_models, b->d_psf32,
+		                       (const float *)b->d_conv, (const float *)b->d_direct, (float *)images_dev,
+		                       b->d_tile_base_out, b->n_out_tiles, b->finish_smem, b->env->n_sm, stream);
 		for (int pass = 0; b->any_fft && pass < 3; pass++) {
 			for (const auto &j : b->f32_jobs[0][pass]) {
 				pf::launch_fft32(pass, 0, j.n, j.d_jobs, j.n_jobs, b->d_models, (const float *)b->d_conv, nullptr,
@@ -2140,8 +2166,8 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 	PF_CUDA_TRY(cudaMemcpy(b->d_prow_base, prow_base.data(), sizeof(long long) * prow_base.size(), cudaMemcpyHostToDevice));
 	PF_CUDA_TRY(cudaMemcpy(b->d_adj_tile_base, adj_tile_base.data(), sizeof(long long) * adj_tile_base.size(),
 	                       cudaMemcpyHostToDevice));
-	PF_CUDA_TRY(b->dbl ? pf::conv_configure<double>(b->adj_smem, b->adj_shape)
-	                   : pf::conv_configure<float>(b->adj_smem, b->adj_shape));
+	PF_CUDA_TRY(b->dbl ? pf::conv_configure<double>(b->adj_smem, b->adj_shape, 0)
+	                   : pf::conv_configure<float>(b->adj_smem, b->adj_shape, b->conv_kwp));
 	if (!b->dbl && !(b->env->flags & PF_ENV_NO_AUTOTUNE) && b->total_out >= (1ull << 22) && tiles > 0 &&
 	    forced_conv_shape() < 0) {
 		// the autotuner, adjoint convolution: each block shape timed over the
@@ -2187,7 +2213,7 @@ pf_status pf_batch_enable_adjoint(pf_batch *b)
 			PF_CUDA_TRY(cudaMemcpy(b->d_adj_tile_base, adj_tile_base.data(), sizeof(long long) * adj_tile_base.size(),
 			                       cudaMemcpyHostToDevice));
 		}
-		PF_CUDA_TRY(pf::conv_configure<float>(b->adj_smem, b->adj_shape));
+		PF_CUDA_TRY(pf::conv_configure<float>(b->adj_smem, b->adj_shape, b->conv_kwp));
 	}
 	b->adjoint = true;
 	return PF_OK;
@@ -2217,14 +2243,14 @@ pf_status pf_backward(pf_batch *b, const void *images_dev, const void *data_dev,
 	stage_end(b, t, stream);
 	if (any_conv) {
 		t = stage_begin(b, ST_ADJCONV, stream);
-		if (b->dbl) pf::launch_conv<double>(1, b->adj_shape, b->d_models, n_models, b->d_psf_norm, (const double *)b->d_gout,
-		                                    nullptr, (double *)b->d_gsrc, b->d_adj_tile_base, b->n_adj_tiles,
-		                                    b->adj_smem, b->env->n_sm, stream);
+		if (b->dbl) pf::launch_conv<double>(1, b->adj_shape, 0, b->d_models, n_models, b->d_psf_norm,
+		                                    (const double *)b->d_gout, nullptr, (double *)b->d_gsrc,
+		                                    b->d_adj_tile_base, b->n_adj_tiles, b->adj_smem, b->env->n_sm, stream);
 		else {
 			if (b->n_adj_tiles > 0) {
-				pf::launch_conv<float>(1, b->adj_shape, b->d_models, n_models, b->d_psf32, (const float *)b->d_gout,
-				                       nullptr, (float *)b->d_gsrc, b->d_adj_tile_base, b->n_adj_tiles, b->adj_smem,
-				                       b->env->n_sm, stream);
+				pf::launch_conv<float>(1, b->adj_shape, b->conv_kwp, b->d_models, n_models, b->d_psf32,
+				                       (const float *)b->d_gout, nullptr, (float *)b->d_gsrc, b->d_adj_tile_base,
+				                       b->n_adj_tiles, b->adj_smem, b->env->n_sm, stream);
 			}
 			for (int pass = 0; b->any_fft && pass < 3; pass++) {
 				for (const auto &j : b->f32_jobs[1][pass]) {
