@@ -30,16 +30,22 @@ namespace pf {
 
 namespace {
 
-// Warps per block and blocks per SM the register allocation is sized for: 4
-// and 4, 128 registers and 16 warps per SM (measured on the 1024-model step
-// with the row segments below: 2.41 ms, against 2.82 ms at 20 warps and 96
-// registers, whose spills fall in the subsampling walk, and 3.21 ms at 24
-// warps).
+// Warps per block, and blocks per SM the register allocation is sized for.
+// The kernel that walks the trees in place: 4 blocks, 128 registers and 16
+// warps per SM (measured on the 1024-model step with the row segments below:
+// 2.41 ms, against 2.82 ms at 20 warps and 96 registers, whose spills fall in
+// the subsampling walk, and 3.21 ms at 24 warps). The kernels that split the
+// trees off (the tile kernel and split_boxes32_kernel): 5 blocks, 96
+// registers, 20 warps (the 4096 uneven models: evaluation 42.9 ms, against
+// 48.5 ms at 16 warps: the split boxes need warps more than registers).
 #ifndef PF_EVAL32_WARPS
 #define PF_EVAL32_WARPS 4
 #endif
 #ifndef PF_EVAL32_MIN_BLOCKS
 #define PF_EVAL32_MIN_BLOCKS 4
+#endif
+#ifndef PF_EVAL32_SPLIT_MIN_BLOCKS
+#define PF_EVAL32_SPLIT_MIN_BLOCKS 5
 #endif
 // phase-A (ring tile) items a warp claims at once (a divisor of 32; 32, 8
 // and 2 measured within 5 % of each other on the 1024-model step)
@@ -733,7 +739,7 @@ __device__ __forceinline__ long long ring_tile(const ModelDev *__restrict__ mode
 // tile is evaluated by the item that first sets its bit in `claims` (zeroed
 // before the launch), so each tile exactly once.
 template <unsigned int KINDS, bool SPLIT>
-__global__ void __launch_bounds__(kWarps32 * 32, PF_EVAL32_MIN_BLOCKS)
+__global__ void __launch_bounds__(kWarps32 * 32, SPLIT ? PF_EVAL32_SPLIT_MIN_BLOCKS : PF_EVAL32_MIN_BLOCKS)
 eval_tiles32_kernel(const ModelDev *__restrict__ models, int n_models, const ProfileDev *__restrict__ profs,
                     unsigned int n_profiles, const double *__restrict__ psf_pool, float *__restrict__ conv_img,
                     float *__restrict__ direct_img, unsigned int n_tiles, unsigned int n_ring_items,
@@ -850,7 +856,7 @@ __device__ void finish_split_box(const SplitPool &pool, unsigned int b, int r, f
 // The split-off boxes (SplitPool), one per warp, each walked depth first
 // below its level; taken one at a time from the pool's work counter.
 template <unsigned int KINDS>
-__global__ void __launch_bounds__(kWarps32 * 32, PF_EVAL32_MIN_BLOCKS)
+__global__ void __launch_bounds__(kWarps32 * 32, PF_EVAL32_SPLIT_MIN_BLOCKS)
 split_boxes32_kernel(const ProfileDev *__restrict__ profs, float *__restrict__ conv_img,
                      float *__restrict__ direct_img, SplitPool pool, DebugRec dbg)
 {
@@ -893,7 +899,8 @@ void launch_eval32(const ModelDev *models, int n_models, const ProfileDev *profs
                    int n_sm, cudaStream_t stream)
 {
 	const unsigned int n_ring = (unsigned int)n_profiles * kRingRows * kRingCols;
-	const int blocks = n_sm * PF_EVAL32_MIN_BLOCKS;
+	// persistent kernels: as many blocks as fit at once
+	const int blocks = n_sm * (pool.box ? PF_EVAL32_SPLIT_MIN_BLOCKS : PF_EVAL32_MIN_BLOCKS);
 	// kernels without the split path where the batch does not split: it costs
 	// the walk registers (measured 2.79 against 3.10 ms for the 1024-model step)
 	if (sersic_only) {

@@ -147,6 +147,29 @@ def test_every_block_shape(envs, shape, monkeypatch):
         assert np.all(np.abs(g32 - g64) <= 1e-3 * np.abs(g64) + 1e-4 * scale), np.abs(g32 - g64).max() / scale
 
 
+@pytest.mark.parametrize("shape", range(N_SHAPES))
+def test_compiled_stride_equals_stride_read_per_model(envs, shape, monkeypatch):
+    """The kernels with the PSF row stride compiled in (taken where every
+    convolved model's PSF is 13 to 32 wide and rounds up to the same multiple
+    of four) give the bits of the kernels that read the stride per model
+    (PF_CONV_STRIDE=0), forward and adjoint, with each block shape, for PSF
+    widths with every kw mod 4 and the tail pass."""
+    env64, env32 = envs
+    monkeypatch.setenv("PF_CONV_SHAPE", str(shape))
+    w, h = 131, 77
+    y, x = np.mgrid[0:h, 0:w]
+    cot = 1.0 + 0.5 * np.sin(x / 7.0) * np.cos(y / 5.0)
+    for kw, kh in ((13, 9), (18, 18), (23, 6), (25, 25), (32, 11)):
+        psf = _psf(kw, kh)
+        profiles = _profiles(w, h)
+        monkeypatch.delenv("PF_CONV_STRIDE", raising=False)
+        img_c, g_c, _ = _run(env32, False, w, h, psf, profiles, cot)
+        monkeypatch.setenv("PF_CONV_STRIDE", "0")
+        img_r, g_r, _ = _run(env32, False, w, h, psf, profiles, cot)
+        assert np.array_equal(img_c, img_r), (kw, kh)
+        assert np.array_equal(g_c, g_r), (kw, kh)
+
+
 def test_block_shapes_covered():
     """The image sizes above select at least four of the five block shapes
     (shape 3 has shape 1's tile, so the least-area rule never picks it)."""
