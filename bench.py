@@ -353,7 +353,7 @@ def gradient_accuracy(specs, par, img64, data, sigma, g32, g64, env64):
 
 
 # DRAM bytes per model of the adjoint direct convolution's launch (ncu, 256-model copy of the workload)
-ADJ_CONV_TRAFFIC_PER_MODEL = (67.9e6 + 25.0e6) / 256
+ADJ_CONV_TRAFFIC_PER_MODEL = (68.1e6 + 27.3e6) / 256
 
 
 def run_ours(args, world, rank, local):
@@ -604,7 +604,7 @@ def run_ours(args, world, rank, local):
     # DRAM bytes per launch, per model of this workload: ncu dram__bytes_read.sum +
     # dram__bytes_write.sum of each kernel on the 256-model copy of the workload
     # (one ncu capture per kernel), divided by 256
-    traffic_per_model = {"eval_ms": 118.5e6 / 256, "backward_ms": 76.3e6 / 256, "finish_ms": 192.3e6 / 256,
+    traffic_per_model = {"eval_ms": 112.2e6 / 256, "backward_ms": 76.3e6 / 256, "finish_ms": 194.6e6 / 256,
                          "adjoint_conv_ms": ADJ_CONV_TRAFFIC_PER_MODEL}
     roof = {"bound": "fp32", "kernel": dom.replace("_ms", ""), "achieved": None, "peak": fp32_peak,
             "unit": "TFLOP/s", "frac": None, "traffic": None,
