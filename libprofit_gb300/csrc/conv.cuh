@@ -308,8 +308,9 @@ conv_kernel(const ModelDev *__restrict__ models, int n_models, const T *__restri
 					// the convolution is zero where the calculation mask is, and the
 					// output is multiplied by the model's mask at the end
 					const bool conv_here = evaluated(m, x + (int)m.pad_x, yo + (int)m.pad_y);
-					const T v = direct[m.draw_off + (size_t)(yo + m.pad_y) * m.draw_w + x + m.pad_x] +
-					            (conv_here ? acc[r][c] : (T)0);
+					const T dir =
+					    m.direct_required ? direct[m.draw_off + (size_t)(yo + m.pad_y) * m.draw_w + x + m.pad_x] : (T)0;
+					const T v = dir + (conv_here ? acc[r][c] : (T)0);
 					if (m.fs > 1 && !m.return_fs) {
 						if (kept(m, x / (int)m.fs, yo / (int)m.fs))
 							atomicAdd(&out[m.out_off + (size_t)(yo / m.fs) * m.out_w + x / m.fs], v);

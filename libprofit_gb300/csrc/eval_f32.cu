@@ -416,6 +416,7 @@ __device__ bool split_root(const SplitPool &pool, const ProfileDev &P, int pi, c
 			X.first_root = r;
 			X.pending = 1;
 			X.conv_required = m.conv_required;
+			X.direct_required = m.direct_required;
 		}
 		else {
 			pool.root[old_last].next = r;
@@ -703,7 +704,7 @@ __device__ __forceinline__ void eval_seg(const ModelDev *__restrict__ models, in
 		}
 		else {
 			if (m.conv_required) conv_img[canvas_idx] = c;
-			direct_img[canvas_idx] = d;
+			if (m.direct_required) direct_img[canvas_idx] = d;  // else all zero, and read as zero
 		}
 	}
 	__syncwarp();
@@ -850,7 +851,7 @@ __device__ void finish_split_box(const SplitPool &pool, unsigned int b, int r, f
 		else d += val;
 	}
 	if (X.conv_required) conv_img[X.idx] = c;
-	direct_img[X.idx] = d;
+	if (X.direct_required) direct_img[X.idx] = d;
 }
 
 // The split-off boxes (SplitPool), one per warp, each walked depth first

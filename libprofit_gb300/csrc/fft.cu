@@ -242,7 +242,7 @@ __global__ void fft_irows_kernel(const ModelDev *__restrict__ models, const FftJ
 			const bool in_draw = dxp >= 0 && dyp >= 0 && dxp < (int)m.draw_w && dyp < (int)m.draw_h;
 			T conv = fx >= 0 && fx < full_w && fx < n ? res[t * n + fx].x * scale : (T)0;
 			if (m.mask_eval && !(in_draw && evaluated(m, dxp, dyp))) conv = (T)0;
-			const T dir = in_draw ? direct[m.draw_off + (size_t)dyp * m.draw_w + dxp] : (T)0;
+			const T dir = in_draw && m.direct_required ? direct[m.draw_off + (size_t)dyp * m.draw_w + dxp] : (T)0;
 			out[m.out_off + (size_t)r * m.out_w + c] = dir + conv;
 		}
 		return;
@@ -252,7 +252,8 @@ __global__ void fft_irows_kernel(const ModelDev *__restrict__ models, const FftJ
 		const int r = jb.first + t;
 		// the convolution zero where the calculation mask is; the model's mask at the end
 		const T conv = evaluated(m, c + (int)m.pad_x, r + (int)m.pad_y) ? res[t * n + c + off_x].x * scale : (T)0;
-		const T v = direct[m.draw_off + (size_t)(r + m.pad_y) * m.draw_w + c + m.pad_x] + conv;
+		const T dir = m.direct_required ? direct[m.draw_off + (size_t)(r + m.pad_y) * m.draw_w + c + m.pad_x] : (T)0;
+		const T v = dir + conv;
 		if (downsample && fine) {
 			fine[m.draw_off + (size_t)(r + m.pad_y) * m.draw_w + c + m.pad_x] = v;
 		}

@@ -678,7 +678,8 @@ irows_kernel(const ModelDev *__restrict__ models, const Job *__restrict__ jobs, 
 			// the convolution is zero where the calculation mask is; the output
 			// is multiplied by the model's mask at the end
 			const float conv = evaluated(m, c + (int)m.pad_x, r + (int)m.pad_y) ? (half ? z.y : z.x) * scale : 0.f;
-			const float v = direct[m.draw_off + (size_t)(r + m.pad_y) * m.draw_w + c + m.pad_x] + conv;
+			const float dir = m.direct_required ? direct[m.draw_off + (size_t)(r + m.pad_y) * m.draw_w + c + m.pad_x] : 0.f;
+			const float v = dir + conv;
 			if (downsample) {
 				if (kept(m, c / (int)m.fs, r / (int)m.fs))
 					atomicAdd(&out[m.out_off + (size_t)(r / m.fs) * m.out_w + c / m.fs], v);

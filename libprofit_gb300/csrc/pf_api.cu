@@ -161,6 +161,7 @@ pf_status validate_profile(const pf_profile_desc &d, bool model_has_psf)
 struct Geometry {
 	uint32_t pad_x, pad_y, draw_w, draw_h, crop_w, crop_h, out_w, out_h;
 	bool conv;
+	bool direct = false;  // some profile draws unconvolved
 	// crop = false with the FFT convolver: the output window in the FFT's
 	// uncropped frame (ModelDev::ufx0..udy0) and the offset Model::evaluate
 	// reports (offset_out); 0 otherwise
@@ -250,8 +251,10 @@ pf_status model_geometry(const pf_model_desc &m, const pf_profile_desc *profiles
 	if (m.finesampling == 0) return fail(PF_ERR_INVALID_PARAMETER, "finesampling must be > 0");
 	const bool has_psf = m.psf_offset >= 0 && m.psf_w > 0 && m.psf_h > 0;
 	g.conv = false;
+	g.direct = false;
 	for (uint32_t i = 0; i < m.n_profiles; i++) {
 		g.conv |= profiles[m.first_profile + i].convolve != 0;
+		g.direct |= profiles[m.first_profile + i].convolve == 0;
 	}
 	if (g.conv && !has_psf) {
 		return fail(PF_ERR_INVALID_PARAMETER, "No psf provided but profile(s) requested convolution");
@@ -1199,6 +1202,7 @@ static pf_status batch_create_impl(pf_env *env, const pf_model_desc *models, siz
 		d.first_profile = (int32_t)m.first_profile;
 		d.n_profiles = (int32_t)m.n_profiles;
 		d.conv_required = g.conv;
+		d.direct_required = g.direct;
 		d.convolver = m.convolver;
 		const bool has_psf = m.psf_offset >= 0 && m.psf_w > 0 && m.psf_h > 0;
 		d.psf_off = has_psf ? m.psf_offset : -1;

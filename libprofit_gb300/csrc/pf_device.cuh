@@ -77,7 +77,10 @@ struct ModelDev {
 	// FFTConvolver's uncropped frame, src/convolve.cpp:263-312)
 	int32_t uncropped;
 	int32_t ufx0, ufy0, udx0, udy0;
-	int32_t pad3;
+	// some profile draws unconvolved: the direct image has content; without
+	// one the single-precision evaluation leaves it unwritten and its readers
+	// take zeros
+	int32_t direct_required;
 };
 
 // The radial profile kinds: the six of the reference and a user-defined one
@@ -284,7 +287,7 @@ struct SplitPixel {
 	int32_t first_root;        // split profiles, in profile order
 	uint32_t pending;          // split profiles not complete
 	int32_t conv_required;
-	int32_t pad;
+	int32_t direct_required;
 };
 
 // The device pool (sized at batch creation; box == nullptr: no splitting).
