@@ -1,18 +1,23 @@
 // Batched single-precision path: FP32 profile values, FP64 where precision
 // decides the result.
 //
-// Same structure as the plain FP64 path (eval_f64.cu): one warp per 32-pixel
-// row tile of a model's drawing area, the model's profiles in order, and a
-// warp-cooperative depth-first recursion for the pixels that
-// RadialProfile::evaluate_cpu subsamples (src/radial.cpp:291-344,
-// subsample_pixel src/radial.cpp:55-135). The differences:
+// Same structure as the plain FP64 path (eval_f64.cu): warps over 32-pixel
+// row tiles of a model's drawing area (here a row segment of up to 8 tiles
+// per work item), the model's profiles in order, and a warp-cooperative
+// depth-first recursion for the pixels that RadialProfile::evaluate_cpu
+// subsamples (src/radial.cpp:291-344, subsample_pixel src/radial.cpp:55-135).
+// The differences:
 //   * profile values are computed in FP32 (profiles_f32.cuh), coordinates
 //     relative to the profile centre, the pixel centre formed with an
 //     error-free float product so that it keeps full relative precision;
-//   * each sub-pixel box is tracked in FP64 relative to the profile centre
-//     (corner and bin), so that boxes 8^-11 pixel wide at the centre of a
-//     high-index Sersic profile keep their geometry; the points inside a box
-//     are FP32 offsets from its corner;
+//   * each sub-pixel box corner is tracked relative to the profile centre as
+//     an unevaluated float pair (hi + lo, an error-free addition per level),
+//     so that boxes 8^-11 pixel wide at the centre of a high-index Sersic
+//     profile keep their geometry; the points inside a box are FP32 offsets
+//     from its corner;
+//   * the file is compiled without multiply-add contraction, its
+//     multiply-adds written as fmaf, so that every kernel instance rounds
+//     alike;
 //   * every decision the reference takes by comparison -- the accuracy test
 //     |testval/subval - 1| > acc, r/rscale > rscale_max, r/rscale >
 //     rscale_switch, the sersic central-pixel test -- is re-taken in FP64

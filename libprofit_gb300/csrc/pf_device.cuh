@@ -9,7 +9,8 @@
 //   * its output image (cropped, optionally downsampled), row-major, in the
 //     caller's buffer.
 // Work is dispatched in tiles of 32 consecutive drawing pixels of one row,
-// one warp per tile, tiles of all models numbered consecutively.
+// a warp per tile or per row segment of tiles, tiles of all models numbered
+// consecutively.
 #pragma once
 
 #include <climits>
