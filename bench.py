@@ -598,7 +598,9 @@ def run_ours(args, world, rank, local):
             kh, kw = s["psf"].shape
             dw, dh = cw + kw // 2 * 2, ch + kh // 2 * 2
             nb = fft_length(cw + kw) // 2 + 1
-            fwd_b += 4.0 * dw * dh + 16.0 * nb * (dh + ch) + 8.0 * cw * ch
+            # the direct canvas is read only where some profile is drawn unconvolved
+            direct = any(not p.get("convolve", False) for _, p in s["profiles"])
+            fwd_b += 4.0 * dw * dh + 16.0 * nb * (dh + ch) + (8.0 if direct else 4.0) * cw * ch
             adj_b += 4.0 * cw * ch + 16.0 * nb * (ch + dh) + 4.0 * dw * dh
         fft_bytes = {"finish_ms": fwd_b, "adjoint_conv_ms": adj_b}
     # DRAM bytes per launch, per model of this workload: ncu dram__bytes_read.sum +
